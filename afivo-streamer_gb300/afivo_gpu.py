@@ -1,0 +1,337 @@
+"""Python host side of the afivo GPU hot path: ctypes bindings of the C-ABI
+(``include/afivo_gpu.h``) and a small object layer that mirrors the Fortran
+API of the path (``mg_fas_vcycle``, ``mg_fas_fmg``, ``af_gc_lvl``,
+``af_tree_maxabs_cc`` ...; afivo/src/m_af_multigrid.f90:14-38,
+afivo/src/m_af_ghostcell.f90:12-20, afivo/src/m_af_utils.f90:773-784).
+
+The compute path is the CUDA library ``libafivo_gpu.so`` built in this
+directory; importing this module fails loudly when it is missing, and no
+operation has a CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libafivo_gpu.so")
+
+AFG_OK = 0
+AFG_ERR_ARG = -1
+AFG_ERR_CUDA = -2
+AFG_ERR_UNSUPPORTED = -3
+AFG_ERR_STATE = -4
+AFG_ERR_DEVICE = -5
+AFG_ERR_NOCONV = -6
+AFG_ERR_NOMEM = -7
+
+AFG_XYZ = 1
+AFG_CYL = 2
+BC_DIRICHLET = -10
+BC_NEUMANN = -11
+BC_CONTINUOUS = -12
+BC_DIRICHLET_COPY = -13
+RB_MG_SIDES = 0
+RB_INTERP = 1
+RB_INTERP_LIM = 2
+FP64 = 0
+MIXED = 1
+CYCLE_DOWN = 1
+CYCLE_UP = 3
+
+_IP = C.POINTER(C.c_int)
+_DP = C.POINTER(C.c_double)
+
+
+class TreeDesc(C.Structure):
+    _fields_ = [
+        ("ndim", C.c_int), ("n_cell", C.c_int), ("coord", C.c_int),
+        ("n_boxes", C.c_int), ("highest_lvl", C.c_int),
+        ("coarse_grid_size", C.c_int * 3),
+        ("lvl", _IP), ("ix", _IP), ("parent", _IP), ("children", _IP),
+        ("neighbors", _IP), ("neighbor_mat", _IP),
+        ("r_min", _DP), ("dr", _DP),
+        ("ids_off", _IP), ("ids", _IP),
+        ("leaves_off", _IP), ("leaves", _IP),
+        ("parents_off", _IP), ("parents", _IP),
+    ]
+
+
+class GcDesc(C.Structure):
+    _fields_ = [("bc_type", C.c_int * 6), ("bc_val", C.c_double * 6),
+                ("rb", C.c_int)]
+
+
+class MgDesc(C.Structure):
+    _fields_ = [
+        ("i_phi", C.c_int), ("i_rhs", C.c_int), ("i_tmp", C.c_int),
+        ("n_cycle_down", C.c_int), ("n_cycle_up", C.c_int),
+        ("helmholtz_lambda", C.c_double),
+        ("bc_type", C.c_int * 6), ("bc_val", C.c_double * 6),
+        ("precision", C.c_int),
+    ]
+
+
+def _ip(a):
+    return a.ctypes.data_as(_IP)
+
+
+def _dp(a):
+    return a.ctypes.data_as(_DP)
+
+
+class TreeDescHolder:
+    """Keeps the numpy arrays behind a TreeDesc alive."""
+
+    def __init__(self, tree):
+        t = tree
+        self.arrays = {
+            "lvl": np.ascontiguousarray(t.lvl, dtype=np.int32),
+            "ix": np.ascontiguousarray(t.ix, dtype=np.int32),
+            "parent": np.ascontiguousarray(t.parent, dtype=np.int32),
+            "children": np.ascontiguousarray(t.children, dtype=np.int32),
+            "neighbors": np.ascontiguousarray(t.neighbors, dtype=np.int32),
+            "neighbor_mat": np.ascontiguousarray(t.neighbor_mat, dtype=np.int32),
+            "r_min": np.ascontiguousarray(t.r_min, dtype=np.float64),
+            "dr": np.ascontiguousarray(t.dr, dtype=np.float64),
+        }
+        (io, i), (lo, l), (po, p) = t.flat_lists()
+        self.arrays.update(ids_off=io, ids=i, leaves_off=lo, leaves=l,
+                           parents_off=po, parents=p)
+        d = TreeDesc()
+        d.ndim = t.ndim
+        d.n_cell = t.n_cell
+        d.coord = t.coord
+        d.n_boxes = t.n_boxes
+        d.highest_lvl = t.highest_lvl
+        for k in range(3):
+            d.coarse_grid_size[k] = int(t.coarse_grid_size[k]) if k < t.ndim else 1
+        for name, arr in self.arrays.items():
+            setattr(d, name, _dp(arr) if arr.dtype == np.float64 else _ip(arr))
+        self.desc = d
+
+
+def gc_desc(bc_type, bc_val=None, rb=RB_MG_SIDES) -> GcDesc:
+    g = GcDesc()
+    for n in range(6):
+        g.bc_type[n] = int(bc_type[n]) if n < len(bc_type) else BC_NEUMANN
+        g.bc_val[n] = float(bc_val[n]) if bc_val is not None and n < len(bc_val) else 0.0
+    g.rb = rb
+    return g
+
+
+def mg_desc(i_phi, i_rhs, i_tmp, bc_type, bc_val=None, lambda2=0.0,
+            n_cycle_down=2, n_cycle_up=2, precision=FP64) -> MgDesc:
+    m = MgDesc()
+    m.i_phi, m.i_rhs, m.i_tmp = i_phi, i_rhs, i_tmp
+    m.n_cycle_down, m.n_cycle_up = n_cycle_down, n_cycle_up
+    m.helmholtz_lambda = float(lambda2)
+    for n in range(6):
+        m.bc_type[n] = int(bc_type[n]) if n < len(bc_type) else BC_NEUMANN
+        m.bc_val[n] = float(bc_val[n]) if bc_val is not None and n < len(bc_val) else 0.0
+    m.precision = precision
+    return m
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} not found: build it with __graft_entry__.build() "
+            "(the GPU path has no CPU fallback)")
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    sig = {
+        "afg_init": (C.c_int, [C.c_int, C.POINTER(P)]),
+        "afg_finalize": (C.c_int, [P]),
+        "afg_last_error": (C.c_char_p, [P]),
+        "afg_tree_sync": (C.c_int, [P, C.POINTER(TreeDesc), C.c_int, C.c_int]),
+        "afg_cc_upload": (C.c_int, [P, C.c_int, C.POINTER(_DP), C.c_longlong]),
+        "afg_cc_download": (C.c_int, [P, C.c_int, C.POINTER(_DP), C.c_longlong]),
+        "afg_fc_upload": (C.c_int, [P, C.c_int, C.POINTER(_DP), C.c_longlong]),
+        "afg_fc_download": (C.c_int, [P, C.c_int, C.POINTER(_DP), C.c_longlong]),
+        "afg_set_cc_methods": (C.c_int, [P, C.c_int, C.POINTER(GcDesc)]),
+        "afg_gc": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
+        "afg_maxabs": (C.c_int, [P, C.c_int, C.c_int, _DP]),
+        "afg_mg_setup": (C.c_int, [P, C.c_int, C.POINTER(MgDesc)]),
+        "afg_mg_set_bc_values": (C.c_int, [P, C.c_int, _DP]),
+        "afg_mg_vcycle": (C.c_int, [P, C.c_int, C.c_int, C.c_int, _DP]),
+        "afg_mg_fmg": (C.c_int, [P, C.c_int, C.c_int, C.c_int, _DP]),
+        "afg_mg_solve": (C.c_int, [P, C.c_int, C.c_double, C.c_int, _IP, _DP]),
+        "afg_mg_gsrb_lvl": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
+        "afg_mg_update_coarse": (C.c_int, [P, C.c_int, C.c_int]),
+        "afg_mg_correct_lvl": (C.c_int, [P, C.c_int, C.c_int]),
+        "afg_mg_coarse_solve": (C.c_int, [P, C.c_int]),
+        "afg_mg_residual": (C.c_int, [P, C.c_int, C.c_int]),
+        "afg_sync": (C.c_int, [P]),
+        "afg_launch_count": (C.c_longlong, [P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+class AfgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"afivo_gpu error {code}: {msg}")
+        self.code = code
+
+
+def box_pointers(cc: np.ndarray):
+    """Per-box pointer array for a host array laid out like the reference's
+    boxes: cc[n_boxes, n_var, ...] (box%cc of box id at row id-1)."""
+    nb = cc.shape[0]
+    stride = cc.strides[0]
+    base = cc.ctypes.data
+    arr = (_DP * nb)()
+    for b in range(nb):
+        arr[b] = C.cast(base + b * stride, _DP)
+    return arr
+
+
+class Context:
+    """One afivo tree mirrored on one GPU (wraps ``afg_ctx``)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        self.ptr = C.c_void_p()
+        rc = self.lib.afg_init(device, C.byref(self.ptr))
+        if rc != AFG_OK:
+            raise AfgError(rc, "afg_init failed (no CUDA device?)")
+        self._tree_holder = None
+        self.n_var = 0
+
+    def check(self, rc, what=""):
+        if rc != AFG_OK:
+            msg = self.lib.afg_last_error(self.ptr)
+            raise AfgError(rc, f"{what}: {msg.decode() if msg else ''}")
+        return rc
+
+    def close(self):
+        if self.ptr:
+            self.lib.afg_finalize(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- tree mirror ------------------------------------------------------
+    def tree_sync(self, tree, n_var_cell: int, n_var_face: int = 0):
+        self._tree_holder = TreeDescHolder(tree)
+        self.tree = tree
+        self.n_var = n_var_cell
+        self.n_var_face = n_var_face
+        self.check(self.lib.afg_tree_sync(self.ptr, C.byref(self._tree_holder.desc),
+                                          n_var_cell, n_var_face), "afg_tree_sync")
+
+    def upload(self, cc: np.ndarray, ivs=None):
+        """Upload variables ivs (1-based) from host boxes cc[n, n_var, ...]."""
+        cc = np.ascontiguousarray(cc, dtype=np.float64)
+        S = int(np.prod(cc.shape[2:]))
+        ptrs = box_pointers(cc)
+        for iv in (ivs if ivs is not None else range(1, cc.shape[1] + 1)):
+            self.check(self.lib.afg_cc_upload(self.ptr, iv, ptrs, (iv - 1) * S), "afg_cc_upload")
+
+    def download(self, cc: np.ndarray, ivs=None):
+        """Download variables ivs into host boxes cc[n, n_var, ...] (in place)."""
+        assert cc.flags.c_contiguous and cc.dtype == np.float64
+        S = int(np.prod(cc.shape[2:]))
+        ptrs = box_pointers(cc)
+        for iv in (ivs if ivs is not None else range(1, cc.shape[1] + 1)):
+            self.check(self.lib.afg_cc_download(self.ptr, iv, ptrs, (iv - 1) * S), "afg_cc_download")
+
+    def upload_fc(self, fc: np.ndarray, ivfs=None):
+        fc = np.ascontiguousarray(fc, dtype=np.float64)
+        F = int(np.prod(fc.shape[2:]))
+        ptrs = box_pointers(fc)
+        for iv in (ivfs if ivfs is not None else range(1, fc.shape[1] + 1)):
+            self.check(self.lib.afg_fc_upload(self.ptr, iv, ptrs, (iv - 1) * F), "afg_fc_upload")
+
+    def download_fc(self, fc: np.ndarray, ivfs=None):
+        assert fc.flags.c_contiguous and fc.dtype == np.float64
+        F = int(np.prod(fc.shape[2:]))
+        ptrs = box_pointers(fc)
+        for iv in (ivfs if ivfs is not None else range(1, fc.shape[1] + 1)):
+            self.check(self.lib.afg_fc_download(self.ptr, iv, ptrs, (iv - 1) * F), "afg_fc_download")
+
+    def set_cc_methods(self, iv, bc_type, bc_val=None, rb=RB_MG_SIDES):
+        g = gc_desc(bc_type, bc_val, rb)
+        self.check(self.lib.afg_set_cc_methods(self.ptr, iv, C.byref(g)), "afg_set_cc_methods")
+
+    def gc(self, iv, lvl=0, corners=True):
+        self.check(self.lib.afg_gc(self.ptr, iv, lvl, int(corners)), "afg_gc")
+
+    def maxabs(self, iv, leaves_only=True) -> float:
+        out = C.c_double()
+        self.check(self.lib.afg_maxabs(self.ptr, iv, int(leaves_only), C.byref(out)), "afg_maxabs")
+        return out.value
+
+    # -- multigrid --------------------------------------------------------
+    def mg_setup(self, mg_id, desc: MgDesc):
+        self.check(self.lib.afg_mg_setup(self.ptr, mg_id, C.byref(desc)), "afg_mg_setup")
+
+    def mg_set_bc_values(self, mg_id, vals):
+        a = np.zeros(6)
+        a[:len(vals)] = vals
+        self.check(self.lib.afg_mg_set_bc_values(self.ptr, mg_id, _dp(a)), "afg_mg_set_bc_values")
+
+    def mg_vcycle(self, mg_id, set_residual=True, max_lvl=0):
+        out = C.c_double(0)
+        self.check(self.lib.afg_mg_vcycle(self.ptr, mg_id, int(set_residual), max_lvl, C.byref(out)),
+                   "afg_mg_vcycle")
+        return out.value
+
+    def mg_fmg(self, mg_id, set_residual=True, have_guess=False):
+        out = C.c_double(0)
+        self.check(self.lib.afg_mg_fmg(self.ptr, mg_id, int(set_residual), int(have_guess), C.byref(out)),
+                   "afg_mg_fmg")
+        return out.value
+
+    def mg_solve(self, mg_id, threshold, max_cycles=50, allow_noconv=False):
+        n = C.c_int(0)
+        res = np.zeros(max_cycles)
+        rc = self.lib.afg_mg_solve(self.ptr, mg_id, threshold, max_cycles, C.byref(n), _dp(res))
+        if not (allow_noconv and rc == AFG_ERR_NOCONV):
+            self.check(rc, "afg_mg_solve")
+        return n.value, res[:n.value].copy()
+
+    def mg_gsrb_lvl(self, mg_id, lvl, cycle_type):
+        self.check(self.lib.afg_mg_gsrb_lvl(self.ptr, mg_id, lvl, cycle_type), "afg_mg_gsrb_lvl")
+
+    def mg_update_coarse(self, mg_id, lvl):
+        self.check(self.lib.afg_mg_update_coarse(self.ptr, mg_id, lvl), "afg_mg_update_coarse")
+
+    def mg_correct_lvl(self, mg_id, lvl):
+        self.check(self.lib.afg_mg_correct_lvl(self.ptr, mg_id, lvl), "afg_mg_correct_lvl")
+
+    def mg_coarse_solve(self, mg_id):
+        self.check(self.lib.afg_mg_coarse_solve(self.ptr, mg_id), "afg_mg_coarse_solve")
+
+    def mg_residual(self, mg_id, max_lvl=0):
+        self.check(self.lib.afg_mg_residual(self.ptr, mg_id, max_lvl), "afg_mg_residual")
+
+    def sync(self):
+        self.check(self.lib.afg_sync(self.ptr), "afg_sync")
+
+    def launch_count(self) -> int:
+        return int(self.lib.afg_launch_count(self.ptr))
+
+
+def new_cc(tree, n_var) -> np.ndarray:
+    """Host boxes laid out like box%cc: [n_boxes, n_var, (k,) j, i]."""
+    n2 = tree.n_cell + 2
+    return np.zeros((tree.n_boxes, n_var) + (n2,) * tree.ndim)

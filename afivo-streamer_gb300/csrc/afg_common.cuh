@@ -1,0 +1,82 @@
+// afg_common.cuh -- device data model shared by all kernels of the afivo hot
+// path on sm_103a.
+//
+// HBM layout: one pool per cell-centred variable, box-major:
+//   pool[slot][(nc+2)^D], slot = box id - 1, cell (i,j[,k]) at
+//   i + (nc+2)*(j + (nc+2)*k), i.e. exactly the per-box, per-variable block of
+//   the reference's box%cc(0:nc+1, ..., iv) (afivo/src/m_af_types.f90:302).
+// Face-centred variables: pool[slot][dim][(nc+1)^D] (box%fc, 303).
+// Box tables are int arrays indexed by slot with neighbour/child/parent ids
+// converted to slots (negative = none, see KTree).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace afg {
+
+constexpr int kNbPhys = -2;   // physical boundary (af_phys_boundary)
+constexpr int kNbRefine = -1; // refinement boundary (af_no_box)
+
+// Device view of the tree tables, passed to kernels by value.
+struct KTree {
+  int D, nc, n2, S, NF;
+  const int* parent;    // [n] parent slot or -1
+  const int* children;  // [n][2^D] child slot or -1
+  const int* nbr;       // [n][2D] neighbour slot, kNbRefine or kNbPhys
+  const int* pnb;       // [n][2D] slot of parent's neighbour (refinement faces)
+  const int* nbmat;     // [n][3^D] same-level box at each offset (or -1)
+  const int* ix;        // [n][D]  box%ix (1-based)
+  const double* r_min;  // [n][D]
+  const double* dr;     // [n][D]
+};
+
+// Ghost-cell method of one variable (bc per domain face + refinement rule).
+struct GcDev {
+  int bc_type[6];
+  double bc_val[6];
+  int rb;
+};
+
+__device__ __forceinline__ int at2(int n2, int i, int j) { return i + n2 * j; }
+__device__ __forceinline__ int at3(int n2, int i, int j, int k) { return i + n2 * (j + n2 * k); }
+
+// cell with normal dimension d at normal index x, tangential indices p (the
+// lower remaining dimension) and q (the higher one)
+template <int D>
+__device__ __forceinline__ int face_at(int n2, int d, int x, int p, int q) {
+  if (D == 2) return d == 0 ? at2(n2, x, p) : at2(n2, p, x);
+  if (d == 0) return at3(n2, x, p, q);
+  if (d == 1) return at3(n2, p, x, q);
+  return at3(n2, p, q, x);
+}
+
+__device__ __forceinline__ int child_offset(const KTree& t, int slot, int d) {
+  return ((t.ix[slot * t.D + d] - 1) & 1) * (t.nc / 2);
+}
+
+// Non-negative doubles order like their bit patterns: max via atomicMax.
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
+  atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+template <typename T>
+__device__ __forceinline__ T block_max(T v, T* sbuf) {
+  for (int o = 16; o > 0; o >>= 1) {
+    T w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = v > w ? v : w;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) sbuf[warp] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  if (warp == 0) {
+    v = lane < nw ? sbuf[lane] : T(0);
+    for (int o = 16; o > 0; o >>= 1) {
+      T w = __shfl_xor_sync(0xffffffffu, v, o);
+      v = v > w ? v : w;
+    }
+  }
+  return v;  // valid in thread 0
+}
+
+}  // namespace afg

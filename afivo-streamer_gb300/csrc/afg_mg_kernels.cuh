@@ -1,0 +1,418 @@
+// afg_mg_kernels.cuh -- FAS multigrid stages on box lists (afivo/src/
+// m_af_multigrid.f90, m_af_stencil.f90, m_af_restrict.f90).
+//
+// Every kernel takes a device list of box slots of one level and processes
+// one box per CTA.  The arithmetic follows the reference expression by
+// expression (left-to-right, no contraction: the library is built with
+// --fmad=false) so that the FP64 instantiation reproduces the CPU oracle
+// bit for bit; the FP32 instantiation is the inner solver of the mixed path.
+#pragma once
+#include "afg_common.cuh"
+
+namespace afg {
+
+// Operator coefficients mg_box_lpl_stencil (m_af_multigrid.f90:1246-1264):
+// c = [-sum(c(2:)) - lambda^2, 1/dx^2, 1/dx^2, 1/dy^2, 1/dy^2(, 1/dz^2 x2)],
+// always formed in FP64 and rounded to T.
+template <int D>
+__device__ __forceinline__ void lpl_coeffs(const KTree& t, int slot, double lambda2, double c[7]) {
+  double inv[3];
+  for (int d = 0; d < D; d++) {
+    const double h = t.dr[slot * D + d];
+    inv[d] = 1 / (h * h);
+  }
+  for (int d = 0; d < D; d++) c[1 + 2 * d] = c[2 + 2 * d] = inv[d];
+  double s = 0;
+  for (int k = 1; k <= 2 * D; k++) s += c[k];
+  c[0] = -s - lambda2;
+}
+
+// Cylindrical correction per radial index i (af_cyl_flux_factors,
+// m_af_types.f90:1199-1211; m_af_stencil.f90:884-906).
+__device__ __forceinline__ void cyl_coeffs(const KTree& t, int slot, int i, const double c[7],
+                                           double& k1, double& k2, double& k3) {
+  const double rmin = t.r_min[slot * 2], h = t.dr[slot * 2];
+  const double r = rmin + (i - 0.5) * h;
+  const double inv_r = 1 / r;
+  const double f1 = (r - 0.5 * h) * inv_r, f2 = (r + 0.5 * h) * inv_r;
+  k2 = f1 * c[1];
+  k3 = f2 * c[2];
+  k1 = c[0] - (k2 - c[1]) - (k3 - c[2]);
+}
+
+// L phi at interior cell (i,j[,k]); stencil_apply_357 (m_af_stencil.f90:367-496)
+template <int D, bool CYL, typename T>
+__device__ __forceinline__ T apply_lpl(const T* __restrict__ p, int n2, int i, int j, int k,
+                                       const T c[7], T k1, T k2, T k3) {
+  if (D == 2) {
+    const int x = at2(n2, i, j);
+    if (CYL)
+      return k1 * p[x] + k2 * p[x - 1] + k3 * p[x + 1] + c[3] * p[x - n2] + c[4] * p[x + n2];
+    return c[0] * p[x] + c[1] * p[x - 1] + c[2] * p[x + 1] + c[3] * p[x - n2] + c[4] * p[x + n2];
+  } else {
+    const int x = at3(n2, i, j, k), sk = n2 * n2;
+    return c[0] * p[x] + c[1] * p[x - 1] + c[2] * p[x + 1] + c[3] * p[x - n2] + c[4] * p[x + n2] +
+           c[5] * p[x - sk] + c[6] * p[x + sk];
+  }
+}
+
+// One red-black half sweep on each box of the list; stencil_gsrb_357
+// (m_af_stencil.f90:838-998).  Updated cells satisfy (i+j[+k]+n) even.
+template <int D, bool CYL, typename T>
+__global__ void __launch_bounds__(256) k_gsrb(KTree t, const int* __restrict__ list, T* __restrict__ phi,
+                                              const T* __restrict__ rhs, int redblack, double lambda2) {
+  const int slot = list[blockIdx.x];
+  const int nc = t.nc, n2 = t.n2, hn = nc / 2;
+  double cd[7];
+  lpl_coeffs<D>(t, slot, lambda2, cd);
+  T c[7];
+  for (int q = 0; q < 7; q++) c[q] = T(cd[q]);
+  const T inv_c1 = T(1 / cd[0]);
+  T* p = phi + (size_t)slot * t.S;
+  const T* f = rhs + (size_t)slot * t.S;
+  const int count = D == 2 ? nc * hn : nc * nc * hn;
+  for (int w = threadIdx.x; w < count; w += blockDim.x) {
+    const int row = w / hn, col = w - row * hn;
+    if (D == 2) {
+      const int j = row + 1;
+      const int i = 2 - ((redblack ^ j) & 1) + 2 * col;
+      const int x = at2(n2, i, j);
+      if (CYL) {
+        double k1, k2, k3;
+        cyl_coeffs(t, slot, i, cd, k1, k2, k3);
+        const T inv1 = T(1 / k1);
+        p[x] = (f[x] - T(k2) * p[x - 1] - T(k3) * p[x + 1] - c[3] * p[x - n2] - c[4] * p[x + n2]) * inv1;
+      } else {
+        p[x] = (f[x] - c[1] * p[x - 1] - c[2] * p[x + 1] - c[3] * p[x - n2] - c[4] * p[x + n2]) * inv_c1;
+      }
+    } else {
+      const int j = row % nc + 1, k = row / nc + 1;
+      const int i = 2 - ((redblack ^ (k + j)) & 1) + 2 * col;
+      const int x = at3(n2, i, j, k), sk = n2 * n2;
+      p[x] = (f[x] - c[1] * p[x - 1] - c[2] * p[x + 1] - c[3] * p[x - n2] - c[4] * p[x + n2] -
+              c[5] * p[x - sk] - c[6] * p[x + sk]) *
+             inv_c1;
+    }
+  }
+}
+
+// Residual on interior cells into tmp (residual_box, m_af_multigrid.f90:
+// 801-810); the max |r| over the boxes flagged in is_leaf is folded into
+// *maxbits (may be null).
+template <int D, bool CYL, typename T>
+__global__ void __launch_bounds__(256) k_residual(KTree t, const int* __restrict__ list, const T* __restrict__ phi,
+                                                  const T* __restrict__ rhs, T* __restrict__ tmp, double lambda2,
+                                                  const unsigned char* __restrict__ is_leaf,
+                                                  unsigned long long* maxbits) {
+  __shared__ T sred[32];
+  const int slot = list[blockIdx.x];
+  const int nc = t.nc, n2 = t.n2;
+  double cd[7];
+  lpl_coeffs<D>(t, slot, lambda2, cd);
+  T c[7];
+  for (int q = 0; q < 7; q++) c[q] = T(cd[q]);
+  const T* p = phi + (size_t)slot * t.S;
+  const T* f = rhs + (size_t)slot * t.S;
+  T* o = tmp + (size_t)slot * t.S;
+  const int count = D == 2 ? nc * nc : nc * nc * nc;
+  T mx = T(0);
+  for (int w = threadIdx.x; w < count; w += blockDim.x) {
+    const int i = w % nc + 1, r = w / nc;
+    const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
+    T k1 = T(0), k2 = T(0), k3 = T(0);
+    if (CYL) {
+      double a, b, e;
+      cyl_coeffs(t, slot, i, cd, a, b, e);
+      k1 = T(a); k2 = T(b); k3 = T(e);
+    }
+    const int x = D == 2 ? at2(n2, i, j) : at3(n2, i, j, k);
+    const T res = f[x] - apply_lpl<D, CYL, T>(p, n2, i, j, k, c, k1, k2, k3);
+    o[x] = res;
+    const T ar = res < T(0) ? -res : res;
+    mx = ar > mx ? ar : mx;
+  }
+  if (maxbits != nullptr && is_leaf[slot]) {
+    mx = block_max<T>(mx, sred);
+    if (threadIdx.x == 0) atomic_max_nonneg(maxbits, double(mx));
+  }
+}
+
+// update_coarse first half (m_af_multigrid.f90:706-719): residual of each
+// child box restricted to its parent's tmp (with the cylindrical weights,
+// af_restrict_box use_geometry=.true., m_af_restrict.f90:62-136), phi
+// restricted without geometry (mg_box_rstr_lpl 1227-1242).  One thread per
+// parent cell covered by the child.
+template <int D, bool CYL, typename T>
+__global__ void __launch_bounds__(256) k_residual_restrict(KTree t, const int* __restrict__ list,
+                                                           T* __restrict__ phi, const T* __restrict__ rhs,
+                                                           T* __restrict__ tmp, double lambda2,
+                                                           int store_child_residual) {
+  const int slot = list[blockIdx.x];
+  const int pslot = t.parent[slot];
+  const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
+  double cd[7];
+  lpl_coeffs<D>(t, slot, lambda2, cd);
+  T c[7];
+  for (int q = 0; q < 7; q++) c[q] = T(cd[q]);
+  const T* p = phi + (size_t)slot * t.S;
+  const T* f = rhs + (size_t)slot * t.S;
+  T* pp = phi + (size_t)pslot * t.S;
+  T* pt = tmp + (size_t)pslot * t.S;
+  T* ct = tmp + (size_t)slot * t.S;
+  const int o0 = child_offset(t, slot, 0), o1 = child_offset(t, slot, 1);
+  const int o2 = D == 3 ? child_offset(t, slot, 2) : 0;
+  const int count = D == 2 ? hnc * hnc : hnc * hnc * hnc;
+  for (int w = threadIdx.x; w < count; w += blockDim.x) {
+    const int i = w % hnc + 1, r = w / hnc;
+    const int j = D == 2 ? r + 1 : r % hnc + 1, k = D == 2 ? 0 : r / hnc + 1;
+    const int ic = o0 + i, jc = o1 + j, kc = o2 + k;
+    const int fi = 2 * i - 1, fj = 2 * j - 1, fk = D == 3 ? 2 * k - 1 : 0;
+    if (D == 2) {
+      T res[2][2];  // [dj][di]
+      for (int dj = 0; dj < 2; dj++)
+        for (int di = 0; di < 2; di++) {
+          T k1 = T(0), k2 = T(0), k3 = T(0);
+          if (CYL) {
+            double a, b, e;
+            cyl_coeffs(t, slot, fi + di, cd, a, b, e);
+            k1 = T(a); k2 = T(b); k3 = T(e);
+          }
+          const int x = at2(n2, fi + di, fj + dj);
+          res[dj][di] = f[x] - apply_lpl<D, CYL, T>(p, n2, fi + di, fj + dj, 0, c, k1, k2, k3);
+          if (store_child_residual) ct[x] = res[dj][di];
+        }
+      T rv;
+      if (CYL) {
+        const double rp = t.r_min[pslot * 2] + (ic - 0.5) * t.dr[pslot * 2];
+        const double tw = 0.25 * t.dr[pslot * 2] / rp;
+        const T w1 = T(1 - tw), w2 = T(1 + tw);
+        T s1 = T(0), s2 = T(0);
+        s1 = s1 + res[0][0]; s1 = s1 + res[1][0];
+        s2 = s2 + res[0][1]; s2 = s2 + res[1][1];
+        rv = T(0.25) * (w1 * s1 + w2 * s2);
+      } else {
+        T s = T(0);
+        s = s + res[0][0]; s = s + res[0][1]; s = s + res[1][0]; s = s + res[1][1];
+        rv = T(0.25) * s;
+      }
+      pt[at2(n2, ic, jc)] = rv;
+      T s = T(0);
+      s = s + p[at2(n2, fi, fj)]; s = s + p[at2(n2, fi + 1, fj)];
+      s = s + p[at2(n2, fi, fj + 1)]; s = s + p[at2(n2, fi + 1, fj + 1)];
+      pp[at2(n2, ic, jc)] = T(0.25) * s;
+    } else {
+      T sr = T(0), sp = T(0);
+      for (int dk = 0; dk < 2; dk++)
+        for (int dj = 0; dj < 2; dj++)
+          for (int di = 0; di < 2; di++) {
+            const int x = at3(n2, fi + di, fj + dj, fk + dk);
+            const T res = f[x] - apply_lpl<D, false, T>(p, n2, fi + di, fj + dj, fk + dk, c, T(0), T(0), T(0));
+            if (store_child_residual) ct[x] = res;
+            sr = sr + res;
+            sp = sp + p[x];
+          }
+      pt[at3(n2, ic, jc, kc)] = T(0.125) * sr;
+      pp[at3(n2, ic, jc, kc)] = T(0.125) * sp;
+    }
+  }
+}
+
+// update_coarse second half (m_af_multigrid.f90:723-737) on the parents of
+// the level: rhs = L phi + tmp (interior), tmp = phi (whole array).  The
+// reference also adds tmp to rhs in the ghost cells; rhs ghost cells are
+// never read, so they are left untouched.  With copy_tmp = 0 this is the
+// rhs part of set_coarse_phi_rhs (742-776).
+template <int D, bool CYL, typename T>
+__global__ void __launch_bounds__(256) k_coarse_fas(KTree t, const int* __restrict__ list,
+                                                    const T* __restrict__ phi, T* __restrict__ rhs,
+                                                    T* __restrict__ tmp, double lambda2, int copy_tmp) {
+  const int slot = list[blockIdx.x];
+  const int nc = t.nc, n2 = t.n2;
+  double cd[7];
+  lpl_coeffs<D>(t, slot, lambda2, cd);
+  T c[7];
+  for (int q = 0; q < 7; q++) c[q] = T(cd[q]);
+  const T* p = phi + (size_t)slot * t.S;
+  T* f = rhs + (size_t)slot * t.S;
+  T* o = tmp + (size_t)slot * t.S;
+  for (int x = threadIdx.x; x < t.S; x += blockDim.x) {
+    const int i = x % n2, r = x / n2;
+    const int j = D == 2 ? r : r % n2, k = D == 2 ? 0 : r / n2;
+    const bool interior = i >= 1 && i <= nc && j >= 1 && j <= nc && (D == 2 || (k >= 1 && k <= nc));
+    if (interior) {
+      T k1 = T(0), k2 = T(0), k3 = T(0);
+      if (CYL) {
+        double a, b, e;
+        cyl_coeffs(t, slot, i, cd, a, b, e);
+        k1 = T(a); k2 = T(b); k3 = T(e);
+      }
+      const T lp = apply_lpl<D, CYL, T>(p, n2, i, j, k, c, k1, k2, k3);
+      f[x] = lp + o[x];
+    }
+    if (copy_tmp) o[x] = p[x];
+  }
+}
+
+// correct_children (m_af_multigrid.f90:624-646): on each parent,
+// tmp = phi - tmp over the whole array, then each child's phi gets the
+// bilinear/trilinear prolongation of tmp added (stencil_prolong_248,
+// m_af_stencil.f90:695-815, coefficients 1267-1284).
+template <int D, typename T>
+__global__ void __launch_bounds__(256) k_correct(KTree t, const int* __restrict__ list, T* __restrict__ phi,
+                                                 T* __restrict__ tmp) {
+  extern __shared__ unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  const int slot = list[blockIdx.x];
+  const int nc = t.nc, n2 = t.n2;
+  T* pp = phi + (size_t)slot * t.S;
+  T* pt = tmp + (size_t)slot * t.S;
+  for (int x = threadIdx.x; x < t.S; x += blockDim.x) {
+    const T v = pp[x] - pt[x];
+    pt[x] = v;
+    sm[x] = v;
+  }
+  __syncthreads();
+  const int nch = 1 << D;
+  const int ncell = D == 2 ? nc * nc : nc * nc * nc;
+  for (int w = threadIdx.x; w < nch * ncell; w += blockDim.x) {
+    const int ch = w / ncell, cw = w - ch * ncell;
+    const int cs = t.children[slot * nch + ch];
+    if (cs < 0) continue;
+    const int i = cw % nc + 1, r = cw / nc;
+    const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
+    const int o0 = child_offset(t, cs, 0), o1 = child_offset(t, cs, 1);
+    const int i1 = o0 + ((i + 1) >> 1), i2 = i1 + 1 - 2 * (i & 1);
+    const int j1 = o1 + ((j + 1) >> 1), j2 = j1 + 1 - 2 * (j & 1);
+    T* cp = phi + (size_t)cs * t.S;
+    if (D == 2) {
+      const int x = at2(n2, i, j);
+      cp[x] = cp[x] + T(9 / 16.0) * sm[at2(n2, i1, j1)] + T(3 / 16.0) * sm[at2(n2, i2, j1)] +
+              T(3 / 16.0) * sm[at2(n2, i1, j2)] + T(1 / 16.0) * sm[at2(n2, i2, j2)];
+    } else {
+      const int o2 = child_offset(t, cs, 2);
+      const int k1 = o2 + ((k + 1) >> 1), k2 = k1 + 1 - 2 * (k & 1);
+      const int x = at3(n2, i, j, k);
+      cp[x] = cp[x] + T(27 / 64.0) * sm[at3(n2, i1, j1, k1)] + T(9 / 64.0) * sm[at3(n2, i2, j1, k1)] +
+              T(9 / 64.0) * sm[at3(n2, i1, j2, k1)] + T(3 / 64.0) * sm[at3(n2, i2, j2, k1)] +
+              T(9 / 64.0) * sm[at3(n2, i1, j1, k2)] + T(3 / 64.0) * sm[at3(n2, i2, j1, k2)] +
+              T(3 / 64.0) * sm[at3(n2, i1, j2, k2)] + T(1 / 64.0) * sm[at3(n2, i2, j2, k2)];
+    }
+  }
+}
+
+// init_phi_rhs (m_af_multigrid.f90:779-799) on one level: phi = 0 on the
+// whole array, rhs restricted to the parent with geometry.
+template <int D, bool CYL, typename T>
+__global__ void __launch_bounds__(256) k_init_phi_rhs(KTree t, const int* __restrict__ list,
+                                                      T* __restrict__ phi, T* __restrict__ rhs) {
+  const int slot = list[blockIdx.x];
+  const int pslot = t.parent[slot];
+  const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
+  T* p = phi + (size_t)slot * t.S;
+  const T* f = rhs + (size_t)slot * t.S;
+  T* pf = rhs + (size_t)pslot * t.S;
+  for (int x = threadIdx.x; x < t.S; x += blockDim.x) p[x] = T(0);
+  const int o0 = child_offset(t, slot, 0), o1 = child_offset(t, slot, 1);
+  const int o2 = D == 3 ? child_offset(t, slot, 2) : 0;
+  const int count = D == 2 ? hnc * hnc : hnc * hnc * hnc;
+  for (int w = threadIdx.x; w < count; w += blockDim.x) {
+    const int i = w % hnc + 1, r = w / hnc;
+    const int j = D == 2 ? r + 1 : r % hnc + 1, k = D == 2 ? 0 : r / hnc + 1;
+    const int ic = o0 + i, jc = o1 + j, kc = o2 + k;
+    const int fi = 2 * i - 1, fj = 2 * j - 1, fk = D == 3 ? 2 * k - 1 : 0;
+    if (D == 2) {
+      T rv;
+      if (CYL) {
+        const double rp = t.r_min[pslot * 2] + (ic - 0.5) * t.dr[pslot * 2];
+        const double tw = 0.25 * t.dr[pslot * 2] / rp;
+        const T w1 = T(1 - tw), w2 = T(1 + tw);
+        T s1 = T(0), s2 = T(0);
+        s1 = s1 + f[at2(n2, fi, fj)]; s1 = s1 + f[at2(n2, fi, fj + 1)];
+        s2 = s2 + f[at2(n2, fi + 1, fj)]; s2 = s2 + f[at2(n2, fi + 1, fj + 1)];
+        rv = T(0.25) * (w1 * s1 + w2 * s2);
+      } else {
+        T s = T(0);
+        s = s + f[at2(n2, fi, fj)]; s = s + f[at2(n2, fi + 1, fj)];
+        s = s + f[at2(n2, fi, fj + 1)]; s = s + f[at2(n2, fi + 1, fj + 1)];
+        rv = T(0.25) * s;
+      }
+      pf[at2(n2, ic, jc)] = rv;
+    } else {
+      T s = T(0);
+      for (int dk = 0; dk < 2; dk++)
+        for (int dj = 0; dj < 2; dj++)
+          for (int di = 0; di < 2; di++) s = s + f[at3(n2, fi + di, fj + dj, fk + dk)];
+      pf[at3(n2, ic, jc, kc)] = T(0.125) * s;
+    }
+  }
+}
+
+// Whole-array copy of one variable on a box list (af_boxes_copy_cc,
+// m_af_utils.f90:579-588).
+template <typename T>
+__global__ void __launch_bounds__(256) k_copy(int S, const int* __restrict__ list, const T* __restrict__ src,
+                                              T* __restrict__ dst) {
+  const int slot = list[blockIdx.x];
+  for (int x = threadIdx.x; x < S; x += blockDim.x) dst[(size_t)slot * S + x] = src[(size_t)slot * S + x];
+}
+
+// Coarse-grid right-hand side with the boundary values folded in
+// (coarse_solver_set_rhs_phi, m_coarse_solver.f90:286-338).
+template <typename T>
+__global__ void k_coarse_gather(int n, int D, const int* __restrict__ cslot, const int* __restrict__ ccell,
+                                const double* __restrict__ b2r, const unsigned char* __restrict__ bmask,
+                                const double* __restrict__ bc_val, const T* __restrict__ rhs, int S,
+                                double* __restrict__ b) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  double v = double(rhs[(size_t)cslot[g] * S + ccell[g]]);
+  const unsigned m = bmask[g];
+  for (int nb = 0; nb < 2 * D; nb++)
+    if (m & (1u << nb)) v = v + b2r[g * 2 * D + nb] * bc_val[nb];
+  b[g] = v;
+}
+
+// x = A^-1 b, one warp per row: 32 strided partial sums then an xor
+// butterfly; the CPU oracle uses the same order.
+__global__ void k_coarse_matvec(int n, const double* __restrict__ ainv, const double* __restrict__ b,
+                                double* __restrict__ x) {
+  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const double* a = ainv + (size_t)row * n;
+  double s = 0.0;
+  for (int c = lane; c < n; c += 32) s = s + a[c] * b[c];
+  for (int o = 16; o > 0; o >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) x[row] = s;
+}
+
+template <typename T>
+__global__ void k_coarse_scatter(int n, const int* __restrict__ cslot, const int* __restrict__ ccell,
+                                 const double* __restrict__ x, T* __restrict__ phi, int S) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  phi[(size_t)cslot[g] * S + ccell[g]] = T(x[g]);
+}
+
+// max |v| over interior cells of the list's boxes
+template <int D, typename T>
+__global__ void __launch_bounds__(256) k_maxabs(KTree t, const int* __restrict__ list, const T* __restrict__ v,
+                                                unsigned long long* maxbits) {
+  __shared__ T sred[32];
+  const int slot = list[blockIdx.x];
+  const int nc = t.nc, n2 = t.n2;
+  const T* a = v + (size_t)slot * t.S;
+  const int count = D == 2 ? nc * nc : nc * nc * nc;
+  T mx = T(0);
+  for (int w = threadIdx.x; w < count; w += blockDim.x) {
+    const int i = w % nc + 1, r = w / nc;
+    const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
+    const T val = a[D == 2 ? at2(n2, i, j) : at3(n2, i, j, k)];
+    const T av = val < T(0) ? -val : val;
+    mx = av > mx ? av : mx;
+  }
+  mx = block_max<T>(mx, sred);
+  if (threadIdx.x == 0) atomic_max_nonneg(maxbits, double(mx));
+}
+
+}  // namespace afg

@@ -1,0 +1,106 @@
+// afg_mixed.cuh -- mixed-precision multigrid solve: an FP64 defect-correction
+// (iterative refinement) loop around the FP32 FAS V-cycle.
+//
+//   r = rhs - L(phi)            FP64, all boxes; max |r| over leaves
+//   L e = r, e = 0 initially    one FP32 V-cycle, homogeneous boundary values
+//   phi = phi + e               FP64, interior and ghost cells
+//
+// L is affine in phi (boundary and refinement-boundary ghost rules are
+// linear), so e's ghost cells, filled by the same rules with zero boundary
+// values, are the ghost-cell correction of phi.  The coarsest-level solve
+// stays FP64 (the dense inverse), as do phi, rhs and the residual.
+// Included by afg_runtime.cu.
+#pragma once
+
+namespace afg {
+
+// r (FP64 residual on interior cells) -> r32, e32 = 0 (whole box), max |r|
+// over leaves into *maxbits.
+template <int D, bool CYL>
+__global__ void __launch_bounds__(256) k_defect(KTree t, const int* __restrict__ list, const double* __restrict__ phi,
+                                                const double* __restrict__ rhs, float* __restrict__ r32,
+                                                float* __restrict__ e32, double lambda2,
+                                                const unsigned char* __restrict__ is_leaf,
+                                                unsigned long long* maxbits) {
+  __shared__ double sred[32];
+  const int slot = list[blockIdx.x];
+  const int nc = t.nc, n2 = t.n2;
+  double cd[7];
+  lpl_coeffs<D>(t, slot, lambda2, cd);
+  const double* p = phi + (size_t)slot * t.S;
+  const double* f = rhs + (size_t)slot * t.S;
+  float* ro = r32 + (size_t)slot * t.S;
+  float* eo = e32 + (size_t)slot * t.S;
+  double mx = 0.0;
+  for (int x = threadIdx.x; x < t.S; x += blockDim.x) {
+    eo[x] = 0.0f;
+    const int i = x % n2, rr = x / n2;
+    const int j = D == 2 ? rr : rr % n2, k = D == 2 ? 0 : rr / n2;
+    const bool interior = i >= 1 && i <= nc && j >= 1 && j <= nc && (D == 2 || (k >= 1 && k <= nc));
+    if (!interior) continue;
+    double k1 = 0, k2 = 0, k3 = 0;
+    if (CYL) cyl_coeffs(t, slot, i, cd, k1, k2, k3);
+    const double res = f[x] - apply_lpl<D, CYL, double>(p, n2, i, j, k, cd, k1, k2, k3);
+    ro[x] = float(res);
+    const double ar = fabs(res);
+    mx = ar > mx ? ar : mx;
+  }
+  if (is_leaf[slot]) {
+    mx = block_max<double>(mx, sred);
+    if (threadIdx.x == 0) atomic_max_nonneg(maxbits, mx);
+  }
+}
+
+// phi += e on whole boxes (ghost cells included)
+__global__ void __launch_bounds__(256) k_add_correction(int S, const int* __restrict__ list, double* __restrict__ phi,
+                                                        const float* __restrict__ e32) {
+  const int slot = list[blockIdx.x];
+  double* p = phi + (size_t)slot * S;
+  const float* e = e32 + (size_t)slot * S;
+  for (int x = threadIdx.x; x < S; x += blockDim.x) p[x] = p[x] + double(e[x]);
+}
+
+}  // namespace afg
+
+static int launch_defect(afg_ctx* ctx, MgSlot& m, const double* phi, const double* rhs, unsigned long long* maxbits) {
+  const int n = ctx->n_all;
+  if (n <= 0) return AFG_OK;
+  KTree t = ktree(ctx);
+  const int* list = lst(ctx, ctx->off_all);
+  if (ctx->D == 3)
+    k_defect<3, false><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, m.d.helmholtz_lambda,
+                                                   ctx->d_is_leaf, maxbits);
+  else if (ctx->coord == AFG_CYL)
+    k_defect<2, true><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, m.d.helmholtz_lambda,
+                                                  ctx->d_is_leaf, maxbits);
+  else
+    k_defect<2, false><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, m.d.helmholtz_lambda,
+                                                   ctx->d_is_leaf, maxbits);
+  ctx->launches++;
+  CKL();
+  return AFG_OK;
+}
+
+static int mixed_solve(afg_ctx* ctx, MgSlot& m, double threshold, int max_cycles, int* n_done, double* residuals) {
+  double* phi = ctx->cc[m.d.i_phi - 1];
+  double* rhs = ctx->cc[m.d.i_rhs - 1];
+  RC(reset_max(ctx, 2));
+  RC(launch_defect(ctx, m, phi, rhs, ctx->d_max + 2));
+  double r = 0;
+  RC(read_max(ctx, 2, &r));
+  int n = 0;
+  while (n < max_cycles) {
+    RC(mg_vcycle<float>(ctx, m, ctx->highest_lvl, m.e32, m.r32, m.t32, false, true, nullptr));
+    k_add_correction<<<ctx->n_all, 256, 0, ctx->stream>>>(ctx->S, lst(ctx, ctx->off_all), phi, m.e32);
+    ctx->launches++;
+    CKL();
+    RC(reset_max(ctx, 2));
+    RC(launch_defect(ctx, m, phi, rhs, ctx->d_max + 2));
+    RC(read_max(ctx, 2, &r));
+    if (residuals) residuals[n] = r;
+    n++;
+    if (r < threshold) break;
+  }
+  if (n_done) *n_done = n;
+  return r < threshold ? AFG_OK : AFG_ERR_NOCONV;
+}

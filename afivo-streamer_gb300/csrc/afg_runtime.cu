@@ -1,0 +1,1070 @@
+// afg_runtime.cu -- C-ABI implementation (include/afivo_gpu.h): device
+// mirror of the afivo tree, variable pools, and the multigrid drivers
+// (mg_fas_vcycle / mg_fas_fmg of afivo/src/m_af_multigrid.f90:137-264 and
+// the V-cycle loop of field_compute, src/m_field.f90:520-524) as sequences
+// of box-list kernels on one CUDA stream.
+//
+// There is no CPU fallback: every entry point either launches its kernels or
+// returns an error code.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/afivo_gpu.h"
+#include "afg_common.cuh"
+#include "afg_gc_kernels.cuh"
+#include "afg_mg_kernels.cuh"
+#include "afg_transport.cuh"
+
+using namespace afg;
+
+namespace {
+
+constexpr int kMaxMg = 16;
+constexpr int kMaxCoarse = 4096;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct MgSlot {
+  bool used = false;
+  afg_mg_desc d{};
+  int n_coarse = 0;
+  double* d_ainv = nullptr;
+  double* d_b = nullptr;
+  double* d_x = nullptr;
+  double* d_b2r = nullptr;       // [n][2D]
+  unsigned char* d_bmask = nullptr;
+  double* d_bcval = nullptr;     // [6]
+  // FP32 inner-solver pools for AFG_MIXED (e, r, tmp)
+  float* e32 = nullptr;
+  float* r32 = nullptr;
+  float* t32 = nullptr;
+};
+
+}  // namespace
+
+struct afg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  long long launches = 0;
+  // tree
+  bool have_tree = false;
+  int D = 2, nc = 16, n2 = 18, S = 324, NF = 289, coord = AFG_XYZ, n_boxes = 0, highest_lvl = 0;
+  int cgs[3] = {1, 1, 1};
+  std::vector<int> h_ix;      // [n][D]
+  std::vector<int> h_nbr;     // [n][2D] raw Fortran ids
+  std::vector<std::vector<int>> lvl_ids, lvl_leaves, lvl_parents;  // 0-based slots
+  // device tables
+  int *d_parent = nullptr, *d_children = nullptr, *d_nbr = nullptr, *d_pnb = nullptr, *d_nbmat = nullptr,
+      *d_ix = nullptr;
+  double *d_rmin = nullptr, *d_dr = nullptr;
+  int* d_lists = nullptr;  // all level lists concatenated
+  std::vector<size_t> off_ids, off_leaves, off_parents;  // per level offsets into d_lists
+  size_t off_all = 0;       // list of all boxes, all levels (level order)
+  size_t off_all_leaves = 0;
+  int n_all = 0;            // boxes in all level lists
+  int n_all_leaves = 0;
+  unsigned char* d_is_leaf = nullptr;
+  int* d_cslot = nullptr;   // coarse unknown -> slot
+  int* d_ccell = nullptr;   // coarse unknown -> cell index
+  // pools
+  int n_var = 0, n_var_face = 0;
+  std::vector<double*> cc;  // [n_var]
+  std::vector<double*> fc;  // [n_var_face]
+  std::vector<GcDev> methods;
+  std::vector<bool> has_method;
+  // scratch
+  unsigned long long* d_max = nullptr;  // 8 slots
+  unsigned long long* h_max = nullptr;  // pinned
+  double* h_stage = nullptr;            // pinned staging
+  size_t stage_elems = 0;
+  MgSlot mg[kMaxMg];
+  // transport state (afg_transport.cuh)
+  TransportState tr;
+};
+
+/* ------------------------------------------------------------------------- */
+static int fail(afg_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define CK(call)                                                                           \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(ctx, AFG_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                                     \
+  } while (0)
+
+#define CKL()                                                                               \
+  do {                                                                                      \
+    cudaError_t e_ = cudaGetLastError();                                                    \
+    if (e_ != cudaSuccess)                                                                  \
+      return fail(ctx, AFG_ERR_CUDA, "kernel launch failed: %s (%s:%d)", cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                                      \
+  } while (0)
+
+template <typename T>
+static cudaError_t dalloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  return cudaMalloc((void**)p, n * sizeof(T));
+}
+
+template <typename T>
+static void dfree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+static KTree ktree(const afg_ctx* c) {
+  KTree t;
+  t.D = c->D;
+  t.nc = c->nc;
+  t.n2 = c->n2;
+  t.S = c->S;
+  t.NF = c->NF;
+  t.parent = c->d_parent;
+  t.children = c->d_children;
+  t.nbr = c->d_nbr;
+  t.pnb = c->d_pnb;
+  t.nbmat = c->d_nbmat;
+  t.ix = c->d_ix;
+  t.r_min = c->d_rmin;
+  t.dr = c->d_dr;
+  return t;
+}
+
+static const int* lst(const afg_ctx* c, size_t off) { return c->d_lists + off; }
+
+static void free_tree(afg_ctx* c) {
+  dfree(c->d_parent); dfree(c->d_children); dfree(c->d_nbr); dfree(c->d_pnb); dfree(c->d_nbmat);
+  dfree(c->d_ix); dfree(c->d_rmin); dfree(c->d_dr); dfree(c->d_lists); dfree(c->d_is_leaf);
+  dfree(c->d_cslot); dfree(c->d_ccell);
+  for (auto& p : c->cc) dfree(p);
+  for (auto& p : c->fc) dfree(p);
+  c->cc.clear();
+  c->fc.clear();
+  for (auto& m : c->mg) {
+    dfree(m.d_ainv); dfree(m.d_b); dfree(m.d_x); dfree(m.d_b2r); dfree(m.d_bmask); dfree(m.d_bcval);
+    dfree(m.e32); dfree(m.r32); dfree(m.t32);
+    m.used = false;
+  }
+  transport_free(c->tr);
+  if (c->h_stage) cudaFreeHost(c->h_stage);
+  c->h_stage = nullptr;
+  c->stage_elems = 0;
+  c->have_tree = false;
+}
+
+/* ------------------------------------------------------------------------- */
+// Generic launchers dispatching on (D, cylindrical, T)
+
+template <typename T>
+static int launch_gc(afg_ctx* ctx, const int* list, int n, T* v, const GcDev& g, int corners) {
+  if (n <= 0) return AFG_OK;
+  KTree t = ktree(ctx);
+  if (ctx->D == 2)
+    k_gc<2, T><<<n, 128, 0, ctx->stream>>>(t, list, v, g, corners);
+  else
+    k_gc<3, T><<<n, 256, 0, ctx->stream>>>(t, list, v, g, corners);
+  ctx->launches++;
+  CKL();
+  return AFG_OK;
+}
+
+template <typename T>
+static int launch_gsrb(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, int rb, double lam) {
+  if (n <= 0) return AFG_OK;
+  KTree t = ktree(ctx);
+  const int threads = ctx->D == 2 ? std::min(256, ctx->nc * ctx->nc / 2) : std::min(256, ctx->nc * ctx->nc * ctx->nc / 2);
+  if (ctx->D == 3)
+    k_gsrb<3, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam);
+  else if (ctx->coord == AFG_CYL)
+    k_gsrb<2, true, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam);
+  else
+    k_gsrb<2, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam);
+  ctx->launches++;
+  CKL();
+  return AFG_OK;
+}
+
+template <typename T>
+static int launch_residual(afg_ctx* ctx, const int* list, int n, const T* phi, const T* rhs, T* tmp, double lam,
+                           unsigned long long* maxbits) {
+  if (n <= 0) return AFG_OK;
+  KTree t = ktree(ctx);
+  if (ctx->D == 3)
+    k_residual<3, false, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, ctx->d_is_leaf, maxbits);
+  else if (ctx->coord == AFG_CYL)
+    k_residual<2, true, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, ctx->d_is_leaf, maxbits);
+  else
+    k_residual<2, false, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, ctx->d_is_leaf, maxbits);
+  ctx->launches++;
+  CKL();
+  return AFG_OK;
+}
+
+template <typename T>
+static int launch_rrestrict(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, T* tmp, double lam,
+                            int store_child) {
+  if (n <= 0) return AFG_OK;
+  KTree t = ktree(ctx);
+  const int hnc = ctx->nc / 2;
+  const int threads = std::max(32, std::min(256, ctx->D == 2 ? hnc * hnc : hnc * hnc * hnc));
+  if (ctx->D == 3)
+    k_residual_restrict<3, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child);
+  else if (ctx->coord == AFG_CYL)
+    k_residual_restrict<2, true, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child);
+  else
+    k_residual_restrict<2, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child);
+  ctx->launches++;
+  CKL();
+  return AFG_OK;
+}
+
+template <typename T>
+static int launch_coarse_fas(afg_ctx* ctx, const int* list, int n, const T* phi, T* rhs, T* tmp, double lam,
+                             int copy_tmp) {
+  if (n <= 0) return AFG_OK;
+  KTree t = ktree(ctx);
+  if (ctx->D == 3)
+    k_coarse_fas<3, false, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp);
+  else if (ctx->coord == AFG_CYL)
+    k_coarse_fas<2, true, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp);
+  else
+    k_coarse_fas<2, false, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp);
+  ctx->launches++;
+  CKL();
+  return AFG_OK;
+}
+
+template <typename T>
+static int launch_correct(afg_ctx* ctx, const int* list, int n, T* phi, T* tmp) {
+  if (n <= 0) return AFG_OK;
+  KTree t = ktree(ctx);
+  const size_t sm = sizeof(T) * ctx->S;
+  if (ctx->D == 3)
+    k_correct<3, T><<<n, 256, sm, ctx->stream>>>(t, list, phi, tmp);
+  else
+    k_correct<2, T><<<n, 256, sm, ctx->stream>>>(t, list, phi, tmp);
+  ctx->launches++;
+  CKL();
+  return AFG_OK;
+}
+
+template <typename T>
+static int launch_init_phi_rhs(afg_ctx* ctx, const int* list, int n, T* phi, T* rhs) {
+  if (n <= 0) return AFG_OK;
+  KTree t = ktree(ctx);
+  if (ctx->D == 3)
+    k_init_phi_rhs<3, false, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs);
+  else if (ctx->coord == AFG_CYL)
+    k_init_phi_rhs<2, true, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs);
+  else
+    k_init_phi_rhs<2, false, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs);
+  ctx->launches++;
+  CKL();
+  return AFG_OK;
+}
+
+template <typename T>
+static int launch_copy(afg_ctx* ctx, const int* list, int n, const T* src, T* dst) {
+  if (n <= 0) return AFG_OK;
+  k_copy<T><<<n, 256, 0, ctx->stream>>>(ctx->S, list, src, dst);
+  ctx->launches++;
+  CKL();
+  return AFG_OK;
+}
+
+template <typename T>
+static int launch_maxabs(afg_ctx* ctx, const int* list, int n, const T* v, unsigned long long* out) {
+  if (n <= 0) return AFG_OK;
+  KTree t = ktree(ctx);
+  if (ctx->D == 3)
+    k_maxabs<3, T><<<n, 256, 0, ctx->stream>>>(t, list, v, out);
+  else
+    k_maxabs<2, T><<<n, 256, 0, ctx->stream>>>(t, list, v, out);
+  ctx->launches++;
+  CKL();
+  return AFG_OK;
+}
+
+#define RC(x)                 \
+  do {                        \
+    int rc_ = (x);            \
+    if (rc_ != AFG_OK) return rc_; \
+  } while (0)
+
+/* ------------------------------------------------------------------------- */
+// Multigrid drivers (templated on the working precision T)
+
+struct MgVars {
+  void* phi;
+  void* rhs;
+  void* tmp;
+};
+
+static GcDev mg_gc(const afg_mg_desc& d, bool homogeneous) {
+  GcDev g;
+  for (int n = 0; n < 6; n++) {
+    g.bc_type[n] = d.bc_type[n];
+    g.bc_val[n] = homogeneous ? 0.0 : d.bc_val[n];
+  }
+  g.rb = AFG_RB_MG_SIDES;
+  return g;
+}
+
+template <typename T>
+static int mg_gc_lvl(afg_ctx* ctx, int lvl, T* phi, const GcDev& g, int corners) {
+  return launch_gc<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, g, corners);
+}
+
+// gsrb_boxes, m_af_multigrid.f90:648-687
+template <typename T>
+static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, T* phi, const T* rhs, const GcDev& g) {
+  const int n_cycle = type == AFG_CYCLE_DOWN ? m.d.n_cycle_down : m.d.n_cycle_up;
+  const int* list = lst(ctx, ctx->off_ids[lvl - 1]);
+  const int n = (int)ctx->lvl_ids[lvl - 1].size();
+  for (int it = 1; it <= 2 * n_cycle; it++) {
+    RC(launch_gsrb<T>(ctx, list, n, phi, rhs, it, m.d.helmholtz_lambda));
+    const int corners = (type != AFG_CYCLE_DOWN && it == 2 * n_cycle) ? 1 : 0;
+    RC(launch_gc<T>(ctx, list, n, phi, g, corners));
+  }
+  return AFG_OK;
+}
+
+// update_coarse, m_af_multigrid.f90:691-738
+template <typename T>
+static int mg_update_coarse(afg_ctx* ctx, const MgSlot& m, int lvl, T* phi, T* rhs, T* tmp, const GcDev& g) {
+  RC(launch_rrestrict<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs, tmp,
+                         m.d.helmholtz_lambda, 0));
+  RC(mg_gc_lvl<T>(ctx, lvl - 1, phi, g, 1));
+  RC(launch_coarse_fas<T>(ctx, lst(ctx, ctx->off_parents[lvl - 2]), (int)ctx->lvl_parents[lvl - 2].size(), phi, rhs,
+                          tmp, m.d.helmholtz_lambda, 1));
+  return AFG_OK;
+}
+
+// set_coarse_phi_rhs, m_af_multigrid.f90:742-776
+template <typename T>
+static int mg_set_coarse_phi_rhs(afg_ctx* ctx, const MgSlot& m, int lvl, T* phi, T* rhs, T* tmp, const GcDev& g) {
+  if (lvl == ctx->highest_lvl) RC(mg_gc_lvl<T>(ctx, lvl, phi, g, 1));
+  RC(launch_rrestrict<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs, tmp,
+                         m.d.helmholtz_lambda, 1));
+  RC(mg_gc_lvl<T>(ctx, lvl - 1, phi, g, 1));
+  RC(launch_coarse_fas<T>(ctx, lst(ctx, ctx->off_parents[lvl - 2]), (int)ctx->lvl_parents[lvl - 2].size(), phi, rhs,
+                          tmp, m.d.helmholtz_lambda, 0));
+  return AFG_OK;
+}
+
+// correct_children(parents of lvl-1) + af_gc_lvl(lvl)
+template <typename T>
+static int mg_correct(afg_ctx* ctx, int lvl, T* phi, T* tmp, const GcDev& g) {
+  RC(launch_correct<T>(ctx, lst(ctx, ctx->off_parents[lvl - 2]), (int)ctx->lvl_parents[lvl - 2].size(), phi, tmp));
+  RC(mg_gc_lvl<T>(ctx, lvl, phi, g, 1));
+  return AFG_OK;
+}
+
+// solve_coarse_grid, m_af_multigrid.f90:266-291 (exact FP64 solve)
+template <typename T>
+static int mg_coarse_solve(afg_ctx* ctx, MgSlot& m, T* phi, const T* rhs, const GcDev& g, bool homogeneous) {
+  const int n = m.n_coarse;
+  const double* bcv = m.d_bcval + (homogeneous ? 6 : 0);
+  k_coarse_gather<T><<<(n + 127) / 128, 128, 0, ctx->stream>>>(n, ctx->D, ctx->d_cslot, ctx->d_ccell, m.d_b2r,
+                                                               m.d_bmask, bcv, rhs, ctx->S, m.d_b);
+  ctx->launches++;
+  CKL();
+  k_coarse_matvec<<<(n + 7) / 8, 256, 0, ctx->stream>>>(n, m.d_ainv, m.d_b, m.d_x);
+  ctx->launches++;
+  CKL();
+  k_coarse_scatter<T><<<(n + 127) / 128, 128, 0, ctx->stream>>>(n, ctx->d_cslot, ctx->d_ccell, m.d_x, phi, ctx->S);
+  ctx->launches++;
+  CKL();
+  return mg_gc_lvl<T>(ctx, 1, phi, g, 1);
+}
+
+template <typename T>
+static int mg_residual_lvls(afg_ctx* ctx, const MgSlot& m, int max_lvl, const T* phi, const T* rhs, T* tmp,
+                            unsigned long long* maxbits) {
+  if (max_lvl == ctx->highest_lvl)  // boxes are independent: one launch over all levels
+    return launch_residual<T>(ctx, lst(ctx, ctx->off_all), ctx->n_all, phi, rhs, tmp, m.d.helmholtz_lambda, maxbits);
+  for (int lvl = 1; lvl <= max_lvl; lvl++)
+    RC(launch_residual<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs, tmp,
+                          m.d.helmholtz_lambda, maxbits));
+  return AFG_OK;
+}
+
+// mg_fas_vcycle, m_af_multigrid.f90:185-264
+template <typename T>
+static int mg_vcycle(afg_ctx* ctx, MgSlot& m, int max_lvl, T* phi, T* rhs, T* tmp, bool set_residual,
+                     bool homogeneous, unsigned long long* maxbits) {
+  const GcDev g = mg_gc(m.d, homogeneous);
+  for (int lvl = max_lvl; lvl >= 2; lvl--) {
+    RC(mg_gsrb_boxes<T>(ctx, m, lvl, AFG_CYCLE_DOWN, phi, rhs, g));
+    RC(mg_update_coarse<T>(ctx, m, lvl, phi, rhs, tmp, g));
+  }
+  RC(mg_coarse_solve<T>(ctx, m, phi, rhs, g, homogeneous));
+  for (int lvl = 2; lvl <= max_lvl; lvl++) {
+    RC(mg_correct<T>(ctx, lvl, phi, tmp, g));
+    RC(mg_gsrb_boxes<T>(ctx, m, lvl, AFG_CYCLE_UP, phi, rhs, g));
+  }
+  if (set_residual) RC(mg_residual_lvls<T>(ctx, m, max_lvl, phi, rhs, tmp, maxbits));
+  return AFG_OK;
+}
+
+// mg_fas_fmg, m_af_multigrid.f90:137-180
+template <typename T>
+static int mg_fmg(afg_ctx* ctx, MgSlot& m, T* phi, T* rhs, T* tmp, bool set_residual, bool have_guess,
+                  unsigned long long* maxbits) {
+  const GcDev g = mg_gc(m.d, false);
+  const int H = ctx->highest_lvl;
+  if (have_guess) {
+    for (int lvl = H; lvl >= 2; lvl--) RC(mg_set_coarse_phi_rhs<T>(ctx, m, lvl, phi, rhs, tmp, g));
+  } else {
+    for (int lvl = H; lvl >= 2; lvl--)
+      RC(launch_init_phi_rhs<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs));
+  }
+  RC(launch_copy<T>(ctx, lst(ctx, ctx->off_ids[0]), (int)ctx->lvl_ids[0].size(), phi, tmp));
+  RC(mg_vcycle<T>(ctx, m, 1, phi, rhs, tmp, set_residual && H == 1, false, maxbits));
+  for (int lvl = 2; lvl <= H; lvl++) {
+    RC(launch_copy<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, tmp));
+    RC(mg_correct<T>(ctx, lvl, phi, tmp, g));
+    RC(mg_vcycle<T>(ctx, m, lvl, phi, rhs, tmp, set_residual && lvl == H, false, maxbits));
+  }
+  return AFG_OK;
+}
+
+static int read_max(afg_ctx* ctx, int slot, double* out) {
+  CK(cudaMemcpyAsync(ctx->h_max + slot, ctx->d_max + slot, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  unsigned long long b = ctx->h_max[slot];
+  double v;
+  memcpy(&v, &b, sizeof(double));
+  *out = v;
+  return AFG_OK;
+}
+
+static int reset_max(afg_ctx* ctx, int slot) {
+  CK(cudaMemsetAsync(ctx->d_max + slot, 0, sizeof(unsigned long long), ctx->stream));
+  return AFG_OK;
+}
+
+#include "afg_mixed.cuh"
+
+/* ========================================================================= */
+extern "C" {
+
+int afg_init(int device, afg_ctx** out) {
+  afg_ctx* ctx = nullptr;
+  if (!out) return AFG_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return AFG_ERR_CUDA;
+  if (device < 0 || device >= ndev) return AFG_ERR_ARG;
+  ctx = new afg_ctx();
+  ctx->device = device;
+  CK(cudaSetDevice(device));
+  CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  CK(dalloc(&ctx->d_max, 8));
+  CK(cudaMallocHost((void**)&ctx->h_max, 8 * sizeof(unsigned long long)));
+  *out = ctx;
+  return AFG_OK;
+}
+
+int afg_finalize(afg_ctx* ctx) {
+  if (!ctx) return AFG_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  free_tree(ctx);
+  dfree(ctx->d_max);
+  if (ctx->h_max) cudaFreeHost(ctx->h_max);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return AFG_OK;
+}
+
+const char* afg_last_error(const afg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+long long afg_launch_count(const afg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int afg_sync(afg_ctx* ctx) {
+  if (!ctx) return AFG_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return AFG_OK;
+}
+
+int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_var_face) {
+  if (!ctx || !t) return AFG_ERR_ARG;
+  if (t->ndim != 2 && t->ndim != 3) return fail(ctx, AFG_ERR_ARG, "ndim must be 2 or 3");
+  if (t->n_cell < 2 || (t->n_cell & 1) || t->n_cell > 64) return fail(ctx, AFG_ERR_ARG, "bad n_cell %d", t->n_cell);
+  if (t->coord == AFG_CYL && t->ndim != 2) return fail(ctx, AFG_ERR_ARG, "cylindrical needs ndim=2");
+  if (t->n_boxes <= 0 || t->highest_lvl <= 0 || n_var_cell <= 0) return fail(ctx, AFG_ERR_ARG, "empty tree");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  free_tree(ctx);
+  const int D = t->ndim, nc = t->n_cell, n = t->n_boxes;
+  ctx->D = D;
+  ctx->nc = nc;
+  ctx->n2 = nc + 2;
+  ctx->S = D == 2 ? (nc + 2) * (nc + 2) : (nc + 2) * (nc + 2) * (nc + 2);
+  ctx->NF = D == 2 ? (nc + 1) * (nc + 1) : (nc + 1) * (nc + 1) * (nc + 1);
+  ctx->coord = t->coord;
+  ctx->n_boxes = n;
+  ctx->highest_lvl = t->highest_lvl;
+  for (int d = 0; d < 3; d++) ctx->cgs[d] = d < D ? t->coarse_grid_size[d] : 1;
+  const int nch = 1 << D, nnb = 2 * D, nm = D == 2 ? 9 : 27;
+  // host tables converted to slots
+  std::vector<int> parent(n), children((size_t)n * nch), nbr((size_t)n * nnb), pnb((size_t)n * nnb, -1),
+      nbmat((size_t)n * nm);
+  for (int b = 0; b < n; b++) {
+    const int p = t->parent[b];
+    if (p < 0 || p > n) return fail(ctx, AFG_ERR_ARG, "bad parent of box %d", b + 1);
+    parent[b] = p - 1;
+    for (int c = 0; c < nch; c++) {
+      const int v = t->children[(size_t)b * nch + c];
+      if (v < 0 || v > n) return fail(ctx, AFG_ERR_ARG, "bad child of box %d", b + 1);
+      children[(size_t)b * nch + c] = v - 1;
+    }
+    for (int k = 0; k < nm; k++) {
+      const int v = t->neighbor_mat[(size_t)b * nm + k];
+      if (v > n) return fail(ctx, AFG_ERR_ARG, "bad neighbor_mat of box %d", b + 1);
+      nbmat[(size_t)b * nm + k] = v > 0 ? v - 1 : -1;
+    }
+  }
+  for (int b = 0; b < n; b++)
+    for (int nb = 0; nb < nnb; nb++) {
+      const int v = t->neighbors[(size_t)b * nnb + nb];
+      if (v > n || v < -1) return fail(ctx, AFG_ERR_ARG, "bad neighbor of box %d", b + 1);
+      if (v > 0) {
+        nbr[(size_t)b * nnb + nb] = v - 1;
+      } else if (v == 0) {
+        nbr[(size_t)b * nnb + nb] = kNbRefine;
+        const int p = parent[b];
+        if (p < 0) return fail(ctx, AFG_ERR_ARG, "level-1 box %d has a refinement boundary", b + 1);
+        const int pn = t->neighbors[(size_t)p * nnb + nb];
+        if (pn <= 0) return fail(ctx, AFG_ERR_ARG, "parent of box %d lacks neighbour %d (2:1 balance)", b + 1, nb + 1);
+        pnb[(size_t)b * nnb + nb] = pn - 1;
+      } else {
+        nbr[(size_t)b * nnb + nb] = kNbPhys;
+      }
+    }
+  ctx->h_ix.assign(t->ix, t->ix + (size_t)n * D);
+  ctx->h_nbr.assign(t->neighbors, t->neighbors + (size_t)n * nnb);
+  // level lists
+  ctx->lvl_ids.assign(t->highest_lvl, {});
+  ctx->lvl_leaves.assign(t->highest_lvl, {});
+  ctx->lvl_parents.assign(t->highest_lvl, {});
+  std::vector<int> all;
+  std::vector<unsigned char> is_leaf(n, 0);
+  for (int l = 0; l < t->highest_lvl; l++) {
+    for (int k = t->ids_off[l]; k < t->ids_off[l + 1]; k++) {
+      const int id = t->ids[k];
+      if (id < 1 || id > n) return fail(ctx, AFG_ERR_ARG, "bad id in level list %d", l + 1);
+      ctx->lvl_ids[l].push_back(id - 1);
+    }
+    for (int k = t->leaves_off[l]; k < t->leaves_off[l + 1]; k++) {
+      const int id = t->leaves[k];
+      if (id < 1 || id > n) return fail(ctx, AFG_ERR_ARG, "bad id in leaf list %d", l + 1);
+      ctx->lvl_leaves[l].push_back(id - 1);
+      is_leaf[id - 1] = 1;
+    }
+    for (int k = t->parents_off[l]; k < t->parents_off[l + 1]; k++) {
+      const int id = t->parents[k];
+      if (id < 1 || id > n) return fail(ctx, AFG_ERR_ARG, "bad id in parent list %d", l + 1);
+      ctx->lvl_parents[l].push_back(id - 1);
+    }
+  }
+  std::vector<int> lists;
+  ctx->off_ids.assign(t->highest_lvl, 0);
+  ctx->off_leaves.assign(t->highest_lvl, 0);
+  ctx->off_parents.assign(t->highest_lvl, 0);
+  for (int l = 0; l < t->highest_lvl; l++) {
+    ctx->off_ids[l] = lists.size();
+    lists.insert(lists.end(), ctx->lvl_ids[l].begin(), ctx->lvl_ids[l].end());
+    ctx->off_leaves[l] = lists.size();
+    lists.insert(lists.end(), ctx->lvl_leaves[l].begin(), ctx->lvl_leaves[l].end());
+    ctx->off_parents[l] = lists.size();
+    lists.insert(lists.end(), ctx->lvl_parents[l].begin(), ctx->lvl_parents[l].end());
+  }
+  ctx->off_all = lists.size();
+  ctx->n_all = 0;
+  for (int l = 0; l < t->highest_lvl; l++) {
+    lists.insert(lists.end(), ctx->lvl_ids[l].begin(), ctx->lvl_ids[l].end());
+    ctx->n_all += (int)ctx->lvl_ids[l].size();
+  }
+  ctx->off_all_leaves = lists.size();
+  ctx->n_all_leaves = 0;
+  for (int l = 0; l < t->highest_lvl; l++) {
+    lists.insert(lists.end(), ctx->lvl_leaves[l].begin(), ctx->lvl_leaves[l].end());
+    ctx->n_all_leaves += (int)ctx->lvl_leaves[l].size();
+  }
+  // coarse grid map (level 1)
+  const long ncoarse = (long)ctx->cgs[0] * ctx->cgs[1] * ctx->cgs[2];
+  std::vector<int> cslot(ncoarse, -1), ccell(ncoarse, 0);
+  if (ncoarse <= kMaxCoarse) {
+    for (int s : ctx->lvl_ids[0]) {
+      const int kn = D == 3 ? nc : 1;
+      for (int k = 1; k <= kn; k++)
+        for (int j = 1; j <= nc; j++)
+          for (int i = 1; i <= nc; i++) {
+            long I = (long)(t->ix[(size_t)s * D + 0] - 1) * nc + (i - 1);
+            long J = (long)(t->ix[(size_t)s * D + 1] - 1) * nc + (j - 1);
+            long K = D == 3 ? (long)(t->ix[(size_t)s * D + 2] - 1) * nc + (k - 1) : 0;
+            if (I >= ctx->cgs[0] || J >= ctx->cgs[1] || K >= ctx->cgs[2])
+              return fail(ctx, AFG_ERR_ARG, "level-1 box outside coarse_grid_size");
+            long g = I + ctx->cgs[0] * (J + (long)ctx->cgs[1] * K);
+            cslot[g] = s;
+            ccell[g] = i + ctx->n2 * (j + ctx->n2 * (D == 3 ? k : 0));
+          }
+    }
+    for (long g = 0; g < ncoarse; g++)
+      if (cslot[g] < 0) return fail(ctx, AFG_ERR_ARG, "coarse grid not covered by level-1 boxes");
+  }
+  // upload tables
+  CK(dalloc(&ctx->d_parent, n));
+  CK(dalloc(&ctx->d_children, (size_t)n * nch));
+  CK(dalloc(&ctx->d_nbr, (size_t)n * nnb));
+  CK(dalloc(&ctx->d_pnb, (size_t)n * nnb));
+  CK(dalloc(&ctx->d_nbmat, (size_t)n * nm));
+  CK(dalloc(&ctx->d_ix, (size_t)n * D));
+  CK(dalloc(&ctx->d_rmin, (size_t)n * D));
+  CK(dalloc(&ctx->d_dr, (size_t)n * D));
+  CK(dalloc(&ctx->d_lists, lists.size()));
+  CK(dalloc(&ctx->d_is_leaf, n));
+  CK(dalloc(&ctx->d_cslot, ncoarse));
+  CK(dalloc(&ctx->d_ccell, ncoarse));
+  CK(cudaMemcpy(ctx->d_parent, parent.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_children, children.data(), sizeof(int) * children.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_nbr, nbr.data(), sizeof(int) * nbr.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_pnb, pnb.data(), sizeof(int) * pnb.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_nbmat, nbmat.data(), sizeof(int) * nbmat.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_ix, t->ix, sizeof(int) * (size_t)n * D, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_rmin, t->r_min, sizeof(double) * (size_t)n * D, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_dr, t->dr, sizeof(double) * (size_t)n * D, cudaMemcpyHostToDevice));
+  if (!lists.empty()) CK(cudaMemcpy(ctx->d_lists, lists.data(), sizeof(int) * lists.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_is_leaf, is_leaf.data(), n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_cslot, cslot.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_ccell, ccell.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
+  // pools
+  ctx->n_var = n_var_cell;
+  ctx->n_var_face = n_var_face;
+  ctx->cc.assign(n_var_cell, nullptr);
+  ctx->fc.assign(std::max(0, n_var_face), nullptr);
+  for (int v = 0; v < n_var_cell; v++) {
+    if (dalloc(&ctx->cc[v], (size_t)n * ctx->S) != cudaSuccess)
+      return fail(ctx, AFG_ERR_NOMEM, "cannot allocate cell pool %d", v + 1);
+    CK(cudaMemsetAsync(ctx->cc[v], 0, sizeof(double) * (size_t)n * ctx->S, ctx->stream));
+  }
+  for (int v = 0; v < n_var_face; v++) {
+    if (dalloc(&ctx->fc[v], (size_t)n * D * ctx->NF) != cudaSuccess)
+      return fail(ctx, AFG_ERR_NOMEM, "cannot allocate face pool %d", v + 1);
+    CK(cudaMemsetAsync(ctx->fc[v], 0, sizeof(double) * (size_t)n * D * ctx->NF, ctx->stream));
+  }
+  ctx->methods.assign(n_var_cell, GcDev{});
+  ctx->has_method.assign(n_var_cell, false);
+  ctx->stage_elems = (size_t)n * std::max(ctx->S, D * ctx->NF);
+  CK(cudaMallocHost((void**)&ctx->h_stage, sizeof(double) * ctx->stage_elems));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_tree = true;
+  return AFG_OK;
+}
+
+static int check_var(afg_ctx* ctx, int iv) {
+  if (!ctx) return AFG_ERR_ARG;
+  if (!ctx->have_tree) return fail(ctx, AFG_ERR_STATE, "no tree: call afg_tree_sync first");
+  if (iv < 1 || iv > ctx->n_var) return fail(ctx, AFG_ERR_ARG, "bad cc variable %d", iv);
+  return AFG_OK;
+}
+
+int afg_cc_upload(afg_ctx* ctx, int iv, const double* const* box_cc, long long off) {
+  RC(check_var(ctx, iv));
+  if (!box_cc) return fail(ctx, AFG_ERR_ARG, "null box_cc");
+  const size_t S = ctx->S;
+  CK(cudaStreamSynchronize(ctx->stream));
+  double* dst = ctx->cc[iv - 1];
+  // runs of consecutive non-null boxes are staged and copied in one call
+  int b = 0;
+  while (b < ctx->n_boxes) {
+    if (!box_cc[b]) { b++; continue; }
+    int e = b;
+    while (e < ctx->n_boxes && box_cc[e]) {
+      memcpy(ctx->h_stage + (size_t)(e - b) * S, box_cc[e] + off, sizeof(double) * S);
+      e++;
+    }
+    CK(cudaMemcpyAsync(dst + (size_t)b * S, ctx->h_stage, sizeof(double) * S * (e - b), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    b = e;
+  }
+  return AFG_OK;
+}
+
+int afg_cc_download(afg_ctx* ctx, int iv, double* const* box_cc, long long off) {
+  RC(check_var(ctx, iv));
+  if (!box_cc) return fail(ctx, AFG_ERR_ARG, "null box_cc");
+  const size_t S = ctx->S;
+  CK(cudaMemcpyAsync(ctx->h_stage, ctx->cc[iv - 1], sizeof(double) * S * ctx->n_boxes, cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int b = 0; b < ctx->n_boxes; b++)
+    if (box_cc[b]) memcpy(box_cc[b] + off, ctx->h_stage + (size_t)b * S, sizeof(double) * S);
+  return AFG_OK;
+}
+
+int afg_fc_upload(afg_ctx* ctx, int ivf, const double* const* box_fc, long long off) {
+  if (!ctx || !ctx->have_tree) return AFG_ERR_STATE;
+  if (ivf < 1 || ivf > ctx->n_var_face || !box_fc) return fail(ctx, AFG_ERR_ARG, "bad fc variable %d", ivf);
+  const size_t F = (size_t)ctx->D * ctx->NF;
+  for (int b = 0; b < ctx->n_boxes; b++)
+    if (box_fc[b]) memcpy(ctx->h_stage + (size_t)b * F, box_fc[b] + off, sizeof(double) * F);
+  CK(cudaMemcpyAsync(ctx->fc[ivf - 1], ctx->h_stage, sizeof(double) * F * ctx->n_boxes, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return AFG_OK;
+}
+
+int afg_fc_download(afg_ctx* ctx, int ivf, double* const* box_fc, long long off) {
+  if (!ctx || !ctx->have_tree) return AFG_ERR_STATE;
+  if (ivf < 1 || ivf > ctx->n_var_face || !box_fc) return fail(ctx, AFG_ERR_ARG, "bad fc variable %d", ivf);
+  const size_t F = (size_t)ctx->D * ctx->NF;
+  CK(cudaMemcpyAsync(ctx->h_stage, ctx->fc[ivf - 1], sizeof(double) * F * ctx->n_boxes, cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int b = 0; b < ctx->n_boxes; b++)
+    if (box_fc[b]) memcpy(box_fc[b] + off, ctx->h_stage + (size_t)b * F, sizeof(double) * F);
+  return AFG_OK;
+}
+
+int afg_set_cc_methods(afg_ctx* ctx, int iv, const afg_gc_desc* gc) {
+  RC(check_var(ctx, iv));
+  if (!gc || gc->rb < 0 || gc->rb > 2) return fail(ctx, AFG_ERR_ARG, "bad ghost-cell method");
+  GcDev g;
+  for (int n = 0; n < 6; n++) {
+    g.bc_type[n] = gc->bc_type[n];
+    g.bc_val[n] = gc->bc_val[n];
+    if (n < 2 * ctx->D && (g.bc_type[n] > -10 || g.bc_type[n] < -13))
+      return fail(ctx, AFG_ERR_ARG, "bad bc type %d on face %d", g.bc_type[n], n + 1);
+  }
+  g.rb = gc->rb;
+  ctx->methods[iv - 1] = g;
+  ctx->has_method[iv - 1] = true;
+  return AFG_OK;
+}
+
+int afg_gc(afg_ctx* ctx, int iv, int lvl, int corners) {
+  RC(check_var(ctx, iv));
+  if (!ctx->has_method[iv - 1]) return fail(ctx, AFG_ERR_STATE, "no ghost-cell methods for variable %d", iv);
+  if (lvl > ctx->highest_lvl) return fail(ctx, AFG_ERR_ARG, "bad level %d", lvl);
+  const GcDev& g = ctx->methods[iv - 1];
+  const int l0 = lvl <= 0 ? 1 : lvl, l1 = lvl <= 0 ? ctx->highest_lvl : lvl;
+  for (int l = l0; l <= l1; l++)
+    RC(launch_gc<double>(ctx, lst(ctx, ctx->off_ids[l - 1]), (int)ctx->lvl_ids[l - 1].size(), ctx->cc[iv - 1], g,
+                         corners));
+  return AFG_OK;
+}
+
+int afg_maxabs(afg_ctx* ctx, int iv, int leaves_only, double* result) {
+  RC(check_var(ctx, iv));
+  if (!result) return AFG_ERR_ARG;
+  RC(reset_max(ctx, 0));
+  if (leaves_only)
+    RC(launch_maxabs<double>(ctx, lst(ctx, ctx->off_all_leaves), ctx->n_all_leaves, ctx->cc[iv - 1], ctx->d_max));
+  else
+    RC(launch_maxabs<double>(ctx, lst(ctx, ctx->off_all), ctx->n_all, ctx->cc[iv - 1], ctx->d_max));
+  return read_max(ctx, 0, result);
+}
+
+/* ---- multigrid ---------------------------------------------------------- */
+
+// Dense coarse matrix with boundary conditions folded in and its inverse
+// (hypre_set_matrix + stencil_handle_boundaries, m_coarse_solver.f90:104-194,
+// 442-491); the inverse replaces hypre's PFMG solve.
+static int build_coarse(afg_ctx* ctx, MgSlot& m) {
+  const int D = ctx->D, nc = ctx->nc;
+  const long n = (long)ctx->cgs[0] * ctx->cgs[1] * ctx->cgs[2];
+  if (n > kMaxCoarse)
+    return fail(ctx, AFG_ERR_UNSUPPORTED, "coarse grid of %ld unknowns exceeds the direct solver limit %d", n,
+                kMaxCoarse);
+  std::vector<double> A((size_t)n * n, 0.0), b2r((size_t)n * 2 * D, 0.0);
+  std::vector<unsigned char> mask(n, 0);
+  std::vector<double> dr(D), rmin(D);
+  for (int s : ctx->lvl_ids[0]) {
+    // per-box coefficients, mg_box_lpl_stencil
+    double h[3], c[7];
+    std::vector<double> hdr((size_t)D), hrm((size_t)D);
+    CK(cudaMemcpy(hdr.data(), ctx->d_dr + (size_t)s * D, sizeof(double) * D, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hrm.data(), ctx->d_rmin + (size_t)s * D, sizeof(double) * D, cudaMemcpyDeviceToHost));
+    for (int d = 0; d < D; d++) h[d] = hdr[d];
+    double inv[3];
+    for (int d = 0; d < D; d++) inv[d] = 1 / (h[d] * h[d]);
+    for (int d = 0; d < D; d++) c[1 + 2 * d] = c[2 + 2 * d] = inv[d];
+    double sum = 0;
+    for (int k = 1; k <= 2 * D; k++) sum += c[k];
+    c[0] = -sum - m.d.helmholtz_lambda;
+    const bool cyl = ctx->coord == AFG_CYL;
+    const int kn = D == 3 ? nc : 1;
+    for (int k = 1; k <= kn; k++)
+      for (int j = 1; j <= nc; j++)
+        for (int i = 1; i <= nc; i++) {
+          double st[7];
+          for (int q = 0; q < 7; q++) st[q] = c[q];
+          if (cyl) {
+            const double r = hrm[0] + (i - 0.5) * h[0];
+            const double inv_r = 1 / r;
+            const double f1 = (r - 0.5 * h[0]) * inv_r, f2 = (r + 0.5 * h[0]) * inv_r;
+            st[1] = f1 * c[1];
+            st[2] = f2 * c[2];
+            st[0] = c[0] - (st[1] - c[1]) - (st[2] - c[2]);
+          }
+          const long I = (long)(ctx->h_ix[(size_t)s * D] - 1) * nc + (i - 1);
+          const long J = (long)(ctx->h_ix[(size_t)s * D + 1] - 1) * nc + (j - 1);
+          const long K = D == 3 ? (long)(ctx->h_ix[(size_t)s * D + 2] - 1) * nc + (k - 1) : 0;
+          const long g = I + ctx->cgs[0] * (J + (long)ctx->cgs[1] * K);
+          const int cidx[3] = {i, j, k};
+          for (int nb = 0; nb < 2 * D; nb++) {
+            if (ctx->h_nbr[(size_t)s * 2 * D + nb] >= 0) continue;
+            const int d = nb / 2;
+            const bool low = (nb % 2) == 0;
+            if (cidx[d] != (low ? 1 : nc)) continue;
+            if (m.d.bc_type[nb] == AFG_BC_DIRICHLET) {
+              st[0] = st[0] - st[nb + 1];
+              b2r[(size_t)g * 2 * D + nb] = -2 * st[nb + 1];
+              st[nb + 1] = 0.0;
+            } else if (m.d.bc_type[nb] == AFG_BC_NEUMANN) {
+              st[0] = st[0] + st[nb + 1];
+              b2r[(size_t)g * 2 * D + nb] = -(st[nb + 1] * h[d]) * (low ? -1 : 1);
+              st[nb + 1] = 0.0;
+            } else {
+              return fail(ctx, AFG_ERR_UNSUPPORTED, "coarse solver supports Dirichlet/Neumann only");
+            }
+            mask[g] |= (unsigned char)(1u << nb);
+          }
+          A[(size_t)g * n + g] += st[0];
+          const long G[3] = {I, J, K};
+          for (int nb = 0; nb < 2 * D; nb++) {
+            if (st[nb + 1] == 0.0) continue;
+            long H[3] = {G[0], G[1], G[2]};
+            H[nb / 2] += (nb % 2) ? 1 : -1;
+            if (H[nb / 2] < 0 || H[nb / 2] >= ctx->cgs[nb / 2])
+              return fail(ctx, AFG_ERR_UNSUPPORTED, "periodic coarse grids are not supported");
+            const long hh = H[0] + ctx->cgs[0] * (H[1] + (long)ctx->cgs[1] * H[2]);
+            A[(size_t)g * n + hh] += st[nb + 1];
+          }
+        }
+  }
+  // Gauss-Jordan with partial pivoting (same steps as the CPU oracle)
+  std::vector<double> Inv((size_t)n * n, 0.0);
+  for (long r = 0; r < n; r++) Inv[(size_t)r * n + r] = 1.0;
+  for (long col = 0; col < n; col++) {
+    long piv = col;
+    double best = std::fabs(A[(size_t)col * n + col]);
+    for (long r = col + 1; r < n; r++) {
+      const double v = std::fabs(A[(size_t)r * n + col]);
+      if (v > best) { best = v; piv = r; }
+    }
+    if (best == 0.0) return fail(ctx, AFG_ERR_ARG, "singular coarse-grid operator (all-Neumann Poisson?)");
+    if (piv != col)
+      for (long q = 0; q < n; q++) {
+        std::swap(A[(size_t)col * n + q], A[(size_t)piv * n + q]);
+        std::swap(Inv[(size_t)col * n + q], Inv[(size_t)piv * n + q]);
+      }
+    const double iv = 1.0 / A[(size_t)col * n + col];
+    for (long q = 0; q < n; q++) {
+      A[(size_t)col * n + q] *= iv;
+      Inv[(size_t)col * n + q] *= iv;
+    }
+    for (long r = 0; r < n; r++) {
+      if (r == col) continue;
+      const double f = A[(size_t)r * n + col];
+      if (f == 0.0) continue;
+      for (long q = 0; q < n; q++) {
+        A[(size_t)r * n + q] -= f * A[(size_t)col * n + q];
+        Inv[(size_t)r * n + q] -= f * Inv[(size_t)col * n + q];
+      }
+    }
+  }
+  m.n_coarse = (int)n;
+  CK(dalloc(&m.d_ainv, (size_t)n * n));
+  CK(dalloc(&m.d_b, n));
+  CK(dalloc(&m.d_x, n));
+  CK(dalloc(&m.d_b2r, (size_t)n * 2 * D));
+  CK(dalloc(&m.d_bmask, n));
+  CK(dalloc(&m.d_bcval, 12));
+  CK(cudaMemcpy(m.d_ainv, Inv.data(), sizeof(double) * n * n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(m.d_b2r, b2r.data(), sizeof(double) * b2r.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(m.d_bmask, mask.data(), n, cudaMemcpyHostToDevice));
+  double bcv[12];
+  for (int q = 0; q < 6; q++) {
+    bcv[q] = m.d.bc_val[q];
+    bcv[6 + q] = 0.0;
+  }
+  CK(cudaMemcpy(m.d_bcval, bcv, sizeof(bcv), cudaMemcpyHostToDevice));
+  return AFG_OK;
+}
+
+static int get_mg(afg_ctx* ctx, int mg_id, MgSlot** out) {
+  if (!ctx) return AFG_ERR_ARG;
+  if (!ctx->have_tree) return fail(ctx, AFG_ERR_STATE, "no tree");
+  if (mg_id < 0 || mg_id >= kMaxMg || !ctx->mg[mg_id].used) return fail(ctx, AFG_ERR_STATE, "mg slot %d not set up", mg_id);
+  *out = &ctx->mg[mg_id];
+  return AFG_OK;
+}
+
+int afg_mg_setup(afg_ctx* ctx, int mg_id, const afg_mg_desc* d) {
+  if (!ctx || !d) return AFG_ERR_ARG;
+  if (!ctx->have_tree) return fail(ctx, AFG_ERR_STATE, "no tree");
+  if (mg_id < 0 || mg_id >= kMaxMg) return fail(ctx, AFG_ERR_ARG, "mg_id out of range");
+  for (int v : {d->i_phi, d->i_rhs, d->i_tmp})
+    if (v < 1 || v > ctx->n_var) return fail(ctx, AFG_ERR_ARG, "bad mg variable %d", v);
+  if (d->i_phi == d->i_rhs || d->i_phi == d->i_tmp || d->i_rhs == d->i_tmp)
+    return fail(ctx, AFG_ERR_ARG, "i_phi, i_rhs and i_tmp must differ");
+  if (d->n_cycle_down < 1 || d->n_cycle_up < 1) return fail(ctx, AFG_ERR_ARG, "n_cycle must be >= 1");
+  if (d->precision != AFG_FP64 && d->precision != AFG_MIXED) return fail(ctx, AFG_ERR_ARG, "bad precision");
+  for (int n = 0; n < 2 * ctx->D; n++)
+    if (d->bc_type[n] != AFG_BC_DIRICHLET && d->bc_type[n] != AFG_BC_NEUMANN)
+      return fail(ctx, AFG_ERR_UNSUPPORTED, "multigrid needs Dirichlet or Neumann sides");
+  MgSlot& m = ctx->mg[mg_id];
+  dfree(m.d_ainv); dfree(m.d_b); dfree(m.d_x); dfree(m.d_b2r); dfree(m.d_bmask); dfree(m.d_bcval);
+  dfree(m.e32); dfree(m.r32); dfree(m.t32);
+  m.used = false;
+  m.d = *d;
+  RC(build_coarse(ctx, m));
+  if (d->precision == AFG_MIXED) {
+    const size_t N = (size_t)ctx->n_boxes * ctx->S;
+    if (dalloc(&m.e32, N) != cudaSuccess || dalloc(&m.r32, N) != cudaSuccess || dalloc(&m.t32, N) != cudaSuccess)
+      return fail(ctx, AFG_ERR_NOMEM, "cannot allocate FP32 pools");
+    CK(cudaMemset(m.e32, 0, N * sizeof(float)));
+    CK(cudaMemset(m.r32, 0, N * sizeof(float)));
+    CK(cudaMemset(m.t32, 0, N * sizeof(float)));
+  }
+  m.used = true;
+  // mg_init: phi gets the multigrid ghost-cell methods
+  GcDev g = mg_gc(m.d, false);
+  ctx->methods[d->i_phi - 1] = g;
+  ctx->has_method[d->i_phi - 1] = true;
+  return AFG_OK;
+}
+
+int afg_mg_set_bc_values(afg_ctx* ctx, int mg_id, const double* v) {
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  if (!v) return AFG_ERR_ARG;
+  for (int q = 0; q < 6; q++) m->d.bc_val[q] = v[q];
+  double bcv[12];
+  for (int q = 0; q < 6; q++) {
+    bcv[q] = v[q];
+    bcv[6 + q] = 0.0;
+  }
+  CK(cudaMemcpyAsync(m->d_bcval, bcv, sizeof(bcv), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->methods[m->d.i_phi - 1] = mg_gc(m->d, false);
+  return AFG_OK;
+}
+
+#define MG_VARS(m)                                 \
+  double* phi = ctx->cc[(m)->d.i_phi - 1];         \
+  double* rhs = ctx->cc[(m)->d.i_rhs - 1];         \
+  double* tmp = ctx->cc[(m)->d.i_tmp - 1];
+
+int afg_mg_gsrb_lvl(afg_ctx* ctx, int mg_id, int lvl, int type) {
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  if (lvl < 1 || lvl > ctx->highest_lvl) return fail(ctx, AFG_ERR_ARG, "bad level");
+  MG_VARS(m);
+  (void)tmp;
+  return mg_gsrb_boxes<double>(ctx, *m, lvl, type, phi, rhs, mg_gc(m->d, false));
+}
+
+int afg_mg_update_coarse(afg_ctx* ctx, int mg_id, int lvl) {
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  if (lvl < 2 || lvl > ctx->highest_lvl) return fail(ctx, AFG_ERR_ARG, "bad level");
+  MG_VARS(m);
+  return mg_update_coarse<double>(ctx, *m, lvl, phi, rhs, tmp, mg_gc(m->d, false));
+}
+
+int afg_mg_correct_lvl(afg_ctx* ctx, int mg_id, int lvl) {
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  if (lvl < 2 || lvl > ctx->highest_lvl) return fail(ctx, AFG_ERR_ARG, "bad level");
+  MG_VARS(m);
+  (void)rhs;
+  return mg_correct<double>(ctx, lvl, phi, tmp, mg_gc(m->d, false));
+}
+
+int afg_mg_coarse_solve(afg_ctx* ctx, int mg_id) {
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  MG_VARS(m);
+  (void)tmp;
+  return mg_coarse_solve<double>(ctx, *m, phi, rhs, mg_gc(m->d, false), false);
+}
+
+int afg_mg_residual(afg_ctx* ctx, int mg_id, int max_lvl) {
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  MG_VARS(m);
+  return mg_residual_lvls<double>(ctx, *m, max_lvl <= 0 ? ctx->highest_lvl : std::min(max_lvl, ctx->highest_lvl),
+                                  phi, rhs, tmp, nullptr);
+}
+
+int afg_mg_vcycle(afg_ctx* ctx, int mg_id, int set_residual, int max_lvl, double* max_res) {
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  MG_VARS(m);
+  const int ml = max_lvl <= 0 ? ctx->highest_lvl : std::min(max_lvl, ctx->highest_lvl);
+  RC(reset_max(ctx, 1));
+  RC(mg_vcycle<double>(ctx, *m, ml, phi, rhs, tmp, set_residual != 0, false, ctx->d_max + 1));
+  if (set_residual && max_res) return read_max(ctx, 1, max_res);
+  return AFG_OK;
+}
+
+int afg_mg_fmg(afg_ctx* ctx, int mg_id, int set_residual, int have_guess, double* max_res) {
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  MG_VARS(m);
+  RC(reset_max(ctx, 1));
+  RC(mg_fmg<double>(ctx, *m, phi, rhs, tmp, set_residual != 0, have_guess != 0, ctx->d_max + 1));
+  if (set_residual && max_res) return read_max(ctx, 1, max_res);
+  return AFG_OK;
+}
+
+int afg_mg_solve(afg_ctx* ctx, int mg_id, double threshold, int max_cycles, int* n_done, double* residuals) {
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  if (max_cycles < 1) return fail(ctx, AFG_ERR_ARG, "max_cycles < 1");
+  if (m->d.precision == AFG_MIXED) return mixed_solve(ctx, *m, threshold, max_cycles, n_done, residuals);
+  MG_VARS(m);
+  int n = 0;
+  double r = 0;
+  for (n = 0; n < max_cycles;) {
+    RC(reset_max(ctx, 1));
+    RC(mg_vcycle<double>(ctx, *m, ctx->highest_lvl, phi, rhs, tmp, true, false, ctx->d_max + 1));
+    RC(read_max(ctx, 1, &r));
+    if (residuals) residuals[n] = r;
+    n++;
+    if (r < threshold) break;
+  }
+  if (n_done) *n_done = n;
+  return r < threshold ? AFG_OK : AFG_ERR_NOCONV;
+}
+
+}  // extern "C"

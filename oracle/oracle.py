@@ -1,0 +1,139 @@
+"""ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+The oracle restates the reference's Fortran algorithms in C++ FP64 with the
+reference's operation order (see oracle_common.h).  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg use it, as the
+checker; the GPU product never calls it.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "afivo-streamer_gb300"))
+import afivo_gpu as ag  # noqa: E402  (only for the shared C struct layouts)
+from build_oracle import build  # noqa: E402
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(build())
+        P = C.c_void_p
+        DP = C.POINTER(C.c_double)
+        IP = C.POINTER(C.c_int)
+        sig = {
+            "orc_create": (P, [C.POINTER(ag.TreeDesc), C.c_int, C.c_int]),
+            "orc_destroy": (None, [P]),
+            "orc_set_num_threads": (C.c_int, [C.c_int]),
+            "orc_set_cc_methods": (C.c_int, [P, C.c_int, C.POINTER(ag.GcDesc)]),
+            "orc_gc": (C.c_int, [P, DP, C.c_int, C.c_int, C.c_int]),
+            "orc_mg_setup": (C.c_int, [P, C.c_int, C.POINTER(ag.MgDesc)]),
+            "orc_mg_set_bc_values": (C.c_int, [P, C.c_int, DP]),
+            "orc_mg_coarse_inverse": (C.c_int, [P, C.c_int, DP, C.c_int]),
+            "orc_mg_gsrb_lvl": (C.c_int, [P, DP, C.c_int, C.c_int, C.c_int]),
+            "orc_mg_update_coarse": (C.c_int, [P, DP, C.c_int, C.c_int]),
+            "orc_mg_correct_lvl": (C.c_int, [P, DP, C.c_int, C.c_int]),
+            "orc_mg_coarse_solve": (C.c_int, [P, DP, C.c_int]),
+            "orc_mg_residual": (C.c_int, [P, DP, C.c_int, C.c_int]),
+            "orc_mg_vcycle": (C.c_int, [P, DP, C.c_int, C.c_int, C.c_int, DP]),
+            "orc_mg_fmg": (C.c_int, [P, DP, C.c_int, C.c_int, C.c_int, DP]),
+            "orc_mg_solve": (C.c_int, [P, DP, C.c_int, C.c_double, C.c_int, IP, DP]),
+            "orc_maxabs": (C.c_double, [P, DP, C.c_int, C.c_int]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def set_num_threads(n: int) -> int:
+    return lib().orc_set_num_threads(n)
+
+
+def _dp(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Oracle:
+    """CPU restatement operating on host boxes cc[n_boxes, n_var, ...]."""
+
+    def __init__(self, tree, n_var, n_var_face=0):
+        self.L = lib()
+        self.holder = ag.TreeDescHolder(tree)
+        self.p = self.L.orc_create(C.byref(self.holder.desc), n_var, n_var_face)
+        self.tree = tree
+        self.n_var = n_var
+
+    def __del__(self):
+        try:
+            self.L.orc_destroy(self.p)
+        except Exception:
+            pass
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            raise RuntimeError(f"oracle {what} failed: {rc}")
+
+    def set_cc_methods(self, iv, bc_type, bc_val=None, rb=ag.RB_MG_SIDES):
+        g = ag.gc_desc(bc_type, bc_val, rb)
+        self._ck(self.L.orc_set_cc_methods(self.p, iv, C.byref(g)), "set_cc_methods")
+
+    def gc(self, cc, iv, lvl=0, corners=True):
+        self._ck(self.L.orc_gc(self.p, _dp(cc), iv, lvl, int(corners)), "gc")
+
+    def mg_setup(self, mg_id, desc):
+        self._ck(self.L.orc_mg_setup(self.p, mg_id, C.byref(desc)), "mg_setup")
+
+    def mg_set_bc_values(self, mg_id, vals):
+        a = np.zeros(6)
+        a[:len(vals)] = vals
+        self._ck(self.L.orc_mg_set_bc_values(self.p, mg_id, _dp(a)), "mg_set_bc_values")
+
+    def coarse_inverse(self, mg_id):
+        n = self.L.orc_mg_coarse_inverse(self.p, mg_id, None, 0)
+        out = np.zeros((n, n))
+        self.L.orc_mg_coarse_inverse(self.p, mg_id, _dp(out), n * n)
+        return out
+
+    def mg_gsrb_lvl(self, cc, mg_id, lvl, t):
+        self._ck(self.L.orc_mg_gsrb_lvl(self.p, _dp(cc), mg_id, lvl, t), "gsrb")
+
+    def mg_update_coarse(self, cc, mg_id, lvl):
+        self._ck(self.L.orc_mg_update_coarse(self.p, _dp(cc), mg_id, lvl), "update_coarse")
+
+    def mg_correct_lvl(self, cc, mg_id, lvl):
+        self._ck(self.L.orc_mg_correct_lvl(self.p, _dp(cc), mg_id, lvl), "correct")
+
+    def mg_coarse_solve(self, cc, mg_id):
+        self._ck(self.L.orc_mg_coarse_solve(self.p, _dp(cc), mg_id), "coarse_solve")
+
+    def mg_residual(self, cc, mg_id, max_lvl=0):
+        self._ck(self.L.orc_mg_residual(self.p, _dp(cc), mg_id, max_lvl), "residual")
+
+    def mg_vcycle(self, cc, mg_id, set_residual=True, max_lvl=0):
+        r = C.c_double(0)
+        self._ck(self.L.orc_mg_vcycle(self.p, _dp(cc), mg_id, int(set_residual), max_lvl, C.byref(r)), "vcycle")
+        return r.value
+
+    def mg_fmg(self, cc, mg_id, set_residual=True, have_guess=False):
+        r = C.c_double(0)
+        self._ck(self.L.orc_mg_fmg(self.p, _dp(cc), mg_id, int(set_residual), int(have_guess), C.byref(r)), "fmg")
+        return r.value
+
+    def mg_solve(self, cc, mg_id, threshold, max_cycles=50):
+        n = C.c_int(0)
+        res = np.zeros(max_cycles)
+        self._ck(self.L.orc_mg_solve(self.p, _dp(cc), mg_id, threshold, max_cycles, C.byref(n), _dp(res)),
+                 "solve")
+        return n.value, res[:n.value].copy()
+
+    def maxabs(self, cc, iv, leaves_only=True):
+        return self.L.orc_maxabs(self.p, _dp(cc), iv, int(leaves_only))

@@ -1,0 +1,208 @@
+"""GPU multigrid parity against the CPU oracle, through the C-ABI.
+
+Single stages (ghost fill, GSRB, update_coarse, correct_children, coarse
+solve, residual) must match the oracle bit for bit (the FP64 kernels follow
+the reference operation order with no contraction); composite cycles
+(V-cycle, FMG, solve loop) within 1e-12 relative as required for the plain
+FP64 path.  The mixed path (FP32 V-cycle inside FP64 defect correction) is
+checked against the FP64 converged solution within 1e-6 relative.
+"""
+import numpy as np
+import pytest
+
+import afivo_gpu as ag
+import afivo_tree as at
+import oracle
+from mgcases import I_PHI, I_RHS, I_TMP, interior, leaf_error, refined_tree, sine_problem
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "2d16": lambda: refined_tree(2, 16, [32, 32], [1e-2, 1e-2], 5, 2, [0.5e-2, 0.8e-2], 0.6e-3, seed=1, frac=0.1),
+    "2d8cyl": lambda: refined_tree(2, 8, [16, 32], [1e-2, 2e-2], 5, 2, [0.0, 1.2e-2], 0.8e-3,
+                                   coord=ag.AFG_CYL, seed=2, frac=0.1),
+    "3d8": lambda: refined_tree(3, 8, [16, 16, 16], [2e-2, 2e-2, 2e-2], 4, 1, [1e-2, 1e-2, 1.2e-2], 1e-3,
+                                seed=3, frac=0.05),
+    "3d4": lambda: refined_tree(3, 4, [8, 8, 8], [1.0, 1.0, 1.0], 4, 1, [0.3, 0.6, 0.5], 0.1, seed=4, frac=0.1),
+}
+
+
+def bc_for(tree, kind=0):
+    D = tree.ndim
+    if kind == 0:  # field_bc_homogeneous: Neumann sides, Dirichlet 0 / V in the last dim
+        bt = [ag.BC_NEUMANN] * (2 * D - 2) + [ag.BC_DIRICHLET, ag.BC_DIRICHLET]
+        bv = [0.0] * (2 * D - 1) + [-3e4]
+    else:
+        bt = [ag.BC_DIRICHLET, ag.BC_NEUMANN] * D
+        bv = [1.5 * n - 2.0 for n in range(2 * D)]
+    return bt, bv
+
+
+@pytest.fixture(scope="module", params=list(CASES))
+def case(request, gpu_lib):
+    tree = CASES[request.param]()
+    ctx = ag.Context(0)
+    ctx.tree_sync(tree, 3)
+    yield request.param, tree, ctx
+    ctx.close()
+
+
+def setup_pair(tree, ctx, seed, lambda2=0.0, kind=0, precision=ag.FP64):
+    bt, bv = bc_for(tree, kind)
+    desc = ag.mg_desc(I_PHI, I_RHS, I_TMP, bt, bv, lambda2=lambda2, precision=precision)
+    rng = np.random.default_rng(seed)
+    cc = ag.new_cc(tree, 3)
+    cc[:] = rng.standard_normal(cc.shape)
+    cc[:, I_RHS - 1] *= 1e6
+    ctx.mg_setup(0, desc)
+    ctx.upload(cc)
+    o = oracle.Oracle(tree, 3)
+    o.mg_setup(0, desc)
+    return desc, cc, o
+
+
+def download(ctx, tree):
+    out = ag.new_cc(tree, 3)
+    ctx.download(out)
+    return out
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def test_ghost_fill_all_rules_bitexact(case):
+    name, tree, ctx = case
+    o = oracle.Oracle(tree, 3)
+    rng = np.random.default_rng(11)
+    cc = ag.new_cc(tree, 3)
+    cc[:] = rng.standard_normal(cc.shape)
+    ctx.upload(cc)
+    D = tree.ndim
+    for iv, rb in ((1, ag.RB_MG_SIDES), (2, ag.RB_INTERP), (3, ag.RB_INTERP_LIM)):
+        bt = [[ag.BC_DIRICHLET, ag.BC_NEUMANN, ag.BC_CONTINUOUS, ag.BC_DIRICHLET_COPY][(n + iv) % 4]
+              for n in range(2 * D)]
+        bv = [0.25 * n - 0.5 for n in range(2 * D)]
+        ctx.set_cc_methods(iv, bt, bv, rb)
+        o.set_cc_methods(iv, bt, bv, rb)
+        for lvl in range(1, tree.highest_lvl + 1):
+            corners = lvl % 2 == 0
+            ctx.gc(iv, lvl, corners)
+            o.gc(cc, iv, lvl, corners)
+    out = download(ctx, tree)
+    assert np.array_equal(out, cc), f"{name}: max diff {np.max(np.abs(out - cc))}"
+
+
+@pytest.mark.parametrize("lambda2", [0.0, 4.0e6])
+def test_gsrb_levels_bitexact(case, lambda2):
+    name, tree, ctx = case
+    desc, cc, o = setup_pair(tree, ctx, 5, lambda2)
+    for lvl in range(2, tree.highest_lvl + 1):
+        ctx.mg_gsrb_lvl(0, lvl, ag.CYCLE_DOWN)
+        o.mg_gsrb_lvl(cc, 0, lvl, ag.CYCLE_DOWN)
+    ctx.mg_gsrb_lvl(0, tree.highest_lvl, ag.CYCLE_UP)
+    o.mg_gsrb_lvl(cc, 0, tree.highest_lvl, ag.CYCLE_UP)
+    out = download(ctx, tree)
+    assert np.array_equal(out[:, 0], cc[:, 0]), f"{name}: {rel(out[:, 0], cc[:, 0])}"
+
+
+def test_update_coarse_and_correct_bitexact(case):
+    name, tree, ctx = case
+    desc, cc, o = setup_pair(tree, ctx, 6, kind=1)
+    H = tree.highest_lvl
+    ctx.mg_update_coarse(0, H)
+    o.mg_update_coarse(cc, 0, H)
+    out = download(ctx, tree)
+    inner = (slice(None),) + interior(tree)
+    assert np.array_equal(out[:, 0], cc[:, 0]), f"phi {rel(out[:, 0], cc[:, 0])}"
+    assert np.array_equal(out[:, 2], cc[:, 2]), f"tmp {rel(out[:, 2], cc[:, 2])}"
+    assert np.array_equal(out[:, 1][inner], cc[:, 1][inner]), "rhs"
+    ctx.mg_correct_lvl(0, H)
+    o.mg_correct_lvl(cc, 0, H)
+    out = download(ctx, tree)
+    assert np.array_equal(out[:, 0], cc[:, 0]), f"phi after correct {rel(out[:, 0], cc[:, 0])}"
+    assert np.array_equal(out[:, 2], cc[:, 2]), "tmp after correct"
+
+
+def test_coarse_solve_and_residual(case):
+    name, tree, ctx = case
+    desc, cc, o = setup_pair(tree, ctx, 7)
+    ctx.mg_coarse_solve(0)
+    o.mg_coarse_solve(cc, 0)
+    ctx.mg_residual(0)
+    o.mg_residual(cc, 0)
+    out = download(ctx, tree)
+    lv1 = tree.lvl_ids[0] - 1
+    assert rel(out[lv1, 0], cc[lv1, 0]) <= 1e-13, rel(out[lv1, 0], cc[lv1, 0])
+    inner = (slice(None),) + interior(tree)
+    assert rel(out[:, 2][inner], cc[:, 2][inner]) <= 1e-12
+
+
+@pytest.mark.parametrize("lambda2", [0.0, 4.0e6])
+def test_vcycle_fp64_parity(case, lambda2):
+    name, tree, ctx = case
+    desc, cc, o = setup_pair(tree, ctx, 8, lambda2)
+    ctx.gc(I_PHI, 0, True)
+    o.gc(cc, I_PHI, 0, True)
+    for _ in range(2):
+        r_gpu = ctx.mg_vcycle(0, True)
+        r_cpu = o.mg_vcycle(cc, 0, True)
+        assert abs(r_gpu - r_cpu) <= 1e-12 * abs(r_cpu)
+    out = download(ctx, tree)
+    inner = (slice(None),) + interior(tree)
+    e_phi = rel(out[:, 0][inner], cc[:, 0][inner])
+    e_tmp = rel(out[:, 2][inner], cc[:, 2][inner])
+    assert e_phi <= 1e-12 and e_tmp <= 1e-12, (name, e_phi, e_tmp)
+
+
+@pytest.mark.parametrize("have_guess", [False, True])
+def test_fmg_fp64_parity(case, have_guess):
+    name, tree, ctx = case
+    desc, cc, o = setup_pair(tree, ctx, 9, kind=1)
+    ctx.gc(I_PHI, 0, True)
+    o.gc(cc, I_PHI, 0, True)
+    r_gpu = ctx.mg_fmg(0, True, have_guess)
+    r_cpu = o.mg_fmg(cc, 0, True, have_guess)
+    out = download(ctx, tree)
+    inner = (slice(None),) + interior(tree)
+    assert rel(out[:, 0][inner], cc[:, 0][inner]) <= 1e-12
+    assert abs(r_gpu - r_cpu) <= 1e-12 * abs(r_cpu)
+
+
+def test_solve_fp64_and_mixed(case):
+    """Solve loop to 1e-8 relative residual: FP64 path equals the oracle; the
+    mixed path reaches the same threshold with field error <= 1e-6 relative
+    to the FP64 solution."""
+    name, tree, ctx = case
+    cyl = tree.coord == ag.AFG_CYL
+    phi_ex, rhs, bc = sine_problem(tree, 0.0, cyl)
+    cc = ag.new_cc(tree, 3)
+    cc[:, I_RHS - 1] = rhs * 1e10
+    desc = ag.mg_desc(I_PHI, I_RHS, I_TMP, bc)
+    o = oracle.Oracle(tree, 3)
+    o.mg_setup(0, desc)
+    ref = cc.copy()
+    o.gc(ref, I_PHI)
+    thr = 1e-8 * o.maxabs(ref, I_RHS)
+    n_cpu, res_cpu = o.mg_solve(ref, 0, thr, 40)
+    # FP64 GPU
+    ctx.mg_setup(0, desc)
+    ctx.upload(cc)
+    ctx.gc(I_PHI, 0, True)
+    n_gpu, res_gpu = ctx.mg_solve(0, thr, 40)
+    out = download(ctx, tree)
+    inner = (slice(None),) + interior(tree)
+    assert n_gpu == n_cpu
+    assert rel(out[:, 0][inner], ref[:, 0][inner]) <= 1e-12
+    # tighten the reference to 1e-12 and compare the mixed result with it
+    o.mg_solve(ref, 0, 1e-12 * o.maxabs(ref, I_RHS), 40)
+    desc_m = ag.mg_desc(I_PHI, I_RHS, I_TMP, bc, precision=ag.MIXED)
+    ctx.mg_setup(1, desc_m)
+    ctx.upload(cc)
+    ctx.gc(I_PHI, 0, True)
+    n_mix, res_mix = ctx.mg_solve(1, thr, 40)
+    assert res_mix[-1] < thr
+    out = download(ctx, tree)
+    e_mix = leaf_error(tree, out, ref[:, 0])
+    assert e_mix <= 1e-6, (name, e_mix, n_mix, res_mix)
+    assert n_mix <= n_cpu + 3, (n_mix, n_cpu)
