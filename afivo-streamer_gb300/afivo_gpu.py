@@ -74,6 +74,47 @@ class MgDesc(C.Structure):
     ]
 
 
+AFG_MAX_SPECIES = 16
+AFG_MAX_REACTIONS = 32
+AFG_MAX_FLUX = 4
+RATE_TABULATED_FIELD = 1
+RATE_CONSTANT = 2
+RATE_LINEAR = 3
+RATE_EXP_V1 = 4
+RATE_EXP_V2 = 5
+RATE_K13 = 18
+RATE_K14 = 19
+LIMITER_VANLEER = 1
+LIMITER_KOREN = 2
+LIMITER_MINMOD = 3
+LIMITER_MC = 4
+LIMITER_GMINMOD43 = 5
+
+
+class Reaction(C.Structure):
+    _fields_ = [("rate_type", C.c_int), ("lt_col", C.c_int), ("rate_factor", C.c_double),
+                ("c", C.c_double * 4), ("n_in", C.c_int), ("ix_in", C.c_int * 4),
+                ("n_out", C.c_int), ("ix_out", C.c_int * 4), ("mult_out", C.c_int * 4)]
+
+
+class TransportDesc(C.Structure):
+    _fields_ = [
+        ("n_species", C.c_int), ("species_iv", C.c_int * AFG_MAX_SPECIES),
+        ("species_charge", C.c_double * AFG_MAX_SPECIES),
+        ("n_flux", C.c_int), ("flux_species", C.c_int * AFG_MAX_FLUX),
+        ("flux_fc", C.c_int * AFG_MAX_FLUX), ("flux_charge_sign", C.c_double * AFG_MAX_FLUX),
+        ("ion_mobility_N", C.c_double * AFG_MAX_FLUX),
+        ("i_electric_fld", C.c_int), ("i_efield_fc", C.c_int), ("i_photo", C.c_int),
+        ("photoi_species", C.c_int), ("gas_number_density", C.c_double),
+        ("species_gc", GcDesc), ("prolong_limiter", C.c_int),
+        ("lt_n_points", C.c_int), ("lt_x_min", C.c_double), ("lt_inv_fac", C.c_double),
+        ("lt_n_cols", C.c_int), ("lt_data", C.POINTER(C.c_double)),
+        ("lt_col_mobility", C.c_int), ("lt_col_diffusion", C.c_int), ("lt_col_alpha", C.c_int),
+        ("n_reactions", C.c_int), ("reactions", Reaction * AFG_MAX_REACTIONS),
+        ("dt_chemistry_nmin", C.c_double), ("dt_chemistry_limit_loss", C.c_int),
+    ]
+
+
 def _ip(a):
     return a.ctypes.data_as(_IP)
 
@@ -171,6 +212,15 @@ def load_library(path: str = LIB_PATH):
         "afg_mg_correct_lvl": (C.c_int, [P, C.c_int, C.c_int]),
         "afg_mg_coarse_solve": (C.c_int, [P, C.c_int]),
         "afg_mg_residual": (C.c_int, [P, C.c_int, C.c_int]),
+        "afg_transport_setup": (C.c_int, [P, C.POINTER(TransportDesc)]),
+        "afg_flux_upwind": (C.c_int, [P, C.c_int, _DP]),
+        "afg_update_densities": (C.c_int, [P, C.c_double, C.c_int, C.c_int, _IP, _DP, C.c_int,
+                                           C.c_int, _DP]),
+        "afg_field_set_rhs": (C.c_int, [P, C.c_int, C.c_int]),
+        "afg_field_from_potential": (C.c_int, [P, C.c_int]),
+        "afg_field_compute": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                        C.c_double, C.c_int, _IP, _DP]),
+        "afg_photoi_helmh": (C.c_int, [P, C.c_double, C.c_int, _IP, _DP, C.c_double, C.c_int]),
         "afg_sync": (C.c_int, [P]),
         "afg_launch_count": (C.c_longlong, [P]),
     }
@@ -324,11 +374,56 @@ class Context:
     def mg_residual(self, mg_id, max_lvl=0):
         self.check(self.lib.afg_mg_residual(self.ptr, mg_id, max_lvl), "afg_mg_residual")
 
+    # -- transport, field, photoionization --------------------------------
+    def transport_setup(self, desc: TransportDesc):
+        self._transport_desc = desc  # keeps lt_data's buffer reachable
+        self.check(self.lib.afg_transport_setup(self.ptr, C.byref(desc)), "afg_transport_setup")
+
+    def flux_upwind(self, s_deriv):
+        out = np.zeros(2)
+        self.check(self.lib.afg_flux_upwind(self.ptr, s_deriv, _dp(out)), "afg_flux_upwind")
+        return out
+
+    def update_densities(self, dt, s_deriv, s_prev, w_prev, s_out, last_step=False):
+        sp = np.ascontiguousarray(s_prev, dtype=np.int32)
+        wp = np.ascontiguousarray(w_prev, dtype=np.float64)
+        chem = C.c_double(0)
+        self.check(self.lib.afg_update_densities(self.ptr, dt, s_deriv, len(sp), _ip(sp), _dp(wp), s_out,
+                                                 int(last_step), C.byref(chem)), "afg_update_densities")
+        return chem.value
+
+    def field_set_rhs(self, i_rhs, s_in):
+        self.check(self.lib.afg_field_set_rhs(self.ptr, i_rhs, s_in), "afg_field_set_rhs")
+
+    def field_from_potential(self, i_phi):
+        self.check(self.lib.afg_field_from_potential(self.ptr, i_phi), "afg_field_from_potential")
+
+    def field_compute(self, mg_id, s_in, have_guess, voltage, domain_len, max_rel_residual, num_vcycles):
+        n = C.c_int(0)
+        r = C.c_double(0)
+        self.check(self.lib.afg_field_compute(self.ptr, mg_id, s_in, int(have_guess), voltage, domain_len,
+                                              max_rel_residual, num_vcycles, C.byref(n), C.byref(r)),
+                   "afg_field_compute")
+        return n.value, r.value
+
+    def photoi_helmh(self, coeff, mg_ids, coeffs, max_rel_residual=1e-2, max_fmg_cycles=10):
+        ids = np.ascontiguousarray(mg_ids, dtype=np.int32)
+        cs = np.ascontiguousarray(coeffs, dtype=np.float64)
+        self.check(self.lib.afg_photoi_helmh(self.ptr, coeff, len(ids), _ip(ids), _dp(cs), max_rel_residual,
+                                             max_fmg_cycles), "afg_photoi_helmh")
+
     def sync(self):
         self.check(self.lib.afg_sync(self.ptr), "afg_sync")
 
     def launch_count(self) -> int:
         return int(self.lib.afg_launch_count(self.ptr))
+
+
+def new_fc(tree, n_var_face) -> np.ndarray:
+    """Host face arrays laid out like box%fc: [n_boxes, n_var_face, D, (k,) j, i]
+    with nc+1 entries per dimension."""
+    n1 = tree.n_cell + 1
+    return np.zeros((tree.n_boxes, n_var_face, tree.ndim) + (n1,) * tree.ndim)
 
 
 def new_cc(tree, n_var) -> np.ndarray:

@@ -17,7 +17,8 @@ OBJ_DIR = os.path.join(HERE, "build")
 UNITS = ["afg_runtime.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3",
               "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-O2", "--expt-relaxed-constexpr"]
+              "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off",
+              "--expt-relaxed-constexpr"]
 
 
 def _nvcc():

@@ -81,25 +81,47 @@ static int launch_defect(afg_ctx* ctx, MgSlot& m, const double* phi, const doubl
   return AFG_OK;
 }
 
+// Composite-grid consistency: coarse leaf cells next to a refined region read
+// the parent boxes' phi, which the composite discretisation defines as the
+// restriction of their children (the FAS fixed point).  Before each defect
+// the parents are therefore restricted top-down (without geometry, as
+// mg_box_rstr_lpl does for phi) and the ghost cells refreshed.
+static int mixed_prepare(afg_ctx* ctx, MgSlot& m, double* phi) {
+  KTree t = ktree(ctx);
+  for (int lvl = ctx->highest_lvl; lvl >= 2; lvl--) {
+    const int n = (int)ctx->lvl_ids[lvl - 1].size();
+    if (n == 0) continue;
+    if (ctx->D == 3)
+      k_restrict_geom<3, false><<<n, 64, 0, ctx->stream>>>(t, lst(ctx, ctx->off_ids[lvl - 1]), phi);
+    else
+      k_restrict_geom<2, false><<<n, 64, 0, ctx->stream>>>(t, lst(ctx, ctx->off_ids[lvl - 1]), phi);
+    ctx->launches++;
+    CKL();
+  }
+  const GcDev g = mg_gc(m.d, false);
+  for (int lvl = 1; lvl <= ctx->highest_lvl; lvl++) RC(mg_gc_lvl<double>(ctx, lvl, phi, g, 1));
+  return AFG_OK;
+}
+
 static int mixed_solve(afg_ctx* ctx, MgSlot& m, double threshold, int max_cycles, int* n_done, double* residuals) {
   double* phi = ctx->cc[m.d.i_phi - 1];
   double* rhs = ctx->cc[m.d.i_rhs - 1];
-  RC(reset_max(ctx, 2));
-  RC(launch_defect(ctx, m, phi, rhs, ctx->d_max + 2));
   double r = 0;
-  RC(read_max(ctx, 2, &r));
   int n = 0;
-  while (n < max_cycles) {
+  for (;;) {
+    RC(mixed_prepare(ctx, m, phi));
+    RC(reset_max(ctx, 2));
+    RC(launch_defect(ctx, m, phi, rhs, ctx->d_max + 2));
+    RC(read_max(ctx, 2, &r));
+    if (n > 0) {
+      if (residuals) residuals[n - 1] = r;
+      if (r < threshold || n >= max_cycles) break;
+    }
     RC(mg_vcycle<float>(ctx, m, ctx->highest_lvl, m.e32, m.r32, m.t32, false, true, nullptr));
     k_add_correction<<<ctx->n_all, 256, 0, ctx->stream>>>(ctx->S, lst(ctx, ctx->off_all), phi, m.e32);
     ctx->launches++;
     CKL();
-    RC(reset_max(ctx, 2));
-    RC(launch_defect(ctx, m, phi, rhs, ctx->d_max + 2));
-    RC(read_max(ctx, 2, &r));
-    if (residuals) residuals[n] = r;
     n++;
-    if (r < threshold) break;
   }
   if (n_done) *n_done = n;
   return r < threshold ? AFG_OK : AFG_ERR_NOCONV;

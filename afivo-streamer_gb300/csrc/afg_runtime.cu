@@ -1068,3 +1068,5 @@ int afg_mg_solve(afg_ctx* ctx, int mg_id, double threshold, int max_cycles, int*
 }
 
 }  // extern "C"
+
+#include "afg_transport_api.cuh"

@@ -1,0 +1,418 @@
+// afg_transport_api.cuh -- host drivers of the transport, field and
+// photoionization entry points (included at the end of afg_runtime.cu).
+#pragma once
+
+static int need_transport(afg_ctx* ctx) {
+  if (!ctx) return AFG_ERR_ARG;
+  if (!ctx->have_tree) return fail(ctx, AFG_ERR_STATE, "no tree");
+  if (!ctx->tr.ready) return fail(ctx, AFG_ERR_STATE, "afg_transport_setup not called");
+  return AFG_OK;
+}
+
+static LtDev lt_dev(const afg_ctx* ctx) {
+  LtDev lt;
+  lt.y = ctx->tr.d_lt;
+  lt.n = ctx->tr.d.lt_n_points;
+  lt.x_min = ctx->tr.d.lt_x_min;
+  lt.inv_fac = ctx->tr.d.lt_inv_fac;
+  return lt;
+}
+
+static GcDev gc_from_desc(const afg_gc_desc& g) {
+  GcDev d;
+  for (int n = 0; n < 6; n++) {
+    d.bc_type[n] = g.bc_type[n];
+    d.bc_val[n] = g.bc_val[n];
+  }
+  d.rb = g.rb;
+  return d;
+}
+
+extern "C" {
+
+int afg_transport_setup(afg_ctx* ctx, const afg_transport_desc* d) {
+  if (!ctx || !d) return AFG_ERR_ARG;
+  if (!ctx->have_tree) return fail(ctx, AFG_ERR_STATE, "no tree");
+  const afg_transport_desc& t = *d;
+  if (t.n_species < 1 || t.n_species > AFG_MAX_SPECIES) return fail(ctx, AFG_ERR_ARG, "bad n_species");
+  if (t.n_flux < 1 || t.n_flux > AFG_MAX_FLUX) return fail(ctx, AFG_ERR_ARG, "bad n_flux");
+  if (t.n_reactions < 0 || t.n_reactions > AFG_MAX_REACTIONS) return fail(ctx, AFG_ERR_ARG, "bad n_reactions");
+  if (t.lt_n_points < 2 || t.lt_n_cols < 1 || !t.lt_data) return fail(ctx, AFG_ERR_ARG, "bad lookup table");
+  if (!(t.gas_number_density > 0)) return fail(ctx, AFG_ERR_ARG, "gas_number_density must be > 0");
+  for (int c : {t.lt_col_mobility, t.lt_col_diffusion, t.lt_col_alpha})
+    if (c < 0 || c >= t.lt_n_cols) return fail(ctx, AFG_ERR_ARG, "lookup-table column out of range");
+  for (int s = 0; s < t.n_species; s++)
+    if (t.species_iv[s] < 1 || t.species_iv[s] > ctx->n_var) return fail(ctx, AFG_ERR_ARG, "bad species variable");
+  for (int f = 0; f < t.n_flux; f++) {
+    if (t.flux_species[f] < 0 || t.flux_species[f] >= t.n_species) return fail(ctx, AFG_ERR_ARG, "bad flux species");
+    if (t.flux_fc[f] < 1 || t.flux_fc[f] > ctx->n_var_face) return fail(ctx, AFG_ERR_ARG, "bad flux fc variable");
+  }
+  if (t.i_electric_fld < 1 || t.i_electric_fld > ctx->n_var) return fail(ctx, AFG_ERR_ARG, "bad i_electric_fld");
+  if (t.i_efield_fc < 1 || t.i_efield_fc > ctx->n_var_face) return fail(ctx, AFG_ERR_ARG, "bad i_efield_fc");
+  if (t.i_photo < 0 || t.i_photo > ctx->n_var) return fail(ctx, AFG_ERR_ARG, "bad i_photo");
+  if (t.photoi_species < 0 || t.photoi_species >= t.n_species) return fail(ctx, AFG_ERR_ARG, "bad photoi_species");
+  for (int n = 2 * ctx->D; n < 6; n++) (void)n;
+  for (int n = 0; n < 2 * ctx->D; n++)
+    if (t.species_gc.bc_type[n] == AFG_BC_CONTINUOUS)
+      return fail(ctx, AFG_ERR_UNSUPPORTED, "two-layer ghost cells support Dirichlet/Neumann/copy only");
+  for (int r = 0; r < t.n_reactions; r++) {
+    const afg_reaction& rc = t.reactions[r];
+    const int rt = rc.rate_type;
+    if (!(rt == AFG_RATE_TABULATED_FIELD || rt == AFG_RATE_CONSTANT || rt == AFG_RATE_LINEAR ||
+          rt == AFG_RATE_EXP_V1 || rt == AFG_RATE_EXP_V2 || rt == AFG_RATE_K13 || rt == AFG_RATE_K14))
+      return fail(ctx, AFG_ERR_UNSUPPORTED, "reaction %d: unsupported rate form %d", r + 1, rt);
+    if (rt == AFG_RATE_TABULATED_FIELD && (rc.lt_col < 0 || rc.lt_col >= t.lt_n_cols))
+      return fail(ctx, AFG_ERR_ARG, "reaction %d: bad table column", r + 1);
+    if (rc.n_in < 0 || rc.n_in > 4 || rc.n_out < 0 || rc.n_out > 4) return fail(ctx, AFG_ERR_ARG, "bad reaction size");
+    for (int q = 0; q < rc.n_in; q++)
+      if (rc.ix_in[q] < 0 || rc.ix_in[q] >= t.n_species) return fail(ctx, AFG_ERR_ARG, "bad reaction species");
+    for (int q = 0; q < rc.n_out; q++)
+      if (rc.ix_out[q] < 0 || rc.ix_out[q] >= t.n_species) return fail(ctx, AFG_ERR_ARG, "bad reaction species");
+  }
+  TransportState& s = ctx->tr;
+  transport_free(s);
+  s.d = t;
+  s.d.lt_data = nullptr;
+  CK(dalloc(&s.d_lt, (size_t)t.lt_n_cols * t.lt_n_points));
+  CK(cudaMemcpy(s.d_lt, t.lt_data, sizeof(double) * t.lt_n_cols * t.lt_n_points, cudaMemcpyHostToDevice));
+  CK(dalloc(&s.d_reactions, std::max(1, t.n_reactions)));
+  if (t.n_reactions > 0)
+    CK(cudaMemcpy(s.d_reactions, t.reactions, sizeof(afg_reaction) * t.n_reactions, cudaMemcpyHostToDevice));
+  // task lists
+  const int D = ctx->D, nnb = 2 * D, nch = 1 << D;
+  std::vector<int> rrb, cflux;
+  std::vector<int> h_children((size_t)ctx->n_boxes * nch);
+  CK(cudaMemcpy(h_children.data(), ctx->d_children, sizeof(int) * h_children.size(), cudaMemcpyDeviceToHost));
+  std::vector<int> h_parent(ctx->n_boxes);
+  CK(cudaMemcpy(h_parent.data(), ctx->d_parent, sizeof(int) * ctx->n_boxes, cudaMemcpyDeviceToHost));
+  for (int l = 0; l < ctx->highest_lvl; l++)
+    for (int sl : ctx->lvl_leaves[l]) {
+      if (h_parent[sl] < 0) continue;
+      bool rb = false;
+      for (int nb = 0; nb < nnb; nb++) rb = rb || ctx->h_nbr[(size_t)sl * nnb + nb] == 0;
+      if (rb) rrb.push_back(sl);
+    }
+  for (int l = 0; l < ctx->highest_lvl - 1; l++)
+    for (int sl : ctx->lvl_parents[l])
+      for (int nb = 0; nb < nnb; nb++) {
+        const int nid = ctx->h_nbr[(size_t)sl * nnb + nb];
+        if (nid <= 0) continue;
+        bool has_children = false;
+        for (int c = 0; c < nch; c++) has_children = has_children || h_children[(size_t)(nid - 1) * nch + c] >= 0;
+        if (has_children) continue;
+        cflux.push_back(sl);
+        cflux.push_back(nb);
+      }
+  s.n_rrb = (int)rrb.size();
+  s.n_cflux = (int)cflux.size() / 2;
+  CK(dalloc(&s.d_rrb, rrb.size()));
+  CK(dalloc(&s.d_cflux, cflux.size()));
+  if (!rrb.empty()) CK(cudaMemcpy(s.d_rrb, rrb.data(), sizeof(int) * rrb.size(), cudaMemcpyHostToDevice));
+  if (!cflux.empty()) CK(cudaMemcpy(s.d_cflux, cflux.data(), sizeof(int) * cflux.size(), cudaMemcpyHostToDevice));
+  // ghost-cell methods of the densities (all states) and of |E|
+  s.ready = true;
+  return AFG_OK;
+}
+
+static FluxArgs flux_args(afg_ctx* ctx, int s_deriv) {
+  const afg_transport_desc& d = ctx->tr.d;
+  FluxArgs a{};
+  a.nf = d.n_flux;
+  for (int f = 0; f < d.n_flux; f++) {
+    a.n[f] = ctx->cc[d.species_iv[d.flux_species[f]] + s_deriv - 1];
+    a.flux[f] = ctx->fc[d.flux_fc[f] - 1];
+    a.sign[f] = d.flux_charge_sign[f];
+    a.mu_ion_N[f] = d.ion_mobility_N[f];
+  }
+  a.E = ctx->cc[d.i_electric_fld - 1];
+  a.Efc = ctx->fc[d.i_efield_fc - 1];
+  a.bc = gc_from_desc(d.species_gc);
+  a.limiter = d.prolong_limiter;
+  a.N_inv = 1 / d.gas_number_density;
+  a.lt = lt_dev(ctx);
+  a.col_mu = d.lt_col_mobility;
+  a.col_dc = d.lt_col_diffusion;
+  a.max_cfl = ctx->d_max + 3;
+  a.max_sigma = ctx->d_max + 4;
+  return a;
+}
+
+int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim) {
+  RC(need_transport(ctx));
+  const afg_transport_desc& d = ctx->tr.d;
+  for (int f = 0; f < d.n_flux; f++) {
+    const int iv = d.species_iv[d.flux_species[f]] + s_deriv;
+    if (iv < 1 || iv > ctx->n_var) return fail(ctx, AFG_ERR_ARG, "bad state s_deriv");
+  }
+  KTree t = ktree(ctx);
+  const bool cyl = ctx->coord == AFG_CYL;
+  // af_restrict_ref_boundary
+  if (ctx->tr.n_rrb > 0) {
+    for (int f = 0; f < d.n_flux; f++) {
+      double* v = ctx->cc[d.species_iv[d.flux_species[f]] + s_deriv - 1];
+      if (ctx->D == 3)
+        k_restrict_geom<3, false><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v);
+      else if (cyl)
+        k_restrict_geom<2, true><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v);
+      else
+        k_restrict_geom<2, false><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v);
+      ctx->launches++;
+      CKL();
+    }
+  }
+  CK(cudaMemsetAsync(ctx->d_max + 3, 0, 2 * sizeof(unsigned long long), ctx->stream));
+  FluxArgs a = flux_args(ctx, s_deriv);
+  const int nc = ctx->nc, m = nc + 4;
+  const int tile = ctx->D == 2 ? m * m : m * m * m;
+  const int nfaces = ctx->D == 2 ? nc * (nc + 1) : nc * nc * (nc + 1);
+  const size_t smem = sizeof(double) * ((size_t)d.n_flux * tile + 2 * (size_t)ctx->D * nfaces);
+  if (smem > 200 * 1024) return fail(ctx, AFG_ERR_UNSUPPORTED, "box too large for the flux kernel");
+  // leaves level by level: refinement-boundary ghosts read the coarse
+  // neighbour's ghost layer written by the previous level
+  for (int l = 0; l < ctx->highest_lvl; l++) {
+    const int n = (int)ctx->lvl_leaves[l].size();
+    if (n == 0) continue;
+    const int* list = lst(ctx, ctx->off_leaves[l]);
+    if (ctx->D == 3) {
+      CK(cudaFuncSetAttribute(k_flux<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_flux<3, false><<<n, 256, smem, ctx->stream>>>(t, list, a);
+    } else if (cyl) {
+      CK(cudaFuncSetAttribute(k_flux<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_flux<2, true><<<n, 256, smem, ctx->stream>>>(t, list, a);
+    } else {
+      CK(cudaFuncSetAttribute(k_flux<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_flux<2, false><<<n, 256, smem, ctx->stream>>>(t, list, a);
+    }
+    ctx->launches++;
+    CKL();
+  }
+  if (ctx->tr.n_cflux > 0) {
+    if (ctx->D == 3)
+      k_consistent_flux<3, false><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a);
+    else if (cyl)
+      k_consistent_flux<2, true><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a);
+    else
+      k_consistent_flux<2, false><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a);
+    ctx->launches++;
+    CKL();
+  }
+  if (dt_lim) {
+    double mc, ms;
+    RC(read_max(ctx, 3, &mc));
+    RC(read_max(ctx, 4, &ms));
+    dt_lim[0] = 1 / mc;
+    dt_lim[1] = kEps0 / (kElem * std::max(ms, 1e-100));
+  }
+  return AFG_OK;
+}
+
+int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev, const int* s_prev, const double* w_prev,
+                         int s_out, int last_step, double* dt_chem) {
+  RC(need_transport(ctx));
+  const afg_transport_desc& d = ctx->tr.d;
+  if (n_prev < 1 || n_prev > 4 || !s_prev || !w_prev) return fail(ctx, AFG_ERR_ARG, "bad previous states");
+  UpdateArgs a{};
+  a.ns = d.n_species;
+  a.nf = d.n_flux;
+  auto var = [&](int s, int st) -> double* {
+    const int iv = d.species_iv[s] + st;
+    return (iv >= 1 && iv <= ctx->n_var) ? ctx->cc[iv - 1] : nullptr;
+  };
+  for (int s = 0; s < d.n_species; s++) {
+    a.out[s] = var(s, s_out);
+    a.deriv[s] = var(s, s_deriv);
+    if (!a.out[s] || !a.deriv[s]) return fail(ctx, AFG_ERR_ARG, "bad time state");
+    for (int m = 0; m < n_prev; m++) {
+      a.prev[m][s] = var(s, s_prev[m]);
+      if (!a.prev[m][s]) return fail(ctx, AFG_ERR_ARG, "bad previous state");
+    }
+  }
+  for (int m = 0; m < n_prev; m++) a.w_prev[m] = w_prev[m];
+  a.n_prev = n_prev;
+  for (int f = 0; f < d.n_flux; f++) {
+    a.flux_species[f] = d.flux_species[f];
+    a.flux[f] = ctx->fc[d.flux_fc[f] - 1];
+  }
+  a.E = ctx->cc[d.i_electric_fld - 1];
+  a.photo = d.i_photo > 0 ? ctx->cc[d.i_photo - 1] : nullptr;
+  a.photoi_species = d.photoi_species;
+  a.dt = dt;
+  a.N_inv = 1 / d.gas_number_density;
+  a.lt = lt_dev(ctx);
+  a.reactions = ctx->tr.d_reactions;
+  a.n_reactions = d.n_reactions;
+  a.last_step = last_step;
+  a.nmin = d.dt_chemistry_nmin;
+  a.limit_loss = d.dt_chemistry_limit_loss;
+  a.min_chem = ctx->d_max + 5;
+  const double big = 1e100;
+  unsigned long long bits;
+  memcpy(&bits, &big, sizeof(bits));
+  CK(cudaMemcpyAsync(ctx->d_max + 5, &bits, sizeof(bits), cudaMemcpyHostToDevice, ctx->stream));
+  KTree t = ktree(ctx);
+  const int n = ctx->n_all_leaves;
+  const int* list = lst(ctx, ctx->off_all_leaves);
+  if (n > 0) {
+    if (ctx->D == 3)
+      k_update<3, false><<<n, 128, 0, ctx->stream>>>(t, list, a);
+    else if (ctx->coord == AFG_CYL)
+      k_update<2, true><<<n, 128, 0, ctx->stream>>>(t, list, a);
+    else
+      k_update<2, false><<<n, 128, 0, ctx->stream>>>(t, list, a);
+    ctx->launches++;
+    CKL();
+  }
+  if (dt_chem) {
+    if (last_step)
+      RC(read_max(ctx, 5, dt_chem));
+    else
+      *dt_chem = 1e100;
+  }
+  return AFG_OK;
+}
+
+int afg_field_set_rhs(afg_ctx* ctx, int i_rhs, int s_in) {
+  RC(need_transport(ctx));
+  RC(check_var(ctx, i_rhs));
+  const afg_transport_desc& d = ctx->tr.d;
+  RhsArgs a{};
+  a.ns = d.n_species;
+  const double fac = -kElem / kEps0;
+  for (int s = 0; s < d.n_species; s++) {
+    const int iv = d.species_iv[s] + s_in;
+    if (iv < 1 || iv > ctx->n_var) return fail(ctx, AFG_ERR_ARG, "bad state s_in");
+    a.n[s] = ctx->cc[iv - 1];
+    a.q[s] = d.species_charge[s] != 0 ? d.species_charge[s] * fac : 0.0;
+  }
+  a.rhs = ctx->cc[i_rhs - 1];
+  if (ctx->n_all_leaves > 0) {
+    k_field_rhs<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ctx->S, lst(ctx, ctx->off_all_leaves), a);
+    ctx->launches++;
+    CKL();
+  }
+  return AFG_OK;
+}
+
+int afg_field_from_potential(afg_ctx* ctx, int i_phi) {
+  RC(need_transport(ctx));
+  RC(check_var(ctx, i_phi));
+  const afg_transport_desc& d = ctx->tr.d;
+  KTree t = ktree(ctx);
+  double* efc = ctx->fc[d.i_efield_fc - 1];
+  double* en = ctx->cc[d.i_electric_fld - 1];
+  if (ctx->D == 3)
+    k_field_grad<3><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en);
+  else
+    k_field_grad<2><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en);
+  ctx->launches++;
+  CKL();
+  if (!ctx->has_method[d.i_electric_fld - 1])
+    return fail(ctx, AFG_ERR_STATE, "no ghost-cell methods for the electric field norm");
+  return afg_gc(ctx, d.i_electric_fld, 0, 1);
+}
+
+int afg_field_compute(afg_ctx* ctx, int mg_id, int s_in, int have_guess, double voltage, double domain_len,
+                      double max_rel_residual, int num_vcycles, int* n_cycles, double* residual) {
+  RC(need_transport(ctx));
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  RC(afg_field_set_rhs(ctx, m->d.i_rhs, s_in));
+  // field_bc_homogeneous: Dirichlet `voltage` on the high face of the last dimension
+  double bcv[6];
+  for (int q = 0; q < 6; q++) bcv[q] = m->d.bc_val[q];
+  bcv[2 * ctx->D - 1] = voltage;
+  RC(afg_mg_set_bc_values(ctx, mg_id, bcv));
+  double max_rhs;
+  RC(afg_maxabs(ctx, m->d.i_rhs, 1, &max_rhs));
+  // af_min_dr: finest dr of the highest level
+  std::vector<double> hdr(ctx->D);
+  const int s_fine = ctx->lvl_ids[ctx->highest_lvl - 1][0];
+  CK(cudaMemcpy(hdr.data(), ctx->d_dr + (size_t)s_fine * ctx->D, sizeof(double) * ctx->D, cudaMemcpyDeviceToHost));
+  double min_dr = hdr[0];
+  for (int q = 1; q < ctx->D; q++) min_dr = std::min(min_dr, hdr[q]);
+  const double threshold =
+      std::max(std::max(1e-6, max_rhs * max_rel_residual), 1e-10 * std::fabs(voltage) / (domain_len * min_dr));
+  int nc_done = 0;
+  double r = 0;
+  if (!have_guess) {
+    double res[100];
+    int i;
+    for (i = 0; i < 100; i++) {
+      RC(afg_mg_fmg(ctx, mg_id, 1, 1, &res[i]));
+      nc_done++;
+      if (res[i] < threshold) break;
+      if (i >= 2) {
+        const double mn = std::min(res[i], std::min(res[i - 1], res[i - 2]));
+        const double mx = std::max(res[i], std::max(res[i - 1], res[i - 2]));
+        const double ratio = mn / mx;
+        if (ratio < 2.0 && ratio > 0.5 && res[i] < 1e8) break;
+      }
+    }
+    if (i == 100) return fail(ctx, AFG_ERR_NOCONV, "no convergence in initial field computation");
+    r = res[std::min(i, 99)];
+  }
+  int nv = 0;
+  if (num_vcycles > 0) {
+    double hist[256];
+    const int rc = afg_mg_solve(ctx, mg_id, threshold, std::min(num_vcycles, 256), &nv, hist);
+    if (rc != AFG_OK && rc != AFG_ERR_NOCONV) return rc;
+    if (nv > 0) r = hist[nv - 1];
+  }
+  nc_done += nv;
+  RC(afg_field_from_potential(ctx, m->d.i_phi));
+  if (n_cycles) *n_cycles = nc_done;
+  if (residual) *residual = r;
+  return AFG_OK;
+}
+
+int afg_photoi_helmh(afg_ctx* ctx, double coeff, int n_modes, const int* mg_ids, const double* coeffs,
+                     double max_rel_residual, int max_fmg_cycles) {
+  RC(need_transport(ctx));
+  const afg_transport_desc& d = ctx->tr.d;
+  if (n_modes < 1 || !mg_ids || !coeffs || d.i_photo <= 0) return fail(ctx, AFG_ERR_ARG, "bad photoionization args");
+  MgSlot* m0;
+  RC(get_mg(ctx, mg_ids[0], &m0));
+  const int i_rhs = m0->d.i_rhs;
+  KTree t = ktree(ctx);
+  // photon production on leaves
+  if (ctx->n_all_leaves > 0) {
+    const double* E = ctx->cc[d.i_electric_fld - 1];
+    const double* ne = ctx->cc[d.species_iv[d.flux_species[0]] - 1];
+    double* rhs = ctx->cc[i_rhs - 1];
+    if (ctx->D == 3)
+      k_photo_source<3><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all_leaves), E, ne, rhs,
+                                                                  lt_dev(ctx), d.lt_col_alpha, d.lt_col_mobility,
+                                                                  d.gas_number_density, coeff);
+    else
+      k_photo_source<2><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all_leaves), E, ne, rhs,
+                                                                  lt_dev(ctx), d.lt_col_alpha, d.lt_col_mobility,
+                                                                  d.gas_number_density, coeff);
+    ctx->launches++;
+    CKL();
+  }
+  // photoi_helmh_compute
+  double* photo = ctx->cc[d.i_photo - 1];
+  CK(cudaMemsetAsync(photo, 0, sizeof(double) * (size_t)ctx->n_boxes * ctx->S, ctx->stream));
+  double max_rhs;
+  RC(afg_maxabs(ctx, i_rhs, 1, &max_rhs));
+  max_rhs = std::max(max_rhs, std::sqrt(2.220446049250313e-16));
+  for (int n = 0; n < n_modes; n++) {
+    MgSlot* m;
+    RC(get_mg(ctx, mg_ids[n], &m));
+    if (m->d.i_rhs != i_rhs) return fail(ctx, AFG_ERR_ARG, "Helmholtz modes must share i_rhs");
+    for (int i = 0; i < max_fmg_cycles; i++) {
+      double res;
+      RC(afg_mg_fmg(ctx, mg_ids[n], 1, 1, &res));
+      if (res / max_rhs < max_rel_residual) break;
+    }
+    if (ctx->n_all_leaves > 0) {
+      k_axpy_boxes<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ctx->S, lst(ctx, ctx->off_all_leaves), photo,
+                                                              ctx->cc[m->d.i_phi - 1], coeffs[n]);
+      ctx->launches++;
+      CKL();
+    }
+  }
+  return AFG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,212 @@
+"""Host-side setup of the streamer fluid model for the GPU path.
+
+This stands in for the reference's host initialisation, which stays on the
+host and outside the hot path: the variable registry (src/m_streamer.f90:
+201-476), the transport lookup table (transport_data_initialize,
+src/m_transport_data.f90:61-220, and LT_create/table_set_x,
+src/lookup_table_fortran/m_lookup_table.f90:186-289), the chemistry
+(chemistry_initialize with the standard two-reaction model when no reaction
+file is given, src/m_chemistry.f90:222-261) and the multigrid options of
+field_initialize / photoi_helmh_initialize (src/m_field.f90:107-395,
+src/m_photoi_helmh.f90:44-160).  It produces the C-ABI descriptors.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+import afivo_gpu as ag
+
+SI_TO_TD = 1e21          # SI_to_Townsend (src/m_gas.f90:39)
+TD_TO_SI = 1e-21
+ELEM = 1.602176634e-19   # UC_elem_charge
+EPS0 = 8.8541878128e-12  # UC_eps0
+KB = 1.380649e-23        # UC_boltzmann_const
+
+
+def gas_number_density(pressure_bar=1.0, temperature=300.0):
+    """N = 1e5 * p / (k_B * T), src/m_gas.f90:174-176."""
+    return 1e5 * pressure_bar / (KB * temperature)
+
+
+def table_x(x_min, x_max, n_points):
+    """get_x / table_set_x for linear spacing (m_lookup_table.f90:205-289)."""
+    tmp = 1.0 / (n_points - 1)
+    x = np.arange(n_points, dtype=np.float64) * tmp
+    x = x_min + x * (x_max - x_min)
+    inv_fac = (n_points - 1) / (x_max - x_min)
+    return x, inv_fac
+
+
+@dataclass
+class Species:
+    name: str
+    charge: float
+
+
+@dataclass
+class StreamerModel:
+    """Variables, transport table and chemistry of a streamer run."""
+    ndim: int
+    n_states: int = 3                 # af_advance_num_steps(heun) + 1 copies
+    species: list = field(default_factory=list)
+    mobile_ions: list = field(default_factory=list)  # (species index, mobility m^2/Vs)
+    photoi_modes: int = 0
+    N: float = gas_number_density()
+    mu: float = 0.03                  # m^2/(V s)
+    dif: float = 0.1                  # m^2/s
+    alpha: callable = None            # alpha(E) in 1/m, E in V/m
+    eta: callable = None
+    reactions: list = field(default_factory=list)  # list of dict (see below)
+    table_size: int = 1000
+    td_max: float = 1000.0
+    bc_species: int = ag.BC_NEUMANN
+
+    # variable layout (1-based tree indices)
+    def __post_init__(self):
+        if not self.species:
+            self.species = [Species("e", -1.0), Species("M+", 1.0), Species("M-", -1.0)]
+        self.i_phi, self.i_electric_fld, self.i_rhs, self.i_tmp = 1, 2, 3, 4
+        nxt = 5
+        self.species_iv = []
+        for _ in self.species:
+            self.species_iv.append(nxt)
+            nxt += self.n_states
+        self.i_photo = 0
+        if self.photoi_modes > 0:
+            self.i_photo = nxt
+            nxt += 1
+        self.i_modes = []
+        for _ in range(self.photoi_modes):
+            self.i_modes.append(nxt)
+            nxt += 1
+        self.n_var_cell = nxt - 1
+        self.f_efield = 1
+        self.f_flux = [2 + n for n in range(1 + len(self.mobile_ions))]
+        self.n_var_face = 1 + len(self.f_flux)
+        self.build_table()
+
+    def build_table(self):
+        """Transport lookup table over the reduced field (columns: mu*N,
+        D*N, alpha/N, eta/N, then one column per tabulated reaction)."""
+        N = self.N
+        x, inv_fac = table_x(0.0, self.td_max, self.table_size)
+        E = x * TD_TO_SI * N
+        with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+            a = self.alpha(E) if self.alpha else np.zeros_like(E)
+            h = self.eta(E) if self.eta else np.zeros_like(E)
+        a = np.where(np.isfinite(a), a, 0.0)
+        h = np.where(np.isfinite(h), h, 0.0)
+        mobN = np.full_like(x, self.mu * N)
+        difN = np.full_like(x, self.dif * N)
+        cols = [mobN, difN, a / N, h / N]
+        self.col_mobility, self.col_diffusion, self.col_alpha, self.col_eta = 0, 1, 2, 3
+        self.lt_x = x
+        self.lt_inv_fac = inv_fac
+        # standard model reactions (src/m_chemistry.f90:232-257):
+        # y = alpha/N * mu*N * Td * Townsend_to_SI * N
+        if not self.reactions:
+            self.reactions = [
+                dict(type=ag.RATE_TABULATED_FIELD, col=len(cols), ix_in=[0], ix_out=[0, 1], mult=[2, 1]),
+            ]
+            cols.append(cols[2] * cols[0] * x * TD_TO_SI * N)
+            if self.eta is not None and len(self.species) > 2:
+                self.reactions.append(
+                    dict(type=ag.RATE_TABULATED_FIELD, col=len(cols), ix_in=[0], ix_out=[2], mult=[1]))
+                cols.append(cols[3] * cols[0] * x * TD_TO_SI * N)
+        self.lt = np.ascontiguousarray(np.stack(cols), dtype=np.float64)  # [n_cols][n_points]
+
+    def transport_desc(self) -> ag.TransportDesc:
+        d = ag.TransportDesc()
+        d.n_species = len(self.species)
+        for s, sp in enumerate(self.species):
+            d.species_iv[s] = self.species_iv[s]
+            d.species_charge[s] = sp.charge
+        d.n_flux = 1 + len(self.mobile_ions)
+        d.flux_species[0] = 0
+        d.flux_fc[0] = self.f_flux[0]
+        d.flux_charge_sign[0] = -1.0
+        for n, (s, mob) in enumerate(self.mobile_ions):
+            d.flux_species[1 + n] = s
+            d.flux_fc[1 + n] = self.f_flux[1 + n]
+            d.flux_charge_sign[1 + n] = float(np.sign(self.species[s].charge))
+            # scaled with the gas number density at 300 K and 1 bar
+            # (src/m_transport_data.f90:206-208)
+            d.ion_mobility_N[1 + n] = mob * (1e5 / (KB * 300))
+        d.i_electric_fld = self.i_electric_fld
+        d.i_efield_fc = self.f_efield
+        d.i_photo = self.i_photo
+        d.photoi_species = 1
+        d.gas_number_density = self.N
+        d.species_gc = ag.gc_desc([self.bc_species] * (2 * self.ndim), None, ag.RB_INTERP_LIM)
+        d.prolong_limiter = ag.LIMITER_MC if self.ndim < 3 else ag.LIMITER_GMINMOD43
+        d.lt_n_points = self.lt.shape[1]
+        d.lt_x_min = float(self.lt_x[0])
+        d.lt_inv_fac = self.lt_inv_fac
+        d.lt_n_cols = self.lt.shape[0]
+        d.lt_data = self.lt.ctypes.data_as(C.POINTER(C.c_double))
+        d.lt_col_mobility = self.col_mobility
+        d.lt_col_diffusion = self.col_diffusion
+        d.lt_col_alpha = self.col_alpha
+        d.n_reactions = len(self.reactions)
+        for n, r in enumerate(self.reactions):
+            R = d.reactions[n]
+            R.rate_type = r["type"]
+            R.lt_col = r.get("col", 0)
+            R.rate_factor = r.get("factor", 1.0)
+            for q, c in enumerate(r.get("c", [])):
+                R.c[q] = c
+            R.n_in = len(r["ix_in"])
+            for q, v in enumerate(r["ix_in"]):
+                R.ix_in[q] = v
+            R.n_out = len(r["ix_out"])
+            for q, v in enumerate(r["ix_out"]):
+                R.ix_out[q] = v
+                R.mult_out[q] = r["mult"][q]
+        d.dt_chemistry_nmin = 0.0
+        d.dt_chemistry_limit_loss = 1
+        return d
+
+    def field_bc(self, voltage):
+        """field_bc_homogeneous (src/m_field.f90:590-610)."""
+        D = self.ndim
+        bt = [ag.BC_NEUMANN] * (2 * D - 2) + [ag.BC_DIRICHLET, ag.BC_DIRICHLET]
+        bv = [0.0] * (2 * D - 1) + [voltage]
+        return bt, bv
+
+    def field_mg(self, voltage, precision=ag.FP64):
+        bt, bv = self.field_bc(voltage)
+        return ag.mg_desc(self.i_phi, self.i_rhs, self.i_tmp, bt, bv, precision=precision)
+
+    def helmholtz_mg(self, lam, precision=ag.FP64):
+        """photoi_helmh_bc: Dirichlet 0 in the last dimension, Neumann 0 else."""
+        D = self.ndim
+        bt = [ag.BC_NEUMANN] * (2 * D - 2) + [ag.BC_DIRICHLET, ag.BC_DIRICHLET]
+        out = []
+        for n, l in enumerate(lam):
+            out.append(ag.mg_desc(self.i_modes[n], self.i_rhs, self.i_tmp, bt, None, lambda2=l * l,
+                                  precision=precision))
+        return out
+
+    def electric_fld_gc(self):
+        """|E|: af_bc_neumann_zero + af_gc_interp (src/m_field.f90:392-393)."""
+        return [ag.BC_NEUMANN] * (2 * self.ndim), None, ag.RB_INTERP
+
+    def photo_gc(self):
+        """i_photo: photoi_helmh_bc + af_gc_interp (src/m_photoi.f90:115)."""
+        D = self.ndim
+        return [ag.BC_NEUMANN] * (2 * D - 2) + [ag.BC_DIRICHLET, ag.BC_DIRICHLET], None, ag.RB_INTERP
+
+
+def baseline_alpha(E):
+    """alpha(E) = 4.3e5 * exp(-2e7/|E|) 1/m (the analytic ionization
+    coefficient of the synthetic streamer workloads)."""
+    E = np.abs(E)
+    with np.errstate(divide="ignore", over="ignore"):
+        return np.where(E > 0, 4.3e5 * np.exp(-2e7 / np.maximum(E, 1e-300)), 0.0)
+
+
+def baseline_eta(E):
+    return np.full_like(np.asarray(E, dtype=np.float64), 2e3)

@@ -201,6 +201,127 @@ int afg_mg_coarse_solve(afg_ctx* ctx, int mg_id);
 /* residual_box (801-810) on all boxes of levels 1..max_lvl into i_tmp. */
 int afg_mg_residual(afg_ctx* ctx, int mg_id, int max_lvl);
 
+/* ---- drift-diffusion transport and sources (src/m_fluid.f90) ------------ */
+
+#define AFG_MAX_SPECIES   16
+#define AFG_MAX_REACTIONS 32
+#define AFG_MAX_FLUX       4
+
+/* Reaction-rate forms, values of rate_* in src/m_chemistry.f90:65-126.  Forms
+ * that depend only on the (constant) gas temperature are evaluated on the
+ * host and passed as AFG_RATE_CONSTANT. */
+#define AFG_RATE_TABULATED_FIELD 1  /* c0 * LT(col, Td)                      */
+#define AFG_RATE_CONSTANT        2  /* c0 * c1                               */
+#define AFG_RATE_LINEAR          3  /* c0 * c1 * (Td - c2)                   */
+#define AFG_RATE_EXP_V1          4  /* c0 * c1 * exp(-(c2/(c3 + Td))**2)     */
+#define AFG_RATE_EXP_V2          5  /* c0 * c1 * exp(-(Td/c2)**2)            */
+#define AFG_RATE_K13            18  /* c0 * c1 * exp(-(c2/(c3 + Td))**c4)    */
+#define AFG_RATE_K14            19  /* c0 * c1 * exp(-(Td/c2)**c3)           */
+
+/* Slope limiters (af_limiter_*_t, afivo/src/m_af_limiters.f90) used by the
+ * two-layer refinement-boundary ghost cells (gc2_prolong_rb). */
+#define AFG_LIMITER_VANLEER   1
+#define AFG_LIMITER_KOREN     2
+#define AFG_LIMITER_MINMOD    3
+#define AFG_LIMITER_MC        4
+#define AFG_LIMITER_GMINMOD43 5
+
+typedef struct afg_reaction {
+  int rate_type;           /* AFG_RATE_*                                    */
+  int lt_col;              /* table column of a tabulated rate (0-based)    */
+  double rate_factor;      /* reactions(n)%rate_factor                      */
+  double c[4];             /* reactions(n)%rate_data                        */
+  int n_in;                /* species consumed (gas species excluded)       */
+  int ix_in[4];            /* indices into the species list (0-based)       */
+  int n_out;
+  int ix_out[4];
+  int mult_out[4];         /* multiplicity_out                              */
+} afg_reaction;
+
+/* Transport model: the variables and tables m_fluid/m_chemistry use
+ * (src/m_streamer.f90:17-71, src/m_transport_data.f90:61-220,
+ * src/m_chemistry.f90:200-300).  All indices are 1-based tree variables
+ * unless stated otherwise; the density of species s in time state st is
+ * cc variable species_iv[s] + st. */
+typedef struct afg_transport_desc {
+  int n_species;
+  int species_iv[AFG_MAX_SPECIES];
+  double species_charge[AFG_MAX_SPECIES];
+  int n_flux;                         /* [0] electrons (drift + diffusion), then mobile ions */
+  int flux_species[AFG_MAX_FLUX];     /* 0-based index into the species list */
+  int flux_fc[AFG_MAX_FLUX];          /* fc variable holding each flux (flux_variables) */
+  double flux_charge_sign[AFG_MAX_FLUX];
+  double ion_mobility_N[AFG_MAX_FLUX];/* mobility*N of mobile ions (entry 0 unused) */
+  int i_electric_fld;                 /* cc |E|  */
+  int i_efield_fc;                    /* fc E    (electric_fld) */
+  int i_photo;                        /* cc photoionization source; 0 = none */
+  int photoi_species;                 /* 0-based species that also gains the photo source */
+  double gas_number_density;          /* N, m^-3 */
+  afg_gc_desc species_gc;             /* bc_species + af_gc_interp_lim */
+  int prolong_limiter;                /* AFG_LIMITER_* of gc2_prolong_rb */
+  /* lookup table over the reduced field Td (td_tbl and chemtbl_fld share the
+   * grid, src/m_chemistry.f90:348): linear x-spacing, rows_cols(n_points, n_cols) */
+  int lt_n_points;
+  double lt_x_min;
+  double lt_inv_fac;
+  int lt_n_cols;
+  const double* lt_data;              /* [n_cols][n_points] (column after column) */
+  int lt_col_mobility;                /* td_mobility: mu*N   */
+  int lt_col_diffusion;               /* td_diffusion: D*N   */
+  int lt_col_alpha;                   /* td_alpha: alpha/N (photoionization source) */
+  int n_reactions;
+  afg_reaction reactions[AFG_MAX_REACTIONS];
+  double dt_chemistry_nmin;           /* dt_chemistry_nmin */
+  int dt_chemistry_limit_loss;        /* dt_chemistry_limit_loss */
+} afg_transport_desc;
+
+/* Store the transport model (transport_data_initialize, chemistry_initialize). */
+int afg_transport_setup(afg_ctx* ctx, const afg_transport_desc* tr);
+
+/* flux_upwind_tree (afivo/src/m_af_flux_schemes.f90:666-712) with the fluid
+ * model's flux_upwind/flux_direction (src/m_fluid.f90:102-227) and the Koren
+ * limiter, for densities of state s_deriv: restriction near refinement
+ * boundaries, two-layer ghost cells, upwind fluxes into the flux fc
+ * variables, af_consistent_fluxes.  dt_lim[0] = CFL limit (before
+ * dt_cfl_number), dt_lim[1] = dielectric relaxation time. */
+int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim);
+
+/* flux_update_densities (m_af_flux_schemes.f90:320-436) with
+ * add_source_terms (src/m_fluid.f90:298-466): state s_out = sum_m w_prev[m] *
+ * state s_prev[m] + dt * (chemistry + photoionization) + dt/dr * flux
+ * divergence, on all leaves.  When last_step != 0, *dt_chem receives the
+ * chemistry time-step limit. */
+int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev,
+                         const int* s_prev, const double* w_prev, int s_out,
+                         int last_step, double* dt_chem);
+
+/* field_set_rhs (src/m_field.f90:406-444): rhs = -e/eps0 * sum q_s n_s
+ * (state s_in) on leaves. */
+int afg_field_set_rhs(afg_ctx* ctx, int i_rhs, int s_in);
+
+/* field_from_potential (src/m_field.f90:531-548): E = -grad(phi) on faces
+ * of all boxes (mg_compute_phi_gradient, m_af_multigrid.f90:1857-1994), |E|
+ * at cell centres (mg_box_field_norm 2015-2045), then ghost cells of |E|. */
+int afg_field_from_potential(afg_ctx* ctx, int i_phi);
+
+/* field_compute (src/m_field.f90:448-528): rhs from the charges of state
+ * s_in, boundary value `voltage` on the highest face of the last dimension,
+ * FMG start when have_guess == 0, V-cycles until max|residual| < threshold
+ * = max(1e-6, max|rhs|*max_rel_residual, 1e-10*|V|/(domain_len*dx_min)),
+ * field from potential.  n_cycles and the final residual are returned. */
+int afg_field_compute(afg_ctx* ctx, int mg_id, int s_in, int have_guess,
+                      double voltage, double domain_len, double max_rel_residual,
+                      int num_vcycles, int* n_cycles, double* residual);
+
+/* photoionization_rate_from_alpha (src/m_photoi.f90:259-291) into i_rhs on
+ * leaves (coeff = eta * quenching factor), then photoi_helmh_compute
+ * (src/m_photoi_helmh.f90:162-204) with the Helmholtz modes in solver slots
+ * mg_ids[0..n_modes-1] (their lambda^2 set at afg_mg_setup):
+ * i_photo = -sum_n coeffs[n] * phi_n on leaves. */
+int afg_photoi_helmh(afg_ctx* ctx, double coeff, int n_modes, const int* mg_ids,
+                     const double* coeffs, double max_rel_residual,
+                     int max_fmg_cycles);
+
 /* Synchronise the context's stream and check the device error word. */
 int afg_sync(afg_ctx* ctx);
 

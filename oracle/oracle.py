@@ -44,6 +44,13 @@ def lib():
             "orc_mg_fmg": (C.c_int, [P, DP, C.c_int, C.c_int, C.c_int, DP]),
             "orc_mg_solve": (C.c_int, [P, DP, C.c_int, C.c_double, C.c_int, IP, DP]),
             "orc_maxabs": (C.c_double, [P, DP, C.c_int, C.c_int]),
+            "orc_transport_setup": (C.c_int, [P, C.POINTER(ag.TransportDesc)]),
+            "orc_flux_upwind": (C.c_int, [P, DP, DP, C.c_int, DP]),
+            "orc_update_densities": (C.c_int, [P, DP, DP, C.c_double, C.c_int, C.c_int, IP, DP, C.c_int,
+                                               C.c_int, DP]),
+            "orc_field_set_rhs": (C.c_int, [P, DP, C.c_int, C.c_int]),
+            "orc_field_from_potential": (C.c_int, [P, DP, DP, C.c_int]),
+            "orc_photoi_source": (C.c_int, [P, DP, C.c_double, C.c_int]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -134,6 +141,33 @@ class Oracle:
         self._ck(self.L.orc_mg_solve(self.p, _dp(cc), mg_id, threshold, max_cycles, C.byref(n), _dp(res)),
                  "solve")
         return n.value, res[:n.value].copy()
+
+    # -- transport ------------------------------------------------------------
+    def transport_setup(self, desc):
+        self._ck(self.L.orc_transport_setup(self.p, C.byref(desc)), "transport_setup")
+
+    def flux_upwind(self, cc, fc, s_deriv):
+        out = np.zeros(2)
+        self._ck(self.L.orc_flux_upwind(self.p, _dp(cc), _dp(fc), s_deriv, _dp(out)), "flux_upwind")
+        return out
+
+    def update_densities(self, cc, fc, dt, s_deriv, s_prev, w_prev, s_out, last_step=False):
+        sp = np.ascontiguousarray(s_prev, dtype=np.int32)
+        wp = np.ascontiguousarray(w_prev, dtype=np.float64)
+        chem = C.c_double(0)
+        self._ck(self.L.orc_update_densities(self.p, _dp(cc), _dp(fc), dt, s_deriv, len(sp),
+                                             sp.ctypes.data_as(C.POINTER(C.c_int)), _dp(wp), s_out,
+                                             int(last_step), C.byref(chem)), "update_densities")
+        return chem.value
+
+    def field_set_rhs(self, cc, i_rhs, s_in):
+        self._ck(self.L.orc_field_set_rhs(self.p, _dp(cc), i_rhs, s_in), "field_set_rhs")
+
+    def field_from_potential(self, cc, fc, i_phi):
+        self._ck(self.L.orc_field_from_potential(self.p, _dp(cc), _dp(fc), i_phi), "field_from_potential")
+
+    def photoi_source(self, cc, coeff, i_rhs):
+        self._ck(self.L.orc_photoi_source(self.p, _dp(cc), coeff, i_rhs), "photoi_source")
 
     def maxabs(self, cc, iv, leaves_only=True):
         return self.L.orc_maxabs(self.p, _dp(cc), iv, int(leaves_only))

@@ -21,7 +21,7 @@ CASES = {
     "2d16": lambda: refined_tree(2, 16, [32, 32], [1e-2, 1e-2], 5, 2, [0.5e-2, 0.8e-2], 0.6e-3, seed=1, frac=0.1),
     "2d8cyl": lambda: refined_tree(2, 8, [16, 32], [1e-2, 2e-2], 5, 2, [0.0, 1.2e-2], 0.8e-3,
                                    coord=ag.AFG_CYL, seed=2, frac=0.1),
-    "3d8": lambda: refined_tree(3, 8, [16, 16, 16], [2e-2, 2e-2, 2e-2], 4, 1, [1e-2, 1e-2, 1.2e-2], 1e-3,
+    "3d8": lambda: refined_tree(3, 8, [8, 8, 8], [2e-2, 2e-2, 2e-2], 5, 2, [1e-2, 1e-2, 1.2e-2], 1e-3,
                                 seed=3, frac=0.05),
     "3d4": lambda: refined_tree(3, 4, [8, 8, 8], [1.0, 1.0, 1.0], 4, 1, [0.3, 0.6, 0.5], 0.1, seed=4, frac=0.1),
 }
