@@ -40,6 +40,7 @@ FP64 = 0
 MIXED = 1
 CYCLE_DOWN = 1
 CYCLE_UP = 3
+KT_NONE, KT_GSRB, KT_GHOST, KT_FLUX, KT_UPDATE, KT_RESIDUAL = 0, 1, 2, 3, 4, 5
 
 _IP = C.POINTER(C.c_int)
 _DP = C.POINTER(C.c_double)
@@ -221,6 +222,13 @@ def load_library(path: str = LIB_PATH):
         "afg_field_compute": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                         C.c_double, C.c_int, _IP, _DP]),
         "afg_photoi_helmh": (C.c_int, [P, C.c_double, C.c_int, _IP, _DP, C.c_double, C.c_int]),
+        "afg_tree_copy_cc": (C.c_int, [P, C.c_int, C.c_int]),
+        "afg_counters": (C.c_int, [P, C.POINTER(C.c_longlong)]),
+        "afg_event_record": (C.c_int, [P, C.c_int]),
+        "afg_event_elapsed": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_float)]),
+        "afg_flush_l2": (C.c_int, [P, C.c_longlong]),
+        "afg_kernel_timing": (C.c_int, [P, C.c_int]),
+        "afg_kernel_stats": (C.c_int, [P, C.POINTER(C.c_longlong), _DP, _DP]),
         "afg_sync": (C.c_int, [P]),
         "afg_launch_count": (C.c_longlong, [P]),
     }
@@ -411,6 +419,35 @@ class Context:
         cs = np.ascontiguousarray(coeffs, dtype=np.float64)
         self.check(self.lib.afg_photoi_helmh(self.ptr, coeff, len(ids), _ip(ids), _dp(cs), max_rel_residual,
                                              max_fmg_cycles), "afg_photoi_helmh")
+
+    def tree_copy_cc(self, iv_from, iv_to):
+        self.check(self.lib.afg_tree_copy_cc(self.ptr, iv_from, iv_to), "afg_tree_copy_cc")
+
+    def counters(self):
+        out = (C.c_longlong * 4)()
+        self.check(self.lib.afg_counters(self.ptr, out), "afg_counters")
+        return dict(launches=out[0], smoother_updates=out[1], transport_updates=out[2], vcycles=out[3])
+
+    def event_record(self, slot):
+        self.check(self.lib.afg_event_record(self.ptr, slot), "afg_event_record")
+
+    def event_elapsed(self, a, b) -> float:
+        ms = C.c_float(0)
+        self.check(self.lib.afg_event_elapsed(self.ptr, a, b, C.byref(ms)), "afg_event_elapsed")
+        return ms.value
+
+    def flush_l2(self, nbytes=256 << 20):
+        self.check(self.lib.afg_flush_l2(self.ptr, nbytes), "afg_flush_l2")
+
+    def kernel_timing(self, cls):
+        self.check(self.lib.afg_kernel_timing(self.ptr, cls), "afg_kernel_timing")
+
+    def kernel_stats(self):
+        n = C.c_longlong(0)
+        ms = C.c_double(0)
+        by = C.c_double(0)
+        self.check(self.lib.afg_kernel_stats(self.ptr, C.byref(n), C.byref(ms), C.byref(by)), "afg_kernel_stats")
+        return n.value, ms.value, by.value
 
     def sync(self):
         self.check(self.lib.afg_sync(self.ptr), "afg_sync")

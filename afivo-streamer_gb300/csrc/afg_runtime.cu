@@ -91,6 +91,15 @@ struct afg_ctx {
   MgSlot mg[kMaxMg];
   // transport state (afg_transport.cuh)
   TransportState tr;
+  // accounting and timing
+  long long ctr[4] = {0, 0, 0, 0};
+  cudaEvent_t ev[64] = {};
+  void* flush_buf = nullptr;
+  size_t flush_bytes = 0;
+  int kt_class = 0;
+  std::vector<cudaEvent_t> kt_ev;  // start/stop pairs
+  size_t kt_used = 0;
+  double kt_bytes = 0;
 };
 
 /* ------------------------------------------------------------------------- */
@@ -153,6 +162,27 @@ static KTree ktree(const afg_ctx* c) {
 
 static const int* lst(const afg_ctx* c, size_t off) { return c->d_lists + off; }
 
+// Per-launch timing of one kernel class (afg_kernel_timing): events around
+// each launch of the selected class, algorithmic bytes summed on the host.
+static void kt_begin(afg_ctx* c, int cls) {
+  if (c->kt_class != cls || cls == AFG_KT_NONE) return;
+  if (c->kt_used + 2 > c->kt_ev.size()) {
+    if (c->kt_ev.size() >= 40000) return;
+    const size_t old = c->kt_ev.size();
+    c->kt_ev.resize(old + 2048);
+    for (size_t q = old; q < c->kt_ev.size(); q++) cudaEventCreate(&c->kt_ev[q]);
+  }
+  cudaEventRecord(c->kt_ev[c->kt_used], c->stream);
+}
+static void kt_end(afg_ctx* c, int cls, double bytes) {
+  if (c->kt_class != cls || cls == AFG_KT_NONE) return;
+  if (c->kt_used + 2 > c->kt_ev.size()) return;
+  cudaEventRecord(c->kt_ev[c->kt_used + 1], c->stream);
+  c->kt_used += 2;
+  c->kt_bytes += bytes;
+}
+static double box_cells(const afg_ctx* c) { return c->D == 2 ? (double)c->nc * c->nc : (double)c->nc * c->nc * c->nc; }
+
 static void free_tree(afg_ctx* c) {
   dfree(c->d_parent); dfree(c->d_children); dfree(c->d_nbr); dfree(c->d_pnb); dfree(c->d_nbmat);
   dfree(c->d_ix); dfree(c->d_rmin); dfree(c->d_dr); dfree(c->d_lists); dfree(c->d_is_leaf);
@@ -180,10 +210,12 @@ template <typename T>
 static int launch_gc(afg_ctx* ctx, const int* list, int n, T* v, const GcDev& g, int corners) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
+  kt_begin(ctx, AFG_KT_GHOST);
   if (ctx->D == 2)
     k_gc<2, T><<<n, 128, 0, ctx->stream>>>(t, list, v, g, corners);
   else
     k_gc<3, T><<<n, 256, 0, ctx->stream>>>(t, list, v, g, corners);
+  kt_end(ctx, AFG_KT_GHOST, 2.0 * sizeof(T) * n * 2 * ctx->D * (box_cells(ctx) / ctx->nc));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -194,12 +226,15 @@ static int launch_gsrb(afg_ctx* ctx, const int* list, int n, T* phi, const T* rh
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   const int threads = ctx->D == 2 ? std::min(256, ctx->nc * ctx->nc / 2) : std::min(256, ctx->nc * ctx->nc * ctx->nc / 2);
+  kt_begin(ctx, AFG_KT_GSRB);
   if (ctx->D == 3)
     k_gsrb<3, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam);
   else if (ctx->coord == AFG_CYL)
     k_gsrb<2, true, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam);
   else
     k_gsrb<2, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam);
+  // half sweep: 1.5 words per cell (read phi and rhs, write phi over two half sweeps)
+  kt_end(ctx, AFG_KT_GSRB, 1.5 * sizeof(T) * n * box_cells(ctx));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -342,6 +377,7 @@ static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, T* ph
   const int n_cycle = type == AFG_CYCLE_DOWN ? m.d.n_cycle_down : m.d.n_cycle_up;
   const int* list = lst(ctx, ctx->off_ids[lvl - 1]);
   const int n = (int)ctx->lvl_ids[lvl - 1].size();
+  ctx->ctr[1] += (long long)n * (long long)box_cells(ctx) * n_cycle;
   for (int it = 1; it <= 2 * n_cycle; it++) {
     RC(launch_gsrb<T>(ctx, list, n, phi, rhs, it, m.d.helmholtz_lambda));
     const int corners = (type != AFG_CYCLE_DOWN && it == 2 * n_cycle) ? 1 : 0;
@@ -415,6 +451,7 @@ template <typename T>
 static int mg_vcycle(afg_ctx* ctx, MgSlot& m, int max_lvl, T* phi, T* rhs, T* tmp, bool set_residual,
                      bool homogeneous, unsigned long long* maxbits) {
   const GcDev g = mg_gc(m.d, homogeneous);
+  ctx->ctr[3]++;
   for (int lvl = max_lvl; lvl >= 2; lvl--) {
     RC(mg_gsrb_boxes<T>(ctx, m, lvl, AFG_CYCLE_DOWN, phi, rhs, g));
     RC(mg_update_coarse<T>(ctx, m, lvl, phi, rhs, tmp, g));
@@ -494,6 +531,10 @@ int afg_finalize(afg_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   free_tree(ctx);
+  for (auto& e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : ctx->kt_ev) cudaEventDestroy(e);
+  if (ctx->flush_buf) cudaFree(ctx->flush_buf);
   dfree(ctx->d_max);
   if (ctx->h_max) cudaFreeHost(ctx->h_max);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1065,6 +1106,74 @@ int afg_mg_solve(afg_ctx* ctx, int mg_id, double threshold, int max_cycles, int*
   }
   if (n_done) *n_done = n;
   return r < threshold ? AFG_OK : AFG_ERR_NOCONV;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int afg_tree_copy_cc(afg_ctx* ctx, int iv_from, int iv_to) {
+  RC(check_var(ctx, iv_from));
+  RC(check_var(ctx, iv_to));
+  return launch_copy<double>(ctx, lst(ctx, ctx->off_all), ctx->n_all, ctx->cc[iv_from - 1], ctx->cc[iv_to - 1]);
+}
+
+int afg_counters(const afg_ctx* ctx, long long* out) {
+  if (!ctx || !out) return AFG_ERR_ARG;
+  out[0] = ctx->launches;
+  for (int q = 1; q < 4; q++) out[q] = ctx->ctr[q];
+  return AFG_OK;
+}
+
+int afg_event_record(afg_ctx* ctx, int slot) {
+  if (!ctx || slot < 0 || slot >= 64) return AFG_ERR_ARG;
+  if (!ctx->ev[slot]) CK(cudaEventCreate(&ctx->ev[slot]));
+  CK(cudaEventRecord(ctx->ev[slot], ctx->stream));
+  return AFG_OK;
+}
+
+int afg_event_elapsed(afg_ctx* ctx, int a, int b, float* ms) {
+  if (!ctx || a < 0 || b < 0 || a >= 64 || b >= 64 || !ms || !ctx->ev[a] || !ctx->ev[b]) return AFG_ERR_ARG;
+  CK(cudaEventSynchronize(ctx->ev[b]));
+  CK(cudaEventElapsedTime(ms, ctx->ev[a], ctx->ev[b]));
+  return AFG_OK;
+}
+
+int afg_flush_l2(afg_ctx* ctx, long long bytes) {
+  if (!ctx || bytes <= 0) return AFG_ERR_ARG;
+  if ((size_t)bytes > ctx->flush_bytes) {
+    if (ctx->flush_buf) cudaFree(ctx->flush_buf);
+    ctx->flush_buf = nullptr;
+    CK(cudaMalloc(&ctx->flush_buf, (size_t)bytes));
+    ctx->flush_bytes = (size_t)bytes;
+  }
+  CK(cudaMemsetAsync(ctx->flush_buf, (int)(ctx->launches & 0xff), (size_t)bytes, ctx->stream));
+  return AFG_OK;
+}
+
+int afg_kernel_timing(afg_ctx* ctx, int cls) {
+  if (!ctx || cls < 0 || cls > AFG_KT_RESIDUAL) return AFG_ERR_ARG;
+  ctx->kt_class = cls;
+  ctx->kt_used = 0;
+  ctx->kt_bytes = 0;
+  return AFG_OK;
+}
+
+int afg_kernel_stats(afg_ctx* ctx, long long* launches, double* ms, double* bytes) {
+  if (!ctx) return AFG_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  double tot = 0;
+  for (size_t q = 0; q + 1 < ctx->kt_used; q += 2) {
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, ctx->kt_ev[q], ctx->kt_ev[q + 1]));
+    tot += t;
+  }
+  if (launches) *launches = (long long)(ctx->kt_used / 2);
+  if (ms) *ms = tot;
+  if (bytes) *bytes = ctx->kt_bytes;
+  ctx->kt_used = 0;
+  ctx->kt_bytes = 0;
+  return AFG_OK;
 }
 
 }  // extern "C"

@@ -173,6 +173,7 @@ int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim) {
     const int n = (int)ctx->lvl_leaves[l].size();
     if (n == 0) continue;
     const int* list = lst(ctx, ctx->off_leaves[l]);
+    kt_begin(ctx, AFG_KT_FLUX);
     if (ctx->D == 3) {
       CK(cudaFuncSetAttribute(k_flux<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       k_flux<3, false><<<n, 256, smem, ctx->stream>>>(t, list, a);
@@ -183,6 +184,8 @@ int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim) {
       CK(cudaFuncSetAttribute(k_flux<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       k_flux<2, false><<<n, 256, smem, ctx->stream>>>(t, list, a);
     }
+    // per leaf cell: read n (flux species), |E|, E on D faces; write D fluxes per species
+    kt_end(ctx, AFG_KT_FLUX, 8.0 * n * box_cells(ctx) * ((d.n_flux + 1 + ctx->D) + ctx->D * d.n_flux));
     ctx->launches++;
     CKL();
   }
@@ -252,13 +255,18 @@ int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev, const
   KTree t = ktree(ctx);
   const int n = ctx->n_all_leaves;
   const int* list = lst(ctx, ctx->off_all_leaves);
+  ctx->ctr[2] += (long long)n * (long long)box_cells(ctx) * d.n_species;
   if (n > 0) {
+    kt_begin(ctx, AFG_KT_UPDATE);
     if (ctx->D == 3)
       k_update<3, false><<<n, 128, 0, ctx->stream>>>(t, list, a);
     else if (ctx->coord == AFG_CYL)
       k_update<2, true><<<n, 128, 0, ctx->stream>>>(t, list, a);
     else
       k_update<2, false><<<n, 128, 0, ctx->stream>>>(t, list, a);
+    // per leaf cell: read S*(n_prev+1) densities (+|E|, D*F fluxes, photo), write S densities
+    kt_end(ctx, AFG_KT_UPDATE, 8.0 * n * box_cells(ctx) *
+                                   (d.n_species * (n_prev + 1) + ctx->D * d.n_flux + 1 + (d.i_photo > 0) + d.n_species));
     ctx->launches++;
     CKL();
   }

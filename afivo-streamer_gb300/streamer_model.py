@@ -210,3 +210,75 @@ def baseline_alpha(E):
 
 def baseline_eta(E):
     return np.full_like(np.asarray(E, dtype=np.float64), 2e3)
+
+
+class StreamerRun:
+    """Time stepping of the hot path through the C-ABI, mirroring the
+    reference's time loop (src/streamer.f90:181-432): photoionization every
+    `photoi_per_steps` steps (photoi_set_src, 242-248), copy_current_state
+    (659-671), af_advance with Heun's method (afivo/src/m_af_advance.f90:
+    160-164) whose stages are forward_euler (src/m_fluid.f90:21-99), and
+    field_compute for the new state (327).  Step rejection is not needed at a
+    fixed dt below the limits and is left to the caller."""
+
+    def __init__(self, ctx, tree, model, voltage, dt, precision=ag.FP64, max_rel_residual=1e-8,
+                 num_vcycles=30, photoi=None, photoi_per_steps=5):
+        self.ctx, self.tree, self.m = ctx, tree, model
+        self.voltage, self.dt = voltage, dt
+        self.precision = precision
+        self.rel = max_rel_residual
+        self.num_vcycles = num_vcycles
+        self.photoi = photoi          # (lambdas 1/m, coeffs 1/m^2, eta*quench)
+        self.photoi_per_steps = photoi_per_steps
+        self.it = 0
+        self.L = float(tree.dr[0, -1] * tree.coarse_grid_size[-1])
+        self.last = {}
+
+    def setup(self):
+        ctx, m = self.ctx, self.m
+        D = self.tree.ndim
+        ctx.transport_setup(m.transport_desc())
+        ctx.set_cc_methods(m.i_electric_fld, *m.electric_fld_gc())
+        for s in range(len(m.species)):
+            for st in range(m.n_states):
+                ctx.set_cc_methods(m.species_iv[s] + st, [m.bc_species] * (2 * D), None, ag.RB_INTERP_LIM)
+        if m.i_photo:
+            ctx.set_cc_methods(m.i_photo, *m.photo_gc())
+        ctx.mg_setup(0, m.field_mg(self.voltage, self.precision))
+        self.mode_ids = []
+        if self.photoi is not None:
+            lam, coeffs, _ = self.photoi
+            for n, d in enumerate(m.helmholtz_mg(lam, self.precision)):
+                ctx.mg_setup(1 + n, d)
+                self.mode_ids.append(1 + n)
+
+    def field(self, s_in, have_guess):
+        n, r = self.ctx.field_compute(0, s_in, have_guess, self.voltage, self.L, self.rel, self.num_vcycles)
+        self.last.setdefault("vcycles", 0)
+        self.last["vcycles"] += n
+        return n, r
+
+    def initial_field(self):
+        self.ctx.gc(self.m.i_phi, 0, True)
+        return self.field(0, False)
+
+    def step(self):
+        ctx, m, dt = self.ctx, self.m, self.dt
+        self.last = {"vcycles": 0}
+        if self.photoi is not None and self.it % self.photoi_per_steps == 0:
+            lam, coeffs, coeff = self.photoi
+            ctx.photoi_helmh(coeff, self.mode_ids, coeffs, 1e-2, 10)
+        # copy_current_state: densities to the backup copy
+        for s in range(len(m.species)):
+            ctx.tree_copy_cc(m.species_iv[s], m.species_iv[s] + m.n_states - 1)
+        # Heun stage 1: forward_euler(dt, s_deriv=0, s_prev=[0], w=[1], s_out=1)
+        lim1 = ctx.flux_upwind(0)
+        ctx.update_densities(dt, 0, [0], [1.0], 1, last_step=False)
+        # stage 2: field for state 1, then forward_euler(dt/2, 1, [0,1], [.5,.5], 0)
+        self.field(1, True)
+        lim2 = ctx.flux_upwind(1)
+        chem = ctx.update_densities(0.5 * dt, 1, [0, 1], [0.5, 0.5], 0, last_step=True)
+        # field of the new state
+        n, r = self.field(0, True)
+        self.last.update(cfl=min(lim1[0], lim2[0]), drt=min(lim1[1], lim2[1]), chem=chem, residual=r)
+        self.it += 1

@@ -322,6 +322,41 @@ int afg_photoi_helmh(afg_ctx* ctx, double coeff, int n_modes, const int* mg_ids,
                      const double* coeffs, double max_rel_residual,
                      int max_fmg_cycles);
 
+/* af_tree_copy_cc (afivo/src/m_af_utils.f90:590-598): whole-array copy of
+ * variable iv_from to iv_to on all boxes (used by copy_current_state,
+ * src/streamer.f90:659-671). */
+int afg_tree_copy_cc(afg_ctx* ctx, int iv_from, int iv_to);
+
+/* ---- accounting and timing (no counterpart in the reference, which keeps
+ * wall-clock accumulators wc_time_* in src/m_streamer.f90:184-190) -------- */
+
+/* out[0] kernel launches, out[1] smoother cell-updates (one GS relaxation of
+ * one cell), out[2] transport cell-updates (leaf cells x species x stages),
+ * out[3] V-cycles performed. */
+int afg_counters(const afg_ctx* ctx, long long* out);
+
+/* Record CUDA event `slot` (0..63) on the context's stream; elapsed time in
+ * ms between two recorded events (synchronises on the second). */
+int afg_event_record(afg_ctx* ctx, int slot);
+int afg_event_elapsed(afg_ctx* ctx, int slot_a, int slot_b, float* ms);
+
+/* Write `bytes` of scratch memory on the stream (evicts the L2 cache
+ * between timed steps). */
+int afg_flush_l2(afg_ctx* ctx, long long bytes);
+
+/* Per-launch timing of one kernel class (AFG_KT_*): when enabled, each launch
+ * of that class is bracketed by events; afg_kernel_stats returns the number
+ * of launches, their summed device time (ms) and their summed algorithmic
+ * bytes (interior cells only), then resets. */
+#define AFG_KT_NONE     0
+#define AFG_KT_GSRB     1  /* red-black half sweep                  */
+#define AFG_KT_GHOST    2  /* ghost-cell fill                       */
+#define AFG_KT_FLUX     3  /* Koren flux                            */
+#define AFG_KT_UPDATE   4  /* density + source update               */
+#define AFG_KT_RESIDUAL 5  /* residual / defect                     */
+int afg_kernel_timing(afg_ctx* ctx, int kernel_class);
+int afg_kernel_stats(afg_ctx* ctx, long long* launches, double* ms, double* bytes);
+
 /* Synchronise the context's stream and check the device error word. */
 int afg_sync(afg_ctx* ctx);
 
