@@ -8,6 +8,7 @@
 // bit for bit; the FP32 instantiation is the inner solver of the mixed path.
 #pragma once
 #include "afg_common.cuh"
+#include "afg_gc_kernels.cuh"
 
 namespace afg {
 
@@ -92,6 +93,62 @@ __global__ void __launch_bounds__(256) k_gsrb(KTree t, const int* __restrict__ l
       p[x] = (f[x] - c[1] * p[x - 1] - c[2] * p[x + 1] - c[3] * p[x - n2] - c[4] * p[x + n2] -
               c[5] * p[x - sk] - c[6] * p[x + sk]) *
              inv_c1;
+    }
+  }
+}
+
+// Red-black half sweep with the ghost-cell refresh fused in: a neighbour
+// outside the box is evaluated on the fly with the box's ghost rule
+// (face_ghost) instead of being read from the ghost layer.  Between half
+// sweeps the reference refreshes every ghost cell (gsrb_boxes,
+// m_af_multigrid.f90:666-684); the on-the-fly value is the value that refresh
+// stores, because each ghost read by a cell of colour c depends only on
+// cells of the other colour, on the coarse level, and on the updated cell
+// itself before its update.  One ghost fill after the last half sweep then
+// leaves memory exactly as the reference does.
+template <int D, bool CYL, typename T>
+__global__ void __launch_bounds__(256) k_gsrb_fused(KTree t, const int* __restrict__ list, T* __restrict__ phi,
+                                                    const T* __restrict__ rhs, int redblack, double lambda2,
+                                                    GcDev g) {
+  const int slot = list[blockIdx.x];
+  const int nc = t.nc, n2 = t.n2, hn = nc / 2;
+  double cd[7];
+  lpl_coeffs<D>(t, slot, lambda2, cd);
+  T c[7];
+  for (int q = 0; q < 7; q++) c[q] = T(cd[q]);
+  const T inv_c1 = T(1 / cd[0]);
+  T* p = phi + (size_t)slot * t.S;
+  const T* f = rhs + (size_t)slot * t.S;
+  const int count = D == 2 ? nc * hn : nc * nc * hn;
+  for (int w = threadIdx.x; w < count; w += blockDim.x) {
+    const int row = w / hn, col = w - row * hn;
+    if (D == 2) {
+      const int j = row + 1;
+      const int i = 2 - ((redblack ^ j) & 1) + 2 * col;
+      const int x = at2(n2, i, j);
+      const T pw = i == 1 ? face_ghost<D, T>(t, phi, slot, 0, j, 0, g) : p[x - 1];
+      const T pe = i == nc ? face_ghost<D, T>(t, phi, slot, 1, j, 0, g) : p[x + 1];
+      const T ps = j == 1 ? face_ghost<D, T>(t, phi, slot, 2, i, 0, g) : p[x - n2];
+      const T pn = j == nc ? face_ghost<D, T>(t, phi, slot, 3, i, 0, g) : p[x + n2];
+      if (CYL) {
+        double k1, k2, k3;
+        cyl_coeffs(t, slot, i, cd, k1, k2, k3);
+        const T inv1 = T(1 / k1);
+        p[x] = (f[x] - T(k2) * pw - T(k3) * pe - c[3] * ps - c[4] * pn) * inv1;
+      } else {
+        p[x] = (f[x] - c[1] * pw - c[2] * pe - c[3] * ps - c[4] * pn) * inv_c1;
+      }
+    } else {
+      const int j = row % nc + 1, k = row / nc + 1;
+      const int i = 2 - ((redblack ^ (k + j)) & 1) + 2 * col;
+      const int x = at3(n2, i, j, k), sk = n2 * n2;
+      const T pw = i == 1 ? face_ghost<D, T>(t, phi, slot, 0, j, k, g) : p[x - 1];
+      const T pe = i == nc ? face_ghost<D, T>(t, phi, slot, 1, j, k, g) : p[x + 1];
+      const T ps = j == 1 ? face_ghost<D, T>(t, phi, slot, 2, i, k, g) : p[x - n2];
+      const T pn = j == nc ? face_ghost<D, T>(t, phi, slot, 3, i, k, g) : p[x + n2];
+      const T pb = k == 1 ? face_ghost<D, T>(t, phi, slot, 4, i, j, g) : p[x - sk];
+      const T pf = k == nc ? face_ghost<D, T>(t, phi, slot, 5, i, j, g) : p[x + sk];
+      p[x] = (f[x] - c[1] * pw - c[2] * pe - c[3] * ps - c[4] * pn - c[5] * pb - c[6] * pf) * inv_c1;
     }
   }
 }

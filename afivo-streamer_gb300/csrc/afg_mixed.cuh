@@ -108,20 +108,29 @@ static int mixed_solve(afg_ctx* ctx, MgSlot& m, double threshold, int max_cycles
   double* rhs = ctx->cc[m.d.i_rhs - 1];
   double r = 0;
   int n = 0;
-  for (;;) {
+  const int mg_id = (int)(&m - ctx->mg);
+  // defect of the current phi
+  RC(run_graph(ctx, gkey("defect", mg_id), [&]() -> int {
     RC(mixed_prepare(ctx, m, phi));
     RC(reset_max(ctx, 2));
-    RC(launch_defect(ctx, m, phi, rhs, ctx->d_max + 2));
+    return launch_defect(ctx, m, phi, rhs, ctx->d_max + 2);
+  }));
+  RC(read_max(ctx, 2, &r));
+  while (n < max_cycles) {
+    // one iteration: FP32 V-cycle on the correction, update, new defect
+    RC(run_graph(ctx, gkey("mixed_iter", mg_id), [&]() -> int {
+      RC(mg_vcycle<float>(ctx, m, ctx->highest_lvl, m.e32, m.r32, m.t32, false, true, nullptr));
+      k_add_correction<<<ctx->n_all, 256, 0, ctx->stream>>>(ctx->S, lst(ctx, ctx->off_all), phi, m.e32);
+      ctx->launches++;
+      CKL();
+      RC(mixed_prepare(ctx, m, phi));
+      RC(reset_max(ctx, 2));
+      return launch_defect(ctx, m, phi, rhs, ctx->d_max + 2);
+    }));
     RC(read_max(ctx, 2, &r));
-    if (n > 0) {
-      if (residuals) residuals[n - 1] = r;
-      if (r < threshold || n >= max_cycles) break;
-    }
-    RC(mg_vcycle<float>(ctx, m, ctx->highest_lvl, m.e32, m.r32, m.t32, false, true, nullptr));
-    k_add_correction<<<ctx->n_all, 256, 0, ctx->stream>>>(ctx->S, lst(ctx, ctx->off_all), phi, m.e32);
-    ctx->launches++;
-    CKL();
+    if (residuals) residuals[n] = r;
     n++;
+    if (r < threshold) break;
   }
   if (n_done) *n_done = n;
   return r < threshold ? AFG_OK : AFG_ERR_NOCONV;

@@ -13,6 +13,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -100,6 +101,17 @@ struct afg_ctx {
   std::vector<cudaEvent_t> kt_ev;  // start/stop pairs
   size_t kt_used = 0;
   double kt_bytes = 0;
+  // CUDA graphs of fixed launch sequences (V-cycle iterations, transport
+  // stages), keyed by what determines the sequence; cleared whenever the
+  // tree, an operator or boundary values change
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0, ctr[4] = {0, 0, 0, 0};
+  };
+  std::map<std::string, Graph> graphs;
+  bool use_graphs = true;
+  bool fused_gsrb = true;
+  bool capturing = false;
 };
 
 /* ------------------------------------------------------------------------- */
@@ -183,7 +195,14 @@ static void kt_end(afg_ctx* c, int cls, double bytes) {
 }
 static double box_cells(const afg_ctx* c) { return c->D == 2 ? (double)c->nc * c->nc : (double)c->nc * c->nc * c->nc; }
 
+static void clear_graphs(afg_ctx* c) {
+  for (auto& kv : c->graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  c->graphs.clear();
+}
+
 static void free_tree(afg_ctx* c) {
+  clear_graphs(c);
   dfree(c->d_parent); dfree(c->d_children); dfree(c->d_nbr); dfree(c->d_pnb); dfree(c->d_nbmat);
   dfree(c->d_ix); dfree(c->d_rmin); dfree(c->d_dr); dfree(c->d_lists); dfree(c->d_is_leaf);
   dfree(c->d_cslot); dfree(c->d_ccell);
@@ -234,6 +253,25 @@ static int launch_gsrb(afg_ctx* ctx, const int* list, int n, T* phi, const T* rh
   else
     k_gsrb<2, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam);
   // half sweep: 1.5 words per cell (read phi and rhs, write phi over two half sweeps)
+  kt_end(ctx, AFG_KT_GSRB, 1.5 * sizeof(T) * n * box_cells(ctx));
+  ctx->launches++;
+  CKL();
+  return AFG_OK;
+}
+
+template <typename T>
+static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, int rb, double lam,
+                             const GcDev& g) {
+  if (n <= 0) return AFG_OK;
+  KTree t = ktree(ctx);
+  const int threads = ctx->D == 2 ? std::min(256, ctx->nc * ctx->nc / 2) : std::min(256, ctx->nc * ctx->nc * ctx->nc / 2);
+  kt_begin(ctx, AFG_KT_GSRB);
+  if (ctx->D == 3)
+    k_gsrb_fused<3, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
+  else if (ctx->coord == AFG_CYL)
+    k_gsrb_fused<2, true, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
+  else
+    k_gsrb_fused<2, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
   kt_end(ctx, AFG_KT_GSRB, 1.5 * sizeof(T) * n * box_cells(ctx));
   ctx->launches++;
   CKL();
@@ -347,6 +385,51 @@ static int launch_maxabs(afg_ctx* ctx, const int* list, int n, const T* v, unsig
     if (rc_ != AFG_OK) return rc_; \
   } while (0)
 
+// Run a fixed launch sequence through a cached CUDA graph: captured on first
+// use, replayed afterwards (one launch instead of hundreds).  The body must
+// not synchronise.  Per-launch kernel timing bypasses the graphs.
+template <typename F>
+static int run_graph(afg_ctx* ctx, const std::string& key, F&& body) {
+  if (!ctx->use_graphs || ctx->kt_class != AFG_KT_NONE || ctx->capturing) return body();
+  auto it = ctx->graphs.find(key);
+  if (it == ctx->graphs.end()) {
+    const long long l0 = ctx->launches;
+    long long c0[4];
+    for (int q = 0; q < 4; q++) c0[q] = ctx->ctr[q];
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    ctx->capturing = true;
+    const int rc = body();
+    ctx->capturing = false;
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc != AFG_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ec != cudaSuccess) return fail(ctx, AFG_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ec));
+    afg_ctx::Graph gr;
+    const cudaError_t ei = cudaGraphInstantiate(&gr.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return fail(ctx, AFG_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ei));
+    gr.launches = ctx->launches - l0;
+    for (int q = 0; q < 4; q++) gr.ctr[q] = ctx->ctr[q] - c0[q];
+    // the capture did not execute anything: undo the accounting, then replay
+    ctx->launches = l0;
+    for (int q = 0; q < 4; q++) ctx->ctr[q] = c0[q];
+    it = ctx->graphs.emplace(key, gr).first;
+  }
+  CK(cudaGraphLaunch(it->second.exec, ctx->stream));
+  ctx->launches += it->second.launches;
+  for (int q = 0; q < 4; q++) ctx->ctr[q] += it->second.ctr[q];
+  return AFG_OK;
+}
+
+static std::string gkey(const char* tag, int a = 0, int b = 0, int c = 0, int d = 0) {
+  char buf[96];
+  snprintf(buf, sizeof(buf), "%s:%d:%d:%d:%d", tag, a, b, c, d);
+  return buf;
+}
+
 /* ------------------------------------------------------------------------- */
 // Multigrid drivers (templated on the working precision T)
 
@@ -378,6 +461,10 @@ static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, T* ph
   const int* list = lst(ctx, ctx->off_ids[lvl - 1]);
   const int n = (int)ctx->lvl_ids[lvl - 1].size();
   ctx->ctr[1] += (long long)n * (long long)box_cells(ctx) * n_cycle;
+  if (ctx->fused_gsrb) {
+    for (int it = 1; it <= 2 * n_cycle; it++) RC(launch_gsrb_fused<T>(ctx, list, n, phi, rhs, it, m.d.helmholtz_lambda, g));
+    return launch_gc<T>(ctx, list, n, phi, g, type != AFG_CYCLE_DOWN ? 1 : 0);
+  }
   for (int it = 1; it <= 2 * n_cycle; it++) {
     RC(launch_gsrb<T>(ctx, list, n, phi, rhs, it, m.d.helmholtz_lambda));
     const int corners = (type != AFG_CYCLE_DOWN && it == 2 * n_cycle) ? 1 : 0;
@@ -797,6 +884,7 @@ int afg_fc_download(afg_ctx* ctx, int ivf, double* const* box_fc, long long off)
 int afg_set_cc_methods(afg_ctx* ctx, int iv, const afg_gc_desc* gc) {
   RC(check_var(ctx, iv));
   if (!gc || gc->rb < 0 || gc->rb > 2) return fail(ctx, AFG_ERR_ARG, "bad ghost-cell method");
+  clear_graphs(ctx);
   GcDev g;
   for (int n = 0; n < 6; n++) {
     g.bc_type[n] = gc->bc_type[n];
@@ -982,6 +1070,7 @@ int afg_mg_setup(afg_ctx* ctx, int mg_id, const afg_mg_desc* d) {
   for (int n = 0; n < 2 * ctx->D; n++)
     if (d->bc_type[n] != AFG_BC_DIRICHLET && d->bc_type[n] != AFG_BC_NEUMANN)
       return fail(ctx, AFG_ERR_UNSUPPORTED, "multigrid needs Dirichlet or Neumann sides");
+  clear_graphs(ctx);
   MgSlot& m = ctx->mg[mg_id];
   dfree(m.d_ainv); dfree(m.d_b); dfree(m.d_x); dfree(m.d_b2r); dfree(m.d_bmask); dfree(m.d_bcval);
   dfree(m.e32); dfree(m.r32); dfree(m.t32);
@@ -1008,6 +1097,10 @@ int afg_mg_set_bc_values(afg_ctx* ctx, int mg_id, const double* v) {
   MgSlot* m;
   RC(get_mg(ctx, mg_id, &m));
   if (!v) return AFG_ERR_ARG;
+  bool same = true;
+  for (int q = 0; q < 6; q++) same = same && m->d.bc_val[q] == v[q];
+  if (same) return AFG_OK;
+  clear_graphs(ctx);  // boundary values are kernel parameters of captured graphs
   for (int q = 0; q < 6; q++) m->d.bc_val[q] = v[q];
   double bcv[12];
   for (int q = 0; q < 6; q++) {
@@ -1072,8 +1165,10 @@ int afg_mg_vcycle(afg_ctx* ctx, int mg_id, int set_residual, int max_lvl, double
   RC(get_mg(ctx, mg_id, &m));
   MG_VARS(m);
   const int ml = max_lvl <= 0 ? ctx->highest_lvl : std::min(max_lvl, ctx->highest_lvl);
-  RC(reset_max(ctx, 1));
-  RC(mg_vcycle<double>(ctx, *m, ml, phi, rhs, tmp, set_residual != 0, false, ctx->d_max + 1));
+  RC(run_graph(ctx, gkey("vcycle", mg_id, ml, set_residual != 0), [&]() -> int {
+    RC(reset_max(ctx, 1));
+    return mg_vcycle<double>(ctx, *m, ml, phi, rhs, tmp, set_residual != 0, false, ctx->d_max + 1);
+  }));
   if (set_residual && max_res) return read_max(ctx, 1, max_res);
   return AFG_OK;
 }
@@ -1082,8 +1177,10 @@ int afg_mg_fmg(afg_ctx* ctx, int mg_id, int set_residual, int have_guess, double
   MgSlot* m;
   RC(get_mg(ctx, mg_id, &m));
   MG_VARS(m);
-  RC(reset_max(ctx, 1));
-  RC(mg_fmg<double>(ctx, *m, phi, rhs, tmp, set_residual != 0, have_guess != 0, ctx->d_max + 1));
+  RC(run_graph(ctx, gkey("fmg", mg_id, set_residual != 0, have_guess != 0), [&]() -> int {
+    RC(reset_max(ctx, 1));
+    return mg_fmg<double>(ctx, *m, phi, rhs, tmp, set_residual != 0, have_guess != 0, ctx->d_max + 1);
+  }));
   if (set_residual && max_res) return read_max(ctx, 1, max_res);
   return AFG_OK;
 }
@@ -1097,8 +1194,10 @@ int afg_mg_solve(afg_ctx* ctx, int mg_id, double threshold, int max_cycles, int*
   int n = 0;
   double r = 0;
   for (n = 0; n < max_cycles;) {
-    RC(reset_max(ctx, 1));
-    RC(mg_vcycle<double>(ctx, *m, ctx->highest_lvl, phi, rhs, tmp, true, false, ctx->d_max + 1));
+    RC(run_graph(ctx, gkey("vcycle", mg_id, ctx->highest_lvl, 1), [&]() -> int {
+      RC(reset_max(ctx, 1));
+      return mg_vcycle<double>(ctx, *m, ctx->highest_lvl, phi, rhs, tmp, true, false, ctx->d_max + 1);
+    }));
     RC(read_max(ctx, 1, &r));
     if (residuals) residuals[n] = r;
     n++;

@@ -69,6 +69,7 @@ int afg_transport_setup(afg_ctx* ctx, const afg_transport_desc* d) {
     for (int q = 0; q < rc.n_out; q++)
       if (rc.ix_out[q] < 0 || rc.ix_out[q] >= t.n_species) return fail(ctx, AFG_ERR_ARG, "bad reaction species");
   }
+  clear_graphs(ctx);
   TransportState& s = ctx->tr;
   transport_free(s);
   s.d = t;
@@ -109,7 +110,17 @@ int afg_transport_setup(afg_ctx* ctx, const afg_transport_desc* d) {
   CK(dalloc(&s.d_cflux, cflux.size()));
   if (!rrb.empty()) CK(cudaMemcpy(s.d_rrb, rrb.data(), sizeof(int) * rrb.size(), cudaMemcpyHostToDevice));
   if (!cflux.empty()) CK(cudaMemcpy(s.d_cflux, cflux.data(), sizeof(int) * cflux.size(), cudaMemcpyHostToDevice));
-  // ghost-cell methods of the densities (all states) and of |E|
+  // dynamic shared memory of the flux kernel (set outside graph capture)
+  {
+    const int nc = ctx->nc, m = nc + 4;
+    const int tile = D == 2 ? m * m : m * m * m;
+    const int nfaces = D == 2 ? nc * (nc + 1) : nc * nc * (nc + 1);
+    const size_t smem = sizeof(double) * ((size_t)t.n_flux * tile + 2 * (size_t)D * nfaces);
+    if (smem > 200 * 1024) return fail(ctx, AFG_ERR_UNSUPPORTED, "box too large for the flux kernel");
+    CK(cudaFuncSetAttribute(k_flux<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_flux<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_flux<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
   s.ready = true;
   return AFG_OK;
 }
@@ -144,61 +155,61 @@ int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim) {
     const int iv = d.species_iv[d.flux_species[f]] + s_deriv;
     if (iv < 1 || iv > ctx->n_var) return fail(ctx, AFG_ERR_ARG, "bad state s_deriv");
   }
-  KTree t = ktree(ctx);
-  const bool cyl = ctx->coord == AFG_CYL;
-  // af_restrict_ref_boundary
-  if (ctx->tr.n_rrb > 0) {
-    for (int f = 0; f < d.n_flux; f++) {
-      double* v = ctx->cc[d.species_iv[d.flux_species[f]] + s_deriv - 1];
-      if (ctx->D == 3)
-        k_restrict_geom<3, false><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v);
-      else if (cyl)
-        k_restrict_geom<2, true><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v);
-      else
-        k_restrict_geom<2, false><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v);
+  RC(run_graph(ctx, gkey("flux", s_deriv), [&]() -> int {
+    KTree t = ktree(ctx);
+    const bool cyl = ctx->coord == AFG_CYL;
+    // af_restrict_ref_boundary
+    if (ctx->tr.n_rrb > 0) {
+      for (int f = 0; f < d.n_flux; f++) {
+        double* v = ctx->cc[d.species_iv[d.flux_species[f]] + s_deriv - 1];
+        if (ctx->D == 3)
+          k_restrict_geom<3, false><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v);
+        else if (cyl)
+          k_restrict_geom<2, true><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v);
+        else
+          k_restrict_geom<2, false><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v);
+        ctx->launches++;
+        CKL();
+      }
+    }
+    CK(cudaMemsetAsync(ctx->d_max + 3, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    FluxArgs a = flux_args(ctx, s_deriv);
+    const int nc = ctx->nc, m = nc + 4;
+    const int tile = ctx->D == 2 ? m * m : m * m * m;
+    const int nfaces = ctx->D == 2 ? nc * (nc + 1) : nc * nc * (nc + 1);
+    const size_t smem = sizeof(double) * ((size_t)d.n_flux * tile + 2 * (size_t)ctx->D * nfaces);
+    if (smem > 200 * 1024) return fail(ctx, AFG_ERR_UNSUPPORTED, "box too large for the flux kernel");
+    // leaves level by level: refinement-boundary ghosts read the coarse
+    // neighbour's ghost layer written by the previous level
+    for (int l = 0; l < ctx->highest_lvl; l++) {
+      const int n = (int)ctx->lvl_leaves[l].size();
+      if (n == 0) continue;
+      const int* list = lst(ctx, ctx->off_leaves[l]);
+      kt_begin(ctx, AFG_KT_FLUX);
+      if (ctx->D == 3) {
+        k_flux<3, false><<<n, 256, smem, ctx->stream>>>(t, list, a);
+      } else if (cyl) {
+        k_flux<2, true><<<n, 256, smem, ctx->stream>>>(t, list, a);
+      } else {
+        k_flux<2, false><<<n, 256, smem, ctx->stream>>>(t, list, a);
+      }
+      // per leaf cell: read n (flux species), |E|, E on D faces; write D fluxes per species
+      kt_end(ctx, AFG_KT_FLUX, 8.0 * n * box_cells(ctx) * ((d.n_flux + 1 + ctx->D) + ctx->D * d.n_flux));
       ctx->launches++;
       CKL();
     }
-  }
-  CK(cudaMemsetAsync(ctx->d_max + 3, 0, 2 * sizeof(unsigned long long), ctx->stream));
-  FluxArgs a = flux_args(ctx, s_deriv);
-  const int nc = ctx->nc, m = nc + 4;
-  const int tile = ctx->D == 2 ? m * m : m * m * m;
-  const int nfaces = ctx->D == 2 ? nc * (nc + 1) : nc * nc * (nc + 1);
-  const size_t smem = sizeof(double) * ((size_t)d.n_flux * tile + 2 * (size_t)ctx->D * nfaces);
-  if (smem > 200 * 1024) return fail(ctx, AFG_ERR_UNSUPPORTED, "box too large for the flux kernel");
-  // leaves level by level: refinement-boundary ghosts read the coarse
-  // neighbour's ghost layer written by the previous level
-  for (int l = 0; l < ctx->highest_lvl; l++) {
-    const int n = (int)ctx->lvl_leaves[l].size();
-    if (n == 0) continue;
-    const int* list = lst(ctx, ctx->off_leaves[l]);
-    kt_begin(ctx, AFG_KT_FLUX);
-    if (ctx->D == 3) {
-      CK(cudaFuncSetAttribute(k_flux<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      k_flux<3, false><<<n, 256, smem, ctx->stream>>>(t, list, a);
-    } else if (cyl) {
-      CK(cudaFuncSetAttribute(k_flux<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      k_flux<2, true><<<n, 256, smem, ctx->stream>>>(t, list, a);
-    } else {
-      CK(cudaFuncSetAttribute(k_flux<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      k_flux<2, false><<<n, 256, smem, ctx->stream>>>(t, list, a);
+    if (ctx->tr.n_cflux > 0) {
+      if (ctx->D == 3)
+        k_consistent_flux<3, false><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a);
+      else if (cyl)
+        k_consistent_flux<2, true><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a);
+      else
+        k_consistent_flux<2, false><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a);
+      ctx->launches++;
+      CKL();
     }
-    // per leaf cell: read n (flux species), |E|, E on D faces; write D fluxes per species
-    kt_end(ctx, AFG_KT_FLUX, 8.0 * n * box_cells(ctx) * ((d.n_flux + 1 + ctx->D) + ctx->D * d.n_flux));
-    ctx->launches++;
-    CKL();
-  }
-  if (ctx->tr.n_cflux > 0) {
-    if (ctx->D == 3)
-      k_consistent_flux<3, false><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a);
-    else if (cyl)
-      k_consistent_flux<2, true><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a);
-    else
-      k_consistent_flux<2, false><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a);
-    ctx->launches++;
-    CKL();
-  }
+    return AFG_OK;
+  }));
   if (dt_lim) {
     double mc, ms;
     RC(read_max(ctx, 3, &mc));
@@ -308,15 +319,17 @@ int afg_field_from_potential(afg_ctx* ctx, int i_phi) {
   KTree t = ktree(ctx);
   double* efc = ctx->fc[d.i_efield_fc - 1];
   double* en = ctx->cc[d.i_electric_fld - 1];
-  if (ctx->D == 3)
-    k_field_grad<3><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en);
-  else
-    k_field_grad<2><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en);
-  ctx->launches++;
-  CKL();
   if (!ctx->has_method[d.i_electric_fld - 1])
     return fail(ctx, AFG_ERR_STATE, "no ghost-cell methods for the electric field norm");
-  return afg_gc(ctx, d.i_electric_fld, 0, 1);
+  return run_graph(ctx, gkey("efield", i_phi), [&]() -> int {
+    if (ctx->D == 3)
+      k_field_grad<3><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en);
+    else
+      k_field_grad<2><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en);
+    ctx->launches++;
+    CKL();
+    return afg_gc(ctx, d.i_electric_fld, 0, 1);
+  });
 }
 
 int afg_field_compute(afg_ctx* ctx, int mg_id, int s_in, int have_guess, double voltage, double domain_len,
