@@ -28,6 +28,20 @@ struct KTree {
   const int* ix;        // [n][D]  box%ix (1-based)
   const double* r_min;  // [n][D]
   const double* dr;     // [n][D]
+  // cylindrical geometry per (box, radial index i=1..nc), 2D only:
+  // [n][nc][4] = flux factors (r -/+ dr/2)/r (af_cyl_flux_factors,
+  // m_af_types.f90:1199-1211) and child weights 1 -/+ dr/(4r)
+  // (af_cyl_child_weights, 1187-1196); null for Cartesian trees
+  const double* geo;
+};
+
+// Operator coefficients of one multigrid slot, precomputed per box:
+// cb[n][8] = c(1..2D+1) of mg_box_lpl_stencil and 1/c(1); for cylindrical
+// trees cy[n][nc][4] = corrected c(1), c(2), c(3) and 1/c(1) per radial index.
+template <typename T>
+struct MgCoef {
+  const T* cb;
+  const T* cy;
 };
 
 // Ghost-cell method of one variable (bc per domain face + refinement rule).

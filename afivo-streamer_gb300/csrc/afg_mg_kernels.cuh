@@ -61,14 +61,12 @@ __device__ __forceinline__ T apply_lpl(const T* __restrict__ p, int n2, int i, i
 // (m_af_stencil.f90:838-998).  Updated cells satisfy (i+j[+k]+n) even.
 template <int D, bool CYL, typename T>
 __global__ void __launch_bounds__(256) k_gsrb(KTree t, const int* __restrict__ list, T* __restrict__ phi,
-                                              const T* __restrict__ rhs, int redblack, double lambda2) {
+                                              const T* __restrict__ rhs, int redblack, MgCoef<T> mc) {
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2, hn = nc / 2;
-  double cd[7];
-  lpl_coeffs<D>(t, slot, lambda2, cd);
   T c[7];
-  for (int q = 0; q < 7; q++) c[q] = T(cd[q]);
-  const T inv_c1 = T(1 / cd[0]);
+  for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
+  const T inv_c1 = mc.cb[slot * 8 + 7];
   T* p = phi + (size_t)slot * t.S;
   const T* f = rhs + (size_t)slot * t.S;
   const int count = D == 2 ? nc * hn : nc * nc * hn;
@@ -79,10 +77,8 @@ __global__ void __launch_bounds__(256) k_gsrb(KTree t, const int* __restrict__ l
       const int i = 2 - ((redblack ^ j) & 1) + 2 * col;
       const int x = at2(n2, i, j);
       if (CYL) {
-        double k1, k2, k3;
-        cyl_coeffs(t, slot, i, cd, k1, k2, k3);
-        const T inv1 = T(1 / k1);
-        p[x] = (f[x] - T(k2) * p[x - 1] - T(k3) * p[x + 1] - c[3] * p[x - n2] - c[4] * p[x + n2]) * inv1;
+        const T* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
+        p[x] = (f[x] - y[1] * p[x - 1] - y[2] * p[x + 1] - c[3] * p[x - n2] - c[4] * p[x + n2]) * y[3];
       } else {
         p[x] = (f[x] - c[1] * p[x - 1] - c[2] * p[x + 1] - c[3] * p[x - n2] - c[4] * p[x + n2]) * inv_c1;
       }
@@ -108,15 +104,13 @@ __global__ void __launch_bounds__(256) k_gsrb(KTree t, const int* __restrict__ l
 // leaves memory exactly as the reference does.
 template <int D, bool CYL, typename T>
 __global__ void __launch_bounds__(256) k_gsrb_fused(KTree t, const int* __restrict__ list, T* __restrict__ phi,
-                                                    const T* __restrict__ rhs, int redblack, double lambda2,
+                                                    const T* __restrict__ rhs, int redblack, MgCoef<T> mc,
                                                     GcDev g) {
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2, hn = nc / 2;
-  double cd[7];
-  lpl_coeffs<D>(t, slot, lambda2, cd);
   T c[7];
-  for (int q = 0; q < 7; q++) c[q] = T(cd[q]);
-  const T inv_c1 = T(1 / cd[0]);
+  for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
+  const T inv_c1 = mc.cb[slot * 8 + 7];
   T* p = phi + (size_t)slot * t.S;
   const T* f = rhs + (size_t)slot * t.S;
   const int count = D == 2 ? nc * hn : nc * nc * hn;
@@ -131,10 +125,8 @@ __global__ void __launch_bounds__(256) k_gsrb_fused(KTree t, const int* __restri
       const T ps = j == 1 ? face_ghost<D, T>(t, phi, slot, 2, i, 0, g) : p[x - n2];
       const T pn = j == nc ? face_ghost<D, T>(t, phi, slot, 3, i, 0, g) : p[x + n2];
       if (CYL) {
-        double k1, k2, k3;
-        cyl_coeffs(t, slot, i, cd, k1, k2, k3);
-        const T inv1 = T(1 / k1);
-        p[x] = (f[x] - T(k2) * pw - T(k3) * pe - c[3] * ps - c[4] * pn) * inv1;
+        const T* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
+        p[x] = (f[x] - y[1] * pw - y[2] * pe - c[3] * ps - c[4] * pn) * y[3];
       } else {
         p[x] = (f[x] - c[1] * pw - c[2] * pe - c[3] * ps - c[4] * pn) * inv_c1;
       }
@@ -158,16 +150,14 @@ __global__ void __launch_bounds__(256) k_gsrb_fused(KTree t, const int* __restri
 // *maxbits (may be null).
 template <int D, bool CYL, typename T>
 __global__ void __launch_bounds__(256) k_residual(KTree t, const int* __restrict__ list, const T* __restrict__ phi,
-                                                  const T* __restrict__ rhs, T* __restrict__ tmp, double lambda2,
+                                                  const T* __restrict__ rhs, T* __restrict__ tmp, MgCoef<T> mc,
                                                   const unsigned char* __restrict__ is_leaf,
                                                   unsigned long long* maxbits) {
   __shared__ T sred[32];
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;
-  double cd[7];
-  lpl_coeffs<D>(t, slot, lambda2, cd);
   T c[7];
-  for (int q = 0; q < 7; q++) c[q] = T(cd[q]);
+  for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
   const T* p = phi + (size_t)slot * t.S;
   const T* f = rhs + (size_t)slot * t.S;
   T* o = tmp + (size_t)slot * t.S;
@@ -178,9 +168,8 @@ __global__ void __launch_bounds__(256) k_residual(KTree t, const int* __restrict
     const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
     T k1 = T(0), k2 = T(0), k3 = T(0);
     if (CYL) {
-      double a, b, e;
-      cyl_coeffs(t, slot, i, cd, a, b, e);
-      k1 = T(a); k2 = T(b); k3 = T(e);
+      const T* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
+      k1 = y[0]; k2 = y[1]; k3 = y[2];
     }
     const int x = D == 2 ? at2(n2, i, j) : at3(n2, i, j, k);
     const T res = f[x] - apply_lpl<D, CYL, T>(p, n2, i, j, k, c, k1, k2, k3);
@@ -202,15 +191,13 @@ __global__ void __launch_bounds__(256) k_residual(KTree t, const int* __restrict
 template <int D, bool CYL, typename T>
 __global__ void __launch_bounds__(256) k_residual_restrict(KTree t, const int* __restrict__ list,
                                                            T* __restrict__ phi, const T* __restrict__ rhs,
-                                                           T* __restrict__ tmp, double lambda2,
+                                                           T* __restrict__ tmp, MgCoef<T> mc,
                                                            int store_child_residual) {
   const int slot = list[blockIdx.x];
   const int pslot = t.parent[slot];
   const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
-  double cd[7];
-  lpl_coeffs<D>(t, slot, lambda2, cd);
   T c[7];
-  for (int q = 0; q < 7; q++) c[q] = T(cd[q]);
+  for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
   const T* p = phi + (size_t)slot * t.S;
   const T* f = rhs + (size_t)slot * t.S;
   T* pp = phi + (size_t)pslot * t.S;
@@ -230,9 +217,8 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t, const int* _
         for (int di = 0; di < 2; di++) {
           T k1 = T(0), k2 = T(0), k3 = T(0);
           if (CYL) {
-            double a, b, e;
-            cyl_coeffs(t, slot, fi + di, cd, a, b, e);
-            k1 = T(a); k2 = T(b); k3 = T(e);
+            const T* y = mc.cy + ((size_t)slot * nc + (fi + di - 1)) * 4;
+            k1 = y[0]; k2 = y[1]; k3 = y[2];
           }
           const int x = at2(n2, fi + di, fj + dj);
           res[dj][di] = f[x] - apply_lpl<D, CYL, T>(p, n2, fi + di, fj + dj, 0, c, k1, k2, k3);
@@ -240,9 +226,8 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t, const int* _
         }
       T rv;
       if (CYL) {
-        const double rp = t.r_min[pslot * 2] + (ic - 0.5) * t.dr[pslot * 2];
-        const double tw = 0.25 * t.dr[pslot * 2] / rp;
-        const T w1 = T(1 - tw), w2 = T(1 + tw);
+        const double* gw = t.geo + ((size_t)pslot * nc + (ic - 1)) * 4;
+        const T w1 = T(gw[2]), w2 = T(gw[3]);
         T s1 = T(0), s2 = T(0);
         s1 = s1 + res[0][0]; s1 = s1 + res[1][0];
         s2 = s2 + res[0][1]; s2 = s2 + res[1][1];
@@ -282,13 +267,11 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t, const int* _
 template <int D, bool CYL, typename T>
 __global__ void __launch_bounds__(256) k_coarse_fas(KTree t, const int* __restrict__ list,
                                                     const T* __restrict__ phi, T* __restrict__ rhs,
-                                                    T* __restrict__ tmp, double lambda2, int copy_tmp) {
+                                                    T* __restrict__ tmp, MgCoef<T> mc, int copy_tmp) {
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;
-  double cd[7];
-  lpl_coeffs<D>(t, slot, lambda2, cd);
   T c[7];
-  for (int q = 0; q < 7; q++) c[q] = T(cd[q]);
+  for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
   const T* p = phi + (size_t)slot * t.S;
   T* f = rhs + (size_t)slot * t.S;
   T* o = tmp + (size_t)slot * t.S;
@@ -299,9 +282,8 @@ __global__ void __launch_bounds__(256) k_coarse_fas(KTree t, const int* __restri
     if (interior) {
       T k1 = T(0), k2 = T(0), k3 = T(0);
       if (CYL) {
-        double a, b, e;
-        cyl_coeffs(t, slot, i, cd, a, b, e);
-        k1 = T(a); k2 = T(b); k3 = T(e);
+        const T* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
+        k1 = y[0]; k2 = y[1]; k3 = y[2];
       }
       const T lp = apply_lpl<D, CYL, T>(p, n2, i, j, k, c, k1, k2, k3);
       f[x] = lp + o[x];
@@ -380,9 +362,8 @@ __global__ void __launch_bounds__(256) k_init_phi_rhs(KTree t, const int* __rest
     if (D == 2) {
       T rv;
       if (CYL) {
-        const double rp = t.r_min[pslot * 2] + (ic - 0.5) * t.dr[pslot * 2];
-        const double tw = 0.25 * t.dr[pslot * 2] / rp;
-        const T w1 = T(1 - tw), w2 = T(1 + tw);
+        const double* gw = t.geo + ((size_t)pslot * nc + (ic - 1)) * 4;
+        const T w1 = T(gw[2]), w2 = T(gw[3]);
         T s1 = T(0), s2 = T(0);
         s1 = s1 + f[at2(n2, fi, fj)]; s1 = s1 + f[at2(n2, fi, fj + 1)];
         s2 = s2 + f[at2(n2, fi + 1, fj)]; s2 = s2 + f[at2(n2, fi + 1, fj + 1)];
@@ -470,6 +451,49 @@ __global__ void __launch_bounds__(256) k_maxabs(KTree t, const int* __restrict__
   }
   mx = block_max<T>(mx, sred);
   if (threadIdx.x == 0) atomic_max_nonneg(maxbits, double(mx));
+}
+
+
+// Coefficient tables (computed once per operator with the formulas of
+// lpl_coeffs / cyl_coeffs, so the values are those the reference computes).
+template <int D>
+__global__ void k_setup_coef(KTree t, int n, double lambda2, int cyl, double* cb64, float* cb32, double* cy64,
+                             float* cy32) {
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= n) return;
+  double cd[7];
+  lpl_coeffs<D>(t, slot, lambda2, cd);
+  for (int q = 0; q < 7; q++) {
+    cb64[slot * 8 + q] = q <= 2 * D ? cd[q] : 0.0;
+    cb32[slot * 8 + q] = q <= 2 * D ? float(cd[q]) : 0.0f;
+  }
+  cb64[slot * 8 + 7] = 1 / cd[0];
+  cb32[slot * 8 + 7] = float(1 / cd[0]);
+  if (cyl) {
+    for (int i = 1; i <= t.nc; i++) {
+      double k1, k2, k3;
+      cyl_coeffs(t, slot, i, cd, k1, k2, k3);
+      double* o = cy64 + ((size_t)slot * t.nc + (i - 1)) * 4;
+      float* o32 = cy32 + ((size_t)slot * t.nc + (i - 1)) * 4;
+      o[0] = k1; o[1] = k2; o[2] = k3; o[3] = 1 / k1;
+      o32[0] = float(k1); o32[1] = float(k2); o32[2] = float(k3); o32[3] = float(1 / k1);
+    }
+  }
+}
+
+__global__ void k_setup_geo(int n, int nc, const double* __restrict__ r_min, const double* __restrict__ dr,
+                            double* __restrict__ geo) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= n * nc) return;
+  const int slot = w / nc, i = w % nc + 1;
+  const double h = dr[slot * 2], r = r_min[slot * 2] + (i - 0.5) * h;
+  const double inv_r = 1 / r;
+  const double tw = 0.25 * h / r;
+  double* o = geo + (size_t)w * 4;
+  o[0] = (r - 0.5 * h) * inv_r;
+  o[1] = (r + 0.5 * h) * inv_r;
+  o[2] = 1 - tw;
+  o[3] = 1 + tw;
 }
 
 }  // namespace afg

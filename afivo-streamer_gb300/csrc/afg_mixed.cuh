@@ -19,14 +19,14 @@ namespace afg {
 template <int D, bool CYL>
 __global__ void __launch_bounds__(256) k_defect(KTree t, const int* __restrict__ list, const double* __restrict__ phi,
                                                 const double* __restrict__ rhs, float* __restrict__ r32,
-                                                float* __restrict__ e32, double lambda2,
+                                                float* __restrict__ e32, MgCoef<double> mc,
                                                 const unsigned char* __restrict__ is_leaf,
                                                 unsigned long long* maxbits) {
   __shared__ double sred[32];
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;
   double cd[7];
-  lpl_coeffs<D>(t, slot, lambda2, cd);
+  for (int q = 0; q < 7; q++) cd[q] = mc.cb[slot * 8 + q];
   const double* p = phi + (size_t)slot * t.S;
   const double* f = rhs + (size_t)slot * t.S;
   float* ro = r32 + (size_t)slot * t.S;
@@ -39,7 +39,10 @@ __global__ void __launch_bounds__(256) k_defect(KTree t, const int* __restrict__
     const bool interior = i >= 1 && i <= nc && j >= 1 && j <= nc && (D == 2 || (k >= 1 && k <= nc));
     if (!interior) continue;
     double k1 = 0, k2 = 0, k3 = 0;
-    if (CYL) cyl_coeffs(t, slot, i, cd, k1, k2, k3);
+    if (CYL) {
+      const double* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
+      k1 = y[0]; k2 = y[1]; k3 = y[2];
+    }
     const double res = f[x] - apply_lpl<D, CYL, double>(p, n2, i, j, k, cd, k1, k2, k3);
     ro[x] = float(res);
     const double ar = fabs(res);
@@ -68,14 +71,14 @@ static int launch_defect(afg_ctx* ctx, MgSlot& m, const double* phi, const doubl
   KTree t = ktree(ctx);
   const int* list = lst(ctx, ctx->off_all);
   if (ctx->D == 3)
-    k_defect<3, false><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, m.d.helmholtz_lambda,
-                                                   ctx->d_is_leaf, maxbits);
+    k_defect<3, false><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), ctx->d_is_leaf,
+                                                   maxbits);
   else if (ctx->coord == AFG_CYL)
-    k_defect<2, true><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, m.d.helmholtz_lambda,
-                                                  ctx->d_is_leaf, maxbits);
+    k_defect<2, true><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), ctx->d_is_leaf,
+                                                  maxbits);
   else
-    k_defect<2, false><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, m.d.helmholtz_lambda,
-                                                   ctx->d_is_leaf, maxbits);
+    k_defect<2, false><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), ctx->d_is_leaf,
+                                                   maxbits);
   ctx->launches++;
   CKL();
   return AFG_OK;

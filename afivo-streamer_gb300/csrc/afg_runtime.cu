@@ -45,6 +45,11 @@ struct MgSlot {
   double* d_b2r = nullptr;       // [n][2D]
   unsigned char* d_bmask = nullptr;
   double* d_bcval = nullptr;     // [6]
+  // coefficient tables (MgCoef): per box, and per radial index if cylindrical
+  double* d_cb64 = nullptr;
+  float* d_cb32 = nullptr;
+  double* d_cy64 = nullptr;
+  float* d_cy32 = nullptr;
   // FP32 inner-solver pools for AFG_MIXED (e, r, tmp)
   float* e32 = nullptr;
   float* r32 = nullptr;
@@ -69,6 +74,7 @@ struct afg_ctx {
   int *d_parent = nullptr, *d_children = nullptr, *d_nbr = nullptr, *d_pnb = nullptr, *d_nbmat = nullptr,
       *d_ix = nullptr;
   double *d_rmin = nullptr, *d_dr = nullptr;
+  double* d_geo = nullptr;  // cylindrical geometry table (KTree::geo)
   int* d_lists = nullptr;  // all level lists concatenated
   std::vector<size_t> off_ids, off_leaves, off_parents;  // per level offsets into d_lists
   size_t off_all = 0;       // list of all boxes, all levels (level order)
@@ -169,8 +175,21 @@ static KTree ktree(const afg_ctx* c) {
   t.ix = c->d_ix;
   t.r_min = c->d_rmin;
   t.dr = c->d_dr;
+  t.geo = c->d_geo;
   return t;
 }
+
+template <typename T>
+static MgCoef<T> coef_of(const MgSlot& m);
+template <>
+MgCoef<double> coef_of<double>(const MgSlot& m) {
+  return MgCoef<double>{m.d_cb64, m.d_cy64};
+}
+template <>
+MgCoef<float> coef_of<float>(const MgSlot& m) {
+  return MgCoef<float>{m.d_cb32, m.d_cy32};
+}
+static MgCoef<double> coef64(const MgSlot& m) { return coef_of<double>(m); }
 
 static const int* lst(const afg_ctx* c, size_t off) { return c->d_lists + off; }
 
@@ -204,7 +223,7 @@ static void clear_graphs(afg_ctx* c) {
 static void free_tree(afg_ctx* c) {
   clear_graphs(c);
   dfree(c->d_parent); dfree(c->d_children); dfree(c->d_nbr); dfree(c->d_pnb); dfree(c->d_nbmat);
-  dfree(c->d_ix); dfree(c->d_rmin); dfree(c->d_dr); dfree(c->d_lists); dfree(c->d_is_leaf);
+  dfree(c->d_ix); dfree(c->d_rmin); dfree(c->d_dr); dfree(c->d_lists); dfree(c->d_is_leaf); dfree(c->d_geo);
   dfree(c->d_cslot); dfree(c->d_ccell);
   for (auto& p : c->cc) dfree(p);
   for (auto& p : c->fc) dfree(p);
@@ -213,6 +232,7 @@ static void free_tree(afg_ctx* c) {
   for (auto& m : c->mg) {
     dfree(m.d_ainv); dfree(m.d_b); dfree(m.d_x); dfree(m.d_b2r); dfree(m.d_bmask); dfree(m.d_bcval);
     dfree(m.e32); dfree(m.r32); dfree(m.t32);
+    dfree(m.d_cb64); dfree(m.d_cb32); dfree(m.d_cy64); dfree(m.d_cy32);
     m.used = false;
   }
   transport_free(c->tr);
@@ -241,7 +261,7 @@ static int launch_gc(afg_ctx* ctx, const int* list, int n, T* v, const GcDev& g,
 }
 
 template <typename T>
-static int launch_gsrb(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, int rb, double lam) {
+static int launch_gsrb(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, int rb, MgCoef<T> lam) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   const int threads = ctx->D == 2 ? std::min(256, ctx->nc * ctx->nc / 2) : std::min(256, ctx->nc * ctx->nc * ctx->nc / 2);
@@ -260,7 +280,7 @@ static int launch_gsrb(afg_ctx* ctx, const int* list, int n, T* phi, const T* rh
 }
 
 template <typename T>
-static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, int rb, double lam,
+static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, int rb, MgCoef<T> lam,
                              const GcDev& g) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
@@ -279,7 +299,7 @@ static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, T* phi, const
 }
 
 template <typename T>
-static int launch_residual(afg_ctx* ctx, const int* list, int n, const T* phi, const T* rhs, T* tmp, double lam,
+static int launch_residual(afg_ctx* ctx, const int* list, int n, const T* phi, const T* rhs, T* tmp, MgCoef<T> lam,
                            unsigned long long* maxbits) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
@@ -295,7 +315,7 @@ static int launch_residual(afg_ctx* ctx, const int* list, int n, const T* phi, c
 }
 
 template <typename T>
-static int launch_rrestrict(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, T* tmp, double lam,
+static int launch_rrestrict(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, T* tmp, MgCoef<T> lam,
                             int store_child) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
@@ -313,7 +333,7 @@ static int launch_rrestrict(afg_ctx* ctx, const int* list, int n, T* phi, const 
 }
 
 template <typename T>
-static int launch_coarse_fas(afg_ctx* ctx, const int* list, int n, const T* phi, T* rhs, T* tmp, double lam,
+static int launch_coarse_fas(afg_ctx* ctx, const int* list, int n, const T* phi, T* rhs, T* tmp, MgCoef<T> lam,
                              int copy_tmp) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
@@ -462,11 +482,11 @@ static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, T* ph
   const int n = (int)ctx->lvl_ids[lvl - 1].size();
   ctx->ctr[1] += (long long)n * (long long)box_cells(ctx) * n_cycle;
   if (ctx->fused_gsrb) {
-    for (int it = 1; it <= 2 * n_cycle; it++) RC(launch_gsrb_fused<T>(ctx, list, n, phi, rhs, it, m.d.helmholtz_lambda, g));
+    for (int it = 1; it <= 2 * n_cycle; it++) RC(launch_gsrb_fused<T>(ctx, list, n, phi, rhs, it, coef_of<T>(m), g));
     return launch_gc<T>(ctx, list, n, phi, g, type != AFG_CYCLE_DOWN ? 1 : 0);
   }
   for (int it = 1; it <= 2 * n_cycle; it++) {
-    RC(launch_gsrb<T>(ctx, list, n, phi, rhs, it, m.d.helmholtz_lambda));
+    RC(launch_gsrb<T>(ctx, list, n, phi, rhs, it, coef_of<T>(m)));
     const int corners = (type != AFG_CYCLE_DOWN && it == 2 * n_cycle) ? 1 : 0;
     RC(launch_gc<T>(ctx, list, n, phi, g, corners));
   }
@@ -477,10 +497,10 @@ static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, T* ph
 template <typename T>
 static int mg_update_coarse(afg_ctx* ctx, const MgSlot& m, int lvl, T* phi, T* rhs, T* tmp, const GcDev& g) {
   RC(launch_rrestrict<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs, tmp,
-                         m.d.helmholtz_lambda, 0));
+                         coef_of<T>(m), 0));
   RC(mg_gc_lvl<T>(ctx, lvl - 1, phi, g, 1));
   RC(launch_coarse_fas<T>(ctx, lst(ctx, ctx->off_parents[lvl - 2]), (int)ctx->lvl_parents[lvl - 2].size(), phi, rhs,
-                          tmp, m.d.helmholtz_lambda, 1));
+                          tmp, coef_of<T>(m), 1));
   return AFG_OK;
 }
 
@@ -489,10 +509,10 @@ template <typename T>
 static int mg_set_coarse_phi_rhs(afg_ctx* ctx, const MgSlot& m, int lvl, T* phi, T* rhs, T* tmp, const GcDev& g) {
   if (lvl == ctx->highest_lvl) RC(mg_gc_lvl<T>(ctx, lvl, phi, g, 1));
   RC(launch_rrestrict<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs, tmp,
-                         m.d.helmholtz_lambda, 1));
+                         coef_of<T>(m), 1));
   RC(mg_gc_lvl<T>(ctx, lvl - 1, phi, g, 1));
   RC(launch_coarse_fas<T>(ctx, lst(ctx, ctx->off_parents[lvl - 2]), (int)ctx->lvl_parents[lvl - 2].size(), phi, rhs,
-                          tmp, m.d.helmholtz_lambda, 0));
+                          tmp, coef_of<T>(m), 0));
   return AFG_OK;
 }
 
@@ -526,10 +546,10 @@ template <typename T>
 static int mg_residual_lvls(afg_ctx* ctx, const MgSlot& m, int max_lvl, const T* phi, const T* rhs, T* tmp,
                             unsigned long long* maxbits) {
   if (max_lvl == ctx->highest_lvl)  // boxes are independent: one launch over all levels
-    return launch_residual<T>(ctx, lst(ctx, ctx->off_all), ctx->n_all, phi, rhs, tmp, m.d.helmholtz_lambda, maxbits);
+    return launch_residual<T>(ctx, lst(ctx, ctx->off_all), ctx->n_all, phi, rhs, tmp, coef_of<T>(m), maxbits);
   for (int lvl = 1; lvl <= max_lvl; lvl++)
     RC(launch_residual<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs, tmp,
-                          m.d.helmholtz_lambda, maxbits));
+                          coef_of<T>(m), maxbits));
   return AFG_OK;
 }
 
@@ -791,6 +811,13 @@ int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_va
   CK(cudaMemcpy(ctx->d_is_leaf, is_leaf.data(), n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_cslot, cslot.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_ccell, ccell.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
+  // cylindrical geometry table
+  if (ctx->coord == AFG_CYL) {
+    CK(dalloc(&ctx->d_geo, (size_t)n * nc * 4));
+    k_setup_geo<<<(n * nc + 255) / 256, 256, 0, ctx->stream>>>(n, nc, ctx->d_rmin, ctx->d_dr, ctx->d_geo);
+    ctx->launches++;
+    CKL();
+  }
   // pools
   ctx->n_var = n_var_cell;
   ctx->n_var_face = n_var_face;
@@ -1074,9 +1101,28 @@ int afg_mg_setup(afg_ctx* ctx, int mg_id, const afg_mg_desc* d) {
   MgSlot& m = ctx->mg[mg_id];
   dfree(m.d_ainv); dfree(m.d_b); dfree(m.d_x); dfree(m.d_b2r); dfree(m.d_bmask); dfree(m.d_bcval);
   dfree(m.e32); dfree(m.r32); dfree(m.t32);
+  dfree(m.d_cb64); dfree(m.d_cb32); dfree(m.d_cy64); dfree(m.d_cy32);
   m.used = false;
   m.d = *d;
   RC(build_coarse(ctx, m));
+  {
+    const int n = ctx->n_boxes, cyl = ctx->coord == AFG_CYL;
+    const size_t ny = cyl ? (size_t)n * ctx->nc * 4 : 1;
+    CK(dalloc(&m.d_cb64, (size_t)n * 8));
+    CK(dalloc(&m.d_cb32, (size_t)n * 8));
+    CK(dalloc(&m.d_cy64, ny));
+    CK(dalloc(&m.d_cy32, ny));
+    KTree t = ktree(ctx);
+    if (ctx->D == 3)
+      k_setup_coef<3><<<(n + 127) / 128, 128, 0, ctx->stream>>>(t, n, d->helmholtz_lambda, 0, m.d_cb64, m.d_cb32,
+                                                               m.d_cy64, m.d_cy32);
+    else
+      k_setup_coef<2><<<(n + 127) / 128, 128, 0, ctx->stream>>>(t, n, d->helmholtz_lambda, cyl, m.d_cb64, m.d_cb32,
+                                                               m.d_cy64, m.d_cy32);
+    ctx->launches++;
+    CKL();
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
   if (d->precision == AFG_MIXED) {
     const size_t N = (size_t)ctx->n_boxes * ctx->S;
     if (dalloc(&m.e32, N) != cudaSuccess || dalloc(&m.r32, N) != cudaSuccess || dalloc(&m.t32, N) != cudaSuccess)

@@ -132,9 +132,8 @@ __global__ void __launch_bounds__(256) k_restrict_geom(KTree t, const int* __res
       const int ic = o0 + i;
       double val;
       if (CYL) {
-        const double rp = t.r_min[pslot * 2] + (ic - 0.5) * t.dr[pslot * 2];
-        const double tw = 0.25 * t.dr[pslot * 2] / rp;
-        const double w1 = 1 - tw, w2 = 1 + tw;
+        const double* gw = t.geo + ((size_t)pslot * nc + (ic - 1)) * 4;
+        const double w1 = gw[2], w2 = gw[3];
         double s1 = 0, s2 = 0;
         s1 = s1 + c[at2(n2, fi, fj)]; s1 = s1 + c[at2(n2, fi, fj + 1)];
         s2 = s2 + c[at2(n2, fi + 1, fj)]; s2 = s2 + c[at2(n2, fi + 1, fj + 1)];
@@ -384,9 +383,8 @@ __global__ void __launch_bounds__(128) k_consistent_flux(KTree t, const int* __r
       if (d == 0) {
         G[fc_at(nf1, i_nb, o + n, 1)] = 0.5 * (F[fc_at(nf1, i, 2 * n - 1, 1)] + F[fc_at(nf1, i, 2 * n, 1)]);
       } else if (CYL) {
-        const double r = t.r_min[nbs * 2] + ((o + n) - 0.5) * t.dr[nbs * 2];
-        const double tmp = 0.25 * t.dr[nbs * 2] / r;
-        const double w1 = 1 - tmp, w2 = 1 + tmp;
+        const double* gw = t.geo + ((size_t)nbs * nc + (o + n - 1)) * 4;
+        const double w1 = gw[2], w2 = gw[3];
         G[fc_at(nf1, o + n, i_nb, 1)] = 0.5 * (w1 * F[fc_at(nf1, 2 * n - 1, i, 1)] + w2 * F[fc_at(nf1, 2 * n, i, 1)]);
       } else {
         G[fc_at(nf1, o + n, i_nb, 1)] = 0.5 * (F[fc_at(nf1, 2 * n - 1, i, 1)] + F[fc_at(nf1, 2 * n, i, 1)]);
@@ -499,10 +497,8 @@ __global__ void __launch_bounds__(256) k_update(KTree t, const int* __restrict__
       const double* F1 = a.flux[f] + ((size_t)slot * D + 1) * t.NF;
       const int kk = D == 3 ? k : 1;
       if (D == 2 && CYL) {
-        const double rr = t.r_min[slot * 2] + (i - 0.5) * t.dr[slot * 2];
-        const double inv_r = 1 / rr;
-        const double h = t.dr[slot * 2];
-        const double f1 = (rr - 0.5 * h) * inv_r, f2 = (rr + 0.5 * h) * inv_r;
+        const double* gw = t.geo + ((size_t)slot * nc + (i - 1)) * 4;
+        const double f1 = gw[0], f2 = gw[1];
         outv[s] = outv[s] + dt_dr[0] * (f1 * F0[fc_at(nf1, i, j, 1)] - f2 * F0[fc_at(nf1, i + 1, j, 1)]) +
                   dt_dr[1] * (F1[fc_at(nf1, i, j, 1)] - F1[fc_at(nf1, i, j + 1, 1)]);
       } else if (D == 2) {

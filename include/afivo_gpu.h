@@ -193,7 +193,9 @@ int afg_mg_solve(afg_ctx* ctx, int mg_id, double threshold, int max_cycles,
 /* Single stages, for parity testing of each kernel against the oracle:
  * gsrb_boxes (648-687), update_coarse (691-738), correct_children (624-646)
  * on the parents of level lvl-1 followed by af_gc_lvl(lvl), and the coarse
- * solve solve_coarse_grid (266-291). */
+ * solve solve_coarse_grid (266-291).  Like the reference's multigrid
+ * routines they need valid ghost cells of i_phi on entry (the smoother
+ * evaluates the ghost rules on the fly between half sweeps). */
 int afg_mg_gsrb_lvl(afg_ctx* ctx, int mg_id, int lvl, int cycle_type);
 int afg_mg_update_coarse(afg_ctx* ctx, int mg_id, int lvl);
 int afg_mg_correct_lvl(afg_ctx* ctx, int mg_id, int lvl);
