@@ -97,12 +97,16 @@ def test_ghost_fill_all_rules_bitexact(case):
 def test_gsrb_levels_bitexact(case, lambda2):
     name, tree, ctx = case
     desc, cc, o = setup_pair(tree, ctx, 5, lambda2)
-    # gsrb_boxes needs valid ghost cells on entry, as at every call site
+    # gsrb_boxes needs valid ghost cells on entry, as at every call site: in
+    # the V-cycle levels are smoothed fine to coarse on the way down, and
+    # ghost cells are refilled before each upward smoothing
     ctx.gc(I_PHI, 0, True)
     o.gc(cc, I_PHI, 0, True)
-    for lvl in range(2, tree.highest_lvl + 1):
+    for lvl in range(tree.highest_lvl, 1, -1):
         ctx.mg_gsrb_lvl(0, lvl, ag.CYCLE_DOWN)
         o.mg_gsrb_lvl(cc, 0, lvl, ag.CYCLE_DOWN)
+    ctx.gc(I_PHI, 0, True)
+    o.gc(cc, I_PHI, 0, True)
     ctx.mg_gsrb_lvl(0, tree.highest_lvl, ag.CYCLE_UP)
     o.mg_gsrb_lvl(cc, 0, tree.highest_lvl, ag.CYCLE_UP)
     out = download(ctx, tree)
