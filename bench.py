@@ -348,7 +348,7 @@ def main():
     ks = kstats[dom]
     achieved = ks["bytes"] / (ks["ms"] * 1e-3) / 1e9 if ks["ms"] > 0 else 0.0
     cpu = None
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and args.cpu_steps > 0:
         v, cores, sps = run_cpu(args.cpu_steps, warmup=0)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{args.cpu_steps} full step(s) of the same workload on the CPU oracle (OpenMP)"}
