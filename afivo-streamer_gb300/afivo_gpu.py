@@ -229,6 +229,7 @@ def load_library(path: str = LIB_PATH):
         "afg_flush_l2": (C.c_int, [P, C.c_longlong]),
         "afg_kernel_timing": (C.c_int, [P, C.c_int]),
         "afg_kernel_stats": (C.c_int, [P, C.POINTER(C.c_longlong), _DP, _DP]),
+        "afg_maxabs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, _DP]),
         "afg_sync": (C.c_int, [P]),
         "afg_launch_count": (C.c_longlong, [P]),
     }
@@ -454,6 +455,18 @@ class Context:
 
     def launch_count(self) -> int:
         return int(self.lib.afg_launch_count(self.ptr))
+
+
+def maxabs_noalloc(d_pool: int, d_slots: int, n_slots: int, ndim: int, n_cell: int, stream: int = 0) -> float:
+    """afg_maxabs_noalloc on caller-owned device buffers (raw device
+    addresses); raises on a non-zero status."""
+    lib = load_library()
+    out = C.c_double(0)
+    rc = lib.afg_maxabs_noalloc(C.c_void_p(d_pool), C.c_void_p(d_slots), n_slots, ndim, n_cell,
+                                C.c_void_p(stream) if stream else None, C.byref(out))
+    if rc != AFG_OK:
+        raise AfgError(rc, "afg_maxabs_noalloc")
+    return out.value
 
 
 def new_fc(tree, n_var_face) -> np.ndarray:

@@ -359,6 +359,26 @@ int afg_flush_l2(afg_ctx* ctx, long long bytes);
 int afg_kernel_timing(afg_ctx* ctx, int kernel_class);
 int afg_kernel_stats(afg_ctx* ctx, long long* launches, double* ms, double* bytes);
 
+/* ---- reduction without device allocation -------------------------------
+ * No counterpart in the reference.  For callers that may not call
+ * cudaMalloc (they own their device arrays through their own allocator or
+ * pool, or run under a fixed device-memory budget) and so cannot create a
+ * context: max |v| over the interior cells of the boxes d_slots[0..n_slots-1]
+ * (0-based box slots, in device memory) of a caller-owned device pool laid
+ * out like one afivo variable, d_pool[slot][(n_cell+2)^ndim] (the
+ * af_tree_maxabs_cc reduction).  Nothing is allocated: the scratch is a
+ * file-scope device array of AFG_NOALLOC_MAX_BOXES + 1 doubles (2 MiB) that
+ * every GPU loading this library holds until the process exits; n_slots
+ * beyond AFG_NOALLOC_MAX_BOXES returns AFG_ERR_ARG.  The first call on a
+ * device looks up the array's device address; make that first call before
+ * any stream capture.  All calls share the array, so calls that overlap on
+ * the GPU (other streams, other threads) race; each call writes every entry
+ * it reads, so nothing needs clearing.  Runs on `stream` (a cudaStream_t,
+ * NULL = default stream) and synchronises it; *result is a host double. */
+#define AFG_NOALLOC_MAX_BOXES 262144
+int afg_maxabs_noalloc(const double* d_pool, const int* d_slots, int n_slots,
+                       int ndim, int n_cell, void* stream, double* result);
+
 /* Synchronise the context's stream and check the device error word. */
 int afg_sync(afg_ctx* ctx);
 
