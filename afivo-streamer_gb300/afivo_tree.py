@@ -120,29 +120,28 @@ class Tree:
         return out
 
 
-def _upsample(a: np.ndarray) -> np.ndarray:
-    for ax in range(a.ndim):
-        a = np.repeat(a, 2, axis=ax)
-    return a
+def _keys(ix: np.ndarray, n: np.ndarray) -> np.ndarray:
+    """Linear keys of 0-based box indices (x fastest), one level."""
+    k = np.zeros(len(ix), dtype=np.int64)
+    for d in range(ix.shape[1] - 1, -1, -1):
+        k = k * int(n[d]) + ix[:, d]
+    return k
 
 
-def _dilate(a: np.ndarray) -> np.ndarray:
-    out = a.copy()
-    D = a.ndim
-    padded = np.pad(a, 1)
-    for off in itertools.product([-1, 0, 1], repeat=D):
-        sl = tuple(slice(1 + o, 1 + o + n) for o, n in zip(off, a.shape))
-        out |= padded[sl]
+def _unkey(k: np.ndarray, n: np.ndarray, D: int) -> np.ndarray:
+    out = np.empty((len(k), D), dtype=np.int64)
+    for d in range(D):
+        out[:, d] = k % int(n[d])
+        k = k // int(n[d])
     return out
 
 
-def _coarsen_any(a: np.ndarray) -> np.ndarray:
-    D = a.ndim
-    shp = []
-    for n in a.shape:
-        shp += [n // 2, 2]
-    r = a.reshape(shp)
-    return r.any(axis=tuple(range(1, 2 * D, 2)))
+def _lookup(keys_sorted: np.ndarray, q: np.ndarray) -> np.ndarray:
+    """Index of q in keys_sorted, -1 where absent."""
+    pos = np.searchsorted(keys_sorted, q)
+    pos = np.minimum(pos, max(len(keys_sorted) - 1, 0))
+    found = (len(keys_sorted) > 0) & (keys_sorted[pos] == q) if len(keys_sorted) else np.zeros(len(q), bool)
+    return np.where(found, pos, -1)
 
 
 def build_tree(ndim: int, n_cell: int, coarse_grid_size, domain_len,
@@ -154,7 +153,8 @@ def build_tree(ndim: int, n_cell: int, coarse_grid_size, domain_len,
     level ``lvl`` (given by their centres) want children; ``None`` refines
     everything (uniform grid).  Level 1 is the coarse grid of
     ``coarse_grid_size`` cells, split into boxes like ``af_set_coarse_grid``
-    (m_af_core.f90:206-340).
+    (m_af_core.f90:206-340).  Boxes are kept as sorted index keys per level,
+    so deep 3D trees cost memory proportional to the number of boxes.
     """
     D = ndim
     nc = n_cell
@@ -167,13 +167,7 @@ def build_tree(ndim: int, n_cell: int, coarse_grid_size, domain_len,
     # af_init: dr_base = (r_max - r_min) / grid_size, r_max = r_min + L
     dr_base = ((rb + dom) - rb) / cgs
     nx1 = cgs // nc
-
-    # Dense per-level arrays, index order [x, y(, z)] (C order in numpy but
-    # we only use them as maps).
-    shapes = [tuple(int(n) * 2 ** l for n in nx1) for l in range(max_lvl)]
-    exists = [np.zeros(s, dtype=bool) for s in shapes]
-    refined = [np.zeros(s, dtype=bool) for s in shapes]
-    exists[0][...] = True
+    nlev = [nx1 * 2 ** l for l in range(max_lvl)]
 
     def lvl_dr(l):
         d = dr_base.copy()
@@ -181,70 +175,62 @@ def build_tree(ndim: int, n_cell: int, coarse_grid_size, domain_len,
             d = 0.5 * d
         return d
 
+    cdix = child_dix(D)
+    all1 = np.stack(np.meshgrid(*[np.arange(int(n)) for n in nx1], indexing="ij"), -1).reshape(-1, D)
+    exists = [np.sort(_keys(all1, nlev[0]))]
+    refined = [np.zeros(0, np.int64) for _ in range(max_lvl)]
     for l in range(max_lvl - 1):
-        ixs = np.argwhere(exists[l])
-        if len(ixs) == 0:
+        ix = _unkey(exists[l], nlev[l], D)
+        if len(ix) == 0:
             break
         if refine is None:
-            want = np.ones(len(ixs), dtype=bool)
+            want = np.ones(len(ix), dtype=bool)
         else:
             drl = lvl_dr(l)
-            centers = rb + (ixs + 0.5) * drl * nc
+            centers = rb + (ix + 0.5) * drl * nc
             want = np.asarray(refine(l + 1, centers, drl), dtype=bool)
-        r = np.zeros(shapes[l], dtype=bool)
-        r[tuple(ixs[want].T)] = True
-        refined[l] = r
-        exists[l + 1] = _upsample(r)
-
-    # 2:1 balance, fine to coarse
-    # (a refined box needs its whole 3^D neighbourhood on its own level; the
-    # parents of newly refined boxes are handled by the next, coarser pass
-    # through the dilation of refined[l-1])
+        refined[l] = exists[l][want]
+        cix = (2 * ix[want][:, None, :] + cdix[None, :, :]).reshape(-1, D)
+        exists.append(np.sort(_keys(cix, nlev[l + 1])))
+    # 2:1 balance, fine to coarse: a refined box needs its whole 3^D
+    # neighbourhood on its own level; the parents of newly refined boxes are
+    # handled by the next, coarser pass through the dilation of refined[l-1]
+    offs = np.array(list(itertools.product([-1, 0, 1], repeat=D)), dtype=np.int64)
     for l in range(max_lvl - 2, 0, -1):
-        refined[l - 1] |= _coarsen_any(_dilate(refined[l]))
+        if len(refined[l]) == 0:
+            continue
+        ix = _unkey(refined[l], nlev[l], D)
+        nbh = (ix[:, None, :] + offs[None, :, :]).reshape(-1, D)
+        ok = np.all((nbh >= 0) & (nbh < nlev[l][None, :]), axis=1)
+        par = np.unique(_keys(nbh[ok] // 2, nlev[l - 1]))
+        refined[l - 1] = np.union1d(refined[l - 1], par)
+    exists = exists[:1]
     for l in range(max_lvl - 1):
-        exists[l + 1] = _upsample(refined[l])
-    refined[max_lvl - 1][...] = False
-
-    # Assign ids
-    idmaps = []
-    lvl_ids = []
-    next_id = 1
-    # level 1: Fortran order (x fastest)
-    idm = np.zeros(shapes[0], dtype=np.int64)
-    cnt = int(np.prod(nx1))
-    grid = np.arange(cnt, dtype=np.int64).reshape(tuple(nx1[::-1])).T
-    idm[...] = grid + 1
-    idmaps.append(idm)
-    lvl_ids.append(np.arange(1, cnt + 1, dtype=np.int64))
-    next_id = cnt + 1
-    cdix = child_dix(D)
-    all_ix = [None]
-    # store ix per level, row = id order
-    ix_of = {}
-    ixs1 = np.argwhere(np.ones(shapes[0], dtype=bool))
-    # order ixs1 by id
-    ids1 = idm[tuple(ixs1.T)]
-    order = np.argsort(ids1)
-    ix_of[0] = ixs1[order]
-    highest = 1
-    for l in range(1, max_lvl):
-        if not exists[l].any():
+        if len(refined[l]) == 0:
             break
-        highest = l + 1
-        pix = ix_of[l - 1]
-        pids = lvl_ids[l - 1]
-        is_ref = refined[l - 1][tuple(pix.T)]
-        pix_r = pix[is_ref]
-        n_par = len(pix_r)
-        cix = (2 * pix_r[:, None, :] + cdix[None, :, :]).reshape(-1, D)
-        cids = next_id + np.arange(n_par * 2 ** D, dtype=np.int64)
-        next_id += len(cids)
-        idm = np.zeros(shapes[l], dtype=np.int64)
-        idm[tuple(cix.T)] = cids
-        idmaps.append(idm)
+        ix = _unkey(refined[l], nlev[l], D)
+        cix = (2 * ix[:, None, :] + cdix[None, :, :]).reshape(-1, D)
+        exists.append(np.sort(_keys(cix, nlev[l + 1])))
+    highest = len(exists)
+
+    # ids: level 1 in Fortran order (x fastest), then children of each
+    # refined parent in parent-id order, child order af_child_dix
+    lvl_ids, ix_of, key_of = [], [], []
+    ix1 = _unkey(exists[0], nlev[0], D)
+    lvl_ids.append(np.arange(1, len(ix1) + 1, dtype=np.int64))
+    ix_of.append(ix1)
+    key_of.append(exists[0])
+    next_id = len(ix1) + 1
+    for l in range(1, highest):
+        pkeys = key_of[l - 1]
+        is_ref = np.isin(pkeys, refined[l - 1])
+        pix = ix_of[l - 1][is_ref]
+        cix = (2 * pix[:, None, :] + cdix[None, :, :]).reshape(-1, D)
+        cids = next_id + np.arange(len(cix), dtype=np.int64)
+        next_id += len(cix)
         lvl_ids.append(cids)
-        ix_of[l] = cix
+        ix_of.append(cix)
+        key_of.append(_keys(cix, nlev[l]))
     n_boxes = next_id - 1
 
     t = Tree(ndim=D, n_cell=nc, coord=coord, coarse_grid_size=cgs,
@@ -266,21 +252,34 @@ def build_tree(ndim: int, n_cell: int, coarse_grid_size, domain_len,
         ids = lvl_ids[l]
         ixl = ix_of[l]
         rows = ids - 1
+        order = np.argsort(key_of[l])
+        skeys = key_of[l][order]
+        sids = ids[order]
+
+        def find(offsets):
+            out = np.empty((len(ixl), len(offsets)), dtype=np.int64)
+            for n, off in enumerate(offsets):
+                q = ixl + off
+                inside = np.all((q >= 0) & (q < nlev[l][None, :]), axis=1)
+                res = np.full(len(q), AF_PHYS_BOUNDARY, dtype=np.int64)
+                pos = _lookup(skeys, _keys(np.where(inside[:, None], q, 0), nlev[l]))
+                res[inside] = np.where(pos[inside] >= 0, sids[np.maximum(pos[inside], 0)], AF_NO_BOX)
+                out[:, n] = res
+            return out
+
         t.lvl[rows] = l + 1
         t.ix[rows] = ixl + 1
-        pad = np.pad(idmaps[l], 1, constant_values=AF_PHYS_BOUNDARY)
-        for n, off in enumerate(nbd):
-            t.neighbors[rows, n] = pad[tuple((ixl + 1 + off).T)]
-        for n, off in enumerate(nmo):
-            t.neighbor_mat[rows, n] = pad[tuple((ixl + 1 + off).T)]
+        t.neighbors[rows] = find(nbd)
+        t.neighbor_mat[rows] = find(nmo)
         if l == 0:
             t.parent[rows] = AF_NO_BOX
             # r_base + (ix - 1) * dr_base * n_cell
             t.r_min[rows] = rb + (ixl.astype(np.float64) * dr_base) * nc
             t.dr[rows] = dr_base
         else:
-            pidm = idmaps[l - 1]
-            pids = pidm[tuple((ixl // 2).T)]
+            porder = np.argsort(key_of[l - 1])
+            ppos = _lookup(key_of[l - 1][porder], _keys(ixl // 2, nlev[l - 1]))
+            pids = lvl_ids[l - 1][porder][ppos]
             t.parent[rows] = pids
             cnum = np.zeros(len(ids), dtype=np.int64)
             for d in range(D):

@@ -439,9 +439,27 @@ __device__ __forceinline__ double rate_of(const LtDev& lt, const afg_reaction& r
   return 0;
 }
 
+// Species arrays are indexed through the reaction tables at run time; to
+// keep them in registers every access goes through a fully unrolled loop over
+// the compile-time bound NSMAX (static indices only).
+template <int NSMAX>
+__device__ __forceinline__ double pick(const double (&v)[NSMAX], int s) {
+  double r = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSMAX; k++)
+    if (k == s) r = v[k];
+  return r;
+}
+template <int NSMAX>
+__device__ __forceinline__ void add_to(double (&v)[NSMAX], int s, double x) {
+#pragma unroll
+  for (int k = 0; k < NSMAX; k++)
+    if (k == s) v[k] = v[k] + x;
+}
+
 // flux_update_densities + add_source_terms for each leaf cell
-template <int D, bool CYL>
-__global__ void __launch_bounds__(256) k_update(KTree t, const int* __restrict__ list, UpdateArgs a) {
+template <int D, bool CYL, int NSMAX>
+__global__ void __launch_bounds__(128) k_update(KTree t, const int* __restrict__ list, UpdateArgs a) {
   __shared__ double sred[32];
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2, nf1 = nc + 1;
@@ -454,13 +472,18 @@ __global__ void __launch_bounds__(256) k_update(KTree t, const int* __restrict__
     const int i = w % nc + 1, r = w / nc;
     const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
     const int x = D == 2 ? at2(n2, i, j) : at3(n2, i, j, k);
-    double outv[AFG_MAX_SPECIES], dens[AFG_MAX_SPECIES], der[AFG_MAX_SPECIES];
-    for (int s = 0; s < a.ns; s++) {
-      double tmp = 0.0;
-      for (int mm = 0; mm < a.n_prev; mm++) tmp = tmp + a.w_prev[mm] * a.prev[mm][s][base + x];
-      outv[s] = tmp;
-      dens[s] = fmax(a.deriv[s][base + x], 0.0);
+    double outv[NSMAX], dens[NSMAX], der[NSMAX];
+#pragma unroll
+    for (int s = 0; s < NSMAX; s++) {
+      outv[s] = 0.0;
+      dens[s] = 0.0;
       der[s] = 0.0;
+      if (s < a.ns) {
+        double tmp = 0.0;
+        for (int mm = 0; mm < a.n_prev; mm++) tmp = tmp + a.w_prev[mm] * a.prev[mm][s][base + x];
+        outv[s] = tmp;
+        dens[s] = fmax(a.deriv[s][base + x], 0.0);
+      }
     }
     const double td = kSiToTd * a.N_inv * a.E[base + x];
     int ix;
@@ -470,51 +493,60 @@ __global__ void __launch_bounds__(256) k_update(KTree t, const int* __restrict__
       const afg_reaction& rc = a.reactions[n];
       double rate = rate_of(a.lt, rc, td, ix, lw);
       double prod = 1.0;
-      for (int q = 0; q < rc.n_in; q++) prod = prod * dens[rc.ix_in[q]];
+      for (int q = 0; q < rc.n_in; q++) prod = prod * pick<NSMAX>(dens, rc.ix_in[q]);
       rate = rate * prod;
-      for (int q = 0; q < rc.n_in; q++) der[rc.ix_in[q]] = der[rc.ix_in[q]] - rate;
-      for (int q = 0; q < rc.n_out; q++) der[rc.ix_out[q]] = der[rc.ix_out[q]] + rate * rc.mult_out[q];
+      for (int q = 0; q < rc.n_in; q++) add_to<NSMAX>(der, rc.ix_in[q], -rate);
+      for (int q = 0; q < rc.n_out; q++) add_to<NSMAX>(der, rc.ix_out[q], rate * rc.mult_out[q]);
     }
     if (a.last_step) {
       const double eps = 1e-100;
       double tmp = 1e100;
-      if (a.nmin > 0) {
-        for (int s = 0; s < a.ns; s++) tmp = fmin(tmp, (dens[s] + a.nmin) / fmax(fabs(der[s]), eps));
-      } else if (a.limit_loss) {
-        for (int s = 0; s < a.ns; s++) tmp = fmin(tmp, fmax(dens[s], eps) / fmax(-der[s], eps));
+#pragma unroll
+      for (int s = 0; s < NSMAX; s++) {
+        if (s >= a.ns) continue;
+        if (a.nmin > 0)
+          tmp = fmin(tmp, (dens[s] + a.nmin) / fmax(fabs(der[s]), eps));
+        else if (a.limit_loss)
+          tmp = fmin(tmp, fmax(dens[s], eps) / fmax(-der[s], eps));
       }
       my_chem = fmin(my_chem, tmp);
     }
     if (a.photo != nullptr) {
       const double ph = a.photo[base + x];
-      der[a.flux_species[0]] = der[a.flux_species[0]] + ph;
-      der[a.photoi_species] = der[a.photoi_species] + ph;
+      add_to<NSMAX>(der, a.flux_species[0], ph);
+      add_to<NSMAX>(der, a.photoi_species, ph);
     }
-    for (int s = 0; s < a.ns; s++) outv[s] = outv[s] + a.dt * der[s];
+#pragma unroll
+    for (int s = 0; s < NSMAX; s++) outv[s] = outv[s] + a.dt * der[s];
     for (int f = 0; f < a.nf; f++) {
       const int s = a.flux_species[f];
       const double* F0 = a.flux[f] + ((size_t)slot * D + 0) * t.NF;
       const double* F1 = a.flux[f] + ((size_t)slot * D + 1) * t.NF;
       const int kk = D == 3 ? k : 1;
+      double div;
       if (D == 2 && CYL) {
         const double* gw = t.geo + ((size_t)slot * nc + (i - 1)) * 4;
         const double f1 = gw[0], f2 = gw[1];
-        outv[s] = outv[s] + dt_dr[0] * (f1 * F0[fc_at(nf1, i, j, 1)] - f2 * F0[fc_at(nf1, i + 1, j, 1)]) +
-                  dt_dr[1] * (F1[fc_at(nf1, i, j, 1)] - F1[fc_at(nf1, i, j + 1, 1)]);
+        div = dt_dr[0] * (f1 * F0[fc_at(nf1, i, j, 1)] - f2 * F0[fc_at(nf1, i + 1, j, 1)]);
+        div = pick<NSMAX>(outv, s) + div + dt_dr[1] * (F1[fc_at(nf1, i, j, 1)] - F1[fc_at(nf1, i, j + 1, 1)]);
       } else if (D == 2) {
-        outv[s] = outv[s] + dt_dr[0] * (F0[fc_at(nf1, i, j, 1)] - F0[fc_at(nf1, i + 1, j, 1)]) +
-                  dt_dr[1] * (F1[fc_at(nf1, i, j, 1)] - F1[fc_at(nf1, i, j + 1, 1)]);
+        div = pick<NSMAX>(outv, s) + dt_dr[0] * (F0[fc_at(nf1, i, j, 1)] - F0[fc_at(nf1, i + 1, j, 1)]) +
+              dt_dr[1] * (F1[fc_at(nf1, i, j, 1)] - F1[fc_at(nf1, i, j + 1, 1)]);
       } else {
         const double* F2 = a.flux[f] + ((size_t)slot * D + 2) * t.NF;
-        outv[s] = outv[s] + dt_dr[0] * (F0[fc_at(nf1, i, j, kk)] - F0[fc_at(nf1, i + 1, j, kk)]) +
-                  dt_dr[1] * (F1[fc_at(nf1, i, j, kk)] - F1[fc_at(nf1, i, j + 1, kk)]) +
-                  dt_dr[2] * (F2[fc_at(nf1, i, j, kk)] - F2[fc_at(nf1, i, j, kk + 1)]);
+        div = pick<NSMAX>(outv, s) + dt_dr[0] * (F0[fc_at(nf1, i, j, kk)] - F0[fc_at(nf1, i + 1, j, kk)]) +
+              dt_dr[1] * (F1[fc_at(nf1, i, j, kk)] - F1[fc_at(nf1, i, j + 1, kk)]) +
+              dt_dr[2] * (F2[fc_at(nf1, i, j, kk)] - F2[fc_at(nf1, i, j, kk + 1)]);
       }
+#pragma unroll
+      for (int q = 0; q < NSMAX; q++)
+        if (q == s) outv[q] = div;
     }
-    for (int s = 0; s < a.ns; s++) a.out[s][base + x] = outv[s];
+#pragma unroll
+    for (int s = 0; s < NSMAX; s++)
+      if (s < a.ns) a.out[s][base + x] = outv[s];
   }
   if (a.last_step) {
-    // min of positive values: max of -x is not monotone in bits, so reduce min
     for (int o = 16; o > 0; o >>= 1) my_chem = fmin(my_chem, __shfl_xor_sync(0xffffffffu, my_chem, o));
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) sred[warp] = my_chem;

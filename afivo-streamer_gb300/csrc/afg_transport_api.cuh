@@ -269,12 +269,22 @@ int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev, const
   ctx->ctr[2] += (long long)n * (long long)box_cells(ctx) * d.n_species;
   if (n > 0) {
     kt_begin(ctx, AFG_KT_UPDATE);
-    if (ctx->D == 3)
-      k_update<3, false><<<n, 128, 0, ctx->stream>>>(t, list, a);
-    else if (ctx->coord == AFG_CYL)
-      k_update<2, true><<<n, 128, 0, ctx->stream>>>(t, list, a);
-    else
-      k_update<2, false><<<n, 128, 0, ctx->stream>>>(t, list, a);
+    const bool cyl = ctx->coord == AFG_CYL;
+#define AFG_LAUNCH_UPDATE(NSM)                                                   \
+  if (ctx->D == 3)                                                               \
+    k_update<3, false, NSM><<<n, 128, 0, ctx->stream>>>(t, list, a);             \
+  else if (cyl)                                                                  \
+    k_update<2, true, NSM><<<n, 128, 0, ctx->stream>>>(t, list, a);              \
+  else                                                                           \
+    k_update<2, false, NSM><<<n, 128, 0, ctx->stream>>>(t, list, a);
+    if (d.n_species <= 4) {
+      AFG_LAUNCH_UPDATE(4)
+    } else if (d.n_species <= 8) {
+      AFG_LAUNCH_UPDATE(8)
+    } else {
+      AFG_LAUNCH_UPDATE(16)
+    }
+#undef AFG_LAUNCH_UPDATE
     // per leaf cell: read S*(n_prev+1) densities (+|E|, D*F fluxes, photo), write S densities
     kt_end(ctx, AFG_KT_UPDATE, 8.0 * n * box_cells(ctx) *
                                    (d.n_species * (n_prev + 1) + ctx->D * d.n_flux + 1 + (d.i_photo > 0) + d.n_species));

@@ -63,6 +63,7 @@ class StreamerModel:
     table_size: int = 1000
     td_max: float = 1000.0
     bc_species: int = ag.BC_NEUMANN
+    photoi_species_index: int = 1     # species that gains the photoionization source with e
 
     # variable layout (1-based tree indices)
     def __post_init__(self):
@@ -138,7 +139,7 @@ class StreamerModel:
         d.i_electric_fld = self.i_electric_fld
         d.i_efield_fc = self.f_efield
         d.i_photo = self.i_photo
-        d.photoi_species = 1
+        d.photoi_species = self.photoi_species_index
         d.gas_number_density = self.N
         d.species_gc = ag.gc_desc([self.bc_species] * (2 * self.ndim), None, ag.RB_INTERP_LIM)
         d.prolong_limiter = ag.LIMITER_MC if self.ndim < 3 else ag.LIMITER_GMINMOD43

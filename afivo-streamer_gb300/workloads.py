@@ -1,0 +1,160 @@
+"""Synthetic streamer workloads (seeded), the inputs of the benchmark.
+
+Two configurations of the hot path are defined here; no public dataset is
+involved (each configuration defines its own inputs):
+
+* ``cyl2d`` -- 2D axisymmetric streamer, r in [0, 1 cm], z in [0, 2 cm],
+  16^2-cell boxes, coarse grid 16x32, uniform to level 5 plus 4 AMR levels
+  around the streamer channel (~0.56 M leaf cells, 9 levels); electrons,
+  positive and negative ions; ionization alpha(E) = 4.3e5 exp(-2e7/|E|),
+  attachment eta = 2e3 1/m, mobility 0.03 m^2/Vs, diffusion 0.1 m^2/s;
+  3-term Helmholtz photoionization; applied field 1.5e6 V/m.
+* ``3d`` -- 3D streamer, 3 cm cube, 8^3-cell boxes, coarse grid one box,
+  uniform to level 6 plus 6 AMR levels around the channel (~99 M leaf cells,
+  ~113 M cells, 12 levels); 5 species (e, N2+, O2+, O2-, O-) with 8
+  field-dependent reactions k(E) = A exp(-B/|E|), A log-uniform in
+  [1e-18, 1e-14] m^3/s and B uniform in [1e7, 3e7] V/m, each evaluated as the
+  reference's rate form k13 c1 exp(-(c2/(c3+Td))^c4) with c1 = A,
+  c2 = B*1e21/N, c3 = 0, c4 = 1 (src/m_chemistry.f90:117-118,751-752);
+  transport as cyl2d; 3-term Helmholtz photoionization; applied field
+  1.5e6 V/m.
+
+The refinement maps stand in for afivo's refinement criterion
+(alpha(E)*dx > 0.8 around a developed streamer, src/m_refine.f90:239-245):
+nested cylinders around the channel axis whose radius halves per level.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+import afivo_gpu as ag
+import afivo_tree as at
+import streamer_model as sm
+
+
+def channel_refinement(base, radii, z_tail, z_head, axis_xy=None):
+    """Refine every box up to level `base`, then boxes within radius
+    radii[l - base] of the channel axis between z_tail and z_head."""
+    def f(lvl, c, dr):
+        if lvl < base:
+            return np.ones(len(c), bool)
+        R = radii[lvl - base]
+        z = c[:, -1]
+        if axis_xy is None:
+            rr = np.abs(c[:, 0])
+        else:
+            rr = np.sqrt(((c[:, :-1] - np.asarray(axis_xy)) ** 2).sum(axis=1))
+        return (rr < R) & (z > z_tail - R) & (z < z_head + R)
+    return f
+
+
+class Workload:
+    name = ""
+    voltage = 0.0
+    dt = 5e-12
+    photoi_lambda = np.array([50.0, 150.0, 500.0])        # 1/m
+    photoi_coeffs = np.array([1e-2, 5e-2, 1e-1]) * 1e4     # 1/m^2
+    photoi_eta_quench = 0.05 * 0.038
+
+    def tree(self, reduced=False):
+        raise NotImplementedError
+
+    def model(self):
+        raise NotImplementedError
+
+    def seed_center(self):
+        raise NotImplementedError
+
+    def fill_variable(self, tree, model, iv, seed=12345):
+        """Initial value of cell-centred variable iv (1-based) on all boxes,
+        ghost cells included: array [n_boxes, 1, (nc+2)^D]."""
+        D, nc = tree.ndim, tree.n_cell
+        n2 = nc + 2
+        out = np.zeros((tree.n_boxes, 1) + (n2,) * D)
+        idx = np.arange(n2) - 0.5
+        X = []  # cell-centre coordinates, broadcastable to [n, (k,) j, i]
+        for d in range(D):
+            shape = [tree.n_boxes] + [1] * D
+            shape[1 + (D - 1 - d)] = n2
+            X.append((tree.r_min[:, d][:, None] + idx[None, :] * tree.dr[:, d][:, None]).reshape(shape))
+        c = self.seed_center()
+        r2 = sum((X[d] - c[d]) ** 2 for d in range(D))
+        sig = self.seed_sigma
+        gauss = 1e15 * np.exp(-r2 / (2 * sig ** 2))
+        L = float(tree.dr[0, -1] * tree.coarse_grid_size[-1])
+        if iv == model.i_phi:
+            out[:, 0] = self.voltage * np.broadcast_to(X[D - 1], gauss.shape) / L
+        elif iv in model.species_iv:
+            s = model.species_iv.index(iv)
+            if s == 0:
+                rng = np.random.default_rng(seed)
+                out[:, 0] = (gauss + 1e9) * (1 + 1e-3 * rng.standard_normal(gauss.shape))
+            elif s == self.positive_species:
+                out[:, 0] = gauss + 1e9
+        return out
+
+
+class Cyl2d(Workload):
+    name = "cyl2d"
+    voltage = -3e4          # 1.5e6 V/m over 2 cm
+    seed_sigma = 0.5e-3
+    positive_species = 1
+
+    def tree(self, reduced=False):
+        return at.build_tree(2, 16, [16, 32], [1e-2, 2e-2], coord=ag.AFG_CYL, max_lvl=9,
+                             refine=channel_refinement(5, [2e-3, 1e-3, 0.6e-3, 0.35e-3], 0.9e-2, 1.4e-2))
+
+    def model(self):
+        return sm.StreamerModel(2, alpha=sm.baseline_alpha, eta=sm.baseline_eta, photoi_modes=3)
+
+    def seed_center(self):
+        return (0.0, 1.2e-2)
+
+
+class Streamer3d(Workload):
+    name = "3d"
+    voltage = -4.5e4        # 1.5e6 V/m over 3 cm
+    seed_sigma = 0.3e-3
+    positive_species = 1
+
+    def tree(self, reduced=False):
+        """The full tree, or (reduced=True) the same construction two levels
+        coarser everywhere (~1/50 of the cells), the CPU baseline's sample."""
+        if reduced:
+            return at.build_tree(3, 8, [8, 8, 8], [3e-2] * 3, max_lvl=10,
+                                 refine=channel_refinement(4, [3.2e-3, 1.7e-3, 1.0e-3, 0.5e-3, 0.25e-3, 0.12e-3],
+                                                           1.2e-2, 1.8e-2, axis_xy=(1.5e-2, 1.5e-2)))
+        return at.build_tree(3, 8, [8, 8, 8], [3e-2] * 3, max_lvl=12,
+                             refine=channel_refinement(6, [3.2e-3, 1.7e-3, 1.0e-3, 0.5e-3, 0.25e-3, 0.12e-3],
+                                                       1.2e-2, 1.8e-2, axis_xy=(1.5e-2, 1.5e-2)))
+
+    def model(self):
+        N = sm.gas_number_density()
+        rng = np.random.default_rng(4242)
+        A = 10 ** rng.uniform(-18, -14, size=8)
+        B = rng.uniform(1e7, 3e7, size=8)
+        # species: 0 e, 1 N2+, 2 O2+, 3 O2-, 4 O-
+        reac = [([0], [0, 1], [2, 1], 0.79 * N),   # e + N2 -> e + e + N2+
+                ([0], [0, 2], [2, 1], 0.21 * N),   # e + O2 -> e + e + O2+
+                ([0], [4], [1], 0.21 * N),         # e + O2 -> O-
+                ([0], [3], [1], 0.21 * N),         # e + O2 (+M) -> O2-
+                ([3], [0], [1], N),                # O2- + M -> e
+                ([4], [0], [1], N),                # O- + M -> e
+                ([1], [2], [1], 0.21 * N),         # N2+ + O2 -> O2+
+                ([0, 2], [], [], 1.0)]             # e + O2+ -> neutrals
+        reactions = []
+        for n, (ins, outs, mult, fac) in enumerate(reac):
+            reactions.append(dict(type=ag.RATE_K13, factor=fac, c=[A[n], B[n] * 1e21 / N, 0.0, 1.0],
+                                  ix_in=ins, ix_out=outs, mult=mult))
+        species = [sm.Species("e", -1.0), sm.Species("N2+", 1.0), sm.Species("O2+", 1.0),
+                   sm.Species("O2-", -1.0), sm.Species("O-", -1.0)]
+        m = sm.StreamerModel(3, species=species, alpha=sm.baseline_alpha, eta=sm.baseline_eta,
+                             reactions=reactions, photoi_modes=3)
+        m.photoi_species_index = 2   # photoionization produces O2+
+        return m
+
+    def seed_center(self):
+        return (1.5e-2, 1.5e-2, 1.7e-2)
+
+
+WORKLOADS = {"cyl2d": Cyl2d, "3d": Streamer3d}
