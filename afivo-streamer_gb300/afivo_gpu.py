@@ -113,6 +113,7 @@ class TransportDesc(C.Structure):
         ("lt_col_mobility", C.c_int), ("lt_col_diffusion", C.c_int), ("lt_col_alpha", C.c_int),
         ("n_reactions", C.c_int), ("reactions", Reaction * AFG_MAX_REACTIONS),
         ("dt_chemistry_nmin", C.c_double), ("dt_chemistry_limit_loss", C.c_int),
+        ("precision", C.c_int),
     ]
 
 
@@ -230,6 +231,8 @@ def load_library(path: str = LIB_PATH):
         "afg_kernel_timing": (C.c_int, [P, C.c_int]),
         "afg_kernel_stats": (C.c_int, [P, C.POINTER(C.c_longlong), _DP, _DP]),
         "afg_maxabs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, _DP]),
+        "afg_host_register": (C.c_int, [P, C.c_void_p, C.c_size_t]),
+        "afg_host_unregister": (C.c_int, [P, C.c_void_p]),
         "afg_sync": (C.c_int, [P]),
         "afg_launch_count": (C.c_longlong, [P]),
     }
@@ -247,16 +250,20 @@ class AfgError(RuntimeError):
         self.code = code
 
 
-def box_pointers(cc: np.ndarray):
+class BoxPointers:
     """Per-box pointer array for a host array laid out like the reference's
-    boxes: cc[n_boxes, n_var, ...] (box%cc of box id at row id-1)."""
-    nb = cc.shape[0]
-    stride = cc.strides[0]
-    base = cc.ctypes.data
-    arr = (_DP * nb)()
-    for b in range(nb):
-        arr[b] = C.cast(base + b * stride, _DP)
-    return arr
+    boxes: cc[n_boxes, n_var, ...] (box%cc of box id at row id-1).  Holds a
+    reference to the array so the pointers stay valid."""
+
+    def __init__(self, cc: np.ndarray):
+        self.array = cc
+        self.addr = (np.uint64(cc.ctypes.data) +
+                     np.arange(cc.shape[0], dtype=np.uint64) * np.uint64(cc.strides[0]))
+        self.ptr = self.addr.ctypes.data_as(C.POINTER(_DP))
+
+
+def box_pointers(cc: np.ndarray):
+    return BoxPointers(cc)
 
 
 class Context:
@@ -297,35 +304,61 @@ class Context:
         self.check(self.lib.afg_tree_sync(self.ptr, C.byref(self._tree_holder.desc),
                                           n_var_cell, n_var_face), "afg_tree_sync")
 
-    def upload(self, cc: np.ndarray, ivs=None):
-        """Upload variables ivs (1-based) from host boxes cc[n, n_var, ...]."""
+    def upload(self, cc: np.ndarray, ivs=None, first_iv=1):
+        """Upload variables ivs (1-based) from host boxes cc[n, n_var, ...];
+        column v of cc holds variable first_iv + v."""
         cc = np.ascontiguousarray(cc, dtype=np.float64)
         S = int(np.prod(cc.shape[2:]))
-        ptrs = box_pointers(cc)
-        for iv in (ivs if ivs is not None else range(1, cc.shape[1] + 1)):
-            self.check(self.lib.afg_cc_upload(self.ptr, iv, ptrs, (iv - 1) * S), "afg_cc_upload")
+        bp = box_pointers(cc)
+        for iv in (ivs if ivs is not None else range(first_iv, first_iv + cc.shape[1])):
+            self.check(self.lib.afg_cc_upload(self.ptr, iv, bp.ptr, (iv - first_iv) * S), "afg_cc_upload")
 
-    def download(self, cc: np.ndarray, ivs=None):
-        """Download variables ivs into host boxes cc[n, n_var, ...] (in place)."""
+    def download(self, cc: np.ndarray, ivs=None, first_iv=1):
+        """Download variables ivs into host boxes cc[n, n_var, ...] (in place);
+        column v of cc receives variable first_iv + v."""
         assert cc.flags.c_contiguous and cc.dtype == np.float64
         S = int(np.prod(cc.shape[2:]))
-        ptrs = box_pointers(cc)
-        for iv in (ivs if ivs is not None else range(1, cc.shape[1] + 1)):
-            self.check(self.lib.afg_cc_download(self.ptr, iv, ptrs, (iv - 1) * S), "afg_cc_download")
+        bp = box_pointers(cc)
+        for iv in (ivs if ivs is not None else range(first_iv, first_iv + cc.shape[1])):
+            self.check(self.lib.afg_cc_download(self.ptr, iv, bp.ptr, (iv - first_iv) * S), "afg_cc_download")
+
+    def upload_vars(self, cc: np.ndarray, ivs, cols=None, bp=None):
+        """Upload column cols[v] (default v) of cc[n, m, ...] into variable ivs[v]."""
+        S = int(np.prod(cc.shape[2:]))
+        bp = bp or box_pointers(cc)
+        for v, iv in enumerate(ivs):
+            col = v if cols is None else cols[v]
+            self.check(self.lib.afg_cc_upload(self.ptr, iv, bp.ptr, col * S), "afg_cc_upload")
+
+    def download_vars(self, cc: np.ndarray, ivs, cols=None, bp=None):
+        """Download variable ivs[v] into column cols[v] (default v) of cc[n, m, ...]."""
+        S = int(np.prod(cc.shape[2:]))
+        bp = bp or box_pointers(cc)
+        for v, iv in enumerate(ivs):
+            col = v if cols is None else cols[v]
+            self.check(self.lib.afg_cc_download(self.ptr, iv, bp.ptr, col * S), "afg_cc_download")
 
     def upload_fc(self, fc: np.ndarray, ivfs=None):
         fc = np.ascontiguousarray(fc, dtype=np.float64)
         F = int(np.prod(fc.shape[2:]))
-        ptrs = box_pointers(fc)
+        bp = box_pointers(fc)
         for iv in (ivfs if ivfs is not None else range(1, fc.shape[1] + 1)):
-            self.check(self.lib.afg_fc_upload(self.ptr, iv, ptrs, (iv - 1) * F), "afg_fc_upload")
+            self.check(self.lib.afg_fc_upload(self.ptr, iv, bp.ptr, (iv - 1) * F), "afg_fc_upload")
 
     def download_fc(self, fc: np.ndarray, ivfs=None):
         assert fc.flags.c_contiguous and fc.dtype == np.float64
         F = int(np.prod(fc.shape[2:]))
-        ptrs = box_pointers(fc)
+        bp = box_pointers(fc)
         for iv in (ivfs if ivfs is not None else range(1, fc.shape[1] + 1)):
-            self.check(self.lib.afg_fc_download(self.ptr, iv, ptrs, (iv - 1) * F), "afg_fc_download")
+            self.check(self.lib.afg_fc_download(self.ptr, iv, bp.ptr, (iv - 1) * F), "afg_fc_download")
+
+    def host_register(self, arr: np.ndarray):
+        """Page-lock the memory of a C-contiguous host array."""
+        assert arr.flags.c_contiguous
+        self.check(self.lib.afg_host_register(self.ptr, arr.ctypes.data, arr.nbytes), "afg_host_register")
+
+    def host_unregister(self, arr: np.ndarray):
+        self.check(self.lib.afg_host_unregister(self.ptr, arr.ctypes.data), "afg_host_unregister")
 
     def set_cc_methods(self, iv, bc_type, bc_val=None, rb=RB_MG_SIDES):
         g = gc_desc(bc_type, bc_val, rb)

@@ -18,7 +18,7 @@ UNITS = ["afg_runtime.cu", "afg_noalloc.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3",
               "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off",
-              "--expt-relaxed-constexpr"]
+              "--expt-relaxed-constexpr", "-Xcompiler", "-fopenmp"]
 
 
 def _nvcc():
@@ -57,7 +57,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     with ThreadPoolExecutor(max_workers=max(1, len(UNITS))) as ex:
         objs = list(ex.map(compile_unit, UNITS))
-    cmd = [nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", LIB] + objs + ["-lcudart"]
+    cmd = [nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", LIB] + objs + ["-lcudart", "-lgomp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

@@ -33,7 +33,54 @@ struct KTree {
   // m_af_types.f90:1199-1211) and child weights 1 -/+ dr/(4r)
   // (af_cyl_child_weights, 1187-1196); null for Cartesian trees
   const double* geo;
+  // 1/dr per box and dimension, computed on the host ([n][D]); a correctly
+  // rounded division, so identical to 1 / dr evaluated on the device
+  const double* idr;
+  const float* idrf;  // the same rounded to FP32
 };
+
+// Double <-> float conversions by IEEE-754 bit manipulation, for the FP32
+// arithmetic of the mixed-precision kernels: integer instructions only, so
+// the conversions do not queue on the FP64 pipe.  d2f truncates the mantissa
+// toward zero (error below one FP32 ulp) and returns signed zero for
+// magnitudes below the FP32 normal range and signed infinity above it (NaN
+// stays NaN); f2d is exact for normal numbers, zero, infinity and NaN and
+// flushes FP32 subnormals to signed zero.
+__device__ __forceinline__ float d2f(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7FFu);
+  const unsigned mant = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  unsigned r;
+  if (e == 0x7FF)
+    r = sign | 0x7F800000u | (mant != 0u || (lo & 0x1FFFFFFFu) != 0u ? 0x400000u : 0u);
+  else if (e - 896 >= 255)
+    r = sign | 0x7F800000u;
+  else if (e - 896 <= 0)
+    r = sign;
+  else
+    r = sign | ((unsigned)(e - 896) << 23) | mant;
+  return __uint_as_float(r);
+}
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned sign = u & 0x80000000u;
+  const unsigned e = (u >> 23) & 0xFFu;
+  const unsigned mant = u & 0x7FFFFFu;
+  unsigned hi, lo;
+  if (e == 0u) {
+    hi = sign;
+    lo = 0u;
+  } else if (e == 0xFFu) {
+    hi = sign | 0x7FF00000u | (mant >> 3);
+    lo = mant << 29;
+  } else {
+    hi = sign | ((e + 896u) << 20) | (mant >> 3);
+    lo = mant << 29;
+  }
+  return __hiloint2double((int)hi, (int)lo);
+}
 
 // Operator coefficients of one multigrid slot, precomputed per box:
 // cb[n][8] = c(1..2D+1) of mg_box_lpl_stencil and 1/c(1); for cylindrical
@@ -69,6 +116,16 @@ __device__ __forceinline__ int child_offset(const KTree& t, int slot, int d) {
 }
 
 // Non-negative doubles order like their bit patterns: max via atomicMax.
+// mx = max(mx, |v|) for non-NaN values; for doubles the magnitudes are
+// compared as integers (the IEEE-754 order of non-negative numbers), which
+// keeps the comparison off the FP64 pipe and returns the same value.
+__device__ __forceinline__ void acc_absmax(double& mx, double v) {
+  const long long b = __double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFll;
+  const long long m = __double_as_longlong(mx);
+  mx = __longlong_as_double(b > m ? b : m);
+}
+__device__ __forceinline__ void acc_absmax(float& mx, float v) { mx = fmaxf(mx, fabsf(v)); }
+
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
   atomicMax(addr, (unsigned long long)__double_as_longlong(v));
 }

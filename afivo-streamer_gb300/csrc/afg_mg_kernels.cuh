@@ -174,8 +174,7 @@ __global__ void __launch_bounds__(256) k_residual(KTree t, const int* __restrict
     const int x = D == 2 ? at2(n2, i, j) : at3(n2, i, j, k);
     const T res = f[x] - apply_lpl<D, CYL, T>(p, n2, i, j, k, c, k1, k2, k3);
     o[x] = res;
-    const T ar = res < T(0) ? -res : res;
-    mx = ar > mx ? ar : mx;
+    acc_absmax(mx, res);
   }
   if (maxbits != nullptr && is_leaf[slot]) {
     mx = block_max<T>(mx, sred);
@@ -445,9 +444,7 @@ __global__ void __launch_bounds__(256) k_maxabs(KTree t, const int* __restrict__
   for (int w = threadIdx.x; w < count; w += blockDim.x) {
     const int i = w % nc + 1, r = w / nc;
     const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
-    const T val = a[D == 2 ? at2(n2, i, j) : at3(n2, i, j, k)];
-    const T av = val < T(0) ? -val : val;
-    mx = av > mx ? av : mx;
+    acc_absmax(mx, a[D == 2 ? at2(n2, i, j) : at3(n2, i, j, k)]);
   }
   mx = block_max<T>(mx, sred);
   if (threadIdx.x == 0) atomic_max_nonneg(maxbits, double(mx));

@@ -15,14 +15,16 @@
 namespace afg {
 
 // r (FP64 residual on interior cells) -> r32, e32 = 0 (whole box), max |r|
-// over leaves into *maxbits.
+// over leaves into *maxbits.  The Cartesian stencil is one FMA chain (8 FP64
+// instructions per cell); r is rounded to FP32 by bit truncation and its
+// maximum taken in FP32.
 template <int D, bool CYL>
 __global__ void __launch_bounds__(256) k_defect(KTree t, const int* __restrict__ list, const double* __restrict__ phi,
                                                 const double* __restrict__ rhs, float* __restrict__ r32,
                                                 float* __restrict__ e32, MgCoef<double> mc,
                                                 const unsigned char* __restrict__ is_leaf,
                                                 unsigned long long* maxbits) {
-  __shared__ double sred[32];
+  __shared__ float sred[32];
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;
   double cd[7];
@@ -31,26 +33,36 @@ __global__ void __launch_bounds__(256) k_defect(KTree t, const int* __restrict__
   const double* f = rhs + (size_t)slot * t.S;
   float* ro = r32 + (size_t)slot * t.S;
   float* eo = e32 + (size_t)slot * t.S;
-  double mx = 0.0;
-  for (int x = threadIdx.x; x < t.S; x += blockDim.x) {
-    eo[x] = 0.0f;
-    const int i = x % n2, rr = x / n2;
-    const int j = D == 2 ? rr : rr % n2, k = D == 2 ? 0 : rr / n2;
-    const bool interior = i >= 1 && i <= nc && j >= 1 && j <= nc && (D == 2 || (k >= 1 && k <= nc));
-    if (!interior) continue;
-    double k1 = 0, k2 = 0, k3 = 0;
-    if (CYL) {
-      const double* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
-      k1 = y[0]; k2 = y[1]; k3 = y[2];
+  for (int x = threadIdx.x; x < t.S; x += blockDim.x) eo[x] = 0.0f;
+  float mx = 0.0f;
+  const int ncell = D == 2 ? nc * nc : nc * nc * nc;
+  for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
+    const int i = w % nc + 1, r = w / nc;
+    const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
+    double lp;
+    int x;
+    if (D == 2) {
+      x = at2(n2, i, j);
+      if (CYL) {
+        const double* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
+        lp = fma(cd[4], p[x + n2], fma(cd[3], p[x - n2], fma(y[2], p[x + 1], fma(y[1], p[x - 1], y[0] * p[x]))));
+      } else {
+        lp = fma(cd[4], p[x + n2], fma(cd[3], p[x - n2], fma(cd[2], p[x + 1], fma(cd[1], p[x - 1], cd[0] * p[x]))));
+      }
+    } else {
+      x = at3(n2, i, j, k);
+      const int sk = n2 * n2;
+      lp = fma(cd[6], p[x + sk],
+               fma(cd[5], p[x - sk],
+                   fma(cd[4], p[x + n2], fma(cd[3], p[x - n2], fma(cd[2], p[x + 1], fma(cd[1], p[x - 1], cd[0] * p[x]))))));
     }
-    const double res = f[x] - apply_lpl<D, CYL, double>(p, n2, i, j, k, cd, k1, k2, k3);
-    ro[x] = float(res);
-    const double ar = fabs(res);
-    mx = ar > mx ? ar : mx;
+    const float res = d2f(f[x] - lp);
+    ro[x] = res;
+    mx = fmaxf(mx, fabsf(res));
   }
   if (is_leaf[slot]) {
-    mx = block_max<double>(mx, sred);
-    if (threadIdx.x == 0) atomic_max_nonneg(maxbits, mx);
+    mx = block_max<float>(mx, sred);
+    if (threadIdx.x == 0) atomic_max_nonneg(maxbits, f2d(mx));
   }
 }
 
@@ -60,7 +72,7 @@ __global__ void __launch_bounds__(256) k_add_correction(int S, const int* __rest
   const int slot = list[blockIdx.x];
   double* p = phi + (size_t)slot * S;
   const float* e = e32 + (size_t)slot * S;
-  for (int x = threadIdx.x; x < S; x += blockDim.x) p[x] = p[x] + double(e[x]);
+  for (int x = threadIdx.x; x < S; x += blockDim.x) p[x] = p[x] + f2d(e[x]);
 }
 
 }  // namespace afg

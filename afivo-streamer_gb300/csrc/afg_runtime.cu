@@ -73,7 +73,8 @@ struct afg_ctx {
   // device tables
   int *d_parent = nullptr, *d_children = nullptr, *d_nbr = nullptr, *d_pnb = nullptr, *d_nbmat = nullptr,
       *d_ix = nullptr;
-  double *d_rmin = nullptr, *d_dr = nullptr;
+  double *d_rmin = nullptr, *d_dr = nullptr, *d_idr = nullptr;
+  float* d_idrf = nullptr;
   double* d_geo = nullptr;  // cylindrical geometry table (KTree::geo)
   int* d_lists = nullptr;  // all level lists concatenated
   std::vector<size_t> off_ids, off_leaves, off_parents;  // per level offsets into d_lists
@@ -101,6 +102,7 @@ struct afg_ctx {
   // accounting and timing
   long long ctr[4] = {0, 0, 0, 0};
   cudaEvent_t ev[64] = {};
+  cudaEvent_t xfer_ev[2] = {};  // download pipeline
   void* flush_buf = nullptr;
   size_t flush_bytes = 0;
   int kt_class = 0;
@@ -176,6 +178,8 @@ static KTree ktree(const afg_ctx* c) {
   t.r_min = c->d_rmin;
   t.dr = c->d_dr;
   t.geo = c->d_geo;
+  t.idr = c->d_idr;
+  t.idrf = c->d_idrf;
   return t;
 }
 
@@ -223,7 +227,7 @@ static void clear_graphs(afg_ctx* c) {
 static void free_tree(afg_ctx* c) {
   clear_graphs(c);
   dfree(c->d_parent); dfree(c->d_children); dfree(c->d_nbr); dfree(c->d_pnb); dfree(c->d_nbmat);
-  dfree(c->d_ix); dfree(c->d_rmin); dfree(c->d_dr); dfree(c->d_lists); dfree(c->d_is_leaf); dfree(c->d_geo);
+  dfree(c->d_ix); dfree(c->d_rmin); dfree(c->d_dr); dfree(c->d_idr); dfree(c->d_idrf); dfree(c->d_lists); dfree(c->d_is_leaf); dfree(c->d_geo);
   dfree(c->d_cslot); dfree(c->d_ccell);
   for (auto& p : c->cc) dfree(p);
   for (auto& p : c->fc) dfree(p);
@@ -629,6 +633,7 @@ int afg_init(int device, afg_ctx** out) {
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   CK(dalloc(&ctx->d_max, 8));
   CK(cudaMallocHost((void**)&ctx->h_max, 8 * sizeof(unsigned long long)));
+  for (auto& e : ctx->xfer_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   *out = ctx;
   return AFG_OK;
 }
@@ -641,6 +646,8 @@ int afg_finalize(afg_ctx* ctx) {
   for (auto& e : ctx->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : ctx->kt_ev) cudaEventDestroy(e);
+  for (auto& e : ctx->xfer_ev)
+    if (e) cudaEventDestroy(e);
   if (ctx->flush_buf) cudaFree(ctx->flush_buf);
   dfree(ctx->d_max);
   if (ctx->h_max) cudaFreeHost(ctx->h_max);
@@ -807,6 +814,18 @@ int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_va
   CK(cudaMemcpy(ctx->d_ix, t->ix, sizeof(int) * (size_t)n * D, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_rmin, t->r_min, sizeof(double) * (size_t)n * D, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_dr, t->dr, sizeof(double) * (size_t)n * D, cudaMemcpyHostToDevice));
+  {
+    std::vector<double> idr((size_t)n * D);
+    std::vector<float> idrf((size_t)n * D);
+    for (size_t q = 0; q < idr.size(); q++) {
+      idr[q] = 1.0 / t->dr[q];
+      idrf[q] = (float)idr[q];
+    }
+    CK(dalloc(&ctx->d_idr, idr.size()));
+    CK(dalloc(&ctx->d_idrf, idrf.size()));
+    CK(cudaMemcpy(ctx->d_idr, idr.data(), sizeof(double) * idr.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_idrf, idrf.data(), sizeof(float) * idrf.size(), cudaMemcpyHostToDevice));
+  }
   if (!lists.empty()) CK(cudaMemcpy(ctx->d_lists, lists.data(), sizeof(int) * lists.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_is_leaf, is_leaf.data(), n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_cslot, cslot.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
@@ -849,62 +868,134 @@ static int check_var(afg_ctx* ctx, int iv) {
   return AFG_OK;
 }
 
+/* ---- host <-> device transfers ------------------------------------------ */
+
+// Boxes per staged chunk: the gather of chunk c+1 overlaps the DMA of chunk c.
+static const size_t kXferChunkBytes = 32u << 20;
+
+static bool is_page_locked(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// All boxes present, equally spaced by a pitch >= E elements, and the whole
+// span page-locked: one pitched DMA moves every box with no host copy.
+static bool pitched_boxes(int n, size_t E, const double* const* box, long long off, size_t* pitch) {
+  if (n <= 0 || !box[0]) return false;
+  if (n == 1) {
+    *pitch = E;
+  } else {
+    if (!box[1] || box[1] <= box[0]) return false;
+    const ptrdiff_t d = box[1] - box[0];
+    if ((size_t)d < E) return false;
+    for (int b = 2; b < n; b++)
+      if (!box[b] || box[b] - box[b - 1] != d) return false;
+    *pitch = (size_t)d;
+  }
+  return is_page_locked(box[0] + off) && is_page_locked(box[n - 1] + off + E - 1);
+}
+
+// Boxes 0..n-1 of a device pool with E elements per box <- host box arrays
+// (null entries skipped: their device data is left as it is).
+static int h2d_boxes(afg_ctx* ctx, double* dst, size_t E, const double* const* box, long long off) {
+  const int n = ctx->n_boxes;
+  size_t pitch = 0;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (pitched_boxes(n, E, box, off, &pitch)) {
+    CK(cudaMemcpy2DAsync(dst, E * sizeof(double), box[0] + off, pitch * sizeof(double), E * sizeof(double), n,
+                         cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return AFG_OK;
+  }
+  const int per = (int)std::max<size_t>(1, kXferChunkBytes / (E * sizeof(double)));
+  for (int b0 = 0; b0 < n; b0 += per) {
+    const int b1 = std::min(n, b0 + per);
+#pragma omp parallel for schedule(static)
+    for (int b = b0; b < b1; b++)
+      if (box[b]) memcpy(ctx->h_stage + (size_t)b * E, box[b] + off, sizeof(double) * E);
+    int b = b0;
+    while (b < b1) {
+      if (!box[b]) { b++; continue; }
+      int e = b;
+      while (e < b1 && box[e]) e++;
+      CK(cudaMemcpyAsync(dst + (size_t)b * E, ctx->h_stage + (size_t)b * E, sizeof(double) * E * (e - b),
+                         cudaMemcpyHostToDevice, ctx->stream));
+      b = e;
+    }
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return AFG_OK;
+}
+
+// Host box arrays <- boxes 0..n-1 of a device pool (null entries skipped).
+static int d2h_boxes(afg_ctx* ctx, const double* src, size_t E, double* const* box, long long off) {
+  const int n = ctx->n_boxes;
+  size_t pitch = 0;
+  if (pitched_boxes(n, E, box, off, &pitch)) {
+    CK(cudaMemcpy2DAsync(box[0] + off, pitch * sizeof(double), src, E * sizeof(double), E * sizeof(double), n,
+                         cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return AFG_OK;
+  }
+  const int per = (int)std::max<size_t>(1, kXferChunkBytes / (E * sizeof(double)));
+  const int nch = (n + per - 1) / per;
+  auto issue = [&](int c) -> cudaError_t {
+    const int b0 = c * per, b1 = std::min(n, b0 + per);
+    cudaError_t e = cudaMemcpyAsync(ctx->h_stage + (size_t)b0 * E, src + (size_t)b0 * E,
+                                    sizeof(double) * E * (b1 - b0), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) return e;
+    return cudaEventRecord(ctx->xfer_ev[c & 1], ctx->stream);
+  };
+  CK(issue(0));
+  for (int c = 0; c < nch; c++) {
+    if (c + 1 < nch) CK(issue(c + 1));
+    CK(cudaEventSynchronize(ctx->xfer_ev[c & 1]));
+    const int b0 = c * per, b1 = std::min(n, b0 + per);
+#pragma omp parallel for schedule(static)
+    for (int b = b0; b < b1; b++)
+      if (box[b]) memcpy(box[b] + off, ctx->h_stage + (size_t)b * E, sizeof(double) * E);
+  }
+  return AFG_OK;
+}
+
 int afg_cc_upload(afg_ctx* ctx, int iv, const double* const* box_cc, long long off) {
   RC(check_var(ctx, iv));
   if (!box_cc) return fail(ctx, AFG_ERR_ARG, "null box_cc");
-  const size_t S = ctx->S;
-  CK(cudaStreamSynchronize(ctx->stream));
-  double* dst = ctx->cc[iv - 1];
-  // runs of consecutive non-null boxes are staged and copied in one call
-  int b = 0;
-  while (b < ctx->n_boxes) {
-    if (!box_cc[b]) { b++; continue; }
-    int e = b;
-    while (e < ctx->n_boxes && box_cc[e]) {
-      memcpy(ctx->h_stage + (size_t)(e - b) * S, box_cc[e] + off, sizeof(double) * S);
-      e++;
-    }
-    CK(cudaMemcpyAsync(dst + (size_t)b * S, ctx->h_stage, sizeof(double) * S * (e - b), cudaMemcpyHostToDevice,
-                       ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
-    b = e;
-  }
-  return AFG_OK;
+  return h2d_boxes(ctx, ctx->cc[iv - 1], ctx->S, box_cc, off);
 }
 
 int afg_cc_download(afg_ctx* ctx, int iv, double* const* box_cc, long long off) {
   RC(check_var(ctx, iv));
   if (!box_cc) return fail(ctx, AFG_ERR_ARG, "null box_cc");
-  const size_t S = ctx->S;
-  CK(cudaMemcpyAsync(ctx->h_stage, ctx->cc[iv - 1], sizeof(double) * S * ctx->n_boxes, cudaMemcpyDeviceToHost,
-                     ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  for (int b = 0; b < ctx->n_boxes; b++)
-    if (box_cc[b]) memcpy(box_cc[b] + off, ctx->h_stage + (size_t)b * S, sizeof(double) * S);
-  return AFG_OK;
+  return d2h_boxes(ctx, ctx->cc[iv - 1], ctx->S, box_cc, off);
 }
 
 int afg_fc_upload(afg_ctx* ctx, int ivf, const double* const* box_fc, long long off) {
   if (!ctx || !ctx->have_tree) return AFG_ERR_STATE;
   if (ivf < 1 || ivf > ctx->n_var_face || !box_fc) return fail(ctx, AFG_ERR_ARG, "bad fc variable %d", ivf);
-  const size_t F = (size_t)ctx->D * ctx->NF;
-  for (int b = 0; b < ctx->n_boxes; b++)
-    if (box_fc[b]) memcpy(ctx->h_stage + (size_t)b * F, box_fc[b] + off, sizeof(double) * F);
-  CK(cudaMemcpyAsync(ctx->fc[ivf - 1], ctx->h_stage, sizeof(double) * F * ctx->n_boxes, cudaMemcpyHostToDevice,
-                     ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  return AFG_OK;
+  return h2d_boxes(ctx, ctx->fc[ivf - 1], (size_t)ctx->D * ctx->NF, box_fc, off);
 }
 
 int afg_fc_download(afg_ctx* ctx, int ivf, double* const* box_fc, long long off) {
   if (!ctx || !ctx->have_tree) return AFG_ERR_STATE;
   if (ivf < 1 || ivf > ctx->n_var_face || !box_fc) return fail(ctx, AFG_ERR_ARG, "bad fc variable %d", ivf);
-  const size_t F = (size_t)ctx->D * ctx->NF;
-  CK(cudaMemcpyAsync(ctx->h_stage, ctx->fc[ivf - 1], sizeof(double) * F * ctx->n_boxes, cudaMemcpyDeviceToHost,
-                     ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  for (int b = 0; b < ctx->n_boxes; b++)
-    if (box_fc[b]) memcpy(box_fc[b] + off, ctx->h_stage + (size_t)b * F, sizeof(double) * F);
+  return d2h_boxes(ctx, ctx->fc[ivf - 1], (size_t)ctx->D * ctx->NF, box_fc, off);
+}
+
+int afg_host_register(afg_ctx* ctx, void* ptr, size_t bytes) {
+  if (!ctx || !ptr || bytes == 0) return AFG_ERR_ARG;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+  return AFG_OK;
+}
+
+int afg_host_unregister(afg_ctx* ctx, void* ptr) {
+  if (!ctx || !ptr) return AFG_ERR_ARG;
+  CK(cudaHostUnregister(ptr));
   return AFG_OK;
 }
 

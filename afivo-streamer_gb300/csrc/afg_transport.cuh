@@ -12,11 +12,14 @@ constexpr double kSiToTd = 1e21;               // SI_to_Townsend (src/m_gas.f90:
 constexpr double kEps0 = 8.8541878128e-12;     // UC_eps0 (src/m_units_constants.f90:13)
 constexpr double kElem = 1.602176634e-19;      // UC_elem_charge (16)
 
+struct Reac32;
 struct TransportState {
   bool ready = false;
   afg_transport_desc d{};
   double* d_lt = nullptr;              // [n_cols][n_points]
   afg_reaction* d_reactions = nullptr; // [n_reactions]
+  float* d_ltf = nullptr;              // the table in FP32 (mixed precision)
+  Reac32* d_reac32 = nullptr;          // reactions in FP32 form
   // task lists (slots): leaves with a refinement boundary and a parent;
   // (coarse box, face) pairs for af_consistent_fluxes
   int* d_rrb = nullptr;
@@ -28,6 +31,8 @@ struct TransportState {
 inline void transport_free(TransportState& s) {
   if (s.d_lt) cudaFree(s.d_lt);
   if (s.d_reactions) cudaFree(s.d_reactions);
+  if (s.d_ltf) cudaFree(s.d_ltf);
+  if (s.d_reac32) cudaFree(s.d_reac32);
   if (s.d_rrb) cudaFree(s.d_rrb);
   if (s.d_cflux) cudaFree(s.d_cflux);
   s = TransportState();
@@ -279,7 +284,7 @@ __global__ void __launch_bounds__(256) k_flux(KTree t, const int* __restrict__ l
     const int dim = w / nfaces, fw = w - dim * nfaces;
     const int f = fw % nf1 + 1, ln = fw / nf1;  // face index along dim, line index
     const int jj = ln % nc + 1, kk = D == 3 ? ln / nc + 1 : 1;
-    const double inv_dx = 1 / t.dr[slot * D + dim];
+    const double inv_dx = t.idr[slot * D + dim];
     int fidx;
     if (D == 2) fidx = dim == 0 ? fc_at(nf1, f, jj, 1) : fc_at(nf1, jj, f, 1);
     else if (dim == 0) fidx = fc_at(nf1, f, jj, kk);
@@ -336,7 +341,7 @@ __global__ void __launch_bounds__(256) k_flux(KTree t, const int* __restrict__ l
     const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 1 : r / nc + 1;
     double cfl = 0.0;
     for (int dim = 0; dim < D; dim++) {
-      const double inv_dx = 1 / t.dr[slot * D + dim];
+      const double inv_dx = t.idr[slot * D + dim];
       int c, ln;
       if (D == 2) { c = dim == 0 ? i : j; ln = dim == 0 ? j - 1 : i - 1; }
       else if (dim == 0) { c = i; ln = (j - 1) + nc * (k - 1); }
@@ -425,16 +430,47 @@ struct UpdateArgs {
   unsigned long long* min_chem;  // bits of a non-negative double (atomicMin)
 };
 
+// x**c for the exponents of the analytic forms: c == 1 returns x, which is
+// what pow(x, 1) returns exactly, and skips the FP64 pow.
+__device__ __forceinline__ double pow_c(double x, double c) { return c == 1.0 ? x : pow(x, c); }
+__device__ __forceinline__ float pow_c(float x, float c) { return c == 1.0f ? x : powf(x, c); }
+
+// Rate coefficient of one reaction (get_rates, src/m_chemistry.f90:672-760).
+// F32: the argument of the exponential and the exponential in FP32 (the
+// mixed-precision transport); the factors c0 * c1 stay FP64.
+template <bool F32>
 __device__ __forceinline__ double rate_of(const LtDev& lt, const afg_reaction& r, double td, int ix, double w) {
   const double c0 = r.rate_factor;
   switch (r.rate_type) {
     case AFG_RATE_TABULATED_FIELD: return c0 * lt_col(lt, r.lt_col, ix, w);
     case AFG_RATE_CONSTANT: return c0 * r.c[0];
     case AFG_RATE_LINEAR: return c0 * r.c[0] * (td - r.c[1]);
-    case AFG_RATE_EXP_V1: { const double q = r.c[1] / (r.c[2] + td); return c0 * r.c[0] * exp(-(q * q)); }
-    case AFG_RATE_EXP_V2: { const double q = td / r.c[1]; return c0 * r.c[0] * exp(-(q * q)); }
-    case AFG_RATE_K13: return c0 * r.c[0] * exp(-pow(r.c[1] / (r.c[2] + td), r.c[3]));
-    case AFG_RATE_K14: return c0 * r.c[0] * exp(-pow(td / r.c[1], r.c[2]));
+    case AFG_RATE_EXP_V1:
+      if (F32) {
+        const float q = (float)r.c[1] / ((float)r.c[2] + (float)td);
+        return c0 * r.c[0] * (double)expf(-(q * q));
+      } else {
+        const double q = r.c[1] / (r.c[2] + td);
+        return c0 * r.c[0] * exp(-(q * q));
+      }
+    case AFG_RATE_EXP_V2:
+      if (F32) {
+        const float q = (float)td / (float)r.c[1];
+        return c0 * r.c[0] * (double)expf(-(q * q));
+      } else {
+        const double q = td / r.c[1];
+        return c0 * r.c[0] * exp(-(q * q));
+      }
+    case AFG_RATE_K13:
+      if (F32)
+        return c0 * r.c[0] * (double)expf(-pow_c((float)r.c[1] / ((float)r.c[2] + (float)td), (float)r.c[3]));
+      else
+        return c0 * r.c[0] * exp(-pow_c(r.c[1] / (r.c[2] + td), r.c[3]));
+    case AFG_RATE_K14:
+      if (F32)
+        return c0 * r.c[0] * (double)expf(-pow_c((float)td / (float)r.c[1], (float)r.c[2]));
+      else
+        return c0 * r.c[0] * exp(-pow_c(td / r.c[1], r.c[2]));
   }
   return 0;
 }
@@ -491,7 +527,7 @@ __global__ void __launch_bounds__(128) k_update(KTree t, const int* __restrict__
     lt_loc(a.lt, td, ix, lw);
     for (int n = 0; n < a.n_reactions; n++) {
       const afg_reaction& rc = a.reactions[n];
-      double rate = rate_of(a.lt, rc, td, ix, lw);
+      double rate = rate_of<false>(a.lt, rc, td, ix, lw);
       double prod = 1.0;
       for (int q = 0; q < rc.n_in; q++) prod = prod * pick<NSMAX>(dens, rc.ix_in[q]);
       rate = rate * prod;
@@ -589,7 +625,7 @@ __global__ void __launch_bounds__(256) k_field_grad(KTree t, const int* __restri
     const int dim = w / nfaces, fw = w - dim * nfaces;
     const int f = fw % nf1 + 1, ln = fw / nf1;
     const int jj = ln % nc + 1, kk = D == 3 ? ln / nc + 1 : 1;
-    const double inv_dr = -1.0 / t.dr[slot * D + dim];
+    const double inv_dr = -t.idr[slot * D + dim];
     int fidx, c1, c0;
     if (D == 2) {
       if (dim == 0) { fidx = fc_at(nf1, f, jj, 1); c1 = at2(n2, f, jj); c0 = at2(n2, f - 1, jj); }

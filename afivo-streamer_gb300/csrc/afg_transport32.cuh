@@ -1,0 +1,422 @@
+// afg_transport32.cuh -- mixed-precision variants of the transport and field
+// kernels (transport precision AFG_MIXED).
+//
+// GB300 issues FP64 at a small fraction of its FP32 rate, so a kernel that
+// does more than about one FP64 instruction per 24 bytes it moves is bound
+// by the FP64 pipe, not by HBM.  These kernels keep the state in FP64 (the
+// densities, |E|, E and the fluxes are read and written as FP64) but do the
+// per-cell arithmetic in FP32, except where it cancels:
+//   - fluxes: velocities, diffusion, the Koren reconstruction and the flux
+//     itself in FP32 (the two-layer ghost values stay FP64, as written back);
+//   - chemistry: rates, products, sources and the dt limit in FP32; the new
+//     density is n0 + sum_m w_m (n_m - n0) + dt (sources - div flux), with the
+//     differences of states and the final sum in FP64 (weights summing to 1);
+//   - field: E = -(phi_1 - phi_0)/dx with the potential difference in FP64,
+//     the scaling and |E| in FP32;
+//   - charge density: FP64 (n_+ - n_- cancels), interior cells only.
+// The same routines of the reference are cited at the FP64 kernels.
+#pragma once
+#include "afg_transport.cuh"
+
+namespace afg {
+
+struct LtDevF {
+  const float* y;  // [n_cols][n]
+  int n;
+  float x_min, inv_fac;
+};
+
+__device__ __forceinline__ void lt_loc_f(const LtDevF& lt, float x, int& ix, float& w) {
+  const float frac = (x - lt.x_min) * lt.inv_fac;
+  if (frac <= 0.0f) {
+    ix = 1;
+    w = 1.0f;
+  } else if (frac >= (float)(lt.n - 1)) {
+    ix = lt.n - 1;
+    w = 0.0f;
+  } else {
+    ix = (int)ceilf(frac);
+    w = (float)ix - frac;
+  }
+}
+__device__ __forceinline__ float lt_col_f(const LtDevF& lt, int col, int ix, float w) {
+  const float* y = lt.y + (size_t)col * lt.n;
+  return w * y[ix - 1] + (1.0f - w) * y[ix];
+}
+
+__device__ __forceinline__ float koren_f(float a, float b) {
+  const float aa = a * a, ab = a * b;
+  if (ab <= 0.0f) return 0.0f;
+  if (aa <= 0.25f * ab) return 2.0f * a;
+  if (aa <= 2.5f * ab) return (b + 2.0f * a) * (1.0f / 3.0f);
+  return 2.0f * b;
+}
+
+struct FluxArgs32 {
+  FluxArgs a;       // pointers and FP64 parameters (ghost layers)
+  LtDevF lt;
+  float N_inv_td;   // SI_to_Townsend / N
+  float N_inv;
+  float sign[AFG_MAX_FLUX];
+  float mu_ion[AFG_MAX_FLUX];  // ion mobility (ion_mobility_N / N)
+};
+
+// flux_upwind_box with FP32 arithmetic (see k_flux for the reference lines)
+template <int D, bool CYL>
+__global__ void __launch_bounds__(256) k_flux32(KTree t, const int* __restrict__ list, FluxArgs32 a32) {
+  extern __shared__ float smf[];
+  __shared__ float sred[32];
+  const FluxArgs& a = a32.a;
+  const int slot = list[blockIdx.x];
+  const int nc = t.nc, n2 = t.n2, m = nc + 4, nf1 = nc + 1;
+  const int tile = D == 2 ? m * m : m * m * m;
+  const int nfaces = D == 2 ? nc * nf1 : nc * nc * nf1;
+  float* big = smf;                      // [nf][tile]
+  float* vf = smf + a.nf * tile;         // [D][nfaces]
+  float* df = vf + D * nfaces;           // [D][nfaces]
+  float* Es = df + D * nfaces;           // [S] cell |E| with ghosts
+  for (int s = 0; s < a.nf; s++) {
+    const double* src = a.n[s] + (size_t)slot * t.S;
+    for (int x = threadIdx.x; x < t.S; x += blockDim.x) {
+      const int i = x % n2, r = x / n2;
+      const int j = D == 2 ? r : r % n2, k = D == 2 ? 0 : r / n2;
+      big[s * tile + big_at<D>(m, i, j, k)] = d2f(src[x]);
+    }
+  }
+  {
+    const double* E = a.E + (size_t)slot * t.S;
+    for (int x = threadIdx.x; x < t.S; x += blockDim.x) Es[x] = d2f(E[x]);
+  }
+  __syncthreads();
+  const int nface = D == 2 ? nc : nc * nc;
+  for (int s = 0; s < a.nf; s++) {
+    double* dst = a.n[s] + (size_t)slot * t.S;
+    for (int w = threadIdx.x; w < 2 * D * nface * 2; w += blockDim.x) {
+      const int layer = w & 1, w2 = w >> 1;
+      const int nb = w2 / nface, pq = w2 - nb * nface;
+      const int p = pq % nc + 1, q = D == 3 ? pq / nc + 1 : 0;
+      const int d = nb >> 1;
+      const bool low = (nb & 1) == 0;
+      const double val = gc2_value<D>(t, a.n[s], slot, nb, layer, p, q, a.bc, a.limiter);
+      const int x = low ? -layer : nc + 1 + layer;
+      big[s * tile + big_face<D>(m, d, x, p, q)] = d2f(val);
+      if (layer == 0) dst[face_at<D>(n2, d, x, p, q)] = val;  // af_gc2_box writes layer 1 back
+    }
+  }
+  __syncthreads();
+  float smax = 0.0f;
+  for (int w = threadIdx.x; w < D * nfaces; w += blockDim.x) {
+    const int dim = w / nfaces, fw = w - dim * nfaces;
+    const int f = fw % nf1 + 1, ln = fw / nf1;
+    const int jj = ln % nc + 1, kk = D == 3 ? ln / nc + 1 : 1;
+    const float inv_dx = t.idrf[slot * D + dim];
+    int fidx;
+    if (D == 2) fidx = dim == 0 ? fc_at(nf1, f, jj, 1) : fc_at(nf1, jj, f, 1);
+    else if (dim == 0) fidx = fc_at(nf1, f, jj, kk);
+    else if (dim == 1) fidx = fc_at(nf1, jj, f, kk);
+    else fidx = fc_at(nf1, jj, kk, f);
+    const float Ex = d2f(a.Efc[((size_t)slot * D + dim) * t.NF + fidx]);
+    auto cidx = [&](int x) -> int {
+      if (D == 2) return dim == 0 ? at2(n2, x, jj) : at2(n2, jj, x);
+      if (dim == 0) return at3(n2, x, jj, kk);
+      if (dim == 1) return at3(n2, jj, x, kk);
+      return at3(n2, jj, kk, x);
+    };
+    auto bidx = [&](int x) -> int {
+      if (D == 2) return dim == 0 ? big_at<D>(m, x, jj, 0) : big_at<D>(m, jj, x, 0);
+      if (dim == 0) return big_at<D>(m, x, jj, kk);
+      if (dim == 1) return big_at<D>(m, jj, x, kk);
+      return big_at<D>(m, jj, kk, x);
+    };
+    const float td = 0.5f * (Es[cidx(f - 1)] + Es[cidx(f)]) * a32.N_inv_td;
+    int ix;
+    float lw;
+    lt_loc_f(a32.lt, td, ix, lw);
+    const float mu = lt_col_f(a32.lt, a.col_mu, ix, lw) * a32.N_inv;
+    const float dc = lt_col_f(a32.lt, a.col_dc, ix, lw) * a32.N_inv;
+    const float v = -mu * Ex;
+    float sigma = 0.0f;
+    for (int s = 0; s < a.nf; s++) {
+      const float* L = big + s * tile;
+      const float lm2 = L[bidx(f - 2)], lm1 = L[bidx(f - 1)], l0 = L[bidx(f)], lp1 = L[bidx(f + 1)];
+      const bool pos = a32.sign[s] * Ex > 0.0f;
+      const float u = pos ? lm1 + 0.5f * koren_f(l0 - lm1, lm1 - lm2) : l0 - 0.5f * koren_f(l0 - lm1, lp1 - l0);
+      float fl;
+      if (s == 0) {
+        fl = v * u - dc * inv_dx * (l0 - lm1);
+        sigma = mu * u;
+      } else {
+        const float vi = a32.sign[s] * a32.mu_ion[s] * Ex;
+        fl = vi * u;
+        sigma = sigma + a32.mu_ion[s] * u;
+      }
+      a.flux[s][((size_t)slot * D + dim) * t.NF + fidx] = f2d(fl);
+    }
+    smax = sigma > smax ? sigma : smax;
+    vf[w] = v;
+    df[w] = dc;
+  }
+  __syncthreads();
+  float cmax = 0.0f;
+  const int ncell = D == 2 ? nc * nc : nc * nc * nc;
+  for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
+    const int i = w % nc + 1, r = w / nc;
+    const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 1 : r / nc + 1;
+    float cfl = 0.0f;
+    for (int dim = 0; dim < D; dim++) {
+      const float inv_dx = t.idrf[slot * D + dim];
+      int c, ln;
+      if (D == 2) { c = dim == 0 ? i : j; ln = dim == 0 ? j - 1 : i - 1; }
+      else if (dim == 0) { c = i; ln = (j - 1) + nc * (k - 1); }
+      else if (dim == 1) { c = j; ln = (i - 1) + nc * (k - 1); }
+      else { c = k; ln = (i - 1) + nc * (j - 1); }
+      const int base = dim * nfaces + ln * nf1;
+      const float vmax = fmaxf(fabsf(vf[base + c]), fabsf(vf[base + c - 1]));
+      const float dmax = fmaxf(df[base + c], df[base + c - 1]);
+      cfl = cfl + (vmax * inv_dx + 2.0f * dmax * (inv_dx * inv_dx));
+    }
+    cmax = cfl > cmax ? cfl : cmax;
+  }
+  cmax = block_max<float>(cmax, sred);
+  if (threadIdx.x == 0) atomic_max_nonneg(a.max_cfl, f2d(cmax));
+  __syncthreads();
+  smax = block_max<float>(smax, sred);
+  if (threadIdx.x == 0) atomic_max_nonneg(a.max_sigma, f2d(smax));
+}
+
+// Reaction in FP32 form: rate = fa * fb * form(Td) (the factors split so that
+// a large rate_factor, e.g. N^2 of a three-body reaction, stays in range).
+struct Reac32 {
+  int rate_type, lt_col;
+  float fa, fb;      // product = rate_factor * c1 (analytic) or rate_factor (tabulated)
+  float c[4];
+  int n_in, ix_in[4], n_out, ix_out[4];
+  float mult_out[4];
+};
+
+__device__ __forceinline__ float rate32(const LtDevF& lt, const Reac32& r, float td, int ix, float w) {
+  switch (r.rate_type) {
+    case AFG_RATE_TABULATED_FIELD: return r.fb * (r.fa * lt_col_f(lt, r.lt_col, ix, w));
+    case AFG_RATE_CONSTANT: return r.fa * r.fb;
+    case AFG_RATE_LINEAR: return r.fa * r.fb * (td - r.c[1]);
+    case AFG_RATE_EXP_V1: { const float q = r.c[1] / (r.c[2] + td); return r.fa * r.fb * expf(-(q * q)); }
+    case AFG_RATE_EXP_V2: { const float q = td / r.c[1]; return r.fa * r.fb * expf(-(q * q)); }
+    case AFG_RATE_K13: return r.fa * r.fb * expf(-pow_c(r.c[1] / (r.c[2] + td), r.c[3]));
+    case AFG_RATE_K14: return r.fa * r.fb * expf(-pow_c(td / r.c[1], r.c[2]));
+  }
+  return 0.0f;
+}
+
+struct UpdateArgs32 {
+  UpdateArgs a;
+  LtDevF lt;
+  const Reac32* reactions;
+  float N_inv_td;
+  float dt;
+  float w_rel[4];   // weights of the differences n_m - n_0 (m >= 1)
+  float nmin;
+};
+
+template <int NSMAX>
+__device__ __forceinline__ float pickf(const float (&v)[NSMAX], int s) {
+  float r = 0.0f;
+#pragma unroll
+  for (int k = 0; k < NSMAX; k++)
+    if (k == s) r = v[k];
+  return r;
+}
+template <int NSMAX>
+__device__ __forceinline__ void add_tof(float (&v)[NSMAX], int s, float x) {
+#pragma unroll
+  for (int k = 0; k < NSMAX; k++)
+    if (k == s) v[k] = v[k] + x;
+}
+
+// flux_update_densities + add_source_terms with FP32 sources; the weights of
+// the previous states sum to one (forward Euler and Heun stages).
+template <int D, bool CYL, int NSMAX>
+__global__ void __launch_bounds__(128) k_update32(KTree t, const int* __restrict__ list, UpdateArgs32 u) {
+  __shared__ float sred[32];
+  const UpdateArgs& a = u.a;
+  const int slot = list[blockIdx.x];
+  const int nc = t.nc, n2 = t.n2, nf1 = nc + 1;
+  const int ncell = D == 2 ? nc * nc : nc * nc * nc;
+  float dt_dr[3];
+  for (int q = 0; q < D; q++) dt_dr[q] = u.dt * t.idrf[slot * D + q];
+  float my_chem = 3.0e38f;
+  const size_t base = (size_t)slot * t.S;
+  for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
+    const int i = w % nc + 1, r = w / nc;
+    const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
+    const int x = D == 2 ? at2(n2, i, j) : at3(n2, i, j, k);
+    float dens[NSMAX], der[NSMAX];
+#pragma unroll
+    for (int s = 0; s < NSMAX; s++) {
+      dens[s] = 0.0f;
+      der[s] = 0.0f;
+      if (s < a.ns) dens[s] = fmaxf(d2f(a.deriv[s][base + x]), 0.0f);
+    }
+    const float td = u.N_inv_td * d2f(a.E[base + x]);
+    int ix;
+    float lw;
+    lt_loc_f(u.lt, td, ix, lw);
+    for (int n = 0; n < a.n_reactions; n++) {
+      const Reac32& rc = u.reactions[n];
+      float rate = rate32(u.lt, rc, td, ix, lw);
+      for (int q = 0; q < rc.n_in; q++) rate = rate * pickf<NSMAX>(dens, rc.ix_in[q]);
+      for (int q = 0; q < rc.n_in; q++) add_tof<NSMAX>(der, rc.ix_in[q], -rate);
+      for (int q = 0; q < rc.n_out; q++) add_tof<NSMAX>(der, rc.ix_out[q], rate * rc.mult_out[q]);
+    }
+    if (a.last_step) {
+      const float eps = 1e-30f;
+      float tmp = 3.0e38f;
+#pragma unroll
+      for (int s = 0; s < NSMAX; s++) {
+        if (s >= a.ns) continue;
+        if (u.nmin > 0.0f)
+          tmp = fminf(tmp, (dens[s] + u.nmin) / fmaxf(fabsf(der[s]), eps));
+        else if (a.limit_loss)
+          tmp = fminf(tmp, fmaxf(dens[s], eps) / fmaxf(-der[s], eps));
+      }
+      my_chem = fminf(my_chem, tmp);
+    }
+    if (a.photo != nullptr) {
+      const float ph = d2f(a.photo[base + x]);
+      add_tof<NSMAX>(der, a.flux_species[0], ph);
+      add_tof<NSMAX>(der, a.photoi_species, ph);
+    }
+    float inc[NSMAX];
+#pragma unroll
+    for (int s = 0; s < NSMAX; s++) inc[s] = u.dt * der[s];
+    for (int f = 0; f < a.nf; f++) {
+      const int s = a.flux_species[f];
+      const double* F0 = a.flux[f] + ((size_t)slot * D + 0) * t.NF;
+      const double* F1 = a.flux[f] + ((size_t)slot * D + 1) * t.NF;
+      const int kk = D == 3 ? k : 1;
+      float div;
+      if (D == 2 && CYL) {
+        const double* gw = t.geo + ((size_t)slot * nc + (i - 1)) * 4;
+        const float f1 = d2f(gw[0]), f2 = d2f(gw[1]);
+        div = dt_dr[0] * (f1 * d2f(F0[fc_at(nf1, i, j, 1)]) - f2 * d2f(F0[fc_at(nf1, i + 1, j, 1)])) +
+              dt_dr[1] * (d2f(F1[fc_at(nf1, i, j, 1)]) - d2f(F1[fc_at(nf1, i, j + 1, 1)]));
+      } else if (D == 2) {
+        div = dt_dr[0] * (d2f(F0[fc_at(nf1, i, j, 1)]) - d2f(F0[fc_at(nf1, i + 1, j, 1)])) +
+              dt_dr[1] * (d2f(F1[fc_at(nf1, i, j, 1)]) - d2f(F1[fc_at(nf1, i, j + 1, 1)]));
+      } else {
+        const double* F2 = a.flux[f] + ((size_t)slot * D + 2) * t.NF;
+        div = dt_dr[0] * (d2f(F0[fc_at(nf1, i, j, kk)]) - d2f(F0[fc_at(nf1, i + 1, j, kk)])) +
+              dt_dr[1] * (d2f(F1[fc_at(nf1, i, j, kk)]) - d2f(F1[fc_at(nf1, i, j + 1, kk)])) +
+              dt_dr[2] * (d2f(F2[fc_at(nf1, i, j, kk)]) - d2f(F2[fc_at(nf1, i, j, kk + 1)]));
+      }
+      add_tof<NSMAX>(inc, s, div);
+    }
+#pragma unroll
+    for (int s = 0; s < NSMAX; s++) {
+      if (s >= a.ns) continue;
+      const double n0 = a.prev[0][s][base + x];
+      float d = inc[s];
+      for (int mm = 1; mm < a.n_prev; mm++) d = d + u.w_rel[mm] * d2f(a.prev[mm][s][base + x] - n0);
+      a.out[s][base + x] = n0 + f2d(d);
+    }
+  }
+  if (a.last_step) {
+    for (int o = 16; o > 0; o >>= 1) my_chem = fminf(my_chem, __shfl_xor_sync(0xffffffffu, my_chem, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sred[warp] = my_chem;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float v = sred[0];
+      for (int q = 1; q < (int)((blockDim.x + 31) >> 5); q++) v = fminf(v, sred[q]);
+      atomicMin(a.min_chem, (unsigned long long)__double_as_longlong(f2d(v)));
+    }
+  }
+}
+
+// E on faces and |E| in cells with FP32 scaling (see k_field_grad)
+template <int D>
+__global__ void __launch_bounds__(256) k_field_grad32(KTree t, const int* __restrict__ list,
+                                                      const double* __restrict__ phi, double* __restrict__ efc,
+                                                      double* __restrict__ enorm) {
+  extern __shared__ float sef[];  // [D][NF], the fc layout of one box
+  const int slot = list[blockIdx.x];
+  const int nc = t.nc, n2 = t.n2, nf1 = nc + 1;
+  const double* p = phi + (size_t)slot * t.S;
+  const int nfaces = D == 2 ? nc * nf1 : nc * nc * nf1;
+  for (int w = threadIdx.x; w < D * nfaces; w += blockDim.x) {
+    const int dim = w / nfaces, fw = w - dim * nfaces;
+    const int f = fw % nf1 + 1, ln = fw / nf1;
+    const int jj = ln % nc + 1, kk = D == 3 ? ln / nc + 1 : 1;
+    const float inv_dr = -t.idrf[slot * D + dim];
+    int fidx, c1, c0;
+    if (D == 2) {
+      if (dim == 0) { fidx = fc_at(nf1, f, jj, 1); c1 = at2(n2, f, jj); c0 = at2(n2, f - 1, jj); }
+      else { fidx = fc_at(nf1, jj, f, 1); c1 = at2(n2, jj, f); c0 = at2(n2, jj, f - 1); }
+    } else if (dim == 0) { fidx = fc_at(nf1, f, jj, kk); c1 = at3(n2, f, jj, kk); c0 = at3(n2, f - 1, jj, kk); }
+    else if (dim == 1) { fidx = fc_at(nf1, jj, f, kk); c1 = at3(n2, jj, f, kk); c0 = at3(n2, jj, f - 1, kk); }
+    else { fidx = fc_at(nf1, jj, kk, f); c1 = at3(n2, jj, kk, f); c0 = at3(n2, jj, kk, f - 1); }
+    const float e = inv_dr * d2f(p[c1] - p[c0]);
+    sef[dim * t.NF + fidx] = e;
+    efc[((size_t)slot * D + dim) * t.NF + fidx] = f2d(e);
+  }
+  __syncthreads();
+  const int ncell = D == 2 ? nc * nc : nc * nc * nc;
+  for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
+    const int i = w % nc + 1, r = w / nc;
+    const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 1 : r / nc + 1;
+    const float a = sef[fc_at(nf1, i, j, k)] + sef[fc_at(nf1, i + 1, j, k)];
+    const float b = sef[t.NF + fc_at(nf1, i, j, k)] + sef[t.NF + fc_at(nf1, i, j + 1, k)];
+    float s = a * a + b * b;
+    if (D == 3) {
+      const float c = sef[2 * t.NF + fc_at(nf1, i, j, k)] + sef[2 * t.NF + fc_at(nf1, i, j, k + 1)];
+      s = s + c * c;
+    }
+    enorm[(size_t)slot * t.S + (D == 2 ? at2(n2, i, j) : at3(n2, i, j, k))] = f2d(0.5f * sqrtf(s));
+  }
+}
+
+// Charge density on interior cells (FP64: n_+ - n_- cancels)
+template <int D>
+__global__ void __launch_bounds__(256) k_field_rhs_interior(KTree t, const int* __restrict__ list, RhsArgs a) {
+  const int slot = list[blockIdx.x];
+  const int nc = t.nc, n2 = t.n2;
+  const int ncell = D == 2 ? nc * nc : nc * nc * nc;
+  const size_t base = (size_t)slot * t.S;
+  for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
+    const int i = w % nc + 1, r = w / nc;
+    const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
+    const size_t x = base + (D == 2 ? at2(n2, i, j) : at3(n2, i, j, k));
+    double v = 0.0;
+    for (int s = 0; s < a.ns; s++)
+      if (a.q[s] != 0.0) v = fma(a.q[s], a.n[s][x], v);
+    a.rhs[x] = v;
+  }
+}
+
+// Photon production (see k_photo_source) with FP32 lookup and products
+template <int D>
+__global__ void __launch_bounds__(256) k_photo_source32(KTree t, const int* __restrict__ list,
+                                                        const double* __restrict__ E, const double* __restrict__ ne,
+                                                        double* __restrict__ rhs, LtDevF lt, int col_alpha,
+                                                        int col_mu, float N_inv_td, float coeff_hi, float coeff_lo) {
+  const int slot = list[blockIdx.x];
+  const int nc = t.nc, n2 = t.n2;
+  const int ncell = D == 2 ? nc * nc : nc * nc * nc;
+  const size_t base = (size_t)slot * t.S;
+  for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
+    const int i = w % nc + 1, r = w / nc;
+    const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
+    const int x = D == 2 ? at2(n2, i, j) : at3(n2, i, j, k);
+    const float fld = d2f(E[base + x]);
+    const float td = fld * N_inv_td;
+    int ix;
+    float w_;
+    lt_loc_f(lt, td, ix, w_);
+    const float alpha = lt_col_f(lt, col_alpha, ix, w_);
+    const float mob = lt_col_f(lt, col_mu, ix, w_);
+    float tmp = ((fld * coeff_hi) * mob) * ((alpha * coeff_lo) * d2f(ne[base + x]));
+    if (tmp < 0.0f) tmp = 0.0f;
+    rhs[base + x] = f2d(tmp);
+  }
+}
+
+}  // namespace afg

@@ -1,6 +1,7 @@
 // afg_transport_api.cuh -- host drivers of the transport, field and
 // photoionization entry points (included at the end of afg_runtime.cu).
 #pragma once
+#include "afg_transport32.cuh"
 
 static int need_transport(afg_ctx* ctx) {
   if (!ctx) return AFG_ERR_ARG;
@@ -18,6 +19,17 @@ static LtDev lt_dev(const afg_ctx* ctx) {
   return lt;
 }
 
+static LtDevF lt_dev_f(const afg_ctx* ctx) {
+  LtDevF lt;
+  lt.y = ctx->tr.d_ltf;
+  lt.n = ctx->tr.d.lt_n_points;
+  lt.x_min = (float)ctx->tr.d.lt_x_min;
+  lt.inv_fac = (float)ctx->tr.d.lt_inv_fac;
+  return lt;
+}
+
+static bool mixed_transport(const afg_ctx* ctx) { return ctx->tr.ready && ctx->tr.d.precision == AFG_MIXED; }
+
 static GcDev gc_from_desc(const afg_gc_desc& g) {
   GcDev d;
   for (int n = 0; n < 6; n++) {
@@ -26,6 +38,13 @@ static GcDev gc_from_desc(const afg_gc_desc& g) {
   }
   d.rb = g.rb;
   return d;
+}
+
+static size_t flux32_smem(const afg_ctx* ctx, int n_flux) {
+  const int D = ctx->D, nc = ctx->nc, m = nc + 4;
+  const int tile = D == 2 ? m * m : m * m * m;
+  const int nfaces = D == 2 ? nc * (nc + 1) : nc * nc * (nc + 1);
+  return sizeof(float) * ((size_t)n_flux * tile + 2 * (size_t)D * nfaces + ctx->S);
 }
 
 extern "C" {
@@ -51,6 +70,7 @@ int afg_transport_setup(afg_ctx* ctx, const afg_transport_desc* d) {
   if (t.i_efield_fc < 1 || t.i_efield_fc > ctx->n_var_face) return fail(ctx, AFG_ERR_ARG, "bad i_efield_fc");
   if (t.i_photo < 0 || t.i_photo > ctx->n_var) return fail(ctx, AFG_ERR_ARG, "bad i_photo");
   if (t.photoi_species < 0 || t.photoi_species >= t.n_species) return fail(ctx, AFG_ERR_ARG, "bad photoi_species");
+  if (t.precision != AFG_FP64 && t.precision != AFG_MIXED) return fail(ctx, AFG_ERR_ARG, "bad precision");
   for (int n = 2 * ctx->D; n < 6; n++) (void)n;
   for (int n = 0; n < 2 * ctx->D; n++)
     if (t.species_gc.bc_type[n] == AFG_BC_CONTINUOUS)
@@ -79,6 +99,41 @@ int afg_transport_setup(afg_ctx* ctx, const afg_transport_desc* d) {
   CK(dalloc(&s.d_reactions, std::max(1, t.n_reactions)));
   if (t.n_reactions > 0)
     CK(cudaMemcpy(s.d_reactions, t.reactions, sizeof(afg_reaction) * t.n_reactions, cudaMemcpyHostToDevice));
+  {
+    // FP32 forms for the mixed-precision kernels
+    std::vector<float> ltf((size_t)t.lt_n_cols * t.lt_n_points);
+    for (size_t q = 0; q < ltf.size(); q++) ltf[q] = (float)t.lt_data[q];
+    CK(dalloc(&s.d_ltf, ltf.size()));
+    CK(cudaMemcpy(s.d_ltf, ltf.data(), sizeof(float) * ltf.size(), cudaMemcpyHostToDevice));
+    std::vector<Reac32> r32(std::max(1, t.n_reactions));
+    for (int r = 0; r < t.n_reactions; r++) {
+      const afg_reaction& rc = t.reactions[r];
+      Reac32& o = r32[r];
+      o.rate_type = rc.rate_type;
+      o.lt_col = rc.lt_col;
+      if (rc.rate_type == AFG_RATE_TABULATED_FIELD) {
+        // rate_factor (up to N^2) split into two factors of FP32 range
+        const double h = std::sqrt(std::fabs(rc.rate_factor));
+        o.fa = (float)(rc.rate_factor < 0 ? -h : h);
+        o.fb = (float)(h > 0 ? std::fabs(rc.rate_factor) / h : 0.0);
+      } else {
+        o.fa = (float)(rc.rate_factor * rc.c[0]);
+        o.fb = 1.0f;
+      }
+      for (int q = 0; q < 4; q++) o.c[q] = (float)rc.c[q];
+      o.n_in = rc.n_in;
+      o.n_out = rc.n_out;
+      for (int q = 0; q < 4; q++) {
+        o.ix_in[q] = rc.ix_in[q];
+        o.ix_out[q] = rc.ix_out[q];
+        o.mult_out[q] = (float)rc.mult_out[q];
+      }
+      if (t.precision == AFG_MIXED && (!std::isfinite(o.fa) || !std::isfinite(o.fb)))
+        return fail(ctx, AFG_ERR_UNSUPPORTED, "reaction %d: rate factor outside the FP32 range", r + 1);
+    }
+    CK(dalloc(&s.d_reac32, r32.size()));
+    CK(cudaMemcpy(s.d_reac32, r32.data(), sizeof(Reac32) * r32.size(), cudaMemcpyHostToDevice));
+  }
   // task lists
   const int D = ctx->D, nnb = 2 * D, nch = 1 << D;
   std::vector<int> rrb, cflux;
@@ -120,6 +175,10 @@ int afg_transport_setup(afg_ctx* ctx, const afg_transport_desc* d) {
     CK(cudaFuncSetAttribute(k_flux<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_flux<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_flux<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem32 = flux32_smem(ctx, t.n_flux);
+    CK(cudaFuncSetAttribute(k_flux32<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32));
+    CK(cudaFuncSetAttribute(k_flux32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32));
+    CK(cudaFuncSetAttribute(k_flux32<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32));
   }
   s.ready = true;
   return AFG_OK;
@@ -186,7 +245,24 @@ int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim) {
       if (n == 0) continue;
       const int* list = lst(ctx, ctx->off_leaves[l]);
       kt_begin(ctx, AFG_KT_FLUX);
-      if (ctx->D == 3) {
+      if (mixed_transport(ctx)) {
+        FluxArgs32 a32{};
+        a32.a = a;
+        a32.lt = lt_dev_f(ctx);
+        a32.N_inv_td = (float)(kSiToTd / d.gas_number_density);
+        a32.N_inv = (float)(1 / d.gas_number_density);
+        for (int f = 0; f < d.n_flux; f++) {
+          a32.sign[f] = (float)d.flux_charge_sign[f];
+          a32.mu_ion[f] = (float)(d.ion_mobility_N[f] / d.gas_number_density);
+        }
+        const size_t smem32 = flux32_smem(ctx, d.n_flux);
+        if (ctx->D == 3)
+          k_flux32<3, false><<<n, 256, smem32, ctx->stream>>>(t, list, a32);
+        else if (cyl)
+          k_flux32<2, true><<<n, 256, smem32, ctx->stream>>>(t, list, a32);
+        else
+          k_flux32<2, false><<<n, 256, smem32, ctx->stream>>>(t, list, a32);
+      } else if (ctx->D == 3) {
         k_flux<3, false><<<n, 256, smem, ctx->stream>>>(t, list, a);
       } else if (cyl) {
         k_flux<2, true><<<n, 256, smem, ctx->stream>>>(t, list, a);
@@ -270,21 +346,49 @@ int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev, const
   if (n > 0) {
     kt_begin(ctx, AFG_KT_UPDATE);
     const bool cyl = ctx->coord == AFG_CYL;
-#define AFG_LAUNCH_UPDATE(NSM)                                                   \
-  if (ctx->D == 3)                                                               \
-    k_update<3, false, NSM><<<n, 128, 0, ctx->stream>>>(t, list, a);             \
-  else if (cyl)                                                                  \
-    k_update<2, true, NSM><<<n, 128, 0, ctx->stream>>>(t, list, a);              \
-  else                                                                           \
-    k_update<2, false, NSM><<<n, 128, 0, ctx->stream>>>(t, list, a);
-    if (d.n_species <= 4) {
-      AFG_LAUNCH_UPDATE(4)
-    } else if (d.n_species <= 8) {
-      AFG_LAUNCH_UPDATE(8)
+    double wsum = 0;
+    for (int m = 0; m < n_prev; m++) wsum += w_prev[m];
+    if (mixed_transport(ctx) && std::fabs(wsum - 1.0) <= 1e-12) {
+      UpdateArgs32 u{};
+      u.a = a;
+      u.lt = lt_dev_f(ctx);
+      u.reactions = ctx->tr.d_reac32;
+      u.N_inv_td = (float)(kSiToTd / d.gas_number_density);
+      u.dt = (float)dt;
+      for (int m = 0; m < n_prev; m++) u.w_rel[m] = (float)w_prev[m];
+      u.nmin = (float)d.dt_chemistry_nmin;
+#define AFG_LAUNCH_UPDATE32(NSM)                                          \
+  if (ctx->D == 3)                                                        \
+    k_update32<3, false, NSM><<<n, 128, 0, ctx->stream>>>(t, list, u);    \
+  else if (cyl)                                                           \
+    k_update32<2, true, NSM><<<n, 128, 0, ctx->stream>>>(t, list, u);     \
+  else                                                                    \
+    k_update32<2, false, NSM><<<n, 128, 0, ctx->stream>>>(t, list, u);
+      if (d.n_species <= 4) {
+        AFG_LAUNCH_UPDATE32(4)
+      } else if (d.n_species <= 8) {
+        AFG_LAUNCH_UPDATE32(8)
+      } else {
+        AFG_LAUNCH_UPDATE32(16)
+      }
+#undef AFG_LAUNCH_UPDATE32
     } else {
-      AFG_LAUNCH_UPDATE(16)
-    }
+#define AFG_LAUNCH_UPDATE(NSM)                                          \
+  if (ctx->D == 3)                                                      \
+    k_update<3, false, NSM><<<n, 128, 0, ctx->stream>>>(t, list, a);    \
+  else if (cyl)                                                         \
+    k_update<2, true, NSM><<<n, 128, 0, ctx->stream>>>(t, list, a);     \
+  else                                                                  \
+    k_update<2, false, NSM><<<n, 128, 0, ctx->stream>>>(t, list, a);
+      if (d.n_species <= 4) {
+        AFG_LAUNCH_UPDATE(4)
+      } else if (d.n_species <= 8) {
+        AFG_LAUNCH_UPDATE(8)
+      } else {
+        AFG_LAUNCH_UPDATE(16)
+      }
 #undef AFG_LAUNCH_UPDATE
+    }
     // per leaf cell: read S*(n_prev+1) densities (+|E|, D*F fluxes, photo), write S densities
     kt_end(ctx, AFG_KT_UPDATE, 8.0 * n * box_cells(ctx) *
                                    (d.n_species * (n_prev + 1) + ctx->D * d.n_flux + 1 + (d.i_photo > 0) + d.n_species));
@@ -315,7 +419,13 @@ int afg_field_set_rhs(afg_ctx* ctx, int i_rhs, int s_in) {
   }
   a.rhs = ctx->cc[i_rhs - 1];
   if (ctx->n_all_leaves > 0) {
-    k_field_rhs<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ctx->S, lst(ctx, ctx->off_all_leaves), a);
+    const int* list = lst(ctx, ctx->off_all_leaves);
+    if (!mixed_transport(ctx))
+      k_field_rhs<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ctx->S, list, a);
+    else if (ctx->D == 3)
+      k_field_rhs_interior<3><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), list, a);
+    else
+      k_field_rhs_interior<2><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), list, a);
     ctx->launches++;
     CKL();
   }
@@ -332,7 +442,16 @@ int afg_field_from_potential(afg_ctx* ctx, int i_phi) {
   if (!ctx->has_method[d.i_electric_fld - 1])
     return fail(ctx, AFG_ERR_STATE, "no ghost-cell methods for the electric field norm");
   return run_graph(ctx, gkey("efield", i_phi), [&]() -> int {
-    if (ctx->D == 3)
+    if (mixed_transport(ctx)) {
+      const int D = ctx->D;
+      const size_t smem = sizeof(float) * D * (size_t)ctx->NF;
+      if (D == 3)
+        k_field_grad32<3><<<ctx->n_all, 256, smem, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1],
+                                                                   efc, en);
+      else
+        k_field_grad32<2><<<ctx->n_all, 256, smem, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1],
+                                                                   efc, en);
+    } else if (ctx->D == 3)
       k_field_grad<3><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en);
     else
       k_field_grad<2><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en);
@@ -410,7 +529,19 @@ int afg_photoi_helmh(afg_ctx* ctx, double coeff, int n_modes, const int* mg_ids,
     const double* E = ctx->cc[d.i_electric_fld - 1];
     const double* ne = ctx->cc[d.species_iv[d.flux_species[0]] - 1];
     double* rhs = ctx->cc[i_rhs - 1];
-    if (ctx->D == 3)
+    if (mixed_transport(ctx)) {
+      const float N_inv_td = (float)(kSiToTd / d.gas_number_density);
+      const double ch = std::sqrt(std::fabs(coeff));
+      const float c_hi = (float)(coeff < 0 ? -ch : ch), c_lo = (float)ch;
+      if (ctx->D == 3)
+        k_photo_source32<3><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all_leaves), E, ne, rhs,
+                                                                        lt_dev_f(ctx), d.lt_col_alpha,
+                                                                        d.lt_col_mobility, N_inv_td, c_hi, c_lo);
+      else
+        k_photo_source32<2><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all_leaves), E, ne, rhs,
+                                                                        lt_dev_f(ctx), d.lt_col_alpha,
+                                                                        d.lt_col_mobility, N_inv_td, c_hi, c_lo);
+    } else if (ctx->D == 3)
       k_photo_source<3><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all_leaves), E, ne, rhs,
                                                                   lt_dev(ctx), d.lt_col_alpha, d.lt_col_mobility,
                                                                   d.gas_number_density, coeff);

@@ -119,7 +119,7 @@ class StreamerModel:
                 cols.append(cols[3] * cols[0] * x * TD_TO_SI * N)
         self.lt = np.ascontiguousarray(np.stack(cols), dtype=np.float64)  # [n_cols][n_points]
 
-    def transport_desc(self) -> ag.TransportDesc:
+    def transport_desc(self, precision=ag.FP64) -> ag.TransportDesc:
         d = ag.TransportDesc()
         d.n_species = len(self.species)
         for s, sp in enumerate(self.species):
@@ -168,6 +168,7 @@ class StreamerModel:
                 R.mult_out[q] = r["mult"][q]
         d.dt_chemistry_nmin = 0.0
         d.dt_chemistry_limit_loss = 1
+        d.precision = precision
         return d
 
     def field_bc(self, voltage):
@@ -238,7 +239,7 @@ class StreamerRun:
     def setup(self):
         ctx, m = self.ctx, self.m
         D = self.tree.ndim
-        ctx.transport_setup(m.transport_desc())
+        ctx.transport_setup(m.transport_desc(self.precision))
         ctx.set_cc_methods(m.i_electric_fld, *m.electric_fld_gc())
         for s in range(len(m.species)):
             for st in range(m.n_states):

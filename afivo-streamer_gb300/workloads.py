@@ -56,7 +56,7 @@ class Workload:
     photoi_coeffs = np.array([1e-2, 5e-2, 1e-1]) * 1e4     # 1/m^2
     photoi_eta_quench = 0.05 * 0.038
 
-    def tree(self, reduced=False):
+    def tree(self, reduced=False, coarsen=0):
         raise NotImplementedError
 
     def model(self):
@@ -65,32 +65,41 @@ class Workload:
     def seed_center(self):
         raise NotImplementedError
 
-    def fill_variable(self, tree, model, iv, seed=12345):
+    def fill_variable(self, tree, model, iv, seed=12345, out=None, chunk=8192):
         """Initial value of cell-centred variable iv (1-based) on all boxes,
-        ghost cells included: array [n_boxes, 1, (nc+2)^D]."""
+        ghost cells included: array [n_boxes, (nc+2)^D] (or written into
+        `out` of that shape).  Computed in chunks of boxes; the noise of
+        chunk c comes from generator (seed, c)."""
         D, nc = tree.ndim, tree.n_cell
         n2 = nc + 2
-        out = np.zeros((tree.n_boxes, 1) + (n2,) * D)
+        if out is None:
+            out = np.empty((tree.n_boxes,) + (n2,) * D)
         idx = np.arange(n2) - 0.5
-        X = []  # cell-centre coordinates, broadcastable to [n, (k,) j, i]
-        for d in range(D):
-            shape = [tree.n_boxes] + [1] * D
-            shape[1 + (D - 1 - d)] = n2
-            X.append((tree.r_min[:, d][:, None] + idx[None, :] * tree.dr[:, d][:, None]).reshape(shape))
         c = self.seed_center()
-        r2 = sum((X[d] - c[d]) ** 2 for d in range(D))
         sig = self.seed_sigma
-        gauss = 1e15 * np.exp(-r2 / (2 * sig ** 2))
         L = float(tree.dr[0, -1] * tree.coarse_grid_size[-1])
-        if iv == model.i_phi:
-            out[:, 0] = self.voltage * np.broadcast_to(X[D - 1], gauss.shape) / L
-        elif iv in model.species_iv:
-            s = model.species_iv.index(iv)
+        s = model.species_iv.index(iv) if iv in model.species_iv else -1
+        for c0 in range(0, tree.n_boxes, chunk):
+            c1 = min(tree.n_boxes, c0 + chunk)
+            m = c1 - c0
+            X = []  # cell-centre coordinates, broadcastable to [m, (k,) j, i]
+            for d in range(D):
+                shape = [m] + [1] * D
+                shape[1 + (D - 1 - d)] = n2
+                X.append((tree.r_min[c0:c1, d][:, None] + idx[None, :] * tree.dr[c0:c1, d][:, None]).reshape(shape))
+            o = out[c0:c1]
+            if iv == model.i_phi:
+                o[...] = self.voltage * np.broadcast_to(X[D - 1], o.shape) / L
+                continue
+            if s != 0 and s != self.positive_species:
+                o[...] = 0.0
+                continue
+            r2 = sum((X[d] - c[d]) ** 2 for d in range(D))
+            g = 1e15 * np.exp(-r2 / (2 * sig ** 2)) + 1e9
             if s == 0:
-                rng = np.random.default_rng(seed)
-                out[:, 0] = (gauss + 1e9) * (1 + 1e-3 * rng.standard_normal(gauss.shape))
-            elif s == self.positive_species:
-                out[:, 0] = gauss + 1e9
+                rng = np.random.default_rng([seed, c0 // chunk])
+                g = g * (1 + 1e-3 * rng.standard_normal(g.shape))
+            o[...] = g
         return out
 
 
@@ -100,7 +109,7 @@ class Cyl2d(Workload):
     seed_sigma = 0.5e-3
     positive_species = 1
 
-    def tree(self, reduced=False):
+    def tree(self, reduced=False, coarsen=0):
         return at.build_tree(2, 16, [16, 32], [1e-2, 2e-2], coord=ag.AFG_CYL, max_lvl=9,
                              refine=channel_refinement(5, [2e-3, 1e-3, 0.6e-3, 0.35e-3], 0.9e-2, 1.4e-2))
 
@@ -117,15 +126,13 @@ class Streamer3d(Workload):
     seed_sigma = 0.3e-3
     positive_species = 1
 
-    def tree(self, reduced=False):
-        """The full tree, or (reduced=True) the same construction two levels
-        coarser everywhere (~1/50 of the cells), the CPU baseline's sample."""
-        if reduced:
-            return at.build_tree(3, 8, [8, 8, 8], [3e-2] * 3, max_lvl=10,
-                                 refine=channel_refinement(4, [3.2e-3, 1.7e-3, 1.0e-3, 0.5e-3, 0.25e-3, 0.12e-3],
-                                                           1.2e-2, 1.8e-2, axis_xy=(1.5e-2, 1.5e-2)))
-        return at.build_tree(3, 8, [8, 8, 8], [3e-2] * 3, max_lvl=12,
-                             refine=channel_refinement(6, [3.2e-3, 1.7e-3, 1.0e-3, 0.5e-3, 0.25e-3, 0.12e-3],
+    def tree(self, reduced=False, coarsen=0):
+        """The full tree, or the same construction `coarsen` levels coarser
+        everywhere (each level ~1/8 of the boxes); reduced=True is coarsen=2
+        (~1/50 of the cells), the CPU baseline's sample."""
+        k = 2 if reduced else coarsen
+        return at.build_tree(3, 8, [8, 8, 8], [3e-2] * 3, max_lvl=12 - k,
+                             refine=channel_refinement(6 - k, [3.2e-3, 1.7e-3, 1.0e-3, 0.5e-3, 0.25e-3, 0.12e-3],
                                                        1.2e-2, 1.8e-2, axis_xy=(1.5e-2, 1.5e-2)))
 
     def model(self):

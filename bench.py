@@ -1,23 +1,32 @@
 """Benchmark of the afivo-streamer hot path on one GB300.
 
-Workload (the configuration the headline metric is quoted on): 2D
-axisymmetric streamer, r in [0, 1 cm], z in [0, 2 cm], 16x16-cell boxes,
-coarse grid 16x32, uniform to level 5 then 4 AMR levels around the streamer
-channel (~0.56 M leaf cells, 9 levels); electrons + positive + negative ions
-(mobility 0.03 m^2/Vs, diffusion 0.1 m^2/s, alpha(E) = 4.3e5 exp(-2e7/|E|),
-eta = 2e3 1/m), 3-term Helmholtz photoionization (lambda 50/150/500 1/m),
-applied field 1.5e6 V/m, Heun time steps of 5e-12 s.  A step is one time step
-of the reference time loop: photoionization every 5 steps, state copy, two
-forward-Euler stages (Koren fluxes + sources), and a Poisson solve to 1e-8
-relative residual after each stage.
+A step is one time step of the reference's time loop over the whole tree:
+photoionization every 5 steps (3-term Helmholtz, FMG), copy of the state,
+two forward-Euler stages of Heun's method (Koren-limited drift-diffusion
+fluxes with consistent coarse fluxes, reaction sources) and a Poisson solve
+to 1e-8 relative residual after each stage.
 
-Metric: cell-updates/s = (smoother cell-updates of all V-cycles + transport
-cell-updates) / time, for the mixed-precision path (FP32 V-cycle inside FP64
-defect correction); the plain FP64 GPU path is timed beside it.  Inputs are
-seeded synthetic data; the L2 cache is flushed between timed steps.
+Workloads (seeded synthetic inputs, afivo-streamer_gb300/workloads.py):
 
---impl reference times the CPU restatement of the same step (the oracle,
-OpenMP on all host cores) on a bounded sample of the same workload.
+* ``3d`` (default; the configuration the headline metric is quoted on): 3D
+  streamer in a 3 cm cube, 8^3-cell boxes, 12 levels, 221,129 boxes,
+  ~99 M leaf cells / ~113 M cells; 5 species with 8 k13-form reactions;
+  applied field 1.5e6 V/m, dt = 5e-12 s.
+* ``cyl2d``: 2D axisymmetric streamer, 16^2-cell boxes, 9 levels,
+  2,918 boxes, ~0.56 M leaf cells; 3 species with tabulated rates.
+
+Metric: cell-updates/s = (smoother cell-updates of every V-cycle + leaf cells
+x species per transport stage) / time.  `value` is the mixed-precision path
+(FP32 V-cycles inside FP64 defect correction, FP64 transport) with the state
+resident in HBM, CUDA events around each step and a 256 MiB L2 flush between
+steps; the plain FP64 path is timed beside it.  `e2e` runs the same steps
+through the C-ABI with the state in page-locked host memory: each step
+uploads the species densities, advances, and downloads the densities and
+|E|, inside the timed region.
+
+`--impl reference` and `cpu_baseline` time the CPU restatement of the same
+step (C++/OpenMP on all host cores) on a bounded sample: for ``3d`` the same
+tree construction two levels coarser (4,361 boxes, ~2.2 M cells).
 """
 import argparse
 import json
@@ -32,57 +41,21 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "afivo-streamer_gb300"))
 
 import afivo_gpu as ag  # noqa: E402
-import afivo_tree as at  # noqa: E402
 import streamer_model as sm  # noqa: E402
+import workloads  # noqa: E402
 
 METRIC = "cell-updates/s & V-cycle ms at 1e-8 rel. residual, mixed vs FP64 on 1 GB300"
 UNIT = "cell-updates/s"
-VOLTAGE = -3e4          # 1.5e6 V/m over 2 cm
-DT = 5e-12
-PHOTOI_LAMBDA = np.array([50.0, 150.0, 500.0])          # 1/m
-PHOTOI_COEFFS = np.array([1e-2, 5e-2, 1e-1]) * 1e4       # 1/m^2
-PHOTOI_ETA_QUENCH = 0.05 * 0.038
-
-
-def streamer_refine(base, radii, z_tail, z_head):
-    def f(lvl, c, dr):
-        if lvl < base:
-            return np.ones(len(c), bool)
-        R = radii[lvl - base]
-        r, z = c[:, 0], c[:, 1]
-        return (r < R) & (z > z_tail - R) & (z < z_head + R)
-    return f
-
-
-def workload_tree():
-    return at.build_tree(2, 16, [16, 32], [1e-2, 2e-2], coord=ag.AFG_CYL, max_lvl=9,
-                         refine=streamer_refine(5, [2e-3, 1e-3, 0.6e-3, 0.35e-3], 0.9e-2, 1.4e-2))
-
-
-def workload_model():
-    return sm.StreamerModel(2, alpha=sm.baseline_alpha, eta=sm.baseline_eta, photoi_modes=3)
-
-
-def initial_state(tree, model, seed=12345):
-    rng = np.random.default_rng(seed)
-    cc = ag.new_cc(tree, model.n_var_cell)
-    fc = ag.new_fc(tree, model.n_var_face)
-    n2 = tree.n_cell + 2
-    idx = np.arange(n2) - 0.5
-    r = tree.r_min[:, 0][:, None, None] + idx[None, None, :] * tree.dr[:, 0][:, None, None]
-    z = tree.r_min[:, 1][:, None, None] + idx[None, :, None] * tree.dr[:, 1][:, None, None]
-    seed_n = 1e15 * np.exp(-(r ** 2 + (z - 1.2e-2) ** 2) / (2 * 0.5e-3 ** 2)) + 1e9
-    noise = 1 + 1e-3 * rng.standard_normal(seed_n.shape)
-    cc[:, model.species_iv[0] - 1] = seed_n * noise
-    cc[:, model.species_iv[1] - 1] = seed_n
-    cc[:, model.species_iv[2] - 1] = 0.0
-    cc[:, model.i_phi - 1] = VOLTAGE * np.broadcast_to(z, seed_n.shape) / 2e-2
-    return cc, fc
-
-
-def work_per_step(ctr0, ctr1):
-    return (ctr1["smoother_updates"] - ctr0["smoother_updates"]) + \
-        (ctr1["transport_updates"] - ctr0["transport_updates"])
+CONFIG_TEXT = {
+    "3d": "3D streamer, 3 cm cube, 8^3 boxes, 12 levels, 221129 boxes (~99 M leaf / ~113 M cells), 5 species, "
+          "8 k13 reactions, 3 Helmholtz photoionization modes, Heun dt=5e-12 s, Poisson to 1e-8 rel.",
+    "cyl2d": "2D axisymmetric streamer, 16^2 boxes, 9 levels, 2918 boxes (~0.56 M leaf cells), 3 species, "
+             "3 Helmholtz photoionization modes, Heun dt=5e-12 s, Poisson to 1e-8 rel.",
+}
+# DRAM bytes (read + write) per box of one launch of a kernel class, from one
+# ncu capture (the profiles/ summary of that workload and kernel gives the
+# command); the traffic of a launch is this times the boxes it processes.
+NCU_DRAM_BYTES_PER_BOX = {}
 
 
 class Clocks:
@@ -132,26 +105,54 @@ class Clocks:
                 "samples": len(sm_mhz)}
 
 
-def run_gpu_arm(args, device):
-    tree = workload_tree()
-    model = workload_model()
-    cc0, fc0 = initial_state(tree, model)
+def work_of(c0, c1):
+    return (c1["smoother_updates"] - c0["smoother_updates"]) + (c1["transport_updates"] - c0["transport_updates"])
+
+
+def initial_host_state(w, tree, model):
+    """Potential and species densities (state 0) on every box: host array
+    [n_boxes, 1 + n_species, (nc+2)^D] in the reference's per-box layout."""
+    ivs = [model.i_phi] + list(model.species_iv)
+    n2 = tree.n_cell + 2
+    H = np.empty((tree.n_boxes, len(ivs)) + (n2,) * tree.ndim)
+    for v, iv in enumerate(ivs):
+        w.fill_variable(tree, model, iv, out=H[:, v])
+    return H, ivs
+
+
+def cuda_profiler(on):
+    """cudaProfilerStart/Stop of the CUDA runtime the library uses (ncu
+    --profile-from-start off captures only the bracketed launches)."""
+    import ctypes
+    rt = ctypes.CDLL("libcudart.so.13")
+    rc = rt.cudaProfilerStart() if on else rt.cudaProfilerStop()
+    if rc != 0:
+        raise RuntimeError(f"cudaProfiler{'Start' if on else 'Stop'} failed: {rc}")
+
+
+def run_gpu_arm(args, device, w):
+    tree = w.tree(coarsen=args.coarsen)
+    model = w.model()
+    H, ivs = initial_host_state(w, tree, model)
+    photoi = (w.photoi_lambda, w.photoi_coeffs, w.photoi_eta_quench)
     ctx = ag.Context(device)
-    ctx.tree_sync(tree, model.n_var_cell, model.n_var_face)
     results = {}
-    for prec_name, prec in (("fp64", ag.FP64), ("mixed", ag.MIXED)):
-        ctx.upload(cc0)
-        ctx.upload_fc(fc0)
-        run = sm.StreamerRun(ctx, tree, model, VOLTAGE, DT, precision=prec, max_rel_residual=1e-8,
-                             num_vcycles=30, photoi=(PHOTOI_LAMBDA, PHOTOI_COEFFS, PHOTOI_ETA_QUENCH))
+    arms = (("mixed", ag.MIXED),) if args.profile else (("fp64", ag.FP64), ("mixed", ag.MIXED))
+    for prec_name, prec in arms:
+        ctx.tree_sync(tree, model.n_var_cell, model.n_var_face)     # zeroed pools
+        ctx.upload_vars(H, ivs)
+        run = sm.StreamerRun(ctx, tree, model, w.voltage, w.dt, precision=prec, max_rel_residual=1e-8,
+                             num_vcycles=30, photoi=photoi)
         run.setup()
         run.initial_field()
         for _ in range(args.warmup):
             run.step()
         ctx.sync()
-        times, work, vcycles = [], 0, 0
+        times, vcycles = [], 0
         clocks = Clocks(device) if prec_name == "mixed" else None
         c0 = ctx.counters()
+        if args.profile:
+            cuda_profiler(True)
         for _ in range(args.steps):
             ctx.flush_l2(256 << 20)
             ctx.event_record(0)
@@ -159,21 +160,28 @@ def run_gpu_arm(args, device):
             ctx.event_record(1)
             times.append(ctx.event_elapsed(0, 1))
             vcycles += run.last["vcycles"]
+        if args.profile:
+            ctx.sync()
+            cuda_profiler(False)
         c1 = ctx.counters()
         clk = clocks.stop() if clocks else None
-        work = work_per_step(c0, c1)
+        work = work_of(c0, c1)
         t_ms = float(np.sum(times))
         res = dict(ms_per_step=t_ms / args.steps, value=work / (t_ms * 1e-3), vcycles_per_step=vcycles / args.steps,
+                   launches=c1["launches"] - c0["launches"],
                    launches_per_step=(c1["launches"] - c0["launches"]) / args.steps,
-                   vcycle_ms=None, clocks=clk, work_per_step=work / args.steps)
-        # V-cycle time: one more solve with the same state, per V-cycle
+                   clocks=clk, work_per_step=work / args.steps)
+        # V-cycle time: one more solve of the current state, per V-cycle
         ctx.sync()
         ctx.event_record(2)
         n, _ = run.field(0, True)
         ctx.event_record(3)
         res["vcycle_ms"] = ctx.event_elapsed(2, 3) / max(1, n)
         results[prec_name] = (res, run)
-    # per-kernel-class device time during one mixed step
+    if args.profile:
+        ctx.close()
+        return tree, results, {}, None
+    # per-kernel-class device time during one mixed step (graphs off while timing)
     run = results["mixed"][1]
     kstats = {}
     for cls, name in ((ag.KT_GSRB, "gsrb"), (ag.KT_GHOST, "ghost"), (ag.KT_FLUX, "flux"), (ag.KT_UPDATE, "update")):
@@ -182,115 +190,84 @@ def run_gpu_arm(args, device):
         n, ms, by = ctx.kernel_stats()
         kstats[name] = dict(launches=n, ms=ms, bytes=by)
     ctx.kernel_timing(ag.KT_NONE)
-    # end to end through the public API: host state in, host state out
-    species_ivs = [iv for iv in model.species_iv]
-    host = ag.new_cc(tree, model.n_var_cell)
-    ctx.download(host)
-    out = np.zeros_like(host)
+    # end to end through the C-ABI: page-locked host state in, densities and |E| out
+    species_ivs = list(model.species_iv)
+    cols = list(range(1, 1 + len(species_ivs)))
+    Eh = np.empty((tree.n_boxes, 1) + H.shape[2:])
+    ctx.host_register(H)
+    ctx.host_register(Eh)
+    bpH, bpE = ag.box_pointers(H), ag.box_pointers(Eh)
+    ctx.download_vars(H, species_ivs, cols=cols, bp=bpH)
     ctx.sync()
-    h2d = d2h = 0
+    c0 = ctx.counters()
+    t_up = t_step = t_down = 0.0
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        ctx.upload(host, species_ivs)
+        ta = time.perf_counter()
+        ctx.upload_vars(H, species_ivs, cols=cols, bp=bpH)
+        tb = time.perf_counter()
         run.step()
-        ctx.download(out, species_ivs + [model.i_electric_fld])
+        ctx.sync()
+        tc = time.perf_counter()
+        ctx.download_vars(H, species_ivs, cols=cols, bp=bpH)
+        ctx.download_vars(Eh, [model.i_electric_fld], bp=bpE)
+        td = time.perf_counter()
+        t_up, t_step, t_down = t_up + tb - ta, t_step + tc - tb, t_down + td - tc
     e2e_s = time.perf_counter() - t0
-    S = int(np.prod(host.shape[2:]))
+    c1 = ctx.counters()
+    ctx.host_unregister(H)
+    ctx.host_unregister(Eh)
+    S = int(np.prod(H.shape[2:]))
     h2d = len(species_ivs) * tree.n_boxes * S * 8
     d2h = (len(species_ivs) + 1) * tree.n_boxes * S * 8
-    work_e2e = results["mixed"][0]["work_per_step"] * args.steps
-    e2e = dict(value=work_e2e / e2e_s, unit=UNIT, h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h,
-               ms_per_step=1e3 * e2e_s / args.steps)
-    launches = ctx.counters()["launches"]
+    e2e = dict(value=work_of(c0, c1) / e2e_s, unit=UNIT, h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h,
+               ms_per_step=1e3 * e2e_s / args.steps,
+               upload_ms_per_step=1e3 * t_up / args.steps, step_ms_per_step=1e3 * t_step / args.steps,
+               download_ms_per_step=1e3 * t_down / args.steps,
+               h2d_gbs=h2d / max(t_up / args.steps, 1e-12) / 1e9, d2h_gbs=d2h / max(t_down / args.steps, 1e-12) / 1e9,
+               transfer_path="pitched DMA from page-locked host boxes (afg_host_register)")
     ctx.close()
-    return tree, results, kstats, e2e, launches
+    return tree, results, kstats, e2e
 
 
-def oracle_step_runner(tree, model):
-    """CPU restatement of the same step (test/baseline infrastructure)."""
+def run_cpu(name, steps, warmup=1, time_limit=None):
+    """The CPU restatement of the step (oracle) on all host cores; for the 3D
+    workload on the reduced tree.  Returns (cell-updates/s, cores, s/step,
+    steps timed, sample text)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    o = oracle.Oracle(tree, model.n_var_cell, model.n_var_face)
-    o.transport_setup(model.transport_desc())
-    D = tree.ndim
-    o.set_cc_methods(model.i_electric_fld, *model.electric_fld_gc())
-    for s in range(len(model.species)):
-        for st in range(model.n_states):
-            o.set_cc_methods(model.species_iv[s] + st, [model.bc_species] * (2 * D), None, ag.RB_INTERP_LIM)
-    o.set_cc_methods(model.i_photo, *model.photo_gc())
-    o.mg_setup(0, model.field_mg(VOLTAGE))
-    for n, d in enumerate(model.helmholtz_mg(PHOTOI_LAMBDA)):
-        o.mg_setup(1 + n, d)
-    L = 2e-2
-    min_dr = float(np.min(tree.dr[tree.lvl_ids[-1][0] - 1]))
-    leaves = np.concatenate(tree.lvl_leaves) - 1
-    n2 = tree.n_cell + 2
-    ncell_leaf = len(leaves) * tree.n_cell ** D
-    level_cells = [len(tree.lvl_ids[l]) * tree.n_cell ** D for l in range(tree.highest_lvl)]
-    vcycle_updates = 4 * sum(level_cells[1:])
-
-    def field(cc, fc, s_in):
-        o.field_set_rhs(cc, model.i_rhs, s_in)
-        max_rhs = o.maxabs(cc, model.i_rhs)
-        thr = max(1e-6, max_rhs * 1e-8, 1e-10 * abs(VOLTAGE) / (L * min_dr))
-        n, _ = o.mg_solve(cc, 0, thr, 30)
-        o.field_from_potential(cc, fc, model.i_phi)
-        return n
-
-    def step(cc, fc, it):
-        work = 0
-        if it % 5 == 0:
-            o.photoi_source(cc, PHOTOI_ETA_QUENCH, model.i_rhs)
-            cc[:, model.i_photo - 1] = 0
-            max_rhs = max(o.maxabs(cc, model.i_rhs), np.sqrt(np.finfo(float).eps))
-            for n in range(3):
-                for i in range(10):
-                    r = o.mg_fmg(cc, 1 + n, True, True)
-                    work += sum(4 * sum(level_cells[1:l]) for l in range(1, tree.highest_lvl + 1))
-                    if r / max_rhs < 1e-2:
-                        break
-                cc[leaves, model.i_photo - 1] -= PHOTOI_COEFFS[n] * cc[leaves, model.i_modes[n] - 1]
-        for s in range(len(model.species)):
-            cc[:, model.species_iv[s] + model.n_states - 2] = cc[:, model.species_iv[s] - 1]
-        o.flux_upwind(cc, fc, 0)
-        o.update_densities(cc, fc, DT, 0, [0], [1.0], 1)
-        nv = field(cc, fc, 1)
-        o.flux_upwind(cc, fc, 1)
-        o.update_densities(cc, fc, 0.5 * DT, 1, [0, 1], [0.5, 0.5], 0, True)
-        nv += field(cc, fc, 0)
-        work += nv * vcycle_updates + 2 * ncell_leaf * len(model.species)
-        return work
-
-    def init(cc, fc):
-        o.gc(cc, model.i_phi, 0, True)
-        o.field_set_rhs(cc, model.i_rhs, 0)
-        for _ in range(20):
-            r = o.mg_fmg(cc, 0, True, False)
-        o.field_from_potential(cc, fc, model.i_phi)
-
-    return init, step
-
-
-def run_cpu(steps, warmup=1):
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
+    from oracle_streamer import OracleStreamerRun
     cores = os.cpu_count() or 1
     oracle.set_num_threads(cores)
-    tree = workload_tree()
-    model = workload_model()
-    cc, fc = initial_state(tree, model)
-    init, step = oracle_step_runner(tree, model)
-    init(cc, fc)
-    it = 0
+    w = workloads.WORKLOADS[name]()
+    reduced = name == "3d"
+    tree = w.tree(reduced=reduced)
+    model = w.model()
+    cc = ag.new_cc(tree, model.n_var_cell)
+    fc = ag.new_fc(tree, model.n_var_face)
+    H, ivs = initial_host_state(w, tree, model)
+    for v, iv in enumerate(ivs):
+        cc[:, iv - 1] = H[:, v]
+    del H
+    run = OracleStreamerRun(tree, model, w.voltage, w.dt, max_rel_residual=1e-8, num_vcycles=30,
+                            photoi=(w.photoi_lambda, w.photoi_coeffs, w.photoi_eta_quench))
+    run.setup()
+    run.initial_field(cc, fc)
     for _ in range(warmup):
-        step(cc, fc, it)
-        it += 1
-    work, t0 = 0, time.perf_counter()
-    for _ in range(steps):
-        work += step(cc, fc, it)
-        it += 1
+        run.step(cc, fc)
+    work, done, t0 = 0, 0, time.perf_counter()
+    while done < steps:
+        work += run.step(cc, fc)
+        done += 1
+        if time_limit is not None and time.perf_counter() - t0 > time_limit:
+            break
     dt = time.perf_counter() - t0
-    return work / dt, cores, dt / steps
+    ncells = tree.n_boxes * tree.n_cell ** tree.ndim
+    sample = (f"{done} step(s) after {warmup} warm-up step(s) of the {'reduced ' if reduced else ''}{name} tree "
+              f"({tree.n_boxes} boxes, {ncells / 1e6:.2f} M cells"
+              f"{', the same construction two levels coarser' if reduced else ''}) on the CPU restatement "
+              f"(C++/OpenMP, {cores} threads)")
+    return work / dt, cores, dt / done, done, sample
 
 
 def peaks():
@@ -308,31 +285,43 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--config", default="3d", choices=sorted(workloads.WORKLOADS))
+    ap.add_argument("--cpu-steps", type=int, default=10, help="CPU baseline sample steps (0 = skip)")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU baseline time bound")
+    ap.add_argument("--coarsen", type=int, default=0,
+                    help="3d only: the same tree construction this many levels coarser (smaller profiling cases)")
+    ap.add_argument("--profile", action="store_true",
+                    help="mixed arm only, timed steps bracketed by cudaProfilerStart/Stop; no e2e or CPU baseline")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    config = {"workload": "2D axisymmetric streamer, 16^2 boxes, coarse 16x32, 9 levels (~0.56 M leaf cells), "
-                          "3 species, 3 Helmholtz photoionization modes, Heun dt=5e-12 s, Poisson to 1e-8 rel.",
-              "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas" if world > 1 else "1 GPU"}
+    config = {"workload": CONFIG_TEXT[args.config] if args.coarsen == 0 else
+              f"{CONFIG_TEXT[args.config]} -- coarsened by {args.coarsen} level(s)", "name": args.config,
+              "l2": "flushed between timed steps (256 MiB write)",
+              "parallelism": "replicas" if world > 1 else "1 GPU"}
     if args.impl == "reference":
         if rank != 0:
             return
-        v, cores, sps = run_cpu(max(1, args.steps), warmup=min(1, args.warmup))
+        warm = max(0, min(1, args.warmup))
+        v, cores, sps, done, sample = run_cpu(args.config, max(1, args.steps), warmup=warm, time_limit=120.0)
         print(json.dumps({
             "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": max(1, args.steps), "warmup": min(1, args.warmup), "ms_per_step": 1e3 * sps,
+            "steps": done, "warmup": warm, "ms_per_step": 1e3 * sps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": config,
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{max(1, args.steps)} full steps of the workload on the CPU oracle"},
+            "data": "synthetic (seeded)", "config": config,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    tree, results, kstats, e2e, launches = run_gpu_arm(args, local)
+    w = workloads.WORKLOADS[args.config]()
+    tree, results, kstats, e2e = run_gpu_arm(args, local, w)
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile": True, "config": config, "mixed": results["mixed"][0]}))
+        return
     mixed, fp64 = results["mixed"][0], results["fp64"][0]
     ms = mixed["ms_per_step"]
     value = mixed["value"]
@@ -347,27 +336,30 @@ def main():
     dom = max(kstats, key=lambda k: kstats[k]["ms"])
     ks = kstats[dom]
     achieved = ks["bytes"] / (ks["ms"] * 1e-3) / 1e9 if ks["ms"] > 0 else 0.0
+    traffic = None
+    per_box = NCU_DRAM_BYTES_PER_BOX.get((args.config, dom))
+    if per_box is not None and ks["launches"]:
+        traffic = per_box * ks.get("boxes", 0) / ks["launches"]
     cpu = None
     if rank == 0 and world == 1 and args.cpu_steps > 0:
-        v, cores, sps = run_cpu(args.cpu_steps, warmup=0)
-        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{args.cpu_steps} full step(s) of the same workload on the CPU oracle (OpenMP)"}
+        v, cores, sps, done, sample = run_cpu(args.config, args.cpu_steps, warmup=1, time_limit=args.cpu_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+               "ms_per_step": 1e3 * sps}
     if rank == 0:
+        keys = ("ms_per_step", "value", "vcycles_per_step", "vcycle_ms", "launches_per_step", "work_per_step")
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (seeded)", "config": config,
             "precision_split": {
-                "mixed": {k: mixed[k] for k in ("ms_per_step", "value", "vcycles_per_step", "vcycle_ms",
-                                                "launches_per_step")},
-                "fp64": {k: fp64[k] for k in ("ms_per_step", "value", "vcycles_per_step", "vcycle_ms",
-                                               "launches_per_step")},
+                "mixed": {k: mixed[k] for k in keys},
+                "fp64": {k: fp64[k] for k in keys},
                 "speedup_mixed_vs_fp64": fp64["ms_per_step"] / mixed["ms_per_step"]},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None},
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic},
             "kernel_classes": kstats,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": mixed["clocks"],
-            "gpu_launches": int(mixed["launches_per_step"] * args.steps),
+            "gpu_launches": int(mixed["launches"]),
         }))
 
 

@@ -28,6 +28,8 @@
 #ifndef AFIVO_GPU_H
 #define AFIVO_GPU_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -139,6 +141,19 @@ int afg_cc_upload(afg_ctx* ctx, int iv, const double* const* box_cc,
                   long long elem_offset);
 int afg_cc_download(afg_ctx* ctx, int iv, double* const* box_cc,
                     long long elem_offset);
+
+/* Transfer paths of the four copy routines: when every box pointer is
+ * non-NULL, the pointers are equally spaced and the host memory is
+ * page-locked (cudaMallocHost, or afg_host_register below), all boxes move in
+ * one pitched DMA; otherwise the boxes are gathered/scattered by host threads
+ * through a page-locked staging buffer, overlapped with the DMA in 32 MiB
+ * chunks.  Every copy has completed when the call returns. */
+
+/* Page-lock (cudaHostRegister) / release caller-owned host memory, e.g. the
+ * storage behind the box arrays passed to the copy routines.  No counterpart
+ * in the reference (its data never leaves the host). */
+int afg_host_register(afg_ctx* ctx, void* ptr, size_t bytes);
+int afg_host_unregister(afg_ctx* ctx, void* ptr);
 
 /* Same for face-centred variable ivf: box_fc[id-1] points at
  * box%fc(1,1[,1],1,1); elem_offset = (ivf-1)*NDIM*(nc+1)^ndim. */
@@ -275,6 +290,12 @@ typedef struct afg_transport_desc {
   afg_reaction reactions[AFG_MAX_REACTIONS];
   double dt_chemistry_nmin;           /* dt_chemistry_nmin */
   int dt_chemistry_limit_loss;        /* dt_chemistry_limit_loss */
+  /* AFG_FP64: the reference's arithmetic.  AFG_MIXED: the state stays FP64
+   * but the per-cell arithmetic of the fluxes, the reaction sources, the
+   * field gradient and the photon production is FP32; state differences,
+   * the charge density and the final density sums stay FP64.  No counterpart
+   * in the reference. */
+  int precision;
 } afg_transport_desc;
 
 /* Store the transport model (transport_data_initialize, chemistry_initialize). */

@@ -1,0 +1,147 @@
+"""CPU restatement of one time step of the streamer hot path.
+
+Test and baseline infrastructure only: the tests compare the GPU time step
+with it, and the benchmark times it as the CPU baseline.  It drives the C++
+restatement (``oracle.Oracle``) in the order of the reference's time loop
+(src/streamer.f90:181-432):
+
+* photoionization every `photoi_per_steps` steps (photoi_set_src,
+  src/streamer.f90:242-248): photon production on the leaves
+  (src/m_photoi_helmh.f90:162-204 via photoi_get_source), then per Helmholtz
+  mode FMG cycles until the residual drops below 1e-2 of the source maximum,
+  and i_photo -= c_n * mode_n on the leaves;
+* copy_current_state (src/streamer.f90:659-671);
+* Heun's method (afivo/src/m_af_advance.f90:160-164) whose stages are
+  forward_euler (src/m_fluid.f90:21-99): fluxes of state s_deriv, densities
+  of the stage, and field_compute (src/m_field.f90:450-520) of the stage's
+  output state.
+
+`step()` returns the cell-updates of the step with the same accounting as the
+GPU counters: smoother updates of every V-cycle ((n_cycle_down + n_cycle_up)
+times the cells of levels 2..max_lvl) plus leaf cells x species per stage.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.join(HERE, "..", "afivo-streamer_gb300"))
+
+import afivo_gpu as ag  # noqa: E402
+import oracle  # noqa: E402
+
+
+class OracleStreamerRun:
+    def __init__(self, tree, model, voltage, dt, max_rel_residual=1e-8, num_vcycles=30, photoi=None,
+                 photoi_per_steps=5):
+        self.tree, self.m = tree, model
+        self.voltage, self.dt = voltage, dt
+        self.rel = max_rel_residual
+        self.num_vcycles = num_vcycles
+        self.photoi = photoi          # (lambdas 1/m, coeffs 1/m^2, eta*quench)
+        self.photoi_per_steps = photoi_per_steps
+        self.it = 0
+        self.L = float(tree.dr[0, -1] * tree.coarse_grid_size[-1])
+        self.o = oracle.Oracle(tree, model.n_var_cell, model.n_var_face)
+        D, nc = tree.ndim, tree.n_cell
+        self.leaves = np.concatenate(tree.lvl_leaves) - 1
+        self.ncell_leaf = len(self.leaves) * nc ** D
+        self.level_cells = [len(tree.lvl_ids[l]) * nc ** D for l in range(tree.highest_lvl)]
+        self.min_dr = float(np.min(tree.dr[tree.lvl_ids[-1][0] - 1]))
+        self.last = {}
+
+    def vcycle_updates(self, max_lvl, mg):
+        return (mg.n_cycle_down + mg.n_cycle_up) * sum(self.level_cells[1:max_lvl])
+
+    def setup(self):
+        o, m = self.o, self.m
+        D = self.tree.ndim
+        o.transport_setup(m.transport_desc())
+        o.set_cc_methods(m.i_electric_fld, *m.electric_fld_gc())
+        for s in range(len(m.species)):
+            for st in range(m.n_states):
+                o.set_cc_methods(m.species_iv[s] + st, [m.bc_species] * (2 * D), None, ag.RB_INTERP_LIM)
+        if m.i_photo:
+            o.set_cc_methods(m.i_photo, *m.photo_gc())
+        self.field_desc = m.field_mg(self.voltage)
+        o.mg_setup(0, self.field_desc)
+        self.mode_descs = []
+        if self.photoi is not None:
+            for n, d in enumerate(m.helmholtz_mg(self.photoi[0])):
+                o.mg_setup(1 + n, d)
+                self.mode_descs.append(d)
+
+    def field(self, cc, fc, s_in, have_guess):
+        """field_compute: rhs, residual threshold, FMG start without a guess,
+        V-cycles to the threshold, E from the potential."""
+        o, m = self.o, self.m
+        H = self.tree.highest_lvl
+        o.field_set_rhs(cc, m.i_rhs, s_in)
+        max_rhs = o.maxabs(cc, m.i_rhs)
+        thr = max(1e-6, max_rhs * self.rel, 1e-10 * abs(self.voltage) / (self.L * self.min_dr))
+        work = nv = 0
+        if not have_guess:
+            res = []
+            for i in range(100):
+                res.append(o.mg_fmg(cc, 0, True, True))
+                nv += 1
+                work += sum(self.vcycle_updates(l, self.field_desc) for l in range(1, H + 1))
+                if res[-1] < thr:
+                    break
+                if i >= 2:
+                    ratio = min(res[-3:]) / max(res[-3:])
+                    if 0.5 < ratio < 2.0 and res[-1] < 1e8:
+                        break
+        for _ in range(self.num_vcycles):
+            r = o.mg_vcycle(cc, 0, True)
+            nv += 1
+            work += self.vcycle_updates(H, self.field_desc)
+            if r < thr:
+                break
+        o.field_from_potential(cc, fc, m.i_phi)
+        self.last["vcycles"] = self.last.get("vcycles", 0) + nv
+        return work
+
+    def initial_field(self, cc, fc):
+        self.o.gc(cc, self.m.i_phi, 0, True)
+        return self.field(cc, fc, 0, False)
+
+    def photoionization(self, cc):
+        o, m = self.o, self.m
+        lam, coeffs, coeff = self.photoi
+        H = self.tree.highest_lvl
+        o.photoi_source(cc, coeff, m.i_rhs)
+        cc[:, m.i_photo - 1] = 0.0
+        max_rhs = max(o.maxabs(cc, m.i_rhs), np.sqrt(np.finfo(float).eps))
+        work = 0
+        for n, d in enumerate(self.mode_descs):
+            for _ in range(10):
+                r = o.mg_fmg(cc, 1 + n, True, True)
+                work += sum(self.vcycle_updates(l, d) for l in range(1, H + 1))
+                if r / max_rhs < 1e-2:
+                    break
+            cc[self.leaves, m.i_photo - 1] -= coeffs[n] * cc[self.leaves, m.i_modes[n] - 1]
+        return work
+
+    def step(self, cc, fc):
+        o, m, dt = self.o, self.m, self.dt
+        self.last = {"vcycles": 0}
+        work = 0
+        if self.photoi is not None and self.it % self.photoi_per_steps == 0:
+            work += self.photoionization(cc)
+        for s in range(len(m.species)):
+            cc[:, m.species_iv[s] + m.n_states - 2] = cc[:, m.species_iv[s] - 1]
+        lim1 = o.flux_upwind(cc, fc, 0)
+        o.update_densities(cc, fc, dt, 0, [0], [1.0], 1)
+        work += self.field(cc, fc, 1, True)
+        lim2 = o.flux_upwind(cc, fc, 1)
+        chem = o.update_densities(cc, fc, 0.5 * dt, 1, [0, 1], [0.5, 0.5], 0, True)
+        work += self.field(cc, fc, 0, True)
+        work += 2 * self.ncell_leaf * len(m.species)
+        self.last.update(cfl=min(lim1[0], lim2[0]), drt=min(lim1[1], lim2[1]), chem=chem)
+        self.it += 1
+        return work
