@@ -39,6 +39,46 @@ struct KTree {
   const float* idrf;  // the same rounded to FP32
 };
 
+// Box size as a compile-time constant: kernels carry a template parameter NC
+// (0 = take the sizes from the tree) and start with t = fix_dims<D, NC>(t0).
+// With NC > 0 the sizes are constants, so the index arithmetic (divisions by
+// nc and nc + 2 in the flat cell and face loops) compiles to shifts and
+// multiplications.
+template <int D, int NC>
+__device__ __forceinline__ KTree fix_dims(KTree t) {
+  if (NC > 0) {
+    t.nc = NC;
+    t.n2 = NC + 2;
+    t.S = D == 2 ? (NC + 2) * (NC + 2) : (NC + 2) * (NC + 2) * (NC + 2);
+    t.NF = D == 2 ? (NC + 1) * (NC + 1) : (NC + 1) * (NC + 1) * (NC + 1);
+  }
+  return t;
+}
+
+// Launch-site dispatch on the box size: 8^3-cell boxes in 3D and 16^2-cell
+// boxes in 2D (the usual afivo-streamer sizes) get their own instantiation,
+// other sizes the generic one.  `ctx` must be in scope.
+#define AFG_NC3(NCV, ...)         \
+  do {                            \
+    if (ctx->nc == 8) {           \
+      constexpr int NCV = 8;      \
+      __VA_ARGS__;                \
+    } else {                      \
+      constexpr int NCV = 0;      \
+      __VA_ARGS__;                \
+    }                             \
+  } while (0)
+#define AFG_NC2(NCV, ...)         \
+  do {                            \
+    if (ctx->nc == 16) {          \
+      constexpr int NCV = 16;     \
+      __VA_ARGS__;                \
+    } else {                      \
+      constexpr int NCV = 0;      \
+      __VA_ARGS__;                \
+    }                             \
+  } while (0)
+
 // Double <-> float conversions by IEEE-754 bit manipulation, for the FP32
 // arithmetic of the mixed-precision kernels: integer instructions only, so
 // the conversions do not queue on the FP64 pipe.  d2f truncates the mantissa
@@ -97,6 +137,23 @@ struct GcDev {
   double bc_val[6];
   int rb;
 };
+
+// bc_type[nb] / bc_val[nb] of a ghost-cell method for a run-time face index,
+// through selects so that the kernel parameter is not copied to local memory
+__device__ __forceinline__ int gc_type(const GcDev& g, int nb) {
+  int r = g.bc_type[0];
+#pragma unroll
+  for (int k = 1; k < 6; k++)
+    if (nb == k) r = g.bc_type[k];
+  return r;
+}
+__device__ __forceinline__ double gc_val(const GcDev& g, int nb) {
+  double r = g.bc_val[0];
+#pragma unroll
+  for (int k = 1; k < 6; k++)
+    if (nb == k) r = g.bc_val[k];
+  return r;
+}
 
 __device__ __forceinline__ int at2(int n2, int i, int j) { return i + n2 * j; }
 __device__ __forceinline__ int at3(int n2, int i, int j, int k) { return i + n2 * (j + n2 * k); }

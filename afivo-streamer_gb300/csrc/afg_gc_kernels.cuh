@@ -36,7 +36,7 @@ __device__ __forceinline__ T face_ghost(const KTree& t, const T* __restrict__ v,
   }
   if (nbs == kNbPhys) {
     const int i1 = low ? 1 : nc, i2 = low ? 2 : nc - 1;
-    return bc_ghost<D, T>(g.bc_type[nb], g.bc_val[nb], t.dr[slot * D + d], low,
+    return bc_ghost<D, T>(gc_type(g, nb), gc_val(g, nb), t.dr[slot * D + d], low,
                           a[face_at<D>(n2, d, i1, p, q)], a[face_at<D>(n2, d, i2, p, q)]);
   }
   // refinement boundary: data of the parent's neighbour
@@ -118,21 +118,24 @@ __device__ void corner_ghosts(const KTree& t, T* __restrict__ v, int slot) {
       const int n = w / nc, pp = w % nc + 1;
       const int dim = c_edge_dim[n];
       const int dx = c_edge_dir[n][0], dy = c_edge_dir[n][1], dz = c_edge_dir[n][2];
-      int x[3] = {(dx == 1) * (nc + 1), (dy == 1) * (nc + 1), (dz == 1) * (nc + 1)};
-      x[dim] = pp;
+      // the edge cell (kept in scalars: no dynamically indexed arrays)
+      const int x0 = dim == 0 ? pp : (dx == 1) * (nc + 1);
+      const int x1 = dim == 1 ? pp : (dy == 1) * (nc + 1);
+      const int x2 = dim == 2 ? pp : (dz == 1) * (nc + 1);
+      const int c = at3(n2, x0, x1, x2);
       const int nbs = nbmat_at(t, slot, dx, dy, dz);
       if (nbs >= 0) {
         const T* b = v + (size_t)nbs * t.S;
-        a[at3(n2, x[0], x[1], x[2])] = b[at3(n2, x[0] - dx * nc, x[1] - dy * nc, x[2] - dz * nc)];
+        a[c] = b[at3(n2, x0 - dx * nc, x1 - dy * nc, x2 - dz * nc)];
       } else {
-        const int o1 = (dim + 1) % 3, o2 = (dim + 2) % 3;
-        int di[3] = {1 - 2 * (x[0] & 1), 1 - 2 * (x[1] & 1), 1 - 2 * (x[2] & 1)};
-        di[dim] = 0;
-        int ia[3] = {x[0], x[1], x[2]}, ib[3] = {x[0], x[1], x[2]};
-        ia[o1] += di[o1];
-        ib[o2] += di[o2];
-        a[at3(n2, x[0], x[1], x[2])] = a[at3(n2, ia[0], ia[1], ia[2])] + a[at3(n2, ib[0], ib[1], ib[2])] -
-                                       a[at3(n2, x[0] + di[0], x[1] + di[1], x[2] + di[2])];
+        // steps towards the interior across the two other dimensions o1 =
+        // dim+1, o2 = dim+2 (mod 3): a(o1 step) + a(o2 step) - a(both)
+        const int s0 = dim == 0 ? 0 : 1 - 2 * (x0 & 1);
+        const int s1 = dim == 1 ? 0 : (1 - 2 * (x1 & 1)) * n2;
+        const int s2 = dim == 2 ? 0 : (1 - 2 * (x2 & 1)) * n2 * n2;
+        const int ua = dim == 0 ? c + s1 : (dim == 1 ? c + s2 : c + s0);
+        const int ub = dim == 0 ? c + s2 : (dim == 1 ? c + s0 : c + s1);
+        a[c] = a[ua] + a[ub] - a[c + s0 + s1 + s2];
       }
     }
     __syncthreads();
@@ -164,14 +167,17 @@ __device__ void corner_ghosts(const KTree& t, T* __restrict__ v, int slot) {
 }
 
 // af_gc_lvl on a box list: one CTA per box.
-template <int D, typename T>
-__global__ void __launch_bounds__(256) k_gc(KTree t, const int* __restrict__ list, T* __restrict__ v,
+template <int D, typename T, int NC = 0>
+__global__ void __launch_bounds__(256) k_gc(KTree t0, const int* __restrict__ list, T* __restrict__ v,
                                             GcDev g, int corners) {
+  const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   const int nc = t.nc;
   const int nface = D == 2 ? nc : nc * nc;
   T* a = v + (size_t)slot * t.S;
-  for (int w = threadIdx.x; w < 2 * D * nface; w += blockDim.x) {
+  // corners: 0 = face ghosts, 1 = faces then edges/corners, 2 = only the
+  // edges/corners (face ghosts already valid)
+  for (int w = threadIdx.x; corners != 2 && w < 2 * D * nface; w += blockDim.x) {
     const int nb = w / nface, pq = w - nb * nface;
     const int p = pq % nc + 1, q = D == 3 ? pq / nc + 1 : 0;
     const int d = nb >> 1;

@@ -59,9 +59,10 @@ __device__ __forceinline__ T apply_lpl(const T* __restrict__ p, int n2, int i, i
 
 // One red-black half sweep on each box of the list; stencil_gsrb_357
 // (m_af_stencil.f90:838-998).  Updated cells satisfy (i+j[+k]+n) even.
-template <int D, bool CYL, typename T>
-__global__ void __launch_bounds__(256) k_gsrb(KTree t, const int* __restrict__ list, T* __restrict__ phi,
+template <int D, bool CYL, typename T, int NC = 0>
+__global__ void __launch_bounds__(256) k_gsrb(KTree t0, const int* __restrict__ list, T* __restrict__ phi,
                                               const T* __restrict__ rhs, int redblack, MgCoef<T> mc) {
+  const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2, hn = nc / 2;
   T c[7];
@@ -102,10 +103,11 @@ __global__ void __launch_bounds__(256) k_gsrb(KTree t, const int* __restrict__ l
 // cells of the other colour, on the coarse level, and on the updated cell
 // itself before its update.  One ghost fill after the last half sweep then
 // leaves memory exactly as the reference does.
-template <int D, bool CYL, typename T>
-__global__ void __launch_bounds__(256) k_gsrb_fused(KTree t, const int* __restrict__ list, T* __restrict__ phi,
+template <int D, bool CYL, typename T, int NC = 0>
+__global__ void __launch_bounds__(256) k_gsrb_fused(KTree t0, const int* __restrict__ list, T* __restrict__ phi,
                                                     const T* __restrict__ rhs, int redblack, MgCoef<T> mc,
                                                     GcDev g) {
+  const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2, hn = nc / 2;
   T c[7];
@@ -148,11 +150,12 @@ __global__ void __launch_bounds__(256) k_gsrb_fused(KTree t, const int* __restri
 // Residual on interior cells into tmp (residual_box, m_af_multigrid.f90:
 // 801-810); the max |r| over the boxes flagged in is_leaf is folded into
 // *maxbits (may be null).
-template <int D, bool CYL, typename T>
-__global__ void __launch_bounds__(256) k_residual(KTree t, const int* __restrict__ list, const T* __restrict__ phi,
+template <int D, bool CYL, typename T, int NC = 0>
+__global__ void __launch_bounds__(256) k_residual(KTree t0, const int* __restrict__ list, const T* __restrict__ phi,
                                                   const T* __restrict__ rhs, T* __restrict__ tmp, MgCoef<T> mc,
                                                   const unsigned char* __restrict__ is_leaf,
                                                   unsigned long long* maxbits) {
+  const KTree t = fix_dims<D, NC>(t0);
   __shared__ T sred[32];
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;
@@ -187,11 +190,12 @@ __global__ void __launch_bounds__(256) k_residual(KTree t, const int* __restrict
 // af_restrict_box use_geometry=.true., m_af_restrict.f90:62-136), phi
 // restricted without geometry (mg_box_rstr_lpl 1227-1242).  One thread per
 // parent cell covered by the child.
-template <int D, bool CYL, typename T>
-__global__ void __launch_bounds__(256) k_residual_restrict(KTree t, const int* __restrict__ list,
+template <int D, bool CYL, typename T, int NC = 0>
+__global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* __restrict__ list,
                                                            T* __restrict__ phi, const T* __restrict__ rhs,
                                                            T* __restrict__ tmp, MgCoef<T> mc,
                                                            int store_child_residual) {
+  const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   const int pslot = t.parent[slot];
   const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
@@ -263,10 +267,11 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t, const int* _
 // reference also adds tmp to rhs in the ghost cells; rhs ghost cells are
 // never read, so they are left untouched.  With copy_tmp = 0 this is the
 // rhs part of set_coarse_phi_rhs (742-776).
-template <int D, bool CYL, typename T>
-__global__ void __launch_bounds__(256) k_coarse_fas(KTree t, const int* __restrict__ list,
+template <int D, bool CYL, typename T, int NC = 0>
+__global__ void __launch_bounds__(256) k_coarse_fas(KTree t0, const int* __restrict__ list,
                                                     const T* __restrict__ phi, T* __restrict__ rhs,
                                                     T* __restrict__ tmp, MgCoef<T> mc, int copy_tmp) {
+  const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;
   T c[7];
@@ -295,9 +300,10 @@ __global__ void __launch_bounds__(256) k_coarse_fas(KTree t, const int* __restri
 // tmp = phi - tmp over the whole array, then each child's phi gets the
 // bilinear/trilinear prolongation of tmp added (stencil_prolong_248,
 // m_af_stencil.f90:695-815, coefficients 1267-1284).
-template <int D, typename T>
-__global__ void __launch_bounds__(256) k_correct(KTree t, const int* __restrict__ list, T* __restrict__ phi,
+template <int D, typename T, int NC = 0>
+__global__ void __launch_bounds__(256) k_correct(KTree t0, const int* __restrict__ list, T* __restrict__ phi,
                                                  T* __restrict__ tmp) {
+  const KTree t = fix_dims<D, NC>(t0);
   extern __shared__ unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   const int slot = list[blockIdx.x];
@@ -340,9 +346,10 @@ __global__ void __launch_bounds__(256) k_correct(KTree t, const int* __restrict_
 
 // init_phi_rhs (m_af_multigrid.f90:779-799) on one level: phi = 0 on the
 // whole array, rhs restricted to the parent with geometry.
-template <int D, bool CYL, typename T>
-__global__ void __launch_bounds__(256) k_init_phi_rhs(KTree t, const int* __restrict__ list,
+template <int D, bool CYL, typename T, int NC = 0>
+__global__ void __launch_bounds__(256) k_init_phi_rhs(KTree t0, const int* __restrict__ list,
                                                       T* __restrict__ phi, T* __restrict__ rhs) {
+  const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   const int pslot = t.parent[slot];
   const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
@@ -432,9 +439,10 @@ __global__ void k_coarse_scatter(int n, const int* __restrict__ cslot, const int
 }
 
 // max |v| over interior cells of the list's boxes
-template <int D, typename T>
-__global__ void __launch_bounds__(256) k_maxabs(KTree t, const int* __restrict__ list, const T* __restrict__ v,
+template <int D, typename T, int NC = 0>
+__global__ void __launch_bounds__(256) k_maxabs(KTree t0, const int* __restrict__ list, const T* __restrict__ v,
                                                 unsigned long long* maxbits) {
+  const KTree t = fix_dims<D, NC>(t0);
   __shared__ T sred[32];
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;

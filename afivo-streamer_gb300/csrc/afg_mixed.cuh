@@ -18,12 +18,13 @@ namespace afg {
 // over leaves into *maxbits.  The Cartesian stencil is one FMA chain (8 FP64
 // instructions per cell); r is rounded to FP32 by bit truncation and its
 // maximum taken in FP32.
-template <int D, bool CYL>
-__global__ void __launch_bounds__(256) k_defect(KTree t, const int* __restrict__ list, const double* __restrict__ phi,
+template <int D, bool CYL, int NC = 0>
+__global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict__ list, const double* __restrict__ phi,
                                                 const double* __restrict__ rhs, float* __restrict__ r32,
                                                 float* __restrict__ e32, MgCoef<double> mc,
                                                 const unsigned char* __restrict__ is_leaf,
                                                 unsigned long long* maxbits) {
+  const KTree t = fix_dims<D, NC>(t0);
   __shared__ float sred[32];
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;
@@ -34,6 +35,8 @@ __global__ void __launch_bounds__(256) k_defect(KTree t, const int* __restrict__
   float* ro = r32 + (size_t)slot * t.S;
   float* eo = e32 + (size_t)slot * t.S;
   for (int x = threadIdx.x; x < t.S; x += blockDim.x) eo[x] = 0.0f;
+  // parents need no defect: the V-cycle's restriction overwrites their rhs
+  if (!is_leaf[slot]) return;
   float mx = 0.0f;
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;
   for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
@@ -60,10 +63,20 @@ __global__ void __launch_bounds__(256) k_defect(KTree t, const int* __restrict__
     ro[x] = res;
     mx = fmaxf(mx, fabsf(res));
   }
-  if (is_leaf[slot]) {
-    mx = block_max<float>(mx, sred);
-    if (threadIdx.x == 0) atomic_max_nonneg(maxbits, f2d(mx));
-  }
+  mx = block_max<float>(mx, sred);
+  if (threadIdx.x == 0) atomic_max_nonneg(maxbits, f2d(mx));
+}
+
+// Whole-box conversions between the FP64 variables and the FP32 buffers
+__global__ void __launch_bounds__(256) k_to_f32(int S, const int* __restrict__ list, const double* __restrict__ src,
+                                                float* __restrict__ dst) {
+  const size_t base = (size_t)list[blockIdx.x] * S;
+  for (int x = threadIdx.x; x < S; x += blockDim.x) dst[base + x] = d2f(src[base + x]);
+}
+__global__ void __launch_bounds__(256) k_to_f64(int S, const int* __restrict__ list, const float* __restrict__ src,
+                                                double* __restrict__ dst) {
+  const size_t base = (size_t)list[blockIdx.x] * S;
+  for (int x = threadIdx.x; x < S; x += blockDim.x) dst[base + x] = f2d(src[base + x]);
 }
 
 // phi += e on whole boxes (ghost cells included)
@@ -83,14 +96,14 @@ static int launch_defect(afg_ctx* ctx, MgSlot& m, const double* phi, const doubl
   KTree t = ktree(ctx);
   const int* list = lst(ctx, ctx->off_all);
   if (ctx->D == 3)
-    k_defect<3, false><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), ctx->d_is_leaf,
-                                                   maxbits);
+    AFG_NC3(NCV_, k_defect<3, false, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), ctx->d_is_leaf,
+                                                   maxbits));
   else if (ctx->coord == AFG_CYL)
-    k_defect<2, true><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), ctx->d_is_leaf,
-                                                  maxbits);
+    AFG_NC2(NCV_, k_defect<2, true, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), ctx->d_is_leaf,
+                                                  maxbits));
   else
-    k_defect<2, false><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), ctx->d_is_leaf,
-                                                   maxbits);
+    AFG_NC2(NCV_, k_defect<2, false, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), ctx->d_is_leaf,
+                                                   maxbits));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -107,15 +120,48 @@ static int mixed_prepare(afg_ctx* ctx, MgSlot& m, double* phi) {
     const int n = (int)ctx->lvl_ids[lvl - 1].size();
     if (n == 0) continue;
     if (ctx->D == 3)
-      k_restrict_geom<3, false><<<n, 64, 0, ctx->stream>>>(t, lst(ctx, ctx->off_ids[lvl - 1]), phi);
+      AFG_NC3(NCV_, k_restrict_geom<3, false, NCV_><<<n, 64, 0, ctx->stream>>>(t, lst(ctx, ctx->off_ids[lvl - 1]), phi));
     else
-      k_restrict_geom<2, false><<<n, 64, 0, ctx->stream>>>(t, lst(ctx, ctx->off_ids[lvl - 1]), phi);
+      AFG_NC2(NCV_, k_restrict_geom<2, false, NCV_><<<n, 64, 0, ctx->stream>>>(t, lst(ctx, ctx->off_ids[lvl - 1]), phi));
     ctx->launches++;
     CKL();
   }
+  // the defect's 7-point stencil and the refinement-boundary rules read face
+  // ghosts only; edges and corners are filled once when the solve ends
   const GcDev g = mg_gc(m.d, false);
-  for (int lvl = 1; lvl <= ctx->highest_lvl; lvl++) RC(mg_gc_lvl<double>(ctx, lvl, phi, g, 1));
+  for (int lvl = 1; lvl <= ctx->highest_lvl; lvl++) RC(mg_gc_lvl<double>(ctx, lvl, phi, g, 0));
   return AFG_OK;
+}
+
+static int mixed_finish(afg_ctx* ctx, MgSlot& m, double* phi) {
+  const GcDev g = mg_gc(m.d, false);
+  for (int lvl = 1; lvl <= ctx->highest_lvl; lvl++) RC(mg_gc_lvl<double>(ctx, lvl, phi, g, 2));
+  return AFG_OK;
+}
+
+// FMG of a mixed-precision slot as one defect-correction step: the FP64
+// defect r = rhs - L(phi) (parents restricted first), an FP32 FMG from zero
+// for the correction L e = r with homogeneous boundary values, phi += e, and
+// (set_residual) the FP64 defect of the result.  Without a guess phi starts
+// from zero, so the first correction is the whole solution.  Repeated calls
+// converge like FP64 FMG cycles down to FP64 accuracy: each FP32 FMG only
+// has to reduce the current defect, not resolve phi itself.
+static int mixed_fmg(afg_ctx* ctx, MgSlot& m, double* phi, double* rhs, bool set_residual, bool have_guess,
+                     unsigned long long* maxbits) {
+  const int n = ctx->n_all;
+  if (n <= 0) return AFG_OK;
+  const int* list = lst(ctx, ctx->off_all);
+  if (!have_guess) CK(cudaMemsetAsync(phi, 0, sizeof(double) * (size_t)ctx->n_boxes * ctx->S, ctx->stream));
+  RC(mixed_prepare(ctx, m, phi));
+  RC(reset_max(ctx, 2));
+  RC(launch_defect(ctx, m, phi, rhs, ctx->d_max + 2));
+  RC(mg_fmg<float>(ctx, m, m.e32, m.r32, m.t32, false, false, nullptr, true));
+  k_add_correction<<<n, 256, 0, ctx->stream>>>(ctx->S, list, phi, m.e32);
+  ctx->launches++;
+  CKL();
+  RC(mixed_prepare(ctx, m, phi));
+  if (set_residual) RC(launch_defect(ctx, m, phi, rhs, maxbits));
+  return mixed_finish(ctx, m, phi);
 }
 
 static int mixed_solve(afg_ctx* ctx, MgSlot& m, double threshold, int max_cycles, int* n_done, double* residuals) {
@@ -147,6 +193,7 @@ static int mixed_solve(afg_ctx* ctx, MgSlot& m, double threshold, int max_cycles
     n++;
     if (r < threshold) break;
   }
+  RC(run_graph(ctx, gkey("mixed_finish", mg_id), [&]() -> int { return mixed_finish(ctx, m, phi); }));
   if (n_done) *n_done = n;
   return r < threshold ? AFG_OK : AFG_ERR_NOCONV;
 }

@@ -15,6 +15,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/afivo_gpu.h"
@@ -103,6 +104,7 @@ struct afg_ctx {
   long long ctr[4] = {0, 0, 0, 0};
   cudaEvent_t ev[64] = {};
   cudaEvent_t xfer_ev[2] = {};  // download pipeline
+  std::vector<std::pair<uintptr_t, size_t>> host_regs;  // ranges page-locked by afg_host_register
   void* flush_buf = nullptr;
   size_t flush_bytes = 0;
   int kt_class = 0;
@@ -255,9 +257,9 @@ static int launch_gc(afg_ctx* ctx, const int* list, int n, T* v, const GcDev& g,
   KTree t = ktree(ctx);
   kt_begin(ctx, AFG_KT_GHOST);
   if (ctx->D == 2)
-    k_gc<2, T><<<n, 128, 0, ctx->stream>>>(t, list, v, g, corners);
+    AFG_NC2(NCV_, k_gc<2, T, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, v, g, corners));
   else
-    k_gc<3, T><<<n, 256, 0, ctx->stream>>>(t, list, v, g, corners);
+    AFG_NC3(NCV_, k_gc<3, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, v, g, corners));
   kt_end(ctx, AFG_KT_GHOST, 2.0 * sizeof(T) * n * 2 * ctx->D * (box_cells(ctx) / ctx->nc));
   ctx->launches++;
   CKL();
@@ -271,11 +273,11 @@ static int launch_gsrb(afg_ctx* ctx, const int* list, int n, T* phi, const T* rh
   const int threads = ctx->D == 2 ? std::min(256, ctx->nc * ctx->nc / 2) : std::min(256, ctx->nc * ctx->nc * ctx->nc / 2);
   kt_begin(ctx, AFG_KT_GSRB);
   if (ctx->D == 3)
-    k_gsrb<3, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam);
+    AFG_NC3(NCV_, k_gsrb<3, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam));
   else if (ctx->coord == AFG_CYL)
-    k_gsrb<2, true, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam);
+    AFG_NC2(NCV_, k_gsrb<2, true, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam));
   else
-    k_gsrb<2, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam);
+    AFG_NC2(NCV_, k_gsrb<2, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam));
   // half sweep: 1.5 words per cell (read phi and rhs, write phi over two half sweeps)
   kt_end(ctx, AFG_KT_GSRB, 1.5 * sizeof(T) * n * box_cells(ctx));
   ctx->launches++;
@@ -291,11 +293,11 @@ static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, T* phi, const
   const int threads = ctx->D == 2 ? std::min(256, ctx->nc * ctx->nc / 2) : std::min(256, ctx->nc * ctx->nc * ctx->nc / 2);
   kt_begin(ctx, AFG_KT_GSRB);
   if (ctx->D == 3)
-    k_gsrb_fused<3, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
+    AFG_NC3(NCV_, k_gsrb_fused<3, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g));
   else if (ctx->coord == AFG_CYL)
-    k_gsrb_fused<2, true, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
+    AFG_NC2(NCV_, k_gsrb_fused<2, true, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g));
   else
-    k_gsrb_fused<2, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
+    AFG_NC2(NCV_, k_gsrb_fused<2, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g));
   kt_end(ctx, AFG_KT_GSRB, 1.5 * sizeof(T) * n * box_cells(ctx));
   ctx->launches++;
   CKL();
@@ -308,11 +310,11 @@ static int launch_residual(afg_ctx* ctx, const int* list, int n, const T* phi, c
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   if (ctx->D == 3)
-    k_residual<3, false, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, ctx->d_is_leaf, maxbits);
+    AFG_NC3(NCV_, k_residual<3, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, ctx->d_is_leaf, maxbits));
   else if (ctx->coord == AFG_CYL)
-    k_residual<2, true, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, ctx->d_is_leaf, maxbits);
+    AFG_NC2(NCV_, k_residual<2, true, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, ctx->d_is_leaf, maxbits));
   else
-    k_residual<2, false, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, ctx->d_is_leaf, maxbits);
+    AFG_NC2(NCV_, k_residual<2, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, ctx->d_is_leaf, maxbits));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -326,11 +328,11 @@ static int launch_rrestrict(afg_ctx* ctx, const int* list, int n, T* phi, const 
   const int hnc = ctx->nc / 2;
   const int threads = std::max(32, std::min(256, ctx->D == 2 ? hnc * hnc : hnc * hnc * hnc));
   if (ctx->D == 3)
-    k_residual_restrict<3, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child);
+    AFG_NC3(NCV_, k_residual_restrict<3, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child));
   else if (ctx->coord == AFG_CYL)
-    k_residual_restrict<2, true, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child);
+    AFG_NC2(NCV_, k_residual_restrict<2, true, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child));
   else
-    k_residual_restrict<2, false, T><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child);
+    AFG_NC2(NCV_, k_residual_restrict<2, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -342,11 +344,11 @@ static int launch_coarse_fas(afg_ctx* ctx, const int* list, int n, const T* phi,
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   if (ctx->D == 3)
-    k_coarse_fas<3, false, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp);
+    AFG_NC3(NCV_, k_coarse_fas<3, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp));
   else if (ctx->coord == AFG_CYL)
-    k_coarse_fas<2, true, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp);
+    AFG_NC2(NCV_, k_coarse_fas<2, true, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp));
   else
-    k_coarse_fas<2, false, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp);
+    AFG_NC2(NCV_, k_coarse_fas<2, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -358,9 +360,9 @@ static int launch_correct(afg_ctx* ctx, const int* list, int n, T* phi, T* tmp) 
   KTree t = ktree(ctx);
   const size_t sm = sizeof(T) * ctx->S;
   if (ctx->D == 3)
-    k_correct<3, T><<<n, 256, sm, ctx->stream>>>(t, list, phi, tmp);
+    AFG_NC3(NCV_, k_correct<3, T, NCV_><<<n, 256, sm, ctx->stream>>>(t, list, phi, tmp));
   else
-    k_correct<2, T><<<n, 256, sm, ctx->stream>>>(t, list, phi, tmp);
+    AFG_NC2(NCV_, k_correct<2, T, NCV_><<<n, 256, sm, ctx->stream>>>(t, list, phi, tmp));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -371,11 +373,11 @@ static int launch_init_phi_rhs(afg_ctx* ctx, const int* list, int n, T* phi, T* 
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   if (ctx->D == 3)
-    k_init_phi_rhs<3, false, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs);
+    AFG_NC3(NCV_, k_init_phi_rhs<3, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs));
   else if (ctx->coord == AFG_CYL)
-    k_init_phi_rhs<2, true, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs);
+    AFG_NC2(NCV_, k_init_phi_rhs<2, true, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs));
   else
-    k_init_phi_rhs<2, false, T><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs);
+    AFG_NC2(NCV_, k_init_phi_rhs<2, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -395,9 +397,9 @@ static int launch_maxabs(afg_ctx* ctx, const int* list, int n, const T* v, unsig
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   if (ctx->D == 3)
-    k_maxabs<3, T><<<n, 256, 0, ctx->stream>>>(t, list, v, out);
+    AFG_NC3(NCV_, k_maxabs<3, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, v, out));
   else
-    k_maxabs<2, T><<<n, 256, 0, ctx->stream>>>(t, list, v, out);
+    AFG_NC2(NCV_, k_maxabs<2, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, v, out));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -579,8 +581,8 @@ static int mg_vcycle(afg_ctx* ctx, MgSlot& m, int max_lvl, T* phi, T* rhs, T* tm
 // mg_fas_fmg, m_af_multigrid.f90:137-180
 template <typename T>
 static int mg_fmg(afg_ctx* ctx, MgSlot& m, T* phi, T* rhs, T* tmp, bool set_residual, bool have_guess,
-                  unsigned long long* maxbits) {
-  const GcDev g = mg_gc(m.d, false);
+                  unsigned long long* maxbits, bool homogeneous = false) {
+  const GcDev g = mg_gc(m.d, homogeneous);
   const int H = ctx->highest_lvl;
   if (have_guess) {
     for (int lvl = H; lvl >= 2; lvl--) RC(mg_set_coarse_phi_rhs<T>(ctx, m, lvl, phi, rhs, tmp, g));
@@ -589,11 +591,11 @@ static int mg_fmg(afg_ctx* ctx, MgSlot& m, T* phi, T* rhs, T* tmp, bool set_resi
       RC(launch_init_phi_rhs<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs));
   }
   RC(launch_copy<T>(ctx, lst(ctx, ctx->off_ids[0]), (int)ctx->lvl_ids[0].size(), phi, tmp));
-  RC(mg_vcycle<T>(ctx, m, 1, phi, rhs, tmp, set_residual && H == 1, false, maxbits));
+  RC(mg_vcycle<T>(ctx, m, 1, phi, rhs, tmp, set_residual && H == 1, homogeneous, maxbits));
   for (int lvl = 2; lvl <= H; lvl++) {
     RC(launch_copy<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, tmp));
     RC(mg_correct<T>(ctx, lvl, phi, tmp, g));
-    RC(mg_vcycle<T>(ctx, m, lvl, phi, rhs, tmp, set_residual && lvl == H, false, maxbits));
+    RC(mg_vcycle<T>(ctx, m, lvl, phi, rhs, tmp, set_residual && lvl == H, homogeneous, maxbits));
   }
   return AFG_OK;
 }
@@ -899,6 +901,56 @@ static bool pitched_boxes(int n, size_t E, const double* const* box, long long o
   return is_page_locked(box[0] + off) && is_page_locked(box[n - 1] + off + E - 1);
 }
 
+// Box copies between a device pool and host boxes in mapped page-locked
+// memory, done by the GPU itself (loads/stores over the host link).
+__global__ void __launch_bounds__(256) k_gather_pitched(double* __restrict__ dst, const double* __restrict__ src,
+                                                        size_t pitch, int E, int n, int vec2) {
+  for (int b = blockIdx.x; b < n; b += gridDim.x) {
+    const double* s = src + (size_t)b * pitch;
+    double* d = dst + (size_t)b * E;
+    if (vec2) {
+      const double2* s2 = reinterpret_cast<const double2*>(s);
+      double2* d2 = reinterpret_cast<double2*>(d);
+      for (int x = threadIdx.x; x < E / 2; x += blockDim.x) d2[x] = s2[x];
+    } else {
+      for (int x = threadIdx.x; x < E; x += blockDim.x) d[x] = s[x];
+    }
+  }
+}
+__global__ void __launch_bounds__(256) k_scatter_pitched(double* __restrict__ dst, const double* __restrict__ src,
+                                                         size_t pitch, int E, int n, int vec2) {
+  for (int b = blockIdx.x; b < n; b += gridDim.x) {
+    const double* s = src + (size_t)b * E;
+    double* d = dst + (size_t)b * pitch;
+    if (vec2) {
+      const double2* s2 = reinterpret_cast<const double2*>(s);
+      double2* d2 = reinterpret_cast<double2*>(d);
+      for (int x = threadIdx.x; x < E / 2; x += blockDim.x) d2[x] = s2[x];
+    } else {
+      for (int x = threadIdx.x; x < E; x += blockDim.x) d[x] = s[x];
+    }
+  }
+}
+
+// Device address of [p, p + bytes) when the whole span lies inside one range
+// page-locked by afg_host_register (mapped, so the GPU may access it);
+// nullptr otherwise.
+static const void* registered_span(afg_ctx* ctx, const void* p, size_t bytes) {
+  const uintptr_t a = (uintptr_t)p;
+  for (const auto& r : ctx->host_regs)
+    if (a >= r.first && a + bytes <= r.first + r.second) {
+      void* dev = nullptr;
+      if (cudaHostGetDevicePointer(&dev, const_cast<void*>(p), 0) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+      }
+      return dev;
+    }
+  return nullptr;
+}
+
+static int xfer_grid(int n) { return std::max(1, std::min(n, 152 * 16)); }
+
 // Boxes 0..n-1 of a device pool with E elements per box <- host box arrays
 // (null entries skipped: their device data is left as it is).
 static int h2d_boxes(afg_ctx* ctx, double* dst, size_t E, const double* const* box, long long off) {
@@ -906,8 +958,16 @@ static int h2d_boxes(afg_ctx* ctx, double* dst, size_t E, const double* const* b
   size_t pitch = 0;
   CK(cudaStreamSynchronize(ctx->stream));
   if (pitched_boxes(n, E, box, off, &pitch)) {
-    CK(cudaMemcpy2DAsync(dst, E * sizeof(double), box[0] + off, pitch * sizeof(double), E * sizeof(double), n,
-                         cudaMemcpyHostToDevice, ctx->stream));
+    const double* first = box[0] + off;
+    const void* dev = registered_span(ctx, first, sizeof(double) * ((size_t)(n - 1) * pitch + E));
+    if (dev) {
+      const int vec2 = ((uintptr_t)dev % 16 == 0) && pitch % 2 == 0 && E % 2 == 0;
+      k_gather_pitched<<<xfer_grid(n), 256, 0, ctx->stream>>>(dst, (const double*)dev, pitch, (int)E, n, vec2);
+      CK(cudaGetLastError());
+    } else {
+      CK(cudaMemcpy2DAsync(dst, E * sizeof(double), first, pitch * sizeof(double), E * sizeof(double), n,
+                           cudaMemcpyHostToDevice, ctx->stream));
+    }
     CK(cudaStreamSynchronize(ctx->stream));
     return AFG_OK;
   }
@@ -936,8 +996,16 @@ static int d2h_boxes(afg_ctx* ctx, const double* src, size_t E, double* const* b
   const int n = ctx->n_boxes;
   size_t pitch = 0;
   if (pitched_boxes(n, E, box, off, &pitch)) {
-    CK(cudaMemcpy2DAsync(box[0] + off, pitch * sizeof(double), src, E * sizeof(double), E * sizeof(double), n,
-                         cudaMemcpyDeviceToHost, ctx->stream));
+    double* first = box[0] + off;
+    const void* dev = registered_span(ctx, first, sizeof(double) * ((size_t)(n - 1) * pitch + E));
+    if (dev) {
+      const int vec2 = ((uintptr_t)dev % 16 == 0) && pitch % 2 == 0 && E % 2 == 0;
+      k_scatter_pitched<<<xfer_grid(n), 256, 0, ctx->stream>>>((double*)dev, src, pitch, (int)E, n, vec2);
+      CK(cudaGetLastError());
+    } else {
+      CK(cudaMemcpy2DAsync(first, pitch * sizeof(double), src, E * sizeof(double), E * sizeof(double), n,
+                           cudaMemcpyDeviceToHost, ctx->stream));
+    }
     CK(cudaStreamSynchronize(ctx->stream));
     return AFG_OK;
   }
@@ -989,12 +1057,19 @@ int afg_fc_download(afg_ctx* ctx, int ivf, double* const* box_fc, long long off)
 int afg_host_register(afg_ctx* ctx, void* ptr, size_t bytes) {
   if (!ctx || !ptr || bytes == 0) return AFG_ERR_ARG;
   CK(cudaSetDevice(ctx->device));
-  CK(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+  CK(cudaHostRegister(ptr, bytes, cudaHostRegisterMapped | cudaHostRegisterPortable));
+  ctx->host_regs.emplace_back((uintptr_t)ptr, bytes);
   return AFG_OK;
 }
 
 int afg_host_unregister(afg_ctx* ctx, void* ptr) {
   if (!ctx || !ptr) return AFG_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (size_t q = 0; q < ctx->host_regs.size(); q++)
+    if (ctx->host_regs[q].first == (uintptr_t)ptr) {
+      ctx->host_regs.erase(ctx->host_regs.begin() + q);
+      break;
+    }
   CK(cudaHostUnregister(ptr));
   return AFG_OK;
 }
@@ -1316,6 +1391,8 @@ int afg_mg_fmg(afg_ctx* ctx, int mg_id, int set_residual, int have_guess, double
   MG_VARS(m);
   RC(run_graph(ctx, gkey("fmg", mg_id, set_residual != 0, have_guess != 0), [&]() -> int {
     RC(reset_max(ctx, 1));
+    if (m->d.precision == AFG_MIXED)
+      return mixed_fmg(ctx, *m, phi, rhs, set_residual != 0, have_guess != 0, ctx->d_max + 1);
     return mg_fmg<double>(ctx, *m, phi, rhs, tmp, set_residual != 0, have_guess != 0, ctx->d_max + 1);
   }));
   if (set_residual && max_res) return read_max(ctx, 1, max_res);
@@ -1351,7 +1428,12 @@ extern "C" {
 int afg_tree_copy_cc(afg_ctx* ctx, int iv_from, int iv_to) {
   RC(check_var(ctx, iv_from));
   RC(check_var(ctx, iv_to));
-  return launch_copy<double>(ctx, lst(ctx, ctx->off_all), ctx->n_all, ctx->cc[iv_from - 1], ctx->cc[iv_to - 1]);
+  // every box of the tree: one copy of the whole pool (slots of boxes not in
+  // use hold no data anyone reads)
+  if (iv_from == iv_to) return AFG_OK;
+  CK(cudaMemcpyAsync(ctx->cc[iv_to - 1], ctx->cc[iv_from - 1], sizeof(double) * (size_t)ctx->n_boxes * ctx->S,
+                     cudaMemcpyDeviceToDevice, ctx->stream));
+  return AFG_OK;
 }
 
 int afg_counters(const afg_ctx* ctx, long long* out) {

@@ -120,8 +120,9 @@ struct FluxArgs {
 };
 
 // af_restrict_box with geometry of one variable (m_af_restrict.f90:62-136)
-template <int D, bool CYL>
-__global__ void __launch_bounds__(256) k_restrict_geom(KTree t, const int* __restrict__ list, double* __restrict__ v) {
+template <int D, bool CYL, int NC = 0>
+__global__ void __launch_bounds__(256) k_restrict_geom(KTree t0, const int* __restrict__ list, double* __restrict__ v) {
+  const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   const int pslot = t.parent[slot];
   const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
@@ -191,7 +192,7 @@ __device__ __forceinline__ double gc2_value(const KTree& t, const double* __rest
   if (nbs == kNbPhys) {
     const double* a = v + (size_t)slot * t.S;
     double c0, c1, c2;
-    switch (g.bc_type[nb]) {
+    switch (gc_type(g, nb)) {
       case AFG_BC_DIRICHLET: c0 = 2; c1 = -1; c2 = c0; break;
       case AFG_BC_NEUMANN: c0 = t.dr[slot * D + d] * (low ? -1 : 1); c1 = 1; c2 = 3 * c0; break;
       default: c0 = 1; c1 = 0; c2 = c0; break;
@@ -199,7 +200,7 @@ __device__ __forceinline__ double gc2_value(const KTree& t, const double* __rest
     if (D == 3 && nb == 3) c2 = c0;  // as in the reference's 3D high-y branch
     const int xi = layer == 0 ? (low ? 1 : nc) : (low ? 2 : nc - 1);
     const double cc0 = layer == 0 ? c0 : c2;
-    return cc0 * g.bc_val[nb] + c1 * a[face_at<D>(n2, d, xi, p, q)];
+    return cc0 * gc_val(g, nb) + c1 * a[face_at<D>(n2, d, xi, p, q)];
   }
   // refinement boundary: limited prolongation from the parent's neighbour
   const int cs = t.pnb[slot * 2 * D + nb];
@@ -231,8 +232,9 @@ __device__ __forceinline__ double gc2_value(const KTree& t, const double* __rest
 // flux_direction of the fluid model (src/m_fluid.f90:102-227): Koren-limited
 // upwind reconstruction, v = -mu(E)*E_x, Gamma = v*u - D/dx*(n_f - n_f-1),
 // ions drift only; CFL sum and conductivity maxima reduced to the device.
-template <int D, bool CYL>
-__global__ void __launch_bounds__(256) k_flux(KTree t, const int* __restrict__ list, FluxArgs a) {
+template <int D, bool CYL, int NC = 0>
+__global__ void __launch_bounds__(256) k_flux(KTree t0, const int* __restrict__ list, FluxArgs a) {
+  const KTree t = fix_dims<D, NC>(t0);
   extern __shared__ double sm[];
   __shared__ double sred[32];
   const int slot = list[blockIdx.x];
@@ -363,9 +365,10 @@ __global__ void __launch_bounds__(256) k_flux(KTree t, const int* __restrict__ l
 
 // af_consistent_fluxes / flux_from_children (afivo/src/m_af_core.f90:
 // 1257-1402): one CTA per (parent box, face) task.
-template <int D, bool CYL>
-__global__ void __launch_bounds__(128) k_consistent_flux(KTree t, const int* __restrict__ tasks, int nf,
+template <int D, bool CYL, int NC = 0>
+__global__ void __launch_bounds__(128) k_consistent_flux(KTree t0, const int* __restrict__ tasks, int nf,
                                                          FluxArgs a) {
+  const KTree t = fix_dims<D, NC>(t0);
   const int slot = tasks[2 * blockIdx.x], nb = tasks[2 * blockIdx.x + 1];
   const int nc = t.nc, nch = nc / 2, d = nb >> 1, nf1 = nc + 1;
   const bool low = (nb & 1) == 0;
@@ -494,8 +497,9 @@ __device__ __forceinline__ void add_to(double (&v)[NSMAX], int s, double x) {
 }
 
 // flux_update_densities + add_source_terms for each leaf cell
-template <int D, bool CYL, int NSMAX>
-__global__ void __launch_bounds__(128) k_update(KTree t, const int* __restrict__ list, UpdateArgs a) {
+template <int D, bool CYL, int NSMAX, int NC = 0>
+__global__ void __launch_bounds__(128) k_update(KTree t0, const int* __restrict__ list, UpdateArgs a) {
+  const KTree t = fix_dims<D, NC>(t0);
   __shared__ double sred[32];
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2, nf1 = nc + 1;
@@ -614,9 +618,10 @@ __global__ void __launch_bounds__(256) k_field_rhs(int S, const int* __restrict_
 
 // mg_box_lpl_gradient with fac = -1 (m_af_multigrid.f90:1902-1994) and
 // mg_box_field_norm (2015-2045) on each box of the list
-template <int D>
-__global__ void __launch_bounds__(256) k_field_grad(KTree t, const int* __restrict__ list, const double* __restrict__ phi,
+template <int D, int NC = 0>
+__global__ void __launch_bounds__(256) k_field_grad(KTree t0, const int* __restrict__ list, const double* __restrict__ phi,
                                                     double* __restrict__ efc, double* __restrict__ enorm) {
+  const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2, nf1 = nc + 1;
   const double* p = phi + (size_t)slot * t.S;
@@ -655,10 +660,11 @@ __global__ void __launch_bounds__(256) k_field_grad(KTree t, const int* __restri
 }
 
 // photoionization_rate_from_alpha (src/m_photoi.f90:259-291) on leaves
-template <int D>
-__global__ void __launch_bounds__(256) k_photo_source(KTree t, const int* __restrict__ list, const double* __restrict__ E,
+template <int D, int NC = 0>
+__global__ void __launch_bounds__(256) k_photo_source(KTree t0, const int* __restrict__ list, const double* __restrict__ E,
                                                       const double* __restrict__ ne, double* __restrict__ rhs, LtDev lt,
                                                       int col_alpha, int col_mu, double N, double coeff) {
+  const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;

@@ -62,8 +62,9 @@ struct FluxArgs32 {
 };
 
 // flux_upwind_box with FP32 arithmetic (see k_flux for the reference lines)
-template <int D, bool CYL>
-__global__ void __launch_bounds__(256) k_flux32(KTree t, const int* __restrict__ list, FluxArgs32 a32) {
+template <int D, bool CYL, int NC = 0>
+__global__ void __launch_bounds__(256) k_flux32(KTree t0, const int* __restrict__ list, FluxArgs32 a32) {
+  const KTree t = fix_dims<D, NC>(t0);
   extern __shared__ float smf[];
   __shared__ float sred[32];
   const FluxArgs& a = a32.a;
@@ -234,8 +235,9 @@ __device__ __forceinline__ void add_tof(float (&v)[NSMAX], int s, float x) {
 
 // flux_update_densities + add_source_terms with FP32 sources; the weights of
 // the previous states sum to one (forward Euler and Heun stages).
-template <int D, bool CYL, int NSMAX>
-__global__ void __launch_bounds__(128) k_update32(KTree t, const int* __restrict__ list, UpdateArgs32 u) {
+template <int D, bool CYL, int NSMAX, int NC = 0>
+__global__ void __launch_bounds__(128) k_update32(KTree t0, const int* __restrict__ list, UpdateArgs32 u) {
+  const KTree t = fix_dims<D, NC>(t0);
   __shared__ float sred[32];
   const UpdateArgs& a = u.a;
   const int slot = list[blockIdx.x];
@@ -333,10 +335,11 @@ __global__ void __launch_bounds__(128) k_update32(KTree t, const int* __restrict
 }
 
 // E on faces and |E| in cells with FP32 scaling (see k_field_grad)
-template <int D>
-__global__ void __launch_bounds__(256) k_field_grad32(KTree t, const int* __restrict__ list,
+template <int D, int NC = 0>
+__global__ void __launch_bounds__(256) k_field_grad32(KTree t0, const int* __restrict__ list,
                                                       const double* __restrict__ phi, double* __restrict__ efc,
                                                       double* __restrict__ enorm) {
+  const KTree t = fix_dims<D, NC>(t0);
   extern __shared__ float sef[];  // [D][NF], the fc layout of one box
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2, nf1 = nc + 1;
@@ -375,8 +378,9 @@ __global__ void __launch_bounds__(256) k_field_grad32(KTree t, const int* __rest
 }
 
 // Charge density on interior cells (FP64: n_+ - n_- cancels)
-template <int D>
-__global__ void __launch_bounds__(256) k_field_rhs_interior(KTree t, const int* __restrict__ list, RhsArgs a) {
+template <int D, int NC = 0>
+__global__ void __launch_bounds__(256) k_field_rhs_interior(KTree t0, const int* __restrict__ list, RhsArgs a) {
+  const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;
@@ -393,11 +397,12 @@ __global__ void __launch_bounds__(256) k_field_rhs_interior(KTree t, const int* 
 }
 
 // Photon production (see k_photo_source) with FP32 lookup and products
-template <int D>
-__global__ void __launch_bounds__(256) k_photo_source32(KTree t, const int* __restrict__ list,
+template <int D, int NC = 0>
+__global__ void __launch_bounds__(256) k_photo_source32(KTree t0, const int* __restrict__ list,
                                                         const double* __restrict__ E, const double* __restrict__ ne,
                                                         double* __restrict__ rhs, LtDevF lt, int col_alpha,
                                                         int col_mu, float N_inv_td, float coeff_hi, float coeff_lo) {
+  const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;

@@ -172,13 +172,20 @@ int afg_transport_setup(afg_ctx* ctx, const afg_transport_desc* d) {
     const int nfaces = D == 2 ? nc * (nc + 1) : nc * nc * (nc + 1);
     const size_t smem = sizeof(double) * ((size_t)t.n_flux * tile + 2 * (size_t)D * nfaces);
     if (smem > 200 * 1024) return fail(ctx, AFG_ERR_UNSUPPORTED, "box too large for the flux kernel");
-    CK(cudaFuncSetAttribute(k_flux<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaFuncSetAttribute(k_flux<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CK(cudaFuncSetAttribute(k_flux<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const size_t smem32 = flux32_smem(ctx, t.n_flux);
-    CK(cudaFuncSetAttribute(k_flux32<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32));
-    CK(cudaFuncSetAttribute(k_flux32<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32));
-    CK(cudaFuncSetAttribute(k_flux32<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32));
+    const cudaFuncAttribute ms = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    CK(cudaFuncSetAttribute(k_flux<3, false, 0>, ms, (int)smem));
+    CK(cudaFuncSetAttribute(k_flux<3, false, 8>, ms, (int)smem));
+    CK(cudaFuncSetAttribute(k_flux<2, true, 0>, ms, (int)smem));
+    CK(cudaFuncSetAttribute(k_flux<2, true, 16>, ms, (int)smem));
+    CK(cudaFuncSetAttribute(k_flux<2, false, 0>, ms, (int)smem));
+    CK(cudaFuncSetAttribute(k_flux<2, false, 16>, ms, (int)smem));
+    CK(cudaFuncSetAttribute(k_flux32<3, false, 0>, ms, (int)smem32));
+    CK(cudaFuncSetAttribute(k_flux32<3, false, 8>, ms, (int)smem32));
+    CK(cudaFuncSetAttribute(k_flux32<2, true, 0>, ms, (int)smem32));
+    CK(cudaFuncSetAttribute(k_flux32<2, true, 16>, ms, (int)smem32));
+    CK(cudaFuncSetAttribute(k_flux32<2, false, 0>, ms, (int)smem32));
+    CK(cudaFuncSetAttribute(k_flux32<2, false, 16>, ms, (int)smem32));
   }
   s.ready = true;
   return AFG_OK;
@@ -222,11 +229,11 @@ int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim) {
       for (int f = 0; f < d.n_flux; f++) {
         double* v = ctx->cc[d.species_iv[d.flux_species[f]] + s_deriv - 1];
         if (ctx->D == 3)
-          k_restrict_geom<3, false><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v);
+          AFG_NC3(NCV_, k_restrict_geom<3, false, NCV_><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v));
         else if (cyl)
-          k_restrict_geom<2, true><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v);
+          AFG_NC2(NCV_, k_restrict_geom<2, true, NCV_><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v));
         else
-          k_restrict_geom<2, false><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v);
+          AFG_NC2(NCV_, k_restrict_geom<2, false, NCV_><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v));
         ctx->launches++;
         CKL();
       }
@@ -257,17 +264,17 @@ int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim) {
         }
         const size_t smem32 = flux32_smem(ctx, d.n_flux);
         if (ctx->D == 3)
-          k_flux32<3, false><<<n, 256, smem32, ctx->stream>>>(t, list, a32);
+          AFG_NC3(NCV_, k_flux32<3, false, NCV_><<<n, 256, smem32, ctx->stream>>>(t, list, a32));
         else if (cyl)
-          k_flux32<2, true><<<n, 256, smem32, ctx->stream>>>(t, list, a32);
+          AFG_NC2(NCV_, k_flux32<2, true, NCV_><<<n, 256, smem32, ctx->stream>>>(t, list, a32));
         else
-          k_flux32<2, false><<<n, 256, smem32, ctx->stream>>>(t, list, a32);
+          AFG_NC2(NCV_, k_flux32<2, false, NCV_><<<n, 256, smem32, ctx->stream>>>(t, list, a32));
       } else if (ctx->D == 3) {
-        k_flux<3, false><<<n, 256, smem, ctx->stream>>>(t, list, a);
+        AFG_NC3(NCV_, k_flux<3, false, NCV_><<<n, 256, smem, ctx->stream>>>(t, list, a));
       } else if (cyl) {
-        k_flux<2, true><<<n, 256, smem, ctx->stream>>>(t, list, a);
+        AFG_NC2(NCV_, k_flux<2, true, NCV_><<<n, 256, smem, ctx->stream>>>(t, list, a));
       } else {
-        k_flux<2, false><<<n, 256, smem, ctx->stream>>>(t, list, a);
+        AFG_NC2(NCV_, k_flux<2, false, NCV_><<<n, 256, smem, ctx->stream>>>(t, list, a));
       }
       // per leaf cell: read n (flux species), |E|, E on D faces; write D fluxes per species
       kt_end(ctx, AFG_KT_FLUX, 8.0 * n * box_cells(ctx) * ((d.n_flux + 1 + ctx->D) + ctx->D * d.n_flux));
@@ -276,11 +283,11 @@ int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim) {
     }
     if (ctx->tr.n_cflux > 0) {
       if (ctx->D == 3)
-        k_consistent_flux<3, false><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a);
+        AFG_NC3(NCV_, k_consistent_flux<3, false, NCV_><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a));
       else if (cyl)
-        k_consistent_flux<2, true><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a);
+        AFG_NC2(NCV_, k_consistent_flux<2, true, NCV_><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a));
       else
-        k_consistent_flux<2, false><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a);
+        AFG_NC2(NCV_, k_consistent_flux<2, false, NCV_><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a));
       ctx->launches++;
       CKL();
     }
@@ -357,13 +364,13 @@ int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev, const
       u.dt = (float)dt;
       for (int m = 0; m < n_prev; m++) u.w_rel[m] = (float)w_prev[m];
       u.nmin = (float)d.dt_chemistry_nmin;
-#define AFG_LAUNCH_UPDATE32(NSM)                                          \
-  if (ctx->D == 3)                                                        \
-    k_update32<3, false, NSM><<<n, 128, 0, ctx->stream>>>(t, list, u);    \
-  else if (cyl)                                                           \
-    k_update32<2, true, NSM><<<n, 128, 0, ctx->stream>>>(t, list, u);     \
-  else                                                                    \
-    k_update32<2, false, NSM><<<n, 128, 0, ctx->stream>>>(t, list, u);
+#define AFG_LAUNCH_UPDATE32(NSM)                                                               \
+  if (ctx->D == 3)                                                                             \
+    AFG_NC3(NCV_, k_update32<3, false, NSM, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, u));    \
+  else if (cyl)                                                                                \
+    AFG_NC2(NCV_, k_update32<2, true, NSM, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, u));     \
+  else                                                                                         \
+    AFG_NC2(NCV_, k_update32<2, false, NSM, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, u));
       if (d.n_species <= 4) {
         AFG_LAUNCH_UPDATE32(4)
       } else if (d.n_species <= 8) {
@@ -373,13 +380,13 @@ int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev, const
       }
 #undef AFG_LAUNCH_UPDATE32
     } else {
-#define AFG_LAUNCH_UPDATE(NSM)                                          \
-  if (ctx->D == 3)                                                      \
-    k_update<3, false, NSM><<<n, 128, 0, ctx->stream>>>(t, list, a);    \
-  else if (cyl)                                                         \
-    k_update<2, true, NSM><<<n, 128, 0, ctx->stream>>>(t, list, a);     \
-  else                                                                  \
-    k_update<2, false, NSM><<<n, 128, 0, ctx->stream>>>(t, list, a);
+#define AFG_LAUNCH_UPDATE(NSM)                                                             \
+  if (ctx->D == 3)                                                                         \
+    AFG_NC3(NCV_, k_update<3, false, NSM, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, a));  \
+  else if (cyl)                                                                            \
+    AFG_NC2(NCV_, k_update<2, true, NSM, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, a));   \
+  else                                                                                     \
+    AFG_NC2(NCV_, k_update<2, false, NSM, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, a));
       if (d.n_species <= 4) {
         AFG_LAUNCH_UPDATE(4)
       } else if (d.n_species <= 8) {
@@ -423,9 +430,9 @@ int afg_field_set_rhs(afg_ctx* ctx, int i_rhs, int s_in) {
     if (!mixed_transport(ctx))
       k_field_rhs<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ctx->S, list, a);
     else if (ctx->D == 3)
-      k_field_rhs_interior<3><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), list, a);
+      AFG_NC3(NCV_, k_field_rhs_interior<3, NCV_><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), list, a));
     else
-      k_field_rhs_interior<2><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), list, a);
+      AFG_NC2(NCV_, k_field_rhs_interior<2, NCV_><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), list, a));
     ctx->launches++;
     CKL();
   }
@@ -446,15 +453,15 @@ int afg_field_from_potential(afg_ctx* ctx, int i_phi) {
       const int D = ctx->D;
       const size_t smem = sizeof(float) * D * (size_t)ctx->NF;
       if (D == 3)
-        k_field_grad32<3><<<ctx->n_all, 256, smem, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1],
-                                                                   efc, en);
+        AFG_NC3(NCV_, k_field_grad32<3, NCV_><<<ctx->n_all, 256, smem, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1],
+                                                                   efc, en));
       else
-        k_field_grad32<2><<<ctx->n_all, 256, smem, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1],
-                                                                   efc, en);
+        AFG_NC2(NCV_, k_field_grad32<2, NCV_><<<ctx->n_all, 256, smem, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1],
+                                                                   efc, en));
     } else if (ctx->D == 3)
-      k_field_grad<3><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en);
+      AFG_NC3(NCV_, k_field_grad<3, NCV_><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en));
     else
-      k_field_grad<2><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en);
+      AFG_NC2(NCV_, k_field_grad<2, NCV_><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en));
     ctx->launches++;
     CKL();
     return afg_gc(ctx, d.i_electric_fld, 0, 1);
@@ -484,6 +491,10 @@ int afg_field_compute(afg_ctx* ctx, int mg_id, int s_in, int have_guess, double 
       std::max(std::max(1e-6, max_rhs * max_rel_residual), 1e-10 * std::fabs(voltage) / (domain_len * min_dr));
   int nc_done = 0;
   double r = 0;
+  // A mixed-precision slot runs FMG in FP32, whose residual floor on fine
+  // meshes can exceed the 1e8 guard of the stall test; there the FMG only
+  // starts the FP64 defect correction below, so a stall ends it at any level.
+  const bool fp32_fmg = m->d.precision == AFG_MIXED;
   if (!have_guess) {
     double res[100];
     int i;
@@ -495,7 +506,7 @@ int afg_field_compute(afg_ctx* ctx, int mg_id, int s_in, int have_guess, double 
         const double mn = std::min(res[i], std::min(res[i - 1], res[i - 2]));
         const double mx = std::max(res[i], std::max(res[i - 1], res[i - 2]));
         const double ratio = mn / mx;
-        if (ratio < 2.0 && ratio > 0.5 && res[i] < 1e8) break;
+        if (ratio < 2.0 && ratio > 0.5 && (res[i] < 1e8 || fp32_fmg)) break;
       }
     }
     if (i == 100) return fail(ctx, AFG_ERR_NOCONV, "no convergence in initial field computation");
@@ -534,21 +545,21 @@ int afg_photoi_helmh(afg_ctx* ctx, double coeff, int n_modes, const int* mg_ids,
       const double ch = std::sqrt(std::fabs(coeff));
       const float c_hi = (float)(coeff < 0 ? -ch : ch), c_lo = (float)ch;
       if (ctx->D == 3)
-        k_photo_source32<3><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all_leaves), E, ne, rhs,
+        AFG_NC3(NCV_, k_photo_source32<3, NCV_><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all_leaves), E, ne, rhs,
                                                                         lt_dev_f(ctx), d.lt_col_alpha,
-                                                                        d.lt_col_mobility, N_inv_td, c_hi, c_lo);
+                                                                        d.lt_col_mobility, N_inv_td, c_hi, c_lo));
       else
-        k_photo_source32<2><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all_leaves), E, ne, rhs,
+        AFG_NC2(NCV_, k_photo_source32<2, NCV_><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all_leaves), E, ne, rhs,
                                                                         lt_dev_f(ctx), d.lt_col_alpha,
-                                                                        d.lt_col_mobility, N_inv_td, c_hi, c_lo);
+                                                                        d.lt_col_mobility, N_inv_td, c_hi, c_lo));
     } else if (ctx->D == 3)
-      k_photo_source<3><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all_leaves), E, ne, rhs,
+      AFG_NC3(NCV_, k_photo_source<3, NCV_><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all_leaves), E, ne, rhs,
                                                                   lt_dev(ctx), d.lt_col_alpha, d.lt_col_mobility,
-                                                                  d.gas_number_density, coeff);
+                                                                  d.gas_number_density, coeff));
     else
-      k_photo_source<2><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all_leaves), E, ne, rhs,
+      AFG_NC2(NCV_, k_photo_source<2, NCV_><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all_leaves), E, ne, rhs,
                                                                   lt_dev(ctx), d.lt_col_alpha, d.lt_col_mobility,
-                                                                  d.gas_number_density, coeff);
+                                                                  d.gas_number_density, coeff));
     ctx->launches++;
     CKL();
   }

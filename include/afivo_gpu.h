@@ -142,16 +142,19 @@ int afg_cc_upload(afg_ctx* ctx, int iv, const double* const* box_cc,
 int afg_cc_download(afg_ctx* ctx, int iv, double* const* box_cc,
                     long long elem_offset);
 
-/* Transfer paths of the four copy routines: when every box pointer is
- * non-NULL, the pointers are equally spaced and the host memory is
- * page-locked (cudaMallocHost, or afg_host_register below), all boxes move in
- * one pitched DMA; otherwise the boxes are gathered/scattered by host threads
- * through a page-locked staging buffer, overlapped with the DMA in 32 MiB
- * chunks.  Every copy has completed when the call returns. */
+/* Transfer paths of the four copy routines, when every box pointer is
+ * non-NULL and the pointers are equally spaced:
+ *   - all boxes inside one range page-locked by afg_host_register: the GPU
+ *     reads/writes the mapped host memory directly (one kernel);
+ *   - other page-locked memory (e.g. cudaMallocHost): one pitched DMA.
+ * Otherwise the boxes are gathered/scattered by host threads through a
+ * page-locked staging buffer, overlapped with the DMA in 32 MiB chunks.
+ * Every copy has completed when the call returns. */
 
-/* Page-lock (cudaHostRegister) / release caller-owned host memory, e.g. the
- * storage behind the box arrays passed to the copy routines.  No counterpart
- * in the reference (its data never leaves the host). */
+/* Page-lock and map (cudaHostRegister) / release caller-owned host memory,
+ * e.g. the storage behind the box arrays passed to the copy routines; the
+ * context remembers the range until afg_host_unregister (same ptr).  No
+ * counterpart in the reference (its data never leaves the host). */
 int afg_host_register(afg_ctx* ctx, void* ptr, size_t bytes);
 int afg_host_unregister(afg_ctx* ctx, void* ptr);
 
@@ -193,7 +196,11 @@ int afg_mg_set_bc_values(afg_ctx* ctx, int mg_id, const double* bc_val);
 int afg_mg_vcycle(afg_ctx* ctx, int mg_id, int set_residual, int max_lvl,
                   double* max_res);
 
-/* mg_fas_fmg (137-180). */
+/* mg_fas_fmg (137-180).  For an AFG_MIXED slot one call is one
+ * defect-correction step: FP64 defect of phi (zero without a guess), FP32
+ * FMG for the correction with homogeneous boundary values, phi += correction;
+ * max_res is the FP64 defect's maximum over the leaves (i_tmp is not
+ * written). */
 int afg_mg_fmg(afg_ctx* ctx, int mg_id, int set_residual, int have_guess,
                double* max_res);
 
@@ -331,7 +338,10 @@ int afg_field_from_potential(afg_ctx* ctx, int i_phi);
  * s_in, boundary value `voltage` on the highest face of the last dimension,
  * FMG start when have_guess == 0, V-cycles until max|residual| < threshold
  * = max(1e-6, max|rhs|*max_rel_residual, 1e-10*|V|/(domain_len*dx_min)),
- * field from potential.  n_cycles and the final residual are returned. */
+ * field from potential.  n_cycles and the final residual are returned.
+ * With an AFG_MIXED slot the FMG start uses the defect-correction FMG of
+ * afg_mg_fmg and its stall test ends it whatever the residual's magnitude;
+ * the V-cycles of the mixed solve then reach the threshold. */
 int afg_field_compute(afg_ctx* ctx, int mg_id, int s_in, int have_guess,
                       double voltage, double domain_len, double max_rel_residual,
                       int num_vcycles, int* n_cycles, double* residual);

@@ -46,6 +46,23 @@ def test_roundtrip(ctx_tree, locked):
     assert np.array_equal(a, b)
 
 
+def test_roundtrip_page_locked_elsewhere(ctx_tree):
+    """Page-locked memory the context did not register: the pitched DMA path."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("torch without CUDA")
+    ctx, tree = ctx_tree
+    n2 = tree.n_cell + 2
+    shape = (tree.n_boxes, 2) + (n2,) * tree.ndim
+    ta = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+    tb = torch.zeros(shape, dtype=torch.float64, pin_memory=True)
+    a, b = ta.numpy(), tb.numpy()
+    a[...] = host(tree, 2, 5)
+    ctx.upload_vars(a, [2, 3])
+    ctx.download_vars(b, [2, 3])
+    assert np.array_equal(a, b)
+
+
 def test_null_boxes_untouched(ctx_tree):
     ctx, tree = ctx_tree
     a = host(tree, 1, 2)
