@@ -57,6 +57,43 @@ __device__ __forceinline__ T apply_lpl(const T* __restrict__ p, int n2, int i, i
   }
 }
 
+// L phi from the centre and neighbour values, in apply_lpl's operation order
+template <int D, bool CYL, typename T>
+__device__ __forceinline__ T lpl_vals(T pc, T pw, T pe, T ps, T pn, T pb, T pf, const T c[7], T k1, T k2, T k3) {
+  if (D == 2) {
+    if (CYL) return k1 * pc + k2 * pw + k3 * pe + c[3] * ps + c[4] * pn;
+    return c[0] * pc + c[1] * pw + c[2] * pe + c[3] * ps + c[4] * pn;
+  }
+  return c[0] * pc + c[1] * pw + c[2] * pe + c[3] * ps + c[4] * pn + c[5] * pb + c[6] * pf;
+}
+
+// apply_lpl with the neighbours across the box faces given by face_ghost,
+// i.e. the values af_gc_box would store in the ghost cells at this moment,
+// so no ghost-cell fill is needed before the stencil.
+template <int D, bool CYL, typename T>
+__device__ __forceinline__ T apply_lpl_otf(const KTree& t, const T* __restrict__ phi, const T* __restrict__ p,
+                                           int slot, int i, int j, int k, const T c[7], T k1, T k2, T k3,
+                                           const GcDev& g) {
+  const int nc = t.nc, n2 = t.n2;
+  if (D == 2) {
+    const int x = at2(n2, i, j);
+    const T pw = i == 1 ? face_ghost<D, T>(t, phi, slot, 0, j, 0, g) : p[x - 1];
+    const T pe = i == nc ? face_ghost<D, T>(t, phi, slot, 1, j, 0, g) : p[x + 1];
+    const T ps = j == 1 ? face_ghost<D, T>(t, phi, slot, 2, i, 0, g) : p[x - n2];
+    const T pn = j == nc ? face_ghost<D, T>(t, phi, slot, 3, i, 0, g) : p[x + n2];
+    return lpl_vals<D, CYL, T>(p[x], pw, pe, ps, pn, T(0), T(0), c, k1, k2, k3);
+  } else {
+    const int x = at3(n2, i, j, k), sk = n2 * n2;
+    const T pw = i == 1 ? face_ghost<D, T>(t, phi, slot, 0, j, k, g) : p[x - 1];
+    const T pe = i == nc ? face_ghost<D, T>(t, phi, slot, 1, j, k, g) : p[x + 1];
+    const T ps = j == 1 ? face_ghost<D, T>(t, phi, slot, 2, i, k, g) : p[x - n2];
+    const T pn = j == nc ? face_ghost<D, T>(t, phi, slot, 3, i, k, g) : p[x + n2];
+    const T pb = k == 1 ? face_ghost<D, T>(t, phi, slot, 4, i, j, g) : p[x - sk];
+    const T pf = k == nc ? face_ghost<D, T>(t, phi, slot, 5, i, j, g) : p[x + sk];
+    return lpl_vals<D, CYL, T>(p[x], pw, pe, ps, pn, pb, pf, c, k1, k2, k3);
+  }
+}
+
 // One red-black half sweep on each box of the list; stencil_gsrb_357
 // (m_af_stencil.f90:838-998).  Updated cells satisfy (i+j[+k]+n) even.
 template <int D, bool CYL, typename T, int NC = 0>
@@ -104,7 +141,7 @@ __global__ void __launch_bounds__(256) k_gsrb(KTree t0, const int* __restrict__ 
 // itself before its update.  One ghost fill after the last half sweep then
 // leaves memory exactly as the reference does.
 template <int D, bool CYL, typename T, int NC = 0>
-__global__ void __launch_bounds__(256) k_gsrb_fused(KTree t0, const int* __restrict__ list, T* __restrict__ phi,
+__global__ void __launch_bounds__(256, 6) k_gsrb_fused(KTree t0, const int* __restrict__ list, T* __restrict__ phi,
                                                     const T* __restrict__ rhs, int redblack, MgCoef<T> mc,
                                                     GcDev g) {
   const KTree t = fix_dims<D, NC>(t0);
@@ -194,7 +231,7 @@ template <int D, bool CYL, typename T, int NC = 0>
 __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* __restrict__ list,
                                                            T* __restrict__ phi, const T* __restrict__ rhs,
                                                            T* __restrict__ tmp, MgCoef<T> mc,
-                                                           int store_child_residual) {
+                                                           int store_child_residual, GcDev g, int otf) {
   const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   const int pslot = t.parent[slot];
@@ -224,7 +261,8 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* 
             k1 = y[0]; k2 = y[1]; k3 = y[2];
           }
           const int x = at2(n2, fi + di, fj + dj);
-          res[dj][di] = f[x] - apply_lpl<D, CYL, T>(p, n2, fi + di, fj + dj, 0, c, k1, k2, k3);
+          res[dj][di] = f[x] - (otf ? apply_lpl_otf<D, CYL, T>(t, phi, p, slot, fi + di, fj + dj, 0, c, k1, k2, k3, g)
+                                    : apply_lpl<D, CYL, T>(p, n2, fi + di, fj + dj, 0, c, k1, k2, k3));
           if (store_child_residual) ct[x] = res[dj][di];
         }
       T rv;
@@ -251,7 +289,10 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* 
         for (int dj = 0; dj < 2; dj++)
           for (int di = 0; di < 2; di++) {
             const int x = at3(n2, fi + di, fj + dj, fk + dk);
-            const T res = f[x] - apply_lpl<D, false, T>(p, n2, fi + di, fj + dj, fk + dk, c, T(0), T(0), T(0));
+            const T res =
+                f[x] - (otf ? apply_lpl_otf<D, false, T>(t, phi, p, slot, fi + di, fj + dj, fk + dk, c, T(0), T(0),
+                                                         T(0), g)
+                            : apply_lpl<D, false, T>(p, n2, fi + di, fj + dj, fk + dk, c, T(0), T(0), T(0)));
             if (store_child_residual) ct[x] = res;
             sr = sr + res;
             sp = sp + p[x];
@@ -267,13 +308,33 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* 
 // reference also adds tmp to rhs in the ghost cells; rhs ghost cells are
 // never read, so they are left untouched.  With copy_tmp = 0 this is the
 // rhs part of set_coarse_phi_rhs (742-776).
+//
+// fill != 0: the parent's ghost cells of phi are filled first (faces, then
+// edges and corners: af_gc_box), so the stencil and the copy into tmp see
+// them; this replaces the level-wide ghost fill between the restriction and
+// this step (leaf boxes of the level need none there: the fused smoother
+// computes its own and the level is filled again after its up smoothing).
 template <int D, bool CYL, typename T, int NC = 0>
 __global__ void __launch_bounds__(256) k_coarse_fas(KTree t0, const int* __restrict__ list,
-                                                    const T* __restrict__ phi, T* __restrict__ rhs,
-                                                    T* __restrict__ tmp, MgCoef<T> mc, int copy_tmp) {
+                                                    T* __restrict__ phi, T* __restrict__ rhs,
+                                                    T* __restrict__ tmp, MgCoef<T> mc, int copy_tmp, int fill,
+                                                    GcDev g) {
   const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;
+  if (fill) {
+    T* a = phi + (size_t)slot * t.S;
+    const int nface = D == 2 ? nc : nc * nc;
+    for (int w = threadIdx.x; w < 2 * D * nface; w += blockDim.x) {
+      const int nb = w / nface, pq = w - nb * nface;
+      const int pi = pq % nc + 1, qi = D == 3 ? pq / nc + 1 : 0;
+      const T val = face_ghost<D, T>(t, phi, slot, nb, pi, qi, g);
+      a[face_at<D>(n2, nb >> 1, (nb & 1) ? nc + 1 : 0, pi, qi)] = val;
+    }
+    __syncthreads();
+    corner_ghosts<D, T>(t, phi, slot);
+    __syncthreads();
+  }
   T c[7];
   for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
   const T* p = phi + (size_t)slot * t.S;

@@ -322,33 +322,33 @@ static int launch_residual(afg_ctx* ctx, const int* list, int n, const T* phi, c
 
 template <typename T>
 static int launch_rrestrict(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, T* tmp, MgCoef<T> lam,
-                            int store_child) {
+                            int store_child, const GcDev& g, int otf) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   const int hnc = ctx->nc / 2;
   const int threads = std::max(32, std::min(256, ctx->D == 2 ? hnc * hnc : hnc * hnc * hnc));
   if (ctx->D == 3)
-    AFG_NC3(NCV_, k_residual_restrict<3, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child));
+    AFG_NC3(NCV_, k_residual_restrict<3, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child, g, otf));
   else if (ctx->coord == AFG_CYL)
-    AFG_NC2(NCV_, k_residual_restrict<2, true, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child));
+    AFG_NC2(NCV_, k_residual_restrict<2, true, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child, g, otf));
   else
-    AFG_NC2(NCV_, k_residual_restrict<2, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child));
+    AFG_NC2(NCV_, k_residual_restrict<2, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child, g, otf));
   ctx->launches++;
   CKL();
   return AFG_OK;
 }
 
 template <typename T>
-static int launch_coarse_fas(afg_ctx* ctx, const int* list, int n, const T* phi, T* rhs, T* tmp, MgCoef<T> lam,
-                             int copy_tmp) {
+static int launch_coarse_fas(afg_ctx* ctx, const int* list, int n, T* phi, T* rhs, T* tmp, MgCoef<T> lam,
+                             int copy_tmp, int fill, const GcDev& g) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   if (ctx->D == 3)
-    AFG_NC3(NCV_, k_coarse_fas<3, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp));
+    AFG_NC3(NCV_, k_coarse_fas<3, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp, fill, g));
   else if (ctx->coord == AFG_CYL)
-    AFG_NC2(NCV_, k_coarse_fas<2, true, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp));
+    AFG_NC2(NCV_, k_coarse_fas<2, true, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp, fill, g));
   else
-    AFG_NC2(NCV_, k_coarse_fas<2, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp));
+    AFG_NC2(NCV_, k_coarse_fas<2, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp, fill, g));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -482,13 +482,15 @@ static int mg_gc_lvl(afg_ctx* ctx, int lvl, T* phi, const GcDev& g, int corners)
 
 // gsrb_boxes, m_af_multigrid.f90:648-687
 template <typename T>
-static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, T* phi, const T* rhs, const GcDev& g) {
+static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, T* phi, const T* rhs, const GcDev& g,
+                         bool fill_down = true) {
   const int n_cycle = type == AFG_CYCLE_DOWN ? m.d.n_cycle_down : m.d.n_cycle_up;
   const int* list = lst(ctx, ctx->off_ids[lvl - 1]);
   const int n = (int)ctx->lvl_ids[lvl - 1].size();
   ctx->ctr[1] += (long long)n * (long long)box_cells(ctx) * n_cycle;
   if (ctx->fused_gsrb) {
     for (int it = 1; it <= 2 * n_cycle; it++) RC(launch_gsrb_fused<T>(ctx, list, n, phi, rhs, it, coef_of<T>(m), g));
+    if (type == AFG_CYCLE_DOWN && !fill_down) return AFG_OK;
     return launch_gc<T>(ctx, list, n, phi, g, type != AFG_CYCLE_DOWN ? 1 : 0);
   }
   for (int it = 1; it <= 2 * n_cycle; it++) {
@@ -499,14 +501,18 @@ static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, T* ph
   return AFG_OK;
 }
 
-// update_coarse, m_af_multigrid.f90:691-738
+// update_coarse (m_af_multigrid.f90:691-738): residual of lvl restricted to
+// the parents, phi restricted, then the parents' ghost fill fused with the
+// FAS right-hand side.  otf: the residual's neighbours across box faces are
+// computed on the fly, so lvl needs no ghost fill after its down smoothing
+// (the V-cycle); otherwise the stored ghost cells are used as they are.
 template <typename T>
-static int mg_update_coarse(afg_ctx* ctx, const MgSlot& m, int lvl, T* phi, T* rhs, T* tmp, const GcDev& g) {
+static int mg_update_coarse(afg_ctx* ctx, const MgSlot& m, int lvl, T* phi, T* rhs, T* tmp, const GcDev& g,
+                            bool otf = true) {
   RC(launch_rrestrict<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs, tmp,
-                         coef_of<T>(m), 0));
-  RC(mg_gc_lvl<T>(ctx, lvl - 1, phi, g, 1));
+                         coef_of<T>(m), 0, g, otf ? 1 : 0));
   RC(launch_coarse_fas<T>(ctx, lst(ctx, ctx->off_parents[lvl - 2]), (int)ctx->lvl_parents[lvl - 2].size(), phi, rhs,
-                          tmp, coef_of<T>(m), 1));
+                          tmp, coef_of<T>(m), 1, 1, g));
   return AFG_OK;
 }
 
@@ -515,18 +521,23 @@ template <typename T>
 static int mg_set_coarse_phi_rhs(afg_ctx* ctx, const MgSlot& m, int lvl, T* phi, T* rhs, T* tmp, const GcDev& g) {
   if (lvl == ctx->highest_lvl) RC(mg_gc_lvl<T>(ctx, lvl, phi, g, 1));
   RC(launch_rrestrict<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs, tmp,
-                         coef_of<T>(m), 1));
+                         coef_of<T>(m), 1, g, 0));
   RC(mg_gc_lvl<T>(ctx, lvl - 1, phi, g, 1));
   RC(launch_coarse_fas<T>(ctx, lst(ctx, ctx->off_parents[lvl - 2]), (int)ctx->lvl_parents[lvl - 2].size(), phi, rhs,
-                          tmp, coef_of<T>(m), 0));
+                          tmp, coef_of<T>(m), 0, 0, g));
   return AFG_OK;
 }
 
-// correct_children(parents of lvl-1) + af_gc_lvl(lvl)
+// correct_children(parents of lvl-1) + af_gc_lvl(lvl).  Inside the V-cycle
+// and FMG the next operation on lvl is the fused smoother, which computes the
+// face ghosts it reads from the neighbours' current values (the same values
+// af_gc_lvl would store) and fills all ghosts when it ends; there the ghost
+// fill is skipped (fill = false), the stored ghost cells of lvl being read
+// by nothing in between.
 template <typename T>
-static int mg_correct(afg_ctx* ctx, int lvl, T* phi, T* tmp, const GcDev& g) {
+static int mg_correct(afg_ctx* ctx, int lvl, T* phi, T* tmp, const GcDev& g, bool fill = true) {
   RC(launch_correct<T>(ctx, lst(ctx, ctx->off_parents[lvl - 2]), (int)ctx->lvl_parents[lvl - 2].size(), phi, tmp));
-  RC(mg_gc_lvl<T>(ctx, lvl, phi, g, 1));
+  if (fill) RC(mg_gc_lvl<T>(ctx, lvl, phi, g, 1));
   return AFG_OK;
 }
 
@@ -566,12 +577,13 @@ static int mg_vcycle(afg_ctx* ctx, MgSlot& m, int max_lvl, T* phi, T* rhs, T* tm
   const GcDev g = mg_gc(m.d, homogeneous);
   ctx->ctr[3]++;
   for (int lvl = max_lvl; lvl >= 2; lvl--) {
-    RC(mg_gsrb_boxes<T>(ctx, m, lvl, AFG_CYCLE_DOWN, phi, rhs, g));
+    // the restriction below computes the face neighbours it needs itself
+    RC(mg_gsrb_boxes<T>(ctx, m, lvl, AFG_CYCLE_DOWN, phi, rhs, g, false));
     RC(mg_update_coarse<T>(ctx, m, lvl, phi, rhs, tmp, g));
   }
   RC(mg_coarse_solve<T>(ctx, m, phi, rhs, g, homogeneous));
   for (int lvl = 2; lvl <= max_lvl; lvl++) {
-    RC(mg_correct<T>(ctx, lvl, phi, tmp, g));
+    RC(mg_correct<T>(ctx, lvl, phi, tmp, g, !ctx->fused_gsrb));
     RC(mg_gsrb_boxes<T>(ctx, m, lvl, AFG_CYCLE_UP, phi, rhs, g));
   }
   if (set_residual) RC(mg_residual_lvls<T>(ctx, m, max_lvl, phi, rhs, tmp, maxbits));
@@ -594,7 +606,7 @@ static int mg_fmg(afg_ctx* ctx, MgSlot& m, T* phi, T* rhs, T* tmp, bool set_resi
   RC(mg_vcycle<T>(ctx, m, 1, phi, rhs, tmp, set_residual && H == 1, homogeneous, maxbits));
   for (int lvl = 2; lvl <= H; lvl++) {
     RC(launch_copy<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, tmp));
-    RC(mg_correct<T>(ctx, lvl, phi, tmp, g));
+    RC(mg_correct<T>(ctx, lvl, phi, tmp, g, !ctx->fused_gsrb));
     RC(mg_vcycle<T>(ctx, m, lvl, phi, rhs, tmp, set_residual && lvl == H, homogeneous, maxbits));
   }
   return AFG_OK;
@@ -1344,7 +1356,10 @@ int afg_mg_update_coarse(afg_ctx* ctx, int mg_id, int lvl) {
   RC(get_mg(ctx, mg_id, &m));
   if (lvl < 2 || lvl > ctx->highest_lvl) return fail(ctx, AFG_ERR_ARG, "bad level");
   MG_VARS(m);
-  return mg_update_coarse<double>(ctx, *m, lvl, phi, rhs, tmp, mg_gc(m->d, false));
+  const GcDev g = mg_gc(m->d, false);
+  RC(mg_update_coarse<double>(ctx, *m, lvl, phi, rhs, tmp, g, false));
+  // the reference fills the whole coarser level, leaves included
+  return mg_gc_lvl<double>(ctx, lvl - 1, phi, g, 1);
 }
 
 int afg_mg_correct_lvl(afg_ctx* ctx, int mg_id, int lvl) {

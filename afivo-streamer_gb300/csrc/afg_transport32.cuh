@@ -236,7 +236,7 @@ __device__ __forceinline__ void add_tof(float (&v)[NSMAX], int s, float x) {
 // flux_update_densities + add_source_terms with FP32 sources; the weights of
 // the previous states sum to one (forward Euler and Heun stages).
 template <int D, bool CYL, int NSMAX, int NC = 0>
-__global__ void __launch_bounds__(128) k_update32(KTree t0, const int* __restrict__ list, UpdateArgs32 u) {
+__global__ void __launch_bounds__(128, 12) k_update32(KTree t0, const int* __restrict__ list, UpdateArgs32 u) {
   const KTree t = fix_dims<D, NC>(t0);
   __shared__ float sred[32];
   const UpdateArgs& a = u.a;
