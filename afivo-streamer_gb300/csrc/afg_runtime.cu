@@ -298,6 +298,8 @@ static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, T* phi, const
     AFG_NC2(NCV_, k_gsrb_fused<2, true, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g));
   else
     AFG_NC2(NCV_, k_gsrb_fused<2, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g));
+  // algorithmic bytes: 3 words per cell per full iteration (read phi and
+  // rhs, write phi), 1.5 words per half sweep
   kt_end(ctx, AFG_KT_GSRB, 1.5 * sizeof(T) * n * box_cells(ctx));
   ctx->launches++;
   CKL();

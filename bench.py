@@ -52,10 +52,13 @@ CONFIG_TEXT = {
     "cyl2d": "2D axisymmetric streamer, 16^2 boxes, 9 levels, 2918 boxes (~0.56 M leaf cells), 3 species, "
              "3 Helmholtz photoionization modes, Heun dt=5e-12 s, Poisson to 1e-8 rel.",
 }
-# DRAM bytes (read + write) per box of one launch of a kernel class, from one
-# ncu capture (the profiles/ summary of that workload and kernel gives the
-# command); the traffic of a launch is this times the boxes it processes.
-NCU_DRAM_BYTES_PER_BOX = {}
+# DRAM traffic of a kernel class relative to its algorithmic bytes, from one
+# ncu capture (dram__bytes.sum.per_second x gpu__time_duration.sum) of the
+# same kernel on the same tree construction one level coarser; traffic grows
+# with the boxes a launch processes, so the ratio carries over to full size.
+# Smoother: 7135 bytes per box and half sweep against 3072 algorithmic
+# (1.5 FP32 words per cell).
+NCU_TRAFFIC_RATIO = {("3d", "gsrb"): 7135.0 / 3072.0}
 
 
 class Clocks:
@@ -337,9 +340,9 @@ def main():
     ks = kstats[dom]
     achieved = ks["bytes"] / (ks["ms"] * 1e-3) / 1e9 if ks["ms"] > 0 else 0.0
     traffic = None
-    per_box = NCU_DRAM_BYTES_PER_BOX.get((args.config, dom))
-    if per_box is not None and ks["launches"]:
-        traffic = per_box * ks.get("boxes", 0) / ks["launches"]
+    ratio = NCU_TRAFFIC_RATIO.get((args.config, dom))
+    if ratio is not None and ks["launches"]:
+        traffic = ratio * ks["bytes"] / ks["launches"]
     cpu = None
     if rank == 0 and world == 1 and args.cpu_steps > 0:
         v, cores, sps, done, sample = run_cpu(args.config, args.cpu_steps, warmup=1, time_limit=args.cpu_seconds)
@@ -356,7 +359,9 @@ def main():
                 "fp64": {k: fp64[k] for k in keys},
                 "speedup_mixed_vs_fp64": fp64["ms_per_step"] / mixed["ms_per_step"]},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic},
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": ks["bytes"] / max(1, ks["launches"]),
+                         "avg_launch_us": 1e3 * ks["ms"] / max(1, ks["launches"])},
             "kernel_classes": kstats,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": mixed["clocks"],
             "gpu_launches": int(mixed["launches"]),
