@@ -22,14 +22,14 @@ __device__ __forceinline__ T bc_ghost(int type, double bval, double drd, bool lo
   return c0 * T(bval) + c1 * x1 + c2 * x2;
 }
 
-// Ghost value of face nb at tangential position (p,q) of box `slot`.
+// Ghost value of face nb at tangential position (p,q) of box `slot`, whose
+// neighbour across that face is nbs (a slot, kNbRefine or kNbPhys).
 template <int D, typename T>
-__device__ __forceinline__ T face_ghost(const KTree& t, const T* __restrict__ v, int slot, int nb,
-                                        int p, int q, const GcDev& g) {
+__device__ __forceinline__ T face_ghost_nb(const KTree& t, const T* __restrict__ v, int slot, int nb, int nbs,
+                                           int p, int q, const GcDev& g) {
   const int nc = t.nc, n2 = t.n2, S = t.S, d = nb >> 1;
   const bool low = (nb & 1) == 0;
   const T* a = v + (size_t)slot * S;
-  const int nbs = t.nbr[slot * 2 * D + nb];
   if (nbs >= 0) {
     const T* b = v + (size_t)nbs * S;
     return b[face_at<D>(n2, d, low ? nc : 1, p, q)];
@@ -95,6 +95,13 @@ __device__ __forceinline__ T face_ghost(const KTree& t, const T* __restrict__ v,
   }
   if (g.rb == 2 && val > T(2) * c1) val = T(2) * c1;
   return val;
+}
+
+// face_ghost_nb with the neighbour slot from the tree's table
+template <int D, typename T>
+__device__ __forceinline__ T face_ghost(const KTree& t, const T* __restrict__ v, int slot, int nb, int p, int q,
+                                        const GcDev& g) {
+  return face_ghost_nb<D, T>(t, v, slot, nb, t.nbr[slot * 2 * D + nb], p, q, g);
 }
 
 __constant__ int c_edge_dim[12] = {0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2};

@@ -184,6 +184,65 @@ __global__ void __launch_bounds__(256, 6) k_gsrb_fused(KTree t0, const int* __re
   }
 }
 
+// The same half sweep for a compile-time box size NC: CPT cells of the colour
+// per thread, all their loads issued before the stores (cells of one colour
+// never read each other), and the box's slot and face neighbours from its
+// 32-byte record (one load instead of a list load and neighbour-table loads).
+// The arithmetic is that of k_gsrb_fused.
+template <int D, bool CYL, typename T, int NC, int CPT>
+__global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT)
+    k_gsrb_rec(KTree t0, const int* __restrict__ rec, T* __restrict__ phi, const T* __restrict__ rhs, int redblack,
+               MgCoef<T> mc, GcDev g) {
+  constexpr int TPB = (D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT;
+  constexpr int nc = NC, n2 = NC + 2, hn = NC / 2, sk = n2 * n2;
+  const KTree t = fix_dims<D, NC>(t0);
+  const int4 r0 = reinterpret_cast<const int4*>(rec)[2 * blockIdx.x];
+  const int4 r1 = reinterpret_cast<const int4*>(rec)[2 * blockIdx.x + 1];
+  const int slot = r0.x;
+  T c[7];
+  for (int q = 0; q < 2 * D + 1; q++) c[q] = mc.cb[slot * 8 + q];
+  const T inv_c1 = mc.cb[slot * 8 + 7];
+  T* p = phi + (size_t)slot * t.S;
+  const T* f = rhs + (size_t)slot * t.S;
+  T val[CPT];
+  int xs[CPT];
+#pragma unroll
+  for (int u = 0; u < CPT; u++) {
+    const int w = (int)threadIdx.x + u * TPB;
+    const int row = w / hn, col = w - row * hn;
+    if (D == 2) {
+      const int j = row + 1;
+      const int i = 2 - ((redblack ^ j) & 1) + 2 * col;
+      const int x = at2(n2, i, j);
+      const T pw = i == 1 ? face_ghost_nb<D, T>(t, phi, slot, 0, r0.y, j, 0, g) : p[x - 1];
+      const T pe = i == nc ? face_ghost_nb<D, T>(t, phi, slot, 1, r0.z, j, 0, g) : p[x + 1];
+      const T ps = j == 1 ? face_ghost_nb<D, T>(t, phi, slot, 2, r0.w, i, 0, g) : p[x - n2];
+      const T pn = j == nc ? face_ghost_nb<D, T>(t, phi, slot, 3, r1.x, i, 0, g) : p[x + n2];
+      if (CYL) {
+        const T* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
+        val[u] = (f[x] - y[1] * pw - y[2] * pe - c[3] * ps - c[4] * pn) * y[3];
+      } else {
+        val[u] = (f[x] - c[1] * pw - c[2] * pe - c[3] * ps - c[4] * pn) * inv_c1;
+      }
+      xs[u] = x;
+    } else {
+      const int j = row % nc + 1, k = row / nc + 1;
+      const int i = 2 - ((redblack ^ (k + j)) & 1) + 2 * col;
+      const int x = at3(n2, i, j, k);
+      const T pw = i == 1 ? face_ghost_nb<D, T>(t, phi, slot, 0, r0.y, j, k, g) : p[x - 1];
+      const T pe = i == nc ? face_ghost_nb<D, T>(t, phi, slot, 1, r0.z, j, k, g) : p[x + 1];
+      const T ps = j == 1 ? face_ghost_nb<D, T>(t, phi, slot, 2, r0.w, i, k, g) : p[x - n2];
+      const T pn = j == nc ? face_ghost_nb<D, T>(t, phi, slot, 3, r1.x, i, k, g) : p[x + n2];
+      const T pb = k == 1 ? face_ghost_nb<D, T>(t, phi, slot, 4, r1.y, i, j, g) : p[x - sk];
+      const T pf = k == nc ? face_ghost_nb<D, T>(t, phi, slot, 5, r1.z, i, j, g) : p[x + sk];
+      val[u] = (f[x] - c[1] * pw - c[2] * pe - c[3] * ps - c[4] * pn - c[5] * pb - c[6] * pf) * inv_c1;
+      xs[u] = x;
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < CPT; u++) p[xs[u]] = val[u];
+}
+
 // Residual on interior cells into tmp (residual_box, m_af_multigrid.f90:
 // 801-810); the max |r| over the boxes flagged in is_leaf is folded into
 // *maxbits (may be null).

@@ -78,6 +78,7 @@ struct afg_ctx {
   float* d_idrf = nullptr;
   double* d_geo = nullptr;  // cylindrical geometry table (KTree::geo)
   int* d_lists = nullptr;  // all level lists concatenated
+  int* d_rec = nullptr;    // per list entry: {slot, neighbour slots per face, pad} (8 ints)
   std::vector<size_t> off_ids, off_leaves, off_parents;  // per level offsets into d_lists
   size_t off_all = 0;       // list of all boxes, all levels (level order)
   size_t off_all_leaves = 0;
@@ -198,6 +199,8 @@ MgCoef<float> coef_of<float>(const MgSlot& m) {
 static MgCoef<double> coef64(const MgSlot& m) { return coef_of<double>(m); }
 
 static const int* lst(const afg_ctx* c, size_t off) { return c->d_lists + off; }
+// the box records of the entries of a list (a pointer into d_lists)
+static const int* rec_of(const afg_ctx* c, const int* list) { return c->d_rec + (list - c->d_lists) * 8; }
 
 // Per-launch timing of one kernel class (afg_kernel_timing): events around
 // each launch of the selected class, algorithmic bytes summed on the host.
@@ -229,7 +232,7 @@ static void clear_graphs(afg_ctx* c) {
 static void free_tree(afg_ctx* c) {
   clear_graphs(c);
   dfree(c->d_parent); dfree(c->d_children); dfree(c->d_nbr); dfree(c->d_pnb); dfree(c->d_nbmat);
-  dfree(c->d_ix); dfree(c->d_rmin); dfree(c->d_dr); dfree(c->d_idr); dfree(c->d_idrf); dfree(c->d_lists); dfree(c->d_is_leaf); dfree(c->d_geo);
+  dfree(c->d_ix); dfree(c->d_rmin); dfree(c->d_dr); dfree(c->d_idr); dfree(c->d_idrf); dfree(c->d_lists); dfree(c->d_rec); dfree(c->d_is_leaf); dfree(c->d_geo);
   dfree(c->d_cslot); dfree(c->d_ccell);
   for (auto& p : c->cc) dfree(p);
   for (auto& p : c->fc) dfree(p);
@@ -292,12 +295,20 @@ static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, T* phi, const
   KTree t = ktree(ctx);
   const int threads = ctx->D == 2 ? std::min(256, ctx->nc * ctx->nc / 2) : std::min(256, ctx->nc * ctx->nc * ctx->nc / 2);
   kt_begin(ctx, AFG_KT_GSRB);
-  if (ctx->D == 3)
-    AFG_NC3(NCV_, k_gsrb_fused<3, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g));
+  const int* rec = rec_of(ctx, list);
+  // the usual box sizes: several cells per thread, box records
+  if (ctx->D == 3 && ctx->nc == 8)
+    k_gsrb_rec<3, false, T, 8, 4><<<n, 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g);
+  else if (ctx->D == 2 && ctx->nc == 16 && ctx->coord == AFG_CYL)
+    k_gsrb_rec<2, true, T, 16, 2><<<n, 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g);
+  else if (ctx->D == 2 && ctx->nc == 16)
+    k_gsrb_rec<2, false, T, 16, 2><<<n, 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g);
+  else if (ctx->D == 3)
+    k_gsrb_fused<3, false, T, 0><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
   else if (ctx->coord == AFG_CYL)
-    AFG_NC2(NCV_, k_gsrb_fused<2, true, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g));
+    k_gsrb_fused<2, true, T, 0><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
   else
-    AFG_NC2(NCV_, k_gsrb_fused<2, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g));
+    k_gsrb_fused<2, false, T, 0><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
   // algorithmic bytes: 3 words per cell per full iteration (read phi and
   // rhs, write phi), 1.5 words per half sweep
   kt_end(ctx, AFG_KT_GSRB, 1.5 * sizeof(T) * n * box_cells(ctx));
@@ -843,6 +854,19 @@ int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_va
     CK(cudaMemcpy(ctx->d_idrf, idrf.data(), sizeof(float) * idrf.size(), cudaMemcpyHostToDevice));
   }
   if (!lists.empty()) CK(cudaMemcpy(ctx->d_lists, lists.data(), sizeof(int) * lists.size(), cudaMemcpyHostToDevice));
+  {
+    // box records: a kernel walking a list gets the slot and the face
+    // neighbours of its box in one 32-byte load
+    std::vector<int> rec(std::max<size_t>(1, lists.size()) * 8, kNbPhys);
+    for (size_t q = 0; q < lists.size(); q++) {
+      const int sl = lists[q];
+      rec[q * 8] = sl;
+      for (int nb = 0; nb < nnb; nb++) rec[q * 8 + 1 + nb] = nbr[(size_t)sl * nnb + nb];
+      rec[q * 8 + 7] = 0;
+    }
+    CK(dalloc(&ctx->d_rec, rec.size()));
+    CK(cudaMemcpy(ctx->d_rec, rec.data(), sizeof(int) * rec.size(), cudaMemcpyHostToDevice));
+  }
   CK(cudaMemcpy(ctx->d_is_leaf, is_leaf.data(), n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_cslot, cslot.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_ccell, ccell.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));

@@ -239,10 +239,15 @@ template <int D, bool CYL, int NSMAX, int NC = 0>
 __global__ void __launch_bounds__(128, 12) k_update32(KTree t0, const int* __restrict__ list, UpdateArgs32 u) {
   const KTree t = fix_dims<D, NC>(t0);
   __shared__ float sred[32];
+  // each thread's species densities and sources in its own shared-memory
+  // column: the reaction table indexes species at run time, which registers
+  // cannot be (one shared-memory access instead of an unrolled select)
+  __shared__ float s_dens[NSMAX * 128], s_der[NSMAX * 128];
   const UpdateArgs& a = u.a;
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2, nf1 = nc + 1;
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;
+  const int tid = threadIdx.x;
   float dt_dr[3];
   for (int q = 0; q < D; q++) dt_dr[q] = u.dt * t.idrf[slot * D + q];
   float my_chem = 3.0e38f;
@@ -251,12 +256,14 @@ __global__ void __launch_bounds__(128, 12) k_update32(KTree t0, const int* __res
     const int i = w % nc + 1, r = w / nc;
     const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
     const int x = D == 2 ? at2(n2, i, j) : at3(n2, i, j, k);
-    float dens[NSMAX], der[NSMAX];
+    float* dens = s_dens + tid;  // species s at dens[s * 128]
+    float* der = s_der + tid;
 #pragma unroll
     for (int s = 0; s < NSMAX; s++) {
-      dens[s] = 0.0f;
-      der[s] = 0.0f;
-      if (s < a.ns) dens[s] = fmaxf(d2f(a.deriv[s][base + x]), 0.0f);
+      if (s < a.ns) {
+        dens[s * 128] = fmaxf(d2f(a.deriv[s][base + x]), 0.0f);
+        der[s * 128] = 0.0f;
+      }
     }
     const float td = u.N_inv_td * d2f(a.E[base + x]);
     int ix;
@@ -265,9 +272,9 @@ __global__ void __launch_bounds__(128, 12) k_update32(KTree t0, const int* __res
     for (int n = 0; n < a.n_reactions; n++) {
       const Reac32& rc = u.reactions[n];
       float rate = rate32(u.lt, rc, td, ix, lw);
-      for (int q = 0; q < rc.n_in; q++) rate = rate * pickf<NSMAX>(dens, rc.ix_in[q]);
-      for (int q = 0; q < rc.n_in; q++) add_tof<NSMAX>(der, rc.ix_in[q], -rate);
-      for (int q = 0; q < rc.n_out; q++) add_tof<NSMAX>(der, rc.ix_out[q], rate * rc.mult_out[q]);
+      for (int q = 0; q < rc.n_in; q++) rate = rate * dens[rc.ix_in[q] * 128];
+      for (int q = 0; q < rc.n_in; q++) der[rc.ix_in[q] * 128] -= rate;
+      for (int q = 0; q < rc.n_out; q++) der[rc.ix_out[q] * 128] += rate * rc.mult_out[q];
     }
     if (a.last_step) {
       const float eps = 1e-30f;
@@ -275,21 +282,22 @@ __global__ void __launch_bounds__(128, 12) k_update32(KTree t0, const int* __res
 #pragma unroll
       for (int s = 0; s < NSMAX; s++) {
         if (s >= a.ns) continue;
+        const float dn = dens[s * 128], dd = der[s * 128];
         if (u.nmin > 0.0f)
-          tmp = fminf(tmp, (dens[s] + u.nmin) / fmaxf(fabsf(der[s]), eps));
+          tmp = fminf(tmp, (dn + u.nmin) / fmaxf(fabsf(dd), eps));
         else if (a.limit_loss)
-          tmp = fminf(tmp, fmaxf(dens[s], eps) / fmaxf(-der[s], eps));
+          tmp = fminf(tmp, fmaxf(dn, eps) / fmaxf(-dd, eps));
       }
       my_chem = fminf(my_chem, tmp);
     }
     if (a.photo != nullptr) {
       const float ph = d2f(a.photo[base + x]);
-      add_tof<NSMAX>(der, a.flux_species[0], ph);
-      add_tof<NSMAX>(der, a.photoi_species, ph);
+      der[a.flux_species[0] * 128] += ph;
+      der[a.photoi_species * 128] += ph;
     }
     float inc[NSMAX];
 #pragma unroll
-    for (int s = 0; s < NSMAX; s++) inc[s] = u.dt * der[s];
+    for (int s = 0; s < NSMAX; s++) inc[s] = s < a.ns ? u.dt * der[s * 128] : 0.0f;
     for (int f = 0; f < a.nf; f++) {
       const int s = a.flux_species[f];
       const double* F0 = a.flux[f] + ((size_t)slot * D + 0) * t.NF;
