@@ -39,6 +39,19 @@ struct KTree {
   const float* idrf;  // the same rounded to FP32
 };
 
+// Box records: per entry of a box list, {slot, neighbour slot of faces
+// 0..2D-1, ..., source flag} in 8 ints, read as two int4 (one 32-byte load);
+// the last int is 1 when a refinement-boundary rule of a finer box reads the
+// box's face ghosts.
+__device__ __forceinline__ void load_rec(const int* __restrict__ rec, int e, int4& r0, int4& r1) {
+  r0 = reinterpret_cast<const int4*>(rec)[2 * e];
+  r1 = reinterpret_cast<const int4*>(rec)[2 * e + 1];
+}
+// neighbour slot of face nb from a record (selects, no local memory)
+__device__ __forceinline__ int rec_nb(const int4& r0, const int4& r1, int nb) {
+  return nb == 0 ? r0.y : nb == 1 ? r0.z : nb == 2 ? r0.w : nb == 3 ? r1.x : nb == 4 ? r1.y : r1.z;
+}
+
 // Box size as a compile-time constant: kernels carry a template parameter NC
 // (0 = take the sizes from the tree) and start with t = fix_dims<D, NC>(t0).
 // With NC > 0 the sizes are constants, so the index arithmetic (divisions by

@@ -175,10 +175,12 @@ __device__ void corner_ghosts(const KTree& t, T* __restrict__ v, int slot) {
 
 // af_gc_lvl on a box list: one CTA per box.
 template <int D, typename T, int NC = 0>
-__global__ void __launch_bounds__(256) k_gc(KTree t0, const int* __restrict__ list, T* __restrict__ v,
+__global__ void __launch_bounds__(256) k_gc(KTree t0, const int* __restrict__ rec, T* __restrict__ v,
                                             GcDev g, int corners) {
   const KTree t = fix_dims<D, NC>(t0);
-  const int slot = list[blockIdx.x];
+  int4 r0, r1;
+  load_rec(rec, blockIdx.x, r0, r1);
+  const int slot = r0.x;
   const int nc = t.nc;
   const int nface = D == 2 ? nc : nc * nc;
   T* a = v + (size_t)slot * t.S;
@@ -189,7 +191,7 @@ __global__ void __launch_bounds__(256) k_gc(KTree t0, const int* __restrict__ li
     const int p = pq % nc + 1, q = D == 3 ? pq / nc + 1 : 0;
     const int d = nb >> 1;
     const bool low = (nb & 1) == 0;
-    const T val = face_ghost<D, T>(t, v, slot, nb, p, q, g);
+    const T val = face_ghost_nb<D, T>(t, v, slot, nb, rec_nb(r0, r1, nb), p, q, g);
     a[face_at<D>(t.n2, d, low ? 0 : nc + 1, p, q)] = val;
   }
   if (corners) {

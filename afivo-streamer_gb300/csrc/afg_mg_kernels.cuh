@@ -73,23 +73,23 @@ __device__ __forceinline__ T lpl_vals(T pc, T pw, T pe, T ps, T pn, T pb, T pf, 
 template <int D, bool CYL, typename T>
 __device__ __forceinline__ T apply_lpl_otf(const KTree& t, const T* __restrict__ phi, const T* __restrict__ p,
                                            int slot, int i, int j, int k, const T c[7], T k1, T k2, T k3,
-                                           const GcDev& g) {
+                                           const GcDev& g, const int4& r0, const int4& r1) {
   const int nc = t.nc, n2 = t.n2;
   if (D == 2) {
     const int x = at2(n2, i, j);
-    const T pw = i == 1 ? face_ghost<D, T>(t, phi, slot, 0, j, 0, g) : p[x - 1];
-    const T pe = i == nc ? face_ghost<D, T>(t, phi, slot, 1, j, 0, g) : p[x + 1];
-    const T ps = j == 1 ? face_ghost<D, T>(t, phi, slot, 2, i, 0, g) : p[x - n2];
-    const T pn = j == nc ? face_ghost<D, T>(t, phi, slot, 3, i, 0, g) : p[x + n2];
+    const T pw = i == 1 ? face_ghost_nb<D, T>(t, phi, slot, 0, r0.y, j, 0, g) : p[x - 1];
+    const T pe = i == nc ? face_ghost_nb<D, T>(t, phi, slot, 1, r0.z, j, 0, g) : p[x + 1];
+    const T ps = j == 1 ? face_ghost_nb<D, T>(t, phi, slot, 2, r0.w, i, 0, g) : p[x - n2];
+    const T pn = j == nc ? face_ghost_nb<D, T>(t, phi, slot, 3, r1.x, i, 0, g) : p[x + n2];
     return lpl_vals<D, CYL, T>(p[x], pw, pe, ps, pn, T(0), T(0), c, k1, k2, k3);
   } else {
     const int x = at3(n2, i, j, k), sk = n2 * n2;
-    const T pw = i == 1 ? face_ghost<D, T>(t, phi, slot, 0, j, k, g) : p[x - 1];
-    const T pe = i == nc ? face_ghost<D, T>(t, phi, slot, 1, j, k, g) : p[x + 1];
-    const T ps = j == 1 ? face_ghost<D, T>(t, phi, slot, 2, i, k, g) : p[x - n2];
-    const T pn = j == nc ? face_ghost<D, T>(t, phi, slot, 3, i, k, g) : p[x + n2];
-    const T pb = k == 1 ? face_ghost<D, T>(t, phi, slot, 4, i, j, g) : p[x - sk];
-    const T pf = k == nc ? face_ghost<D, T>(t, phi, slot, 5, i, j, g) : p[x + sk];
+    const T pw = i == 1 ? face_ghost_nb<D, T>(t, phi, slot, 0, r0.y, j, k, g) : p[x - 1];
+    const T pe = i == nc ? face_ghost_nb<D, T>(t, phi, slot, 1, r0.z, j, k, g) : p[x + 1];
+    const T ps = j == 1 ? face_ghost_nb<D, T>(t, phi, slot, 2, r0.w, i, k, g) : p[x - n2];
+    const T pn = j == nc ? face_ghost_nb<D, T>(t, phi, slot, 3, r1.x, i, k, g) : p[x + n2];
+    const T pb = k == 1 ? face_ghost_nb<D, T>(t, phi, slot, 4, r1.y, i, j, g) : p[x - sk];
+    const T pf = k == nc ? face_ghost_nb<D, T>(t, phi, slot, 5, r1.z, i, j, g) : p[x + sk];
     return lpl_vals<D, CYL, T>(p[x], pw, pe, ps, pn, pb, pf, c, k1, k2, k3);
   }
 }
@@ -287,12 +287,14 @@ __global__ void __launch_bounds__(256) k_residual(KTree t0, const int* __restric
 // restricted without geometry (mg_box_rstr_lpl 1227-1242).  One thread per
 // parent cell covered by the child.
 template <int D, bool CYL, typename T, int NC = 0>
-__global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* __restrict__ list,
+__global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* __restrict__ rec,
                                                            T* __restrict__ phi, const T* __restrict__ rhs,
                                                            T* __restrict__ tmp, MgCoef<T> mc,
                                                            int store_child_residual, GcDev g, int otf) {
   const KTree t = fix_dims<D, NC>(t0);
-  const int slot = list[blockIdx.x];
+  int4 r0, r1;
+  load_rec(rec, blockIdx.x, r0, r1);
+  const int slot = r0.x;
   const int pslot = t.parent[slot];
   const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
   T c[7];
@@ -320,7 +322,7 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* 
             k1 = y[0]; k2 = y[1]; k3 = y[2];
           }
           const int x = at2(n2, fi + di, fj + dj);
-          res[dj][di] = f[x] - (otf ? apply_lpl_otf<D, CYL, T>(t, phi, p, slot, fi + di, fj + dj, 0, c, k1, k2, k3, g)
+          res[dj][di] = f[x] - (otf ? apply_lpl_otf<D, CYL, T>(t, phi, p, slot, fi + di, fj + dj, 0, c, k1, k2, k3, g, r0, r1)
                                     : apply_lpl<D, CYL, T>(p, n2, fi + di, fj + dj, 0, c, k1, k2, k3));
           if (store_child_residual) ct[x] = res[dj][di];
         }
@@ -350,7 +352,7 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* 
             const int x = at3(n2, fi + di, fj + dj, fk + dk);
             const T res =
                 f[x] - (otf ? apply_lpl_otf<D, false, T>(t, phi, p, slot, fi + di, fj + dj, fk + dk, c, T(0), T(0),
-                                                         T(0), g)
+                                                         T(0), g, r0, r1)
                             : apply_lpl<D, false, T>(p, n2, fi + di, fj + dj, fk + dk, c, T(0), T(0), T(0)));
             if (store_child_residual) ct[x] = res;
             sr = sr + res;
@@ -374,12 +376,14 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* 
 // this step (leaf boxes of the level need none there: the fused smoother
 // computes its own and the level is filled again after its up smoothing).
 template <int D, bool CYL, typename T, int NC = 0>
-__global__ void __launch_bounds__(256) k_coarse_fas(KTree t0, const int* __restrict__ list,
+__global__ void __launch_bounds__(256) k_coarse_fas(KTree t0, const int* __restrict__ rec,
                                                     T* __restrict__ phi, T* __restrict__ rhs,
                                                     T* __restrict__ tmp, MgCoef<T> mc, int copy_tmp, int fill,
                                                     GcDev g) {
   const KTree t = fix_dims<D, NC>(t0);
-  const int slot = list[blockIdx.x];
+  int4 r0, r1;
+  load_rec(rec, blockIdx.x, r0, r1);
+  const int slot = r0.x;
   const int nc = t.nc, n2 = t.n2;
   if (fill) {
     T* a = phi + (size_t)slot * t.S;
@@ -387,7 +391,7 @@ __global__ void __launch_bounds__(256) k_coarse_fas(KTree t0, const int* __restr
     for (int w = threadIdx.x; w < 2 * D * nface; w += blockDim.x) {
       const int nb = w / nface, pq = w - nb * nface;
       const int pi = pq % nc + 1, qi = D == 3 ? pq / nc + 1 : 0;
-      const T val = face_ghost<D, T>(t, phi, slot, nb, pi, qi, g);
+      const T val = face_ghost_nb<D, T>(t, phi, slot, nb, rec_nb(r0, r1, nb), pi, qi, g);
       a[face_at<D>(n2, nb >> 1, (nb & 1) ? nc + 1 : 0, pi, qi)] = val;
     }
     __syncthreads();

@@ -15,28 +15,46 @@
 namespace afg {
 
 // r (FP64 residual on interior cells) -> r32, e32 = 0 (whole box), max |r|
-// over leaves into *maxbits.  The Cartesian stencil is one FMA chain (8 FP64
-// instructions per cell); r is rounded to FP32 by bit truncation and its
-// maximum taken in FP32.
+// over leaves into *maxbits.  Leaves only (the V-cycle's restriction
+// overwrites the parents' right-hand side).  Each block first fills its own
+// box's face ghosts of phi (face_ghost_nb: same-level copies, boundary and
+// refinement rules; boxes flagged as refinement sources were filled before
+// the launch and are left alone, since finer boxes' rules read them), then
+// applies the stencil to the stored values.  The Cartesian stencil is one
+// FMA chain (8 FP64 instructions per cell); r is rounded to FP32 by bit
+// truncation and its maximum taken in FP32.
 template <int D, bool CYL, int NC = 0>
-__global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict__ list, const double* __restrict__ phi,
+__global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict__ rec, double* __restrict__ phi,
                                                 const double* __restrict__ rhs, float* __restrict__ r32,
-                                                float* __restrict__ e32, MgCoef<double> mc,
+                                                float* __restrict__ e32, MgCoef<double> mc, GcDev g,
                                                 const unsigned char* __restrict__ is_leaf,
                                                 unsigned long long* maxbits) {
   const KTree t = fix_dims<D, NC>(t0);
   __shared__ float sred[32];
-  const int slot = list[blockIdx.x];
+  int4 r0, r1;
+  load_rec(rec, blockIdx.x, r0, r1);
+  const int slot = r0.x;
   const int nc = t.nc, n2 = t.n2;
-  double cd[7];
-  for (int q = 0; q < 7; q++) cd[q] = mc.cb[slot * 8 + q];
-  const double* p = phi + (size_t)slot * t.S;
-  const double* f = rhs + (size_t)slot * t.S;
-  float* ro = r32 + (size_t)slot * t.S;
   float* eo = e32 + (size_t)slot * t.S;
   for (int x = threadIdx.x; x < t.S; x += blockDim.x) eo[x] = 0.0f;
   // parents need no defect: the V-cycle's restriction overwrites their rhs
   if (!is_leaf[slot]) return;
+  double* pw_ = phi + (size_t)slot * t.S;
+  if (r1.w == 0) {
+    const int nface = D == 2 ? nc : nc * nc;
+    for (int w = threadIdx.x; w < 2 * D * nface; w += blockDim.x) {
+      const int nb = w / nface, pq = w - nb * nface;
+      const int pi = pq % nc + 1, qi = D == 3 ? pq / nc + 1 : 0;
+      const double val = face_ghost_nb<D, double>(t, phi, slot, nb, rec_nb(r0, r1, nb), pi, qi, g);
+      pw_[face_at<D>(n2, nb >> 1, (nb & 1) ? nc + 1 : 0, pi, qi)] = val;
+    }
+  }
+  __syncthreads();
+  double cd[7];
+  for (int q = 0; q < 7; q++) cd[q] = mc.cb[slot * 8 + q];
+  const double* p = pw_;
+  const double* f = rhs + (size_t)slot * t.S;
+  float* ro = r32 + (size_t)slot * t.S;
   float mx = 0.0f;
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;
   for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
@@ -90,19 +108,20 @@ __global__ void __launch_bounds__(256) k_add_correction(int S, const int* __rest
 
 }  // namespace afg
 
-static int launch_defect(afg_ctx* ctx, MgSlot& m, const double* phi, const double* rhs, unsigned long long* maxbits) {
+static int launch_defect(afg_ctx* ctx, MgSlot& m, double* phi, const double* rhs, unsigned long long* maxbits) {
   const int n = ctx->n_all;
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
-  const int* list = lst(ctx, ctx->off_all);
+  const int* list = rec_of(ctx, lst(ctx, ctx->off_all));
+  const GcDev g = mg_gc(m.d, false);
   if (ctx->D == 3)
-    AFG_NC3(NCV_, k_defect<3, false, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), ctx->d_is_leaf,
+    AFG_NC3(NCV_, k_defect<3, false, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), g, ctx->d_is_leaf,
                                                    maxbits));
   else if (ctx->coord == AFG_CYL)
-    AFG_NC2(NCV_, k_defect<2, true, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), ctx->d_is_leaf,
+    AFG_NC2(NCV_, k_defect<2, true, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), g, ctx->d_is_leaf,
                                                   maxbits));
   else
-    AFG_NC2(NCV_, k_defect<2, false, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), ctx->d_is_leaf,
+    AFG_NC2(NCV_, k_defect<2, false, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), g, ctx->d_is_leaf,
                                                    maxbits));
   ctx->launches++;
   CKL();
@@ -126,16 +145,20 @@ static int mixed_prepare(afg_ctx* ctx, MgSlot& m, double* phi) {
     ctx->launches++;
     CKL();
   }
-  // the defect's 7-point stencil and the refinement-boundary rules read face
-  // ghosts only; edges and corners are filled once when the solve ends
+  // The defect fills the face ghosts of the leaves itself, but its
+  // refinement-boundary rules read face ghosts of the coarse source boxes;
+  // those (level by level, coarse to fine: their own rules read coarser
+  // sources) are filled here, before the launch.
   const GcDev g = mg_gc(m.d, false);
-  for (int lvl = 1; lvl <= ctx->highest_lvl; lvl++) RC(mg_gc_lvl<double>(ctx, lvl, phi, g, 0));
+  for (int lvl = 1; lvl <= ctx->highest_lvl; lvl++)
+    RC(launch_gc<double>(ctx, lst(ctx, ctx->off_rbsrc[lvl - 1]), (int)ctx->lvl_rbsrc[lvl - 1].size(), phi, g, 0));
   return AFG_OK;
 }
 
+// all ghost cells of phi (faces, edges, corners) when the solve ends
 static int mixed_finish(afg_ctx* ctx, MgSlot& m, double* phi) {
   const GcDev g = mg_gc(m.d, false);
-  for (int lvl = 1; lvl <= ctx->highest_lvl; lvl++) RC(mg_gc_lvl<double>(ctx, lvl, phi, g, 2));
+  for (int lvl = 1; lvl <= ctx->highest_lvl; lvl++) RC(mg_gc_lvl<double>(ctx, lvl, phi, g, 1));
   return AFG_OK;
 }
 

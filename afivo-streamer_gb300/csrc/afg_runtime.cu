@@ -80,6 +80,10 @@ struct afg_ctx {
   int* d_lists = nullptr;  // all level lists concatenated
   int* d_rec = nullptr;    // per list entry: {slot, neighbour slots per face, pad} (8 ints)
   std::vector<size_t> off_ids, off_leaves, off_parents;  // per level offsets into d_lists
+  // per level: boxes whose face ghosts a refinement-boundary rule of a finer
+  // box reads (parents' neighbours across refinement faces), and offsets
+  std::vector<std::vector<int>> lvl_rbsrc;
+  std::vector<size_t> off_rbsrc;
   size_t off_all = 0;       // list of all boxes, all levels (level order)
   size_t off_all_leaves = 0;
   int n_all = 0;            // boxes in all level lists
@@ -260,9 +264,9 @@ static int launch_gc(afg_ctx* ctx, const int* list, int n, T* v, const GcDev& g,
   KTree t = ktree(ctx);
   kt_begin(ctx, AFG_KT_GHOST);
   if (ctx->D == 2)
-    AFG_NC2(NCV_, k_gc<2, T, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, v, g, corners));
+    AFG_NC2(NCV_, k_gc<2, T, NCV_><<<n, 128, 0, ctx->stream>>>(t, rec_of(ctx, list), v, g, corners));
   else
-    AFG_NC3(NCV_, k_gc<3, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, v, g, corners));
+    AFG_NC3(NCV_, k_gc<3, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, rec_of(ctx, list), v, g, corners));
   kt_end(ctx, AFG_KT_GHOST, 2.0 * sizeof(T) * n * 2 * ctx->D * (box_cells(ctx) / ctx->nc));
   ctx->launches++;
   CKL();
@@ -341,11 +345,11 @@ static int launch_rrestrict(afg_ctx* ctx, const int* list, int n, T* phi, const 
   const int hnc = ctx->nc / 2;
   const int threads = std::max(32, std::min(256, ctx->D == 2 ? hnc * hnc : hnc * hnc * hnc));
   if (ctx->D == 3)
-    AFG_NC3(NCV_, k_residual_restrict<3, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child, g, otf));
+    AFG_NC3(NCV_, k_residual_restrict<3, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, store_child, g, otf));
   else if (ctx->coord == AFG_CYL)
-    AFG_NC2(NCV_, k_residual_restrict<2, true, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child, g, otf));
+    AFG_NC2(NCV_, k_residual_restrict<2, true, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, store_child, g, otf));
   else
-    AFG_NC2(NCV_, k_residual_restrict<2, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, store_child, g, otf));
+    AFG_NC2(NCV_, k_residual_restrict<2, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, store_child, g, otf));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -357,11 +361,11 @@ static int launch_coarse_fas(afg_ctx* ctx, const int* list, int n, T* phi, T* rh
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   if (ctx->D == 3)
-    AFG_NC3(NCV_, k_coarse_fas<3, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp, fill, g));
+    AFG_NC3(NCV_, k_coarse_fas<3, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, copy_tmp, fill, g));
   else if (ctx->coord == AFG_CYL)
-    AFG_NC2(NCV_, k_coarse_fas<2, true, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp, fill, g));
+    AFG_NC2(NCV_, k_coarse_fas<2, true, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, copy_tmp, fill, g));
   else
-    AFG_NC2(NCV_, k_coarse_fas<2, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, copy_tmp, fill, g));
+    AFG_NC2(NCV_, k_coarse_fas<2, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, copy_tmp, fill, g));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -792,6 +796,20 @@ int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_va
     lists.insert(lists.end(), ctx->lvl_ids[l].begin(), ctx->lvl_ids[l].end());
     ctx->n_all += (int)ctx->lvl_ids[l].size();
   }
+  {
+    std::vector<unsigned char> src(n, 0);
+    for (int b = 0; b < n; b++)
+      for (int nb = 0; nb < nnb; nb++)
+        if (nbr[(size_t)b * nnb + nb] == kNbRefine) src[pnb[(size_t)b * nnb + nb]] = 1;
+    ctx->lvl_rbsrc.assign(t->highest_lvl, {});
+    ctx->off_rbsrc.assign(t->highest_lvl, 0);
+    for (int l = 0; l < t->highest_lvl; l++) {
+      for (int sl : ctx->lvl_ids[l])
+        if (src[sl]) ctx->lvl_rbsrc[l].push_back(sl);
+      ctx->off_rbsrc[l] = lists.size();
+      lists.insert(lists.end(), ctx->lvl_rbsrc[l].begin(), ctx->lvl_rbsrc[l].end());
+    }
+  }
   ctx->off_all_leaves = lists.size();
   ctx->n_all_leaves = 0;
   for (int l = 0; l < t->highest_lvl; l++) {
@@ -857,12 +875,16 @@ int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_va
   {
     // box records: a kernel walking a list gets the slot and the face
     // neighbours of its box in one 32-byte load
+    std::vector<unsigned char> src(n, 0);
+    for (int b = 0; b < n; b++)
+      for (int nb = 0; nb < nnb; nb++)
+        if (nbr[(size_t)b * nnb + nb] == kNbRefine) src[pnb[(size_t)b * nnb + nb]] = 1;
     std::vector<int> rec(std::max<size_t>(1, lists.size()) * 8, kNbPhys);
     for (size_t q = 0; q < lists.size(); q++) {
       const int sl = lists[q];
       rec[q * 8] = sl;
       for (int nb = 0; nb < nnb; nb++) rec[q * 8 + 1 + nb] = nbr[(size_t)sl * nnb + nb];
-      rec[q * 8 + 7] = 0;
+      rec[q * 8 + 7] = src[sl];  // 1: the box is a refinement-boundary source
     }
     CK(dalloc(&ctx->d_rec, rec.size()));
     CK(cudaMemcpy(ctx->d_rec, rec.data(), sizeof(int) * rec.size(), cudaMemcpyHostToDevice));
