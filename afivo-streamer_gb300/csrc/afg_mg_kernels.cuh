@@ -190,7 +190,8 @@ __global__ void __launch_bounds__(256, 6) k_gsrb_fused(KTree t0, const int* __re
 // 32-byte record (one load instead of a list load and neighbour-table loads).
 // The arithmetic is that of k_gsrb_fused.
 template <int D, bool CYL, typename T, int NC, int CPT>
-__global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT)
+__global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT,
+                                  1536 / ((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT))
     k_gsrb_rec(KTree t0, const int* __restrict__ rec, T* __restrict__ phi, const T* __restrict__ rhs, int redblack,
                MgCoef<T> mc, GcDev g) {
   constexpr int TPB = (D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT;

@@ -30,6 +30,8 @@ namespace {
 
 constexpr int kMaxMg = 16;
 constexpr int kMaxCoarse = 4096;
+constexpr int kModeSlot = 8, kMaxSlots = 8 + 16;  // device maxima slots
+constexpr int kMaxBranch = 8;                      // side streams
 
 struct DevBuf {
   void* p = nullptr;
@@ -98,8 +100,13 @@ struct afg_ctx {
   std::vector<GcDev> methods;
   std::vector<bool> has_method;
   // scratch
-  unsigned long long* d_max = nullptr;  // 8 slots
+  // device maxima (bits of non-negative doubles): slots 0..7 by role, slots
+  // kModeSlot + n per Helmholtz mode n
+  unsigned long long* d_max = nullptr;
   unsigned long long* h_max = nullptr;  // pinned
+  // side streams and events for independent branches (photoionization modes)
+  cudaStream_t side[kMaxBranch] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[kMaxBranch] = {};
   double* h_stage = nullptr;            // pinned staging
   size_t stage_elems = 0;
   MgSlot mg[kMaxMg];
@@ -662,8 +669,11 @@ int afg_init(int device, afg_ctx** out) {
   ctx->device = device;
   CK(cudaSetDevice(device));
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
-  CK(dalloc(&ctx->d_max, 8));
-  CK(cudaMallocHost((void**)&ctx->h_max, 8 * sizeof(unsigned long long)));
+  CK(dalloc(&ctx->d_max, kMaxSlots));
+  CK(cudaMallocHost((void**)&ctx->h_max, kMaxSlots * sizeof(unsigned long long)));
+  for (auto& st : ctx->side) CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+  for (auto& e : ctx->ev_join) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (auto& e : ctx->xfer_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   *out = ctx;
   return AFG_OK;
@@ -682,6 +692,11 @@ int afg_finalize(afg_ctx* ctx) {
   if (ctx->flush_buf) cudaFree(ctx->flush_buf);
   dfree(ctx->d_max);
   if (ctx->h_max) cudaFreeHost(ctx->h_max);
+  for (auto& st : ctx->side)
+    if (st) cudaStreamDestroy(st);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  for (auto& e : ctx->ev_join)
+    if (e) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return AFG_OK;

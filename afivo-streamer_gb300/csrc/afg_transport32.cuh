@@ -106,6 +106,7 @@ __global__ void __launch_bounds__(256) k_flux32(KTree t0, const int* __restrict_
   }
   __syncthreads();
   float smax = 0.0f;
+  #pragma unroll 2
   for (int w = threadIdx.x; w < D * nfaces; w += blockDim.x) {
     const int dim = w / nfaces, fw = w - dim * nfaces;
     const int f = fw % nf1 + 1, ln = fw / nf1;
@@ -353,6 +354,7 @@ __global__ void __launch_bounds__(256) k_field_grad32(KTree t0, const int* __res
   const int nc = t.nc, n2 = t.n2, nf1 = nc + 1;
   const double* p = phi + (size_t)slot * t.S;
   const int nfaces = D == 2 ? nc * nf1 : nc * nc * nf1;
+  #pragma unroll 4
   for (int w = threadIdx.x; w < D * nfaces; w += blockDim.x) {
     const int dim = w / nfaces, fw = w - dim * nfaces;
     const int f = fw % nf1 + 1, ln = fw / nf1;
@@ -371,6 +373,7 @@ __global__ void __launch_bounds__(256) k_field_grad32(KTree t0, const int* __res
   }
   __syncthreads();
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;
+  #pragma unroll 2
   for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
     const int i = w % nc + 1, r = w / nc;
     const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 1 : r / nc + 1;
@@ -393,6 +396,7 @@ __global__ void __launch_bounds__(256) k_field_rhs_interior(KTree t0, const int*
   const int nc = t.nc, n2 = t.n2;
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;
   const size_t base = (size_t)slot * t.S;
+  #pragma unroll 2
   for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
     const int i = w % nc + 1, r = w / nc;
     const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;

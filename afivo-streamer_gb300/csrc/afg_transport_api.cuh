@@ -569,11 +569,63 @@ int afg_photoi_helmh(afg_ctx* ctx, double coeff, int n_modes, const int* mg_ids,
   double max_rhs;
   RC(afg_maxabs(ctx, i_rhs, 1, &max_rhs));
   max_rhs = std::max(max_rhs, std::sqrt(2.220446049250313e-16));
+  bool all_mixed = n_modes <= kMaxBranch && n_modes <= kMaxSlots - kModeSlot;
   for (int n = 0; n < n_modes; n++) {
     MgSlot* m;
     RC(get_mg(ctx, mg_ids[n], &m));
     if (m->d.i_rhs != i_rhs) return fail(ctx, AFG_ERR_ARG, "Helmholtz modes must share i_rhs");
-    for (int i = 0; i < max_fmg_cycles; i++) {
+    if (m->d.precision != AFG_MIXED) all_mixed = false;
+    for (int q = 0; q < n; q++)
+      if (mg_ids[q] == mg_ids[n]) all_mixed = false;
+  }
+  if (all_mixed) {
+    // Mixed-precision modes own all the buffers they write (phi_n, the FP32
+    // correction, right-hand side and tmp, the coarse-solve vectors) and only
+    // read the shared source, so their FMG cycles run as parallel branches
+    // (side streams forked from and joined to the context's stream, one
+    // graph per set of unconverged modes).  Each mode still gets FMG cycles
+    // until its own residual criterion holds, as in the sequential loop, so
+    // the results are the same.
+    std::vector<int> active(n_modes);
+    for (int n = 0; n < n_modes; n++) active[n] = n;
+    for (int it = 0; it < max_fmg_cycles && !active.empty(); it++) {
+      int mask = 0;
+      for (int n : active) mask |= 1 << n;
+      RC(run_graph(ctx, gkey("photoi_fmg", mask, mg_ids[0], n_modes), [&]() -> int {
+        cudaStream_t main = ctx->stream;
+        CK(cudaEventRecord(ctx->ev_fork, main));
+        for (size_t q = 0; q < active.size(); q++) {
+          const int n = active[q];
+          MgSlot* m = &ctx->mg[mg_ids[n]];
+          CK(cudaStreamWaitEvent(ctx->side[q], ctx->ev_fork, 0));
+          ctx->stream = ctx->side[q];
+          int rc = reset_max(ctx, kModeSlot + n);
+          if (rc == AFG_OK)
+            rc = mixed_fmg(ctx, *m, ctx->cc[m->d.i_phi - 1], ctx->cc[m->d.i_rhs - 1], true, true,
+                           ctx->d_max + kModeSlot + n);
+          ctx->stream = main;
+          RC(rc);
+          CK(cudaEventRecord(ctx->ev_join[q], ctx->side[q]));
+          CK(cudaStreamWaitEvent(main, ctx->ev_join[q], 0));
+        }
+        return AFG_OK;
+      }));
+      CK(cudaMemcpyAsync(ctx->h_max + kModeSlot, ctx->d_max + kModeSlot, sizeof(unsigned long long) * n_modes,
+                         cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+      std::vector<int> still;
+      for (int n : active) {
+        double res;
+        memcpy(&res, ctx->h_max + kModeSlot + n, sizeof(double));
+        if (!(res / max_rhs < max_rel_residual)) still.push_back(n);
+      }
+      active.swap(still);
+    }
+  }
+  for (int n = 0; n < n_modes; n++) {
+    MgSlot* m;
+    RC(get_mg(ctx, mg_ids[n], &m));
+    for (int i = 0; !all_mixed && i < max_fmg_cycles; i++) {
       double res;
       RC(afg_mg_fmg(ctx, mg_ids[n], 1, 1, &res));
       if (res / max_rhs < max_rel_residual) break;
