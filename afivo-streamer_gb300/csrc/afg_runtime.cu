@@ -86,6 +86,10 @@ struct afg_ctx {
   // box reads (parents' neighbours across refinement faces), and offsets
   std::vector<std::vector<int>> lvl_rbsrc;
   std::vector<size_t> off_rbsrc;
+  // per level: parents and refinement sources (the boxes whose ghost cells a
+  // correction V-cycle reads after the level's up smoothing), and offsets
+  std::vector<std::vector<int>> lvl_gcneed;
+  std::vector<size_t> off_gcneed;
   size_t off_all = 0;       // list of all boxes, all levels (level order)
   size_t off_all_leaves = 0;
   int n_all = 0;            // boxes in all level lists
@@ -507,7 +511,7 @@ static int mg_gc_lvl(afg_ctx* ctx, int lvl, T* phi, const GcDev& g, int corners)
 // gsrb_boxes, m_af_multigrid.f90:648-687
 template <typename T>
 static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, T* phi, const T* rhs, const GcDev& g,
-                         bool fill_down = true) {
+                         bool fill_down = true, bool fill_needed_only = false) {
   const int n_cycle = type == AFG_CYCLE_DOWN ? m.d.n_cycle_down : m.d.n_cycle_up;
   const int* list = lst(ctx, ctx->off_ids[lvl - 1]);
   const int n = (int)ctx->lvl_ids[lvl - 1].size();
@@ -515,6 +519,8 @@ static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, T* ph
   if (ctx->fused_gsrb) {
     for (int it = 1; it <= 2 * n_cycle; it++) RC(launch_gsrb_fused<T>(ctx, list, n, phi, rhs, it, coef_of<T>(m), g));
     if (type == AFG_CYCLE_DOWN && !fill_down) return AFG_OK;
+    if (type != AFG_CYCLE_DOWN && fill_needed_only)
+      return launch_gc<T>(ctx, lst(ctx, ctx->off_gcneed[lvl - 1]), (int)ctx->lvl_gcneed[lvl - 1].size(), phi, g, 1);
     return launch_gc<T>(ctx, list, n, phi, g, type != AFG_CYCLE_DOWN ? 1 : 0);
   }
   for (int it = 1; it <= 2 * n_cycle; it++) {
@@ -606,9 +612,14 @@ static int mg_vcycle(afg_ctx* ctx, MgSlot& m, int max_lvl, T* phi, T* rhs, T* tm
     RC(mg_update_coarse<T>(ctx, m, lvl, phi, rhs, tmp, g));
   }
   RC(mg_coarse_solve<T>(ctx, m, phi, rhs, g, homogeneous));
+  // A correction V-cycle (homogeneous, no residual: the mixed path's inner
+  // cycles) fills after the up smoothing only the ghost cells read later:
+  // those of parents (prolongation to the next level) and of refinement
+  // sources (the next level's refinement rules).
+  const bool needed_only = homogeneous && !set_residual;
   for (int lvl = 2; lvl <= max_lvl; lvl++) {
     RC(mg_correct<T>(ctx, lvl, phi, tmp, g, !ctx->fused_gsrb));
-    RC(mg_gsrb_boxes<T>(ctx, m, lvl, AFG_CYCLE_UP, phi, rhs, g));
+    RC(mg_gsrb_boxes<T>(ctx, m, lvl, AFG_CYCLE_UP, phi, rhs, g, true, needed_only));
   }
   if (set_residual) RC(mg_residual_lvls<T>(ctx, m, max_lvl, phi, rhs, tmp, maxbits));
   return AFG_OK;
@@ -818,11 +829,17 @@ int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_va
         if (nbr[(size_t)b * nnb + nb] == kNbRefine) src[pnb[(size_t)b * nnb + nb]] = 1;
     ctx->lvl_rbsrc.assign(t->highest_lvl, {});
     ctx->off_rbsrc.assign(t->highest_lvl, 0);
+    ctx->lvl_gcneed.assign(t->highest_lvl, {});
+    ctx->off_gcneed.assign(t->highest_lvl, 0);
     for (int l = 0; l < t->highest_lvl; l++) {
-      for (int sl : ctx->lvl_ids[l])
+      for (int sl : ctx->lvl_ids[l]) {
         if (src[sl]) ctx->lvl_rbsrc[l].push_back(sl);
+        if (src[sl] || !is_leaf[sl]) ctx->lvl_gcneed[l].push_back(sl);
+      }
       ctx->off_rbsrc[l] = lists.size();
       lists.insert(lists.end(), ctx->lvl_rbsrc[l].begin(), ctx->lvl_rbsrc[l].end());
+      ctx->off_gcneed[l] = lists.size();
+      lists.insert(lists.end(), ctx->lvl_gcneed[l].begin(), ctx->lvl_gcneed[l].end());
     }
   }
   ctx->off_all_leaves = lists.size();
