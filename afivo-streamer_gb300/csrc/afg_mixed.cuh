@@ -108,6 +108,9 @@ __global__ void __launch_bounds__(256) k_add_correction(int S, const int* __rest
 
 }  // namespace afg
 
+// All boxes: the correction starts at zero everywhere (an FMG from zero
+// prolongs the change of the level-1 correction, so it must start at zero
+// there too); the defect itself is computed on leaves.
 static int launch_defect(afg_ctx* ctx, MgSlot& m, double* phi, const double* rhs, unsigned long long* maxbits) {
   const int n = ctx->n_all;
   if (n <= 0) return AFG_OK;
@@ -171,9 +174,10 @@ static int mixed_finish(afg_ctx* ctx, MgSlot& m, double* phi) {
 // has to reduce the current defect, not resolve phi itself.
 static int mixed_fmg(afg_ctx* ctx, MgSlot& m, double* phi, double* rhs, bool set_residual, bool have_guess,
                      unsigned long long* maxbits) {
-  const int n = ctx->n_all;
+  const int n = ctx->n_all_leaves;
   if (n <= 0) return AFG_OK;
-  const int* list = lst(ctx, ctx->off_all);
+  // phi += e on the leaves; the parents are restricted from them next
+  const int* list = lst(ctx, ctx->off_all_leaves);
   if (!have_guess) CK(cudaMemsetAsync(phi, 0, sizeof(double) * (size_t)ctx->n_boxes * ctx->S, ctx->stream));
   RC(mixed_prepare(ctx, m, phi));
   RC(reset_max(ctx, 2));
@@ -204,7 +208,9 @@ static int mixed_solve(afg_ctx* ctx, MgSlot& m, double threshold, int max_cycles
     // one iteration: FP32 V-cycle on the correction, update, new defect
     RC(run_graph(ctx, gkey("mixed_iter", mg_id), [&]() -> int {
       RC(mg_vcycle<float>(ctx, m, ctx->highest_lvl, m.e32, m.r32, m.t32, false, true, nullptr));
-      k_add_correction<<<ctx->n_all, 256, 0, ctx->stream>>>(ctx->S, lst(ctx, ctx->off_all), phi, m.e32);
+      // leaves only: mixed_prepare restricts the parents from them
+      k_add_correction<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ctx->S, lst(ctx, ctx->off_all_leaves), phi,
+                                                                  m.e32);
       ctx->launches++;
       CKL();
       RC(mixed_prepare(ctx, m, phi));

@@ -179,11 +179,10 @@ __device__ __forceinline__ int big_face(int m, int d, int x, int p, int q) {
 // same-level copy, gc2_prolong_rb (753-856) or bc_to_gc2 (282-375).
 // layer 0 is adjacent to the box, layer 1 the outer one.
 template <int D>
-__device__ __forceinline__ double gc2_value(const KTree& t, const double* __restrict__ v, int slot, int nb, int layer,
-                                            int p, int q, const GcDev& g, int limiter) {
+__device__ __forceinline__ double gc2_value(const KTree& t, const double* __restrict__ v, int slot, int nb, int nbs,
+                                            int layer, int p, int q, const GcDev& g, int limiter) {
   const int nc = t.nc, n2 = t.n2, d = nb >> 1;
   const bool low = (nb & 1) == 0;
-  const int nbs = t.nbr[slot * 2 * D + nb];
   if (nbs >= 0) {
     const double* b = v + (size_t)nbs * t.S;
     const int x = low ? nc - layer : 1 + layer;
@@ -262,7 +261,7 @@ __global__ void __launch_bounds__(256) k_flux(KTree t0, const int* __restrict__ 
       const int p = pq % nc + 1, q = D == 3 ? pq / nc + 1 : 0;
       const int d = nb >> 1;
       const bool low = (nb & 1) == 0;
-      const double val = gc2_value<D>(t, a.n[s], slot, nb, layer, p, q, a.bc, a.limiter);
+      const double val = gc2_value<D>(t, a.n[s], slot, nb, t.nbr[slot * 2 * D + nb], layer, p, q, a.bc, a.limiter);
       const int x = low ? -layer : nc + 1 + layer;
       big[s * tile + big_face<D>(m, d, x, p, q)] = val;
     }

@@ -63,12 +63,14 @@ struct FluxArgs32 {
 
 // flux_upwind_box with FP32 arithmetic (see k_flux for the reference lines)
 template <int D, bool CYL, int NC = 0>
-__global__ void __launch_bounds__(256) k_flux32(KTree t0, const int* __restrict__ list, FluxArgs32 a32) {
+__global__ void __launch_bounds__(256) k_flux32(KTree t0, const int* __restrict__ rec, FluxArgs32 a32) {
   const KTree t = fix_dims<D, NC>(t0);
   extern __shared__ float smf[];
   __shared__ float sred[32];
+  __shared__ int srec[8];  // the box record, read by the ghost-layer loop
   const FluxArgs& a = a32.a;
-  const int slot = list[blockIdx.x];
+  if (threadIdx.x < 8) srec[threadIdx.x] = rec[8 * blockIdx.x + threadIdx.x];
+  const int slot = rec[8 * blockIdx.x];
   const int nc = t.nc, n2 = t.n2, m = nc + 4, nf1 = nc + 1;
   const int tile = D == 2 ? m * m : m * m * m;
   const int nfaces = D == 2 ? nc * nf1 : nc * nc * nf1;
@@ -98,7 +100,7 @@ __global__ void __launch_bounds__(256) k_flux32(KTree t0, const int* __restrict_
       const int p = pq % nc + 1, q = D == 3 ? pq / nc + 1 : 0;
       const int d = nb >> 1;
       const bool low = (nb & 1) == 0;
-      const double val = gc2_value<D>(t, a.n[s], slot, nb, layer, p, q, a.bc, a.limiter);
+      const double val = gc2_value<D>(t, a.n[s], slot, nb, srec[1 + nb], layer, p, q, a.bc, a.limiter);
       const int x = low ? -layer : nc + 1 + layer;
       big[s * tile + big_face<D>(m, d, x, p, q)] = d2f(val);
       if (layer == 0) dst[face_at<D>(n2, d, x, p, q)] = val;  // af_gc2_box writes layer 1 back
@@ -217,6 +219,7 @@ struct UpdateArgs32 {
   float dt;
   float w_rel[4];   // weights of the differences n_m - n_0 (m >= 1)
   float nmin;
+  int prev_is_deriv;  // m with s_prev[m] == s_deriv (its values are reused), or -1
 };
 
 template <int NSMAX>
@@ -244,6 +247,7 @@ __global__ void __launch_bounds__(128, 12) k_update32(KTree t0, const int* __res
   // column: the reaction table indexes species at run time, which registers
   // cannot be (one shared-memory access instead of an unrolled select)
   __shared__ float s_dens[NSMAX * 128], s_der[NSMAX * 128];
+  __shared__ double s_raw[NSMAX * 128];  // the derivative state as read
   const UpdateArgs& a = u.a;
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2, nf1 = nc + 1;
@@ -262,7 +266,9 @@ __global__ void __launch_bounds__(128, 12) k_update32(KTree t0, const int* __res
 #pragma unroll
     for (int s = 0; s < NSMAX; s++) {
       if (s < a.ns) {
-        dens[s * 128] = fmaxf(d2f(a.deriv[s][base + x]), 0.0f);
+        const double raw = a.deriv[s][base + x];
+        s_raw[s * 128 + tid] = raw;
+        dens[s * 128] = fmaxf(d2f(raw), 0.0f);
         der[s * 128] = 0.0f;
       }
     }
@@ -324,9 +330,12 @@ __global__ void __launch_bounds__(128, 12) k_update32(KTree t0, const int* __res
 #pragma unroll
     for (int s = 0; s < NSMAX; s++) {
       if (s >= a.ns) continue;
-      const double n0 = a.prev[0][s][base + x];
+      const double n0 = u.prev_is_deriv == 0 ? s_raw[s * 128 + tid] : a.prev[0][s][base + x];
       float d = inc[s];
-      for (int mm = 1; mm < a.n_prev; mm++) d = d + u.w_rel[mm] * d2f(a.prev[mm][s][base + x] - n0);
+      for (int mm = 1; mm < a.n_prev; mm++) {
+        const double nm = u.prev_is_deriv == mm ? s_raw[s * 128 + tid] : a.prev[mm][s][base + x];
+        d = d + u.w_rel[mm] * d2f(nm - n0);
+      }
       a.out[s][base + x] = n0 + f2d(d);
     }
   }
@@ -390,13 +399,16 @@ __global__ void __launch_bounds__(256) k_field_grad32(KTree t0, const int* __res
 
 // Charge density on interior cells (FP64: n_+ - n_- cancels)
 template <int D, int NC = 0>
-__global__ void __launch_bounds__(256) k_field_rhs_interior(KTree t0, const int* __restrict__ list, RhsArgs a) {
+__global__ void __launch_bounds__(256) k_field_rhs_interior(KTree t0, const int* __restrict__ list, RhsArgs a,
+                                                            unsigned long long* maxbits) {
   const KTree t = fix_dims<D, NC>(t0);
+  __shared__ double sred[32];
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;
   const size_t base = (size_t)slot * t.S;
-  #pragma unroll 2
+  double mx = 0.0;
+#pragma unroll 2
   for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
     const int i = w % nc + 1, r = w / nc;
     const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
@@ -405,6 +417,12 @@ __global__ void __launch_bounds__(256) k_field_rhs_interior(KTree t0, const int*
     for (int s = 0; s < a.ns; s++)
       if (a.q[s] != 0.0) v = fma(a.q[s], a.n[s][x], v);
     a.rhs[x] = v;
+    acc_absmax(mx, v);
+  }
+  // max |rhs| over the leaves (af_tree_maxabs_cc), fused
+  if (maxbits != nullptr) {
+    mx = block_max<double>(mx, sred);
+    if (threadIdx.x == 0) atomic_max_nonneg(maxbits, mx);
   }
 }
 

@@ -264,11 +264,11 @@ int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim) {
         }
         const size_t smem32 = flux32_smem(ctx, d.n_flux);
         if (ctx->D == 3)
-          AFG_NC3(NCV_, k_flux32<3, false, NCV_><<<n, 256, smem32, ctx->stream>>>(t, list, a32));
+          AFG_NC3(NCV_, k_flux32<3, false, NCV_><<<n, 256, smem32, ctx->stream>>>(t, rec_of(ctx, list), a32));
         else if (cyl)
-          AFG_NC2(NCV_, k_flux32<2, true, NCV_><<<n, 256, smem32, ctx->stream>>>(t, list, a32));
+          AFG_NC2(NCV_, k_flux32<2, true, NCV_><<<n, 256, smem32, ctx->stream>>>(t, rec_of(ctx, list), a32));
         else
-          AFG_NC2(NCV_, k_flux32<2, false, NCV_><<<n, 256, smem32, ctx->stream>>>(t, list, a32));
+          AFG_NC2(NCV_, k_flux32<2, false, NCV_><<<n, 256, smem32, ctx->stream>>>(t, rec_of(ctx, list), a32));
       } else if (ctx->D == 3) {
         AFG_NC3(NCV_, k_flux<3, false, NCV_><<<n, 256, smem, ctx->stream>>>(t, list, a));
       } else if (cyl) {
@@ -364,6 +364,9 @@ int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev, const
       u.dt = (float)dt;
       for (int m = 0; m < n_prev; m++) u.w_rel[m] = (float)w_prev[m];
       u.nmin = (float)d.dt_chemistry_nmin;
+      u.prev_is_deriv = -1;
+      for (int m = 0; m < n_prev; m++)
+        if (s_prev[m] == s_deriv) u.prev_is_deriv = m;
 #define AFG_LAUNCH_UPDATE32(NSM)                                                               \
   if (ctx->D == 3)                                                                             \
     AFG_NC3(NCV_, k_update32<3, false, NSM, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, u));    \
@@ -411,7 +414,13 @@ int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev, const
   return AFG_OK;
 }
 
-int afg_field_set_rhs(afg_ctx* ctx, int i_rhs, int s_in) {
+// field_set_rhs; with maxbits the FP32-path kernel also folds max |rhs|
+// over the leaves into *maxbits (reset by the caller)
+static int field_set_rhs(afg_ctx* ctx, int i_rhs, int s_in, unsigned long long* maxbits);
+
+int afg_field_set_rhs(afg_ctx* ctx, int i_rhs, int s_in) { return field_set_rhs(ctx, i_rhs, s_in, nullptr); }
+
+static int field_set_rhs(afg_ctx* ctx, int i_rhs, int s_in, unsigned long long* maxbits) {
   RC(need_transport(ctx));
   RC(check_var(ctx, i_rhs));
   const afg_transport_desc& d = ctx->tr.d;
@@ -430,9 +439,9 @@ int afg_field_set_rhs(afg_ctx* ctx, int i_rhs, int s_in) {
     if (!mixed_transport(ctx))
       k_field_rhs<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ctx->S, list, a);
     else if (ctx->D == 3)
-      AFG_NC3(NCV_, k_field_rhs_interior<3, NCV_><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), list, a));
+      AFG_NC3(NCV_, k_field_rhs_interior<3, NCV_><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), list, a, maxbits));
     else
-      AFG_NC2(NCV_, k_field_rhs_interior<2, NCV_><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), list, a));
+      AFG_NC2(NCV_, k_field_rhs_interior<2, NCV_><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), list, a, maxbits));
     ctx->launches++;
     CKL();
   }
@@ -473,14 +482,22 @@ int afg_field_compute(afg_ctx* ctx, int mg_id, int s_in, int have_guess, double 
   RC(need_transport(ctx));
   MgSlot* m;
   RC(get_mg(ctx, mg_id, &m));
-  RC(afg_field_set_rhs(ctx, m->d.i_rhs, s_in));
+  double max_rhs;
+  if (mixed_transport(ctx)) {
+    RC(reset_max(ctx, 0));
+    RC(field_set_rhs(ctx, m->d.i_rhs, s_in, ctx->d_max));
+  } else {
+    RC(field_set_rhs(ctx, m->d.i_rhs, s_in, nullptr));
+  }
   // field_bc_homogeneous: Dirichlet `voltage` on the high face of the last dimension
   double bcv[6];
   for (int q = 0; q < 6; q++) bcv[q] = m->d.bc_val[q];
   bcv[2 * ctx->D - 1] = voltage;
   RC(afg_mg_set_bc_values(ctx, mg_id, bcv));
-  double max_rhs;
-  RC(afg_maxabs(ctx, m->d.i_rhs, 1, &max_rhs));
+  if (mixed_transport(ctx))
+    RC(read_max(ctx, 0, &max_rhs));
+  else
+    RC(afg_maxabs(ctx, m->d.i_rhs, 1, &max_rhs));
   // af_min_dr: finest dr of the highest level
   std::vector<double> hdr(ctx->D);
   const int s_fine = ctx->lvl_ids[ctx->highest_lvl - 1][0];
