@@ -232,6 +232,8 @@ def load_library(path: str = LIB_PATH):
         "afg_kernel_stats": (C.c_int, [P, C.POINTER(C.c_longlong), _DP, _DP]),
         "afg_maxabs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, _DP]),
         "afg_host_register": (C.c_int, [P, C.c_void_p, C.c_size_t]),
+        "afg_cc_download_async": (C.c_int, [P, C.c_int, C.POINTER(_DP), C.c_longlong]),
+        "afg_transfers_wait": (C.c_int, [P]),
         "afg_host_unregister": (C.c_int, [P, C.c_void_p]),
         "afg_sync": (C.c_int, [P]),
         "afg_launch_count": (C.c_longlong, [P]),
@@ -337,6 +339,19 @@ class Context:
         for v, iv in enumerate(ivs):
             col = v if cols is None else cols[v]
             self.check(self.lib.afg_cc_download(self.ptr, iv, bp.ptr, col * S), "afg_cc_download")
+
+    def download_vars_async(self, cc: np.ndarray, ivs, cols=None, bp=None):
+        """Start downloading variable ivs[v] into column cols[v] of cc (see
+        afg_cc_download_async); keep `bp` alive until transfers_wait()."""
+        S = int(np.prod(cc.shape[2:]))
+        bp = bp or box_pointers(cc)
+        for v, iv in enumerate(ivs):
+            col = v if cols is None else cols[v]
+            self.check(self.lib.afg_cc_download_async(self.ptr, iv, bp.ptr, col * S), "afg_cc_download_async")
+        return bp
+
+    def transfers_wait(self):
+        self.check(self.lib.afg_transfers_wait(self.ptr), "afg_transfers_wait")
 
     def upload_fc(self, fc: np.ndarray, ivfs=None):
         fc = np.ascontiguousarray(fc, dtype=np.float64)

@@ -111,6 +111,9 @@ struct afg_ctx {
   // side streams and events for independent branches (photoionization modes)
   cudaStream_t side[kMaxBranch] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[kMaxBranch] = {};
+  // asynchronous downloads (afg_cc_download_async)
+  cudaStream_t xfer_stream = nullptr;
+  cudaEvent_t ev_xfer = nullptr;
   double* h_stage = nullptr;            // pinned staging
   size_t stage_elems = 0;
   MgSlot mg[kMaxMg];
@@ -683,6 +686,8 @@ int afg_init(int device, afg_ctx** out) {
   CK(dalloc(&ctx->d_max, kMaxSlots));
   CK(cudaMallocHost((void**)&ctx->h_max, kMaxSlots * sizeof(unsigned long long)));
   for (auto& st : ctx->side) CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&ctx->xfer_stream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&ctx->ev_xfer, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
   for (auto& e : ctx->ev_join) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (auto& e : ctx->xfer_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -703,6 +708,11 @@ int afg_finalize(afg_ctx* ctx) {
   if (ctx->flush_buf) cudaFree(ctx->flush_buf);
   dfree(ctx->d_max);
   if (ctx->h_max) cudaFreeHost(ctx->h_max);
+  if (ctx->xfer_stream) {
+    cudaStreamSynchronize(ctx->xfer_stream);
+    cudaStreamDestroy(ctx->xfer_stream);
+  }
+  if (ctx->ev_xfer) cudaEventDestroy(ctx->ev_xfer);
   for (auto& st : ctx->side)
     if (st) cudaStreamDestroy(st);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
@@ -1024,6 +1034,31 @@ __global__ void __launch_bounds__(256) k_scatter_pitched(double* __restrict__ ds
   }
 }
 
+// The same scatter with a small grid for copies that overlap other work: few
+// blocks (the link, not the SMs, is the limit), each thread moving one
+// double2 of four boxes at a time so enough bytes are in flight.
+constexpr int kXferAsyncBlocks = 64;
+__global__ void __launch_bounds__(256) k_scatter_pitched_narrow(double* __restrict__ dst,
+                                                                const double* __restrict__ src, size_t pitch, int E,
+                                                                int n) {
+  const int G = gridDim.x, h = E / 2;
+  for (int b0 = blockIdx.x; b0 < n; b0 += 4 * G) {
+    for (int x = threadIdx.x; x < h; x += blockDim.x) {
+      double2 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int b = b0 + u * G;
+        if (b < n) v[u] = reinterpret_cast<const double2*>(src + (size_t)b * E)[x];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int b = b0 + u * G;
+        if (b < n) reinterpret_cast<double2*>(dst + (size_t)b * pitch)[x] = v[u];
+      }
+    }
+  }
+}
+
 // Device address of [p, p + bytes) when the whole span lies inside one range
 // page-locked by afg_host_register (mapped, so the GPU may access it);
 // nullptr otherwise.
@@ -1119,6 +1154,39 @@ static int d2h_boxes(afg_ctx* ctx, const double* src, size_t E, double* const* b
     for (int b = b0; b < b1; b++)
       if (box[b]) memcpy(box[b] + off, ctx->h_stage + (size_t)b * E, sizeof(double) * E);
   }
+  return AFG_OK;
+}
+
+int afg_cc_download_async(afg_ctx* ctx, int iv, double* const* box_cc, long long off) {
+  RC(check_var(ctx, iv));
+  if (!box_cc) return fail(ctx, AFG_ERR_ARG, "null box_cc");
+  const size_t E = ctx->S;
+  const int n = ctx->n_boxes;
+  size_t pitch = 0;
+  if (pitched_boxes(n, E, box_cc, off, &pitch)) {
+    double* first = box_cc[0] + off;
+    const void* dev = registered_span(ctx, first, sizeof(double) * ((size_t)(n - 1) * pitch + E));
+    if (dev) {
+      // ordered after all work issued so far on the context's stream
+      CK(cudaEventRecord(ctx->ev_xfer, ctx->stream));
+      CK(cudaStreamWaitEvent(ctx->xfer_stream, ctx->ev_xfer, 0));
+      const int vec2 = ((uintptr_t)dev % 16 == 0) && pitch % 2 == 0 && E % 2 == 0;
+      if (vec2)
+        k_scatter_pitched_narrow<<<kXferAsyncBlocks, 256, 0, ctx->xfer_stream>>>((double*)dev, ctx->cc[iv - 1],
+                                                                                 pitch, (int)E, n);
+      else
+        k_scatter_pitched<<<kXferAsyncBlocks, 256, 0, ctx->xfer_stream>>>((double*)dev, ctx->cc[iv - 1], pitch,
+                                                                          (int)E, n, 0);
+      CK(cudaGetLastError());
+      return AFG_OK;
+    }
+  }
+  return d2h_boxes(ctx, ctx->cc[iv - 1], E, box_cc, off);
+}
+
+int afg_transfers_wait(afg_ctx* ctx) {
+  if (!ctx) return AFG_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->xfer_stream));
   return AFG_OK;
 }
 

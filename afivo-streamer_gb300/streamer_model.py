@@ -264,7 +264,10 @@ class StreamerRun:
         self.ctx.gc(self.m.i_phi, 0, True)
         return self.field(0, False)
 
-    def step(self):
+    def step(self, after_update=None):
+        """One time step; after_update() (optional) is called once the new
+        densities are computed and before the field of the new state, which
+        writes no density (e.g. to start their download)."""
         ctx, m, dt = self.ctx, self.m, self.dt
         self.last = {"vcycles": 0}
         if self.photoi is not None and self.it % self.photoi_per_steps == 0:
@@ -280,6 +283,8 @@ class StreamerRun:
         self.field(1, True)
         lim2 = ctx.flux_upwind(1)
         chem = ctx.update_densities(0.5 * dt, 1, [0, 1], [0.5, 0.5], 0, last_step=True)
+        if after_update is not None:
+            after_update()
         # field of the new state
         n, r = self.field(0, True)
         self.last.update(cfl=min(lim1[0], lim2[0]), drt=min(lim1[1], lim2[1]), chem=chem, residual=r)

@@ -151,6 +151,18 @@ int afg_cc_download(afg_ctx* ctx, int iv, double* const* box_cc,
  * page-locked staging buffer, overlapped with the DMA in 32 MiB chunks.
  * Every copy has completed when the call returns. */
 
+/* As afg_cc_download, but for boxes inside a range registered with
+ * afg_host_register (equally spaced pointers) the copy is only started: it
+ * runs on a transfer stream after all work issued so far and the call returns
+ * at once, so it can overlap later work that does not write variable iv.
+ * The caller must not write iv on the device, nor read or free the host
+ * boxes, before afg_transfers_wait.  Other host memory: a synchronous copy.
+ * No counterpart in the reference. */
+int afg_cc_download_async(afg_ctx* ctx, int iv, double* const* box_cc,
+                          long long elem_offset);
+/* Wait for the copies started by afg_cc_download_async. */
+int afg_transfers_wait(afg_ctx* ctx);
+
 /* Page-lock and map (cudaHostRegister) / release caller-owned host memory,
  * e.g. the storage behind the box arrays passed to the copy routines; the
  * context remembers the range until afg_host_unregister (same ptr).  No

@@ -63,6 +63,29 @@ def test_roundtrip_page_locked_elsewhere(ctx_tree):
     assert np.array_equal(a, b)
 
 
+def test_async_download_overlaps_later_work(ctx_tree):
+    """afg_cc_download_async: the copy is ordered after earlier work and
+    completes by afg_transfers_wait, while later work on other variables
+    proceeds."""
+    ctx, tree = ctx_tree
+    a = host(tree, 2, 6)
+    ctx.upload_vars(a, [1, 2])
+    b = np.zeros_like(a)
+    ctx.host_register(b)
+    try:
+        ctx.tree_copy_cc(1, 3)                 # earlier work reading variable 1
+        bp = ctx.download_vars_async(b, [1])   # ordered after it
+        ctx.tree_copy_cc(2, 3)                 # later work, not writing variable 1
+        ctx.transfers_wait()
+        ctx.sync()
+    finally:
+        ctx.host_unregister(b)
+    assert np.array_equal(b[:, 0], a[:, 0])
+    c = np.zeros((tree.n_boxes, 1) + a.shape[2:])
+    ctx.download_vars(c, [3])
+    assert np.array_equal(c[:, 0], a[:, 1])
+
+
 def test_null_boxes_untouched(ctx_tree):
     ctx, tree = ctx_tree
     a = host(tree, 1, 2)
