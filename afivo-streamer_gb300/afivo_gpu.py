@@ -234,6 +234,8 @@ def load_library(path: str = LIB_PATH):
         "afg_host_register": (C.c_int, [P, C.c_void_p, C.c_size_t]),
         "afg_cc_download_async": (C.c_int, [P, C.c_int, C.POINTER(_DP), C.c_longlong]),
         "afg_transfers_wait": (C.c_int, [P]),
+        "afg_autotune": (C.c_int, [P, C.c_int]),
+        "afg_tuning": (C.c_int, [P, _IP]),
         "afg_host_unregister": (C.c_int, [P, C.c_void_p]),
         "afg_sync": (C.c_int, [P]),
         "afg_launch_count": (C.c_longlong, [P]),
@@ -349,6 +351,14 @@ class Context:
             col = v if cols is None else cols[v]
             self.check(self.lib.afg_cc_download_async(self.ptr, iv, bp.ptr, col * S), "afg_cc_download_async")
         return bp
+
+    def autotune(self, mg_id):
+        self.check(self.lib.afg_autotune(self.ptr, mg_id), "afg_autotune")
+
+    def tuning(self):
+        out = (C.c_int * 2)()
+        self.check(self.lib.afg_tuning(self.ptr, out), "afg_tuning")
+        return {"gsrb_cells_per_thread_fp32": out[0], "gsrb_cells_per_thread_fp64": out[1]}
 
     def transfers_wait(self):
         self.check(self.lib.afg_transfers_wait(self.ptr), "afg_transfers_wait")

@@ -111,6 +111,9 @@ struct afg_ctx {
   // side streams and events for independent branches (photoionization modes)
   cudaStream_t side[kMaxBranch] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[kMaxBranch] = {};
+  // smoother work shape (cells of a colour per thread) for the specialized
+  // box sizes: [0] FP32, [1] FP64; picked by the autotuner, 0 = default
+  int gsrb_cpt[2] = {0, 0};
   // asynchronous downloads (afg_cc_download_async)
   cudaStream_t xfer_stream = nullptr;
   cudaEvent_t ev_xfer = nullptr;
@@ -306,6 +309,45 @@ static int launch_gsrb(afg_ctx* ctx, const int* list, int n, T* phi, const T* rh
   return AFG_OK;
 }
 
+static bool gsrb_rec_specialized(const afg_ctx* ctx) {
+  return (ctx->D == 3 && ctx->nc == 8) || (ctx->D == 2 && ctx->nc == 16);
+}
+template <typename T>
+static int gsrb_cpt_of(const afg_ctx* ctx) {
+  const int c = ctx->gsrb_cpt[sizeof(T) == 8 ? 1 : 0];
+  return c > 0 ? c : (ctx->D == 3 ? 4 : 2);
+}
+
+// record-driven half sweep with `cpt` cells of the colour per thread
+// (3D 8^3: 1, 2, 4, 8; 2D 16^2: 1, 2, 4)
+template <typename T>
+static int launch_gsrb_rec(afg_ctx* ctx, const int* rec, int n, T* phi, const T* rhs, int rb, MgCoef<T> lam,
+                           const GcDev& g, int cpt) {
+  KTree t = ktree(ctx);
+  if (ctx->D == 3) {
+    switch (cpt) {
+      case 1: k_gsrb_rec<3, false, T, 8, 1><<<n, 256, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      case 2: k_gsrb_rec<3, false, T, 8, 2><<<n, 128, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      case 8: k_gsrb_rec<3, false, T, 8, 8><<<n, 32, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      default: k_gsrb_rec<3, false, T, 8, 4><<<n, 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+    }
+  } else if (ctx->coord == AFG_CYL) {
+    switch (cpt) {
+      case 1: k_gsrb_rec<2, true, T, 16, 1><<<n, 128, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      case 4: k_gsrb_rec<2, true, T, 16, 4><<<n, 32, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      default: k_gsrb_rec<2, true, T, 16, 2><<<n, 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+    }
+  } else {
+    switch (cpt) {
+      case 1: k_gsrb_rec<2, false, T, 16, 1><<<n, 128, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      case 4: k_gsrb_rec<2, false, T, 16, 4><<<n, 32, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      default: k_gsrb_rec<2, false, T, 16, 2><<<n, 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+    }
+  }
+  CKL();
+  return AFG_OK;
+}
+
 template <typename T>
 static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, int rb, MgCoef<T> lam,
                              const GcDev& g) {
@@ -313,15 +355,11 @@ static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, T* phi, const
   KTree t = ktree(ctx);
   const int threads = ctx->D == 2 ? std::min(256, ctx->nc * ctx->nc / 2) : std::min(256, ctx->nc * ctx->nc * ctx->nc / 2);
   kt_begin(ctx, AFG_KT_GSRB);
-  const int* rec = rec_of(ctx, list);
-  // the usual box sizes: several cells per thread, box records
-  if (ctx->D == 3 && ctx->nc == 8)
-    k_gsrb_rec<3, false, T, 8, 4><<<n, 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g);
-  else if (ctx->D == 2 && ctx->nc == 16 && ctx->coord == AFG_CYL)
-    k_gsrb_rec<2, true, T, 16, 2><<<n, 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g);
-  else if (ctx->D == 2 && ctx->nc == 16)
-    k_gsrb_rec<2, false, T, 16, 2><<<n, 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g);
-  else if (ctx->D == 3)
+  // the usual box sizes: several cells per thread (tuned), box records
+  if (gsrb_rec_specialized(ctx)) {
+    const int rc = launch_gsrb_rec<T>(ctx, rec_of(ctx, list), n, phi, rhs, rb, lam, g, gsrb_cpt_of<T>(ctx));
+    if (rc != AFG_OK) return rc;
+  } else if (ctx->D == 3)
     k_gsrb_fused<3, false, T, 0><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
   else if (ctx->coord == AFG_CYL)
     k_gsrb_fused<2, true, T, 0><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
@@ -666,6 +704,56 @@ static int reset_max(afg_ctx* ctx, int slot) {
   return AFG_OK;
 }
 
+// Autotuner of the smoother's work shape: on the level with the most boxes,
+// time every cells-per-thread variant of the FP32 half sweep (CUDA events,
+// best of 3 after a warm-up) on the slot's FP32 buffers, which are scratch
+// outside a solve, and keep the fastest.  All variants do the same
+// arithmetic, so the choice changes speed only.
+static int autotune_gsrb(afg_ctx* ctx, MgSlot& m) {
+  if (!gsrb_rec_specialized(ctx) || !m.e32) return AFG_OK;
+  int best_l = 0;
+  for (int l = 0; l < ctx->highest_lvl; l++)
+    if (ctx->lvl_ids[l].size() > ctx->lvl_ids[best_l].size()) best_l = l;
+  const int n = (int)ctx->lvl_ids[best_l].size();
+  if (n < 256) return AFG_OK;  // too small to time; the default stays
+  const int* rec = rec_of(ctx, lst(ctx, ctx->off_ids[best_l]));
+  const GcDev g = mg_gc(m.d, true);
+  const int cands3[] = {1, 2, 4, 8}, cands2[] = {1, 2, 4};
+  const int* cands = ctx->D == 3 ? cands3 : cands2;
+  const int nc = ctx->D == 3 ? 4 : 3;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int best_c = gsrb_cpt_of<float>(ctx);
+  int rc = AFG_OK;
+  for (int q = 0; q < nc && rc == AFG_OK; q++) {
+    float tmin = 1e30f;
+    for (int r = 0; r < 4 && rc == AFG_OK; r++) {
+      cudaEventRecord(e0, ctx->stream);
+      rc = launch_gsrb_rec<float>(ctx, rec, n, m.e32, m.r32, 1 + (r & 1), coef_of<float>(m), g, cands[q]);
+      cudaEventRecord(e1, ctx->stream);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (r > 0) tmin = std::min(tmin, ms);
+    }
+    if (tmin < best) {
+      best = tmin;
+      best_c = cands[q];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  RC(rc);
+  ctx->gsrb_cpt[0] = best_c;
+  // the correction buffers were only smoothed with zero data; clear them
+  const size_t N = (size_t)ctx->n_boxes * ctx->S;
+  CK(cudaMemsetAsync(m.e32, 0, N * sizeof(float), ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return AFG_OK;
+}
+
 #include "afg_mixed.cuh"
 
 /* ========================================================================= */
@@ -961,6 +1049,7 @@ int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_va
   ctx->stage_elems = (size_t)n * std::max(ctx->S, D * ctx->NF);
   CK(cudaMallocHost((void**)&ctx->h_stage, sizeof(double) * ctx->stage_elems));
   CK(cudaStreamSynchronize(ctx->stream));
+  ctx->gsrb_cpt[0] = ctx->gsrb_cpt[1] = 0;  // a new tree is tuned again
   ctx->have_tree = true;
   return AFG_OK;
 }
@@ -1456,6 +1545,7 @@ int afg_mg_setup(afg_ctx* ctx, int mg_id, const afg_mg_desc* d) {
     CK(cudaMemset(m.e32, 0, N * sizeof(float)));
     CK(cudaMemset(m.r32, 0, N * sizeof(float)));
     CK(cudaMemset(m.t32, 0, N * sizeof(float)));
+    if (ctx->gsrb_cpt[0] == 0) RC(autotune_gsrb(ctx, m));
   }
   m.used = true;
   // mg_init: phi gets the multigrid ghost-cell methods
@@ -1596,6 +1686,22 @@ int afg_tree_copy_cc(afg_ctx* ctx, int iv_from, int iv_to) {
   if (iv_from == iv_to) return AFG_OK;
   CK(cudaMemcpyAsync(ctx->cc[iv_to - 1], ctx->cc[iv_from - 1], sizeof(double) * (size_t)ctx->n_boxes * ctx->S,
                      cudaMemcpyDeviceToDevice, ctx->stream));
+  return AFG_OK;
+}
+
+int afg_autotune(afg_ctx* ctx, int mg_id) {
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  if (m->d.precision != AFG_MIXED) return fail(ctx, AFG_ERR_ARG, "autotuning needs a mixed-precision slot (scratch)");
+  clear_graphs(ctx);
+  return autotune_gsrb(ctx, *m);
+}
+
+int afg_tuning(const afg_ctx* ctx, int* out) {
+  if (!ctx || !out) return AFG_ERR_ARG;
+  const bool sp = gsrb_rec_specialized(ctx);
+  out[0] = sp ? gsrb_cpt_of<float>(ctx) : 0;
+  out[1] = sp ? gsrb_cpt_of<double>(ctx) : 0;
   return AFG_OK;
 }
 

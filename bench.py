@@ -183,8 +183,10 @@ def run_gpu_arm(args, device, w):
         res["vcycle_ms"] = ctx.event_elapsed(2, 3) / max(1, n)
         results[prec_name] = (res, run)
     if args.profile:
+        tuning = ctx.tuning()
         ctx.close()
-        return tree, results, {}, None
+        return tree, results, {}, None, tuning
+    tuning = ctx.tuning()
     # per-kernel-class device time during one mixed step (graphs off while timing)
     run = results["mixed"][1]
     kstats = {}
@@ -234,7 +236,7 @@ def run_gpu_arm(args, device, w):
                transfer_path="zero-copy kernels on host boxes page-locked by afg_host_register; the species "
                              "download overlaps the step's final field solve (afg_cc_download_async)")
     ctx.close()
-    return tree, results, kstats, e2e
+    return tree, results, kstats, e2e, tuning
 
 
 def run_cpu(name, steps, warmup=1, time_limit=None):
@@ -324,7 +326,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("gloo")
     w = workloads.WORKLOADS[args.config]()
-    tree, results, kstats, e2e = run_gpu_arm(args, local, w)
+    tree, results, kstats, e2e, tuning = run_gpu_arm(args, local, w)
     if args.profile:
         if rank == 0:
             print(json.dumps({"profile": True, "config": config, "mixed": results["mixed"][0]}))
@@ -366,7 +368,7 @@ def main():
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "algorithmic_bytes_per_launch": ks["bytes"] / max(1, ks["launches"]),
                          "avg_launch_us": 1e3 * ks["ms"] / max(1, ks["launches"])},
-            "kernel_classes": kstats,
+            "kernel_classes": kstats, "tuning": tuning,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": mixed["clocks"],
             "gpu_launches": int(mixed["launches"]),
         }))

@@ -160,6 +160,16 @@ int afg_cc_download(afg_ctx* ctx, int iv, double* const* box_cc,
  * No counterpart in the reference. */
 int afg_cc_download_async(afg_ctx* ctx, int iv, double* const* box_cc,
                           long long elem_offset);
+/* Autotuner: the work shape of the smoother (cells per thread, i.e. threads
+ * per box) is timed on the largest level and the fastest kept.  It runs when
+ * the first AFG_MIXED slot is set up on a tree (its FP32 buffers are the
+ * scratch); afg_autotune repeats it for slot mg_id (AFG_MIXED).  All variants
+ * compute the same values.  afg_tuning reports the choice: out[0] FP32,
+ * out[1] FP64 cells per thread (0: not a tuned box size).  No counterpart in
+ * the reference. */
+int afg_autotune(afg_ctx* ctx, int mg_id);
+int afg_tuning(const afg_ctx* ctx, int* out);
+
 /* Wait for the copies started by afg_cc_download_async. */
 int afg_transfers_wait(afg_ctx* ctx);
 
