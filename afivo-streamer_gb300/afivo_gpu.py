@@ -197,6 +197,12 @@ def load_library(path: str = LIB_PATH):
         "afg_finalize": (C.c_int, [P]),
         "afg_last_error": (C.c_char_p, [P]),
         "afg_tree_sync": (C.c_int, [P, C.POINTER(TreeDesc), C.c_int, C.c_int]),
+        "afg_tree_sync_batched": (C.c_int, [P, C.POINTER(TreeDesc), C.c_int, C.c_int, C.c_int, _IP]),
+        "afg_n_instances": (C.c_int, [P]),
+        "afg_mg_set_bc_values_inst": (C.c_int, [P, C.c_int, _DP]),
+        "afg_mg_solve_inst": (C.c_int, [P, C.c_int, _DP, C.c_int, _IP, _DP]),
+        "afg_field_compute_inst": (C.c_int, [P, C.c_int, C.c_int, C.c_int, _DP, C.c_double, C.c_double,
+                                             C.c_int, _IP, _DP]),
         "afg_cc_upload": (C.c_int, [P, C.c_int, C.POINTER(_DP), C.c_longlong]),
         "afg_cc_download": (C.c_int, [P, C.c_int, C.POINTER(_DP), C.c_longlong]),
         "afg_fc_upload": (C.c_int, [P, C.c_int, C.POINTER(_DP), C.c_longlong]),
@@ -300,13 +306,25 @@ class Context:
             pass
 
     # -- tree mirror ------------------------------------------------------
-    def tree_sync(self, tree, n_var_cell: int, n_var_face: int = 0):
+    def tree_sync(self, tree, n_var_cell: int, n_var_face: int = 0, box_inst=None):
+        """Mirror `tree`; with box_inst (instance of each box, 0-based) the
+        tree is a forest of independent instances (afg_tree_sync_batched)."""
         self._tree_holder = TreeDescHolder(tree)
         self.tree = tree
         self.n_var = n_var_cell
         self.n_var_face = n_var_face
-        self.check(self.lib.afg_tree_sync(self.ptr, C.byref(self._tree_holder.desc),
-                                          n_var_cell, n_var_face), "afg_tree_sync")
+        if box_inst is None:
+            self.check(self.lib.afg_tree_sync(self.ptr, C.byref(self._tree_holder.desc),
+                                              n_var_cell, n_var_face), "afg_tree_sync")
+            return
+        self._box_inst = np.ascontiguousarray(box_inst, dtype=np.int32)
+        n_inst = int(self._box_inst.max()) + 1
+        self.check(self.lib.afg_tree_sync_batched(self.ptr, C.byref(self._tree_holder.desc), n_var_cell,
+                                                  n_var_face, n_inst, _ip(self._box_inst)),
+                   "afg_tree_sync_batched")
+
+    def n_instances(self):
+        return self.lib.afg_n_instances(self.ptr)
 
     def upload(self, cc: np.ndarray, ivs=None, first_iv=1):
         """Upload variables ivs (1-based) from host boxes cc[n, n_var, ...];
@@ -406,6 +424,22 @@ class Context:
         a[:len(vals)] = vals
         self.check(self.lib.afg_mg_set_bc_values(self.ptr, mg_id, _dp(a)), "afg_mg_set_bc_values")
 
+    def mg_set_bc_values_inst(self, mg_id, vals):
+        """vals[q][face] per instance of a batched tree."""
+        v = np.asarray(vals, dtype=np.float64)
+        a = np.zeros((v.shape[0], 6))
+        a[:, :v.shape[1]] = v
+        self.check(self.lib.afg_mg_set_bc_values_inst(self.ptr, mg_id, _dp(a)), "afg_mg_set_bc_values_inst")
+
+    def mg_solve_inst(self, mg_id, thresholds, max_cycles=50, allow_noconv=False):
+        thr = np.ascontiguousarray(thresholds, dtype=np.float64)
+        n = np.zeros(len(thr), dtype=np.int32)
+        res = np.zeros(len(thr))
+        rc = self.lib.afg_mg_solve_inst(self.ptr, mg_id, _dp(thr), max_cycles, _ip(n), _dp(res))
+        if not (allow_noconv and rc == AFG_ERR_NOCONV):
+            self.check(rc, "afg_mg_solve_inst")
+        return n, res
+
     def mg_vcycle(self, mg_id, set_residual=True, max_lvl=0):
         out = C.c_double(0)
         self.check(self.lib.afg_mg_vcycle(self.ptr, mg_id, int(set_residual), max_lvl, C.byref(out)),
@@ -472,6 +506,17 @@ class Context:
                                               max_rel_residual, num_vcycles, C.byref(n), C.byref(r)),
                    "afg_field_compute")
         return n.value, r.value
+
+    def field_compute_inst(self, mg_id, s_in, have_guess, voltages, domain_len, max_rel_residual, num_vcycles):
+        """field_compute of every instance of a batched tree with its own
+        voltage; per-instance cycle counts and final residuals."""
+        v = np.ascontiguousarray(voltages, dtype=np.float64)
+        n = np.zeros(len(v), dtype=np.int32)
+        r = np.zeros(len(v))
+        self.check(self.lib.afg_field_compute_inst(self.ptr, mg_id, s_in, int(have_guess), _dp(v), domain_len,
+                                                   max_rel_residual, num_vcycles, _ip(n), _dp(r)),
+                   "afg_field_compute_inst")
+        return n, r
 
     def photoi_helmh(self, coeff, mg_ids, coeffs, max_rel_residual=1e-2, max_fmg_cycles=10):
         ids = np.ascontiguousarray(mg_ids, dtype=np.int32)

@@ -324,3 +324,43 @@ def seeded_refinement(center, sigma, base_lvl, rng=None, frac=0.0):
             m |= (rng.random(len(centers)) < frac) & (d < 2.5 * radius)
         return m
     return f
+
+
+def forest(trees):
+    """Independent trees as one forest for a batched context
+    (afg_tree_sync_batched): the box ids of tree q follow those of trees
+    0..q-1, every id-valued table is shifted accordingly (0 = no box and -1 =
+    physical boundary stay), and each level list is the concatenation of the
+    trees' lists of that level.  All trees must share ndim, n_cell, the
+    coordinate system and the coarse grid.  Returns the forest and the
+    instance (0-based) of each of its boxes."""
+    t0 = trees[0]
+    for t in trees[1:]:
+        if (t.ndim, t.n_cell, t.coord) != (t0.ndim, t0.n_cell, t0.coord) or \
+                np.any(np.asarray(t.coarse_grid_size) != np.asarray(t0.coarse_grid_size)):
+            raise ValueError("forest trees need the same ndim, n_cell, coordinates and coarse grid")
+    offs = np.cumsum([0] + [t.n_boxes for t in trees])
+
+    def shift(a, off):
+        a = np.asarray(a)
+        return np.where(a > 0, a + off, a)
+
+    H = max(t.highest_lvl for t in trees)
+    f = Tree(ndim=t0.ndim, n_cell=t0.n_cell, coord=t0.coord, coarse_grid_size=np.asarray(t0.coarse_grid_size),
+             r_base=t0.r_base, dr_base=t0.dr_base, n_boxes=int(offs[-1]), highest_lvl=H)
+    f.lvl = np.concatenate([t.lvl for t in trees])
+    f.ix = np.concatenate([t.ix for t in trees])
+    f.parent = np.concatenate([shift(t.parent, o) for t, o in zip(trees, offs)])
+    f.children = np.concatenate([shift(t.children, o) for t, o in zip(trees, offs)])
+    f.neighbors = np.concatenate([shift(t.neighbors, o) for t, o in zip(trees, offs)])
+    f.neighbor_mat = np.concatenate([shift(t.neighbor_mat, o) for t, o in zip(trees, offs)])
+    f.r_min = np.concatenate([t.r_min for t in trees])
+    f.dr = np.concatenate([t.dr for t in trees])
+    for name in ("lvl_ids", "lvl_leaves", "lvl_parents"):
+        per_level = []
+        for l in range(H):
+            parts = [np.asarray(getattr(t, name)[l]) + o for t, o in zip(trees, offs) if l < t.highest_lvl]
+            per_level.append(np.concatenate(parts).astype(np.int64) if parts else np.zeros(0, np.int64))
+        setattr(f, name, per_level)
+    box_inst = np.concatenate([np.full(t.n_boxes, q, dtype=np.int32) for q, t in enumerate(trees)])
+    return f, box_inst

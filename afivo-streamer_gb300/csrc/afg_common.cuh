@@ -37,7 +37,24 @@ struct KTree {
   // rounded division, so identical to 1 / dr evaluated on the device
   const double* idr;
   const float* idrf;  // the same rounded to FP32
+  // Batched independent instances (null for a single tree): instance of
+  // each slot, and per instance a flag that freezes it (set for instances
+  // whose solve has converged while others continue): kernels of the solve
+  // loops leave the boxes of a frozen instance untouched.
+  const int* inst;
+  const int* frozen;
 };
+
+// maxima slots per instance in the device maxima array ([instance][slot])
+constexpr int kMaxSlotsDev = 24;
+
+__device__ __forceinline__ bool box_frozen(const KTree& t, int slot) {
+  return t.frozen != nullptr && t.frozen[t.inst[slot]] != 0;
+}
+// the maxima word of the box's instance (batched trees) or the word itself
+__device__ __forceinline__ unsigned long long* inst_max(const KTree& t, unsigned long long* m, int slot) {
+  return t.inst != nullptr ? m + (size_t)t.inst[slot] * kMaxSlotsDev : m;
+}
 
 // Box records: per entry of a box list, {slot, neighbour slot of faces
 // 0..2D-1, ..., source flag} in 8 ints, read as two int4 (one 32-byte load);
@@ -149,6 +166,9 @@ struct GcDev {
   int bc_type[6];
   double bc_val[6];
   int rb;
+  // batched trees: boundary values per instance [instance][6] in device
+  // memory, replacing bc_val (null: bc_val holds them)
+  const double* ival = nullptr;
 };
 
 // bc_type[nb] / bc_val[nb] of a ghost-cell method for a run-time face index,
@@ -166,6 +186,10 @@ __device__ __forceinline__ double gc_val(const GcDev& g, int nb) {
   for (int k = 1; k < 6; k++)
     if (nb == k) r = g.bc_val[k];
   return r;
+}
+// boundary value of face nb for box `slot` (its instance's on batched trees)
+__device__ __forceinline__ double gc_val(const GcDev& g, int nb, const KTree& t, int slot) {
+  return g.ival != nullptr ? g.ival[t.inst[slot] * 6 + nb] : gc_val(g, nb);
 }
 
 __device__ __forceinline__ int at2(int n2, int i, int j) { return i + n2 * j; }

@@ -36,7 +36,7 @@ __device__ __forceinline__ T face_ghost_nb(const KTree& t, const T* __restrict__
   }
   if (nbs == kNbPhys) {
     const int i1 = low ? 1 : nc, i2 = low ? 2 : nc - 1;
-    return bc_ghost<D, T>(gc_type(g, nb), gc_val(g, nb), t.dr[slot * D + d], low,
+    return bc_ghost<D, T>(gc_type(g, nb), gc_val(g, nb, t, slot), t.dr[slot * D + d], low,
                           a[face_at<D>(n2, d, i1, p, q)], a[face_at<D>(n2, d, i2, p, q)]);
   }
   // refinement boundary: data of the parent's neighbour
@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(256) k_gc(KTree t0, const int* __restrict__ re
   int4 r0, r1;
   load_rec(rec, blockIdx.x, r0, r1);
   const int slot = r0.x;
+  if (box_frozen(t, slot)) return;
   const int nc = t.nc;
   const int nface = D == 2 ? nc : nc * nc;
   T* a = v + (size_t)slot * t.S;

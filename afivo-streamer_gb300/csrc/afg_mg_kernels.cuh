@@ -101,6 +101,7 @@ __global__ void __launch_bounds__(256) k_gsrb(KTree t0, const int* __restrict__ 
                                               const T* __restrict__ rhs, int redblack, MgCoef<T> mc) {
   const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
+  if (box_frozen(t, slot)) return;
   const int nc = t.nc, n2 = t.n2, hn = nc / 2;
   T c[7];
   for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
@@ -146,6 +147,7 @@ __global__ void __launch_bounds__(256, 6) k_gsrb_fused(KTree t0, const int* __re
                                                     GcDev g) {
   const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
+  if (box_frozen(t, slot)) return;
   const int nc = t.nc, n2 = t.n2, hn = nc / 2;
   T c[7];
   for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
@@ -200,6 +202,7 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
   const int4 r0 = reinterpret_cast<const int4*>(rec)[2 * blockIdx.x];
   const int4 r1 = reinterpret_cast<const int4*>(rec)[2 * blockIdx.x + 1];
   const int slot = r0.x;
+  if (box_frozen(t, slot)) return;
   T c[7];
   for (int q = 0; q < 2 * D + 1; q++) c[q] = mc.cb[slot * 8 + q];
   const T inv_c1 = mc.cb[slot * 8 + 7];
@@ -255,6 +258,7 @@ __global__ void __launch_bounds__(256) k_residual(KTree t0, const int* __restric
   const KTree t = fix_dims<D, NC>(t0);
   __shared__ T sred[32];
   const int slot = list[blockIdx.x];
+  if (box_frozen(t, slot)) return;
   const int nc = t.nc, n2 = t.n2;
   T c[7];
   for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
@@ -278,7 +282,7 @@ __global__ void __launch_bounds__(256) k_residual(KTree t0, const int* __restric
   }
   if (maxbits != nullptr && is_leaf[slot]) {
     mx = block_max<T>(mx, sred);
-    if (threadIdx.x == 0) atomic_max_nonneg(maxbits, double(mx));
+    if (threadIdx.x == 0) atomic_max_nonneg(inst_max(t, maxbits, slot), double(mx));
   }
 }
 
@@ -296,6 +300,7 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* 
   int4 r0, r1;
   load_rec(rec, blockIdx.x, r0, r1);
   const int slot = r0.x;
+  if (box_frozen(t, slot)) return;
   const int pslot = t.parent[slot];
   const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
   T c[7];
@@ -385,6 +390,7 @@ __global__ void __launch_bounds__(256) k_coarse_fas(KTree t0, const int* __restr
   int4 r0, r1;
   load_rec(rec, blockIdx.x, r0, r1);
   const int slot = r0.x;
+  if (box_frozen(t, slot)) return;
   const int nc = t.nc, n2 = t.n2;
   if (fill) {
     T* a = phi + (size_t)slot * t.S;
@@ -432,6 +438,7 @@ __global__ void __launch_bounds__(256) k_correct(KTree t0, const int* __restrict
   extern __shared__ unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   const int slot = list[blockIdx.x];
+  if (box_frozen(t, slot)) return;
   const int nc = t.nc, n2 = t.n2;
   T* pp = phi + (size_t)slot * t.S;
   T* pt = tmp + (size_t)slot * t.S;
@@ -476,6 +483,7 @@ __global__ void __launch_bounds__(256) k_init_phi_rhs(KTree t0, const int* __res
                                                       T* __restrict__ phi, T* __restrict__ rhs) {
   const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
+  if (box_frozen(t, slot)) return;
   const int pslot = t.parent[slot];
   const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
   T* p = phi + (size_t)slot * t.S;
@@ -519,48 +527,71 @@ __global__ void __launch_bounds__(256) k_init_phi_rhs(KTree t0, const int* __res
 // Whole-array copy of one variable on a box list (af_boxes_copy_cc,
 // m_af_utils.f90:579-588).
 template <typename T>
-__global__ void __launch_bounds__(256) k_copy(int S, const int* __restrict__ list, const T* __restrict__ src,
+__global__ void __launch_bounds__(256) k_copy(KTree t, const int* __restrict__ list, const T* __restrict__ src,
                                               T* __restrict__ dst) {
   const int slot = list[blockIdx.x];
+  if (box_frozen(t, slot)) return;
+  const int S = t.S;
   for (int x = threadIdx.x; x < S; x += blockDim.x) dst[(size_t)slot * S + x] = src[(size_t)slot * S + x];
 }
 
 // Coarse-grid right-hand side with the boundary values folded in
-// (coarse_solver_set_rhs_phi, m_coarse_solver.f90:286-338).
+// (coarse_solver_set_rhs_phi, m_coarse_solver.f90:286-338).  Batched trees
+// stack one coarse grid of nloc unknowns per instance (n = n_inst * nloc):
+// the boundary tables are per local unknown, the values per instance
+// (bc_val + instance * bc_stride).
 template <typename T>
-__global__ void k_coarse_gather(int n, int D, const int* __restrict__ cslot, const int* __restrict__ ccell,
+__global__ void k_coarse_gather(int n, int nloc, int D, const int* __restrict__ cslot, const int* __restrict__ ccell,
                                 const double* __restrict__ b2r, const unsigned char* __restrict__ bmask,
-                                const double* __restrict__ bc_val, const T* __restrict__ rhs, int S,
+                                const double* __restrict__ bc_val, int bc_stride, const T* __restrict__ rhs, int S,
                                 double* __restrict__ b) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
+  const int q = g / nloc, gl = g - q * nloc;
+  const double* bv = bc_val + (size_t)q * bc_stride;
   double v = double(rhs[(size_t)cslot[g] * S + ccell[g]]);
-  const unsigned m = bmask[g];
+  const unsigned m = bmask[gl];
   for (int nb = 0; nb < 2 * D; nb++)
-    if (m & (1u << nb)) v = v + b2r[g * 2 * D + nb] * bc_val[nb];
+    if (m & (1u << nb)) v = v + b2r[gl * 2 * D + nb] * bv[nb];
   b[g] = v;
 }
 
-// x = A^-1 b, one warp per row: 32 strided partial sums then an xor
-// butterfly; the CPU oracle uses the same order.
-__global__ void k_coarse_matvec(int n, const double* __restrict__ ainv, const double* __restrict__ b,
+// x = A^-1 b per instance (the same inverse of nloc x nloc for all), one
+// warp per row: 32 strided partial sums then an xor butterfly; the CPU
+// oracle uses the same order.
+__global__ void k_coarse_matvec(int n, int nloc, const double* __restrict__ ainv, const double* __restrict__ b,
                                 double* __restrict__ x) {
   const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (row >= n) return;
-  const double* a = ainv + (size_t)row * n;
+  const int q = row / nloc, rl = row - q * nloc;
+  const double* a = ainv + (size_t)rl * nloc;
+  const double* bq = b + (size_t)q * nloc;
   double s = 0.0;
-  for (int c = lane; c < n; c += 32) s = s + a[c] * b[c];
+  for (int c = lane; c < nloc; c += 32) s = s + a[c] * bq[c];
   for (int o = 16; o > 0; o >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) x[row] = s;
 }
 
 template <typename T>
-__global__ void k_coarse_scatter(int n, const int* __restrict__ cslot, const int* __restrict__ ccell,
-                                 const double* __restrict__ x, T* __restrict__ phi, int S) {
+__global__ void k_coarse_scatter(KTree t, int n, const int* __restrict__ cslot, const int* __restrict__ ccell,
+                                 const double* __restrict__ x, T* __restrict__ phi) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
-  phi[(size_t)cslot[g] * S + ccell[g]] = T(x[g]);
+  const int slot = cslot[g];
+  if (box_frozen(t, slot)) return;
+  phi[(size_t)slot * t.S + ccell[g]] = T(x[g]);
+}
+
+// Freeze flags of batched instances as the kernels read them: the converged
+// instances (base) and those whose highest level lies outside [lo, hi].  An
+// FMG step at level l runs with [l, inf) (instances without level l are
+// finished with their FMG) and its residual with [l, l].
+__global__ void k_inst_mask(int n, const int* __restrict__ base, const int* __restrict__ hl, int lo, int hi,
+                            int* __restrict__ eff) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  eff[q] = (base[q] != 0 || hl[q] < lo || hl[q] > hi) ? 1 : 0;
 }
 
 // max |v| over interior cells of the list's boxes
@@ -580,7 +611,7 @@ __global__ void __launch_bounds__(256) k_maxabs(KTree t0, const int* __restrict_
     acc_absmax(mx, a[D == 2 ? at2(n2, i, j) : at3(n2, i, j, k)]);
   }
   mx = block_max<T>(mx, sred);
-  if (threadIdx.x == 0) atomic_max_nonneg(maxbits, double(mx));
+  if (threadIdx.x == 0) atomic_max_nonneg(inst_max(t, maxbits, slot), double(mx));
 }
 
 

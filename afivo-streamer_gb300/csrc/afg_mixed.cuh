@@ -34,6 +34,7 @@ __global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict_
   int4 r0, r1;
   load_rec(rec, blockIdx.x, r0, r1);
   const int slot = r0.x;
+  if (box_frozen(t, slot)) return;
   const int nc = t.nc, n2 = t.n2;
   float* eo = e32 + (size_t)slot * t.S;
   for (int x = threadIdx.x; x < t.S; x += blockDim.x) eo[x] = 0.0f;
@@ -82,7 +83,7 @@ __global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict_
     mx = fmaxf(mx, fabsf(res));
   }
   mx = block_max<float>(mx, sred);
-  if (threadIdx.x == 0) atomic_max_nonneg(maxbits, f2d(mx));
+  if (threadIdx.x == 0) atomic_max_nonneg(inst_max(t, maxbits, slot), f2d(mx));
 }
 
 // Whole-box conversions between the FP64 variables and the FP32 buffers
@@ -98,9 +99,11 @@ __global__ void __launch_bounds__(256) k_to_f64(int S, const int* __restrict__ l
 }
 
 // phi += e on whole boxes (ghost cells included)
-__global__ void __launch_bounds__(256) k_add_correction(int S, const int* __restrict__ list, double* __restrict__ phi,
+__global__ void __launch_bounds__(256) k_add_correction(KTree t, const int* __restrict__ list, double* __restrict__ phi,
                                                         const float* __restrict__ e32) {
   const int slot = list[blockIdx.x];
+  if (box_frozen(t, slot)) return;
+  const int S = t.S;
   double* p = phi + (size_t)slot * S;
   const float* e = e32 + (size_t)slot * S;
   for (int x = threadIdx.x; x < S; x += blockDim.x) p[x] = p[x] + f2d(e[x]);
@@ -116,7 +119,7 @@ static int launch_defect(afg_ctx* ctx, MgSlot& m, double* phi, const double* rhs
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   const int* list = rec_of(ctx, lst(ctx, ctx->off_all));
-  const GcDev g = mg_gc(m.d, false);
+  const GcDev g = mg_gc(ctx, m, false);
   if (ctx->D == 3)
     AFG_NC3(NCV_, k_defect<3, false, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), g, ctx->d_is_leaf,
                                                    maxbits));
@@ -152,7 +155,7 @@ static int mixed_prepare(afg_ctx* ctx, MgSlot& m, double* phi) {
   // refinement-boundary rules read face ghosts of the coarse source boxes;
   // those (level by level, coarse to fine: their own rules read coarser
   // sources) are filled here, before the launch.
-  const GcDev g = mg_gc(m.d, false);
+  const GcDev g = mg_gc(ctx, m, false);
   for (int lvl = 1; lvl <= ctx->highest_lvl; lvl++)
     RC(launch_gc<double>(ctx, lst(ctx, ctx->off_rbsrc[lvl - 1]), (int)ctx->lvl_rbsrc[lvl - 1].size(), phi, g, 0));
   return AFG_OK;
@@ -160,7 +163,7 @@ static int mixed_prepare(afg_ctx* ctx, MgSlot& m, double* phi) {
 
 // all ghost cells of phi (faces, edges, corners) when the solve ends
 static int mixed_finish(afg_ctx* ctx, MgSlot& m, double* phi) {
-  const GcDev g = mg_gc(m.d, false);
+  const GcDev g = mg_gc(ctx, m, false);
   for (int lvl = 1; lvl <= ctx->highest_lvl; lvl++) RC(mg_gc_lvl<double>(ctx, lvl, phi, g, 1));
   return AFG_OK;
 }
@@ -183,46 +186,10 @@ static int mixed_fmg(afg_ctx* ctx, MgSlot& m, double* phi, double* rhs, bool set
   RC(reset_max(ctx, 2));
   RC(launch_defect(ctx, m, phi, rhs, ctx->d_max + 2));
   RC(mg_fmg<float>(ctx, m, m.e32, m.r32, m.t32, false, false, nullptr, true));
-  k_add_correction<<<n, 256, 0, ctx->stream>>>(ctx->S, list, phi, m.e32);
+  k_add_correction<<<n, 256, 0, ctx->stream>>>(ktree(ctx), list, phi, m.e32);
   ctx->launches++;
   CKL();
   RC(mixed_prepare(ctx, m, phi));
   if (set_residual) RC(launch_defect(ctx, m, phi, rhs, maxbits));
   return mixed_finish(ctx, m, phi);
-}
-
-static int mixed_solve(afg_ctx* ctx, MgSlot& m, double threshold, int max_cycles, int* n_done, double* residuals) {
-  double* phi = ctx->cc[m.d.i_phi - 1];
-  double* rhs = ctx->cc[m.d.i_rhs - 1];
-  double r = 0;
-  int n = 0;
-  const int mg_id = (int)(&m - ctx->mg);
-  // defect of the current phi
-  RC(run_graph(ctx, gkey("defect", mg_id), [&]() -> int {
-    RC(mixed_prepare(ctx, m, phi));
-    RC(reset_max(ctx, 2));
-    return launch_defect(ctx, m, phi, rhs, ctx->d_max + 2);
-  }));
-  RC(read_max(ctx, 2, &r));
-  while (n < max_cycles) {
-    // one iteration: FP32 V-cycle on the correction, update, new defect
-    RC(run_graph(ctx, gkey("mixed_iter", mg_id), [&]() -> int {
-      RC(mg_vcycle<float>(ctx, m, ctx->highest_lvl, m.e32, m.r32, m.t32, false, true, nullptr));
-      // leaves only: mixed_prepare restricts the parents from them
-      k_add_correction<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ctx->S, lst(ctx, ctx->off_all_leaves), phi,
-                                                                  m.e32);
-      ctx->launches++;
-      CKL();
-      RC(mixed_prepare(ctx, m, phi));
-      RC(reset_max(ctx, 2));
-      return launch_defect(ctx, m, phi, rhs, ctx->d_max + 2);
-    }));
-    RC(read_max(ctx, 2, &r));
-    if (residuals) residuals[n] = r;
-    n++;
-    if (r < threshold) break;
-  }
-  RC(run_graph(ctx, gkey("mixed_finish", mg_id), [&]() -> int { return mixed_finish(ctx, m, phi); }));
-  if (n_done) *n_done = n;
-  return r < threshold ? AFG_OK : AFG_ERR_NOCONV;
 }

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -30,7 +31,7 @@ namespace {
 
 constexpr int kMaxMg = 16;
 constexpr int kMaxCoarse = 4096;
-constexpr int kModeSlot = 8, kMaxSlots = 8 + 16;  // device maxima slots
+constexpr int kModeSlot = 8, kMaxSlots = kMaxSlotsDev;  // device maxima slots (per instance)
 constexpr int kMaxBranch = 8;                      // side streams
 
 struct DevBuf {
@@ -47,7 +48,9 @@ struct MgSlot {
   double* d_x = nullptr;
   double* d_b2r = nullptr;       // [n][2D]
   unsigned char* d_bmask = nullptr;
-  double* d_bcval = nullptr;     // [6]
+  // boundary values per instance row (one row for a single tree), then a
+  // row of zeros (homogeneous): [(rows + 1)][6]
+  double* d_bcval = nullptr;
   // coefficient tables (MgCoef): per box, and per radial index if cylindrical
   double* d_cb64 = nullptr;
   float* d_cb32 = nullptr;
@@ -95,8 +98,22 @@ struct afg_ctx {
   int n_all = 0;            // boxes in all level lists
   int n_all_leaves = 0;
   unsigned char* d_is_leaf = nullptr;
-  int* d_cslot = nullptr;   // coarse unknown -> slot
+  int* d_cslot = nullptr;   // coarse unknown -> slot (instance-major on batched trees)
   int* d_ccell = nullptr;   // coarse unknown -> cell index
+  // Batched independent instances (afg_tree_sync_batched); n_inst = 0 for a
+  // single tree.  The coarse grids of all instances are alike (nloc
+  // unknowns each) and share one inverse.
+  int n_inst = 0;
+  std::vector<int> h_inst;              // [n_boxes] instance of each slot
+  std::vector<int> inst_hl;             // highest level per instance
+  std::vector<double> inst_min_dr;      // finest dr per instance
+  std::vector<std::vector<long long>> inst_cells;  // [instance][level] cells
+  int* d_inst = nullptr;
+  int* d_frozen = nullptr;       // flags the kernels read
+  int* d_frozen_base = nullptr;  // instances whose solve has converged
+  int* d_inst_hl = nullptr;
+  int* h_frozen = nullptr;       // pinned staging of the flags
+  int max_rows = 1;              // instance rows of d_max / h_max
   // pools
   int n_var = 0, n_var_face = 0;
   std::vector<double*> cc;  // [n_var]
@@ -204,8 +221,13 @@ static KTree ktree(const afg_ctx* c) {
   t.geo = c->d_geo;
   t.idr = c->d_idr;
   t.idrf = c->d_idrf;
+  t.inst = c->n_inst > 0 ? c->d_inst : nullptr;
+  t.frozen = c->n_inst > 0 ? c->d_frozen : nullptr;
   return t;
 }
+
+// instance rows of the per-instance tables (1 for a single tree)
+static int inst_rows(const afg_ctx* c) { return c->n_inst > 0 ? c->n_inst : 1; }
 
 template <typename T>
 static MgCoef<T> coef_of(const MgSlot& m);
@@ -255,6 +277,14 @@ static void free_tree(afg_ctx* c) {
   dfree(c->d_parent); dfree(c->d_children); dfree(c->d_nbr); dfree(c->d_pnb); dfree(c->d_nbmat);
   dfree(c->d_ix); dfree(c->d_rmin); dfree(c->d_dr); dfree(c->d_idr); dfree(c->d_idrf); dfree(c->d_lists); dfree(c->d_rec); dfree(c->d_is_leaf); dfree(c->d_geo);
   dfree(c->d_cslot); dfree(c->d_ccell);
+  dfree(c->d_inst); dfree(c->d_frozen); dfree(c->d_frozen_base); dfree(c->d_inst_hl);
+  if (c->h_frozen) cudaFreeHost(c->h_frozen);
+  c->h_frozen = nullptr;
+  c->n_inst = 0;
+  c->h_inst.clear();
+  c->inst_hl.clear();
+  c->inst_min_dr.clear();
+  c->inst_cells.clear();
   for (auto& p : c->cc) dfree(p);
   for (auto& p : c->fc) dfree(p);
   c->cc.clear();
@@ -455,7 +485,7 @@ static int launch_init_phi_rhs(afg_ctx* ctx, const int* list, int n, T* phi, T* 
 template <typename T>
 static int launch_copy(afg_ctx* ctx, const int* list, int n, const T* src, T* dst) {
   if (n <= 0) return AFG_OK;
-  k_copy<T><<<n, 256, 0, ctx->stream>>>(ctx->S, list, src, dst);
+  k_copy<T><<<n, 256, 0, ctx->stream>>>(ktree(ctx), list, src, dst);
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -534,13 +564,16 @@ struct MgVars {
   void* tmp;
 };
 
-static GcDev mg_gc(const afg_mg_desc& d, bool homogeneous) {
+// Ghost-cell method of a multigrid slot's phi; on batched trees the boundary
+// values are read per instance from the slot's device rows.
+static GcDev mg_gc(const afg_ctx* ctx, const MgSlot& m, bool homogeneous) {
   GcDev g;
   for (int n = 0; n < 6; n++) {
-    g.bc_type[n] = d.bc_type[n];
-    g.bc_val[n] = homogeneous ? 0.0 : d.bc_val[n];
+    g.bc_type[n] = m.d.bc_type[n];
+    g.bc_val[n] = homogeneous ? 0.0 : m.d.bc_val[n];
   }
   g.rb = AFG_RB_MG_SIDES;
+  g.ival = ctx->n_inst > 0 && !homogeneous ? m.d_bcval : nullptr;
   return g;
 }
 
@@ -613,21 +646,35 @@ static int mg_correct(afg_ctx* ctx, int lvl, T* phi, T* tmp, const GcDev& g, boo
 }
 
 // solve_coarse_grid, m_af_multigrid.f90:266-291 (exact FP64 solve)
+// (batched trees: every instance's coarse grid with the shared inverse and
+// its own boundary values)
 template <typename T>
 static int mg_coarse_solve(afg_ctx* ctx, MgSlot& m, T* phi, const T* rhs, const GcDev& g, bool homogeneous) {
-  const int n = m.n_coarse;
-  const double* bcv = m.d_bcval + (homogeneous ? 6 : 0);
-  k_coarse_gather<T><<<(n + 127) / 128, 128, 0, ctx->stream>>>(n, ctx->D, ctx->d_cslot, ctx->d_ccell, m.d_b2r,
-                                                               m.d_bmask, bcv, rhs, ctx->S, m.d_b);
+  const int nloc = m.n_coarse, rows = inst_rows(ctx), n = nloc * rows;
+  const double* bcv = m.d_bcval + (homogeneous ? 6 * rows : 0);
+  const int stride = homogeneous ? 0 : 6;
+  k_coarse_gather<T><<<(n + 127) / 128, 128, 0, ctx->stream>>>(n, nloc, ctx->D, ctx->d_cslot, ctx->d_ccell, m.d_b2r,
+                                                               m.d_bmask, bcv, stride, rhs, ctx->S, m.d_b);
   ctx->launches++;
   CKL();
-  k_coarse_matvec<<<(n + 7) / 8, 256, 0, ctx->stream>>>(n, m.d_ainv, m.d_b, m.d_x);
+  k_coarse_matvec<<<(n + 7) / 8, 256, 0, ctx->stream>>>(n, nloc, m.d_ainv, m.d_b, m.d_x);
   ctx->launches++;
   CKL();
-  k_coarse_scatter<T><<<(n + 127) / 128, 128, 0, ctx->stream>>>(n, ctx->d_cslot, ctx->d_ccell, m.d_x, phi, ctx->S);
+  k_coarse_scatter<T><<<(n + 127) / 128, 128, 0, ctx->stream>>>(ktree(ctx), n, ctx->d_cslot, ctx->d_ccell, m.d_x, phi);
   ctx->launches++;
   CKL();
   return mg_gc_lvl<T>(ctx, 1, phi, g, 1);
+}
+
+// Freeze flags seen by the kernels of a batched tree: converged instances
+// plus those whose highest level is outside [lo, hi] (no-op on one tree).
+static int inst_mask(afg_ctx* ctx, int lo, int hi) {
+  if (ctx->n_inst <= 0) return AFG_OK;
+  k_inst_mask<<<(ctx->n_inst + 127) / 128, 128, 0, ctx->stream>>>(ctx->n_inst, ctx->d_frozen_base, ctx->d_inst_hl, lo,
+                                                                  hi, ctx->d_frozen);
+  ctx->launches++;
+  CKL();
+  return AFG_OK;
 }
 
 template <typename T>
@@ -645,7 +692,7 @@ static int mg_residual_lvls(afg_ctx* ctx, const MgSlot& m, int max_lvl, const T*
 template <typename T>
 static int mg_vcycle(afg_ctx* ctx, MgSlot& m, int max_lvl, T* phi, T* rhs, T* tmp, bool set_residual,
                      bool homogeneous, unsigned long long* maxbits) {
-  const GcDev g = mg_gc(m.d, homogeneous);
+  const GcDev g = mg_gc(ctx, m, homogeneous);
   ctx->ctr[3]++;
   for (int lvl = max_lvl; lvl >= 2; lvl--) {
     // the restriction below computes the face neighbours it needs itself
@@ -670,7 +717,7 @@ static int mg_vcycle(afg_ctx* ctx, MgSlot& m, int max_lvl, T* phi, T* rhs, T* tm
 template <typename T>
 static int mg_fmg(afg_ctx* ctx, MgSlot& m, T* phi, T* rhs, T* tmp, bool set_residual, bool have_guess,
                   unsigned long long* maxbits, bool homogeneous = false) {
-  const GcDev g = mg_gc(m.d, homogeneous);
+  const GcDev g = mg_gc(ctx, m, homogeneous);
   const int H = ctx->highest_lvl;
   if (have_guess) {
     for (int lvl = H; lvl >= 2; lvl--) RC(mg_set_coarse_phi_rhs<T>(ctx, m, lvl, phi, rhs, tmp, g));
@@ -679,28 +726,78 @@ static int mg_fmg(afg_ctx* ctx, MgSlot& m, T* phi, T* rhs, T* tmp, bool set_resi
       RC(launch_init_phi_rhs<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs));
   }
   RC(launch_copy<T>(ctx, lst(ctx, ctx->off_ids[0]), (int)ctx->lvl_ids[0].size(), phi, tmp));
-  RC(mg_vcycle<T>(ctx, m, 1, phi, rhs, tmp, set_residual && H == 1, homogeneous, maxbits));
-  for (int lvl = 2; lvl <= H; lvl++) {
-    RC(launch_copy<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, tmp));
-    RC(mg_correct<T>(ctx, lvl, phi, tmp, g, !ctx->fused_gsrb));
-    RC(mg_vcycle<T>(ctx, m, lvl, phi, rhs, tmp, set_residual && lvl == H, homogeneous, maxbits));
+  if (ctx->n_inst <= 0) {
+    RC(mg_vcycle<T>(ctx, m, 1, phi, rhs, tmp, set_residual && H == 1, homogeneous, maxbits));
+    for (int lvl = 2; lvl <= H; lvl++) {
+      RC(launch_copy<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, tmp));
+      RC(mg_correct<T>(ctx, lvl, phi, tmp, g, !ctx->fused_gsrb));
+      RC(mg_vcycle<T>(ctx, m, lvl, phi, rhs, tmp, set_residual && lvl == H, homogeneous, maxbits));
+    }
+    return AFG_OK;
   }
-  return AFG_OK;
+  // Batched instances of different depths: the V-cycle at level lvl runs on
+  // the instances that have that level (an instance's FMG ends at its own
+  // highest level), and the residual of an instance is taken after its last
+  // V-cycle; then the flags return to the converged set.
+  for (int lvl = 1; lvl <= H; lvl++) {
+    RC(inst_mask(ctx, lvl, INT_MAX));
+    if (lvl > 1) {
+      RC(launch_copy<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, tmp));
+      RC(mg_correct<T>(ctx, lvl, phi, tmp, g, !ctx->fused_gsrb));
+    }
+    RC(mg_vcycle<T>(ctx, m, lvl, phi, rhs, tmp, false, homogeneous, maxbits));
+    if (set_residual) {
+      RC(inst_mask(ctx, lvl, lvl));
+      RC(mg_residual_lvls<T>(ctx, m, lvl, phi, rhs, tmp, maxbits));
+    }
+  }
+  return inst_mask(ctx, 0, INT_MAX);
 }
 
-static int read_max(afg_ctx* ctx, int slot, double* out) {
-  CK(cudaMemcpyAsync(ctx->h_max + slot, ctx->d_max + slot, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                     ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  unsigned long long b = ctx->h_max[slot];
+// Slots of the device maxima: 0 right-hand side / max-norm, 1 V-cycle and
+// FMG residual, 2 defect, 3-4 transport limits, 5 chemistry limit, from
+// kModeSlot per Helmholtz mode.  On batched trees the residual-type slots
+// hold one word per instance (row q at d_max + q * kMaxSlots); the
+// transport limits stay global (row 0).
+static bool inst_slot(const afg_ctx* ctx, int slot) { return ctx->n_inst > 0 && (slot < 3 || slot > 5); }
+
+static double bits_to_double(unsigned long long b) {
   double v;
   memcpy(&v, &b, sizeof(double));
-  *out = v;
+  return v;
+}
+
+// value of slot for instance q after read_max (batched trees)
+static double inst_value(const afg_ctx* ctx, int slot, int q) {
+  return bits_to_double(ctx->h_max[(size_t)q * kMaxSlots + slot]);
+}
+
+// the slot's maximum (over all instances of a batched tree)
+static int read_max(afg_ctx* ctx, int slot, double* out) {
+  if (!inst_slot(ctx, slot)) {
+    CK(cudaMemcpyAsync(ctx->h_max + slot, ctx->d_max + slot, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    *out = bits_to_double(ctx->h_max[slot]);
+    return AFG_OK;
+  }
+  const size_t pitch = kMaxSlots * sizeof(unsigned long long);
+  CK(cudaMemcpy2DAsync(ctx->h_max + slot, pitch, ctx->d_max + slot, pitch, sizeof(unsigned long long), ctx->n_inst,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  double mx = 0;
+  for (int q = 0; q < ctx->n_inst; q++) mx = std::max(mx, inst_value(ctx, slot, q));
+  *out = mx;
   return AFG_OK;
 }
 
 static int reset_max(afg_ctx* ctx, int slot) {
-  CK(cudaMemsetAsync(ctx->d_max + slot, 0, sizeof(unsigned long long), ctx->stream));
+  if (!inst_slot(ctx, slot)) {
+    CK(cudaMemsetAsync(ctx->d_max + slot, 0, sizeof(unsigned long long), ctx->stream));
+    return AFG_OK;
+  }
+  const size_t pitch = kMaxSlots * sizeof(unsigned long long);
+  CK(cudaMemset2DAsync(ctx->d_max + slot, pitch, 0, sizeof(unsigned long long), ctx->n_inst, ctx->stream));
   return AFG_OK;
 }
 
@@ -717,7 +814,7 @@ static int autotune_gsrb(afg_ctx* ctx, MgSlot& m) {
   const int n = (int)ctx->lvl_ids[best_l].size();
   if (n < 256) return AFG_OK;  // too small to time; the default stays
   const int* rec = rec_of(ctx, lst(ctx, ctx->off_ids[best_l]));
-  const GcDev g = mg_gc(m.d, true);
+  const GcDev g = mg_gc(ctx, m, true);
   const int cands3[] = {1, 2, 4, 8}, cands2[] = {1, 2, 4};
   const int* cands = ctx->D == 3 ? cands3 : cands2;
   const int nc = ctx->D == 3 ? 4 : 3;
@@ -755,6 +852,169 @@ static int autotune_gsrb(afg_ctx* ctx, MgSlot& m) {
 }
 
 #include "afg_mixed.cuh"
+
+/* ------------------------------------------------------------------------- */
+// Batched independent instances: per-instance convergence.  A solve loop
+// freezes the instances that have converged while the others continue
+// (kernels skip their boxes), so every instance ends exactly where a solve
+// of its own tree would; replayed graphs stay valid because the flags live
+// in device memory.
+
+// base freeze flags (converged instances) from the host, also as the flags
+// the kernels read; the pinned copy may change again after the next sync
+static int set_frozen(afg_ctx* ctx, const std::vector<char>& done) {
+  if (ctx->n_inst <= 0) return AFG_OK;
+  for (int q = 0; q < ctx->n_inst; q++) ctx->h_frozen[q] = done[q] ? 1 : 0;
+  CK(cudaMemcpyAsync(ctx->d_frozen_base, ctx->h_frozen, sizeof(int) * ctx->n_inst, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_frozen, ctx->d_frozen_base, sizeof(int) * ctx->n_inst, cudaMemcpyDeviceToDevice,
+                     ctx->stream));
+  return AFG_OK;
+}
+
+// smoother cell updates of one V-cycle of instance q (levels 2..its highest)
+static long long inst_vcycle_work(const afg_ctx* ctx, const MgSlot& m, int q) {
+  long long w = 0;
+  for (int l = 2; l <= ctx->inst_hl[q]; l++) w += ctx->inst_cells[q][l - 1];
+  return w * (m.d.n_cycle_down + m.d.n_cycle_up);
+}
+
+// ... of one FMG of instance q (a V-cycle up to each of its levels)
+static long long inst_fmg_work(const afg_ctx* ctx, const MgSlot& m, int q) {
+  long long w = 0;
+  for (int top = 2; top <= ctx->inst_hl[q]; top++)
+    for (int l = 2; l <= top; l++) w += ctx->inst_cells[q][l - 1];
+  return w * (m.d.n_cycle_down + m.d.n_cycle_up);
+}
+
+// The cell-update counter of a V-cycle or FMG launch sequence counts every
+// box of the levels it visits; on a batched tree remove the updates that
+// frozen instances, and instances past the end of their own FMG, skipped.
+static void inst_uncount(afg_ctx* ctx, const MgSlot& m, bool fmg) {
+  if (ctx->n_inst <= 0) return;
+  const int H = ctx->highest_lvl;
+  for (int q = 0; q < ctx->n_inst; q++) {
+    const long long V = inst_vcycle_work(ctx, m, q), extra = fmg ? (H - ctx->inst_hl[q]) * V : 0;
+    ctx->ctr[1] -= extra + (ctx->h_frozen[q] ? (fmg ? inst_fmg_work(ctx, m, q) : V) : 0);
+  }
+}
+
+// the launch sequences of one solve iteration (shared by the single-tree
+// and the batched loops, so both replay the same graphs)
+static int vcycle_graph(afg_ctx* ctx, MgSlot& m) {
+  const int mg_id = (int)(&m - ctx->mg);
+  double* phi = ctx->cc[m.d.i_phi - 1];
+  double* rhs = ctx->cc[m.d.i_rhs - 1];
+  double* tmp = ctx->cc[m.d.i_tmp - 1];
+  RC(run_graph(ctx, gkey("vcycle", mg_id, ctx->highest_lvl, 1), [&]() -> int {
+    RC(reset_max(ctx, 1));
+    return mg_vcycle<double>(ctx, m, ctx->highest_lvl, phi, rhs, tmp, true, false, ctx->d_max + 1);
+  }));
+  inst_uncount(ctx, m, false);
+  return AFG_OK;
+}
+
+static int mixed_defect_graph(afg_ctx* ctx, MgSlot& m) {
+  const int mg_id = (int)(&m - ctx->mg);
+  double* phi = ctx->cc[m.d.i_phi - 1];
+  double* rhs = ctx->cc[m.d.i_rhs - 1];
+  return run_graph(ctx, gkey("defect", mg_id), [&]() -> int {
+    RC(mixed_prepare(ctx, m, phi));
+    RC(reset_max(ctx, 2));
+    return launch_defect(ctx, m, phi, rhs, ctx->d_max + 2);
+  });
+}
+
+static int mixed_iter_graph(afg_ctx* ctx, MgSlot& m) {
+  const int mg_id = (int)(&m - ctx->mg);
+  double* phi = ctx->cc[m.d.i_phi - 1];
+  double* rhs = ctx->cc[m.d.i_rhs - 1];
+  RC(run_graph(ctx, gkey("mixed_iter", mg_id), [&]() -> int {
+    RC(mg_vcycle<float>(ctx, m, ctx->highest_lvl, m.e32, m.r32, m.t32, false, true, nullptr));
+    // leaves only: mixed_prepare restricts the parents from them
+    k_add_correction<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), lst(ctx, ctx->off_all_leaves), phi,
+                                                                m.e32);
+    ctx->launches++;
+    CKL();
+    RC(mixed_prepare(ctx, m, phi));
+    RC(reset_max(ctx, 2));
+    return launch_defect(ctx, m, phi, rhs, ctx->d_max + 2);
+  }));
+  inst_uncount(ctx, m, false);
+  return AFG_OK;
+}
+
+// afg_mg_solve of a mixed-precision slot on one tree: FP64 defect, then
+// iterations of FP32 V-cycle on the correction, update and new defect until
+// the defect is below the threshold; all ghost cells of phi at the end.
+static int mixed_solve(afg_ctx* ctx, MgSlot& m, double threshold, int max_cycles, int* n_done, double* residuals) {
+  double* phi = ctx->cc[m.d.i_phi - 1];
+  double r = 0;
+  int n = 0;
+  const int mg_id = (int)(&m - ctx->mg);
+  RC(mixed_defect_graph(ctx, m));
+  RC(read_max(ctx, 2, &r));
+  while (n < max_cycles) {
+    RC(mixed_iter_graph(ctx, m));
+    RC(read_max(ctx, 2, &r));
+    if (residuals) residuals[n] = r;
+    n++;
+    if (r < threshold) break;
+  }
+  RC(run_graph(ctx, gkey("mixed_finish", mg_id), [&]() -> int { return mixed_finish(ctx, m, phi); }));
+  if (n_done) *n_done = n;
+  return r < threshold ? AFG_OK : AFG_ERR_NOCONV;
+}
+
+// Solve loop of a batched tree: per instance until its residual is below
+// thr[q] (at most max_cycles iterations); n_done[q] iterations and the last
+// residual res[q] per instance (either may be null).
+static int mg_solve_inst(afg_ctx* ctx, MgSlot& m, const double* thr, int max_cycles, int* n_done, double* res) {
+  const int Q = ctx->n_inst;
+  const bool mixed = m.d.precision == AFG_MIXED;
+  const int slot = mixed ? 2 : 1;
+  std::vector<char> done(Q, 0);
+  std::vector<int> cyc(Q, 0);
+  std::vector<double> r(Q, 0.0);
+  double mx;
+  RC(set_frozen(ctx, done));
+  if (mixed) {
+    // the defect of the current phi; as on one tree, at least one
+    // iteration follows
+    RC(mixed_defect_graph(ctx, m));
+    RC(read_max(ctx, 2, &mx));
+    for (int q = 0; q < Q; q++) r[q] = inst_value(ctx, 2, q);
+  }
+  auto all_done = [&]() {
+    for (int q = 0; q < Q; q++)
+      if (!done[q]) return false;
+    return true;
+  };
+  for (int it = 0; it < max_cycles && !all_done(); it++) {
+    RC(set_frozen(ctx, done));
+    RC(mixed ? mixed_iter_graph(ctx, m) : vcycle_graph(ctx, m));
+    RC(read_max(ctx, slot, &mx));
+    for (int q = 0; q < Q; q++) {
+      if (done[q]) continue;
+      r[q] = inst_value(ctx, slot, q);
+      cyc[q]++;
+      done[q] = r[q] < thr[q];
+    }
+  }
+  const bool ok = all_done();
+  std::fill(done.begin(), done.end(), 0);
+  RC(set_frozen(ctx, done));
+  if (mixed) {
+    const int mg_id = (int)(&m - ctx->mg);
+    double* phi = ctx->cc[m.d.i_phi - 1];
+    RC(run_graph(ctx, gkey("mixed_finish", mg_id), [&]() -> int { return mixed_finish(ctx, m, phi); }));
+  }
+  for (int q = 0; q < Q; q++) {
+    if (n_done) n_done[q] = cyc[q];
+    if (res) res[q] = r[q];
+  }
+  return ok ? AFG_OK : AFG_ERR_NOCONV;
+}
 
 /* ========================================================================= */
 extern "C" {
@@ -822,7 +1082,13 @@ int afg_sync(afg_ctx* ctx) {
 }
 
 int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_var_face) {
+  return afg_tree_sync_batched(ctx, t, n_var_cell, n_var_face, 0, nullptr);
+}
+
+int afg_tree_sync_batched(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_var_face, int n_inst,
+                          const int* box_inst) {
   if (!ctx || !t) return AFG_ERR_ARG;
+  if (n_inst < 0 || (n_inst > 0 && !box_inst)) return fail(ctx, AFG_ERR_ARG, "bad instance table");
   if (t->ndim != 2 && t->ndim != 3) return fail(ctx, AFG_ERR_ARG, "ndim must be 2 or 3");
   if (t->n_cell < 2 || (t->n_cell & 1) || t->n_cell > 64) return fail(ctx, AFG_ERR_ARG, "bad n_cell %d", t->n_cell);
   if (t->coord == AFG_CYL && t->ndim != 2) return fail(ctx, AFG_ERR_ARG, "cylindrical needs ndim=2");
@@ -878,6 +1144,28 @@ int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_va
     }
   ctx->h_ix.assign(t->ix, t->ix + (size_t)n * D);
   ctx->h_nbr.assign(t->neighbors, t->neighbors + (size_t)n * nnb);
+  // independent instances: every relation of a box stays inside its instance
+  if (n_inst > 0) {
+    ctx->h_inst.assign(box_inst, box_inst + n);
+    for (int b = 0; b < n; b++) {
+      const int q = box_inst[b];
+      if (q < 0 || q >= n_inst) return fail(ctx, AFG_ERR_ARG, "box %d: instance %d out of range", b + 1, q);
+      if (parent[b] >= 0 && box_inst[parent[b]] != q) return fail(ctx, AFG_ERR_ARG, "box %d: parent in another instance", b + 1);
+      for (int c = 0; c < nch; c++) {
+        const int v = children[(size_t)b * nch + c];
+        if (v >= 0 && box_inst[v] != q) return fail(ctx, AFG_ERR_ARG, "box %d: child in another instance", b + 1);
+      }
+      for (int k = 0; k < nnb; k++) {
+        const int v = nbr[(size_t)b * nnb + k];
+        if (v >= 0 && box_inst[v] != q) return fail(ctx, AFG_ERR_ARG, "box %d: neighbour in another instance", b + 1);
+      }
+      for (int k = 0; k < nm; k++) {
+        const int v = nbmat[(size_t)b * nm + k];
+        if (v >= 0 && box_inst[v] != q) return fail(ctx, AFG_ERR_ARG, "box %d: neighbor_mat in another instance", b + 1);
+      }
+    }
+  }
+  const int rows = n_inst > 0 ? n_inst : 1;
   // level lists
   ctx->lvl_ids.assign(t->highest_lvl, {});
   ctx->lvl_leaves.assign(t->highest_lvl, {});
@@ -946,11 +1234,16 @@ int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_va
     lists.insert(lists.end(), ctx->lvl_leaves[l].begin(), ctx->lvl_leaves[l].end());
     ctx->n_all_leaves += (int)ctx->lvl_leaves[l].size();
   }
-  // coarse grid map (level 1)
-  const long ncoarse = (long)ctx->cgs[0] * ctx->cgs[1] * ctx->cgs[2];
+  // coarse grid map (level 1); a batched tree stacks the instances' coarse
+  // grids (instance-major), which must be alike: same boxes at the same
+  // places with the same geometry
+  const long nloc = (long)ctx->cgs[0] * ctx->cgs[1] * ctx->cgs[2];
+  const long ncoarse = nloc * rows;
   std::vector<int> cslot(ncoarse, -1), ccell(ncoarse, 0);
-  if (ncoarse <= kMaxCoarse) {
+  if (nloc <= kMaxCoarse) {
+    std::vector<int> first(nloc, -1);  // instance-0 box of each coarse cell
     for (int s : ctx->lvl_ids[0]) {
+      const long q = n_inst > 0 ? box_inst[s] : 0;
       const int kn = D == 3 ? nc : 1;
       for (int k = 1; k <= kn; k++)
         for (int j = 1; j <= nc; j++)
@@ -960,11 +1253,22 @@ int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_va
             long K = D == 3 ? (long)(t->ix[(size_t)s * D + 2] - 1) * nc + (k - 1) : 0;
             if (I >= ctx->cgs[0] || J >= ctx->cgs[1] || K >= ctx->cgs[2])
               return fail(ctx, AFG_ERR_ARG, "level-1 box outside coarse_grid_size");
-            long g = I + ctx->cgs[0] * (J + (long)ctx->cgs[1] * K);
+            const long gl = I + ctx->cgs[0] * (J + (long)ctx->cgs[1] * K), g = q * nloc + gl;
+            if (cslot[g] >= 0) return fail(ctx, AFG_ERR_ARG, "level-1 boxes overlap");
             cslot[g] = s;
             ccell[g] = i + ctx->n2 * (j + ctx->n2 * (D == 3 ? k : 0));
+            if (q == 0) first[gl] = s;
           }
     }
+    if (n_inst > 0)
+      for (long g = 0; g < ncoarse; g++) {
+        const int s = cslot[g], s0 = first[g % nloc];
+        if (s < 0 || s0 < 0) continue;
+        for (int d = 0; d < D; d++)
+          if (t->dr[(size_t)s * D + d] != t->dr[(size_t)s0 * D + d] ||
+              t->r_min[(size_t)s * D + d] != t->r_min[(size_t)s0 * D + d])
+            return fail(ctx, AFG_ERR_UNSUPPORTED, "instances need alike coarse grids (box %d)", s + 1);
+      }
     for (long g = 0; g < ncoarse; g++)
       if (cslot[g] < 0) return fail(ctx, AFG_ERR_ARG, "coarse grid not covered by level-1 boxes");
   }
@@ -1022,6 +1326,46 @@ int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, int n_va
   CK(cudaMemcpy(ctx->d_is_leaf, is_leaf.data(), n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_cslot, cslot.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_ccell, ccell.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
+  // per-instance tables: depth, finest dr (af_min_dr), cells per level
+  ctx->inst_hl.assign(rows, 0);
+  ctx->inst_min_dr.assign(rows, 0.0);
+  ctx->inst_cells.assign(rows, std::vector<long long>(t->highest_lvl, 0));
+  const long long cells_box = D == 2 ? (long long)nc * nc : (long long)nc * nc * nc;
+  for (int l = 0; l < t->highest_lvl; l++)
+    for (int s : ctx->lvl_ids[l]) {
+      const int q = n_inst > 0 ? box_inst[s] : 0;
+      ctx->inst_cells[q][l] += cells_box;
+      if (l + 1 > ctx->inst_hl[q]) {
+        ctx->inst_hl[q] = l + 1;
+        double mdr = t->dr[(size_t)s * D];
+        for (int d = 1; d < D; d++) mdr = std::min(mdr, t->dr[(size_t)s * D + d]);
+        ctx->inst_min_dr[q] = mdr;
+      }
+    }
+  for (int q = 0; q < rows; q++)
+    if (ctx->inst_hl[q] == 0) return fail(ctx, AFG_ERR_ARG, "instance %d has no boxes", q);
+  if (rows > ctx->max_rows) {
+    dfree(ctx->d_max);
+    cudaFreeHost(ctx->h_max);
+    ctx->h_max = nullptr;
+    CK(dalloc(&ctx->d_max, (size_t)rows * kMaxSlots));
+    CK(cudaMallocHost((void**)&ctx->h_max, (size_t)rows * kMaxSlots * sizeof(unsigned long long)));
+    ctx->max_rows = rows;
+  }
+  CK(cudaMemset(ctx->d_max, 0, (size_t)ctx->max_rows * kMaxSlots * sizeof(unsigned long long)));
+  if (n_inst > 0) {
+    CK(dalloc(&ctx->d_inst, n));
+    CK(dalloc(&ctx->d_frozen, n_inst));
+    CK(dalloc(&ctx->d_frozen_base, n_inst));
+    CK(dalloc(&ctx->d_inst_hl, n_inst));
+    CK(cudaMallocHost((void**)&ctx->h_frozen, sizeof(int) * n_inst));
+    memset(ctx->h_frozen, 0, sizeof(int) * n_inst);
+    CK(cudaMemcpy(ctx->d_inst, box_inst, sizeof(int) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemset(ctx->d_frozen, 0, sizeof(int) * n_inst));
+    CK(cudaMemset(ctx->d_frozen_base, 0, sizeof(int) * n_inst));
+    CK(cudaMemcpy(ctx->d_inst_hl, ctx->inst_hl.data(), sizeof(int) * n_inst, cudaMemcpyHostToDevice));
+    ctx->n_inst = n_inst;
+  }
   // cylindrical geometry table
   if (ctx->coord == AFG_CYL) {
     CK(dalloc(&ctx->d_geo, (size_t)n * nc * 4));
@@ -1378,6 +1722,8 @@ static int build_coarse(afg_ctx* ctx, MgSlot& m) {
   std::vector<unsigned char> mask(n, 0);
   std::vector<double> dr(D), rmin(D);
   for (int s : ctx->lvl_ids[0]) {
+    // batched trees: the coarse grids are alike; the first one defines it
+    if (ctx->n_inst > 0 && ctx->h_inst[s] != 0) continue;
     // per-box coefficients, mg_box_lpl_stencil
     double h[3], c[7];
     std::vector<double> hdr((size_t)D), hrm((size_t)D);
@@ -1473,21 +1819,20 @@ static int build_coarse(afg_ctx* ctx, MgSlot& m) {
     }
   }
   m.n_coarse = (int)n;
+  const int rows = inst_rows(ctx);
   CK(dalloc(&m.d_ainv, (size_t)n * n));
-  CK(dalloc(&m.d_b, n));
-  CK(dalloc(&m.d_x, n));
+  CK(dalloc(&m.d_b, (size_t)n * rows));
+  CK(dalloc(&m.d_x, (size_t)n * rows));
   CK(dalloc(&m.d_b2r, (size_t)n * 2 * D));
   CK(dalloc(&m.d_bmask, n));
-  CK(dalloc(&m.d_bcval, 12));
+  CK(dalloc(&m.d_bcval, (size_t)(rows + 1) * 6));
   CK(cudaMemcpy(m.d_ainv, Inv.data(), sizeof(double) * n * n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(m.d_b2r, b2r.data(), sizeof(double) * b2r.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(m.d_bmask, mask.data(), n, cudaMemcpyHostToDevice));
-  double bcv[12];
-  for (int q = 0; q < 6; q++) {
-    bcv[q] = m.d.bc_val[q];
-    bcv[6 + q] = 0.0;
-  }
-  CK(cudaMemcpy(m.d_bcval, bcv, sizeof(bcv), cudaMemcpyHostToDevice));
+  std::vector<double> bcv((size_t)(rows + 1) * 6, 0.0);
+  for (int r = 0; r < rows; r++)
+    for (int q = 0; q < 6; q++) bcv[(size_t)r * 6 + q] = m.d.bc_val[q];
+  CK(cudaMemcpy(m.d_bcval, bcv.data(), sizeof(double) * bcv.size(), cudaMemcpyHostToDevice));
   return AFG_OK;
 }
 
@@ -1549,7 +1894,7 @@ int afg_mg_setup(afg_ctx* ctx, int mg_id, const afg_mg_desc* d) {
   }
   m.used = true;
   // mg_init: phi gets the multigrid ghost-cell methods
-  GcDev g = mg_gc(m.d, false);
+  GcDev g = mg_gc(ctx, m, false);
   ctx->methods[d->i_phi - 1] = g;
   ctx->has_method[d->i_phi - 1] = true;
   return AFG_OK;
@@ -1564,14 +1909,24 @@ int afg_mg_set_bc_values(afg_ctx* ctx, int mg_id, const double* v) {
   if (same) return AFG_OK;
   clear_graphs(ctx);  // boundary values are kernel parameters of captured graphs
   for (int q = 0; q < 6; q++) m->d.bc_val[q] = v[q];
-  double bcv[12];
-  for (int q = 0; q < 6; q++) {
-    bcv[q] = v[q];
-    bcv[6 + q] = 0.0;
-  }
-  CK(cudaMemcpyAsync(m->d_bcval, bcv, sizeof(bcv), cudaMemcpyHostToDevice, ctx->stream));
+  const int rows = inst_rows(ctx);
+  std::vector<double> bcv((size_t)rows * 6);
+  for (int r = 0; r < rows; r++)
+    for (int q = 0; q < 6; q++) bcv[(size_t)r * 6 + q] = v[q];
+  CK(cudaMemcpyAsync(m->d_bcval, bcv.data(), sizeof(double) * bcv.size(), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  ctx->methods[m->d.i_phi - 1] = mg_gc(m->d, false);
+  ctx->methods[m->d.i_phi - 1] = mg_gc(ctx, *m, false);
+  return AFG_OK;
+}
+
+int afg_mg_set_bc_values_inst(afg_ctx* ctx, int mg_id, const double* v) {
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  if (!v) return AFG_ERR_ARG;
+  if (ctx->n_inst <= 0) return afg_mg_set_bc_values(ctx, mg_id, v);
+  // read by the kernels from device memory: captured graphs stay valid
+  CK(cudaMemcpyAsync(m->d_bcval, v, sizeof(double) * 6 * ctx->n_inst, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   return AFG_OK;
 }
 
@@ -1586,7 +1941,7 @@ int afg_mg_gsrb_lvl(afg_ctx* ctx, int mg_id, int lvl, int type) {
   if (lvl < 1 || lvl > ctx->highest_lvl) return fail(ctx, AFG_ERR_ARG, "bad level");
   MG_VARS(m);
   (void)tmp;
-  return mg_gsrb_boxes<double>(ctx, *m, lvl, type, phi, rhs, mg_gc(m->d, false));
+  return mg_gsrb_boxes<double>(ctx, *m, lvl, type, phi, rhs, mg_gc(ctx, *m, false));
 }
 
 int afg_mg_update_coarse(afg_ctx* ctx, int mg_id, int lvl) {
@@ -1594,7 +1949,7 @@ int afg_mg_update_coarse(afg_ctx* ctx, int mg_id, int lvl) {
   RC(get_mg(ctx, mg_id, &m));
   if (lvl < 2 || lvl > ctx->highest_lvl) return fail(ctx, AFG_ERR_ARG, "bad level");
   MG_VARS(m);
-  const GcDev g = mg_gc(m->d, false);
+  const GcDev g = mg_gc(ctx, *m, false);
   RC(mg_update_coarse<double>(ctx, *m, lvl, phi, rhs, tmp, g, false));
   // the reference fills the whole coarser level, leaves included
   return mg_gc_lvl<double>(ctx, lvl - 1, phi, g, 1);
@@ -1606,7 +1961,7 @@ int afg_mg_correct_lvl(afg_ctx* ctx, int mg_id, int lvl) {
   if (lvl < 2 || lvl > ctx->highest_lvl) return fail(ctx, AFG_ERR_ARG, "bad level");
   MG_VARS(m);
   (void)rhs;
-  return mg_correct<double>(ctx, lvl, phi, tmp, mg_gc(m->d, false));
+  return mg_correct<double>(ctx, lvl, phi, tmp, mg_gc(ctx, *m, false));
 }
 
 int afg_mg_coarse_solve(afg_ctx* ctx, int mg_id) {
@@ -1614,7 +1969,7 @@ int afg_mg_coarse_solve(afg_ctx* ctx, int mg_id) {
   RC(get_mg(ctx, mg_id, &m));
   MG_VARS(m);
   (void)tmp;
-  return mg_coarse_solve<double>(ctx, *m, phi, rhs, mg_gc(m->d, false), false);
+  return mg_coarse_solve<double>(ctx, *m, phi, rhs, mg_gc(ctx, *m, false), false);
 }
 
 int afg_mg_residual(afg_ctx* ctx, int mg_id, int max_lvl) {
@@ -1634,6 +1989,7 @@ int afg_mg_vcycle(afg_ctx* ctx, int mg_id, int set_residual, int max_lvl, double
     RC(reset_max(ctx, 1));
     return mg_vcycle<double>(ctx, *m, ml, phi, rhs, tmp, set_residual != 0, false, ctx->d_max + 1);
   }));
+  inst_uncount(ctx, *m, false);
   if (set_residual && max_res) return read_max(ctx, 1, max_res);
   return AFG_OK;
 }
@@ -1648,6 +2004,7 @@ int afg_mg_fmg(afg_ctx* ctx, int mg_id, int set_residual, int have_guess, double
       return mixed_fmg(ctx, *m, phi, rhs, set_residual != 0, have_guess != 0, ctx->d_max + 1);
     return mg_fmg<double>(ctx, *m, phi, rhs, tmp, set_residual != 0, have_guess != 0, ctx->d_max + 1);
   }));
+  inst_uncount(ctx, *m, true);
   if (set_residual && max_res) return read_max(ctx, 1, max_res);
   return AFG_OK;
 }
@@ -1656,15 +2013,23 @@ int afg_mg_solve(afg_ctx* ctx, int mg_id, double threshold, int max_cycles, int*
   MgSlot* m;
   RC(get_mg(ctx, mg_id, &m));
   if (max_cycles < 1) return fail(ctx, AFG_ERR_ARG, "max_cycles < 1");
+  if (ctx->n_inst > 0) {
+    // the same threshold for every instance; the most iterations and the
+    // largest final residual are reported
+    std::vector<double> thr(ctx->n_inst, threshold), res(ctx->n_inst);
+    std::vector<int> nd(ctx->n_inst);
+    const int rc = mg_solve_inst(ctx, *m, thr.data(), max_cycles, nd.data(), res.data());
+    if (rc != AFG_OK && rc != AFG_ERR_NOCONV) return rc;
+    const int n = *std::max_element(nd.begin(), nd.end());
+    if (n_done) *n_done = n;
+    if (residuals && n > 0) residuals[n - 1] = *std::max_element(res.begin(), res.end());
+    return rc;
+  }
   if (m->d.precision == AFG_MIXED) return mixed_solve(ctx, *m, threshold, max_cycles, n_done, residuals);
-  MG_VARS(m);
   int n = 0;
   double r = 0;
   for (n = 0; n < max_cycles;) {
-    RC(run_graph(ctx, gkey("vcycle", mg_id, ctx->highest_lvl, 1), [&]() -> int {
-      RC(reset_max(ctx, 1));
-      return mg_vcycle<double>(ctx, *m, ctx->highest_lvl, phi, rhs, tmp, true, false, ctx->d_max + 1);
-    }));
+    RC(vcycle_graph(ctx, *m));
     RC(read_max(ctx, 1, &r));
     if (residuals) residuals[n] = r;
     n++;
@@ -1677,6 +2042,17 @@ int afg_mg_solve(afg_ctx* ctx, int mg_id, double threshold, int max_cycles, int*
 }  // extern "C"
 
 extern "C" {
+
+int afg_mg_solve_inst(afg_ctx* ctx, int mg_id, const double* threshold, int max_cycles, int* n_done,
+                      double* residual) {
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  if (ctx->n_inst <= 0) return fail(ctx, AFG_ERR_STATE, "not a batched tree");
+  if (max_cycles < 1 || !threshold) return fail(ctx, AFG_ERR_ARG, "bad solve arguments");
+  return mg_solve_inst(ctx, *m, threshold, max_cycles, n_done, residual);
+}
+
+int afg_n_instances(const afg_ctx* ctx) { return ctx ? ctx->n_inst : 0; }
 
 int afg_tree_copy_cc(afg_ctx* ctx, int iv_from, int iv_to) {
   RC(check_var(ctx, iv_from));

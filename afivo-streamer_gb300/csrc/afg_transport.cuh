@@ -124,6 +124,7 @@ template <int D, bool CYL, int NC = 0>
 __global__ void __launch_bounds__(256) k_restrict_geom(KTree t0, const int* __restrict__ list, double* __restrict__ v) {
   const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
+  if (box_frozen(t, slot)) return;
   const int pslot = t.parent[slot];
   const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
   const double* c = v + (size_t)slot * t.S;
@@ -199,7 +200,7 @@ __device__ __forceinline__ double gc2_value(const KTree& t, const double* __rest
     if (D == 3 && nb == 3) c2 = c0;  // as in the reference's 3D high-y branch
     const int xi = layer == 0 ? (low ? 1 : nc) : (low ? 2 : nc - 1);
     const double cc0 = layer == 0 ? c0 : c2;
-    return cc0 * gc_val(g, nb) + c1 * a[face_at<D>(n2, d, xi, p, q)];
+    return cc0 * gc_val(g, nb, t, slot) + c1 * a[face_at<D>(n2, d, xi, p, q)];
   }
   // refinement boundary: limited prolongation from the parent's neighbour
   const int cs = t.pnb[slot * 2 * D + nb];

@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(256) k_field_rhs_interior(KTree t0, const int*
   // max |rhs| over the leaves (af_tree_maxabs_cc), fused
   if (maxbits != nullptr) {
     mx = block_max<double>(mx, sred);
-    if (threadIdx.x == 0) atomic_max_nonneg(maxbits, mx);
+    if (threadIdx.x == 0) atomic_max_nonneg(inst_max(t, maxbits, slot), mx);
   }
 }
 

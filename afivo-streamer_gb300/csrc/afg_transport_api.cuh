@@ -477,11 +477,101 @@ int afg_field_from_potential(afg_ctx* ctx, int i_phi) {
   });
 }
 
+int afg_field_compute_inst(afg_ctx* ctx, int mg_id, int s_in, int have_guess, const double* voltage,
+                           double domain_len, double max_rel_residual, int num_vcycles, int* n_cycles,
+                           double* residual) {
+  RC(need_transport(ctx));
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  if (ctx->n_inst <= 0) return fail(ctx, AFG_ERR_STATE, "not a batched tree");
+  if (!voltage) return fail(ctx, AFG_ERR_ARG, "voltage per instance needed");
+  const int Q = ctx->n_inst;
+  double mx;
+  if (mixed_transport(ctx)) {
+    RC(reset_max(ctx, 0));
+    RC(field_set_rhs(ctx, m->d.i_rhs, s_in, ctx->d_max));
+    RC(read_max(ctx, 0, &mx));
+  } else {
+    RC(field_set_rhs(ctx, m->d.i_rhs, s_in, nullptr));
+    RC(afg_maxabs(ctx, m->d.i_rhs, 1, &mx));
+  }
+  // field_bc_homogeneous per instance, and the threshold of each instance
+  // (the rule of the single-tree path with its own rhs maximum, voltage and
+  // finest dr)
+  std::vector<double> bcv((size_t)Q * 6), thr(Q), r(Q, 0.0);
+  std::vector<int> cyc(Q, 0);
+  for (int q = 0; q < Q; q++) {
+    for (int k = 0; k < 6; k++) bcv[(size_t)q * 6 + k] = m->d.bc_val[k];
+    bcv[(size_t)q * 6 + 2 * ctx->D - 1] = voltage[q];
+    const double max_rhs = inst_value(ctx, 0, q);
+    thr[q] = std::max(std::max(1e-6, max_rhs * max_rel_residual),
+                      1e-10 * std::fabs(voltage[q]) / (domain_len * ctx->inst_min_dr[q]));
+  }
+  RC(afg_mg_set_bc_values_inst(ctx, mg_id, bcv.data()));
+  if (!have_guess) {
+    const bool fp32_fmg = m->d.precision == AFG_MIXED;
+    std::vector<char> done(Q, 0);
+    std::vector<std::vector<double>> hist(Q);
+    bool all = false;
+    for (int i = 0; i < 100 && !all; i++) {
+      RC(set_frozen(ctx, done));
+      RC(afg_mg_fmg(ctx, mg_id, 1, 1, &mx));
+      all = true;
+      for (int q = 0; q < Q; q++) {
+        if (done[q]) continue;
+        const double v = inst_value(ctx, 1, q);
+        hist[q].push_back(v);
+        cyc[q]++;
+        r[q] = v;
+        if (v < thr[q]) {
+          done[q] = 1;
+        } else if (hist[q].size() >= 3) {
+          const size_t k = hist[q].size();
+          const double mn = std::min(v, std::min(hist[q][k - 2], hist[q][k - 3]));
+          const double mxh = std::max(v, std::max(hist[q][k - 2], hist[q][k - 3]));
+          const double ratio = mn / mxh;
+          if (ratio < 2.0 && ratio > 0.5 && (v < 1e8 || fp32_fmg)) done[q] = 1;
+        }
+        all = all && done[q];
+      }
+    }
+    std::fill(done.begin(), done.end(), 0);
+    RC(set_frozen(ctx, done));
+    if (!all) return fail(ctx, AFG_ERR_NOCONV, "no convergence in initial field computation");
+  }
+  if (num_vcycles > 0) {
+    std::vector<int> nv(Q);
+    std::vector<double> rv(Q);
+    const int rc = mg_solve_inst(ctx, *m, thr.data(), std::min(num_vcycles, 256), nv.data(), rv.data());
+    if (rc != AFG_OK && rc != AFG_ERR_NOCONV) return rc;
+    for (int q = 0; q < Q; q++) {
+      cyc[q] += nv[q];
+      if (nv[q] > 0) r[q] = rv[q];
+    }
+  }
+  RC(afg_field_from_potential(ctx, m->d.i_phi));
+  for (int q = 0; q < Q; q++) {
+    if (n_cycles) n_cycles[q] = cyc[q];
+    if (residual) residual[q] = r[q];
+  }
+  return AFG_OK;
+}
+
 int afg_field_compute(afg_ctx* ctx, int mg_id, int s_in, int have_guess, double voltage, double domain_len,
                       double max_rel_residual, int num_vcycles, int* n_cycles, double* residual) {
   RC(need_transport(ctx));
   MgSlot* m;
   RC(get_mg(ctx, mg_id, &m));
+  if (ctx->n_inst > 0) {
+    // one voltage for all instances; the most cycles and largest residual
+    std::vector<double> v(ctx->n_inst, voltage), res(ctx->n_inst);
+    std::vector<int> nc(ctx->n_inst);
+    RC(afg_field_compute_inst(ctx, mg_id, s_in, have_guess, v.data(), domain_len, max_rel_residual, num_vcycles,
+                              nc.data(), res.data()));
+    if (n_cycles) *n_cycles = *std::max_element(nc.begin(), nc.end());
+    if (residual) *residual = *std::max_element(res.begin(), res.end());
+    return AFG_OK;
+  }
   double max_rhs;
   if (mixed_transport(ctx)) {
     RC(reset_max(ctx, 0));
@@ -548,6 +638,7 @@ int afg_photoi_helmh(afg_ctx* ctx, double coeff, int n_modes, const int* mg_ids,
   RC(need_transport(ctx));
   const afg_transport_desc& d = ctx->tr.d;
   if (n_modes < 1 || !mg_ids || !coeffs || d.i_photo <= 0) return fail(ctx, AFG_ERR_ARG, "bad photoionization args");
+  if (ctx->n_inst > 0) return fail(ctx, AFG_ERR_UNSUPPORTED, "photoionization of batched instances");
   MgSlot* m0;
   RC(get_mg(ctx, mg_ids[0], &m0));
   const int i_rhs = m0->d.i_rhs;

@@ -214,17 +214,53 @@ def baseline_eta(E):
     return np.full_like(np.asarray(E, dtype=np.float64), 2e3)
 
 
+_THIRD, _SIXTH = 1 / 3.0, 1 / 6.0
+
+# The explicit integrators of af_advance (afivo/src/m_af_advance.f90:150-199)
+# as their forward_euler stages: (dt factor, s_deriv, s_prev, w_prev, s_out).
+# The IMEX schemes need an implicit solver and are not on this path.
+INTEGRATORS = {
+    "forward_euler": [(1.0, 0, [0], [1.0], 0)],
+    "midpoint": [(0.5, 0, [0], [1.0], 1), (1.0, 1, [0], [1.0], 0)],
+    "heun": [(1.0, 0, [0], [1.0], 1), (0.5, 1, [0, 1], [0.5, 0.5], 0)],
+    "ssprk33": [(1.0, 0, [0], [1.0], 1), (0.25, 1, [0, 1], [0.75, 0.25], 2),
+                (2 * _THIRD, 2, [0, 2], [_THIRD, 2 * _THIRD], 0)],
+    "ssprk43": [(0.5, 0, [0], [1.0], 1), (0.5, 1, [1], [1.0], 2),
+                (_SIXTH, 2, [0, 2], [2 * _THIRD, _THIRD], 3), (0.5, 3, [3], [1.0], 0)],
+    "rk4": [(0.5, 0, [0], [1.0], 1), (0.5, 1, [0], [1.0], 2), (1.0, 2, [0], [1.0], 3),
+            (_SIXTH, 3, [0, 1, 2, 3], [-_THIRD, _THIRD, 2 * _THIRD, _THIRD], 0)],
+}
+
+
+def states_needed(integrator):
+    """Copies of every density: one per integrator step plus the backup copy
+    of copy_current_state (src/streamer.f90:659-671)."""
+    return len(INTEGRATORS[integrator]) + 1
+
+
 class StreamerRun:
     """Time stepping of the hot path through the C-ABI, mirroring the
     reference's time loop (src/streamer.f90:181-432): photoionization every
     `photoi_per_steps` steps (photoi_set_src, 242-248), copy_current_state
-    (659-671), af_advance with Heun's method (afivo/src/m_af_advance.f90:
-    160-164) whose stages are forward_euler (src/m_fluid.f90:21-99), and
-    field_compute for the new state (327).  Step rejection is not needed at a
-    fixed dt below the limits and is left to the caller."""
+    (659-671), af_advance (afivo/src/m_af_advance.f90:121-214) whose stages
+    are forward_euler (src/m_fluid.f90:21-99: field of the stage's input
+    state from the second stage on, fluxes, densities), and field_compute for
+    the new state (327).  Step rejection is not needed at a fixed dt below
+    the limits and is left to the caller.
+
+    On a batched context (a forest of independent instances) `voltage` is
+    an array with one applied voltage per instance; the field solves then
+    converge per instance (afg_field_compute_inst) and last["vcycles_inst"]
+    counts each instance's cycles."""
 
     def __init__(self, ctx, tree, model, voltage, dt, precision=ag.FP64, max_rel_residual=1e-8,
-                 num_vcycles=30, photoi=None, photoi_per_steps=5):
+                 num_vcycles=30, photoi=None, photoi_per_steps=5, integrator="heun"):
+        if model.n_states < states_needed(integrator):
+            raise ValueError(f"{integrator} needs {states_needed(integrator)} copies of each density")
+        self.stages = INTEGRATORS[integrator]
+        self.batched = np.ndim(voltage) == 1
+        if self.batched and photoi is not None:
+            raise ValueError("photoionization of batched instances is not supported")
         self.ctx, self.tree, self.m = ctx, tree, model
         self.voltage, self.dt = voltage, dt
         self.precision = precision
@@ -246,7 +282,8 @@ class StreamerRun:
                 ctx.set_cc_methods(m.species_iv[s] + st, [m.bc_species] * (2 * D), None, ag.RB_INTERP_LIM)
         if m.i_photo:
             ctx.set_cc_methods(m.i_photo, *m.photo_gc())
-        ctx.mg_setup(0, m.field_mg(self.voltage, self.precision))
+        v0 = float(self.voltage[0]) if self.batched else self.voltage
+        ctx.mg_setup(0, m.field_mg(v0, self.precision))
         self.mode_ids = []
         if self.photoi is not None:
             lam, coeffs, _ = self.photoi
@@ -255,6 +292,12 @@ class StreamerRun:
                 self.mode_ids.append(1 + n)
 
     def field(self, s_in, have_guess):
+        if self.batched:
+            n, r = self.ctx.field_compute_inst(0, s_in, have_guess, self.voltage, self.L, self.rel,
+                                               self.num_vcycles)
+            self.last["vcycles_inst"] = self.last.get("vcycles_inst", 0) + n
+            self.last["vcycles"] = self.last.get("vcycles", 0) + int(n.max())
+            return int(n.max()), float(r.max())
         n, r = self.ctx.field_compute(0, s_in, have_guess, self.voltage, self.L, self.rel, self.num_vcycles)
         self.last.setdefault("vcycles", 0)
         self.last["vcycles"] += n
@@ -276,16 +319,18 @@ class StreamerRun:
         # copy_current_state: densities to the backup copy
         for s in range(len(m.species)):
             ctx.tree_copy_cc(m.species_iv[s], m.species_iv[s] + m.n_states - 1)
-        # Heun stage 1: forward_euler(dt, s_deriv=0, s_prev=[0], w=[1], s_out=1)
-        lim1 = ctx.flux_upwind(0)
-        ctx.update_densities(dt, 0, [0], [1.0], 1, last_step=False)
-        # stage 2: field for state 1, then forward_euler(dt/2, 1, [0,1], [.5,.5], 0)
-        self.field(1, True)
-        lim2 = ctx.flux_upwind(1)
-        chem = ctx.update_densities(0.5 * dt, 1, [0, 1], [0.5, 0.5], 0, last_step=True)
+        cfl = drt = 1e100
+        chem = 0.0
+        for i, (f, s_deriv, s_prev, w_prev, s_out) in enumerate(self.stages, 1):
+            if i > 1:
+                self.field(s_deriv, True)
+            lim = ctx.flux_upwind(s_deriv)
+            cfl, drt = min(cfl, lim[0]), min(drt, lim[1])
+            chem = ctx.update_densities(f * dt, s_deriv, s_prev, w_prev, s_out,
+                                        last_step=(i == len(self.stages)))
         if after_update is not None:
             after_update()
         # field of the new state
         n, r = self.field(0, True)
-        self.last.update(cfl=min(lim1[0], lim2[0]), drt=min(lim1[1], lim2[1]), chem=chem, residual=r)
+        self.last.update(cfl=cfl, drt=drt, chem=chem, residual=r)
         self.it += 1

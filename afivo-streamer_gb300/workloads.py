@@ -1,8 +1,17 @@
 """Synthetic streamer workloads (seeded), the inputs of the benchmark.
 
-Two configurations of the hot path are defined here; no public dataset is
+Four configurations of the hot path are defined here; no public dataset is
 involved (each configuration defines its own inputs):
 
+* ``cart2d`` -- the plain method in FP64: 2D Cartesian 1 cm x 1 cm, uniform
+  256x256 grid of 16^2-cell boxes with the multigrid hierarchy coarsened to
+  one box (5 levels, 341 boxes); electrons plus equal positive ions as a
+  Gaussian seed 1e15 exp(-r^2/(2 (0.5 mm)^2)) m^-3 at (0.5 cm, 0.8 cm) on a
+  1e9 m^-3 background; phi = 0 at y = 0, -3e4 V at y = 1 cm, Neumann sides;
+  mobility 0.03 m^2/Vs, diffusion 0.1 m^2/s, ionization
+  alpha(E) = 4.3e5 exp(-2e7/|E|), immobile ions, no photoionization;
+  forward Euler at dt = 1e-12 s with one Poisson solve to 1e-10 relative
+  residual per step.
 * ``cyl2d`` -- 2D axisymmetric streamer, r in [0, 1 cm], z in [0, 2 cm],
   16^2-cell boxes, coarse grid 16x32, uniform to level 5 plus 4 AMR levels
   around the streamer channel (~0.56 M leaf cells, 9 levels); electrons,
@@ -18,6 +27,9 @@ involved (each configuration defines its own inputs):
   c2 = B*1e21/N, c3 = 0, c4 = 1 (src/m_chemistry.f90:117-118,751-752);
   transport as cyl2d; 3-term Helmholtz photoionization; applied field
   1.5e6 V/m.
+
+* ``batch`` -- 256 independent 2D axisymmetric Poisson + transport
+  instances of uneven size (BatchCyl2d), run as one forest.
 
 The refinement maps stand in for afivo's refinement criterion
 (alpha(E)*dx > 0.8 around a developed streamer, src/m_refine.f90:239-245):
@@ -52,9 +64,20 @@ class Workload:
     name = ""
     voltage = 0.0
     dt = 5e-12
+    integrator = "heun"
+    max_rel_residual = 1e-8
+    use_photoi = True
+    noise = 1e-3                                           # relative electron noise
+    amplitude = 1e15                                       # seed peak density (1/m^3)
     photoi_lambda = np.array([50.0, 150.0, 500.0])        # 1/m
     photoi_coeffs = np.array([1e-2, 5e-2, 1e-1]) * 1e4     # 1/m^2
     photoi_eta_quench = 0.05 * 0.038
+
+    def run_kwargs(self):
+        """Keyword arguments of StreamerRun / OracleStreamerRun."""
+        return dict(max_rel_residual=self.max_rel_residual, num_vcycles=30, integrator=self.integrator,
+                    photoi=((self.photoi_lambda, self.photoi_coeffs, self.photoi_eta_quench)
+                            if self.use_photoi else None))
 
     def tree(self, reduced=False, coarsen=0):
         raise NotImplementedError
@@ -64,6 +87,17 @@ class Workload:
 
     def seed_center(self):
         raise NotImplementedError
+
+    def initial_host_state(self, tree, model, seed=12345):
+        """Potential and species densities (state 0) on every box: host array
+        [n_boxes, 1 + n_species, (nc+2)^D] in the reference's per-box layout,
+        and the variable indices of its columns."""
+        ivs = [model.i_phi] + list(model.species_iv)
+        n2 = tree.n_cell + 2
+        H = np.empty((tree.n_boxes, len(ivs)) + (n2,) * tree.ndim)
+        for v, iv in enumerate(ivs):
+            self.fill_variable(tree, model, iv, seed=seed, out=H[:, v])
+        return H, ivs
 
     def fill_variable(self, tree, model, iv, seed=12345, out=None, chunk=8192):
         """Initial value of cell-centred variable iv (1-based) on all boxes,
@@ -95,12 +129,35 @@ class Workload:
                 o[...] = 0.0
                 continue
             r2 = sum((X[d] - c[d]) ** 2 for d in range(D))
-            g = 1e15 * np.exp(-r2 / (2 * sig ** 2)) + 1e9
-            if s == 0:
+            g = self.amplitude * np.exp(-r2 / (2 * sig ** 2)) + 1e9
+            if s == 0 and self.noise:
                 rng = np.random.default_rng([seed, c0 // chunk])
-                g = g * (1 + 1e-3 * rng.standard_normal(g.shape))
+                g = g * (1 + self.noise * rng.standard_normal(g.shape))
             o[...] = g
         return out
+
+
+class Cart2d(Workload):
+    name = "cart2d"
+    voltage = -3e4
+    dt = 1e-12
+    integrator = "forward_euler"
+    max_rel_residual = 1e-10
+    use_photoi = False
+    noise = 0.0
+    seed_sigma = 0.5e-3
+    positive_species = 1
+
+    def tree(self, reduced=False, coarsen=0):
+        return at.build_tree(2, 16, [16, 16], [1e-2, 1e-2], max_lvl=5 - coarsen)
+
+    def model(self):
+        return sm.StreamerModel(2, n_states=sm.states_needed(self.integrator),
+                                species=[sm.Species("e", -1.0), sm.Species("M+", 1.0)],
+                                alpha=sm.baseline_alpha)
+
+    def seed_center(self):
+        return (0.5e-2, 0.8e-2)
 
 
 class Cyl2d(Workload):
@@ -164,4 +221,73 @@ class Streamer3d(Workload):
         return (1.5e-2, 1.5e-2, 1.7e-2)
 
 
-WORKLOADS = {"cyl2d": Cyl2d, "3d": Streamer3d}
+class CylInstance(Workload):
+    """One instance of the batched configuration: 2D axisymmetric,
+    r in [0, 1 cm], z in [0, 1 cm], uniform grid of `side`^2 cells in 16^2
+    boxes (coarse grid one box, log2(side/16)+1 levels), the cyl2d transport
+    and chemistry without photoionization."""
+    name = "cyl-instance"
+    seed_sigma = 0.5e-3
+    positive_species = 1
+    use_photoi = False
+
+    def __init__(self, side, voltage, amplitude):
+        self.side, self.voltage, self.amplitude = int(side), float(voltage), float(amplitude)
+
+    def tree(self, reduced=False, coarsen=0):
+        levels = int(np.log2(self.side // 16)) + 1
+        return at.build_tree(2, 16, [16, 16], [1e-2, 1e-2], coord=ag.AFG_CYL, max_lvl=levels)
+
+    def model(self):
+        return sm.StreamerModel(2, alpha=sm.baseline_alpha, eta=sm.baseline_eta)
+
+    def seed_center(self):
+        return (0.0, 0.8e-2)
+
+
+class BatchCyl2d:
+    """Batched uneven instances: n_inst independent 2D axisymmetric
+    Poisson + transport instances; grid sides drawn uniformly from
+    {64, 128, 256, 512}, applied voltages uniformly from 15-35 kV over 1 cm
+    (negative, as the other workloads), seed amplitudes log-uniform in
+    [1e13, 1e16] m^-3, all from one seed (expected 22.3 M leaf cells for 256
+    instances)."""
+    name = "batch"
+    dt = 5e-12
+    integrator = "heun"
+    max_rel_residual = 1e-8
+    domain_len = 1e-2
+
+    def __init__(self, n_inst=256, seed=2024, sides=(64, 128, 256, 512)):
+        rng = np.random.default_rng(seed)
+        self.sides = rng.choice(np.asarray(sides), size=n_inst)
+        self.voltages = -rng.uniform(15e3, 35e3, size=n_inst)
+        self.amplitudes = 10 ** rng.uniform(13, 16, size=n_inst)
+        self.instances = [CylInstance(s, v, a) for s, v, a in zip(self.sides, self.voltages, self.amplitudes)]
+
+    def model(self):
+        return self.instances[0].model()
+
+    def run_kwargs(self):
+        return dict(max_rel_residual=self.max_rel_residual, num_vcycles=30, integrator=self.integrator, photoi=None)
+
+    def trees(self):
+        return [w.tree() for w in self.instances]
+
+    def forest(self, trees=None):
+        """(forest tree, instance of each box, instance trees)"""
+        trees = trees if trees is not None else self.trees()
+        f, box_inst = at.forest(trees)
+        return f, box_inst, trees
+
+    def initial_host_state(self, trees, model):
+        """Per-instance initial states stacked in forest box order (as
+        Workload.initial_host_state)."""
+        parts, ivs = [], None
+        for q, (w, t) in enumerate(zip(self.instances, trees)):
+            H, ivs = w.initial_host_state(t, model, seed=12345 + q)
+            parts.append(H)
+        return np.concatenate(parts), ivs
+
+
+WORKLOADS = {"cart2d": Cart2d, "cyl2d": Cyl2d, "3d": Streamer3d}

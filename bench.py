@@ -14,6 +14,8 @@ Workloads (seeded synthetic inputs, afivo-streamer_gb300/workloads.py):
   applied field 1.5e6 V/m, dt = 5e-12 s.
 * ``cyl2d``: 2D axisymmetric streamer, 16^2-cell boxes, 9 levels,
   2,918 boxes, ~0.56 M leaf cells; 3 species with tabulated rates.
+* ``cart2d``: the plain 2D Cartesian method on a uniform 256^2 grid (341
+  boxes of 16^2 cells), forward Euler, Poisson to 1e-10 relative residual.
 
 Metric: cell-updates/s = (smoother cell-updates of every V-cycle + leaf cells
 x species per transport stage) / time.  `value` is the mixed-precision path
@@ -52,6 +54,11 @@ CONFIG_TEXT = {
           "8 k13 reactions, 3 Helmholtz photoionization modes, Heun dt=5e-12 s, Poisson to 1e-8 rel.",
     "cyl2d": "2D axisymmetric streamer, 16^2 boxes, 9 levels, 2918 boxes (~0.56 M leaf cells), 3 species, "
              "3 Helmholtz photoionization modes, Heun dt=5e-12 s, Poisson to 1e-8 rel.",
+    "cart2d": "2D Cartesian 1 cm^2, uniform 256^2 grid of 16^2 boxes, 5 levels, 341 boxes, electrons + ions, "
+              "alpha(E) ionization, forward Euler dt=1e-12 s, Poisson to 1e-10 rel.",
+    "batch": "256 independent 2D axisymmetric Poisson + transport instances (1 cm^2, 16^2 boxes, uniform "
+             "grids with sides drawn from {64,128,256,512}, voltages 15-35 kV, seed amplitudes 1e13-1e16), "
+             "one forest in one context, 3 species, Heun dt=5e-12 s, Poisson to 1e-8 rel. per instance",
 }
 # DRAM traffic of a kernel class relative to its algorithmic bytes, from one
 # ncu capture (dram__bytes.sum.per_second x gpu__time_duration.sum) of the
@@ -114,14 +121,7 @@ def work_of(c0, c1):
 
 
 def initial_host_state(w, tree, model):
-    """Potential and species densities (state 0) on every box: host array
-    [n_boxes, 1 + n_species, (nc+2)^D] in the reference's per-box layout."""
-    ivs = [model.i_phi] + list(model.species_iv)
-    n2 = tree.n_cell + 2
-    H = np.empty((tree.n_boxes, len(ivs)) + (n2,) * tree.ndim)
-    for v, iv in enumerate(ivs):
-        w.fill_variable(tree, model, iv, out=H[:, v])
-    return H, ivs
+    return w.initial_host_state(tree, model)
 
 
 def cuda_profiler(on):
@@ -134,19 +134,57 @@ def cuda_profiler(on):
         raise RuntimeError(f"cudaProfiler{'Start' if on else 'Stop'} failed: {rc}")
 
 
-def run_gpu_arm(args, device, w):
+def problem(args, w):
+    """(tree, model, host state, its variables, voltage(s), box instances,
+    instance trees) of a workload; the batched workload is a forest."""
+    if isinstance(w, workloads.BatchCyl2d):
+        tree, box_inst, trees = w.forest()
+        model = w.model()
+        H, ivs = w.initial_host_state(trees, model)
+        return tree, model, H, ivs, w.voltages, box_inst, trees
     tree = w.tree(coarsen=args.coarsen)
     model = w.model()
     H, ivs = initial_host_state(w, tree, model)
-    photoi = (w.photoi_lambda, w.photoi_coeffs, w.photoi_eta_quench)
+    return tree, model, H, ivs, w.voltage, None, None
+
+
+def run_one_at_a_time(args, device, w, trees, model, H, ivs):
+    """The batched workload's instances advanced one after another, each in
+    its own context (mixed precision, the same steps and L2 flushes as the
+    forest); returns cell-updates/s over the summed step times."""
+    offs = np.cumsum([0] + [t.n_boxes for t in trees])
+    t_ms, work = 0.0, 0
+    for q, t in enumerate(trees):
+        ctx = ag.Context(device)
+        ctx.tree_sync(t, model.n_var_cell, model.n_var_face)
+        ctx.upload_vars(H[offs[q]:offs[q + 1]], ivs)
+        run = sm.StreamerRun(ctx, t, model, float(w.voltages[q]), w.dt, precision=ag.MIXED, **w.run_kwargs())
+        run.setup()
+        run.initial_field()
+        for _ in range(args.warmup):
+            run.step()
+        c0 = ctx.counters()
+        for _ in range(args.steps):
+            ctx.flush_l2(256 << 20)
+            ctx.event_record(0)
+            run.step()
+            ctx.event_record(1)
+            t_ms += ctx.event_elapsed(0, 1)
+        work += work_of(c0, ctx.counters())
+        ctx.close()
+    return dict(value=work / (t_ms * 1e-3), ms_per_step=t_ms / args.steps, work_per_step=work / args.steps,
+                instances=len(trees))
+
+
+def run_gpu_arm(args, device, w):
+    tree, model, H, ivs, voltage, box_inst, trees = problem(args, w)
     ctx = ag.Context(device)
     results = {}
     arms = (("mixed", ag.MIXED),) if args.profile else (("fp64", ag.FP64), ("mixed", ag.MIXED))
     for prec_name, prec in arms:
-        ctx.tree_sync(tree, model.n_var_cell, model.n_var_face)     # zeroed pools
+        ctx.tree_sync(tree, model.n_var_cell, model.n_var_face, box_inst=box_inst)     # zeroed pools
         ctx.upload_vars(H, ivs)
-        run = sm.StreamerRun(ctx, tree, model, w.voltage, w.dt, precision=prec, max_rel_residual=1e-8,
-                             num_vcycles=30, photoi=photoi)
+        run = sm.StreamerRun(ctx, tree, model, voltage, w.dt, precision=prec, **w.run_kwargs())
         run.setup()
         run.initial_field()
         for _ in range(args.warmup):
@@ -196,6 +234,9 @@ def run_gpu_arm(args, device, w):
         n, ms, by = ctx.kernel_stats()
         kstats[name] = dict(launches=n, ms=ms, bytes=by)
     ctx.kernel_timing(ag.KT_NONE)
+    # the batched workload's instances one at a time, from the same initial
+    # state (before the end-to-end run below overwrites the host state)
+    one = run_one_at_a_time(args, device, w, trees, model, H, ivs) if trees is not None else None
     # end to end through the C-ABI: page-locked host state in, densities and |E| out
     species_ivs = list(model.species_iv)
     cols = list(range(1, 1 + len(species_ivs)))
@@ -236,6 +277,8 @@ def run_gpu_arm(args, device, w):
                transfer_path="zero-copy kernels on host boxes page-locked by afg_host_register; the species "
                              "download overlaps the step's final field solve (afg_cc_download_async)")
     ctx.close()
+    if one is not None:
+        e2e["one_at_a_time"] = one
     return tree, results, kstats, e2e, tuning
 
 
@@ -248,6 +291,8 @@ def run_cpu(name, steps, warmup=1, time_limit=None):
     from oracle_streamer import OracleStreamerRun
     cores = os.cpu_count() or 1
     oracle.set_num_threads(cores)
+    if name == "batch":
+        return run_cpu_batch(steps, warmup, time_limit, cores)
     w = workloads.WORKLOADS[name]()
     reduced = name == "3d"
     tree = w.tree(reduced=reduced)
@@ -258,8 +303,7 @@ def run_cpu(name, steps, warmup=1, time_limit=None):
     for v, iv in enumerate(ivs):
         cc[:, iv - 1] = H[:, v]
     del H
-    run = OracleStreamerRun(tree, model, w.voltage, w.dt, max_rel_residual=1e-8, num_vcycles=30,
-                            photoi=(w.photoi_lambda, w.photoi_coeffs, w.photoi_eta_quench))
+    run = OracleStreamerRun(tree, model, w.voltage, w.dt, **w.run_kwargs())
     run.setup()
     run.initial_field(cc, fc)
     for _ in range(warmup):
@@ -279,6 +323,40 @@ def run_cpu(name, steps, warmup=1, time_limit=None):
     return work / dt, cores, dt / done, done, sample
 
 
+def run_cpu_batch(steps, warmup, time_limit, cores):
+    """The batched workload on the CPU restatement: instances one after
+    another (as the reference runs them), `steps` steps each, until the time
+    bound is spent."""
+    from oracle_streamer import OracleStreamerRun
+    b = workloads.BatchCyl2d()
+    model = b.model()
+    work, t_run, done_inst, done_steps = 0, 0.0, 0, 0
+    t_all = time.perf_counter()
+    for q, w in enumerate(b.instances):
+        tree = w.tree()
+        H, ivs = w.initial_host_state(tree, model, seed=12345 + q)
+        cc = ag.new_cc(tree, model.n_var_cell)
+        fc = ag.new_fc(tree, model.n_var_face)
+        for v, iv in enumerate(ivs):
+            cc[:, iv - 1] = H[:, v]
+        run = OracleStreamerRun(tree, model, w.voltage, b.dt, **b.run_kwargs())
+        run.setup()
+        run.initial_field(cc, fc)
+        for _ in range(warmup):
+            run.step(cc, fc)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            work += run.step(cc, fc)
+            done_steps += 1
+        t_run += time.perf_counter() - t0
+        done_inst += 1
+        if time_limit is not None and time.perf_counter() - t_all > time_limit:
+            break
+    sample = (f"the first {done_inst} of {len(b.instances)} batched instances, one after another, {steps} step(s) "
+              f"each after {warmup} warm-up step(s), on the CPU restatement (C++/OpenMP, {cores} threads)")
+    return work / t_run, cores, t_run / max(1, done_steps), done_steps, sample
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -294,7 +372,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="3d", choices=sorted(workloads.WORKLOADS))
+    ap.add_argument("--config", default="3d", choices=sorted(workloads.WORKLOADS) + ["batch"])
     ap.add_argument("--cpu-steps", type=int, default=10, help="CPU baseline sample steps (0 = skip)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU baseline time bound")
     ap.add_argument("--coarsen", type=int, default=0,
@@ -325,8 +403,9 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    w = workloads.WORKLOADS[args.config]()
+    w = workloads.BatchCyl2d() if args.config == "batch" else workloads.WORKLOADS[args.config]()
     tree, results, kstats, e2e, tuning = run_gpu_arm(args, local, w)
+    one = e2e.pop("one_at_a_time", None) if e2e else None
     if args.profile:
         if rank == 0:
             print(json.dumps({"profile": True, "config": config, "mixed": results["mixed"][0]}))
@@ -369,6 +448,7 @@ def main():
                          "algorithmic_bytes_per_launch": ks["bytes"] / max(1, ks["launches"]),
                          "avg_launch_us": 1e3 * ks["ms"] / max(1, ks["launches"])},
             "kernel_classes": kstats, "tuning": tuning,
+            **({"one_at_a_time": dict(one, speedup_batched=value / one["value"])} if one else {}),
             "cpu_baseline": cpu, "e2e": e2e, "clocks": mixed["clocks"],
             "gpu_launches": int(mixed["launches"]),
         }))

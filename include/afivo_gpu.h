@@ -133,6 +133,25 @@ const char* afg_last_error(const afg_ctx* ctx);
 int afg_tree_sync(afg_ctx* ctx, const afg_tree_desc* tree,
                   int n_var_cell, int n_var_face);
 
+/* Batched independent instances (no counterpart in the reference, which runs
+ * one tree per process): `tree` is a forest of n_inst trees with disjoint box
+ * ids, box_inst[id-1] in 0..n_inst-1 the instance of box id.  No parent,
+ * child or neighbour relation may cross instances, and the coarse grids
+ * (level 1) must be alike: the same coarse_grid_size, with boxes at the same
+ * ix with the same r_min and dr (the instances share one factored
+ * coarse-grid operator; uneven grids differ in their number of levels).
+ * Every level is then processed in one launch per stage for all instances.
+ * Boundary values of a multigrid slot can differ per instance
+ * (afg_mg_set_bc_values_inst); afg_field_compute_inst and afg_mg_solve_inst
+ * converge each instance to its own threshold, freezing converged instances,
+ * so each instance's result is the same as a run of its own tree.
+ * Photoionization of batched instances is not supported. */
+int afg_tree_sync_batched(afg_ctx* ctx, const afg_tree_desc* tree,
+                          int n_var_cell, int n_var_face, int n_inst,
+                          const int* box_inst);
+/* number of instances of a batched tree (0 for a single tree) */
+int afg_n_instances(const afg_ctx* ctx);
+
 /* Copy cell-centred variable iv between host boxes and the device pool.
  * box_cc[id-1] points at box%cc(0,0[,0],1) of box id (NULL = skip); the data
  * of variable iv starts elem_offset doubles after it ((iv-1)*(nc+2)^ndim for
@@ -211,6 +230,8 @@ int afg_mg_setup(afg_ctx* ctx, int mg_id, const afg_mg_desc* mg);
 /* Change only the boundary values of slot mg_id (e.g. a new applied voltage,
  * field_set_voltage src/m_field.f90:551-586); kinds must stay the same. */
 int afg_mg_set_bc_values(afg_ctx* ctx, int mg_id, const double* bc_val);
+/* Batched trees: boundary values per instance, bc_val[q*6 + face]. */
+int afg_mg_set_bc_values_inst(afg_ctx* ctx, int mg_id, const double* bc_val);
 
 /* mg_fas_vcycle (185-264).  max_lvl <= 0 means tree%highest_lvl.  When
  * set_residual != 0 the residual is stored in i_tmp and, if max_res is not
@@ -233,6 +254,12 @@ int afg_mg_fmg(afg_ctx* ctx, int mg_id, int set_residual, int have_guess,
  * residual are returned; residuals[] (may be NULL) receives the history. */
 int afg_mg_solve(afg_ctx* ctx, int mg_id, double threshold, int max_cycles,
                  int* n_done, double* residuals);
+/* Batched trees: per instance until its residual < threshold[q];
+ * n_done[q] iterations and residual[q] (either may be NULL).  On a batched
+ * tree afg_mg_solve applies one threshold to all instances and reports the
+ * most iterations (residuals[n_done-1] = the largest final residual). */
+int afg_mg_solve_inst(afg_ctx* ctx, int mg_id, const double* threshold,
+                      int max_cycles, int* n_done, double* residual);
 
 /* Single stages, for parity testing of each kernel against the oracle:
  * gsrb_boxes (648-687), update_coarse (691-738), correct_children (624-646)
@@ -367,6 +394,15 @@ int afg_field_from_potential(afg_ctx* ctx, int i_phi);
 int afg_field_compute(afg_ctx* ctx, int mg_id, int s_in, int have_guess,
                       double voltage, double domain_len, double max_rel_residual,
                       int num_vcycles, int* n_cycles, double* residual);
+/* Batched trees: field_compute of every instance with its own voltage[q]
+ * (boundary value and threshold, with the instance's own max|rhs| and
+ * finest dr); n_cycles[q] FMG + V-cycles and residual[q] per instance.  On
+ * a batched tree afg_field_compute uses one voltage for all instances and
+ * reports the most cycles and the largest residual. */
+int afg_field_compute_inst(afg_ctx* ctx, int mg_id, int s_in, int have_guess,
+                           const double* voltage, double domain_len,
+                           double max_rel_residual, int num_vcycles,
+                           int* n_cycles, double* residual);
 
 /* photoionization_rate_from_alpha (src/m_photoi.f90:259-291) into i_rhs on
  * leaves (coeff = eta * quenching factor), then photoi_helmh_compute

@@ -11,10 +11,11 @@ restatement (``oracle.Oracle``) in the order of the reference's time loop
   mode FMG cycles until the residual drops below 1e-2 of the source maximum,
   and i_photo -= c_n * mode_n on the leaves;
 * copy_current_state (src/streamer.f90:659-671);
-* Heun's method (afivo/src/m_af_advance.f90:160-164) whose stages are
-  forward_euler (src/m_fluid.f90:21-99): fluxes of state s_deriv, densities
-  of the stage, and field_compute (src/m_field.f90:450-520) of the stage's
-  output state.
+* an explicit integrator of af_advance (afivo/src/m_af_advance.f90:150-199;
+  Heun's method by default) whose stages are forward_euler
+  (src/m_fluid.f90:21-99): field_compute (src/m_field.f90:450-520) of the
+  stage's input state from the second stage on, fluxes of that state and the
+  densities of the stage; then the field of the new state.
 
 `step()` returns the cell-updates of the step with the same accounting as the
 GPU counters: smoother updates of every V-cycle ((n_cycle_down + n_cycle_up)
@@ -35,9 +36,28 @@ import afivo_gpu as ag  # noqa: E402
 import oracle  # noqa: E402
 
 
+_THIRD, _SIXTH = 1 / 3.0, 1 / 6.0
+
+# forward_euler calls of af_advance's explicit integrators
+# (afivo/src/m_af_advance.f90:150-199): (dt factor, s_deriv, s_prev, w_prev,
+# s_out) per stage
+STAGES = {
+    "forward_euler": [(1.0, 0, [0], [1.0], 0)],
+    "midpoint": [(0.5, 0, [0], [1.0], 1), (1.0, 1, [0], [1.0], 0)],
+    "heun": [(1.0, 0, [0], [1.0], 1), (0.5, 1, [0, 1], [0.5, 0.5], 0)],
+    "ssprk33": [(1.0, 0, [0], [1.0], 1), (0.25, 1, [0, 1], [0.75, 0.25], 2),
+                (2 * _THIRD, 2, [0, 2], [_THIRD, 2 * _THIRD], 0)],
+    "ssprk43": [(0.5, 0, [0], [1.0], 1), (0.5, 1, [1], [1.0], 2),
+                (_SIXTH, 2, [0, 2], [2 * _THIRD, _THIRD], 3), (0.5, 3, [3], [1.0], 0)],
+    "rk4": [(0.5, 0, [0], [1.0], 1), (0.5, 1, [0], [1.0], 2), (1.0, 2, [0], [1.0], 3),
+            (_SIXTH, 3, [0, 1, 2, 3], [-_THIRD, _THIRD, 2 * _THIRD, _THIRD], 0)],
+}
+
+
 class OracleStreamerRun:
     def __init__(self, tree, model, voltage, dt, max_rel_residual=1e-8, num_vcycles=30, photoi=None,
-                 photoi_per_steps=5):
+                 photoi_per_steps=5, integrator="heun"):
+        self.stages = STAGES[integrator]
         self.tree, self.m = tree, model
         self.voltage, self.dt = voltage, dt
         self.rel = max_rel_residual
@@ -135,13 +155,16 @@ class OracleStreamerRun:
             work += self.photoionization(cc)
         for s in range(len(m.species)):
             cc[:, m.species_iv[s] + m.n_states - 2] = cc[:, m.species_iv[s] - 1]
-        lim1 = o.flux_upwind(cc, fc, 0)
-        o.update_densities(cc, fc, dt, 0, [0], [1.0], 1)
-        work += self.field(cc, fc, 1, True)
-        lim2 = o.flux_upwind(cc, fc, 1)
-        chem = o.update_densities(cc, fc, 0.5 * dt, 1, [0, 1], [0.5, 0.5], 0, True)
+        cfl = drt = 1e100
+        chem = 0.0
+        for i, (f, s_deriv, s_prev, w_prev, s_out) in enumerate(self.stages, 1):
+            if i > 1:
+                work += self.field(cc, fc, s_deriv, True)
+            lim = o.flux_upwind(cc, fc, s_deriv)
+            cfl, drt = min(cfl, lim[0]), min(drt, lim[1])
+            chem = o.update_densities(cc, fc, f * dt, s_deriv, s_prev, w_prev, s_out, i == len(self.stages))
         work += self.field(cc, fc, 0, True)
-        work += 2 * self.ncell_leaf * len(m.species)
-        self.last.update(cfl=min(lim1[0], lim2[0]), drt=min(lim1[1], lim2[1]), chem=chem)
+        work += len(self.stages) * self.ncell_leaf * len(m.species)
+        self.last.update(cfl=cfl, drt=drt, chem=chem)
         self.it += 1
         return work

@@ -44,3 +44,26 @@ def test_tree_invariants(ndim):
 def test_uniform_counts():
     t = at.uniform_tree(2, 16, [16, 16], [1e-2, 1e-2], 5)
     assert t.n_boxes == 341 and t.n_cells(True) == 65536 and t.n_cells() == 87296
+
+
+def test_forest_tables():
+    """Forest of independent trees: ids of tree q shifted by the boxes of
+    the trees before it, relations kept inside each tree, level lists
+    concatenated, instance of each box."""
+    import afivo_tree as at
+    t1 = at.build_tree(2, 8, [8, 8], [1.0, 1.0], max_lvl=2)
+    t2 = at.build_tree(2, 8, [8, 8], [1.0, 1.0], max_lvl=3)
+    f, inst = at.forest([t1, t2])
+    assert f.n_boxes == t1.n_boxes + t2.n_boxes and f.highest_lvl == 3
+    assert list(inst) == [0] * t1.n_boxes + [1] * t2.n_boxes
+    o = t1.n_boxes
+    np.testing.assert_array_equal(f.parent[o:], np.where(t2.parent > 0, t2.parent + o, t2.parent))
+    np.testing.assert_array_equal(f.neighbors[o:], np.where(t2.neighbors > 0, t2.neighbors + o, t2.neighbors))
+    np.testing.assert_array_equal(f.children[:o], t1.children)
+    for l in range(3):
+        want = ([t1.lvl_ids[l]] if l < 2 else []) + [t2.lvl_ids[l] + o]
+        np.testing.assert_array_equal(f.lvl_ids[l], np.concatenate(want))
+    for b in range(f.n_boxes):
+        for v in list(f.neighbors[b]) + list(f.children[b]) + [f.parent[b]]:
+            if v > 0:
+                assert inst[v - 1] == inst[b]
