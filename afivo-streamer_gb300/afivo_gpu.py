@@ -38,6 +38,8 @@ RB_INTERP = 1
 RB_INTERP_LIM = 2
 FP64 = 0
 MIXED = 1
+GSRB_STAGED = 16       # smoother variant code flag: shared-memory-staged persistent kernel
+GSRB_STAGED_RHS = 32   # ... with the rhs block staged too
 CYCLE_DOWN = 1
 CYCLE_UP = 3
 KT_NONE, KT_GSRB, KT_GHOST, KT_FLUX, KT_UPDATE, KT_RESIDUAL = 0, 1, 2, 3, 4, 5
@@ -242,6 +244,7 @@ def load_library(path: str = LIB_PATH):
         "afg_transfers_wait": (C.c_int, [P]),
         "afg_autotune": (C.c_int, [P, C.c_int]),
         "afg_tuning": (C.c_int, [P, _IP]),
+        "afg_set_tuning": (C.c_int, [P, _IP]),
         "afg_host_unregister": (C.c_int, [P, C.c_void_p]),
         "afg_sync": (C.c_int, [P]),
         "afg_launch_count": (C.c_longlong, [P]),
@@ -374,9 +377,22 @@ class Context:
         self.check(self.lib.afg_autotune(self.ptr, mg_id), "afg_autotune")
 
     def tuning(self):
+        """Smoother variants in use (afg_tuning), decoded."""
         out = (C.c_int * 2)()
         self.check(self.lib.afg_tuning(self.ptr, out), "afg_tuning")
-        return {"gsrb_cells_per_thread_fp32": out[0], "gsrb_cells_per_thread_fp64": out[1]}
+
+        def name(v):
+            if v <= 0:
+                return "generic"
+            if v & GSRB_STAGED:
+                what = "phi and rhs" if v & GSRB_STAGED_RHS else "phi"
+                return f"{what} staged in shared memory (bulk copies), {v & 15} cells/thread"
+            return f"{v} cells/thread"
+        return {"gsrb_fp32": name(out[0]), "gsrb_fp64": name(out[1]), "codes": [out[0], out[1]]}
+
+    def set_tuning(self, fp32, fp64):
+        a = np.array([fp32, fp64], dtype=np.int32)
+        self.check(self.lib.afg_set_tuning(self.ptr, _ip(a)), "afg_set_tuning")
 
     def transfers_wait(self):
         self.check(self.lib.afg_transfers_wait(self.ptr), "afg_transfers_wait")

@@ -9,6 +9,7 @@
 #pragma once
 #include "afg_common.cuh"
 #include "afg_gc_kernels.cuh"
+#include "afg_tma.cuh"
 
 namespace afg {
 
@@ -245,6 +246,139 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
   }
 #pragma unroll
   for (int u = 0; u < CPT; u++) p[xs[u]] = val[u];
+}
+
+// The same half sweep with the boxes staged in shared memory: a persistent
+// grid walks the record list, each CTA copying the next box's phi block
+// ((nc+2)^D values, ghost layers included; with SR also its rhs block) into
+// shared memory with bulk asynchronous copies while it updates the current
+// box from the previous copy (two stages, one mbarrier each).  Without SR
+// the right-hand side, read once per cell, is loaded from global memory
+// before the wait (half the shared memory, more CTAs per SM).  Per box, first the face
+// ghosts that this half sweep reads (those next to cells of its colour, half
+// of each face) are evaluated cooperatively with face_ghost_nb on global
+// memory (the values af_gc would store) into the staged block; then every
+// thread updates its cells from shared memory alone, without branches.
+// Interior neighbours are cells of the other colour, which no CTA writes in
+// a half sweep, so the staged copy is current.  Results go to global memory;
+// the arithmetic is that of k_gsrb_rec.  A wait that times out (1 s) sets
+// *err; the CTA then waits (bounded) for its copies in flight and returns.
+template <int D, bool CYL, typename T, int NC, int CPT, bool SR>
+__global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT)
+    k_gsrb_tma(KTree t0, const int* __restrict__ rec, int n, T* __restrict__ phi, const T* __restrict__ rhs,
+               int redblack, MgCoef<T> mc, GcDev g, unsigned* err) {
+  constexpr int TPB = (D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT;
+  constexpr int nc = NC, n2 = NC + 2, hn = NC / 2, sk = n2 * n2;
+  constexpr int S = D == 2 ? n2 * n2 : n2 * n2 * n2;
+  constexpr int NGF = D == 2 ? hn : nc * hn;  // ghosts read per face and half sweep
+  constexpr unsigned BYTES = S * sizeof(T);
+  static_assert(BYTES % 16 == 0, "bulk copies need 16-byte multiples");
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  T* sphi = reinterpret_cast<T*>(smem_raw);  // [2][S]
+  T* srhs = sphi + 2 * S;                     // [2][S] when SR
+  __shared__ __align__(8) unsigned long long bar[2];
+  const KTree t = fix_dims<D, NC>(t0);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  // thread 0: copies of list entry e into stage st
+  auto issue = [&](int e, int st) {
+    const int s = rec[8 * e];
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&bar[st], SR ? 2 * BYTES : BYTES);
+    bulk_copy_g2s(sphi + st * S, phi + (size_t)s * S, BYTES, &bar[st]);
+    if (SR) bulk_copy_g2s(srhs + st * S, rhs + (size_t)s * S, BYTES, &bar[st]);
+  };
+  if (threadIdx.x == 0 && (int)blockIdx.x < n) issue(blockIdx.x, 0);
+  int it = 0;
+  for (int e = blockIdx.x; e < n; e += gridDim.x, it++) {
+    const int st = it & 1;
+    const bool next = e + (int)gridDim.x < n;
+    if (threadIdx.x == 0 && next) issue(e + gridDim.x, st ^ 1);
+    const int4 r0 = reinterpret_cast<const int4*>(rec)[2 * e];
+    const int4 r1 = reinterpret_cast<const int4*>(rec)[2 * e + 1];
+    const int slot = r0.x;
+    T c[7];
+    for (int q = 0; q < 2 * D + 1; q++) c[q] = mc.cb[slot * 8 + q];
+    const T inv_c1 = mc.cb[slot * 8 + 7];
+    // this thread's cells and their right-hand sides, loaded before the wait
+    const T* f = rhs + (size_t)slot * S;
+    T fv[CPT];
+    int xs[CPT];
+#pragma unroll
+    for (int u = 0; u < CPT; u++) {
+      const int w = (int)threadIdx.x + u * TPB;
+      const int row = w / hn, col = w - row * hn;
+      if (D == 2) {
+        const int j = row + 1;
+        xs[u] = at2(n2, 2 - ((redblack ^ j) & 1) + 2 * col, j);
+      } else {
+        const int j = row % nc + 1, k = row / nc + 1;
+        xs[u] = at3(n2, 2 - ((redblack ^ (k + j)) & 1) + 2 * col, j, k);
+      }
+      if (!SR) fv[u] = f[xs[u]];
+    }
+    const bool ok = mbar_wait(&bar[st], (it >> 1) & 1);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(err, 1u);
+        mbar_wait(&bar[st], (it >> 1) & 1);
+        if (next) mbar_wait(&bar[st ^ 1], ((it + 1) >> 1) & 1);
+      }
+      return;
+    }
+    const bool active = !box_frozen(t, slot);
+    T* P = sphi + st * S;
+    if (SR) {
+#pragma unroll
+      for (int u = 0; u < CPT; u++) fv[u] = srhs[st * S + xs[u]];
+    }
+    // face ghosts next to cells of this colour: cell (i, j[, k]) is updated
+    // when i + j (+ k) + redblack is even
+    for (int w = threadIdx.x; active && w < 2 * D * NGF; w += TPB) {
+      const int nb = w / NGF, m = w - nb * NGF, d = nb >> 1;
+      const bool low = (nb & 1) == 0;
+      const int a = low ? 1 : nc;  // normal index of the adjacent cell
+      int pt, qt;
+      if (D == 2) {
+        qt = 0;
+        pt = 2 * m + 1 + ((a + 1 + redblack) & 1);
+      } else {
+        qt = m / hn + 1;
+        pt = 2 * (m - (qt - 1) * hn) + 1 + ((a + 1 + qt + redblack) & 1);
+      }
+      P[face_at<D>(n2, d, low ? 0 : nc + 1, pt, qt)] =
+          face_ghost_nb<D, T>(t, phi, slot, nb, rec_nb(r0, r1, nb), pt, qt, g);
+    }
+    __syncthreads();
+    if (active) {
+      T* p = phi + (size_t)slot * S;
+      T val[CPT];
+#pragma unroll
+      for (int u = 0; u < CPT; u++) {
+        const int x = xs[u];
+        if (D == 2) {
+          if (CYL) {
+            const int i = x % n2;
+            const T* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
+            val[u] = (fv[u] - y[1] * P[x - 1] - y[2] * P[x + 1] - c[3] * P[x - n2] - c[4] * P[x + n2]) * y[3];
+          } else {
+            val[u] = (fv[u] - c[1] * P[x - 1] - c[2] * P[x + 1] - c[3] * P[x - n2] - c[4] * P[x + n2]) * inv_c1;
+          }
+        } else {
+          val[u] = (fv[u] - c[1] * P[x - 1] - c[2] * P[x + 1] - c[3] * P[x - n2] - c[4] * P[x + n2] -
+                    c[5] * P[x - sk] - c[6] * P[x + sk]) *
+                   inv_c1;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < CPT; u++) p[xs[u]] = val[u];
+    }
+    __syncthreads();  // stage st is read completely before it is refilled
+  }
 }
 
 // Residual on interior cells into tmp (residual_box, m_af_multigrid.f90:

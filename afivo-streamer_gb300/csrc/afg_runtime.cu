@@ -125,6 +125,11 @@ struct afg_ctx {
   // kModeSlot + n per Helmholtz mode n
   unsigned long long* d_max = nullptr;
   unsigned long long* h_max = nullptr;  // pinned
+  // error word raised by kernels whose bounded waits timed out, checked
+  // whenever maxima are read back (pinned copy in h_err)
+  unsigned* d_err = nullptr;
+  unsigned* h_err = nullptr;
+  int n_sm = 0;
   // side streams and events for independent branches (photoionization modes)
   cudaStream_t side[kMaxBranch] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[kMaxBranch] = {};
@@ -348,12 +353,58 @@ static int gsrb_cpt_of(const afg_ctx* ctx) {
   return c > 0 ? c : (ctx->D == 3 ? 4 : 2);
 }
 
+// Persistent grid of the shared-memory-staged smoother: as many CTAs as fit
+// on the GPU at once (occupancy of the instantiation with its shared memory)
+template <int D, bool CYL, typename T, int NC, int CPT, bool SR>
+static int launch_gsrb_tma(afg_ctx* ctx, const int* rec, int n, T* phi, const T* rhs, int rb, MgCoef<T> lam,
+                           const GcDev& g) {
+  constexpr int TPB = (D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT;
+  constexpr int S = D == 2 ? (NC + 2) * (NC + 2) : (NC + 2) * (NC + 2) * (NC + 2);
+  constexpr size_t smem = (SR ? 4 : 2) * S * sizeof(T);
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gsrb_tma<D, CYL, T, NC, CPT, SR>, TPB, smem));
+    per_sm = std::max(1, per_sm);
+  }
+  const int grid = std::min(n, per_sm * ctx->n_sm);
+  k_gsrb_tma<D, CYL, T, NC, CPT, SR><<<grid, TPB, smem, ctx->stream>>>(ktree(ctx), rec, n, phi, rhs, rb, lam, g,
+                                                                       ctx->d_err);
+  return AFG_OK;
+}
+
+template <int D, bool CYL, typename T, int NC, int CPT>
+static int launch_gsrb_tma(afg_ctx* ctx, bool sr, const int* rec, int n, T* phi, const T* rhs, int rb,
+                           MgCoef<T> lam, const GcDev& g) {
+  return sr ? launch_gsrb_tma<D, CYL, T, NC, CPT, true>(ctx, rec, n, phi, rhs, rb, lam, g)
+            : launch_gsrb_tma<D, CYL, T, NC, CPT, false>(ctx, rec, n, phi, rhs, rb, lam, g);
+}
+
 // record-driven half sweep with `cpt` cells of the colour per thread
-// (3D 8^3: 1, 2, 4, 8; 2D 16^2: 1, 2, 4)
+// (3D 8^3: 1, 2, 4, 8; 2D 16^2: 1, 2, 4); cpt | kGsrbTma selects the
+// shared-memory-staged persistent variant (3D: 2, 4; 2D: 1, 2), with
+// | kGsrbTmaRhs the right-hand side staged too
+constexpr int kGsrbTma = 16, kGsrbTmaRhs = 32;
 template <typename T>
 static int launch_gsrb_rec(afg_ctx* ctx, const int* rec, int n, T* phi, const T* rhs, int rb, MgCoef<T> lam,
                            const GcDev& g, int cpt) {
   KTree t = ktree(ctx);
+  if (cpt & kGsrbTma) {
+    const int c = cpt & (kGsrbTma - 1);
+    const bool sr = (cpt & kGsrbTmaRhs) != 0;
+    int rc;
+    if (ctx->D == 3)
+      rc = c == 2 ? launch_gsrb_tma<3, false, T, 8, 2>(ctx, sr, rec, n, phi, rhs, rb, lam, g)
+                  : launch_gsrb_tma<3, false, T, 8, 4>(ctx, sr, rec, n, phi, rhs, rb, lam, g);
+    else if (ctx->coord == AFG_CYL)
+      rc = c == 1 ? launch_gsrb_tma<2, true, T, 16, 1>(ctx, sr, rec, n, phi, rhs, rb, lam, g)
+                  : launch_gsrb_tma<2, true, T, 16, 2>(ctx, sr, rec, n, phi, rhs, rb, lam, g);
+    else
+      rc = c == 1 ? launch_gsrb_tma<2, false, T, 16, 1>(ctx, sr, rec, n, phi, rhs, rb, lam, g)
+                  : launch_gsrb_tma<2, false, T, 16, 2>(ctx, sr, rec, n, phi, rhs, rb, lam, g);
+    if (rc != AFG_OK) return rc;
+    CKL();
+    return AFG_OK;
+  }
   if (ctx->D == 3) {
     switch (cpt) {
       case 1: k_gsrb_rec<3, false, T, 8, 1><<<n, 256, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
@@ -774,10 +825,12 @@ static double inst_value(const afg_ctx* ctx, int slot, int q) {
 
 // the slot's maximum (over all instances of a batched tree)
 static int read_max(afg_ctx* ctx, int slot, double* out) {
+  CK(cudaMemcpyAsync(ctx->h_err, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
   if (!inst_slot(ctx, slot)) {
     CK(cudaMemcpyAsync(ctx->h_max + slot, ctx->d_max + slot, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                        ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (*ctx->h_err) return fail(ctx, AFG_ERR_CUDA, "a bounded wait on a copy into shared memory timed out");
     *out = bits_to_double(ctx->h_max[slot]);
     return AFG_OK;
   }
@@ -785,6 +838,7 @@ static int read_max(afg_ctx* ctx, int slot, double* out) {
   CK(cudaMemcpy2DAsync(ctx->h_max + slot, pitch, ctx->d_max + slot, pitch, sizeof(unsigned long long), ctx->n_inst,
                        cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  if (*ctx->h_err) return fail(ctx, AFG_ERR_CUDA, "a bounded wait on a copy into shared memory timed out");
   double mx = 0;
   for (int q = 0; q < ctx->n_inst; q++) mx = std::max(mx, inst_value(ctx, slot, q));
   *out = mx;
@@ -803,7 +857,7 @@ static int reset_max(afg_ctx* ctx, int slot) {
 
 // Autotuner of the smoother's work shape: on the level with the most boxes,
 // time every cells-per-thread variant of the FP32 half sweep (CUDA events,
-// best of 3 after a warm-up) on the slot's FP32 buffers, which are scratch
+// best of 7 after a warm-up) on the slot's FP32 buffers, which are scratch
 // outside a solve, and keep the fastest.  All variants do the same
 // arithmetic, so the choice changes speed only.
 static int autotune_gsrb(afg_ctx* ctx, MgSlot& m) {
@@ -815,9 +869,10 @@ static int autotune_gsrb(afg_ctx* ctx, MgSlot& m) {
   if (n < 256) return AFG_OK;  // too small to time; the default stays
   const int* rec = rec_of(ctx, lst(ctx, ctx->off_ids[best_l]));
   const GcDev g = mg_gc(ctx, m, true);
-  const int cands3[] = {1, 2, 4, 8}, cands2[] = {1, 2, 4};
+  const int S = kGsrbTma, R = kGsrbTma | kGsrbTmaRhs;
+  const int cands3[] = {1, 2, 4, 8, S | 2, S | 4, R | 2, R | 4}, cands2[] = {1, 2, 4, S | 1, S | 2, R | 1, R | 2};
   const int* cands = ctx->D == 3 ? cands3 : cands2;
-  const int nc = ctx->D == 3 ? 4 : 3;
+  const int nc = ctx->D == 3 ? 8 : 7;
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -826,7 +881,7 @@ static int autotune_gsrb(afg_ctx* ctx, MgSlot& m) {
   int rc = AFG_OK;
   for (int q = 0; q < nc && rc == AFG_OK; q++) {
     float tmin = 1e30f;
-    for (int r = 0; r < 4 && rc == AFG_OK; r++) {
+    for (int r = 0; r < 8 && rc == AFG_OK; r++) {
       cudaEventRecord(e0, ctx->stream);
       rc = launch_gsrb_rec<float>(ctx, rec, n, m.e32, m.r32, 1 + (r & 1), coef_of<float>(m), g, cands[q]);
       cudaEventRecord(e1, ctx->stream);
@@ -1033,6 +1088,11 @@ int afg_init(int device, afg_ctx** out) {
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   CK(dalloc(&ctx->d_max, kMaxSlots));
   CK(cudaMallocHost((void**)&ctx->h_max, kMaxSlots * sizeof(unsigned long long)));
+  CK(dalloc(&ctx->d_err, 1));
+  CK(cudaMemset(ctx->d_err, 0, sizeof(unsigned)));
+  CK(cudaMallocHost((void**)&ctx->h_err, sizeof(unsigned)));
+  *ctx->h_err = 0;
+  CK(cudaDeviceGetAttribute(&ctx->n_sm, cudaDevAttrMultiProcessorCount, device));
   for (auto& st : ctx->side) CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&ctx->xfer_stream, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&ctx->ev_xfer, cudaEventDisableTiming));
@@ -1056,6 +1116,8 @@ int afg_finalize(afg_ctx* ctx) {
   if (ctx->flush_buf) cudaFree(ctx->flush_buf);
   dfree(ctx->d_max);
   if (ctx->h_max) cudaFreeHost(ctx->h_max);
+  dfree(ctx->d_err);
+  if (ctx->h_err) cudaFreeHost(ctx->h_err);
   if (ctx->xfer_stream) {
     cudaStreamSynchronize(ctx->xfer_stream);
     cudaStreamDestroy(ctx->xfer_stream);
@@ -2071,6 +2133,22 @@ int afg_autotune(afg_ctx* ctx, int mg_id) {
   if (m->d.precision != AFG_MIXED) return fail(ctx, AFG_ERR_ARG, "autotuning needs a mixed-precision slot (scratch)");
   clear_graphs(ctx);
   return autotune_gsrb(ctx, *m);
+}
+
+int afg_set_tuning(afg_ctx* ctx, const int* in) {
+  if (!ctx || !in) return AFG_ERR_ARG;
+  if (!ctx->have_tree) return fail(ctx, AFG_ERR_STATE, "no tree");
+  const int S = kGsrbTma, R = kGsrbTma | kGsrbTmaRhs;
+  const int ok3[] = {0, 1, 2, 4, 8, S | 2, S | 4, R | 2, R | 4}, ok2[] = {0, 1, 2, 4, S | 1, S | 2, R | 1, R | 2};
+  for (int k = 0; k < 2; k++) {
+    bool ok = false;
+    for (int v : (ctx->D == 3 ? std::vector<int>(ok3, ok3 + 9) : std::vector<int>(ok2, ok2 + 8))) ok = ok || in[k] == v;
+    if (!ok) return fail(ctx, AFG_ERR_ARG, "bad smoother variant %d", in[k]);
+  }
+  clear_graphs(ctx);  // launch shapes are part of captured graphs
+  ctx->gsrb_cpt[0] = in[0];
+  ctx->gsrb_cpt[1] = in[1];
+  return AFG_OK;
 }
 
 int afg_tuning(const afg_ctx* ctx, int* out) {

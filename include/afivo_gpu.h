@@ -188,6 +188,13 @@ int afg_cc_download_async(afg_ctx* ctx, int iv, double* const* box_cc,
  * the reference. */
 int afg_autotune(afg_ctx* ctx, int mg_id);
 int afg_tuning(const afg_ctx* ctx, int* out);
+/* Set the smoother variants instead (in[0] FP32, in[1] FP64; 0 = default):
+ * cells per thread 1, 2, 4, 8 (3D 8^3) or 1, 2, 4 (2D 16^2), or 16 + cells
+ * per thread for the shared-memory-staged persistent variant (bulk copies of
+ * each box's phi into shared memory, double-buffered; 3D: 18, 20; 2D: 17,
+ * 18), plus 32 when the rhs block is staged as well (3D: 50, 52; 2D: 49,
+ * 50).  afg_tuning reports the codes the same way. */
+int afg_set_tuning(afg_ctx* ctx, const int* in);
 
 /* Wait for the copies started by afg_cc_download_async. */
 int afg_transfers_wait(afg_ctx* ctx);

@@ -213,3 +213,56 @@ def test_solve_fp64_and_mixed(case):
     e_mix = leaf_error(tree, out, ref[:, 0])
     assert e_mix <= 1e-6, (name, e_mix, n_mix, res_mix)
     assert n_mix <= n_cpu + 3, (n_mix, n_cpu)
+
+
+_R = ag.GSRB_STAGED | ag.GSRB_STAGED_RHS
+VARIANTS = {2: [1, 2, 4, ag.GSRB_STAGED | 1, ag.GSRB_STAGED | 2, _R | 1, _R | 2],
+            3: [1, 2, 4, 8, ag.GSRB_STAGED | 2, ag.GSRB_STAGED | 4, _R | 2, _R | 4]}
+
+
+@pytest.mark.parametrize("name", ["2d16", "3d8"])
+def test_smoother_variants_fp64_bitexact(name, gpu_lib):
+    """Every smoother variant of the box sizes with compile-time kernels
+    (cells per thread, and the shared-memory-staged persistent kernel fed by
+    bulk copies) gives the oracle's smoothing bit for bit in FP64."""
+    tree = CASES[name]()
+    ctx = ag.Context(0)
+    ctx.tree_sync(tree, 3)
+    for v in VARIANTS[tree.ndim]:
+        ctx.set_tuning(0, v)
+        desc, cc, o = setup_pair(tree, ctx, 5, 4.0e6)
+        ctx.gc(I_PHI, 0, True)
+        o.gc(cc, I_PHI, 0, True)
+        for lvl in range(tree.highest_lvl, 1, -1):
+            ctx.mg_gsrb_lvl(0, lvl, ag.CYCLE_DOWN)
+            o.mg_gsrb_lvl(cc, 0, lvl, ag.CYCLE_DOWN)
+        out = download(ctx, tree)
+        assert np.array_equal(out[:, 0], cc[:, 0]), f"{name} variant {v}: {rel(out[:, 0], cc[:, 0])}"
+    ctx.close()
+
+
+@pytest.mark.parametrize("name", ["2d16", "3d8"])
+def test_smoother_variants_fp32_identical(name, gpu_lib):
+    """The FP32 smoother variants compute the same values: mixed-precision
+    solves with each variant end bit for bit alike."""
+    tree = CASES[name]()
+    cyl = tree.coord == ag.AFG_CYL
+    phi_ex, rhs, bc = sine_problem(tree, 0.0, cyl)
+    cc = ag.new_cc(tree, 3)
+    cc[:, I_RHS - 1] = rhs * 1e10
+    desc = ag.mg_desc(I_PHI, I_RHS, I_TMP, bc, precision=ag.MIXED)
+    ctx = ag.Context(0)
+    ctx.tree_sync(tree, 3)
+    ref = None
+    for v in VARIANTS[tree.ndim]:
+        ctx.mg_setup(0, desc)
+        ctx.set_tuning(v, 0)
+        ctx.upload(cc)
+        ctx.gc(I_PHI, 0, True)
+        thr = 1e-8 * np.max(np.abs(rhs * 1e10))
+        ctx.mg_solve(0, thr, 40)
+        out = download(ctx, tree)
+        if ref is None:
+            ref = out
+        assert np.array_equal(out.view(np.uint64), ref.view(np.uint64)), f"{name} variant {v}"
+    ctx.close()
