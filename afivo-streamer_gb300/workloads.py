@@ -28,6 +28,8 @@ involved (each configuration defines its own inputs):
   transport as cyl2d; 3-term Helmholtz photoionization; applied field
   1.5e6 V/m.
 
+* ``poisson3d`` -- 3D Poisson + 3 Helmholtz modes, 2 cm cube, 8^3 boxes,
+  10 levels (~41 M cells) refined around a Gaussian seed (Poisson3d).
 * ``batch`` -- 256 independent 2D axisymmetric Poisson + transport
   instances of uneven size (BatchCyl2d), run as one forest.
 
@@ -221,6 +223,43 @@ class Streamer3d(Workload):
         return (1.5e-2, 1.5e-2, 1.7e-2)
 
 
+class Poisson3d(Workload):
+    """3D Poisson + Helmholtz configuration: 2 cm cube, 8^3-cell boxes,
+    uniform to level 5 plus 5 AMR levels (10 levels, ~41 M cells) from a
+    seeded refinement map around a Gaussian seed of sigma = 0.3 mm at the
+    centre: spheres whose radius shrinks per level, with a seeded
+    modulation of their surface (uneven per-level box counts).  The
+    Poisson right-hand side comes from the seed's charge, the applied field
+    is 1.5e6 V/m; three Helmholtz modes (photoionization) share the source."""
+    name = "poisson3d"
+    voltage = -3e4
+    seed_sigma = 0.3e-3
+    positive_species = 1
+    radii = (6.3e-3, 3.8e-3, 2.15e-3, 1.3e-3, 0.75e-3)
+
+    def tree(self, reduced=False, coarsen=0):
+        c = np.asarray(self.seed_center())
+        radii = self.radii
+        rng = np.random.default_rng(2026)
+        a, b, ph = rng.uniform(20, 40, 3), rng.uniform(5, 15, 3), rng.uniform(0, 2 * np.pi, 3)
+
+        def refine(lvl, cen, dr):
+            if lvl < 5:
+                return np.ones(len(cen), bool)
+            R = radii[lvl - 5]
+            d = np.sqrt(((cen - c) ** 2).sum(axis=1))
+            mod = 1 + 0.25 * np.sin(a[0] * cen[:, 0] / R + b[0] * cen[:, 1] / R + ph[0]) * \
+                np.cos(a[1] * cen[:, 2] / R + ph[1])
+            return d < R * mod
+        return at.build_tree(3, 8, [8, 8, 8], [2e-2] * 3, max_lvl=10 - coarsen, refine=refine)
+
+    def model(self):
+        return sm.StreamerModel(3, alpha=sm.baseline_alpha, eta=sm.baseline_eta, photoi_modes=3)
+
+    def seed_center(self):
+        return (1e-2, 1e-2, 1e-2)
+
+
 class CylInstance(Workload):
     """One instance of the batched configuration: 2D axisymmetric,
     r in [0, 1 cm], z in [0, 1 cm], uniform grid of `side`^2 cells in 16^2
@@ -290,4 +329,4 @@ class BatchCyl2d:
         return np.concatenate(parts), ivs
 
 
-WORKLOADS = {"cart2d": Cart2d, "cyl2d": Cyl2d, "3d": Streamer3d}
+WORKLOADS = {"cart2d": Cart2d, "cyl2d": Cyl2d, "3d": Streamer3d, "poisson3d": Poisson3d}

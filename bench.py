@@ -56,6 +56,8 @@ CONFIG_TEXT = {
              "3 Helmholtz photoionization modes, Heun dt=5e-12 s, Poisson to 1e-8 rel.",
     "cart2d": "2D Cartesian 1 cm^2, uniform 256^2 grid of 16^2 boxes, 5 levels, 341 boxes, electrons + ions, "
               "alpha(E) ionization, forward Euler dt=1e-12 s, Poisson to 1e-10 rel.",
+    "poisson3d": "3D Poisson + 3 Helmholtz modes: 2 cm cube, 8^3 boxes, 10 levels (uniform to level 5, 5 AMR "
+                 "levels around a sigma=0.3 mm Gaussian seed), 80665 boxes, ~41 M cells; Poisson to 1e-8 rel.",
     "batch": "256 independent 2D axisymmetric Poisson + transport instances (1 cm^2, 16^2 boxes, uniform "
              "grids with sides drawn from {64,128,256,512}, voltages 15-35 kV, seed amplitudes 1e13-1e16), "
              "one forest in one context, 3 species, Heun dt=5e-12 s, Poisson to 1e-8 rel. per instance",
@@ -146,6 +148,88 @@ def problem(args, w):
     model = w.model()
     H, ivs = initial_host_state(w, tree, model)
     return tree, model, H, ivs, w.voltage, None, None
+
+
+def run_poisson3d(args, device, config):
+    """The 3D Poisson + Helmholtz configuration: per precision, a Poisson
+    solve from scratch (FMG start + V-cycles to 1e-8 relative residual), K
+    further solve iterations timed on their own (V-cycle ms; in the mixed
+    path one iteration = FP32 V-cycle + FP64 defect correction), the
+    smoother's kernel time and algorithmic GB/s over those iterations, and
+    the three Helmholtz modes (photoionization, FMG to 1e-2); the mixed
+    results against the FP64 ones (phi, |E| and the photoionization source on
+    the leaves)."""
+    w = workloads.Poisson3d()
+    tree = w.tree(coarsen=args.coarsen)
+    model = w.model()
+    H, ivs = w.initial_host_state(tree, model)
+    ctx = ag.Context(device)
+    K = max(3, args.steps)
+    lam, coeffs, coeff = w.photoi_lambda, w.photoi_coeffs, w.photoi_eta_quench
+    out, fields = {}, {}
+    leaves = np.concatenate(tree.lvl_leaves) - 1
+    n2 = tree.n_cell + 2
+    inner = (slice(None),) + (slice(1, n2 - 1),) * tree.ndim
+    for name, prec in (("fp64", ag.FP64), ("mixed", ag.MIXED)):
+        ctx.tree_sync(tree, model.n_var_cell, model.n_var_face)
+        ctx.upload_vars(H, ivs)
+        run = sm.StreamerRun(ctx, tree, model, w.voltage, w.dt, precision=prec, **w.run_kwargs())
+        run.setup()
+        for _ in range(args.warmup):           # graphs captured, tuning done
+            ctx.gc(model.i_phi, 0, True)
+            run.field(0, False)
+            ctx.photoi_helmh(coeff, run.mode_ids, coeffs, 1e-2, 10)
+        ctx.sync()
+        ctx.flush_l2(256 << 20)
+        ctx.event_record(0)
+        n_solve, r_solve = run.field(0, False)
+        ctx.event_record(1)
+        solve_ms = ctx.event_elapsed(0, 1)
+        c0 = ctx.counters()
+        ctx.flush_l2(256 << 20)
+        ctx.event_record(2)
+        ctx.mg_solve(0, 0.0, K, allow_noconv=True)
+        ctx.event_record(3)
+        it_ms = ctx.event_elapsed(2, 3) / K
+        work = ctx.counters()["smoother_updates"] - c0["smoother_updates"]
+        ctx.kernel_timing(ag.KT_GSRB)
+        ctx.mg_solve(0, 0.0, K, allow_noconv=True)
+        gl, gms, gby = ctx.kernel_stats()
+        ctx.kernel_timing(ag.KT_NONE)
+        ctx.flush_l2(256 << 20)
+        ctx.event_record(4)
+        ctx.photoi_helmh(coeff, run.mode_ids, coeffs, 1e-2, 10)
+        ctx.event_record(5)
+        photo_ms = ctx.event_elapsed(4, 5)
+        cc = ag.new_cc(tree, model.n_var_cell)
+        ctx.download(cc)
+        fields[name] = {iv: cc[leaves, iv - 1][inner] for iv in (model.i_phi, model.i_electric_fld, model.i_photo)}
+        out[name] = dict(solve_ms=solve_ms, solve_cycles=n_solve, solve_residual=r_solve, vcycle_ms=it_ms,
+                         cell_updates_per_s=work / (it_ms * K * 1e-3),
+                         smoother=dict(launches=gl, ms_per_vcycle=gms / K, algorithmic_gbs=gby / (gms * 1e-3) / 1e9),
+                         photoi_3_modes_ms=photo_ms, tuning=ctx.tuning())
+    ctx.close()
+    err = {}
+    for key, iv in (("phi", model.i_phi), ("E", model.i_electric_fld), ("photoi_source", model.i_photo)):
+        a, b = fields["mixed"][iv], fields["fp64"][iv]
+        err[key] = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+    peak, peak_kind = peaks()
+    sm32, sm64 = out["mixed"]["smoother"], out["fp64"]["smoother"]
+    print(json.dumps({
+        "metric": "V-cycle ms & smoother HBM GB/s, FP32 vs FP64 smoothers (3D Poisson + 3 Helmholtz modes)",
+        "value": out["mixed"]["vcycle_ms"], "unit": "ms per V-cycle (mixed)", "higher_is_better": False,
+        "n_gpus": 1, "steps": K, "warmup": args.warmup, "dtype": "f64+f32", "data": "synthetic (seeded)",
+        "config": dict(config, boxes=tree.n_boxes, cells=tree.n_cells(), leaf_cells=tree.n_cells(True),
+                       boxes_per_level=[len(x) for x in tree.lvl_ids]),
+        "fp64": out["fp64"], "mixed": out["mixed"],
+        "speedup_mixed_vs_fp64": {"vcycle": out["fp64"]["vcycle_ms"] / out["mixed"]["vcycle_ms"],
+                                  "solve": out["fp64"]["solve_ms"] / out["mixed"]["solve_ms"],
+                                  "photoi": out["fp64"]["photoi_3_modes_ms"] / out["mixed"]["photoi_3_modes_ms"]},
+        "error_mixed_vs_fp64": err,
+        "roofline": {"bound": "hbm", "kernel": "gsrb (FP32 smoother)", "achieved": sm32["algorithmic_gbs"],
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": sm32["algorithmic_gbs"] / peak,
+                     "fp64_smoother_frac": sm64["algorithmic_gbs"] / peak, "traffic": None},
+    }))
 
 
 def run_one_at_a_time(args, device, w, trees, model, H, ivs):
@@ -294,6 +378,8 @@ def run_cpu(name, steps, warmup=1, time_limit=None):
     if name == "batch":
         return run_cpu_batch(steps, warmup, time_limit, cores)
     w = workloads.WORKLOADS[name]()
+    if name == "poisson3d":
+        return run_cpu_poisson3d(w, steps, warmup, time_limit, cores)
     reduced = name == "3d"
     tree = w.tree(reduced=reduced)
     model = w.model()
@@ -320,6 +406,36 @@ def run_cpu(name, steps, warmup=1, time_limit=None):
               f"({tree.n_boxes} boxes, {ncells / 1e6:.2f} M cells"
               f"{', the same construction two levels coarser' if reduced else ''}) on the CPU restatement "
               f"(C++/OpenMP, {cores} threads)")
+    return work / dt, cores, dt / done, done, sample
+
+
+def run_cpu_poisson3d(w, steps, warmup, time_limit, cores):
+    """The 3D Poisson configuration on the CPU restatement: FP64 solve
+    iterations (V-cycles) on the same construction two levels coarser."""
+    from oracle_streamer import OracleStreamerRun
+    tree = w.tree(coarsen=2)
+    model = w.model()
+    cc = ag.new_cc(tree, model.n_var_cell)
+    fc = ag.new_fc(tree, model.n_var_face)
+    H, ivs = w.initial_host_state(tree, model)
+    for v, iv in enumerate(ivs):
+        cc[:, iv - 1] = H[:, v]
+    kw = w.run_kwargs()
+    kw["photoi"] = None
+    run = OracleStreamerRun(tree, model, w.voltage, w.dt, **kw)
+    run.setup()
+    run.initial_field(cc, fc)
+    o = run.o
+    work, done, t0 = 0, 0, time.perf_counter()
+    while done < max(1, steps):
+        o.mg_vcycle(cc, 0, True)
+        work += run.vcycle_updates(tree.highest_lvl, run.field_desc)
+        done += 1
+        if time_limit is not None and time.perf_counter() - t0 > time_limit:
+            break
+    dt = time.perf_counter() - t0
+    sample = (f"{done} FP64 V-cycle(s) of the poisson3d tree two levels coarser ({tree.n_boxes} boxes, "
+              f"{tree.n_cells() / 1e6:.2f} M cells) on the CPU restatement (C++/OpenMP, {cores} threads)")
     return work / dt, cores, dt / done, done, sample
 
 
@@ -403,6 +519,10 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
+    if args.config == "poisson3d":
+        if rank == 0:
+            run_poisson3d(args, local, config)
+        return
     w = workloads.BatchCyl2d() if args.config == "batch" else workloads.WORKLOADS[args.config]()
     tree, results, kstats, e2e, tuning = run_gpu_arm(args, local, w)
     one = e2e.pop("one_at_a_time", None) if e2e else None
