@@ -62,13 +62,13 @@ CONFIG_TEXT = {
              "grids with sides drawn from {64,128,256,512}, voltages 15-35 kV, seed amplitudes 1e13-1e16), "
              "one forest in one context, 3 species, Heun dt=5e-12 s, Poisson to 1e-8 rel. per instance",
 }
-# DRAM traffic of a kernel class relative to its algorithmic bytes, from one
-# ncu capture (dram__bytes.sum.per_second x gpu__time_duration.sum) of the
-# same kernel on the same tree construction one level coarser; traffic grows
-# with the boxes a launch processes, so the ratio carries over to full size.
-# Smoother: 7135 bytes per box and half sweep against 3072 algorithmic
-# (1.5 FP32 words per cell).
-NCU_TRAFFIC_RATIO = {("3d", "gsrb"): 7135.0 / 3072.0}
+# DRAM traffic of a kernel class relative to its algorithmic bytes, from the
+# ncu capture of every launch of one step of the same workload
+# (dram__bytes_read.sum + dram__bytes_write.sum; profiles/
+# dram_per_kernel_streamer_steps.md).  The FP32 smoother (staged variant):
+# 3D 82.71 GB over the step's 5 V-cycles against 27.17 GB algorithmic (1.5
+# FP32 words per cell and half sweep); batch 14.47 GB against 7.43 GB.
+NCU_TRAFFIC_RATIO = {("3d", "gsrb"): 82.71 / 27.17, ("batch", "gsrb"): 14.47 / 7.43}
 
 
 class Clocks:
