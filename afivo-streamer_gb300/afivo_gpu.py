@@ -245,6 +245,7 @@ def load_library(path: str = LIB_PATH):
         "afg_autotune": (C.c_int, [P, C.c_int]),
         "afg_tuning": (C.c_int, [P, _IP]),
         "afg_set_tuning": (C.c_int, [P, _IP]),
+        "afg_set_photoi_lockstep": (C.c_int, [P, C.c_int]),
         "afg_host_unregister": (C.c_int, [P, C.c_void_p]),
         "afg_sync": (C.c_int, [P]),
         "afg_launch_count": (C.c_longlong, [P]),
@@ -389,6 +390,9 @@ class Context:
                 return f"{what} staged in shared memory (bulk copies), {v & 15} cells/thread"
             return f"{v} cells/thread"
         return {"gsrb_fp32": name(out[0]), "gsrb_fp64": name(out[1]), "codes": [out[0], out[1]]}
+
+    def set_photoi_lockstep(self, on):
+        self.check(self.lib.afg_set_photoi_lockstep(self.ptr, int(on)), "afg_set_photoi_lockstep")
 
     def set_tuning(self, fp32, fp64):
         a = np.array([fp32, fp64], dtype=np.int32)

@@ -161,6 +161,55 @@ struct MgCoef {
   const T* cy;
 };
 
+// Several multigrid problems on the same tree advanced in lockstep (the
+// Helmholtz modes of photoionization as multiple right-hand sides): a launch
+// carries one pointer per problem and blockIdx.y selects it.  A single
+// pointer converts to an argument holding it in every element (one problem,
+// or a buffer all problems share).  The element is picked by selects on
+// constant indices, so the parameter array is never indexed dynamically (no
+// local-memory copy).
+constexpr int kMaxModes = 8;
+template <typename T>
+struct ModeArg {
+  T* p[kMaxModes] = {};
+  ModeArg() = default;
+  __host__ __device__ ModeArg(T* q) {  // the same pointer for every problem
+    for (int k = 0; k < kMaxModes; k++) p[k] = q;
+  }
+  template <typename U>  // the same pointers with added const
+  __host__ __device__ ModeArg(const ModeArg<U>& o) {
+    for (int k = 0; k < kMaxModes; k++) p[k] = o.p[k];
+  }
+  __device__ __forceinline__ T* get() const {
+    const unsigned y = blockIdx.y;
+    T* r = p[0];
+#pragma unroll
+    for (unsigned k = 1; k < kMaxModes; k++)
+      if (y == k) r = p[k];
+    return r;
+  }
+};
+template <typename T>
+struct ModeCoef {
+  const T* cb[kMaxModes] = {};
+  const T* cy[kMaxModes] = {};
+  ModeCoef() = default;
+  __host__ __device__ ModeCoef(MgCoef<T> q) {  // the same tables for every problem
+    for (int k = 0; k < kMaxModes; k++) {
+      cb[k] = q.cb;
+      cy[k] = q.cy;
+    }
+  }
+  __device__ __forceinline__ MgCoef<T> get() const {
+    const unsigned y = blockIdx.y;
+    MgCoef<T> r{cb[0], cy[0]};
+#pragma unroll
+    for (unsigned k = 1; k < kMaxModes; k++)
+      if (y == k) r = MgCoef<T>{cb[k], cy[k]};
+    return r;
+  }
+};
+
 // Ghost-cell method of one variable (bc per domain face + refinement rule).
 struct GcDev {
   int bc_type[6];

@@ -175,9 +175,10 @@ __device__ void corner_ghosts(const KTree& t, T* __restrict__ v, int slot) {
 
 // af_gc_lvl on a box list: one CTA per box.
 template <int D, typename T, int NC = 0>
-__global__ void __launch_bounds__(256) k_gc(KTree t0, const int* __restrict__ rec, T* __restrict__ v,
-                                            GcDev g, int corners) {
+__global__ void __launch_bounds__(256) k_gc(KTree t0, const int* __restrict__ rec, ModeArg<T> v_, GcDev g,
+                                            int corners) {
   const KTree t = fix_dims<D, NC>(t0);
+  T* __restrict__ v = v_.get();
   int4 r0, r1;
   load_rec(rec, blockIdx.x, r0, r1);
   const int slot = r0.x;

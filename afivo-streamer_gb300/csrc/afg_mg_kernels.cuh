@@ -143,10 +143,13 @@ __global__ void __launch_bounds__(256) k_gsrb(KTree t0, const int* __restrict__ 
 // itself before its update.  One ghost fill after the last half sweep then
 // leaves memory exactly as the reference does.
 template <int D, bool CYL, typename T, int NC = 0>
-__global__ void __launch_bounds__(256, 6) k_gsrb_fused(KTree t0, const int* __restrict__ list, T* __restrict__ phi,
-                                                    const T* __restrict__ rhs, int redblack, MgCoef<T> mc,
+__global__ void __launch_bounds__(256, 6) k_gsrb_fused(KTree t0, const int* __restrict__ list, ModeArg<T> phi_,
+                                                    ModeArg<const T> rhs_, int redblack, ModeCoef<T> mc_,
                                                     GcDev g) {
   const KTree t = fix_dims<D, NC>(t0);
+  T* __restrict__ phi = phi_.get();
+  const T* __restrict__ rhs = rhs_.get();
+  const MgCoef<T> mc = mc_.get();
   const int slot = list[blockIdx.x];
   if (box_frozen(t, slot)) return;
   const int nc = t.nc, n2 = t.n2, hn = nc / 2;
@@ -195,11 +198,14 @@ __global__ void __launch_bounds__(256, 6) k_gsrb_fused(KTree t0, const int* __re
 template <int D, bool CYL, typename T, int NC, int CPT>
 __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT,
                                   1536 / ((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT))
-    k_gsrb_rec(KTree t0, const int* __restrict__ rec, T* __restrict__ phi, const T* __restrict__ rhs, int redblack,
-               MgCoef<T> mc, GcDev g) {
+    k_gsrb_rec(KTree t0, const int* __restrict__ rec, ModeArg<T> phi_, ModeArg<const T> rhs_, int redblack,
+               ModeCoef<T> mc_, GcDev g) {
   constexpr int TPB = (D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT;
   constexpr int nc = NC, n2 = NC + 2, hn = NC / 2, sk = n2 * n2;
   const KTree t = fix_dims<D, NC>(t0);
+  T* __restrict__ phi = phi_.get();
+  const T* __restrict__ rhs = rhs_.get();
+  const MgCoef<T> mc = mc_.get();
   const int4 r0 = reinterpret_cast<const int4*>(rec)[2 * blockIdx.x];
   const int4 r1 = reinterpret_cast<const int4*>(rec)[2 * blockIdx.x + 1];
   const int slot = r0.x;
@@ -265,8 +271,11 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
 // *err; the CTA then waits (bounded) for its copies in flight and returns.
 template <int D, bool CYL, typename T, int NC, int CPT, bool SR>
 __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT)
-    k_gsrb_tma(KTree t0, const int* __restrict__ rec, int n, T* __restrict__ phi, const T* __restrict__ rhs,
-               int redblack, MgCoef<T> mc, GcDev g, unsigned* err) {
+    k_gsrb_tma(KTree t0, const int* __restrict__ rec, int n, ModeArg<T> phi_, ModeArg<const T> rhs_, int redblack,
+               ModeCoef<T> mc_, GcDev g, unsigned* err) {
+  T* __restrict__ phi = phi_.get();
+  const T* __restrict__ rhs = rhs_.get();
+  const MgCoef<T> mc = mc_.get();
   constexpr int TPB = (D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT;
   constexpr int nc = NC, n2 = NC + 2, hn = NC / 2, sk = n2 * n2;
   constexpr int S = D == 2 ? n2 * n2 : n2 * n2 * n2;
@@ -427,10 +436,14 @@ __global__ void __launch_bounds__(256) k_residual(KTree t0, const int* __restric
 // parent cell covered by the child.
 template <int D, bool CYL, typename T, int NC = 0>
 __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* __restrict__ rec,
-                                                           T* __restrict__ phi, const T* __restrict__ rhs,
-                                                           T* __restrict__ tmp, MgCoef<T> mc,
-                                                           int store_child_residual, GcDev g, int otf) {
+                                                           ModeArg<T> phi_, ModeArg<const T> rhs_, ModeArg<T> tmp_,
+                                                           ModeCoef<T> mc_, int store_child_residual, GcDev g,
+                                                           int otf) {
   const KTree t = fix_dims<D, NC>(t0);
+  T* __restrict__ phi = phi_.get();
+  const T* __restrict__ rhs = rhs_.get();
+  T* __restrict__ tmp = tmp_.get();
+  const MgCoef<T> mc = mc_.get();
   int4 r0, r1;
   load_rec(rec, blockIdx.x, r0, r1);
   const int slot = r0.x;
@@ -516,11 +529,14 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* 
 // this step (leaf boxes of the level need none there: the fused smoother
 // computes its own and the level is filled again after its up smoothing).
 template <int D, bool CYL, typename T, int NC = 0>
-__global__ void __launch_bounds__(256) k_coarse_fas(KTree t0, const int* __restrict__ rec,
-                                                    T* __restrict__ phi, T* __restrict__ rhs,
-                                                    T* __restrict__ tmp, MgCoef<T> mc, int copy_tmp, int fill,
-                                                    GcDev g) {
+__global__ void __launch_bounds__(256) k_coarse_fas(KTree t0, const int* __restrict__ rec, ModeArg<T> phi_,
+                                                    ModeArg<T> rhs_, ModeArg<T> tmp_, ModeCoef<T> mc_, int copy_tmp,
+                                                    int fill, GcDev g) {
   const KTree t = fix_dims<D, NC>(t0);
+  T* __restrict__ phi = phi_.get();
+  T* __restrict__ rhs = rhs_.get();
+  T* __restrict__ tmp = tmp_.get();
+  const MgCoef<T> mc = mc_.get();
   int4 r0, r1;
   load_rec(rec, blockIdx.x, r0, r1);
   const int slot = r0.x;
@@ -566,9 +582,11 @@ __global__ void __launch_bounds__(256) k_coarse_fas(KTree t0, const int* __restr
 // bilinear/trilinear prolongation of tmp added (stencil_prolong_248,
 // m_af_stencil.f90:695-815, coefficients 1267-1284).
 template <int D, typename T, int NC = 0>
-__global__ void __launch_bounds__(256) k_correct(KTree t0, const int* __restrict__ list, T* __restrict__ phi,
-                                                 T* __restrict__ tmp) {
+__global__ void __launch_bounds__(256) k_correct(KTree t0, const int* __restrict__ list, ModeArg<T> phi_,
+                                                 ModeArg<T> tmp_) {
   const KTree t = fix_dims<D, NC>(t0);
+  T* __restrict__ phi = phi_.get();
+  T* __restrict__ tmp = tmp_.get();
   extern __shared__ unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   const int slot = list[blockIdx.x];
@@ -613,9 +631,11 @@ __global__ void __launch_bounds__(256) k_correct(KTree t0, const int* __restrict
 // init_phi_rhs (m_af_multigrid.f90:779-799) on one level: phi = 0 on the
 // whole array, rhs restricted to the parent with geometry.
 template <int D, bool CYL, typename T, int NC = 0>
-__global__ void __launch_bounds__(256) k_init_phi_rhs(KTree t0, const int* __restrict__ list,
-                                                      T* __restrict__ phi, T* __restrict__ rhs) {
+__global__ void __launch_bounds__(256) k_init_phi_rhs(KTree t0, const int* __restrict__ list, ModeArg<T> phi_,
+                                                      ModeArg<T> rhs_) {
   const KTree t = fix_dims<D, NC>(t0);
+  T* __restrict__ phi = phi_.get();
+  T* __restrict__ rhs = rhs_.get();
   const int slot = list[blockIdx.x];
   if (box_frozen(t, slot)) return;
   const int pslot = t.parent[slot];
@@ -661,8 +681,10 @@ __global__ void __launch_bounds__(256) k_init_phi_rhs(KTree t0, const int* __res
 // Whole-array copy of one variable on a box list (af_boxes_copy_cc,
 // m_af_utils.f90:579-588).
 template <typename T>
-__global__ void __launch_bounds__(256) k_copy(KTree t, const int* __restrict__ list, const T* __restrict__ src,
-                                              T* __restrict__ dst) {
+__global__ void __launch_bounds__(256) k_copy(KTree t, const int* __restrict__ list, ModeArg<const T> src_,
+                                              ModeArg<T> dst_) {
+  const T* __restrict__ src = src_.get();
+  T* __restrict__ dst = dst_.get();
   const int slot = list[blockIdx.x];
   if (box_frozen(t, slot)) return;
   const int S = t.S;
@@ -677,8 +699,10 @@ __global__ void __launch_bounds__(256) k_copy(KTree t, const int* __restrict__ l
 template <typename T>
 __global__ void k_coarse_gather(int n, int nloc, int D, const int* __restrict__ cslot, const int* __restrict__ ccell,
                                 const double* __restrict__ b2r, const unsigned char* __restrict__ bmask,
-                                const double* __restrict__ bc_val, int bc_stride, const T* __restrict__ rhs, int S,
-                                double* __restrict__ b) {
+                                const double* __restrict__ bc_val, int bc_stride, ModeArg<const T> rhs_, int S,
+                                ModeArg<double> b_) {
+  const T* __restrict__ rhs = rhs_.get();
+  double* __restrict__ b = b_.get();
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
   const int q = g / nloc, gl = g - q * nloc;
@@ -693,8 +717,11 @@ __global__ void k_coarse_gather(int n, int nloc, int D, const int* __restrict__ 
 // x = A^-1 b per instance (the same inverse of nloc x nloc for all), one
 // warp per row: 32 strided partial sums then an xor butterfly; the CPU
 // oracle uses the same order.
-__global__ void k_coarse_matvec(int n, int nloc, const double* __restrict__ ainv, const double* __restrict__ b,
-                                double* __restrict__ x) {
+__global__ void k_coarse_matvec(int n, int nloc, ModeArg<const double> ainv_, ModeArg<const double> b_,
+                                ModeArg<double> x_) {
+  const double* __restrict__ ainv = ainv_.get();
+  const double* __restrict__ b = b_.get();
+  double* __restrict__ x = x_.get();
   const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (row >= n) return;
@@ -709,7 +736,9 @@ __global__ void k_coarse_matvec(int n, int nloc, const double* __restrict__ ainv
 
 template <typename T>
 __global__ void k_coarse_scatter(KTree t, int n, const int* __restrict__ cslot, const int* __restrict__ ccell,
-                                 const double* __restrict__ x, T* __restrict__ phi) {
+                                 ModeArg<const double> x_, ModeArg<T> phi_) {
+  const double* __restrict__ x = x_.get();
+  T* __restrict__ phi = phi_.get();
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
   const int slot = cslot[g];

@@ -24,12 +24,18 @@ namespace afg {
 // FMA chain (8 FP64 instructions per cell); r is rounded to FP32 by bit
 // truncation and its maximum taken in FP32.
 template <int D, bool CYL, int NC = 0>
-__global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict__ rec, double* __restrict__ phi,
-                                                const double* __restrict__ rhs, float* __restrict__ r32,
-                                                float* __restrict__ e32, MgCoef<double> mc, GcDev g,
+__global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict__ rec, ModeArg<double> phi_,
+                                                ModeArg<const double> rhs_, ModeArg<float> r32_,
+                                                ModeArg<float> e32_, ModeCoef<double> mc_, GcDev g,
                                                 const unsigned char* __restrict__ is_leaf,
-                                                unsigned long long* maxbits) {
+                                                ModeArg<unsigned long long> maxbits_) {
   const KTree t = fix_dims<D, NC>(t0);
+  double* __restrict__ phi = phi_.get();
+  const double* __restrict__ rhs = rhs_.get();
+  float* __restrict__ r32 = r32_.get();
+  float* __restrict__ e32 = e32_.get();
+  const MgCoef<double> mc = mc_.get();
+  unsigned long long* maxbits = maxbits_.get();
   __shared__ float sred[32];
   int4 r0, r1;
   load_rec(rec, blockIdx.x, r0, r1);
@@ -99,8 +105,10 @@ __global__ void __launch_bounds__(256) k_to_f64(int S, const int* __restrict__ l
 }
 
 // phi += e on whole boxes (ghost cells included)
-__global__ void __launch_bounds__(256) k_add_correction(KTree t, const int* __restrict__ list, double* __restrict__ phi,
-                                                        const float* __restrict__ e32) {
+__global__ void __launch_bounds__(256) k_add_correction(KTree t, const int* __restrict__ list, ModeArg<double> phi_,
+                                                        ModeArg<const float> e32_) {
+  double* __restrict__ phi = phi_.get();
+  const float* __restrict__ e32 = e32_.get();
   const int slot = list[blockIdx.x];
   if (box_frozen(t, slot)) return;
   const int S = t.S;
@@ -114,20 +122,24 @@ __global__ void __launch_bounds__(256) k_add_correction(KTree t, const int* __re
 // All boxes: the correction starts at zero everywhere (an FMG from zero
 // prolongs the change of the level-1 correction, so it must start at zero
 // there too); the defect itself is computed on leaves.
-static int launch_defect(afg_ctx* ctx, MgSlot& m, double* phi, const double* rhs, unsigned long long* maxbits) {
+static int launch_defect(afg_ctx* ctx, MgSlot& m, ModeArg<double> phi, ModeArg<const double> rhs,
+                         ModeArg<unsigned long long> maxbits) {
   const int n = ctx->n_all;
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   const int* list = rec_of(ctx, lst(ctx, ctx->off_all));
   const GcDev g = mg_gc(ctx, m, false);
+  const ModeArg<float> r32 = slot_bufs(ctx, m, &MgSlot::r32), e32 = slot_bufs(ctx, m, &MgSlot::e32);
+  const ModeCoef<double> c = coefs<double>(ctx, m);
+  const dim3 grid(n, ctx->ky);
   if (ctx->D == 3)
-    AFG_NC3(NCV_, k_defect<3, false, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), g, ctx->d_is_leaf,
+    AFG_NC3(NCV_, k_defect<3, false, NCV_><<<grid, 256, 0, ctx->stream>>>(t, list, phi, rhs, r32, e32, c, g, ctx->d_is_leaf,
                                                    maxbits));
   else if (ctx->coord == AFG_CYL)
-    AFG_NC2(NCV_, k_defect<2, true, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), g, ctx->d_is_leaf,
+    AFG_NC2(NCV_, k_defect<2, true, NCV_><<<grid, 256, 0, ctx->stream>>>(t, list, phi, rhs, r32, e32, c, g, ctx->d_is_leaf,
                                                   maxbits));
   else
-    AFG_NC2(NCV_, k_defect<2, false, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, m.r32, m.e32, coef64(m), g, ctx->d_is_leaf,
+    AFG_NC2(NCV_, k_defect<2, false, NCV_><<<grid, 256, 0, ctx->stream>>>(t, list, phi, rhs, r32, e32, c, g, ctx->d_is_leaf,
                                                    maxbits));
   ctx->launches++;
   CKL();
@@ -139,15 +151,16 @@ static int launch_defect(afg_ctx* ctx, MgSlot& m, double* phi, const double* rhs
 // restriction of their children (the FAS fixed point).  Before each defect
 // the parents are therefore restricted top-down (without geometry, as
 // mg_box_rstr_lpl does for phi) and the ghost cells refreshed.
-static int mixed_prepare(afg_ctx* ctx, MgSlot& m, double* phi) {
+static int mixed_prepare(afg_ctx* ctx, MgSlot& m, ModeArg<double> phi) {
   KTree t = ktree(ctx);
   for (int lvl = ctx->highest_lvl; lvl >= 2; lvl--) {
     const int n = (int)ctx->lvl_ids[lvl - 1].size();
     if (n == 0) continue;
+    const dim3 grid(n, ctx->ky);
     if (ctx->D == 3)
-      AFG_NC3(NCV_, k_restrict_geom<3, false, NCV_><<<n, 64, 0, ctx->stream>>>(t, lst(ctx, ctx->off_ids[lvl - 1]), phi));
+      AFG_NC3(NCV_, k_restrict_geom<3, false, NCV_><<<grid, 64, 0, ctx->stream>>>(t, lst(ctx, ctx->off_ids[lvl - 1]), phi));
     else
-      AFG_NC2(NCV_, k_restrict_geom<2, false, NCV_><<<n, 64, 0, ctx->stream>>>(t, lst(ctx, ctx->off_ids[lvl - 1]), phi));
+      AFG_NC2(NCV_, k_restrict_geom<2, false, NCV_><<<grid, 64, 0, ctx->stream>>>(t, lst(ctx, ctx->off_ids[lvl - 1]), phi));
     ctx->launches++;
     CKL();
   }
@@ -162,7 +175,7 @@ static int mixed_prepare(afg_ctx* ctx, MgSlot& m, double* phi) {
 }
 
 // all ghost cells of phi (faces, edges, corners) when the solve ends
-static int mixed_finish(afg_ctx* ctx, MgSlot& m, double* phi) {
+static int mixed_finish(afg_ctx* ctx, MgSlot& m, ModeArg<double> phi) {
   const GcDev g = mg_gc(ctx, m, false);
   for (int lvl = 1; lvl <= ctx->highest_lvl; lvl++) RC(mg_gc_lvl<double>(ctx, lvl, phi, g, 1));
   return AFG_OK;
@@ -175,18 +188,25 @@ static int mixed_finish(afg_ctx* ctx, MgSlot& m, double* phi) {
 // from zero, so the first correction is the whole solution.  Repeated calls
 // converge like FP64 FMG cycles down to FP64 accuracy: each FP32 FMG only
 // has to reduce the current defect, not resolve phi itself.
-static int mixed_fmg(afg_ctx* ctx, MgSlot& m, double* phi, double* rhs, bool set_residual, bool have_guess,
-                     unsigned long long* maxbits) {
+// (lockstep slots: phi, rhs and maxbits per slot, the FP32 buffers of
+// each slot)
+static int mixed_fmg(afg_ctx* ctx, MgSlot& m, ModeArg<double> phi, ModeArg<double> rhs, bool set_residual,
+                     bool have_guess, ModeArg<unsigned long long> maxbits) {
   const int n = ctx->n_all_leaves;
   if (n <= 0) return AFG_OK;
   // phi += e on the leaves; the parents are restricted from them next
   const int* list = lst(ctx, ctx->off_all_leaves);
-  if (!have_guess) CK(cudaMemsetAsync(phi, 0, sizeof(double) * (size_t)ctx->n_boxes * ctx->S, ctx->stream));
+  if (!have_guess)
+    for (int k = 0; k < ctx->ky; k++)
+      CK(cudaMemsetAsync(phi.p[k], 0, sizeof(double) * (size_t)ctx->n_boxes * ctx->S, ctx->stream));
   RC(mixed_prepare(ctx, m, phi));
   RC(reset_max(ctx, 2));
-  RC(launch_defect(ctx, m, phi, rhs, ctx->d_max + 2));
-  RC(mg_fmg<float>(ctx, m, m.e32, m.r32, m.t32, false, false, nullptr, true));
-  k_add_correction<<<n, 256, 0, ctx->stream>>>(ktree(ctx), list, phi, m.e32);
+  // the first defect's maximum is not used: every slot folds it into word 2
+  RC(launch_defect(ctx, m, phi, rhs, ModeArg<unsigned long long>(ctx->d_max + 2)));
+  RC(mg_fmg<float>(ctx, m, slot_bufs(ctx, m, &MgSlot::e32), slot_bufs(ctx, m, &MgSlot::r32),
+                   slot_bufs(ctx, m, &MgSlot::t32), false, false, nullptr, true));
+  k_add_correction<<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(ktree(ctx), list, phi,
+                                                             ModeArg<const float>(slot_bufs(ctx, m, &MgSlot::e32)));
   ctx->launches++;
   CKL();
   RC(mixed_prepare(ctx, m, phi));

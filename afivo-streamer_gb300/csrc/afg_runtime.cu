@@ -136,6 +136,12 @@ struct afg_ctx {
   // smoother work shape (cells of a colour per thread) for the specialized
   // box sizes: [0] FP32, [1] FP64; picked by the autotuner, 0 = default
   int gsrb_cpt[2] = {0, 0};
+  // lockstep problems (Helmholtz modes as multiple right-hand sides): while
+  // ky > 1 every multigrid launch covers the slots grp[0..ky-1], blockIdx.y
+  // selecting the slot; ky = 1 otherwise
+  int ky = 1;
+  MgSlot* grp[kMaxModes] = {};
+  bool photoi_lockstep = true;  // Helmholtz modes in lockstep (else parallel branches)
   // asynchronous downloads (afg_cc_download_async)
   cudaStream_t xfer_stream = nullptr;
   cudaEvent_t ev_xfer = nullptr;
@@ -311,15 +317,15 @@ static void free_tree(afg_ctx* c) {
 // Generic launchers dispatching on (D, cylindrical, T)
 
 template <typename T>
-static int launch_gc(afg_ctx* ctx, const int* list, int n, T* v, const GcDev& g, int corners) {
+static int launch_gc(afg_ctx* ctx, const int* list, int n, ModeArg<T> v, const GcDev& g, int corners) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   kt_begin(ctx, AFG_KT_GHOST);
   if (ctx->D == 2)
-    AFG_NC2(NCV_, k_gc<2, T, NCV_><<<n, 128, 0, ctx->stream>>>(t, rec_of(ctx, list), v, g, corners));
+    AFG_NC2(NCV_, k_gc<2, T, NCV_><<<dim3(n, ctx->ky), 128, 0, ctx->stream>>>(t, rec_of(ctx, list), v, g, corners));
   else
-    AFG_NC3(NCV_, k_gc<3, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, rec_of(ctx, list), v, g, corners));
-  kt_end(ctx, AFG_KT_GHOST, 2.0 * sizeof(T) * n * 2 * ctx->D * (box_cells(ctx) / ctx->nc));
+    AFG_NC3(NCV_, k_gc<3, T, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, rec_of(ctx, list), v, g, corners));
+  kt_end(ctx, AFG_KT_GHOST, 2.0 * sizeof(T) * n * ctx->ky * 2 * ctx->D * (box_cells(ctx) / ctx->nc));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -356,8 +362,8 @@ static int gsrb_cpt_of(const afg_ctx* ctx) {
 // Persistent grid of the shared-memory-staged smoother: as many CTAs as fit
 // on the GPU at once (occupancy of the instantiation with its shared memory)
 template <int D, bool CYL, typename T, int NC, int CPT, bool SR>
-static int launch_gsrb_tma(afg_ctx* ctx, const int* rec, int n, T* phi, const T* rhs, int rb, MgCoef<T> lam,
-                           const GcDev& g) {
+static int launch_gsrb_tma(afg_ctx* ctx, const int* rec, int n, ModeArg<T> phi, ModeArg<const T> rhs, int rb,
+                           ModeCoef<T> lam, const GcDev& g) {
   constexpr int TPB = (D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT;
   constexpr int S = D == 2 ? (NC + 2) * (NC + 2) : (NC + 2) * (NC + 2) * (NC + 2);
   constexpr size_t smem = (SR ? 4 : 2) * S * sizeof(T);
@@ -366,15 +372,15 @@ static int launch_gsrb_tma(afg_ctx* ctx, const int* rec, int n, T* phi, const T*
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gsrb_tma<D, CYL, T, NC, CPT, SR>, TPB, smem));
     per_sm = std::max(1, per_sm);
   }
-  const int grid = std::min(n, per_sm * ctx->n_sm);
-  k_gsrb_tma<D, CYL, T, NC, CPT, SR><<<grid, TPB, smem, ctx->stream>>>(ktree(ctx), rec, n, phi, rhs, rb, lam, g,
-                                                                       ctx->d_err);
+  const int grid = std::min(n, std::max(1, per_sm * ctx->n_sm / ctx->ky));
+  k_gsrb_tma<D, CYL, T, NC, CPT, SR><<<dim3(grid, ctx->ky), TPB, smem, ctx->stream>>>(ktree(ctx), rec, n, phi, rhs,
+                                                                                      rb, lam, g, ctx->d_err);
   return AFG_OK;
 }
 
 template <int D, bool CYL, typename T, int NC, int CPT>
-static int launch_gsrb_tma(afg_ctx* ctx, bool sr, const int* rec, int n, T* phi, const T* rhs, int rb,
-                           MgCoef<T> lam, const GcDev& g) {
+static int launch_gsrb_tma(afg_ctx* ctx, bool sr, const int* rec, int n, ModeArg<T> phi, ModeArg<const T> rhs,
+                           int rb, ModeCoef<T> lam, const GcDev& g) {
   return sr ? launch_gsrb_tma<D, CYL, T, NC, CPT, true>(ctx, rec, n, phi, rhs, rb, lam, g)
             : launch_gsrb_tma<D, CYL, T, NC, CPT, false>(ctx, rec, n, phi, rhs, rb, lam, g);
 }
@@ -385,8 +391,8 @@ static int launch_gsrb_tma(afg_ctx* ctx, bool sr, const int* rec, int n, T* phi,
 // | kGsrbTmaRhs the right-hand side staged too
 constexpr int kGsrbTma = 16, kGsrbTmaRhs = 32;
 template <typename T>
-static int launch_gsrb_rec(afg_ctx* ctx, const int* rec, int n, T* phi, const T* rhs, int rb, MgCoef<T> lam,
-                           const GcDev& g, int cpt) {
+static int launch_gsrb_rec(afg_ctx* ctx, const int* rec, int n, ModeArg<T> phi, ModeArg<const T> rhs, int rb,
+                           ModeCoef<T> lam, const GcDev& g, int cpt) {
   KTree t = ktree(ctx);
   if (cpt & kGsrbTma) {
     const int c = cpt & (kGsrbTma - 1);
@@ -407,22 +413,22 @@ static int launch_gsrb_rec(afg_ctx* ctx, const int* rec, int n, T* phi, const T*
   }
   if (ctx->D == 3) {
     switch (cpt) {
-      case 1: k_gsrb_rec<3, false, T, 8, 1><<<n, 256, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
-      case 2: k_gsrb_rec<3, false, T, 8, 2><<<n, 128, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
-      case 8: k_gsrb_rec<3, false, T, 8, 8><<<n, 32, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
-      default: k_gsrb_rec<3, false, T, 8, 4><<<n, 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      case 1: k_gsrb_rec<3, false, T, 8, 1><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      case 2: k_gsrb_rec<3, false, T, 8, 2><<<dim3(n, ctx->ky), 128, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      case 8: k_gsrb_rec<3, false, T, 8, 8><<<dim3(n, ctx->ky), 32, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      default: k_gsrb_rec<3, false, T, 8, 4><<<dim3(n, ctx->ky), 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
     }
   } else if (ctx->coord == AFG_CYL) {
     switch (cpt) {
-      case 1: k_gsrb_rec<2, true, T, 16, 1><<<n, 128, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
-      case 4: k_gsrb_rec<2, true, T, 16, 4><<<n, 32, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
-      default: k_gsrb_rec<2, true, T, 16, 2><<<n, 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      case 1: k_gsrb_rec<2, true, T, 16, 1><<<dim3(n, ctx->ky), 128, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      case 4: k_gsrb_rec<2, true, T, 16, 4><<<dim3(n, ctx->ky), 32, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      default: k_gsrb_rec<2, true, T, 16, 2><<<dim3(n, ctx->ky), 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
     }
   } else {
     switch (cpt) {
-      case 1: k_gsrb_rec<2, false, T, 16, 1><<<n, 128, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
-      case 4: k_gsrb_rec<2, false, T, 16, 4><<<n, 32, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
-      default: k_gsrb_rec<2, false, T, 16, 2><<<n, 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      case 1: k_gsrb_rec<2, false, T, 16, 1><<<dim3(n, ctx->ky), 128, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      case 4: k_gsrb_rec<2, false, T, 16, 4><<<dim3(n, ctx->ky), 32, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
+      default: k_gsrb_rec<2, false, T, 16, 2><<<dim3(n, ctx->ky), 64, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g); break;
     }
   }
   CKL();
@@ -430,8 +436,8 @@ static int launch_gsrb_rec(afg_ctx* ctx, const int* rec, int n, T* phi, const T*
 }
 
 template <typename T>
-static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, int rb, MgCoef<T> lam,
-                             const GcDev& g) {
+static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, ModeArg<const T> rhs, int rb,
+                             ModeCoef<T> lam, const GcDev& g) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   const int threads = ctx->D == 2 ? std::min(256, ctx->nc * ctx->nc / 2) : std::min(256, ctx->nc * ctx->nc * ctx->nc / 2);
@@ -441,14 +447,14 @@ static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, T* phi, const
     const int rc = launch_gsrb_rec<T>(ctx, rec_of(ctx, list), n, phi, rhs, rb, lam, g, gsrb_cpt_of<T>(ctx));
     if (rc != AFG_OK) return rc;
   } else if (ctx->D == 3)
-    k_gsrb_fused<3, false, T, 0><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
+    k_gsrb_fused<3, false, T, 0><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
   else if (ctx->coord == AFG_CYL)
-    k_gsrb_fused<2, true, T, 0><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
+    k_gsrb_fused<2, true, T, 0><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
   else
-    k_gsrb_fused<2, false, T, 0><<<n, threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
+    k_gsrb_fused<2, false, T, 0><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, list, phi, rhs, rb, lam, g);
   // algorithmic bytes: 3 words per cell per full iteration (read phi and
   // rhs, write phi), 1.5 words per half sweep
-  kt_end(ctx, AFG_KT_GSRB, 1.5 * sizeof(T) * n * box_cells(ctx));
+  kt_end(ctx, AFG_KT_GSRB, 1.5 * sizeof(T) * n * ctx->ky * box_cells(ctx));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -471,72 +477,72 @@ static int launch_residual(afg_ctx* ctx, const int* list, int n, const T* phi, c
 }
 
 template <typename T>
-static int launch_rrestrict(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, T* tmp, MgCoef<T> lam,
-                            int store_child, const GcDev& g, int otf) {
+static int launch_rrestrict(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, ModeArg<const T> rhs,
+                            ModeArg<T> tmp, ModeCoef<T> lam, int store_child, const GcDev& g, int otf) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   const int hnc = ctx->nc / 2;
   const int threads = std::max(32, std::min(256, ctx->D == 2 ? hnc * hnc : hnc * hnc * hnc));
   if (ctx->D == 3)
-    AFG_NC3(NCV_, k_residual_restrict<3, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, store_child, g, otf));
+    AFG_NC3(NCV_, k_residual_restrict<3, false, T, NCV_><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, store_child, g, otf));
   else if (ctx->coord == AFG_CYL)
-    AFG_NC2(NCV_, k_residual_restrict<2, true, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, store_child, g, otf));
+    AFG_NC2(NCV_, k_residual_restrict<2, true, T, NCV_><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, store_child, g, otf));
   else
-    AFG_NC2(NCV_, k_residual_restrict<2, false, T, NCV_><<<n, threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, store_child, g, otf));
+    AFG_NC2(NCV_, k_residual_restrict<2, false, T, NCV_><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, store_child, g, otf));
   ctx->launches++;
   CKL();
   return AFG_OK;
 }
 
 template <typename T>
-static int launch_coarse_fas(afg_ctx* ctx, const int* list, int n, T* phi, T* rhs, T* tmp, MgCoef<T> lam,
-                             int copy_tmp, int fill, const GcDev& g) {
+static int launch_coarse_fas(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, ModeArg<T> rhs, ModeArg<T> tmp,
+                             ModeCoef<T> lam, int copy_tmp, int fill, const GcDev& g) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   if (ctx->D == 3)
-    AFG_NC3(NCV_, k_coarse_fas<3, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, copy_tmp, fill, g));
+    AFG_NC3(NCV_, k_coarse_fas<3, false, T, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, copy_tmp, fill, g));
   else if (ctx->coord == AFG_CYL)
-    AFG_NC2(NCV_, k_coarse_fas<2, true, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, copy_tmp, fill, g));
+    AFG_NC2(NCV_, k_coarse_fas<2, true, T, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, copy_tmp, fill, g));
   else
-    AFG_NC2(NCV_, k_coarse_fas<2, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, copy_tmp, fill, g));
+    AFG_NC2(NCV_, k_coarse_fas<2, false, T, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, copy_tmp, fill, g));
   ctx->launches++;
   CKL();
   return AFG_OK;
 }
 
 template <typename T>
-static int launch_correct(afg_ctx* ctx, const int* list, int n, T* phi, T* tmp) {
+static int launch_correct(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, ModeArg<T> tmp) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   const size_t sm = sizeof(T) * ctx->S;
   if (ctx->D == 3)
-    AFG_NC3(NCV_, k_correct<3, T, NCV_><<<n, 256, sm, ctx->stream>>>(t, list, phi, tmp));
+    AFG_NC3(NCV_, k_correct<3, T, NCV_><<<dim3(n, ctx->ky), 256, sm, ctx->stream>>>(t, list, phi, tmp));
   else
-    AFG_NC2(NCV_, k_correct<2, T, NCV_><<<n, 256, sm, ctx->stream>>>(t, list, phi, tmp));
+    AFG_NC2(NCV_, k_correct<2, T, NCV_><<<dim3(n, ctx->ky), 256, sm, ctx->stream>>>(t, list, phi, tmp));
   ctx->launches++;
   CKL();
   return AFG_OK;
 }
 
 template <typename T>
-static int launch_init_phi_rhs(afg_ctx* ctx, const int* list, int n, T* phi, T* rhs) {
+static int launch_init_phi_rhs(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, ModeArg<T> rhs) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   if (ctx->D == 3)
-    AFG_NC3(NCV_, k_init_phi_rhs<3, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs));
+    AFG_NC3(NCV_, k_init_phi_rhs<3, false, T, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, list, phi, rhs));
   else if (ctx->coord == AFG_CYL)
-    AFG_NC2(NCV_, k_init_phi_rhs<2, true, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs));
+    AFG_NC2(NCV_, k_init_phi_rhs<2, true, T, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, list, phi, rhs));
   else
-    AFG_NC2(NCV_, k_init_phi_rhs<2, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs));
+    AFG_NC2(NCV_, k_init_phi_rhs<2, false, T, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, list, phi, rhs));
   ctx->launches++;
   CKL();
   return AFG_OK;
 }
 
 template <typename T>
-static int launch_copy(afg_ctx* ctx, const int* list, int n, const T* src, T* dst) {
+static int launch_copy(afg_ctx* ctx, const int* list, int n, ModeArg<const T> src, ModeArg<T> dst) {
   if (n <= 0) return AFG_OK;
-  k_copy<T><<<n, 256, 0, ctx->stream>>>(ktree(ctx), list, src, dst);
+  k_copy<T><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(ktree(ctx), list, src, dst);
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -609,11 +615,26 @@ static std::string gkey(const char* tag, int a = 0, int b = 0, int c = 0, int d 
 /* ------------------------------------------------------------------------- */
 // Multigrid drivers (templated on the working precision T)
 
-struct MgVars {
-  void* phi;
-  void* rhs;
-  void* tmp;
-};
+// Operator coefficients of slot m, or of every lockstep slot grp[0..ky-1]
+// (grp[0] is m) for a launch covering them
+template <typename T>
+static ModeCoef<T> coefs(const afg_ctx* ctx, const MgSlot& m) {
+  ModeCoef<T> c(coef_of<T>(m));
+  for (int k = 1; k < ctx->ky; k++) {
+    const MgCoef<T> q = coef_of<T>(*ctx->grp[k]);
+    c.cb[k] = q.cb;
+    c.cy[k] = q.cy;
+  }
+  return c;
+}
+
+// a per-slot buffer (member `f` of MgSlot) of m, or of every lockstep slot
+template <typename T>
+static ModeArg<T> slot_bufs(const afg_ctx* ctx, const MgSlot& m, T* MgSlot::*f) {
+  ModeArg<T> a(m.*f);
+  for (int k = 1; k < ctx->ky; k++) a.p[k] = ctx->grp[k]->*f;
+  return a;
+}
 
 // Ghost-cell method of a multigrid slot's phi; on batched trees the boundary
 // values are read per instance from the slot's device rows.
@@ -629,27 +650,28 @@ static GcDev mg_gc(const afg_ctx* ctx, const MgSlot& m, bool homogeneous) {
 }
 
 template <typename T>
-static int mg_gc_lvl(afg_ctx* ctx, int lvl, T* phi, const GcDev& g, int corners) {
+static int mg_gc_lvl(afg_ctx* ctx, int lvl, ModeArg<T> phi, const GcDev& g, int corners) {
   return launch_gc<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, g, corners);
 }
 
 // gsrb_boxes, m_af_multigrid.f90:648-687
 template <typename T>
-static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, T* phi, const T* rhs, const GcDev& g,
-                         bool fill_down = true, bool fill_needed_only = false) {
+static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, ModeArg<T> phi, ModeArg<const T> rhs,
+                         const GcDev& g, bool fill_down = true, bool fill_needed_only = false) {
   const int n_cycle = type == AFG_CYCLE_DOWN ? m.d.n_cycle_down : m.d.n_cycle_up;
   const int* list = lst(ctx, ctx->off_ids[lvl - 1]);
   const int n = (int)ctx->lvl_ids[lvl - 1].size();
-  ctx->ctr[1] += (long long)n * (long long)box_cells(ctx) * n_cycle;
+  ctx->ctr[1] += (long long)n * (long long)box_cells(ctx) * n_cycle * ctx->ky;
   if (ctx->fused_gsrb) {
-    for (int it = 1; it <= 2 * n_cycle; it++) RC(launch_gsrb_fused<T>(ctx, list, n, phi, rhs, it, coef_of<T>(m), g));
+    for (int it = 1; it <= 2 * n_cycle; it++) RC(launch_gsrb_fused<T>(ctx, list, n, phi, rhs, it, coefs<T>(ctx, m), g));
     if (type == AFG_CYCLE_DOWN && !fill_down) return AFG_OK;
     if (type != AFG_CYCLE_DOWN && fill_needed_only)
       return launch_gc<T>(ctx, lst(ctx, ctx->off_gcneed[lvl - 1]), (int)ctx->lvl_gcneed[lvl - 1].size(), phi, g, 1);
     return launch_gc<T>(ctx, list, n, phi, g, type != AFG_CYCLE_DOWN ? 1 : 0);
   }
+  // unfused reference order (one problem at a time)
   for (int it = 1; it <= 2 * n_cycle; it++) {
-    RC(launch_gsrb<T>(ctx, list, n, phi, rhs, it, coef_of<T>(m)));
+    RC(launch_gsrb<T>(ctx, list, n, phi.p[0], rhs.p[0], it, coef_of<T>(m)));
     const int corners = (type != AFG_CYCLE_DOWN && it == 2 * n_cycle) ? 1 : 0;
     RC(launch_gc<T>(ctx, list, n, phi, g, corners));
   }
@@ -662,24 +684,25 @@ static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, T* ph
 // computed on the fly, so lvl needs no ghost fill after its down smoothing
 // (the V-cycle); otherwise the stored ghost cells are used as they are.
 template <typename T>
-static int mg_update_coarse(afg_ctx* ctx, const MgSlot& m, int lvl, T* phi, T* rhs, T* tmp, const GcDev& g,
-                            bool otf = true) {
+static int mg_update_coarse(afg_ctx* ctx, const MgSlot& m, int lvl, ModeArg<T> phi, ModeArg<T> rhs, ModeArg<T> tmp,
+                            const GcDev& g, bool otf = true) {
   RC(launch_rrestrict<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs, tmp,
-                         coef_of<T>(m), 0, g, otf ? 1 : 0));
+                         coefs<T>(ctx, m), 0, g, otf ? 1 : 0));
   RC(launch_coarse_fas<T>(ctx, lst(ctx, ctx->off_parents[lvl - 2]), (int)ctx->lvl_parents[lvl - 2].size(), phi, rhs,
-                          tmp, coef_of<T>(m), 1, 1, g));
+                          tmp, coefs<T>(ctx, m), 1, 1, g));
   return AFG_OK;
 }
 
 // set_coarse_phi_rhs, m_af_multigrid.f90:742-776
 template <typename T>
-static int mg_set_coarse_phi_rhs(afg_ctx* ctx, const MgSlot& m, int lvl, T* phi, T* rhs, T* tmp, const GcDev& g) {
+static int mg_set_coarse_phi_rhs(afg_ctx* ctx, const MgSlot& m, int lvl, ModeArg<T> phi, ModeArg<T> rhs,
+                                 ModeArg<T> tmp, const GcDev& g) {
   if (lvl == ctx->highest_lvl) RC(mg_gc_lvl<T>(ctx, lvl, phi, g, 1));
   RC(launch_rrestrict<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs, tmp,
-                         coef_of<T>(m), 1, g, 0));
+                         coefs<T>(ctx, m), 1, g, 0));
   RC(mg_gc_lvl<T>(ctx, lvl - 1, phi, g, 1));
   RC(launch_coarse_fas<T>(ctx, lst(ctx, ctx->off_parents[lvl - 2]), (int)ctx->lvl_parents[lvl - 2].size(), phi, rhs,
-                          tmp, coef_of<T>(m), 0, 0, g));
+                          tmp, coefs<T>(ctx, m), 0, 0, g));
   return AFG_OK;
 }
 
@@ -690,7 +713,7 @@ static int mg_set_coarse_phi_rhs(afg_ctx* ctx, const MgSlot& m, int lvl, T* phi,
 // fill is skipped (fill = false), the stored ghost cells of lvl being read
 // by nothing in between.
 template <typename T>
-static int mg_correct(afg_ctx* ctx, int lvl, T* phi, T* tmp, const GcDev& g, bool fill = true) {
+static int mg_correct(afg_ctx* ctx, int lvl, ModeArg<T> phi, ModeArg<T> tmp, const GcDev& g, bool fill = true) {
   RC(launch_correct<T>(ctx, lst(ctx, ctx->off_parents[lvl - 2]), (int)ctx->lvl_parents[lvl - 2].size(), phi, tmp));
   if (fill) RC(mg_gc_lvl<T>(ctx, lvl, phi, g, 1));
   return AFG_OK;
@@ -698,20 +721,27 @@ static int mg_correct(afg_ctx* ctx, int lvl, T* phi, T* tmp, const GcDev& g, boo
 
 // solve_coarse_grid, m_af_multigrid.f90:266-291 (exact FP64 solve)
 // (batched trees: every instance's coarse grid with the shared inverse and
-// its own boundary values)
+// its own boundary values; lockstep slots: each its own inverse and vectors,
+// the boundary tables and values those of m, equal for all of them)
 template <typename T>
-static int mg_coarse_solve(afg_ctx* ctx, MgSlot& m, T* phi, const T* rhs, const GcDev& g, bool homogeneous) {
+static int mg_coarse_solve(afg_ctx* ctx, MgSlot& m, ModeArg<T> phi, ModeArg<const T> rhs, const GcDev& g,
+                           bool homogeneous) {
   const int nloc = m.n_coarse, rows = inst_rows(ctx), n = nloc * rows;
   const double* bcv = m.d_bcval + (homogeneous ? 6 * rows : 0);
   const int stride = homogeneous ? 0 : 6;
-  k_coarse_gather<T><<<(n + 127) / 128, 128, 0, ctx->stream>>>(n, nloc, ctx->D, ctx->d_cslot, ctx->d_ccell, m.d_b2r,
-                                                               m.d_bmask, bcv, stride, rhs, ctx->S, m.d_b);
+  const ModeArg<double> b = slot_bufs(ctx, m, &MgSlot::d_b), x = slot_bufs(ctx, m, &MgSlot::d_x);
+  ModeArg<const double> ainv(m.d_ainv);
+  for (int k = 1; k < ctx->ky; k++) ainv.p[k] = ctx->grp[k]->d_ainv;
+  const dim3 g128((n + 127) / 128, ctx->ky), g8((n + 7) / 8, ctx->ky);
+  k_coarse_gather<T><<<g128, 128, 0, ctx->stream>>>(n, nloc, ctx->D, ctx->d_cslot, ctx->d_ccell, m.d_b2r, m.d_bmask,
+                                                    bcv, stride, rhs, ctx->S, b);
   ctx->launches++;
   CKL();
-  k_coarse_matvec<<<(n + 7) / 8, 256, 0, ctx->stream>>>(n, nloc, m.d_ainv, m.d_b, m.d_x);
+  k_coarse_matvec<<<g8, 256, 0, ctx->stream>>>(n, nloc, ainv, ModeArg<const double>(b), x);
   ctx->launches++;
   CKL();
-  k_coarse_scatter<T><<<(n + 127) / 128, 128, 0, ctx->stream>>>(ktree(ctx), n, ctx->d_cslot, ctx->d_ccell, m.d_x, phi);
+  k_coarse_scatter<T><<<g128, 128, 0, ctx->stream>>>(ktree(ctx), n, ctx->d_cslot, ctx->d_ccell,
+                                                     ModeArg<const double>(x), phi);
   ctx->launches++;
   CKL();
   return mg_gc_lvl<T>(ctx, 1, phi, g, 1);
@@ -739,12 +769,13 @@ static int mg_residual_lvls(afg_ctx* ctx, const MgSlot& m, int max_lvl, const T*
   return AFG_OK;
 }
 
-// mg_fas_vcycle, m_af_multigrid.f90:185-264
+// mg_fas_vcycle, m_af_multigrid.f90:185-264 (the residual, set_residual,
+// for one problem at a time)
 template <typename T>
-static int mg_vcycle(afg_ctx* ctx, MgSlot& m, int max_lvl, T* phi, T* rhs, T* tmp, bool set_residual,
-                     bool homogeneous, unsigned long long* maxbits) {
+static int mg_vcycle(afg_ctx* ctx, MgSlot& m, int max_lvl, ModeArg<T> phi, ModeArg<T> rhs, ModeArg<T> tmp,
+                     bool set_residual, bool homogeneous, unsigned long long* maxbits) {
   const GcDev g = mg_gc(ctx, m, homogeneous);
-  ctx->ctr[3]++;
+  ctx->ctr[3] += ctx->ky;
   for (int lvl = max_lvl; lvl >= 2; lvl--) {
     // the restriction below computes the face neighbours it needs itself
     RC(mg_gsrb_boxes<T>(ctx, m, lvl, AFG_CYCLE_DOWN, phi, rhs, g, false));
@@ -760,14 +791,14 @@ static int mg_vcycle(afg_ctx* ctx, MgSlot& m, int max_lvl, T* phi, T* rhs, T* tm
     RC(mg_correct<T>(ctx, lvl, phi, tmp, g, !ctx->fused_gsrb));
     RC(mg_gsrb_boxes<T>(ctx, m, lvl, AFG_CYCLE_UP, phi, rhs, g, true, needed_only));
   }
-  if (set_residual) RC(mg_residual_lvls<T>(ctx, m, max_lvl, phi, rhs, tmp, maxbits));
+  if (set_residual) RC(mg_residual_lvls<T>(ctx, m, max_lvl, phi.p[0], rhs.p[0], tmp.p[0], maxbits));
   return AFG_OK;
 }
 
 // mg_fas_fmg, m_af_multigrid.f90:137-180
 template <typename T>
-static int mg_fmg(afg_ctx* ctx, MgSlot& m, T* phi, T* rhs, T* tmp, bool set_residual, bool have_guess,
-                  unsigned long long* maxbits, bool homogeneous = false) {
+static int mg_fmg(afg_ctx* ctx, MgSlot& m, ModeArg<T> phi, ModeArg<T> rhs, ModeArg<T> tmp, bool set_residual,
+                  bool have_guess, unsigned long long* maxbits, bool homogeneous = false) {
   const GcDev g = mg_gc(ctx, m, homogeneous);
   const int H = ctx->highest_lvl;
   if (have_guess) {
@@ -799,7 +830,7 @@ static int mg_fmg(afg_ctx* ctx, MgSlot& m, T* phi, T* rhs, T* tmp, bool set_resi
     RC(mg_vcycle<T>(ctx, m, lvl, phi, rhs, tmp, false, homogeneous, maxbits));
     if (set_residual) {
       RC(inst_mask(ctx, lvl, lvl));
-      RC(mg_residual_lvls<T>(ctx, m, lvl, phi, rhs, tmp, maxbits));
+      RC(mg_residual_lvls<T>(ctx, m, lvl, phi.p[0], rhs.p[0], tmp.p[0], maxbits));
     }
   }
   return inst_mask(ctx, 0, INT_MAX);
@@ -2115,6 +2146,12 @@ int afg_mg_solve_inst(afg_ctx* ctx, int mg_id, const double* threshold, int max_
 }
 
 int afg_n_instances(const afg_ctx* ctx) { return ctx ? ctx->n_inst : 0; }
+
+int afg_set_photoi_lockstep(afg_ctx* ctx, int on) {
+  if (!ctx) return AFG_ERR_ARG;
+  ctx->photoi_lockstep = on != 0;
+  return AFG_OK;
+}
 
 int afg_tree_copy_cc(afg_ctx* ctx, int iv_from, int iv_to) {
   RC(check_var(ctx, iv_from));

@@ -121,8 +121,9 @@ struct FluxArgs {
 
 // af_restrict_box with geometry of one variable (m_af_restrict.f90:62-136)
 template <int D, bool CYL, int NC = 0>
-__global__ void __launch_bounds__(256) k_restrict_geom(KTree t0, const int* __restrict__ list, double* __restrict__ v) {
+__global__ void __launch_bounds__(256) k_restrict_geom(KTree t0, const int* __restrict__ list, ModeArg<double> v_) {
   const KTree t = fix_dims<D, NC>(t0);
+  double* __restrict__ v = v_.get();
   const int slot = list[blockIdx.x];
   if (box_frozen(t, slot)) return;
   const int pslot = t.parent[slot];

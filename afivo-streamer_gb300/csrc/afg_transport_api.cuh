@@ -686,7 +686,52 @@ int afg_photoi_helmh(afg_ctx* ctx, double coeff, int n_modes, const int* mg_ids,
     for (int q = 0; q < n; q++)
       if (mg_ids[q] == mg_ids[n]) all_mixed = false;
   }
-  if (all_mixed) {
+  // Lockstep (multiple right-hand sides in one sweep): modes with the same
+  // boundary conditions and cycle counts run every launch of their
+  // defect-correction FMG together, blockIdx.y selecting the mode; converged
+  // modes leave the set, as in the per-mode loop.  Each mode's arithmetic is
+  // the same as alone, so the results are too.
+  bool lockstep = all_mixed && ctx->photoi_lockstep && ctx->fused_gsrb && n_modes <= kMaxModes;
+  for (int n = 1; lockstep && n < n_modes; n++) {
+    const afg_mg_desc &a = ctx->mg[mg_ids[0]].d, &b = ctx->mg[mg_ids[n]].d;
+    lockstep = a.n_cycle_down == b.n_cycle_down && a.n_cycle_up == b.n_cycle_up;
+    for (int q = 0; q < 6; q++) lockstep = lockstep && a.bc_type[q] == b.bc_type[q] && a.bc_val[q] == b.bc_val[q];
+  }
+  if (lockstep) {
+    std::vector<int> active(n_modes);
+    for (int n = 0; n < n_modes; n++) active[n] = n;
+    for (int it = 0; it < max_fmg_cycles && !active.empty(); it++) {
+      int mask = 0;
+      for (int n : active) mask |= 1 << n;
+      ModeArg<double> phi, rhs;
+      ModeArg<unsigned long long> mx;
+      for (size_t q = 0; q < active.size(); q++) {
+        MgSlot* m = &ctx->mg[mg_ids[active[q]]];
+        ctx->grp[q] = m;
+        phi.p[q] = ctx->cc[m->d.i_phi - 1];
+        rhs.p[q] = ctx->cc[m->d.i_rhs - 1];
+        mx.p[q] = ctx->d_max + kModeSlot + active[q];
+      }
+      ctx->ky = (int)active.size();
+      const int rc = run_graph(ctx, gkey("photoi_lockstep", mask, mg_ids[0], n_modes), [&]() -> int {
+        for (int n : active) RC(reset_max(ctx, kModeSlot + n));
+        return mixed_fmg(ctx, *ctx->grp[0], phi, rhs, true, true, mx);
+      });
+      ctx->ky = 1;
+      for (auto& g : ctx->grp) g = nullptr;
+      RC(rc);
+      CK(cudaMemcpyAsync(ctx->h_max + kModeSlot, ctx->d_max + kModeSlot, sizeof(unsigned long long) * n_modes,
+                         cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+      std::vector<int> still;
+      for (int n : active) {
+        double res;
+        memcpy(&res, ctx->h_max + kModeSlot + n, sizeof(double));
+        if (!(res / max_rhs < max_rel_residual)) still.push_back(n);
+      }
+      active.swap(still);
+    }
+  } else if (all_mixed) {
     // Mixed-precision modes own all the buffers they write (phi_n, the FP32
     // correction, right-hand side and tmp, the coarse-solve vectors) and only
     // read the shared source, so their FMG cycles run as parallel branches

@@ -419,6 +419,12 @@ int afg_field_compute_inst(afg_ctx* ctx, int mg_id, int s_in, int have_guess,
 int afg_photoi_helmh(afg_ctx* ctx, double coeff, int n_modes, const int* mg_ids,
                      const double* coeffs, double max_rel_residual,
                      int max_fmg_cycles);
+/* How afg_photoi_helmh advances AFG_MIXED modes (at most 8, with the same
+ * boundary conditions and cycle counts): on != 0 (default) in lockstep, as
+ * multiple right-hand sides of one FMG whose every launch covers all modes
+ * not yet converged; on == 0 as parallel CUDA-graph branches, one per mode.
+ * Both give the same results.  No counterpart in the reference. */
+int afg_set_photoi_lockstep(afg_ctx* ctx, int on);
 
 /* af_tree_copy_cc (afivo/src/m_af_utils.f90:590-598): whole-array copy of
  * variable iv_from to iv_to on all boxes (used by copy_current_state,
