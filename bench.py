@@ -279,7 +279,9 @@ def run_gpu_arm(args, device, w):
         c0 = ctx.counters()
         if args.profile:
             cuda_profiler(True)
+        photo_steps = []
         for _ in range(args.steps):
+            photo_steps.append(run.photoi is not None and run.it % run.photoi_per_steps == 0)
             ctx.flush_l2(256 << 20)
             ctx.event_record(0)
             run.step()
@@ -296,7 +298,12 @@ def run_gpu_arm(args, device, w):
         res = dict(ms_per_step=t_ms / args.steps, value=work / (t_ms * 1e-3), vcycles_per_step=vcycles / args.steps,
                    launches=c1["launches"] - c0["launches"],
                    launches_per_step=(c1["launches"] - c0["launches"]) / args.steps,
-                   clocks=clk, work_per_step=work / args.steps)
+                   clocks=clk, work_per_step=work / args.steps,
+                   step_ms=[round(x, 3) for x in times],
+                   photoi_step_ms=(float(np.mean([x for x, p in zip(times, photo_steps) if p]))
+                                   if any(photo_steps) else None),
+                   plain_step_ms=(float(np.mean([x for x, p in zip(times, photo_steps) if not p]))
+                                  if not all(photo_steps) else None))
         # V-cycle time: one more solve of the current state, per V-cycle
         ctx.sync()
         ctx.event_record(2)
@@ -554,7 +561,8 @@ def main():
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
                "ms_per_step": 1e3 * sps}
     if rank == 0:
-        keys = ("ms_per_step", "value", "vcycles_per_step", "vcycle_ms", "launches_per_step", "work_per_step")
+        keys = ("ms_per_step", "value", "vcycles_per_step", "vcycle_ms", "launches_per_step", "work_per_step",
+                "photoi_step_ms", "plain_step_ms", "step_ms")
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
