@@ -100,6 +100,27 @@ class Reaction(C.Structure):
                 ("n_out", C.c_int), ("ix_out", C.c_int * 4), ("mult_out", C.c_int * 4)]
 
 
+AFG_MAX_REFINE_ITEMS = 8
+REF_RM, REF_KEEP, REF_DO = -1, 0, 1
+_R3 = C.c_double * 3
+
+
+class RefineDesc(C.Structure):
+    """afg_refine_desc: parameters of default_refinement (src/m_refine.f90)."""
+    _fields_ = [
+        ("i_electron", C.c_int), ("i_electric_fld", C.c_int), ("lt_col_alpha", C.c_int),
+        ("lt_col_eta", C.c_int), ("use_alpha_effective", C.c_int), ("gas_number_density", C.c_double),
+        ("adx", C.c_double), ("adx_fac", C.c_double), ("min_dens", C.c_double), ("derefine_dx", C.c_double),
+        ("max_dx", C.c_double), ("min_dx", C.c_double), ("ref_buffer", C.c_int),
+        ("n_seeds", C.c_int), ("seed_r0", _R3 * AFG_MAX_REFINE_ITEMS), ("seed_r1", _R3 * AFG_MAX_REFINE_ITEMS),
+        ("seed_width", C.c_double * AFG_MAX_REFINE_ITEMS), ("init_fac", C.c_double),
+        ("n_regions", C.c_int), ("region_rmin", _R3 * AFG_MAX_REFINE_ITEMS),
+        ("region_rmax", _R3 * AFG_MAX_REFINE_ITEMS), ("region_dr", C.c_double * AFG_MAX_REFINE_ITEMS),
+        ("n_limits", C.c_int), ("limit_rmin", _R3 * AFG_MAX_REFINE_ITEMS),
+        ("limit_rmax", _R3 * AFG_MAX_REFINE_ITEMS), ("limit_dr", C.c_double * AFG_MAX_REFINE_ITEMS),
+    ]
+
+
 class TransportDesc(C.Structure):
     _fields_ = [
         ("n_species", C.c_int), ("species_iv", C.c_int * AFG_MAX_SPECIES),
@@ -246,6 +267,9 @@ def load_library(path: str = LIB_PATH):
         "afg_tuning": (C.c_int, [P, _IP]),
         "afg_set_tuning": (C.c_int, [P, _IP]),
         "afg_set_photoi_lockstep": (C.c_int, [P, C.c_int]),
+        "afg_refine_flags": (C.c_int, [P, C.POINTER(RefineDesc), _IP]),
+        "afg_prolong_limit": (C.c_int, [P, C.c_int, C.c_int, _IP, C.c_int]),
+        "afg_tree_remap": (C.c_int, [P, C.POINTER(TreeDesc), _IP]),
         "afg_host_unregister": (C.c_int, [P, C.c_void_p]),
         "afg_sync": (C.c_int, [P]),
         "afg_launch_count": (C.c_longlong, [P]),
@@ -326,6 +350,25 @@ class Context:
         self.check(self.lib.afg_tree_sync_batched(self.ptr, C.byref(self._tree_holder.desc), n_var_cell,
                                                   n_var_face, n_inst, _ip(self._box_inst)),
                    "afg_tree_sync_batched")
+
+    def refine_flags(self, desc):
+        """Box refinement flags (REF_RM / REF_KEEP / REF_DO per box)."""
+        out = np.zeros(self.tree.n_boxes, dtype=np.int32)
+        self.check(self.lib.afg_refine_flags(self.ptr, C.byref(desc), _ip(out)), "afg_refine_flags")
+        return out
+
+    def prolong_limit(self, iv, ids, limiter):
+        a = np.ascontiguousarray(ids, dtype=np.int32)
+        self.check(self.lib.afg_prolong_limit(self.ptr, iv, len(a), _ip(a), limiter), "afg_prolong_limit")
+
+    def tree_remap(self, tree, old_id):
+        """Mirror `tree` keeping the data: old_id[b] = id of new box b+1 in
+        the previous tree (0 = new box)."""
+        holder = TreeDescHolder(tree)
+        o = np.ascontiguousarray(old_id, dtype=np.int32)
+        self.check(self.lib.afg_tree_remap(self.ptr, C.byref(holder.desc), _ip(o)), "afg_tree_remap")
+        self._tree_holder = holder
+        self.tree = tree
 
     def n_instances(self):
         return self.lib.afg_n_instances(self.ptr)

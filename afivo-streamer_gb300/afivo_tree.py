@@ -364,3 +364,15 @@ def forest(trees):
         setattr(f, name, per_level)
     box_inst = np.concatenate([np.full(t.n_boxes, q, dtype=np.int32) for q, t in enumerate(trees)])
     return f, box_inst
+
+
+def remap_ids(old: Tree, new: Tree) -> np.ndarray:
+    """For each box of `new`, its id in `old` (same level and ix), 0 for a
+    box that `old` does not have: the old_id table of afg_tree_remap."""
+    def keys(t):
+        return {(int(t.lvl[b]),) + tuple(int(v) for v in t.ix[b]): b + 1 for b in range(t.n_boxes)}
+    ko = keys(old)
+    out = np.zeros(new.n_boxes, dtype=np.int32)
+    for b in range(new.n_boxes):
+        out[b] = ko.get((int(new.lvl[b]),) + tuple(int(v) for v in new.ix[b]), 0)
+    return out

@@ -75,6 +75,7 @@ struct afg_ctx {
   int cgs[3] = {1, 1, 1};
   std::vector<int> h_ix;      // [n][D]
   std::vector<int> h_nbr;     // [n][2D] raw Fortran ids
+  std::vector<int> h_parent;  // [n] parent slot or -1
   std::vector<std::vector<int>> lvl_ids, lvl_leaves, lvl_parents;  // 0-based slots
   // device tables
   int *d_parent = nullptr, *d_children = nullptr, *d_nbr = nullptr, *d_pnb = nullptr, *d_nbmat = nullptr,
@@ -1236,6 +1237,7 @@ int afg_tree_sync_batched(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, 
       }
     }
   ctx->h_ix.assign(t->ix, t->ix + (size_t)n * D);
+  ctx->h_parent = parent;
   ctx->h_nbr.assign(t->neighbors, t->neighbors + (size_t)n * nnb);
   // independent instances: every relation of a box stays inside its instance
   if (n_inst > 0) {
@@ -2257,3 +2259,4 @@ int afg_kernel_stats(afg_ctx* ctx, long long* launches, double* ms, double* byte
 }  // extern "C"
 
 #include "afg_transport_api.cuh"
+#include "afg_amr.cuh"

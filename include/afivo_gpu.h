@@ -431,6 +431,75 @@ int afg_set_photoi_lockstep(afg_ctx* ctx, int on);
  * src/streamer.f90:659-671). */
 int afg_tree_copy_cc(afg_ctx* ctx, int iv_from, int iv_to);
 
+/* ---- adaptive refinement on the device (src/streamer.f90:397-428) -------
+ * The refinement decision per cell and box, the prolongation into new boxes
+ * and the move of the data to the new tree run on the GPU; the change of the
+ * tree itself (af_adjust_refinement's 2:1 balancing and box bookkeeping,
+ * afivo/src/m_af_core.f90:697-822) stays with the caller. */
+
+#define AFG_MAX_REFINE_ITEMS 8
+#define AFG_REF_RM   -1   /* af_rm_ref   (afivo/src/m_af_types.f90:23) */
+#define AFG_REF_KEEP  0   /* af_keep_ref (26)                          */
+#define AFG_REF_DO    1   /* af_do_ref   (29)                          */
+
+/* default_refinement (src/m_refine.f90:197-298) with the constant gas
+ * density; the time-dependent switches are evaluated by the caller: seeds are
+ * passed only while global_time < refine_init_time, regions only while
+ * global_time <= their stop time.  Boxes with an electrode surface are not
+ * supported (no LSF boxes on this path). */
+typedef struct afg_refine_desc {
+  int i_electron;              /* cc variable of the electron density       */
+  int i_electric_fld;          /* cc variable of |E|                        */
+  int lt_col_alpha;            /* transport-table column of alpha/N          */
+  int lt_col_eta;              /* ... of eta/N (use_alpha_effective)         */
+  int use_alpha_effective;     /* refine_use_alpha_effective                */
+  double gas_number_density;   /* gas_number_density                        */
+  double adx;                  /* refine_adx                                */
+  double adx_fac;              /* refine_adx_fac                            */
+  double min_dens;             /* refine_min_dens                           */
+  double derefine_dx;          /* derefine_dx                               */
+  double max_dx;               /* refine_max_dx                             */
+  double min_dx;               /* refine_min_dx                             */
+  int ref_buffer;              /* refine_buffer_width (cells)               */
+  int n_seeds;                 /* init_conds seeds (lines r0 - r1)          */
+  double seed_r0[AFG_MAX_REFINE_ITEMS][3];
+  double seed_r1[AFG_MAX_REFINE_ITEMS][3];
+  double seed_width[AFG_MAX_REFINE_ITEMS];
+  double init_fac;             /* refine_init_fac                           */
+  int n_regions;               /* refine_regions_* (active ones)            */
+  double region_rmin[AFG_MAX_REFINE_ITEMS][3];
+  double region_rmax[AFG_MAX_REFINE_ITEMS][3];
+  double region_dr[AFG_MAX_REFINE_ITEMS];
+  int n_limits;                /* refine_limits_*                           */
+  double limit_rmin[AFG_MAX_REFINE_ITEMS][3];
+  double limit_rmax[AFG_MAX_REFINE_ITEMS][3];
+  double limit_dr[AFG_MAX_REFINE_ITEMS];
+} afg_refine_desc;
+
+/* The flag pass of consistent_ref_flags (afivo/src/m_af_core.f90:929-991)
+ * with default_refinement as ref_subr and cell_to_ref_flags (1095-1149) for
+ * the leaves and the parents of leaves: box_flags[id-1] receives -1
+ * (af_rm_ref), 0 (af_keep_ref) or 1 (af_do_ref), the maximum over all
+ * contributions as in the reference (boxes without any: 0).  The max-level
+ * clamp and the 2:1 consistency passes follow on the host. */
+int afg_refine_flags(afg_ctx* ctx, const afg_refine_desc* d, int* box_flags);
+
+/* af_prolong_limit (afivo/src/m_af_prolong.f90:311-420) of variable iv into
+ * the n boxes ids[] (1-based) from their parents, slopes limited with
+ * AFG_LIMITER_* (m_af_limiters.f90:41-66); the children's interior is
+ * overwritten.  As in the reference the parents' ghost cells of iv must be
+ * valid; no box of ids[] may be the parent of another (the boxes are filled
+ * concurrently). */
+int afg_prolong_limit(afg_ctx* ctx, int iv, int n, const int* ids, int limiter);
+
+/* Mirror a new tree (after the caller's af_adjust_refinement) keeping the
+ * data: old_id[id-1] is the id box id had in the previous tree, 0 for a new
+ * box (whose data starts at zero and is then filled by afg_prolong_limit).
+ * All cell- and face-centred variables move; operators, ghost-cell methods
+ * and the transport model are set up again as after afg_tree_sync.  Not for
+ * batched trees. */
+int afg_tree_remap(afg_ctx* ctx, const afg_tree_desc* tree, const int* old_id);
+
 /* ---- accounting and timing (no counterpart in the reference, which keeps
  * wall-clock accumulators wc_time_* in src/m_streamer.f90:184-190) -------- */
 

@@ -51,6 +51,8 @@ def lib():
             "orc_field_set_rhs": (C.c_int, [P, DP, C.c_int, C.c_int]),
             "orc_field_from_potential": (C.c_int, [P, DP, DP, C.c_int]),
             "orc_photoi_source": (C.c_int, [P, DP, C.c_double, C.c_int]),
+            "orc_refine_flags": (C.c_int, [P, DP, C.c_void_p, C.POINTER(C.c_int)]),
+            "orc_prolong_limit": (C.c_int, [P, DP, C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -168,6 +170,17 @@ class Oracle:
 
     def photoi_source(self, cc, coeff, i_rhs):
         self._ck(self.L.orc_photoi_source(self.p, _dp(cc), coeff, i_rhs), "photoi_source")
+
+    def refine_flags(self, cc, desc):
+        out = np.zeros(self.tree.n_boxes, dtype=np.int32)
+        self._ck(self.L.orc_refine_flags(self.p, _dp(cc), C.addressof(desc),
+                                         out.ctypes.data_as(C.POINTER(C.c_int))), "refine_flags")
+        return out
+
+    def prolong_limit(self, cc, iv, ids, limiter):
+        a = np.ascontiguousarray(ids, dtype=np.int32)
+        self._ck(self.L.orc_prolong_limit(self.p, _dp(cc), iv, len(a), a.ctypes.data_as(C.POINTER(C.c_int)),
+                                          limiter), "prolong_limit")
 
     def maxabs(self, cc, iv, leaves_only=True):
         return self.L.orc_maxabs(self.p, _dp(cc), iv, int(leaves_only))

@@ -715,4 +715,214 @@ int orc_photoi_source(void* p, double* cc, double coeff, int i_rhs) {
   return AFG_OK;
 }
 
+
+/* default_refinement (src/m_refine.f90:197-298) for one box: cell flags,
+ * i fastest; constant gas density, no electrode boxes. */
+static void default_refinement(const Tree& t, const double* cc, int id, const afg_refine_desc& a,
+                               std::vector<int>& cf) {
+  const int nc = t.nc, D = t.D;
+  const double* E = t.var(const_cast<double*>(cc), id, a.i_electric_fld);
+  const double* ne = t.var(const_cast<double*>(cc), id, a.i_electron);
+  double max_dx = t.dr_of(id, 0), min_dx = t.dr_of(id, 0);
+  for (int d = 1; d < D; d++) {
+    max_dx = std::max(max_dx, t.dr_of(id, d));
+    min_dx = std::min(min_dx, t.dr_of(id, d));
+  }
+  const int kn = D == 3 ? nc : 1;
+  cf.assign((size_t)nc * nc * kn, AFG_REF_KEEP);
+  for (int k = 1; k <= kn; k++)
+    for (int j = 1; j <= nc; j++)
+      for (int i = 1; i <= nc; i++) {
+        const int x = D == 3 ? t.at(i, j, k) : t.at(i, j);
+        const double gas_dens = a.gas_number_density;
+        const double fld = E[x] * SI_TO_TD / gas_dens;
+        int ix;
+        double w;
+        lt_loc(g_tr.d, a.adx_fac * fld, ix, w);
+        double alpha;
+        if (a.use_alpha_effective) {
+          alpha = (lt_col(g_tr, a.lt_col_alpha, ix, w) - lt_col(g_tr, a.lt_col_eta, ix, w)) * gas_dens / a.adx_fac;
+          alpha = std::max(0.0, alpha);
+        } else {
+          alpha = lt_col(g_tr, a.lt_col_alpha, ix, w) * gas_dens / a.adx_fac;
+        }
+        const double adx = max_dx * alpha;
+        int f;
+        if (adx > a.adx && ne[x] > a.min_dens)
+          f = AFG_REF_DO;
+        else if (adx < 0.125 * a.adx && max_dx < a.derefine_dx)
+          f = AFG_REF_RM;
+        else
+          f = AFG_REF_KEEP;
+        /* GM_dist_line (src/m_geometry.f90:23-51) from the cell centre */
+        const int cix[3] = {i, j, k};
+        double rc[3];
+        for (int d = 0; d < D; d++) rc[d] = t.rmin_of(id, d) + (cix[d] - 0.5) * t.dr_of(id, d);
+        for (int n = 0; n < a.n_seeds; n++) {
+          double len2 = 0, frac = 0;
+          for (int d = 0; d < D; d++) {
+            len2 = len2 + (a.seed_r1[n][d] - a.seed_r0[n][d]) * (a.seed_r1[n][d] - a.seed_r0[n][d]);
+            frac = frac + (rc[d] - a.seed_r0[n][d]) * (a.seed_r1[n][d] - a.seed_r0[n][d]);
+          }
+          double s2 = 0;
+          for (int d = 0; d < D; d++) {
+            double dv;
+            if (frac <= 0)
+              dv = rc[d] - a.seed_r0[n][d];
+            else if (frac >= len2)
+              dv = rc[d] - a.seed_r1[n][d];
+            else
+              dv = rc[d] - (a.seed_r0[n][d] + frac / len2 * (a.seed_r1[n][d] - a.seed_r0[n][d]));
+            s2 = s2 + dv * dv;
+          }
+          const double dist = std::sqrt(s2);
+          if (dist - a.seed_width[n] < 2 * max_dx && max_dx > a.init_fac * a.seed_width[n]) f = AFG_REF_DO;
+        }
+        cf[(size_t)(i - 1) + nc * ((j - 1) + (size_t)nc * (k - 1))] = f;
+      }
+  double rmin[3], rmax[3];
+  for (int d = 0; d < D; d++) {
+    rmin[d] = t.rmin_of(id, d);
+    rmax[d] = t.rmin_of(id, d) + t.dr_of(id, d) * nc;
+  }
+  const int hc = nc / 2;
+  const size_t centre = (size_t)(hc - 1) + nc * ((hc - 1) + (size_t)nc * (D == 3 ? hc - 1 : 0));
+  for (int n = 0; n < a.n_regions; n++) {
+    bool all = max_dx > a.region_dr[n];
+    for (int d = 0; d < D; d++) all = all && rmax[d] >= a.region_rmin[n][d] && rmin[d] <= a.region_rmax[n][d];
+    if (all) cf[centre] = AFG_REF_DO;
+  }
+  for (int n = 0; n < a.n_limits; n++) {
+    bool all = max_dx < 2 * a.limit_dr[n];
+    for (int d = 0; d < D; d++) all = all && rmin[d] >= a.limit_rmin[n][d] && rmax[d] <= a.limit_rmax[n][d];
+    if (all)
+      for (auto& f : cf)
+        if (f == AFG_REF_DO) f = AFG_REF_KEEP;
+  }
+  if (max_dx > a.max_dx) {
+    for (auto& f : cf) f = AFG_REF_DO;
+  } else if (min_dx < 2 * a.min_dx) {
+    for (auto& f : cf)
+      if (f == AFG_REF_DO) f = AFG_REF_KEEP;
+  }
+}
+
+/* cell_to_ref_flags (afivo/src/m_af_core.f90:1095-1149) */
+static void cell_to_ref_flags(const Tree& t, const std::vector<int>& cf, int id, int buf, std::vector<int>& rf) {
+  const int nc = t.nc, D = t.D, kn = D == 3 ? nc : 1;
+  bool any_do = false, any_keep = false;
+  for (int f : cf) {
+    any_do = any_do || f == AFG_REF_DO;
+    any_keep = any_keep || f == AFG_REF_KEEP;
+  }
+  if (any_do)
+    rf[id - 1] = AFG_REF_DO;
+  else if (any_keep)
+    rf[id - 1] = std::max(rf[id - 1], (int)AFG_REF_KEEP);
+  else
+    rf[id - 1] = std::max(rf[id - 1], (int)AFG_REF_RM);
+  if (buf <= 0) return;
+  for (int dz = (D == 3 ? -1 : 0); dz <= (D == 3 ? 1 : 0); dz++)
+    for (int dy = -1; dy <= 1; dy++)
+      for (int dx = -1; dx <= 1; dx++) {
+        if (dx == 0 && dy == 0 && dz == 0) continue;
+        const int nb_id = t.mat_of(id, dx, dy, dz);
+        if (nb_id <= 0) continue;
+        const int dir[3] = {dx, dy, dz};
+        int lo[3] = {1, 1, 1}, hi[3] = {nc, nc, kn};
+        for (int d = 0; d < D; d++) {
+          if (dir[d] == 1) lo[d] = nc - buf + 1;
+          if (dir[d] == -1) hi[d] = buf;
+        }
+        bool found = false;
+        for (int k = lo[2]; k <= hi[2] && !found; k++)
+          for (int j = lo[1]; j <= hi[1] && !found; j++)
+            for (int i = lo[0]; i <= hi[0]; i++)
+              if (cf[(size_t)(i - 1) + nc * ((j - 1) + (size_t)nc * (k - 1))] == AFG_REF_DO) {
+                found = true;
+                break;
+              }
+        if (found) rf[nb_id - 1] = AFG_REF_DO;
+      }
+}
+
+/* The flag pass of consistent_ref_flags (afivo/src/m_af_core.f90:929-991):
+ * leaves, and for the first child of a parent that is itself not refined,
+ * the parent; one sequential pass (the reference's per-thread copies are
+ * combined with max, which the order does not change). */
+int orc_refine_flags(void* p, const double* cc, const afg_refine_desc* a, int* flags) {
+  Oracle* o = static_cast<Oracle*>(p);
+  const Tree& t = o->t;
+  const int unset = -2147483647 - 1;
+  std::vector<int> rf(t.n_boxes, unset), cf;
+  for (int lvl = 1; lvl <= t.highest_lvl; lvl++)
+    for (int id : t.leaves[lvl - 1]) {
+      default_refinement(t, cc, id, *a, cf);
+      cell_to_ref_flags(t, cf, id, a->ref_buffer, rf);
+      if (lvl > 1) {
+        const int p_id = t.parent[id - 1];
+        /* af_ix_to_ichild: child number from the parity of ix */
+        int ich = 1;
+        for (int d = 0; d < t.D; d++) ich += ((t.ix_of(id, d) - 1) & 1) << d;
+        int i_ch;
+        for (i_ch = 1; i_ch < ich; i_ch++) {
+          const int ch_id = t.child_of(p_id, i_ch - 1);
+          if (t.child_of(ch_id, 0) <= 0) break;
+        }
+        if (i_ch == ich) {
+          default_refinement(t, cc, p_id, *a, cf);
+          cell_to_ref_flags(t, cf, p_id, a->ref_buffer, rf);
+        }
+      }
+    }
+  for (int b = 0; b < t.n_boxes; b++) flags[b] = rf[b] == unset ? AFG_REF_KEEP : rf[b];
+  return AFG_OK;
+}
+
+/* af_prolong_limit (afivo/src/m_af_prolong.f90:311-420) into boxes ids[] */
+int orc_prolong_limit(void* p, double* cc, int iv, int n, const int* ids, int limiter) {
+  Oracle* o = static_cast<Oracle*>(p);
+  const Tree& t = o->t;
+  const int nc = t.nc, hnc = nc / 2, D = t.D;
+  for (int q = 0; q < n; q++) {
+    const int id = ids[q], p_id = t.parent[id - 1];
+    const double* P = t.var(cc, p_id, iv);
+    double* C = t.var(cc, id, iv);
+    const int o0 = t.child_offset(id, 0), o1 = t.child_offset(id, 1), o2 = D == 3 ? t.child_offset(id, 2) : 0;
+    for (int k = 1; k <= (D == 3 ? nc : 1); k++)
+      for (int j = 1; j <= nc; j++)
+        for (int i = 1; i <= nc; i++) C[D == 3 ? t.at(i, j, k) : t.at(i, j)] = 0;
+    for (int k = 1; k <= (D == 3 ? hnc : 1); k++)
+      for (int j = 1; j <= hnc; j++)
+        for (int i = 1; i <= hnc; i++) {
+          const int ic = i + o0, jc = j + o1, kc = k + o2;
+          const int fi = 2 * i - 1, fj = 2 * j - 1, fk = 2 * k - 1;
+          if (D == 2) {
+            const double f0 = P[t.at(ic, jc)];
+            const double f1 = 0.25 * limiter_apply(P[t.at(ic, jc)] - P[t.at(ic - 1, jc)],
+                                                   P[t.at(ic + 1, jc)] - P[t.at(ic, jc)], limiter);
+            const double f2 = 0.25 * limiter_apply(P[t.at(ic, jc)] - P[t.at(ic, jc - 1)],
+                                                   P[t.at(ic, jc + 1)] - P[t.at(ic, jc)], limiter);
+            C[t.at(fi, fj)] = f0 - f1 - f2 + C[t.at(fi, fj)];
+            C[t.at(fi + 1, fj)] = f0 + f1 - f2 + C[t.at(fi + 1, fj)];
+            C[t.at(fi, fj + 1)] = f0 - f1 + f2 + C[t.at(fi, fj + 1)];
+            C[t.at(fi + 1, fj + 1)] = f0 + f1 + f2 + C[t.at(fi + 1, fj + 1)];
+          } else {
+            const double c0 = P[t.at(ic, jc, kc)];
+            const double f1 = 0.25 * limiter_apply(c0 - P[t.at(ic - 1, jc, kc)], P[t.at(ic + 1, jc, kc)] - c0, limiter);
+            const double f2 = 0.25 * limiter_apply(c0 - P[t.at(ic, jc - 1, kc)], P[t.at(ic, jc + 1, kc)] - c0, limiter);
+            const double f3 = 0.25 * limiter_apply(c0 - P[t.at(ic, jc, kc - 1)], P[t.at(ic, jc, kc + 1)] - c0, limiter);
+            for (int dk = 0; dk < 2; dk++)
+              for (int dj = 0; dj < 2; dj++)
+                for (int di = 0; di < 2; di++) {
+                  const int x = t.at(fi + di, fj + dj, fk + dk);
+                  const double s1 = di ? f1 : -f1, s2 = dj ? f2 : -f2, s3 = dk ? f3 : -f3;
+                  C[x] = c0 + s1 + s2 + s3 + C[x];
+                }
+          }
+        }
+  }
+  return AFG_OK;
+}
+
 }  // extern "C"
