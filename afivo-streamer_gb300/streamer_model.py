@@ -171,6 +171,23 @@ class StreamerModel:
         d.precision = precision
         return d
 
+    def refine_desc(self, **kw):
+        """default_refinement parameters with the reference's defaults
+        (src/m_refine.f90:10-60: refine_buffer_width 4, refine_min_dx 1e-7,
+        refine_max_dx 1e-3, refine_adx 1, refine_adx_fac 1, derefine_dx 1e-4,
+        refine_min_dens -1e99), this model's lookup-table columns and gas
+        density; keyword arguments override fields of afg_refine_desc."""
+        d = ag.RefineDesc()
+        d.i_electron, d.i_electric_fld = self.species_iv[0], self.i_electric_fld
+        d.lt_col_alpha, d.lt_col_eta = self.col_alpha, self.col_eta
+        d.gas_number_density = self.N
+        d.adx, d.adx_fac, d.min_dens = 1.0, 1.0, -1e99
+        d.derefine_dx, d.max_dx, d.min_dx = 1e-4, 1e-3, 1e-7
+        d.ref_buffer, d.init_fac = 4, 0.25
+        for k, v in kw.items():
+            setattr(d, k, v)
+        return d
+
     def field_bc(self, voltage):
         """field_bc_homogeneous (src/m_field.f90:590-610)."""
         D = self.ndim

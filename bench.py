@@ -325,6 +325,25 @@ def run_gpu_arm(args, device, w):
         n, ms, by = ctx.kernel_stats()
         kstats[name] = dict(launches=n, ms=ms, bytes=by)
     ctx.kernel_timing(ag.KT_NONE)
+    # device-side refinement on the state after the timed steps: box flags of
+    # default_refinement (reference defaults) and the limited prolongation of
+    # one variable into the finest level's boxes
+    amr = None
+    if trees is None:
+        ctx.sync()
+        t0 = time.perf_counter()
+        flags = ctx.refine_flags(model.refine_desc())
+        t_flags = time.perf_counter() - t0
+        fine = tree.lvl_ids[-1]
+        iv = model.species_iv[0] + model.n_states - 1   # the backup copy: scratch after the step
+        ctx.event_record(2)
+        ctx.prolong_limit(iv, fine, ag.LIMITER_MC)
+        ctx.event_record(3)
+        amr = dict(refine_flags_ms=1e3 * t_flags, boxes_do=int(np.sum(flags == ag.REF_DO)),
+                   boxes_rm=int(np.sum(flags == ag.REF_RM)), prolong_limit_ms=ctx.event_elapsed(2, 3),
+                   prolong_boxes=len(fine),
+                   note="refine_flags_ms is wall clock through the C-ABI (list build, upload, kernel, "
+                        "flags download); prolong_limit_ms device time for one variable")
     # the batched workload's instances one at a time, from the same initial
     # state (before the end-to-end run below overwrites the host state)
     one = run_one_at_a_time(args, device, w, trees, model, H, ivs) if trees is not None else None
@@ -370,6 +389,8 @@ def run_gpu_arm(args, device, w):
     ctx.close()
     if one is not None:
         e2e["one_at_a_time"] = one
+    if amr is not None:
+        e2e["amr"] = amr
     return tree, results, kstats, e2e, tuning
 
 
@@ -533,6 +554,7 @@ def main():
     w = workloads.BatchCyl2d() if args.config == "batch" else workloads.WORKLOADS[args.config]()
     tree, results, kstats, e2e, tuning = run_gpu_arm(args, local, w)
     one = e2e.pop("one_at_a_time", None) if e2e else None
+    amr = e2e.pop("amr", None) if e2e else None
     if args.profile:
         if rank == 0:
             print(json.dumps({"profile": True, "config": config, "mixed": results["mixed"][0]}))
@@ -577,6 +599,7 @@ def main():
                          "avg_launch_us": 1e3 * ks["ms"] / max(1, ks["launches"])},
             "kernel_classes": kstats, "tuning": tuning,
             **({"one_at_a_time": dict(one, speedup_batched=value / one["value"])} if one else {}),
+            **({"amr": amr} if amr else {}),
             "cpu_baseline": cpu, "e2e": e2e, "clocks": mixed["clocks"],
             "gpu_launches": int(mixed["launches"]),
         }))
