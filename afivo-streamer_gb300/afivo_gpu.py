@@ -267,6 +267,7 @@ def load_library(path: str = LIB_PATH):
         "afg_tuning": (C.c_int, [P, _IP]),
         "afg_set_tuning": (C.c_int, [P, _IP]),
         "afg_set_photoi_lockstep": (C.c_int, [P, C.c_int]),
+        "afg_check_bounded_wait": (C.c_int, [P, _DP]),
         "afg_refine_flags": (C.c_int, [P, C.POINTER(RefineDesc), _IP]),
         "afg_prolong_limit": (C.c_int, [P, C.c_int, C.c_int, _IP, C.c_int]),
         "afg_tree_remap": (C.c_int, [P, C.POINTER(TreeDesc), _IP]),
@@ -433,6 +434,13 @@ class Context:
                 return f"{what} staged in shared memory (bulk copies), {v & 15} cells/thread"
             return f"{v} cells/thread"
         return {"gsrb_fp32": name(out[0]), "gsrb_fp64": name(out[1]), "codes": [out[0], out[1]]}
+
+    def check_bounded_wait(self):
+        """(status, ms): AFG_ERR_DEVICE when a timed-out device wait was
+        detected and reported through the error word."""
+        ms = C.c_double(0)
+        rc = self.lib.afg_check_bounded_wait(self.ptr, C.byref(ms))
+        return rc, ms.value
 
     def set_photoi_lockstep(self, on):
         self.check(self.lib.afg_set_photoi_lockstep(self.ptr, int(on)), "afg_set_photoi_lockstep")

@@ -376,3 +376,62 @@ def remap_ids(old: Tree, new: Tree) -> np.ndarray:
     for b in range(new.n_boxes):
         out[b] = ko.get((int(new.lvl[b]),) + tuple(int(v) for v in new.ix[b]), 0)
     return out
+
+
+AF_REFINE, AF_DEREFINE = 2, -2     # af_refine / af_derefine (m_af_types.f90)
+AF_RM_REF, AF_KEEP_REF, AF_DO_REF = -1, 0, 1
+
+
+def adjust_refinement(tree: Tree, flags, max_lvl: int) -> Tree:
+    """Host side of af_adjust_refinement (afivo/src/m_af_core.f90:697-1091)
+    after the flag pass: the max-level clamp (995-999), ensure_two_one_balance
+    (1015-1055) and handle_derefinement_flags (1057-1088) on the box flags,
+    then the new tree: old leaves flagged for refinement get children, the
+    children of parents flagged for derefinement go, everything else stays.
+    The tree is rebuilt by build_tree, whose balancing also covers diagonal
+    neighbours (the device kernels need it for corner ghost cells)."""
+    f = np.asarray(flags, dtype=np.int64).copy()
+    H = tree.highest_lvl
+    has_ch = (tree.children > 0).any(axis=1)
+    if H >= max_lvl:
+        ids = tree.lvl_ids[max_lvl - 1] - 1
+        f[ids] = np.where(f[ids] == AF_DO_REF, AF_KEEP_REF, f[ids])
+    for lvl in range(H, 0, -1):
+        for id_ in tree.lvl_leaves[lvl - 1]:
+            b = id_ - 1
+            if f[b] in (AF_DO_REF, AF_REFINE):
+                f[b] = AF_REFINE
+                for nb, nb_id in enumerate(tree.neighbors[b]):
+                    if nb_id == AF_NO_BOX:
+                        p = tree.parent[b]
+                        f[tree.neighbors[p - 1][nb] - 1] = AF_REFINE
+            elif f[b] == AF_RM_REF:
+                for nb_id in tree.neighbors[b]:
+                    if nb_id > AF_NO_BOX and (has_ch[nb_id - 1] or f[nb_id - 1] > AF_KEEP_REF):
+                        f[b] = AF_KEEP_REF
+                        break
+    for lvl in range(H - 1, 0, -1):
+        for id_ in tree.lvl_parents[lvl - 1]:
+            c = tree.children[id_ - 1] - 1
+            if np.all(has_ch[c]):
+                continue
+            if np.all(f[c] == AF_RM_REF) and f[id_ - 1] <= AF_KEEP_REF:
+                f[id_ - 1] = AF_DEREFINE
+            else:
+                f[id_ - 1] = AF_KEEP_REF
+                f[c] = np.where(f[c] != AF_DEREFINE, np.maximum(f[c], AF_KEEP_REF), f[c])
+    # boxes of the old tree that have children in the new one, by (lvl, ix)
+    wants = {}
+    for b in range(tree.n_boxes):
+        key = (int(tree.lvl[b]),) + tuple(int(v) for v in tree.ix[b])
+        wants[key] = bool(f[b] == AF_REFINE) if not has_ch[b] else bool(f[b] != AF_DEREFINE)
+    D, nc = tree.ndim, tree.n_cell
+    rb = np.asarray(tree.r_base, dtype=np.float64)
+
+    def refine(lvl, centers, drl):
+        ix = np.floor((centers - rb) / (drl * nc)).astype(np.int64) + 1
+        return np.array([wants.get((lvl,) + tuple(int(v) for v in row), False) for row in ix], dtype=bool)
+
+    dom = np.asarray(tree.dr_base, dtype=np.float64) * np.asarray(tree.coarse_grid_size)
+    return build_tree(D, nc, tree.coarse_grid_size, dom, r_base=tree.r_base, coord=tree.coord,
+                      max_lvl=max(max_lvl, H), refine=refine)

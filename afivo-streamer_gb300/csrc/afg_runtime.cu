@@ -1169,6 +1169,33 @@ const char* afg_last_error(const afg_ctx* ctx) { return ctx ? ctx->err.c_str() :
 
 long long afg_launch_count(const afg_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
+int afg_check_bounded_wait(afg_ctx* ctx, double* waited_ms) {
+  if (!ctx) return AFG_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  cudaEventRecord(e0, ctx->stream);
+  k_wait_check<<<1, 32, 0, ctx->stream>>>(256u, ctx->d_err);
+  cudaEventRecord(e1, ctx->stream);
+  ctx->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0;
+  if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return fail(ctx, AFG_ERR_CUDA, "bounded-wait check: %s", cudaGetErrorString(e));
+  if (waited_ms) *waited_ms = ms;
+  // the error word is read like after every solve iteration, then cleared
+  double unused;
+  const int rc = read_max(ctx, 1, &unused);
+  CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (rc == AFG_OK) return fail(ctx, AFG_ERR_STATE, "the timed-out wait was not reported");
+  return rc == AFG_ERR_CUDA ? AFG_ERR_DEVICE : rc;
+}
+
 int afg_sync(afg_ctx* ctx) {
   if (!ctx) return AFG_ERR_ARG;
   CK(cudaStreamSynchronize(ctx->stream));

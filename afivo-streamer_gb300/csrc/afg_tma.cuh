@@ -65,3 +65,25 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
 }
 
 }  // namespace afg
+
+namespace afg {
+
+// Check of the bounded-wait path used by the staged kernels: one thread
+// announces `bytes` of copies on a fresh mbarrier and issues none, so the
+// phase cannot complete; the wait gives up after kWaitLimitNs and raises
+// *err exactly as a staged kernel does.  No copy is in flight when the CTA
+// returns.
+__global__ void k_wait_check(unsigned bytes, unsigned* err) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_arrive_expect_tx(&bar, bytes);
+  __syncthreads();
+  const bool ok = mbar_wait(&bar, 0);
+  if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicExch(err, 1u);
+}
+
+}  // namespace afg

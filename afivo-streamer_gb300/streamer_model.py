@@ -18,6 +18,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 import afivo_gpu as ag
+import afivo_tree as at
 
 SI_TO_TD = 1e21          # SI_to_Townsend (src/m_gas.f90:39)
 TD_TO_SI = 1e-21
@@ -319,6 +320,32 @@ class StreamerRun:
         self.last.setdefault("vcycles", 0)
         self.last["vcycles"] += n
         return n, r
+
+    def refine(self, desc, max_lvl, limiter=ag.LIMITER_MC):
+        """One refinement of the mesh with the data on the device
+        (src/streamer.f90:397-428): box flags from afg_refine_flags, the new
+        tree from the host's af_adjust_refinement (afivo_tree), the data moved
+        by afg_tree_remap, the new boxes' densities and potential filled by
+        afg_prolong_limit level by level (after a ghost fill of the parents'
+        level), the operators set up again and the field of the new mesh.
+        Returns the box flags and the old id of every new box."""
+        ctx, m = self.ctx, self.m
+        flags = ctx.refine_flags(desc)
+        new = at.adjust_refinement(self.tree, flags, max_lvl)
+        old_id = at.remap_ids(self.tree, new)
+        ctx.tree_remap(new, old_id)
+        self.tree = new
+        self.setup()
+        ivs = [m.species_iv[s] for s in range(len(m.species))] + [m.i_phi]
+        fresh = np.nonzero(old_id == 0)[0] + 1
+        lv = new.lvl[fresh - 1]
+        for lvl in sorted(set(lv.tolist())):
+            ids = fresh[lv == lvl]
+            for iv in ivs:
+                ctx.gc(iv, lvl - 1, True)
+                ctx.prolong_limit(iv, ids, limiter)
+        self.field(0, True)
+        return flags, old_id
 
     def initial_field(self):
         self.ctx.gc(self.m.i_phi, 0, True)

@@ -196,6 +196,15 @@ int afg_tuning(const afg_ctx* ctx, int* out);
  * 50).  afg_tuning reports the codes the same way. */
 int afg_set_tuning(afg_ctx* ctx, const int* in);
 
+/* Check of the device-side failure path: a kernel whose bounded mbarrier
+ * wait cannot complete (copies announced, none issued) gives up after 1 s,
+ * raises the context's error word and returns; the error is read back as
+ * after every solve iteration and cleared.  Returns AFG_ERR_DEVICE when the
+ * timeout was detected and reported (the expected outcome; the context stays
+ * usable), waited_ms the kernel's duration.  No counterpart in the
+ * reference. */
+int afg_check_bounded_wait(afg_ctx* ctx, double* waited_ms);
+
 /* Wait for the copies started by afg_cc_download_async. */
 int afg_transfers_wait(afg_ctx* ctx);
 

@@ -33,6 +33,7 @@ sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.join(HERE, "..", "afivo-streamer_gb300"))
 
 import afivo_gpu as ag  # noqa: E402
+import afivo_tree as at  # noqa: E402
 import oracle  # noqa: E402
 
 
@@ -58,6 +59,7 @@ class OracleStreamerRun:
     def __init__(self, tree, model, voltage, dt, max_rel_residual=1e-8, num_vcycles=30, photoi=None,
                  photoi_per_steps=5, integrator="heun"):
         self.stages = STAGES[integrator]
+        self.integrator = integrator
         self.tree, self.m = tree, model
         self.voltage, self.dt = voltage, dt
         self.rel = max_rel_residual
@@ -125,6 +127,37 @@ class OracleStreamerRun:
         o.field_from_potential(cc, fc, m.i_phi)
         self.last["vcycles"] = self.last.get("vcycles", 0) + nv
         return work
+
+    def refine(self, cc, fc, desc, max_lvl, limiter=ag.LIMITER_MC):
+        """The refinement cycle of StreamerRun.refine on the restatement:
+        flags (orc_refine_flags), the host's new tree (afivo_tree), the data
+        moved by box, prolongation of the new boxes level by level, the field
+        of the new mesh.  Returns the new state arrays, the flags and the old
+        ids."""
+        m = self.m
+        flags = self.o.refine_flags(cc, desc)
+        new = at.adjust_refinement(self.tree, flags, max_lvl)
+        old_id = at.remap_ids(self.tree, new)
+        keep = old_id > 0
+        cc2 = ag.new_cc(new, m.n_var_cell)
+        fc2 = ag.new_fc(new, m.n_var_face)
+        cc2[keep] = cc[old_id[keep] - 1]
+        fc2[keep] = fc[old_id[keep] - 1]
+        it = self.it
+        self.__init__(new, m, self.voltage, self.dt, max_rel_residual=self.rel, num_vcycles=self.num_vcycles,
+                      photoi=self.photoi, photoi_per_steps=self.photoi_per_steps, integrator=self.integrator)
+        self.it = it
+        self.setup()
+        ivs = [m.species_iv[s] for s in range(len(m.species))] + [m.i_phi]
+        fresh = np.nonzero(old_id == 0)[0] + 1
+        lv = new.lvl[fresh - 1]
+        for lvl in sorted(set(lv.tolist())):
+            ids = fresh[lv == lvl]
+            for iv in ivs:
+                self.o.gc(cc2, iv, lvl - 1, True)
+                self.o.prolong_limit(cc2, iv, ids, limiter)
+        self.field(cc2, fc2, 0, True)
+        return cc2, fc2, flags, old_id
 
     def initial_field(self, cc, fc):
         self.o.gc(cc, self.m.i_phi, 0, True)

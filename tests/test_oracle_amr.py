@@ -78,3 +78,35 @@ def test_prolong_limit_linear_and_conservative():
         n2 = tree.n_cell + 2
         inner = (slice(None),) + (slice(1, n2 - 1),) * 2
         assert np.allclose(out[ids - 1, 0][inner], cc[ids - 1, 0][inner], rtol=0, atol=1e-12)
+
+
+def test_adjust_refinement_keep_and_conservative_prolongation():
+    """No flags change: the same tree back, every box mapped to itself.
+    Refining leaves and prolonging (Cartesian): the mean of the 2^D new
+    cells equals the parent cell (af_prolong_limit is conservative)."""
+    tree = refined_tree(2, 8, [16, 16], [1e-2, 1e-2], 4, 1, [0.5e-2, 0.5e-2], 1e-3, seed=3, frac=0.2)
+    same = at.adjust_refinement(tree, np.zeros(tree.n_boxes, np.int32), 4)
+    assert np.array_equal(at.remap_ids(tree, same), np.arange(1, tree.n_boxes + 1))
+    flags = np.zeros(tree.n_boxes, np.int32)
+    flags[tree.lvl_leaves[-1] - 1] = ag.REF_DO
+    new = at.adjust_refinement(tree, flags, 5)
+    old = at.remap_ids(tree, new)
+    fresh = np.nonzero(old == 0)[0] + 1
+    assert new.highest_lvl == 5 and len(fresh) > 0
+    rng = np.random.default_rng(1)
+    cc = ag.new_cc(new, 1)
+    cc[:] = 1 + rng.random(cc.shape)
+    o = oracle.Oracle(new, 1)
+    o.set_cc_methods(1, [ag.BC_NEUMANN] * 4, None, ag.RB_INTERP_LIM)
+    lv = new.lvl[fresh - 1]
+    for lvl in sorted(set(lv.tolist())):
+        o.gc(cc, 1, lvl - 1, True)
+        o.prolong_limit(cc, 1, fresh[lv == lvl], ag.LIMITER_MC)
+    n2, nc = new.n_cell + 2, new.n_cell
+    for b in fresh[:20]:
+        p = new.parent[b - 1]
+        ch = cc[b - 1, 0].reshape(n2, n2)[1:-1, 1:-1]
+        ox, oy = ((new.ix[b - 1] - 1) & 1) * (nc // 2)
+        par = cc[p - 1, 0].reshape(n2, n2)[1 + oy:1 + oy + nc // 2, 1 + ox:1 + ox + nc // 2]
+        mean = 0.25 * (ch[0::2, 0::2] + ch[1::2, 0::2] + ch[0::2, 1::2] + ch[1::2, 1::2])
+        assert np.allclose(mean, par, rtol=1e-14, atol=0)
