@@ -17,22 +17,9 @@ namespace afg {
 constexpr int kNbPhys = -2;   // physical boundary (af_phys_boundary)
 constexpr int kNbRefine = -1; // refinement boundary (af_no_box)
 
-// FP32 block layout (the mixed solve's internal correction buffers): cell
-// (i, j[, k]), 0 <= i, j, k <= nc+1, at 7 + i + py*j (+ pz*k) with rows of
-// py = a multiple of 8 values >= nc + 8 and pz = py*(nc+2), blocks of S32 =
-// a multiple of 8 values.  Interior rows start on a 32-byte boundary, so the
-// nc interior values of a row fill whole 32-byte sectors (one for nc = 8, two
-// for nc = 16; afivo's rows of nc+2 values straddle one more).  The ghost cell
-// i = nc+1 of a row takes slot 0 of the next row, which no cell uses.
-__host__ __device__ constexpr int lay32_py(int nc) { return (nc + 15) / 8 * 8; }
-__host__ __device__ constexpr int lay32_S(int D, int nc) {
-  return (7 + (nc + 1) + lay32_py(nc) * (nc + 1) + (D == 3 ? lay32_py(nc) * (nc + 2) * (nc + 1) : 0) + 1 + 7) / 8 * 8;
-}
-
 // Device view of the tree tables, passed to kernels by value.
 struct KTree {
   int D, nc, n2, S, NF;
-  int py32, pz32, S32;  // FP32 block layout (lay32_py, lay32_S)
   const int* parent;    // [n] parent slot or -1
   const int* children;  // [n][2^D] child slot or -1
   const int* nbr;       // [n][2D] neighbour slot, kNbRefine or kNbPhys
@@ -94,47 +81,9 @@ __device__ __forceinline__ KTree fix_dims(KTree t) {
     t.n2 = NC + 2;
     t.S = D == 2 ? (NC + 2) * (NC + 2) : (NC + 2) * (NC + 2) * (NC + 2);
     t.NF = D == 2 ? (NC + 1) * (NC + 1) : (NC + 1) * (NC + 1) * (NC + 1);
-    t.py32 = lay32_py(NC);
-    t.pz32 = lay32_py(NC) * (NC + 2);
-    t.S32 = lay32_S(D, NC);
   }
   return t;
 }
-
-// Block layout of a variable of type T: FP64 variables keep afivo's layout
-// (x0 = 0, rows of nc+2), FP32 buffers the sector-aligned one above.  Kernels
-// templated on the value type index every block through it.
-struct Lay {
-  int x0, py, pz, S;
-  __device__ __forceinline__ int at2(int i, int j) const { return x0 + i + py * j; }
-  __device__ __forceinline__ int at3(int i, int j, int k) const { return x0 + i + py * j + pz * k; }
-  // cell with normal dimension d at normal index x, tangential indices p
-  // (the lower remaining dimension) and q (the higher one)
-  template <int D>
-  __device__ __forceinline__ int face(int d, int x, int p, int q) const {
-    if (D == 2) return d == 0 ? at2(x, p) : at2(p, x);
-    if (d == 0) return at3(x, p, q);
-    if (d == 1) return at3(p, x, q);
-    return at3(p, q, x);
-  }
-  template <int D>
-  __device__ __forceinline__ int at(int i, int j, int k) const {
-    return D == 2 ? at2(i, j) : at3(i, j, k);
-  }
-};
-template <typename T>
-__device__ __forceinline__ Lay lay(const KTree& t) {
-  if (sizeof(T) == 4) return Lay{7, t.py32, t.pz32, t.S32};
-  return Lay{0, t.n2, t.n2 * t.n2, t.S};
-}
-// the same as compile-time constants for a box size NC
-template <typename T, int D, int NC>
-struct LayC {
-  static constexpr int x0 = sizeof(T) == 4 ? 7 : 0;
-  static constexpr int py = sizeof(T) == 4 ? lay32_py(NC) : NC + 2;
-  static constexpr int pz = py * (NC + 2);
-  static constexpr int S = sizeof(T) == 4 ? lay32_S(D, NC) : (D == 2 ? (NC + 2) * (NC + 2) : (NC + 2) * (NC + 2) * (NC + 2));
-};
 
 // Launch-site dispatch on the box size: 8^3-cell boxes in 3D and 16^2-cell
 // boxes in 2D (the usual afivo-streamer sizes) get their own instantiation,

@@ -27,18 +27,17 @@ __device__ __forceinline__ T bc_ghost(int type, double bval, double drd, bool lo
 template <int D, typename T>
 __device__ __forceinline__ T face_ghost_nb(const KTree& t, const T* __restrict__ v, int slot, int nb, int nbs,
                                            int p, int q, const GcDev& g) {
-  const Lay L = lay<T>(t);
-  const int nc = t.nc, S = L.S, d = nb >> 1;
+  const int nc = t.nc, n2 = t.n2, S = t.S, d = nb >> 1;
   const bool low = (nb & 1) == 0;
   const T* a = v + (size_t)slot * S;
   if (nbs >= 0) {
     const T* b = v + (size_t)nbs * S;
-    return b[L.face<D>(d, low ? nc : 1, p, q)];
+    return b[face_at<D>(n2, d, low ? nc : 1, p, q)];
   }
   if (nbs == kNbPhys) {
     const int i1 = low ? 1 : nc, i2 = low ? 2 : nc - 1;
     return bc_ghost<D, T>(gc_type(g, nb), gc_val(g, nb, t, slot), t.dr[slot * D + d], low,
-                          a[L.face<D>(d, i1, p, q)], a[L.face<D>(d, i2, p, q)]);
+                          a[face_at<D>(n2, d, i1, p, q)], a[face_at<D>(n2, d, i2, p, q)]);
   }
   // refinement boundary: data of the parent's neighbour
   const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
@@ -54,43 +53,43 @@ __device__ __forceinline__ T face_ghost_nb(const KTree& t, const T* __restrict__
     T gcv;
     if (D == 2) {
       const int i = (p + 1) >> 1;  // tmp index
-      const T tm = C[L.face<D>(d, cx, off1 + i - 1, 0)];
-      const T t0 = C[L.face<D>(d, cx, off1 + i, 0)];
-      const T tp = C[L.face<D>(d, cx, off1 + i + 1, 0)];
+      const T tm = C[face_at<D>(n2, d, cx, off1 + i - 1, 0)];
+      const T t0 = C[face_at<D>(n2, d, cx, off1 + i, 0)];
+      const T tp = C[face_at<D>(n2, d, cx, off1 + i + 1, 0)];
       const T grad = T(0.125) * (tp - tm);
       gcv = (p & 1) ? t0 - grad : t0 + grad;
     } else {
       const int i = (p + 1) >> 1, j = (q + 1) >> 1;
-      const T t0 = C[L.face<D>(d, cx, off1 + i, off2 + j)];
-      const T g1 = T(0.125) * (C[L.face<D>(d, cx, off1 + i + 1, off2 + j)] -
-                               C[L.face<D>(d, cx, off1 + i - 1, off2 + j)]);
-      const T g2 = T(0.125) * (C[L.face<D>(d, cx, off1 + i, off2 + j + 1)] -
-                               C[L.face<D>(d, cx, off1 + i, off2 + j - 1)]);
+      const T t0 = C[face_at<D>(n2, d, cx, off1 + i, off2 + j)];
+      const T g1 = T(0.125) * (C[face_at<D>(n2, d, cx, off1 + i + 1, off2 + j)] -
+                               C[face_at<D>(n2, d, cx, off1 + i - 1, off2 + j)]);
+      const T g2 = T(0.125) * (C[face_at<D>(n2, d, cx, off1 + i, off2 + j + 1)] -
+                               C[face_at<D>(n2, d, cx, off1 + i, off2 + j - 1)]);
       const T s1 = (p & 1) ? t0 - g1 : t0 + g1;
       gcv = (q & 1) ? s1 - g2 : s1 + g2;
     }
-    return T(0.5) * gcv + T(0.75) * a[L.face<D>(d, ix, p, q)] -
-           T(0.25) * a[L.face<D>(d, ix + dix, p, q)];
+    return T(0.5) * gcv + T(0.75) * a[face_at<D>(n2, d, ix, p, q)] -
+           T(0.25) * a[face_at<D>(n2, d, ix + dix, p, q)];
   }
   // af_gc_interp(_lim)
   const T third = T(1 / 3.0), sixth = T(1 / 6.0);
   const int p1 = off1 + ((p + 1) >> 1), p2 = p1 + 1 - 2 * (p & 1);
-  const T f = a[L.face<D>(d, low ? 1 : nc, p, q)];
+  const T f = a[face_at<D>(n2, d, low ? 1 : nc, p, q)];
   T val, c1;
   if (D == 2) {
-    c1 = C[L.face<D>(d, cx, p1, 0)];
-    const T c2 = C[L.face<D>(d, cx, p2, 0)];
+    c1 = C[face_at<D>(n2, d, cx, p1, 0)];
+    const T c2 = C[face_at<D>(n2, d, cx, p2, 0)];
     val = T(0.5) * c1 + sixth * c2 + third * f;
   } else {
     const int q1 = off2 + ((q + 1) >> 1), q2 = q1 + 1 - 2 * (q & 1);
-    c1 = C[L.face<D>(d, cx, p1, q1)];
+    c1 = C[face_at<D>(n2, d, cx, p1, q1)];
     T c2, c3;
     if (d < 2) {
-      c2 = C[L.face<D>(d, cx, p2, q1)];
-      c3 = C[L.face<D>(d, cx, p1, q2)];
+      c2 = C[face_at<D>(n2, d, cx, p2, q1)];
+      c3 = C[face_at<D>(n2, d, cx, p1, q2)];
     } else {
-      c2 = C[L.face<D>(d, cx, p1, q2)];
-      c3 = C[L.face<D>(d, cx, p2, q1)];
+      c2 = C[face_at<D>(n2, d, cx, p1, q2)];
+      c3 = C[face_at<D>(n2, d, cx, p2, q1)];
     }
     val = third * c1 + sixth * c2 + sixth * c3 + third * f;
   }
@@ -119,9 +118,8 @@ __device__ __forceinline__ int nbmat_at(const KTree& t, int slot, int dx, int dy
 // Edge (3D) and corner ghosts of one box; face ghosts must be in place.
 template <int D, typename T>
 __device__ void corner_ghosts(const KTree& t, T* __restrict__ v, int slot) {
-  const Lay L = lay<T>(t);
-  const int nc = t.nc;
-  T* a = v + (size_t)slot * L.S;
+  const int nc = t.nc, n2 = t.n2;
+  T* a = v + (size_t)slot * t.S;
   if (D == 3) {
     for (int w = threadIdx.x; w < 12 * nc; w += blockDim.x) {
       const int n = w / nc, pp = w % nc + 1;
@@ -131,17 +129,17 @@ __device__ void corner_ghosts(const KTree& t, T* __restrict__ v, int slot) {
       const int x0 = dim == 0 ? pp : (dx == 1) * (nc + 1);
       const int x1 = dim == 1 ? pp : (dy == 1) * (nc + 1);
       const int x2 = dim == 2 ? pp : (dz == 1) * (nc + 1);
-      const int c = L.at3(x0, x1, x2);
+      const int c = at3(n2, x0, x1, x2);
       const int nbs = nbmat_at(t, slot, dx, dy, dz);
       if (nbs >= 0) {
-        const T* b = v + (size_t)nbs * L.S;
-        a[c] = b[L.at3(x0 - dx * nc, x1 - dy * nc, x2 - dz * nc)];
+        const T* b = v + (size_t)nbs * t.S;
+        a[c] = b[at3(n2, x0 - dx * nc, x1 - dy * nc, x2 - dz * nc)];
       } else {
         // steps towards the interior across the two other dimensions o1 =
         // dim+1, o2 = dim+2 (mod 3): a(o1 step) + a(o2 step) - a(both)
         const int s0 = dim == 0 ? 0 : 1 - 2 * (x0 & 1);
-        const int s1 = dim == 1 ? 0 : (1 - 2 * (x1 & 1)) * L.py;
-        const int s2 = dim == 2 ? 0 : (1 - 2 * (x2 & 1)) * L.pz;
+        const int s1 = dim == 1 ? 0 : (1 - 2 * (x1 & 1)) * n2;
+        const int s2 = dim == 2 ? 0 : (1 - 2 * (x2 & 1)) * n2 * n2;
         const int ua = dim == 0 ? c + s1 : (dim == 1 ? c + s2 : c + s0);
         const int ub = dim == 0 ? c + s2 : (dim == 1 ? c + s0 : c + s1);
         a[c] = a[ua] + a[ub] - a[c + s0 + s1 + s2];
@@ -158,18 +156,18 @@ __device__ void corner_ghosts(const KTree& t, T* __restrict__ v, int slot) {
     const int di = 1 - 2 * (x & 1), dj = 1 - 2 * (y & 1), dk = 1 - 2 * (z & 1);
     if (D == 2) {
       if (nbs >= 0) {
-        const T* b = v + (size_t)nbs * L.S;
-        a[L.at2(x, y)] = b[L.at2(x - dx * nc, y - dy * nc)];
+        const T* b = v + (size_t)nbs * t.S;
+        a[at2(n2, x, y)] = b[at2(n2, x - dx * nc, y - dy * nc)];
       } else {
-        a[L.at2(x, y)] = a[L.at2(x + di, y)] + a[L.at2(x, y + dj)] - a[L.at2(x + di, y + dj)];
+        a[at2(n2, x, y)] = a[at2(n2, x + di, y)] + a[at2(n2, x, y + dj)] - a[at2(n2, x + di, y + dj)];
       }
     } else {
       if (nbs >= 0) {
-        const T* b = v + (size_t)nbs * L.S;
-        a[L.at3(x, y, z)] = b[L.at3(x - dx * nc, y - dy * nc, z - dz * nc)];
+        const T* b = v + (size_t)nbs * t.S;
+        a[at3(n2, x, y, z)] = b[at3(n2, x - dx * nc, y - dy * nc, z - dz * nc)];
       } else {
-        a[L.at3(x, y, z)] = a[L.at3(x, y + dj, z + dk)] + a[L.at3(x + di, y, z + dk)] +
-                              a[L.at3(x + di, y + dj, z)] - T(2) * a[L.at3(x + di, y + dj, z + dk)];
+        a[at3(n2, x, y, z)] = a[at3(n2, x, y + dj, z + dk)] + a[at3(n2, x + di, y, z + dk)] +
+                              a[at3(n2, x + di, y + dj, z)] - T(2) * a[at3(n2, x + di, y + dj, z + dk)];
       }
     }
   }
@@ -185,10 +183,9 @@ __global__ void __launch_bounds__(256) k_gc(KTree t0, const int* __restrict__ re
   load_rec(rec, blockIdx.x, r0, r1);
   const int slot = r0.x;
   if (box_frozen(t, slot)) return;
-  const Lay L = lay<T>(t);
   const int nc = t.nc;
   const int nface = D == 2 ? nc : nc * nc;
-  T* a = v + (size_t)slot * L.S;
+  T* a = v + (size_t)slot * t.S;
   // corners: 0 = face ghosts, 1 = faces then edges/corners, 2 = only the
   // edges/corners (face ghosts already valid)
   for (int w = threadIdx.x; corners != 2 && w < 2 * D * nface; w += blockDim.x) {
@@ -197,7 +194,7 @@ __global__ void __launch_bounds__(256) k_gc(KTree t0, const int* __restrict__ re
     const int d = nb >> 1;
     const bool low = (nb & 1) == 0;
     const T val = face_ghost_nb<D, T>(t, v, slot, nb, rec_nb(r0, r1, nb), p, q, g);
-    a[L.face<D>(d, low ? 0 : nc + 1, p, q)] = val;
+    a[face_at<D>(t.n2, d, low ? 0 : nc + 1, p, q)] = val;
   }
   if (corners) {
     __syncthreads();

@@ -44,17 +44,16 @@ __device__ __forceinline__ void cyl_coeffs(const KTree& t, int slot, int i, cons
 
 // L phi at interior cell (i,j[,k]); stencil_apply_357 (m_af_stencil.f90:367-496)
 template <int D, bool CYL, typename T>
-__device__ __forceinline__ T apply_lpl(const T* __restrict__ p, const Lay& L, int i, int j, int k,
+__device__ __forceinline__ T apply_lpl(const T* __restrict__ p, int n2, int i, int j, int k,
                                        const T c[7], T k1, T k2, T k3) {
-  const int py = L.py;
   if (D == 2) {
-    const int x = L.at2(i, j);
+    const int x = at2(n2, i, j);
     if (CYL)
-      return k1 * p[x] + k2 * p[x - 1] + k3 * p[x + 1] + c[3] * p[x - py] + c[4] * p[x + py];
-    return c[0] * p[x] + c[1] * p[x - 1] + c[2] * p[x + 1] + c[3] * p[x - py] + c[4] * p[x + py];
+      return k1 * p[x] + k2 * p[x - 1] + k3 * p[x + 1] + c[3] * p[x - n2] + c[4] * p[x + n2];
+    return c[0] * p[x] + c[1] * p[x - 1] + c[2] * p[x + 1] + c[3] * p[x - n2] + c[4] * p[x + n2];
   } else {
-    const int x = L.at3(i, j, k), sk = L.pz;
-    return c[0] * p[x] + c[1] * p[x - 1] + c[2] * p[x + 1] + c[3] * p[x - py] + c[4] * p[x + py] +
+    const int x = at3(n2, i, j, k), sk = n2 * n2;
+    return c[0] * p[x] + c[1] * p[x - 1] + c[2] * p[x + 1] + c[3] * p[x - n2] + c[4] * p[x + n2] +
            c[5] * p[x - sk] + c[6] * p[x + sk];
   }
 }
@@ -76,21 +75,20 @@ template <int D, bool CYL, typename T>
 __device__ __forceinline__ T apply_lpl_otf(const KTree& t, const T* __restrict__ phi, const T* __restrict__ p,
                                            int slot, int i, int j, int k, const T c[7], T k1, T k2, T k3,
                                            const GcDev& g, const int4& r0, const int4& r1) {
-  const Lay L = lay<T>(t);
-  const int nc = t.nc, py = L.py;
+  const int nc = t.nc, n2 = t.n2;
   if (D == 2) {
-    const int x = L.at2(i, j);
+    const int x = at2(n2, i, j);
     const T pw = i == 1 ? face_ghost_nb<D, T>(t, phi, slot, 0, r0.y, j, 0, g) : p[x - 1];
     const T pe = i == nc ? face_ghost_nb<D, T>(t, phi, slot, 1, r0.z, j, 0, g) : p[x + 1];
-    const T ps = j == 1 ? face_ghost_nb<D, T>(t, phi, slot, 2, r0.w, i, 0, g) : p[x - py];
-    const T pn = j == nc ? face_ghost_nb<D, T>(t, phi, slot, 3, r1.x, i, 0, g) : p[x + py];
+    const T ps = j == 1 ? face_ghost_nb<D, T>(t, phi, slot, 2, r0.w, i, 0, g) : p[x - n2];
+    const T pn = j == nc ? face_ghost_nb<D, T>(t, phi, slot, 3, r1.x, i, 0, g) : p[x + n2];
     return lpl_vals<D, CYL, T>(p[x], pw, pe, ps, pn, T(0), T(0), c, k1, k2, k3);
   } else {
-    const int x = L.at3(i, j, k), sk = L.pz;
+    const int x = at3(n2, i, j, k), sk = n2 * n2;
     const T pw = i == 1 ? face_ghost_nb<D, T>(t, phi, slot, 0, r0.y, j, k, g) : p[x - 1];
     const T pe = i == nc ? face_ghost_nb<D, T>(t, phi, slot, 1, r0.z, j, k, g) : p[x + 1];
-    const T ps = j == 1 ? face_ghost_nb<D, T>(t, phi, slot, 2, r0.w, i, k, g) : p[x - py];
-    const T pn = j == nc ? face_ghost_nb<D, T>(t, phi, slot, 3, r1.x, i, k, g) : p[x + py];
+    const T ps = j == 1 ? face_ghost_nb<D, T>(t, phi, slot, 2, r0.w, i, k, g) : p[x - n2];
+    const T pn = j == nc ? face_ghost_nb<D, T>(t, phi, slot, 3, r1.x, i, k, g) : p[x + n2];
     const T pb = k == 1 ? face_ghost_nb<D, T>(t, phi, slot, 4, r1.y, i, j, g) : p[x - sk];
     const T pf = k == nc ? face_ghost_nb<D, T>(t, phi, slot, 5, r1.z, i, j, g) : p[x + sk];
     return lpl_vals<D, CYL, T>(p[x], pw, pe, ps, pn, pb, pf, c, k1, k2, k3);
@@ -105,31 +103,30 @@ __global__ void __launch_bounds__(256) k_gsrb(KTree t0, const int* __restrict__ 
   const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
   if (box_frozen(t, slot)) return;
-  const Lay L = lay<T>(t);
-  const int nc = t.nc, py = L.py, hn = nc / 2;
+  const int nc = t.nc, n2 = t.n2, hn = nc / 2;
   T c[7];
   for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
   const T inv_c1 = mc.cb[slot * 8 + 7];
-  T* p = phi + (size_t)slot * L.S;
-  const T* f = rhs + (size_t)slot * L.S;
+  T* p = phi + (size_t)slot * t.S;
+  const T* f = rhs + (size_t)slot * t.S;
   const int count = D == 2 ? nc * hn : nc * nc * hn;
   for (int w = threadIdx.x; w < count; w += blockDim.x) {
     const int row = w / hn, col = w - row * hn;
     if (D == 2) {
       const int j = row + 1;
       const int i = 2 - ((redblack ^ j) & 1) + 2 * col;
-      const int x = L.at2(i, j);
+      const int x = at2(n2, i, j);
       if (CYL) {
         const T* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
-        p[x] = (f[x] - y[1] * p[x - 1] - y[2] * p[x + 1] - c[3] * p[x - py] - c[4] * p[x + py]) * y[3];
+        p[x] = (f[x] - y[1] * p[x - 1] - y[2] * p[x + 1] - c[3] * p[x - n2] - c[4] * p[x + n2]) * y[3];
       } else {
-        p[x] = (f[x] - c[1] * p[x - 1] - c[2] * p[x + 1] - c[3] * p[x - py] - c[4] * p[x + py]) * inv_c1;
+        p[x] = (f[x] - c[1] * p[x - 1] - c[2] * p[x + 1] - c[3] * p[x - n2] - c[4] * p[x + n2]) * inv_c1;
       }
     } else {
       const int j = row % nc + 1, k = row / nc + 1;
       const int i = 2 - ((redblack ^ (k + j)) & 1) + 2 * col;
-      const int x = L.at3(i, j, k), sk = L.pz;
-      p[x] = (f[x] - c[1] * p[x - 1] - c[2] * p[x + 1] - c[3] * p[x - py] - c[4] * p[x + py] -
+      const int x = at3(n2, i, j, k), sk = n2 * n2;
+      p[x] = (f[x] - c[1] * p[x - 1] - c[2] * p[x + 1] - c[3] * p[x - n2] - c[4] * p[x + n2] -
               c[5] * p[x - sk] - c[6] * p[x + sk]) *
              inv_c1;
     }
@@ -155,24 +152,23 @@ __global__ void __launch_bounds__(256, 6) k_gsrb_fused(KTree t0, const int* __re
   const MgCoef<T> mc = mc_.get();
   const int slot = list[blockIdx.x];
   if (box_frozen(t, slot)) return;
-  const Lay L = lay<T>(t);
-  const int nc = t.nc, py = L.py, hn = nc / 2;
+  const int nc = t.nc, n2 = t.n2, hn = nc / 2;
   T c[7];
   for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
   const T inv_c1 = mc.cb[slot * 8 + 7];
-  T* p = phi + (size_t)slot * L.S;
-  const T* f = rhs + (size_t)slot * L.S;
+  T* p = phi + (size_t)slot * t.S;
+  const T* f = rhs + (size_t)slot * t.S;
   const int count = D == 2 ? nc * hn : nc * nc * hn;
   for (int w = threadIdx.x; w < count; w += blockDim.x) {
     const int row = w / hn, col = w - row * hn;
     if (D == 2) {
       const int j = row + 1;
       const int i = 2 - ((redblack ^ j) & 1) + 2 * col;
-      const int x = L.at2(i, j);
+      const int x = at2(n2, i, j);
       const T pw = i == 1 ? face_ghost<D, T>(t, phi, slot, 0, j, 0, g) : p[x - 1];
       const T pe = i == nc ? face_ghost<D, T>(t, phi, slot, 1, j, 0, g) : p[x + 1];
-      const T ps = j == 1 ? face_ghost<D, T>(t, phi, slot, 2, i, 0, g) : p[x - py];
-      const T pn = j == nc ? face_ghost<D, T>(t, phi, slot, 3, i, 0, g) : p[x + py];
+      const T ps = j == 1 ? face_ghost<D, T>(t, phi, slot, 2, i, 0, g) : p[x - n2];
+      const T pn = j == nc ? face_ghost<D, T>(t, phi, slot, 3, i, 0, g) : p[x + n2];
       if (CYL) {
         const T* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
         p[x] = (f[x] - y[1] * pw - y[2] * pe - c[3] * ps - c[4] * pn) * y[3];
@@ -182,11 +178,11 @@ __global__ void __launch_bounds__(256, 6) k_gsrb_fused(KTree t0, const int* __re
     } else {
       const int j = row % nc + 1, k = row / nc + 1;
       const int i = 2 - ((redblack ^ (k + j)) & 1) + 2 * col;
-      const int x = L.at3(i, j, k), sk = L.pz;
+      const int x = at3(n2, i, j, k), sk = n2 * n2;
       const T pw = i == 1 ? face_ghost<D, T>(t, phi, slot, 0, j, k, g) : p[x - 1];
       const T pe = i == nc ? face_ghost<D, T>(t, phi, slot, 1, j, k, g) : p[x + 1];
-      const T ps = j == 1 ? face_ghost<D, T>(t, phi, slot, 2, i, k, g) : p[x - py];
-      const T pn = j == nc ? face_ghost<D, T>(t, phi, slot, 3, i, k, g) : p[x + py];
+      const T ps = j == 1 ? face_ghost<D, T>(t, phi, slot, 2, i, k, g) : p[x - n2];
+      const T pn = j == nc ? face_ghost<D, T>(t, phi, slot, 3, i, k, g) : p[x + n2];
       const T pb = k == 1 ? face_ghost<D, T>(t, phi, slot, 4, i, j, g) : p[x - sk];
       const T pf = k == nc ? face_ghost<D, T>(t, phi, slot, 5, i, j, g) : p[x + sk];
       p[x] = (f[x] - c[1] * pw - c[2] * pe - c[3] * ps - c[4] * pn - c[5] * pb - c[6] * pf) * inv_c1;
@@ -205,10 +201,8 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
     k_gsrb_rec(KTree t0, const int* __restrict__ rec, ModeArg<T> phi_, ModeArg<const T> rhs_, int redblack,
                ModeCoef<T> mc_, GcDev g) {
   constexpr int TPB = (D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT;
-  using LC = LayC<T, D, NC>;
-  constexpr int nc = NC, py = LC::py, hn = NC / 2, sk = LC::pz;
+  constexpr int nc = NC, n2 = NC + 2, hn = NC / 2, sk = n2 * n2;
   const KTree t = fix_dims<D, NC>(t0);
-  const Lay L = lay<T>(t);
   T* __restrict__ phi = phi_.get();
   const T* __restrict__ rhs = rhs_.get();
   const MgCoef<T> mc = mc_.get();
@@ -219,8 +213,8 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
   T c[7];
   for (int q = 0; q < 2 * D + 1; q++) c[q] = mc.cb[slot * 8 + q];
   const T inv_c1 = mc.cb[slot * 8 + 7];
-  T* p = phi + (size_t)slot * L.S;
-  const T* f = rhs + (size_t)slot * L.S;
+  T* p = phi + (size_t)slot * t.S;
+  const T* f = rhs + (size_t)slot * t.S;
   T val[CPT];
   int xs[CPT];
 #pragma unroll
@@ -230,11 +224,11 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
     if (D == 2) {
       const int j = row + 1;
       const int i = 2 - ((redblack ^ j) & 1) + 2 * col;
-      const int x = L.at2(i, j);
+      const int x = at2(n2, i, j);
       const T pw = i == 1 ? face_ghost_nb<D, T>(t, phi, slot, 0, r0.y, j, 0, g) : p[x - 1];
       const T pe = i == nc ? face_ghost_nb<D, T>(t, phi, slot, 1, r0.z, j, 0, g) : p[x + 1];
-      const T ps = j == 1 ? face_ghost_nb<D, T>(t, phi, slot, 2, r0.w, i, 0, g) : p[x - py];
-      const T pn = j == nc ? face_ghost_nb<D, T>(t, phi, slot, 3, r1.x, i, 0, g) : p[x + py];
+      const T ps = j == 1 ? face_ghost_nb<D, T>(t, phi, slot, 2, r0.w, i, 0, g) : p[x - n2];
+      const T pn = j == nc ? face_ghost_nb<D, T>(t, phi, slot, 3, r1.x, i, 0, g) : p[x + n2];
       if (CYL) {
         const T* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
         val[u] = (f[x] - y[1] * pw - y[2] * pe - c[3] * ps - c[4] * pn) * y[3];
@@ -245,11 +239,11 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
     } else {
       const int j = row % nc + 1, k = row / nc + 1;
       const int i = 2 - ((redblack ^ (k + j)) & 1) + 2 * col;
-      const int x = L.at3(i, j, k);
+      const int x = at3(n2, i, j, k);
       const T pw = i == 1 ? face_ghost_nb<D, T>(t, phi, slot, 0, r0.y, j, k, g) : p[x - 1];
       const T pe = i == nc ? face_ghost_nb<D, T>(t, phi, slot, 1, r0.z, j, k, g) : p[x + 1];
-      const T ps = j == 1 ? face_ghost_nb<D, T>(t, phi, slot, 2, r0.w, i, k, g) : p[x - py];
-      const T pn = j == nc ? face_ghost_nb<D, T>(t, phi, slot, 3, r1.x, i, k, g) : p[x + py];
+      const T ps = j == 1 ? face_ghost_nb<D, T>(t, phi, slot, 2, r0.w, i, k, g) : p[x - n2];
+      const T pn = j == nc ? face_ghost_nb<D, T>(t, phi, slot, 3, r1.x, i, k, g) : p[x + n2];
       const T pb = k == 1 ? face_ghost_nb<D, T>(t, phi, slot, 4, r1.y, i, j, g) : p[x - sk];
       const T pf = k == nc ? face_ghost_nb<D, T>(t, phi, slot, 5, r1.z, i, j, g) : p[x + sk];
       val[u] = (f[x] - c[1] * pw - c[2] * pe - c[3] * ps - c[4] * pn - c[5] * pb - c[6] * pf) * inv_c1;
@@ -260,38 +254,21 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
   for (int u = 0; u < CPT; u++) p[xs[u]] = val[u];
 }
 
-// Shared-memory stage layout of k_gsrb_tma: FP32 blocks in rows of SPY = a
-// multiple of 4 values >= nc + 4 with the interior at a 16-byte boundary
-// (x0 = 3; the ghost i = nc+1 takes slot 0 of the next row), FP64 blocks as
-// stored (afivo's layout); SS values per stage, a multiple of 16 bytes.
-template <typename T, int D, int NC>
-struct StageLay {
-  static constexpr bool ROWS = sizeof(T) == 4;
-  static constexpr int x0 = ROWS ? 3 : 0;
-  static constexpr int py = ROWS ? (NC + 7) / 4 * 4 : NC + 2;
-  static constexpr int pz = py * (NC + 2);
-  static constexpr int SS = ROWS ? (x0 + (NC + 1) + py * (NC + 1) + (D == 3 ? pz * (NC + 1) : 0) + 1 + 3) / 4 * 4
-                                 : LayC<T, D, NC>::S;
-};
-
 // The same half sweep with the boxes staged in shared memory: a persistent
-// grid walks the record list, each CTA copying the next box's phi into
+// grid walks the record list, each CTA copying the next box's phi block
+// ((nc+2)^D values, ghost layers included; with SR also its rhs block) into
 // shared memory with bulk asynchronous copies while it updates the current
-// box from the previous copy (two stages, one mbarrier each).  FP32 blocks
-// (sector-aligned layout): the interior rows only, one copy of nc values per
-// row issued by the first warp, into the denser stage layout of StageLay;
-// FP64 blocks (afivo's layout, rows not 16-byte aligned): the whole block.
-// With SR the rhs is staged the same way; without, the right-hand side, read
-// once per cell, is loaded from global memory before the wait (half the
-// shared memory, more CTAs per SM).  Per box, first the face ghosts that this
-// half sweep reads (those next to cells of its colour, half of each face)
-// are evaluated cooperatively with face_ghost_nb on global memory (the
-// values af_gc would store) into the stage; then every thread updates its
-// cells from shared memory alone, without branches.  Interior neighbours are
-// cells of the other colour, which no CTA writes in a half sweep, so the
-// staged copy is current.  Results go to global memory; the arithmetic is
-// that of k_gsrb_rec.  A wait that times out (1 s) sets *err; the CTA then
-// waits (bounded) for its copies in flight and returns.
+// box from the previous copy (two stages, one mbarrier each).  Without SR
+// the right-hand side, read once per cell, is loaded from global memory
+// before the wait (half the shared memory, more CTAs per SM).  Per box, first the face
+// ghosts that this half sweep reads (those next to cells of its colour, half
+// of each face) are evaluated cooperatively with face_ghost_nb on global
+// memory (the values af_gc would store) into the staged block; then every
+// thread updates its cells from shared memory alone, without branches.
+// Interior neighbours are cells of the other colour, which no CTA writes in
+// a half sweep, so the staged copy is current.  Results go to global memory;
+// the arithmetic is that of k_gsrb_rec.  A wait that times out (1 s) sets
+// *err; the CTA then waits (bounded) for its copies in flight and returns.
 template <int D, bool CYL, typename T, int NC, int CPT, bool SR>
 __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT)
     k_gsrb_tma(KTree t0, const int* __restrict__ rec, int n, ModeArg<T> phi_, ModeArg<const T> rhs_, int redblack,
@@ -300,80 +277,56 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
   const T* __restrict__ rhs = rhs_.get();
   const MgCoef<T> mc = mc_.get();
   constexpr int TPB = (D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT;
-  using LC = LayC<T, D, NC>;
-  using SL = StageLay<T, D, NC>;
-  constexpr int nc = NC, hn = NC / 2, py = LC::py;
-  constexpr int S = LC::S, SS = SL::SS, spy = SL::py, spz = SL::pz;
+  constexpr int nc = NC, n2 = NC + 2, hn = NC / 2, sk = n2 * n2;
+  constexpr int S = D == 2 ? n2 * n2 : n2 * n2 * n2;
   constexpr int NGF = D == 2 ? hn : nc * hn;  // ghosts read per face and half sweep
-  constexpr bool ROWS = SL::ROWS;
-  constexpr int NROW = D == 2 ? NC : NC * NC;
-  constexpr unsigned ROWB = NC * sizeof(T);
-  constexpr unsigned BYTES = ROWS ? NROW * ROWB : S * sizeof(T);
-  static_assert(BYTES % 16 == 0 && ROWB % 16 == 0 && (SS * sizeof(T)) % 16 == 0, "bulk copies need 16-byte multiples");
-  static_assert(!ROWS || ((LC::x0 + 1) % 8 == 0 && py % 8 == 0 && (SL::x0 + 1) % 4 == 0 && spy % 4 == 0),
-                "FP32 interior rows start on 32-byte (global) and 16-byte (shared) boundaries");
-  static_assert(TPB >= 32, "the first warp issues the copies");
+  constexpr unsigned BYTES = S * sizeof(T);
+  static_assert(BYTES % 16 == 0, "bulk copies need 16-byte multiples");
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  T* sphi = reinterpret_cast<T*>(smem_raw);  // [2][SS]
-  T* srhs = sphi + 2 * SS;                    // [2][SS] when SR
+  T* sphi = reinterpret_cast<T*>(smem_raw);  // [2][S]
+  T* srhs = sphi + 2 * S;                     // [2][S] when SR
   __shared__ __align__(8) unsigned long long bar[2];
   const KTree t = fix_dims<D, NC>(t0);
-  const Lay L = lay<T>(t);
-  const Lay LS{SL::x0, spy, spz, SS};
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
   }
   __syncthreads();
-  // first warp: copies of list entry e into stage st (thread 0 posts the
-  // expected bytes before any copy is issued)
+  // thread 0: copies of list entry e into stage st
   auto issue = [&](int e, int st) {
     const int s = rec[8 * e];
     fence_proxy_async_smem();
-    if (threadIdx.x == 0) mbar_arrive_expect_tx(&bar[st], SR ? 2 * BYTES : BYTES);
-    if (ROWS) {
-      __syncwarp();
-      for (int r = threadIdx.x; r < NROW; r += 32) {
-        const int j = D == 2 ? r + 1 : r % NC + 1, k = D == 2 ? 0 : r / NC + 1;
-        const int xg = L.at<D>(1, j, k), xm = LS.at<D>(1, j, k);
-        bulk_copy_g2s(sphi + st * SS + xm, phi + (size_t)s * S + xg, ROWB, &bar[st]);
-        if (SR) bulk_copy_g2s(srhs + st * SS + xm, rhs + (size_t)s * S + xg, ROWB, &bar[st]);
-      }
-    } else if (threadIdx.x == 0) {
-      bulk_copy_g2s(sphi + st * SS, phi + (size_t)s * S, BYTES, &bar[st]);
-      if (SR) bulk_copy_g2s(srhs + st * SS, rhs + (size_t)s * S, BYTES, &bar[st]);
-    }
+    mbar_arrive_expect_tx(&bar[st], SR ? 2 * BYTES : BYTES);
+    bulk_copy_g2s(sphi + st * S, phi + (size_t)s * S, BYTES, &bar[st]);
+    if (SR) bulk_copy_g2s(srhs + st * S, rhs + (size_t)s * S, BYTES, &bar[st]);
   };
-  if (threadIdx.x < 32 && (int)blockIdx.x < n) issue(blockIdx.x, 0);
+  if (threadIdx.x == 0 && (int)blockIdx.x < n) issue(blockIdx.x, 0);
   int it = 0;
   for (int e = blockIdx.x; e < n; e += gridDim.x, it++) {
     const int st = it & 1;
     const bool next = e + (int)gridDim.x < n;
-    if (threadIdx.x < 32 && next) issue(e + gridDim.x, st ^ 1);
+    if (threadIdx.x == 0 && next) issue(e + gridDim.x, st ^ 1);
     const int4 r0 = reinterpret_cast<const int4*>(rec)[2 * e];
     const int4 r1 = reinterpret_cast<const int4*>(rec)[2 * e + 1];
     const int slot = r0.x;
     T c[7];
     for (int q = 0; q < 2 * D + 1; q++) c[q] = mc.cb[slot * 8 + q];
     const T inv_c1 = mc.cb[slot * 8 + 7];
-    // this thread's cells (global and stage indices) and their right-hand
-    // sides, loaded before the wait
+    // this thread's cells and their right-hand sides, loaded before the wait
     const T* f = rhs + (size_t)slot * S;
     T fv[CPT];
-    int xs[CPT], xm[CPT];
+    int xs[CPT];
 #pragma unroll
     for (int u = 0; u < CPT; u++) {
       const int w = (int)threadIdx.x + u * TPB;
       const int row = w / hn, col = w - row * hn;
       if (D == 2) {
-        const int j = row + 1, i = 2 - ((redblack ^ j) & 1) + 2 * col;
-        xs[u] = L.at2(i, j);
-        xm[u] = LS.at2(i, j);
+        const int j = row + 1;
+        xs[u] = at2(n2, 2 - ((redblack ^ j) & 1) + 2 * col, j);
       } else {
-        const int j = row % nc + 1, k = row / nc + 1, i = 2 - ((redblack ^ (k + j)) & 1) + 2 * col;
-        xs[u] = L.at3(i, j, k);
-        xm[u] = LS.at3(i, j, k);
+        const int j = row % nc + 1, k = row / nc + 1;
+        xs[u] = at3(n2, 2 - ((redblack ^ (k + j)) & 1) + 2 * col, j, k);
       }
       if (!SR) fv[u] = f[xs[u]];
     }
@@ -387,10 +340,10 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
       return;
     }
     const bool active = !box_frozen(t, slot);
-    T* P = sphi + st * SS;
+    T* P = sphi + st * S;
     if (SR) {
 #pragma unroll
-      for (int u = 0; u < CPT; u++) fv[u] = srhs[st * SS + xm[u]];
+      for (int u = 0; u < CPT; u++) fv[u] = srhs[st * S + xs[u]];
     }
     // face ghosts next to cells of this colour: cell (i, j[, k]) is updated
     // when i + j (+ k) + redblack is even
@@ -406,7 +359,7 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
         qt = m / hn + 1;
         pt = 2 * (m - (qt - 1) * hn) + 1 + ((a + 1 + qt + redblack) & 1);
       }
-      P[LS.face<D>(d, low ? 0 : nc + 1, pt, qt)] =
+      P[face_at<D>(n2, d, low ? 0 : nc + 1, pt, qt)] =
           face_ghost_nb<D, T>(t, phi, slot, nb, rec_nb(r0, r1, nb), pt, qt, g);
     }
     __syncthreads();
@@ -415,18 +368,18 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
       T val[CPT];
 #pragma unroll
       for (int u = 0; u < CPT; u++) {
-        const int x = xm[u];
+        const int x = xs[u];
         if (D == 2) {
           if (CYL) {
-            const int i = (xs[u] - LC::x0) % py;
+            const int i = x % n2;
             const T* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
-            val[u] = (fv[u] - y[1] * P[x - 1] - y[2] * P[x + 1] - c[3] * P[x - spy] - c[4] * P[x + spy]) * y[3];
+            val[u] = (fv[u] - y[1] * P[x - 1] - y[2] * P[x + 1] - c[3] * P[x - n2] - c[4] * P[x + n2]) * y[3];
           } else {
-            val[u] = (fv[u] - c[1] * P[x - 1] - c[2] * P[x + 1] - c[3] * P[x - spy] - c[4] * P[x + spy]) * inv_c1;
+            val[u] = (fv[u] - c[1] * P[x - 1] - c[2] * P[x + 1] - c[3] * P[x - n2] - c[4] * P[x + n2]) * inv_c1;
           }
         } else {
-          val[u] = (fv[u] - c[1] * P[x - 1] - c[2] * P[x + 1] - c[3] * P[x - spy] - c[4] * P[x + spy] -
-                    c[5] * P[x - spz] - c[6] * P[x + spz]) *
+          val[u] = (fv[u] - c[1] * P[x - 1] - c[2] * P[x + 1] - c[3] * P[x - n2] - c[4] * P[x + n2] -
+                    c[5] * P[x - sk] - c[6] * P[x + sk]) *
                    inv_c1;
         }
       }
@@ -449,13 +402,12 @@ __global__ void __launch_bounds__(256) k_residual(KTree t0, const int* __restric
   __shared__ T sred[32];
   const int slot = list[blockIdx.x];
   if (box_frozen(t, slot)) return;
-  const Lay L = lay<T>(t);
-  const int nc = t.nc;
+  const int nc = t.nc, n2 = t.n2;
   T c[7];
   for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
-  const T* p = phi + (size_t)slot * L.S;
-  const T* f = rhs + (size_t)slot * L.S;
-  T* o = tmp + (size_t)slot * L.S;
+  const T* p = phi + (size_t)slot * t.S;
+  const T* f = rhs + (size_t)slot * t.S;
+  T* o = tmp + (size_t)slot * t.S;
   const int count = D == 2 ? nc * nc : nc * nc * nc;
   T mx = T(0);
   for (int w = threadIdx.x; w < count; w += blockDim.x) {
@@ -466,8 +418,8 @@ __global__ void __launch_bounds__(256) k_residual(KTree t0, const int* __restric
       const T* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
       k1 = y[0]; k2 = y[1]; k3 = y[2];
     }
-    const int x = D == 2 ? L.at2(i, j) : L.at3(i, j, k);
-    const T res = f[x] - apply_lpl<D, CYL, T>(p, L, i, j, k, c, k1, k2, k3);
+    const int x = D == 2 ? at2(n2, i, j) : at3(n2, i, j, k);
+    const T res = f[x] - apply_lpl<D, CYL, T>(p, n2, i, j, k, c, k1, k2, k3);
     o[x] = res;
     acc_absmax(mx, res);
   }
@@ -497,15 +449,14 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* 
   const int slot = r0.x;
   if (box_frozen(t, slot)) return;
   const int pslot = t.parent[slot];
-  const Lay L = lay<T>(t);
-  const int nc = t.nc, hnc = nc / 2;
+  const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
   T c[7];
   for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
-  const T* p = phi + (size_t)slot * L.S;
-  const T* f = rhs + (size_t)slot * L.S;
-  T* pp = phi + (size_t)pslot * L.S;
-  T* pt = tmp + (size_t)pslot * L.S;
-  T* ct = tmp + (size_t)slot * L.S;
+  const T* p = phi + (size_t)slot * t.S;
+  const T* f = rhs + (size_t)slot * t.S;
+  T* pp = phi + (size_t)pslot * t.S;
+  T* pt = tmp + (size_t)pslot * t.S;
+  T* ct = tmp + (size_t)slot * t.S;
   const int o0 = child_offset(t, slot, 0), o1 = child_offset(t, slot, 1);
   const int o2 = D == 3 ? child_offset(t, slot, 2) : 0;
   const int count = D == 2 ? hnc * hnc : hnc * hnc * hnc;
@@ -523,9 +474,9 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* 
             const T* y = mc.cy + ((size_t)slot * nc + (fi + di - 1)) * 4;
             k1 = y[0]; k2 = y[1]; k3 = y[2];
           }
-          const int x = L.at2(fi + di, fj + dj);
+          const int x = at2(n2, fi + di, fj + dj);
           res[dj][di] = f[x] - (otf ? apply_lpl_otf<D, CYL, T>(t, phi, p, slot, fi + di, fj + dj, 0, c, k1, k2, k3, g, r0, r1)
-                                    : apply_lpl<D, CYL, T>(p, L, fi + di, fj + dj, 0, c, k1, k2, k3));
+                                    : apply_lpl<D, CYL, T>(p, n2, fi + di, fj + dj, 0, c, k1, k2, k3));
           if (store_child_residual) ct[x] = res[dj][di];
         }
       T rv;
@@ -541,27 +492,27 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* 
         s = s + res[0][0]; s = s + res[0][1]; s = s + res[1][0]; s = s + res[1][1];
         rv = T(0.25) * s;
       }
-      pt[L.at2(ic, jc)] = rv;
+      pt[at2(n2, ic, jc)] = rv;
       T s = T(0);
-      s = s + p[L.at2(fi, fj)]; s = s + p[L.at2(fi + 1, fj)];
-      s = s + p[L.at2(fi, fj + 1)]; s = s + p[L.at2(fi + 1, fj + 1)];
-      pp[L.at2(ic, jc)] = T(0.25) * s;
+      s = s + p[at2(n2, fi, fj)]; s = s + p[at2(n2, fi + 1, fj)];
+      s = s + p[at2(n2, fi, fj + 1)]; s = s + p[at2(n2, fi + 1, fj + 1)];
+      pp[at2(n2, ic, jc)] = T(0.25) * s;
     } else {
       T sr = T(0), sp = T(0);
       for (int dk = 0; dk < 2; dk++)
         for (int dj = 0; dj < 2; dj++)
           for (int di = 0; di < 2; di++) {
-            const int x = L.at3(fi + di, fj + dj, fk + dk);
+            const int x = at3(n2, fi + di, fj + dj, fk + dk);
             const T res =
                 f[x] - (otf ? apply_lpl_otf<D, false, T>(t, phi, p, slot, fi + di, fj + dj, fk + dk, c, T(0), T(0),
                                                          T(0), g, r0, r1)
-                            : apply_lpl<D, false, T>(p, L, fi + di, fj + dj, fk + dk, c, T(0), T(0), T(0)));
+                            : apply_lpl<D, false, T>(p, n2, fi + di, fj + dj, fk + dk, c, T(0), T(0), T(0)));
             if (store_child_residual) ct[x] = res;
             sr = sr + res;
             sp = sp + p[x];
           }
-      pt[L.at3(ic, jc, kc)] = T(0.125) * sr;
-      pp[L.at3(ic, jc, kc)] = T(0.125) * sp;
+      pt[at3(n2, ic, jc, kc)] = T(0.125) * sr;
+      pp[at3(n2, ic, jc, kc)] = T(0.125) * sp;
     }
   }
 }
@@ -590,16 +541,15 @@ __global__ void __launch_bounds__(256) k_coarse_fas(KTree t0, const int* __restr
   load_rec(rec, blockIdx.x, r0, r1);
   const int slot = r0.x;
   if (box_frozen(t, slot)) return;
-  const Lay L = lay<T>(t);
-  const int nc = t.nc, n2 = nc + 2;
+  const int nc = t.nc, n2 = t.n2;
   if (fill) {
-    T* a = phi + (size_t)slot * L.S;
+    T* a = phi + (size_t)slot * t.S;
     const int nface = D == 2 ? nc : nc * nc;
     for (int w = threadIdx.x; w < 2 * D * nface; w += blockDim.x) {
       const int nb = w / nface, pq = w - nb * nface;
       const int pi = pq % nc + 1, qi = D == 3 ? pq / nc + 1 : 0;
       const T val = face_ghost_nb<D, T>(t, phi, slot, nb, rec_nb(r0, r1, nb), pi, qi, g);
-      a[L.face<D>(nb >> 1, (nb & 1) ? nc + 1 : 0, pi, qi)] = val;
+      a[face_at<D>(n2, nb >> 1, (nb & 1) ? nc + 1 : 0, pi, qi)] = val;
     }
     __syncthreads();
     corner_ghosts<D, T>(t, phi, slot);
@@ -607,14 +557,12 @@ __global__ void __launch_bounds__(256) k_coarse_fas(KTree t0, const int* __restr
   }
   T c[7];
   for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
-  const T* p = phi + (size_t)slot * L.S;
-  T* f = rhs + (size_t)slot * L.S;
-  T* o = tmp + (size_t)slot * L.S;
-  const int ncell = D == 2 ? n2 * n2 : n2 * n2 * n2;
-  for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
-    const int i = w % n2, r = w / n2;
+  const T* p = phi + (size_t)slot * t.S;
+  T* f = rhs + (size_t)slot * t.S;
+  T* o = tmp + (size_t)slot * t.S;
+  for (int x = threadIdx.x; x < t.S; x += blockDim.x) {
+    const int i = x % n2, r = x / n2;
     const int j = D == 2 ? r : r % n2, k = D == 2 ? 0 : r / n2;
-    const int x = L.at<D>(i, j, k);
     const bool interior = i >= 1 && i <= nc && j >= 1 && j <= nc && (D == 2 || (k >= 1 && k <= nc));
     if (interior) {
       T k1 = T(0), k2 = T(0), k3 = T(0);
@@ -622,7 +570,7 @@ __global__ void __launch_bounds__(256) k_coarse_fas(KTree t0, const int* __restr
         const T* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
         k1 = y[0]; k2 = y[1]; k3 = y[2];
       }
-      const T lp = apply_lpl<D, CYL, T>(p, L, i, j, k, c, k1, k2, k3);
+      const T lp = apply_lpl<D, CYL, T>(p, n2, i, j, k, c, k1, k2, k3);
       f[x] = lp + o[x];
     }
     if (copy_tmp) o[x] = p[x];
@@ -643,11 +591,10 @@ __global__ void __launch_bounds__(256) k_correct(KTree t0, const int* __restrict
   T* sm = reinterpret_cast<T*>(smem_raw);
   const int slot = list[blockIdx.x];
   if (box_frozen(t, slot)) return;
-  const Lay L = lay<T>(t);
-  const int nc = t.nc;
-  T* pp = phi + (size_t)slot * L.S;
-  T* pt = tmp + (size_t)slot * L.S;
-  for (int x = threadIdx.x; x < L.S; x += blockDim.x) {
+  const int nc = t.nc, n2 = t.n2;
+  T* pp = phi + (size_t)slot * t.S;
+  T* pt = tmp + (size_t)slot * t.S;
+  for (int x = threadIdx.x; x < t.S; x += blockDim.x) {
     const T v = pp[x] - pt[x];
     pt[x] = v;
     sm[x] = v;
@@ -664,19 +611,19 @@ __global__ void __launch_bounds__(256) k_correct(KTree t0, const int* __restrict
     const int o0 = child_offset(t, cs, 0), o1 = child_offset(t, cs, 1);
     const int i1 = o0 + ((i + 1) >> 1), i2 = i1 + 1 - 2 * (i & 1);
     const int j1 = o1 + ((j + 1) >> 1), j2 = j1 + 1 - 2 * (j & 1);
-    T* cp = phi + (size_t)cs * L.S;
+    T* cp = phi + (size_t)cs * t.S;
     if (D == 2) {
-      const int x = L.at2(i, j);
-      cp[x] = cp[x] + T(9 / 16.0) * sm[L.at2(i1, j1)] + T(3 / 16.0) * sm[L.at2(i2, j1)] +
-              T(3 / 16.0) * sm[L.at2(i1, j2)] + T(1 / 16.0) * sm[L.at2(i2, j2)];
+      const int x = at2(n2, i, j);
+      cp[x] = cp[x] + T(9 / 16.0) * sm[at2(n2, i1, j1)] + T(3 / 16.0) * sm[at2(n2, i2, j1)] +
+              T(3 / 16.0) * sm[at2(n2, i1, j2)] + T(1 / 16.0) * sm[at2(n2, i2, j2)];
     } else {
       const int o2 = child_offset(t, cs, 2);
       const int k1 = o2 + ((k + 1) >> 1), k2 = k1 + 1 - 2 * (k & 1);
-      const int x = L.at3(i, j, k);
-      cp[x] = cp[x] + T(27 / 64.0) * sm[L.at3(i1, j1, k1)] + T(9 / 64.0) * sm[L.at3(i2, j1, k1)] +
-              T(9 / 64.0) * sm[L.at3(i1, j2, k1)] + T(3 / 64.0) * sm[L.at3(i2, j2, k1)] +
-              T(9 / 64.0) * sm[L.at3(i1, j1, k2)] + T(3 / 64.0) * sm[L.at3(i2, j1, k2)] +
-              T(3 / 64.0) * sm[L.at3(i1, j2, k2)] + T(1 / 64.0) * sm[L.at3(i2, j2, k2)];
+      const int x = at3(n2, i, j, k);
+      cp[x] = cp[x] + T(27 / 64.0) * sm[at3(n2, i1, j1, k1)] + T(9 / 64.0) * sm[at3(n2, i2, j1, k1)] +
+              T(9 / 64.0) * sm[at3(n2, i1, j2, k1)] + T(3 / 64.0) * sm[at3(n2, i2, j2, k1)] +
+              T(9 / 64.0) * sm[at3(n2, i1, j1, k2)] + T(3 / 64.0) * sm[at3(n2, i2, j1, k2)] +
+              T(3 / 64.0) * sm[at3(n2, i1, j2, k2)] + T(1 / 64.0) * sm[at3(n2, i2, j2, k2)];
     }
   }
 }
@@ -692,12 +639,11 @@ __global__ void __launch_bounds__(256) k_init_phi_rhs(KTree t0, const int* __res
   const int slot = list[blockIdx.x];
   if (box_frozen(t, slot)) return;
   const int pslot = t.parent[slot];
-  const Lay L = lay<T>(t);
-  const int nc = t.nc, hnc = nc / 2;
-  T* p = phi + (size_t)slot * L.S;
-  const T* f = rhs + (size_t)slot * L.S;
-  T* pf = rhs + (size_t)pslot * L.S;
-  for (int x = threadIdx.x; x < L.S; x += blockDim.x) p[x] = T(0);
+  const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
+  T* p = phi + (size_t)slot * t.S;
+  const T* f = rhs + (size_t)slot * t.S;
+  T* pf = rhs + (size_t)pslot * t.S;
+  for (int x = threadIdx.x; x < t.S; x += blockDim.x) p[x] = T(0);
   const int o0 = child_offset(t, slot, 0), o1 = child_offset(t, slot, 1);
   const int o2 = D == 3 ? child_offset(t, slot, 2) : 0;
   const int count = D == 2 ? hnc * hnc : hnc * hnc * hnc;
@@ -712,22 +658,22 @@ __global__ void __launch_bounds__(256) k_init_phi_rhs(KTree t0, const int* __res
         const double* gw = t.geo + ((size_t)pslot * nc + (ic - 1)) * 4;
         const T w1 = T(gw[2]), w2 = T(gw[3]);
         T s1 = T(0), s2 = T(0);
-        s1 = s1 + f[L.at2(fi, fj)]; s1 = s1 + f[L.at2(fi, fj + 1)];
-        s2 = s2 + f[L.at2(fi + 1, fj)]; s2 = s2 + f[L.at2(fi + 1, fj + 1)];
+        s1 = s1 + f[at2(n2, fi, fj)]; s1 = s1 + f[at2(n2, fi, fj + 1)];
+        s2 = s2 + f[at2(n2, fi + 1, fj)]; s2 = s2 + f[at2(n2, fi + 1, fj + 1)];
         rv = T(0.25) * (w1 * s1 + w2 * s2);
       } else {
         T s = T(0);
-        s = s + f[L.at2(fi, fj)]; s = s + f[L.at2(fi + 1, fj)];
-        s = s + f[L.at2(fi, fj + 1)]; s = s + f[L.at2(fi + 1, fj + 1)];
+        s = s + f[at2(n2, fi, fj)]; s = s + f[at2(n2, fi + 1, fj)];
+        s = s + f[at2(n2, fi, fj + 1)]; s = s + f[at2(n2, fi + 1, fj + 1)];
         rv = T(0.25) * s;
       }
-      pf[L.at2(ic, jc)] = rv;
+      pf[at2(n2, ic, jc)] = rv;
     } else {
       T s = T(0);
       for (int dk = 0; dk < 2; dk++)
         for (int dj = 0; dj < 2; dj++)
-          for (int di = 0; di < 2; di++) s = s + f[L.at3(fi + di, fj + dj, fk + dk)];
-      pf[L.at3(ic, jc, kc)] = T(0.125) * s;
+          for (int di = 0; di < 2; di++) s = s + f[at3(n2, fi + di, fj + dj, fk + dk)];
+      pf[at3(n2, ic, jc, kc)] = T(0.125) * s;
     }
   }
 }
@@ -741,7 +687,7 @@ __global__ void __launch_bounds__(256) k_copy(KTree t, const int* __restrict__ l
   T* __restrict__ dst = dst_.get();
   const int slot = list[blockIdx.x];
   if (box_frozen(t, slot)) return;
-  const int S = lay<T>(t).S;
+  const int S = t.S;
   for (int x = threadIdx.x; x < S; x += blockDim.x) dst[(size_t)slot * S + x] = src[(size_t)slot * S + x];
 }
 
@@ -797,7 +743,7 @@ __global__ void k_coarse_scatter(KTree t, int n, const int* __restrict__ cslot, 
   if (g >= n) return;
   const int slot = cslot[g];
   if (box_frozen(t, slot)) return;
-  phi[(size_t)slot * lay<T>(t).S + ccell[g]] = T(x[g]);
+  phi[(size_t)slot * t.S + ccell[g]] = T(x[g]);
 }
 
 // Freeze flags of batched instances as the kernels read them: the converged
@@ -818,15 +764,14 @@ __global__ void __launch_bounds__(256) k_maxabs(KTree t0, const int* __restrict_
   const KTree t = fix_dims<D, NC>(t0);
   __shared__ T sred[32];
   const int slot = list[blockIdx.x];
-  const Lay L = lay<T>(t);
-  const int nc = t.nc;
-  const T* a = v + (size_t)slot * L.S;
+  const int nc = t.nc, n2 = t.n2;
+  const T* a = v + (size_t)slot * t.S;
   const int count = D == 2 ? nc * nc : nc * nc * nc;
   T mx = T(0);
   for (int w = threadIdx.x; w < count; w += blockDim.x) {
     const int i = w % nc + 1, r = w / nc;
     const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
-    acc_absmax(mx, a[D == 2 ? L.at2(i, j) : L.at3(i, j, k)]);
+    acc_absmax(mx, a[D == 2 ? at2(n2, i, j) : at3(n2, i, j, k)]);
   }
   mx = block_max<T>(mx, sred);
   if (threadIdx.x == 0) atomic_max_nonneg(inst_max(t, maxbits, slot), double(mx));

@@ -42,9 +42,8 @@ __global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict_
   const int slot = r0.x;
   if (box_frozen(t, slot)) return;
   const int nc = t.nc, n2 = t.n2;
-  const Lay L32 = lay<float>(t);
-  float* eo = e32 + (size_t)slot * L32.S;
-  for (int x = threadIdx.x; x < L32.S; x += blockDim.x) eo[x] = 0.0f;
+  float* eo = e32 + (size_t)slot * t.S;
+  for (int x = threadIdx.x; x < t.S; x += blockDim.x) eo[x] = 0.0f;
   // parents need no defect: the V-cycle's restriction overwrites their rhs
   if (!is_leaf[slot]) return;
   double* pw_ = phi + (size_t)slot * t.S;
@@ -62,7 +61,7 @@ __global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict_
   for (int q = 0; q < 7; q++) cd[q] = mc.cb[slot * 8 + q];
   const double* p = pw_;
   const double* f = rhs + (size_t)slot * t.S;
-  float* ro = r32 + (size_t)slot * L32.S;
+  float* ro = r32 + (size_t)slot * t.S;
   float mx = 0.0f;
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;
   for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
@@ -86,32 +85,36 @@ __global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict_
                    fma(cd[4], p[x + n2], fma(cd[3], p[x - n2], fma(cd[2], p[x + 1], fma(cd[1], p[x - 1], cd[0] * p[x]))))));
     }
     const float res = d2f(f[x] - lp);
-    ro[L32.at<D>(i, j, k)] = res;
+    ro[x] = res;
     mx = fmaxf(mx, fabsf(res));
   }
   mx = block_max<float>(mx, sred);
   if (threadIdx.x == 0) atomic_max_nonneg(inst_max(t, maxbits, slot), f2d(mx));
 }
 
-// phi += e on whole boxes (ghost cells included); phi in afivo's layout
-// (cell w of the (nc+2)^D block at w), e in the FP32 layout
-template <int D, int NC = 0>
-__global__ void __launch_bounds__(256) k_add_correction(KTree t0, const int* __restrict__ list, ModeArg<double> phi_,
+// Whole-box conversions between the FP64 variables and the FP32 buffers
+__global__ void __launch_bounds__(256) k_to_f32(int S, const int* __restrict__ list, const double* __restrict__ src,
+                                                float* __restrict__ dst) {
+  const size_t base = (size_t)list[blockIdx.x] * S;
+  for (int x = threadIdx.x; x < S; x += blockDim.x) dst[base + x] = d2f(src[base + x]);
+}
+__global__ void __launch_bounds__(256) k_to_f64(int S, const int* __restrict__ list, const float* __restrict__ src,
+                                                double* __restrict__ dst) {
+  const size_t base = (size_t)list[blockIdx.x] * S;
+  for (int x = threadIdx.x; x < S; x += blockDim.x) dst[base + x] = f2d(src[base + x]);
+}
+
+// phi += e on whole boxes (ghost cells included)
+__global__ void __launch_bounds__(256) k_add_correction(KTree t, const int* __restrict__ list, ModeArg<double> phi_,
                                                         ModeArg<const float> e32_) {
-  const KTree t = fix_dims<D, NC>(t0);
   double* __restrict__ phi = phi_.get();
   const float* __restrict__ e32 = e32_.get();
   const int slot = list[blockIdx.x];
   if (box_frozen(t, slot)) return;
-  const Lay L32 = lay<float>(t);
-  const int n2 = t.n2;
-  double* p = phi + (size_t)slot * t.S;
-  const float* e = e32 + (size_t)slot * L32.S;
-  for (int w = threadIdx.x; w < t.S; w += blockDim.x) {
-    const int i = w % n2, r = w / n2;
-    const int j = D == 2 ? r : r % n2, k = D == 2 ? 0 : r / n2;
-    p[w] = p[w] + f2d(e[L32.at<D>(i, j, k)]);
-  }
+  const int S = t.S;
+  double* p = phi + (size_t)slot * S;
+  const float* e = e32 + (size_t)slot * S;
+  for (int x = threadIdx.x; x < S; x += blockDim.x) p[x] = p[x] + f2d(e[x]);
 }
 
 }  // namespace afg
@@ -138,20 +141,6 @@ static int launch_defect(afg_ctx* ctx, MgSlot& m, ModeArg<double> phi, ModeArg<c
   else
     AFG_NC2(NCV_, k_defect<2, false, NCV_><<<grid, 256, 0, ctx->stream>>>(t, list, phi, rhs, r32, e32, c, g, ctx->d_is_leaf,
                                                    maxbits));
-  ctx->launches++;
-  CKL();
-  return AFG_OK;
-}
-
-// phi += e on the boxes of a list
-static int launch_add_correction(afg_ctx* ctx, const int* list, int n, ModeArg<double> phi, ModeArg<const float> e32) {
-  if (n <= 0) return AFG_OK;
-  const KTree t = ktree(ctx);
-  const dim3 grid(n, ctx->ky);
-  if (ctx->D == 3)
-    AFG_NC3(NCV_, k_add_correction<3, NCV_><<<grid, 256, 0, ctx->stream>>>(t, list, phi, e32));
-  else
-    AFG_NC2(NCV_, k_add_correction<2, NCV_><<<grid, 256, 0, ctx->stream>>>(t, list, phi, e32));
   ctx->launches++;
   CKL();
   return AFG_OK;
@@ -216,7 +205,10 @@ static int mixed_fmg(afg_ctx* ctx, MgSlot& m, ModeArg<double> phi, ModeArg<doubl
   RC(launch_defect(ctx, m, phi, rhs, ModeArg<unsigned long long>(ctx->d_max + 2)));
   RC(mg_fmg<float>(ctx, m, slot_bufs(ctx, m, &MgSlot::e32), slot_bufs(ctx, m, &MgSlot::r32),
                    slot_bufs(ctx, m, &MgSlot::t32), false, false, nullptr, true));
-  RC(launch_add_correction(ctx, list, n, phi, ModeArg<const float>(slot_bufs(ctx, m, &MgSlot::e32))));
+  k_add_correction<<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(ktree(ctx), list, phi,
+                                                             ModeArg<const float>(slot_bufs(ctx, m, &MgSlot::e32)));
+  ctx->launches++;
+  CKL();
   RC(mixed_prepare(ctx, m, phi));
   if (set_residual) RC(launch_defect(ctx, m, phi, rhs, maxbits));
   return mixed_finish(ctx, m, phi);

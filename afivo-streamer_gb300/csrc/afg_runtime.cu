@@ -72,7 +72,6 @@ struct afg_ctx {
   // tree
   bool have_tree = false;
   int D = 2, nc = 16, n2 = 18, S = 324, NF = 289, coord = AFG_XYZ, n_boxes = 0, highest_lvl = 0;
-  int S32 = lay32_S(2, 16);  // values per box of the FP32 buffers (sector-aligned layout)
   int cgs[3] = {1, 1, 1};
   std::vector<int> h_ix;      // [n][D]
   std::vector<int> h_nbr;     // [n][2D] raw Fortran ids
@@ -102,7 +101,6 @@ struct afg_ctx {
   unsigned char* d_is_leaf = nullptr;
   int* d_cslot = nullptr;   // coarse unknown -> slot (instance-major on batched trees)
   int* d_ccell = nullptr;   // coarse unknown -> cell index
-  int* d_ccell32 = nullptr; // the same in the FP32 layout
   // Batched independent instances (afg_tree_sync_batched); n_inst = 0 for a
   // single tree.  The coarse grids of all instances are alike (nloc
   // unknowns each) and share one inverse.
@@ -224,9 +222,6 @@ static KTree ktree(const afg_ctx* c) {
   t.n2 = c->n2;
   t.S = c->S;
   t.NF = c->NF;
-  t.py32 = lay32_py(c->nc);
-  t.pz32 = lay32_py(c->nc) * (c->nc + 2);
-  t.S32 = c->S32;
   t.parent = c->d_parent;
   t.children = c->d_children;
   t.nbr = c->d_nbr;
@@ -293,7 +288,7 @@ static void free_tree(afg_ctx* c) {
   clear_graphs(c);
   dfree(c->d_parent); dfree(c->d_children); dfree(c->d_nbr); dfree(c->d_pnb); dfree(c->d_nbmat);
   dfree(c->d_ix); dfree(c->d_rmin); dfree(c->d_dr); dfree(c->d_idr); dfree(c->d_idrf); dfree(c->d_lists); dfree(c->d_rec); dfree(c->d_is_leaf); dfree(c->d_geo);
-  dfree(c->d_cslot); dfree(c->d_ccell); dfree(c->d_ccell32);
+  dfree(c->d_cslot); dfree(c->d_ccell);
   dfree(c->d_inst); dfree(c->d_frozen); dfree(c->d_frozen_base); dfree(c->d_inst_hl);
   if (c->h_frozen) cudaFreeHost(c->h_frozen);
   c->h_frozen = nullptr;
@@ -371,7 +366,8 @@ template <int D, bool CYL, typename T, int NC, int CPT, bool SR>
 static int launch_gsrb_tma(afg_ctx* ctx, const int* rec, int n, ModeArg<T> phi, ModeArg<const T> rhs, int rb,
                            ModeCoef<T> lam, const GcDev& g) {
   constexpr int TPB = (D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT;
-  constexpr size_t smem = (SR ? 4 : 2) * StageLay<T, D, NC>::SS * sizeof(T);
+  constexpr int S = D == 2 ? (NC + 2) * (NC + 2) : (NC + 2) * (NC + 2) * (NC + 2);
+  constexpr size_t smem = (SR ? 4 : 2) * S * sizeof(T);
   static int per_sm = 0;
   if (per_sm == 0) {
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gsrb_tma<D, CYL, T, NC, CPT, SR>, TPB, smem));
@@ -519,7 +515,7 @@ template <typename T>
 static int launch_correct(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, ModeArg<T> tmp) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
-  const size_t sm = sizeof(T) * (sizeof(T) == 4 ? ctx->S32 : ctx->S);
+  const size_t sm = sizeof(T) * ctx->S;
   if (ctx->D == 3)
     AFG_NC3(NCV_, k_correct<3, T, NCV_><<<dim3(n, ctx->ky), 256, sm, ctx->stream>>>(t, list, phi, tmp));
   else
@@ -738,15 +734,14 @@ static int mg_coarse_solve(afg_ctx* ctx, MgSlot& m, ModeArg<T> phi, ModeArg<cons
   ModeArg<const double> ainv(m.d_ainv);
   for (int k = 1; k < ctx->ky; k++) ainv.p[k] = ctx->grp[k]->d_ainv;
   const dim3 g128((n + 127) / 128, ctx->ky), g8((n + 7) / 8, ctx->ky);
-  const int* ccell = sizeof(T) == 4 ? ctx->d_ccell32 : ctx->d_ccell;
-  k_coarse_gather<T><<<g128, 128, 0, ctx->stream>>>(n, nloc, ctx->D, ctx->d_cslot, ccell, m.d_b2r, m.d_bmask,
-                                                    bcv, stride, rhs, sizeof(T) == 4 ? ctx->S32 : ctx->S, b);
+  k_coarse_gather<T><<<g128, 128, 0, ctx->stream>>>(n, nloc, ctx->D, ctx->d_cslot, ctx->d_ccell, m.d_b2r, m.d_bmask,
+                                                    bcv, stride, rhs, ctx->S, b);
   ctx->launches++;
   CKL();
   k_coarse_matvec<<<g8, 256, 0, ctx->stream>>>(n, nloc, ainv, ModeArg<const double>(b), x);
   ctx->launches++;
   CKL();
-  k_coarse_scatter<T><<<g128, 128, 0, ctx->stream>>>(ktree(ctx), n, ctx->d_cslot, ccell,
+  k_coarse_scatter<T><<<g128, 128, 0, ctx->stream>>>(ktree(ctx), n, ctx->d_cslot, ctx->d_ccell,
                                                      ModeArg<const double>(x), phi);
   ctx->launches++;
   CKL();
@@ -937,7 +932,7 @@ static int autotune_gsrb(afg_ctx* ctx, MgSlot& m) {
   RC(rc);
   ctx->gsrb_cpt[0] = best_c;
   // the correction buffers were only smoothed with zero data; clear them
-  const size_t N = (size_t)ctx->n_boxes * ctx->S32;
+  const size_t N = (size_t)ctx->n_boxes * ctx->S;
   CK(cudaMemsetAsync(m.e32, 0, N * sizeof(float), ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return AFG_OK;
@@ -1024,7 +1019,10 @@ static int mixed_iter_graph(afg_ctx* ctx, MgSlot& m) {
   RC(run_graph(ctx, gkey("mixed_iter", mg_id), [&]() -> int {
     RC(mg_vcycle<float>(ctx, m, ctx->highest_lvl, m.e32, m.r32, m.t32, false, true, nullptr));
     // leaves only: mixed_prepare restricts the parents from them
-    RC(launch_add_correction(ctx, lst(ctx, ctx->off_all_leaves), ctx->n_all_leaves, phi, m.e32));
+    k_add_correction<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), lst(ctx, ctx->off_all_leaves), phi,
+                                                                m.e32);
+    ctx->launches++;
+    CKL();
     RC(mixed_prepare(ctx, m, phi));
     RC(reset_max(ctx, 2));
     return launch_defect(ctx, m, phi, rhs, ctx->d_max + 2);
@@ -1224,7 +1222,6 @@ int afg_tree_sync_batched(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, 
   ctx->nc = nc;
   ctx->n2 = nc + 2;
   ctx->S = D == 2 ? (nc + 2) * (nc + 2) : (nc + 2) * (nc + 2) * (nc + 2);
-  ctx->S32 = lay32_S(D, nc);
   ctx->NF = D == 2 ? (nc + 1) * (nc + 1) : (nc + 1) * (nc + 1) * (nc + 1);
   ctx->coord = t->coord;
   ctx->n_boxes = n;
@@ -1364,7 +1361,7 @@ int afg_tree_sync_batched(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, 
   // places with the same geometry
   const long nloc = (long)ctx->cgs[0] * ctx->cgs[1] * ctx->cgs[2];
   const long ncoarse = nloc * rows;
-  std::vector<int> cslot(ncoarse, -1), ccell(ncoarse, 0), ccell32(ncoarse, 0);
+  std::vector<int> cslot(ncoarse, -1), ccell(ncoarse, 0);
   if (nloc <= kMaxCoarse) {
     std::vector<int> first(nloc, -1);  // instance-0 box of each coarse cell
     for (int s : ctx->lvl_ids[0]) {
@@ -1382,7 +1379,6 @@ int afg_tree_sync_batched(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, 
             if (cslot[g] >= 0) return fail(ctx, AFG_ERR_ARG, "level-1 boxes overlap");
             cslot[g] = s;
             ccell[g] = i + ctx->n2 * (j + ctx->n2 * (D == 3 ? k : 0));
-            ccell32[g] = 7 + i + lay32_py(nc) * (j + (nc + 2) * (D == 3 ? k : 0));
             if (q == 0) first[gl] = s;
           }
     }
@@ -1411,7 +1407,6 @@ int afg_tree_sync_batched(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, 
   CK(dalloc(&ctx->d_is_leaf, n));
   CK(dalloc(&ctx->d_cslot, ncoarse));
   CK(dalloc(&ctx->d_ccell, ncoarse));
-  CK(dalloc(&ctx->d_ccell32, ncoarse));
   CK(cudaMemcpy(ctx->d_parent, parent.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_children, children.data(), sizeof(int) * children.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_nbr, nbr.data(), sizeof(int) * nbr.size(), cudaMemcpyHostToDevice));
@@ -1453,7 +1448,6 @@ int afg_tree_sync_batched(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, 
   CK(cudaMemcpy(ctx->d_is_leaf, is_leaf.data(), n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_cslot, cslot.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_ccell, ccell.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(ctx->d_ccell32, ccell32.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
   // per-instance tables: depth, finest dr (af_min_dr), cells per level
   ctx->inst_hl.assign(rows, 0);
   ctx->inst_min_dr.assign(rows, 0.0);
@@ -2012,7 +2006,7 @@ int afg_mg_setup(afg_ctx* ctx, int mg_id, const afg_mg_desc* d) {
     CK(cudaStreamSynchronize(ctx->stream));
   }
   if (d->precision == AFG_MIXED) {
-    const size_t N = (size_t)ctx->n_boxes * ctx->S32;
+    const size_t N = (size_t)ctx->n_boxes * ctx->S;
     if (dalloc(&m.e32, N) != cudaSuccess || dalloc(&m.r32, N) != cudaSuccess || dalloc(&m.t32, N) != cudaSuccess)
       return fail(ctx, AFG_ERR_NOMEM, "cannot allocate FP32 pools");
     CK(cudaMemset(m.e32, 0, N * sizeof(float)));
