@@ -65,6 +65,9 @@ class StreamerModel:
     td_max: float = 1000.0
     bc_species: int = ag.BC_NEUMANN
     photoi_species_index: int = 1     # species that gains the photoionization source with e
+    # a transport table read from data (x in Td, its inv_fac, and the columns
+    # mobility*N, diffusion*N, alpha/N, eta/N); replaces mu/dif/alpha/eta
+    tabulated: dict = None
 
     # variable layout (1-based tree indices)
     def __post_init__(self):
@@ -94,16 +97,22 @@ class StreamerModel:
         """Transport lookup table over the reduced field (columns: mu*N,
         D*N, alpha/N, eta/N, then one column per tabulated reaction)."""
         N = self.N
-        x, inv_fac = table_x(0.0, self.td_max, self.table_size)
-        E = x * TD_TO_SI * N
-        with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
-            a = self.alpha(E) if self.alpha else np.zeros_like(E)
-            h = self.eta(E) if self.eta else np.zeros_like(E)
-        a = np.where(np.isfinite(a), a, 0.0)
-        h = np.where(np.isfinite(h), h, 0.0)
-        mobN = np.full_like(x, self.mu * N)
-        difN = np.full_like(x, self.dif * N)
-        cols = [mobN, difN, a / N, h / N]
+        if self.tabulated is not None:
+            x, inv_fac = self.tabulated["x"], self.tabulated["inv_fac"]
+            cols = [np.asarray(c, dtype=np.float64) for c in self.tabulated["cols"]]
+            has_eta = True
+        else:
+            x, inv_fac = table_x(0.0, self.td_max, self.table_size)
+            E = x * TD_TO_SI * N
+            with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+                a = self.alpha(E) if self.alpha else np.zeros_like(E)
+                h = self.eta(E) if self.eta else np.zeros_like(E)
+            a = np.where(np.isfinite(a), a, 0.0)
+            h = np.where(np.isfinite(h), h, 0.0)
+            mobN = np.full_like(x, self.mu * N)
+            difN = np.full_like(x, self.dif * N)
+            cols = [mobN, difN, a / N, h / N]
+            has_eta = self.eta is not None
         self.col_mobility, self.col_diffusion, self.col_alpha, self.col_eta = 0, 1, 2, 3
         self.lt_x = x
         self.lt_inv_fac = inv_fac
@@ -114,7 +123,7 @@ class StreamerModel:
                 dict(type=ag.RATE_TABULATED_FIELD, col=len(cols), ix_in=[0], ix_out=[0, 1], mult=[2, 1]),
             ]
             cols.append(cols[2] * cols[0] * x * TD_TO_SI * N)
-            if self.eta is not None and len(self.species) > 2:
+            if has_eta and len(self.species) > 2:
                 self.reactions.append(
                     dict(type=ag.RATE_TABULATED_FIELD, col=len(cols), ix_in=[0], ix_out=[2], mult=[1]))
                 cols.append(cols[3] * cols[0] * x * TD_TO_SI * N)

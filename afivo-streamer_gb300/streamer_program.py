@@ -1,0 +1,623 @@
+"""The reference's `streamer` program around the hot path, for the
+configurations this path supports.
+
+This is the caller side of the hot path: it reads a reference configuration
+file (`.cfg`, the m_config format), builds the transport lookup table from
+the reference's transport-data file, sets the initial conditions, runs the
+initial refinement loop and the time loop with the reference's time-step
+control, refinement cadence and output times, and writes the regression-log
+rows the reference's own tests compare (`output_regression_log`,
+src/m_output.f90:787-842).  Every numerical stage runs on an engine: the
+GPU engine (`GpuEngine`, through the C-ABI) here, the CPU restatement in the
+oracle's tests.  What it restates:
+
+* `.cfg` syntax and the defaults of the keys it reads (m_config; defaults in
+  src/m_streamer.f90, m_refine.f90, m_dt.f90, m_field.f90, m_table_data.f90,
+  m_init_cond.f90, m_output.f90, m_gas.f90);
+* table_from_file (src/m_table_data.f90:86-176), LT_get_spaced_data /
+  LT_lin_interp_list (src/lookup_table_fortran/m_lookup_table.f90:142-254),
+  the old-style transport table (src/m_transport_data.f90:61-106) and the
+  standard two-reaction chemistry (src/m_chemistry.f90:222-257);
+* init_cond_set_box (src/m_init_cond.f90:214-293) with GM_density_line
+  (src/m_geometry.f90);
+* set_initial_conditions (src/streamer.f90:480-533) and the time loop
+  (src/streamer.f90:181-432).
+
+Keys whose values would need code outside the path (electrodes, dielectrics,
+photoionization, gas dynamics, other integrators' IMEX forms, chemistry
+files, stochastic densities, energy equation) raise `Unsupported`.
+"""
+from __future__ import annotations
+
+import math
+import os
+import shlex
+
+import numpy as np
+
+import afivo_gpu as ag
+import afivo_tree as at
+import streamer_model as sm
+
+
+class Unsupported(ValueError):
+    """A configuration value this path does not implement."""
+
+
+# ---------------------------------------------------------------------------
+# configuration files
+
+
+def read_cfg(path):
+    """m_config's file format: `name = value(s)` lines, `[section]` lines that
+    prefix the following names with `section%`, `#` comments.  Returns
+    {name: [tokens]} with string tokens."""
+    out = {}
+    prefix = ""
+    with open(path) as f:
+        for raw in f:
+            line = raw.split("#", 1)[0].strip()
+            if not line:
+                continue
+            if line.startswith("[") and line.endswith("]"):
+                prefix = line[1:-1].strip() + "%"
+                continue
+            if "=" not in line:
+                raise ValueError(f"{path}: cannot parse line: {raw.strip()}")
+            name, val = line.split("=", 1)
+            name = name.strip()
+            if "%" not in name:
+                name = prefix + name
+            out[name] = shlex.split(val.replace(",", " "))
+    return out
+
+
+def _to_float(tok):
+    return float(tok.lower().replace("d", "e"))
+
+
+def _to_bool(tok):
+    t = tok.lower().strip(".")
+    if t in ("t", "true"):
+        return True
+    if t in ("f", "false"):
+        return False
+    raise ValueError(f"not a logical: {tok}")
+
+
+class ProgramConfig:
+    """The settings of one run with the reference's defaults; `path` is a
+    `.cfg` file, `overrides` a dict of extra `name: value` entries."""
+
+    def __init__(self, path=None, overrides=None, ndim=2):
+        raw = read_cfg(path) if path else {}
+        for k, v in (overrides or {}).items():
+            raw[k] = [str(x) for x in (v if isinstance(v, (list, tuple)) else [v])]
+        self.raw, self.used = raw, set()
+        self.base_dir = os.path.dirname(os.path.abspath(path)) if path else os.getcwd()
+        D = self.ndim = ndim
+        g = self._get
+        # m_streamer.f90
+        self.cylindrical = g("cylindrical", False, bool)
+        self.end_time = g("end_time", 10e-9)
+        self.box_size = g("box_size", 8, int)
+        self.domain_len = g("domain_len", [16e-3] * D, n=D)
+        self.domain_origin = g("domain_origin", [0.0] * D, n=D)
+        self.coarse_grid_size = g("coarse_grid_size", [-1] * D, int, n=D)
+        self.periodic = g("periodic", [False] * D, bool, n=D)
+        self.multigrid_num_vcycles = g("multigrid_num_vcycles", 2, int)
+        self.multigrid_max_rel_residual = g("multigrid_max_rel_residual", 1e-4)
+        self.prolong_density = g("prolong_density", "limit", str)
+        self.species_boundary_condition = g("species_boundary_condition", "neumann_zero", str)
+        self.memory_limit_GB = g("memory_limit_GB", 4.0 ** (D - 1))
+        # m_gas.f90
+        self.gas_pressure = g("gas%pressure", 1.0)
+        self.gas_temperature = g("gas%temperature", 300.0)
+        self.gas_components = g("gas%components", ["N2", "O2"], str, n=None)
+        self.gas_fractions = g("gas%fractions", [0.8, 0.2], n=None)
+        # m_field.f90
+        self.field_amplitude = g("field_amplitude", None)
+        self.field_bc_type = g("field_bc_type", "homogeneous", str)
+        # m_transport_data.f90, m_table_data.f90
+        self.input_data_file = g("input_data%file", None, str)
+        self.input_data_old_style = g("input_data%old_style", False, bool)
+        self.table_size = g("table_data%size", 1000, int)
+        self.table_min_townsend = g("table_data%min_townsend", 0.0)
+        self.table_max_townsend = g("table_data%max_townsend", -1.0)
+        self.input_interpolation = g("table_data%input_interpolation", "linear", str)
+        self.table_xspacing = g("table_data%xspacing", "linear", str)
+        # m_init_cond.f90
+        self.background_density = g("background_density", 0.0)
+        self.seed_density = g("seed_density", [], n=None)
+        n_seed = len(self.seed_density)
+        self.seed_rel_r0 = g("seed_rel_r0", [], n=None)
+        self.seed_rel_r1 = g("seed_rel_r1", [], n=None)
+        self.seed_charge_type = g("seed_charge_type", [], int, n=None)
+        self.seed_width = g("seed_width", [], n=None)
+        self.seed_falloff = g("seed_falloff", ["smoothstep"] * n_seed, str, n=None)
+        self.seed_density2 = g("seed_density2", list(self.seed_density), n=None)
+        # m_refine.f90
+        self.refine_buffer_width = g("refine_buffer_width", 4, int)
+        self.refine_per_steps = g("refine_per_steps", 2, int)
+        self.refine_min_dx = g("refine_min_dx", 1.0e-7)
+        self.refine_max_dx = g("refine_max_dx", 1.0e-3)
+        self.refine_adx = g("refine_adx", 1.0)
+        self.refine_adx_fac = g("refine_adx_fac", 1.0)
+        self.derefine_dx = g("derefine_dx", 1e-4)
+        self.refine_init_time = g("refine_init_time", 10e-9)
+        self.refine_init_fac = g("refine_init_fac", 0.25)
+        self.refine_min_dens = g("refine_min_dens", -1.0e99)
+        self.refine_use_alpha_effective = g("refine_use_alpha_effective", False, bool)
+        # m_dt.f90
+        self.dt_max = g("dt_max", 1.0e-11)
+        self.dt_min = g("dt_min", 1.0e-14)
+        self.dt_safety_factor = g("dt_safety_factor", 0.9)
+        self.dt_cfl_number = g("dt_cfl_number", 0.5)
+        self.dt_chemistry_nmin = g("dt_chemistry_nmin", -1.0)
+        self.dt_chemistry_limit_loss = g("dt_chemistry_limit_loss", True, bool)
+        self.dt_max_growth_factor = g("dt_max_growth_factor", 2.0)
+        self.time_integrator = g("time_integrator", "heuns_method", str)
+        # m_output.f90
+        self.output_dt = g("output%dt", 1.0e-10)
+        self.output_name = g("output%name", "output/sim", str)
+        self.output_regression_test = g("output%regression_test", False, bool)
+        self._check_supported()
+
+    def _get(self, name, default, typ=float, n=1):
+        if name not in self.raw:
+            return default
+        self.used.add(name)
+        toks = self.raw[name]
+        conv = {float: _to_float, int: int, bool: _to_bool, str: str}[typ]
+        vals = [conv(t) for t in toks]
+        if n == 1:
+            if len(vals) != 1:
+                raise ValueError(f"{name}: expected one value, got {toks}")
+            return vals[0]
+        if n is not None and len(vals) != n:
+            raise ValueError(f"{name}: expected {n} values, got {toks}")
+        return vals
+
+    # keys that only affect output files or are informational
+    _IGNORED = {"output%name", "memory_limit_GB", "output%regression_test", "output%dt"}
+    # keys whose given value must equal the supported one
+    _FIXED = {
+        "photoi%enabled": False, "use_electrode": False, "use_dielectric": False,
+        "gas%dynamics": False, "compute_power_density": False,
+    }
+
+    def _check_supported(self):
+        for name, want in self._FIXED.items():
+            if name in self.raw:
+                self.used.add(name)
+                if _to_bool(self.raw[name][0]) != want:
+                    raise Unsupported(f"{name} = {self.raw[name][0]} is not supported on this path")
+        if not self.input_data_old_style:
+            raise Unsupported("only input_data%old_style = t transport data is supported")
+        if self.input_interpolation != "linear" or self.table_xspacing != "linear":
+            raise Unsupported("only linear table interpolation and spacing are supported")
+        if any(self.periodic):
+            raise Unsupported("periodic domains are not supported")
+        if self.field_bc_type != "homogeneous" or self.field_amplitude is None:
+            raise Unsupported("only field_amplitude with field_bc_type = homogeneous is supported")
+        if self.species_boundary_condition != "neumann_zero" or self.prolong_density != "limit":
+            raise Unsupported("species_boundary_condition / prolong_density other than the defaults")
+        if self.time_integrator not in TIME_INTEGRATORS:
+            raise Unsupported(f"time_integrator = {self.time_integrator}")
+        unknown = set(self.raw) - self.used - self._IGNORED
+        if unknown:
+            raise Unsupported("configuration keys not supported on this path: " + ", ".join(sorted(unknown)))
+
+
+# af_integrator_names (afivo/src/m_af_advance.f90) -> the stage tables of
+# streamer_model.INTEGRATORS
+TIME_INTEGRATORS = {
+    "forward_euler": "forward_euler", "midpoint_method": "midpoint", "heuns_method": "heun",
+    "ssprk33": "ssprk33", "ssprk43": "ssprk43", "rk4": "rk4",
+}
+
+
+# ---------------------------------------------------------------------------
+# transport data and lookup tables
+
+
+def table_from_file(path, data_name):
+    """table_from_file (src/m_table_data.f90:86-176): find the line equal to
+    `data_name`, read FACTOR:/COMMENT: lines up to a line of dashes, then two
+    columns until the next dashes; y is multiplied by the factor."""
+    with open(path) as f:
+        lines = [ln.rstrip("\n") for ln in f]
+    n = 0
+    while n < len(lines) and lines[n].rstrip() != data_name:
+        n += 1
+    if n == len(lines):
+        raise ValueError(f"{path}: no data named '{data_name}'")
+    n += 1
+    factor = 1.0
+    while True:
+        s = lines[n].strip()
+        n += 1
+        if s.startswith("-----"):
+            break
+        if s.startswith("FACTOR:"):
+            factor = _to_float(s[7:].split()[0])
+        elif not s.startswith("COMMENT:"):
+            raise ValueError(f"{path}: unknown statement '{s}'")
+    xs, ys = [], []
+    while True:
+        s = lines[n].strip()
+        n += 1
+        if s.startswith("-----"):
+            break
+        if s == "" or s.startswith("#"):
+            continue
+        a, b = s.split()[:2]
+        xs.append(_to_float(a))
+        ys.append(_to_float(b))
+    return np.array(xs), factor * np.array(ys)
+
+
+def lin_interp_list(x_list, y_list, x):
+    """LT_lin_interp_list with find_index_adaptive (m_lookup_table.f90:
+    101-181): clamped at both ends; inside, the first index whose x is >= the
+    value and the weights (1 - t, t)."""
+    if x <= x_list[0]:
+        return y_list[0]
+    if x >= x_list[-1]:
+        return y_list[-1]
+    ix = int(np.searchsorted(x_list, x, side="left"))   # first x_list[ix] >= x
+    t = (x - x_list[ix - 1]) / (x_list[ix] - x_list[ix - 1])
+    return (1 - t) * y_list[ix - 1] + t * y_list[ix]
+
+
+def spaced_data(x_in, y_in, new_x):
+    """LT_get_spaced_data (m_lookup_table.f90:240-254)."""
+    if np.min(np.diff(x_in)) <= 0:
+        raise ValueError("transport data x should strictly increase")
+    return np.array([lin_interp_list(x_in, y_in, float(x)) for x in new_x])
+
+
+def old_style_columns(path, N, table_size, td_min, td_max_cfg):
+    """The four columns of td_tbl from old-style data
+    (src/m_transport_data.f90:68-105): mobility*N, diffusion*N, alpha/N,
+    eta/N on a linear table in Td from table_min_townsend to the last field
+    of the mobility data (or table_max_townsend)."""
+    def rd(name, scale_y):
+        x, y = table_from_file(path, name)
+        x = x * sm.SI_TO_TD / N
+        y = y * N if scale_y else y / N
+        return x, y
+    xm, ym = rd("efield[V/m]_vs_mu[m2/Vs]", True)
+    td_max = xm[-1] if td_max_cfg < 0 else td_max_cfg
+    x, inv_fac = sm.table_x(td_min, td_max, table_size)
+    cols = [spaced_data(xm, ym, x)]
+    for name, up in (("efield[V/m]_vs_dif[m2/s]", True), ("efield[V/m]_vs_alpha[1/m]", False),
+                     ("efield[V/m]_vs_eta[1/m]", False)):
+        cols.append(spaced_data(*rd(name, up), x))
+    return x, inv_fac, cols
+
+
+def model_from_config(cfg: ProgramConfig) -> sm.StreamerModel:
+    """The fluid model of a configuration: species e, M+, M- of the standard
+    chemistry, the old-style transport table, the integrator's state copies."""
+    N = sm.gas_number_density(cfg.gas_pressure, cfg.gas_temperature)
+    path = cfg.input_data_file
+    if not os.path.isabs(path):
+        path = os.path.join(cfg.base_dir, path)
+    x, inv_fac, cols = old_style_columns(path, N, cfg.table_size, cfg.table_min_townsend,
+                                         cfg.table_max_townsend)
+    integ = TIME_INTEGRATORS[cfg.time_integrator]
+    m = sm.StreamerModel(ndim=cfg.ndim, n_states=sm.states_needed(integ), N=N,
+                         tabulated=dict(x=x, inv_fac=inv_fac, cols=cols))
+    m.integrator = integ
+    return m
+
+
+# ---------------------------------------------------------------------------
+# initial conditions
+
+
+def box_centers_with_ghosts(tree, ids):
+    """af_r_cc over cells 0..nc+1 of boxes `ids` (1-based): shape
+    [len(ids), D, (k,) j, i] (C order, i fastest)."""
+    nc, D = tree.n_cell, tree.ndim
+    idx = np.arange(0, nc + 2, dtype=np.float64) - 0.5
+    out = np.empty((len(ids), D) + (nc + 2,) * D)
+    for d in range(D):
+        shape = [1] * D
+        shape[D - 1 - d] = nc + 2
+        r = tree.r_min[ids - 1, d][:, None] + idx[None, :] * tree.dr[ids - 1, d][:, None]
+        out[:, d] = r.reshape((len(ids),) + tuple(shape))
+    return out
+
+
+def _dist_vec_line(r, r0, r1):
+    """GM_dist_vec_line (src/m_geometry.f90): r has the dimension first."""
+    D = r.shape[0]
+    line_len2 = 0.0
+    for d in range(D):
+        line_len2 = line_len2 + (r1[d] - r0[d]) * (r1[d] - r0[d])
+    frac = np.zeros(r.shape[1:])
+    for d in range(D):
+        frac = frac + (r[d] - r0[d]) * (r1[d] - r0[d])
+    lo, hi = frac <= 0.0, frac >= line_len2
+    dv = np.empty_like(r)
+    for d in range(D):
+        mid = r[d] - (r0[d] + frac / line_len2 * (r1[d] - r0[d])) if line_len2 > 0 else r[d] - r0[d]
+        dv[d] = np.where(lo, r[d] - r0[d], np.where(hi, r[d] - r1[d], mid))
+    frac = np.where(lo, 0.0, np.where(hi, 1.0, frac / line_len2 if line_len2 > 0 else 0.0))
+    return dv, frac
+
+
+def density_line(r, r0, r1, n0, n1, width, falloff):
+    """GM_density_line (src/m_geometry.f90) for the fall-off types sigmoid,
+    gaussian, smoothstep and step; r has the dimension first."""
+    dv, frac = _dist_vec_line(r, r0, r1)
+    s = np.zeros(r.shape[1:])
+    for d in range(r.shape[0]):
+        s = s + dv[d] * dv[d]
+    dist = np.sqrt(s)
+    if falloff == "smoothstep":
+        t = dist / width - 1
+        val = np.where(dist < width, 1.0,
+                       np.where(dist < 2 * width, 1 - (3 * (t * t) - 2 * (t * t * t)), 0.0))
+    elif falloff == "gaussian":
+        q = dist / width
+        val = np.exp(-(q * q))
+    elif falloff == "sigmoid":
+        tmp = dist / width
+        with np.errstate(over="ignore"):
+            val = np.where(tmp > math.log(0.5 * np.finfo(np.float64).max), 0.0, 2 / (1 + np.exp(tmp)))
+    elif falloff == "step":
+        val = np.where(dist < width, 1.0, 0.0)
+    else:
+        raise Unsupported(f"seed_falloff = {falloff}")
+    return val * (frac * n0 + (1 - frac) * n1)
+
+
+def seeds(cfg: ProgramConfig):
+    """Seed end points in metres (src/m_init_cond.f90:98-101)."""
+    D = cfg.ndim
+    L, O = np.asarray(cfg.domain_len), np.asarray(cfg.domain_origin)
+    out = []
+    for n in range(len(cfg.seed_density)):
+        r0 = np.asarray(cfg.seed_rel_r0[D * n:D * (n + 1)]) * L + O
+        r1 = np.asarray(cfg.seed_rel_r1[D * n:D * (n + 1)]) * L + O
+        out.append((r0, r1))
+    return out
+
+
+def initial_densities(cfg: ProgramConfig, tree, ids):
+    """init_cond_set_box (src/m_init_cond.f90:214-293) for boxes `ids`,
+    ghost cells included: (electrons, positive ions), each
+    [len(ids), (nc+2)^D]."""
+    r = box_centers_with_ghosts(tree, ids)
+    n2 = (tree.n_cell + 2) ** tree.ndim
+    e = np.full(r.shape[:1] + r.shape[2:], cfg.background_density)
+    ion = e.copy()
+    rr = np.moveaxis(r, 1, 0)
+    for n, (r0, r1) in enumerate(seeds(cfg)):
+        dens = density_line(rr, r0, r1, cfg.seed_density[n], cfg.seed_density2[n], cfg.seed_width[n],
+                            cfg.seed_falloff[n])
+        ct = cfg.seed_charge_type[n]
+        if ct == -1:
+            e = e + dens
+        elif ct == 0:
+            ion = ion + dens
+            e = e + dens
+        elif ct == 1:
+            ion = ion + dens
+        else:
+            raise ValueError("invalid seed_charge_type")
+    return e.reshape(len(ids), n2), ion.reshape(len(ids), n2)
+
+
+def refine_desc(cfg: ProgramConfig, model: sm.StreamerModel, time: float):
+    """default_refinement's parameters (src/m_refine.f90:197-298) at `time`:
+    the seed rule only while time < refine_init_time."""
+    d = model.refine_desc(adx=cfg.refine_adx, adx_fac=cfg.refine_adx_fac, min_dens=cfg.refine_min_dens,
+                          derefine_dx=cfg.derefine_dx, max_dx=cfg.refine_max_dx, min_dx=cfg.refine_min_dx,
+                          ref_buffer=cfg.refine_buffer_width, init_fac=cfg.refine_init_fac,
+                          use_alpha_effective=int(cfg.refine_use_alpha_effective))
+    if time < cfg.refine_init_time:
+        sd = seeds(cfg)
+        if len(sd) > ag.AFG_MAX_REFINE_ITEMS:
+            raise Unsupported("too many seeds")
+        d.n_seeds = len(sd)
+        for n, (r0, r1) in enumerate(sd):
+            for k in range(cfg.ndim):
+                d.seed_r0[n][k] = r0[k]
+                d.seed_r1[n][k] = r1[k]
+            d.seed_width[n] = cfg.seed_width[n]
+    return d
+
+
+def total_volume(tree):
+    """af_total_volume (afivo/src/m_af_types.f90:805-825): the coarse boxes'
+    volume, rings of pi (r1^2 - r0^2) L_z in 2D cylindrical coordinates."""
+    box_len = tree.n_cell * np.asarray(tree.dr_base, dtype=np.float64)
+    ids = np.asarray(tree.lvl_ids[0]) - 1
+    if tree.ndim == 2 and tree.coord == at.AF_CYL:
+        vol = 0.0
+        for b in ids:
+            r0 = float(tree.r_min[b, 0])
+            r1 = r0 + box_len[0]
+            vol = vol + math.pi * (r1 ** 2 - r0 ** 2) * box_len[-1]
+        return vol
+    return len(ids) * float(np.prod(box_len))
+
+
+def regression_values(tree, leaf_values):
+    """output_regression_log's columns (src/m_output.f90:787-842) for one
+    species: sum(n)/vol and sum(n^2)/vol over leaves with af_tree_sum_cc's
+    level-by-level accumulation (afivo/src/m_af_utils.f90:966-1026; in 2D
+    cylindrical coordinates the sum of 2 pi r n per cell, sum_2pr_box), and
+    the maximum over leaves.  `leaf_values[l]` holds the interiors of the
+    leaves of level l+1 as [n_leaves, nc^D] in the reference's cell order
+    (i fastest)."""
+    nc, D = tree.n_cell, tree.ndim
+    cyl = D == 2 and tree.coord == at.AF_CYL
+    twopi = 2 * math.acos(-1.0)
+    s1 = s2 = 0.0
+    mx = -np.finfo(np.float64).max / 10
+    for lvl in range(1, tree.highest_lvl + 1):
+        v = leaf_values[lvl - 1]
+        if v.size == 0:
+            continue
+        ids = np.asarray(tree.lvl_leaves[lvl - 1]) - 1
+        fac = float(np.prod(tree.dr[ids[0]]))
+        for q, b in enumerate(ids):
+            x = v[q]
+            if cyl:
+                r = tree.r_min[b, 0] + (np.arange(1, nc + 1) - 0.5) * tree.dr[b, 0]
+                w = np.tile(r, nc)
+                t1 = float(np.sum(x * w)) * twopi
+                t2 = float(np.sum(x * x * w)) * twopi
+            else:
+                t1, t2 = float(np.sum(x)), float(np.sum(x * x))
+            s1 = s1 + fac * t1
+            s2 = s2 + fac * t2
+        mx = max(mx, float(v.max()))
+    vol = total_volume(tree)
+    return s1 / vol, s2 / vol, mx
+
+
+# ---------------------------------------------------------------------------
+# the program
+
+
+AF_MAX_LVL = 30                     # af_max_lvl (afivo/src/m_af_types.f90)
+MAX_ATTEMPTS_PER_TIME_STEP = 10     # src/streamer.f90
+
+
+class Program:
+    """set_initial_conditions and the time loop of the `streamer` program
+    (src/streamer.f90:181-432, 480-533) over an engine.
+
+    `engine_factory(tree, model, voltage, cfg)` returns an object with:
+    `tree`; `set_initial(ids, electrons, ions)` (state 0 of the first two
+    species, ghost cells included); `field(have_guess)` (field_compute of
+    state 0); `advance(dt)` (copy_current_state, the integrator's
+    forward_euler stages; returns the last stage's dt limit
+    min(dt_max, cfl_number/max cfl_sum, dielectric relaxation time,
+    chemistry limit)); `restore()` (restore_previous_state);
+    `refine(desc, restrict_first)` (af_restrict_tree + af_gc_tree of the
+    densities when `restrict_first`, the refinement flags, af_adjust_refinement
+    with auto_prolong; returns (n_add, n_rm, added ids)); and
+    `leaf_values(species)` (interiors of the leaves per level).
+    """
+
+    def __init__(self, cfg: ProgramConfig, engine_factory, log=None):
+        self.cfg = cfg
+        self.model = model_from_config(cfg)
+        D = cfg.ndim
+        L = np.asarray(cfg.domain_len, dtype=np.float64)
+        cgs = list(cfg.coarse_grid_size)
+        if all(c == -1 for c in cgs):
+            cgs = [cfg.box_size * int(round(v / L.min())) for v in L]
+        self.cgs = np.asarray(cgs)
+        self.voltage = -cfg.domain_len[D - 1] * cfg.field_amplitude
+        self.factory = engine_factory
+        self.log = log
+        self.rows = []
+        self.n_steps = self.n_rejected = 0
+
+    def _say(self, *a):
+        if self.log:
+            self.log(*a)
+
+    def initial_tree(self):
+        """af_init plus af_refine_up_to_lvl to the first level whose grid
+        spacing is at most refine_max_dx (src/streamer.f90:486-490)."""
+        dr_base = np.asarray(self.cfg.domain_len) / self.cgs
+        for lvl in range(1, AF_MAX_LVL):
+            if np.all(dr_base / 2.0 ** (lvl - 1) <= self.cfg.refine_max_dx):
+                break
+        coord = at.AF_CYL if self.cfg.cylindrical else at.AF_XYZ
+        return at.uniform_tree(self.cfg.ndim, self.cfg.box_size, self.cgs, self.cfg.domain_len, lvl,
+                               coord=coord, r_base=np.asarray(self.cfg.domain_origin, dtype=np.float64))
+
+    def set_initial_conditions(self):
+        cfg = self.cfg
+        tree = self.initial_tree()
+        self.engine = eng = self.factory(tree, self.model, self.voltage, cfg)
+        ids = np.arange(1, tree.n_boxes + 1, dtype=np.int32)
+        eng.set_initial(ids, *initial_densities(cfg, tree, ids))
+        for n in range(100):
+            eng.field(False)
+            n_add, n_rm, added = eng.refine(refine_desc(cfg, self.model, 0.0), False)
+            self._say(f"initial refinement {n}: +{n_add} -{n_rm} boxes, {eng.tree.n_boxes} in use")
+            if len(added):
+                eng.set_initial(added, *initial_densities(cfg, eng.tree, added))
+            if n_add == 0:
+                break
+
+    def regression_row(self, cnt, time, dt):
+        vals = [self.engine_values(s) for s in range(len(self.model.species))]
+        row = [cnt, time, dt] + [v[0] for v in vals] + [v[1] for v in vals] + [v[2] for v in vals]
+        self.rows.append(row)
+        self._say("row", " ".join(f"{x:.8e}" for x in row[1:]))
+        return row
+
+    def engine_values(self, s):
+        return regression_values(self.engine.tree, self.engine.leaf_values(s))
+
+    def run(self, end_time=None, max_outputs=None):
+        """The time loop until `end_time` (default: the configuration's), or
+        until `max_outputs` rows after the initial one; returns the rows of
+        the regression log."""
+        cfg, eng = self.cfg, self.engine
+        end_time = cfg.end_time if end_time is None else end_time
+        time = global_time = 0.0
+        dt = global_dt = cfg.dt_min
+        it = it_last_output = output_cnt = 0
+        time_last_output = time
+        frac_rejected = 0.0
+        self.regression_row(0, global_time, global_dt)
+        while True:
+            it += 1
+            if time >= end_time or (max_outputs is not None and output_cnt >= max_outputs):
+                break
+            write_out = time + dt >= time_last_output + cfg.output_dt
+            if write_out:
+                dt = min(dt, max(0.0, time_last_output + cfg.output_dt - time))
+            dt_lim = 1e100
+            for n in range(MAX_ATTEMPTS_PER_TIME_STEP):
+                lim = eng.advance(dt)
+                time = time + dt
+                dt_lim = min(dt_lim, lim)
+                if dt <= lim:
+                    break
+                self.n_rejected += 1
+                dt = cfg.dt_safety_factor * lim
+                time = global_time
+                write_out = False
+                eng.restore()
+            else:
+                raise RuntimeError("All time steps were rejected")
+            frac_rejected = 0.99 * frac_rejected + (0.01 if n > 0 else 0.0)
+            eng.field(True)
+            growth = 1.0 if frac_rejected > 0.1 else cfg.dt_max_growth_factor
+            dt = min(growth * global_dt, cfg.dt_safety_factor * min(dt_lim, cfg.dt_max))
+            global_dt, global_time = dt, time
+            self.n_steps += 1
+            if global_dt < cfg.dt_min:
+                raise RuntimeError(f"dt too small ({global_dt:.4e})")
+            if write_out:
+                output_cnt += 1
+                time_last_output, it_last_output = global_time, it
+                self.regression_row(output_cnt, global_time, global_dt)
+            if it % cfg.refine_per_steps == 0:
+                n_add, n_rm, _ = eng.refine(refine_desc(cfg, self.model, global_time), True)
+                if n_add > 0 or n_rm > 0:
+                    eng.field(True)
+        return self.rows
+
+
+def read_regression_log(path):
+    """Rows of a regression log (src/m_output.f90:787-842): header names and
+    a float array [n_rows, 3 + 3 * n_species]."""
+    with open(path) as f:
+        head = f.readline().split()
+        rows = [[float(v) for v in ln.split()] for ln in f if ln.strip()]
+    return head, np.array(rows)

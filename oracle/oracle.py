@@ -53,6 +53,8 @@ def lib():
             "orc_photoi_source": (C.c_int, [P, DP, C.c_double, C.c_int]),
             "orc_refine_flags": (C.c_int, [P, DP, C.c_void_p, C.POINTER(C.c_int)]),
             "orc_prolong_limit": (C.c_int, [P, DP, C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int]),
+            "orc_prolong_linear": (C.c_int, [P, DP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+            "orc_restrict_tree": (C.c_int, [P, DP, C.c_int]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -181,6 +183,14 @@ class Oracle:
         a = np.ascontiguousarray(ids, dtype=np.int32)
         self._ck(self.L.orc_prolong_limit(self.p, _dp(cc), iv, len(a), a.ctypes.data_as(C.POINTER(C.c_int)),
                                           limiter), "prolong_limit")
+
+    def prolong_linear(self, cc, iv, ids):
+        a = np.ascontiguousarray(ids, dtype=np.int32)
+        self._ck(self.L.orc_prolong_linear(self.p, _dp(cc), iv, len(a), a.ctypes.data_as(C.POINTER(C.c_int))),
+                 "prolong_linear")
+
+    def restrict_tree(self, cc, iv):
+        self._ck(self.L.orc_restrict_tree(self.p, _dp(cc), iv), "restrict_tree")
 
     def maxabs(self, cc, iv, leaves_only=True):
         return self.L.orc_maxabs(self.p, _dp(cc), iv, int(leaves_only))

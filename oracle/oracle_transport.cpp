@@ -925,4 +925,84 @@ int orc_prolong_limit(void* p, double* cc, int iv, int n, const int* ids, int li
   return AFG_OK;
 }
 
+/* af_prolong_linear with add = .false. (afivo/src/m_af_prolong.f90:531-679)
+ * into boxes ids[]: per fine cell the parent value (weight 9/16, 27/64 in
+ * 3D), its face neighbours (3/16; 9/64), and in 3D edge (3/64) and corner
+ * (1/64) neighbours, 2D corner (1/16), summed in the reference's order and
+ * added to the zeroed child cell. */
+int orc_prolong_linear(void* p, double* cc, int iv, int n, const int* ids) {
+  Oracle* o = static_cast<Oracle*>(p);
+  const Tree& t = o->t;
+  const int nc = t.nc, hnc = nc / 2, D = t.D;
+  for (int q = 0; q < n; q++) {
+    const int id = ids[q], p_id = t.parent[id - 1];
+    if (p_id <= 0) return AFG_ERR_ARG;
+    const double* P = t.var(cc, p_id, iv);
+    double* C = t.var(cc, id, iv);
+    const int o0 = t.child_offset(id, 0), o1 = t.child_offset(id, 1), o2 = D == 3 ? t.child_offset(id, 2) : 0;
+    for (int k = 1; k <= (D == 3 ? nc : 1); k++)
+      for (int j = 1; j <= nc; j++)
+        for (int i = 1; i <= nc; i++) C[D == 3 ? t.at(i, j, k) : t.at(i, j)] = 0;
+    if (D == 2) {
+      const double f1 = 1 / 16.0, f3 = 3 / 16.0, f9 = 9 / 16.0;
+      for (int j = 1; j <= hnc; j++)
+        for (int i = 1; i <= hnc; i++) {
+          const int ic = i + o0, jc = j + o1, fi = 2 * i - 1, fj = 2 * j - 1;
+          const double f0 = f9 * P[t.at(ic, jc)];
+          const double flx = f3 * P[t.at(ic - 1, jc)], fhx = f3 * P[t.at(ic + 1, jc)];
+          const double fly = f3 * P[t.at(ic, jc - 1)], fhy = f3 * P[t.at(ic, jc + 1)];
+          const double fll = f1 * P[t.at(ic - 1, jc - 1)], fhl = f1 * P[t.at(ic + 1, jc - 1)];
+          const double flh = f1 * P[t.at(ic - 1, jc + 1)], fhh = f1 * P[t.at(ic + 1, jc + 1)];
+          C[t.at(fi, fj)] = f0 + flx + fly + fll + C[t.at(fi, fj)];
+          C[t.at(fi + 1, fj)] = f0 + fhx + fly + fhl + C[t.at(fi + 1, fj)];
+          C[t.at(fi, fj + 1)] = f0 + flx + fhy + flh + C[t.at(fi, fj + 1)];
+          C[t.at(fi + 1, fj + 1)] = f0 + fhx + fhy + fhh + C[t.at(fi + 1, fj + 1)];
+        }
+    } else {
+      const double w[4] = {27 / 64.0, 9 / 64.0, 3 / 64.0, 1 / 64.0};  // by number of offsets
+      for (int k = 1; k <= hnc; k++)
+        for (int j = 1; j <= hnc; j++)
+          for (int i = 1; i <= hnc; i++) {
+            const int ic = i + o0, jc = j + o1, kc = k + o2;
+            const int fi = 2 * i - 1, fj = 2 * j - 1, fk = 2 * k - 1;
+            for (int dk = 0; dk < 2; dk++)
+              for (int dj = 0; dj < 2; dj++)
+                for (int di = 0; di < 2; di++) {
+                  const int sx = di ? 1 : -1, sy = dj ? 1 : -1, sz = dk ? 1 : -1;
+                  /* terms in the reference's order: 000, x00, 0y0, 00z, xy0, x0z, 0yz, xyz */
+                  const int ox[8] = {0, sx, 0, 0, sx, sx, 0, sx};
+                  const int oy[8] = {0, 0, sy, 0, sy, 0, sy, sy};
+                  const int oz[8] = {0, 0, 0, sz, 0, sz, sz, sz};
+                  const int x = t.at(fi + di, fj + dj, fk + dk);
+                  double s = w[0] * P[t.at(ic, jc, kc)];
+                  for (int m = 1; m < 8; m++) {
+                    const int nof = (ox[m] != 0) + (oy[m] != 0) + (oz[m] != 0);
+                    s = s + w[nof] * P[t.at(ic + ox[m], jc + oy[m], kc + oz[m])];
+                  }
+                  C[x] = s + C[x];
+                }
+          }
+    }
+  }
+  return AFG_OK;
+}
+
+/* af_restrict_tree (afivo/src/m_af_restrict.f90:50-59) of one variable:
+ * from the highest level's parents down to level 1, each child restricted
+ * into its parent by af_restrict_box with geometry */
+int orc_restrict_tree(void* p, double* cc, int iv) {
+  Oracle* o = static_cast<Oracle*>(p);
+  const Tree& t = o->t;
+  for (int lvl = t.highest_lvl - 1; lvl >= 1; lvl--) {
+    const std::vector<int>& par = t.parents[lvl - 1];
+#pragma omp parallel for schedule(static)
+    for (size_t q = 0; q < par.size(); q++)
+      for (int c = 0; c < t.nchild(); c++) {
+        const int ch = t.child_of(par[q], c);
+        if (ch > 0) restrict_box_geom(t, cc, ch, iv);
+      }
+  }
+  return AFG_OK;
+}
+
 }  // extern "C"

@@ -1,0 +1,27 @@
+"""Copy the reference's regression-test inputs and stored logs used as
+golden fixtures (run in a checkout that has the reference next to it).
+
+The files are the reference's own data: two configurations of its
+`standard_2d` program (Cartesian and axisymmetric, no photoionization), the
+old-style transport data they read, and the regression logs its test runner
+compares at rtol 1e-5 (programs/standard_2d/tests/, tools/compare_logs.py).
+"""
+import os
+import shutil
+import sys
+
+SRC = "programs/standard_2d/tests"
+FILES = ["test_2d.cfg", "test_2d_rtest.log", "test_cyl.cfg", "test_cyl_rtest.log",
+         "td_air_siglo_swarm.txt"]
+
+
+def main(reference_root):
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "standard_2d")
+    os.makedirs(out, exist_ok=True)
+    for f in FILES:
+        shutil.copyfile(os.path.join(reference_root, SRC, f), os.path.join(out, f))
+        print("copied", f)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
