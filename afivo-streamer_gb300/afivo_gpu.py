@@ -270,6 +270,8 @@ def load_library(path: str = LIB_PATH):
         "afg_check_bounded_wait": (C.c_int, [P, _DP]),
         "afg_refine_flags": (C.c_int, [P, C.POINTER(RefineDesc), _IP]),
         "afg_prolong_limit": (C.c_int, [P, C.c_int, C.c_int, _IP, C.c_int]),
+        "afg_prolong_linear": (C.c_int, [P, C.c_int, C.c_int, _IP]),
+        "afg_restrict_tree": (C.c_int, [P, C.c_int]),
         "afg_tree_remap": (C.c_int, [P, C.POINTER(TreeDesc), _IP]),
         "afg_host_unregister": (C.c_int, [P, C.c_void_p]),
         "afg_sync": (C.c_int, [P]),
@@ -361,6 +363,13 @@ class Context:
     def prolong_limit(self, iv, ids, limiter):
         a = np.ascontiguousarray(ids, dtype=np.int32)
         self.check(self.lib.afg_prolong_limit(self.ptr, iv, len(a), _ip(a), limiter), "afg_prolong_limit")
+
+    def prolong_linear(self, iv, ids):
+        a = np.ascontiguousarray(ids, dtype=np.int32)
+        self.check(self.lib.afg_prolong_linear(self.ptr, iv, len(a), _ip(a)), "afg_prolong_linear")
+
+    def restrict_tree(self, iv):
+        self.check(self.lib.afg_restrict_tree(self.ptr, iv), "afg_restrict_tree")
 
     def tree_remap(self, tree, old_id):
         """Mirror `tree` keeping the data: old_id[b] = id of new box b+1 in

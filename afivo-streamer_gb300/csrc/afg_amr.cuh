@@ -193,6 +193,60 @@ __global__ void __launch_bounds__(128) k_prolong_limit(KTree t, const int* __res
   }
 }
 
+// af_prolong_linear with add = .false. (m_af_prolong.f90:531-679): one CTA
+// per child box, one thread per parent cell of the child's quadrant/octant.
+// Each fine cell sums the weighted parent values in the reference's order
+// (centre, x, y, z, xy, xz, yz, xyz neighbour on the fine cell's side) and
+// adds the zeroed child value.  Weights 9,3,3,1 /16 in 2D, 27,9,3,1 /64 in
+// 3D by the number of offsets; all are exact in binary.
+template <int D>
+__global__ void __launch_bounds__(128) k_prolong_linear(KTree t, const int* __restrict__ list, double* __restrict__ v) {
+  const int slot = list[blockIdx.x];
+  const int pslot = t.parent[slot];
+  const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
+  const double* P = v + (size_t)pslot * t.S;
+  double* Cc = v + (size_t)slot * t.S;
+  const int o0 = child_offset(t, slot, 0), o1 = child_offset(t, slot, 1);
+  const int o2 = D == 3 ? child_offset(t, slot, 2) : 0;
+  const int count = D == 2 ? hnc * hnc : hnc * hnc * hnc;
+  const int sy = n2, sz = n2 * n2;
+  for (int w = threadIdx.x; w < count; w += blockDim.x) {
+    const int i = w % hnc + 1, r = w / hnc;
+    const int j = D == 2 ? r + 1 : r % hnc + 1, k = D == 2 ? 0 : r / hnc + 1;
+    const int ic = i + o0, jc = j + o1, kc = k + o2;
+    const int fi = 2 * i - 1, fj = 2 * j - 1, fk = 2 * k - 1;
+    if (D == 2) {
+      const double f1 = 1 / 16.0, f3 = 3 / 16.0, f9 = 9 / 16.0;
+      const int p = at2(n2, ic, jc);
+      const double f0 = f9 * P[p];
+      const double flx = f3 * P[p - 1], fhx = f3 * P[p + 1];
+      const double fly = f3 * P[p - sy], fhy = f3 * P[p + sy];
+      const double fll = f1 * P[p - 1 - sy], fhl = f1 * P[p + 1 - sy];
+      const double flh = f1 * P[p - 1 + sy], fhh = f1 * P[p + 1 + sy];
+      Cc[at2(n2, fi, fj)] = f0 + flx + fly + fll + 0.0;
+      Cc[at2(n2, fi + 1, fj)] = f0 + fhx + fly + fhl + 0.0;
+      Cc[at2(n2, fi, fj + 1)] = f0 + flx + fhy + flh + 0.0;
+      Cc[at2(n2, fi + 1, fj + 1)] = f0 + fhx + fhy + fhh + 0.0;
+    } else {
+      const double wt[4] = {27 / 64.0, 9 / 64.0, 3 / 64.0, 1 / 64.0};
+      const int p = at3(n2, ic, jc, kc);
+      for (int oct = 0; oct < 8; oct++) {
+        const int di = oct & 1, dj = (oct >> 1) & 1, dk = oct >> 2;
+        const int sx1 = di ? 1 : -1, sy1 = dj ? sy : -sy, sz1 = dk ? sz : -sz;
+        double s = wt[0] * P[p];
+        s = s + wt[1] * P[p + sx1];
+        s = s + wt[1] * P[p + sy1];
+        s = s + wt[1] * P[p + sz1];
+        s = s + wt[2] * P[p + sx1 + sy1];
+        s = s + wt[2] * P[p + sx1 + sz1];
+        s = s + wt[2] * P[p + sy1 + sz1];
+        s = s + wt[3] * P[p + sx1 + sy1 + sz1];
+        Cc[at3(n2, fi + di, fj + dj, fk + dk)] = s + 0.0;
+      }
+    }
+  }
+}
+
 // new pool slot <- old pool slot (whole box), for boxes that persist
 __global__ void __launch_bounds__(256) k_remap_boxes(int n_new, int S, const int* __restrict__ old_slot,
                                                      const double* __restrict__ src, double* __restrict__ dst) {
@@ -297,6 +351,58 @@ int afg_prolong_limit(afg_ctx* ctx, int iv, int n, const int* ids, int limiter) 
   }
   dfree(d_list);
   if (e != cudaSuccess) return fail(ctx, AFG_ERR_CUDA, "prolongation: %s", cudaGetErrorString(e));
+  return AFG_OK;
+}
+
+int afg_prolong_linear(afg_ctx* ctx, int iv, int n, const int* ids) {
+  RC(check_var(ctx, iv));
+  if (n < 0 || (n > 0 && !ids)) return fail(ctx, AFG_ERR_ARG, "bad box list");
+  if (n == 0) return AFG_OK;
+  std::vector<int> slots(n);
+  for (int q = 0; q < n; q++) {
+    if (ids[q] < 1 || ids[q] > ctx->n_boxes) return fail(ctx, AFG_ERR_ARG, "bad box id %d", ids[q]);
+    slots[q] = ids[q] - 1;
+    if (ctx->h_parent[slots[q]] < 0) return fail(ctx, AFG_ERR_ARG, "box %d has no parent", ids[q]);
+  }
+  int* d_list = nullptr;
+  CK(dalloc(&d_list, n));
+  cudaError_t e = cudaMemcpy(d_list, slots.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    KTree t = ktree(ctx);
+    if (ctx->D == 3)
+      k_prolong_linear<3><<<n, 128, 0, ctx->stream>>>(t, d_list, ctx->cc[iv - 1]);
+    else
+      k_prolong_linear<2><<<n, 128, 0, ctx->stream>>>(t, d_list, ctx->cc[iv - 1]);
+    ctx->launches++;
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  }
+  dfree(d_list);
+  if (e != cudaSuccess) return fail(ctx, AFG_ERR_CUDA, "linear prolongation: %s", cudaGetErrorString(e));
+  return AFG_OK;
+}
+
+int afg_restrict_tree(afg_ctx* ctx, int iv) {
+  RC(check_var(ctx, iv));
+  KTree t = ktree(ctx);
+  const bool cyl = ctx->coord == AFG_CYL;
+  double* v = ctx->cc[iv - 1];
+  for (int lvl = ctx->highest_lvl; lvl >= 2; lvl--) {
+    const int n = (int)ctx->lvl_ids[lvl - 1].size();
+    if (n == 0) continue;
+    const int* list = lst(ctx, ctx->off_ids[lvl - 1]);
+    if (ctx->D == 3)
+      AFG_NC3(NCV_, k_restrict_geom<3, false, NCV_><<<n, 64, 0, ctx->stream>>>(t, list, v));
+    else if (cyl)
+      AFG_NC2(NCV_, k_restrict_geom<2, true, NCV_><<<n, 64, 0, ctx->stream>>>(t, list, v));
+    else
+      AFG_NC2(NCV_, k_restrict_geom<2, false, NCV_><<<n, 64, 0, ctx->stream>>>(t, list, v));
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, AFG_ERR_CUDA, "restriction: %s", cudaGetErrorString(e));
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return fail(ctx, AFG_ERR_CUDA, "restriction: %s", cudaGetErrorString(e));
   return AFG_OK;
 }
 

@@ -621,3 +621,127 @@ def read_regression_log(path):
         head = f.readline().split()
         rows = [[float(v) for v in ln.split()] for ln in f if ln.strip()]
     return head, np.array(rows)
+
+
+class GpuEngine:
+    """The program's engine on one GPU through the C-ABI.  The state lives on
+    the device; the host sees it only for the initial values of new boxes
+    (afg_cc_upload of the chosen boxes) and the regression rows (download of
+    one density).  `precision` selects the FP64 path (the reference's
+    arithmetic) or AFG_MIXED (FP32 inner multigrid and transport with an FP64
+    state)."""
+
+    def __init__(self, tree, model, voltage, cfg, precision=ag.FP64, ctx=None):
+        self.ctx = ctx if ctx is not None else ag.Context(0)
+        self.m, self.cfg, self.voltage, self.precision = model, cfg, voltage, precision
+        # one extra variable: the backup of phi kept by copy_current_state
+        self.iv_phi_copy = model.n_var_cell + 1
+        self.n_var = model.n_var_cell + 1
+        self.stages = sm.INTEGRATORS[model.integrator]
+        self.tree = tree
+        self.ctx.tree_sync(tree, self.n_var, model.n_var_face)
+        self.run = sm.StreamerRun(self.ctx, tree, model, voltage, 0.0, precision,
+                                  max_rel_residual=cfg.multigrid_max_rel_residual,
+                                  num_vcycles=cfg.multigrid_num_vcycles, integrator=model.integrator)
+        self._setup()
+
+    def _setup(self):
+        m = self.m
+        self.run.tree = self.tree
+        self.run.setup()
+        # rhs: af_bc_neumann_zero + af_gc_interp (src/streamer.f90:74-79)
+        self.ctx.set_cc_methods(m.i_rhs, [ag.BC_NEUMANN] * (2 * self.tree.ndim), None, ag.RB_INTERP)
+
+    def set_initial(self, ids, e, ion):
+        m, t = self.m, self.tree
+        h = ag.new_cc(t, 2)
+        idx = np.asarray(ids, dtype=np.int64) - 1
+        h[idx, 0] = e.reshape((len(idx),) + h.shape[2:])
+        h[idx, 1] = ion.reshape((len(idx),) + h.shape[2:])
+        bp = ag.box_pointers(h)
+        keep = np.zeros(t.n_boxes, dtype=bool)
+        keep[idx] = True
+        bp.addr[~keep] = 0
+        self.ctx.upload_vars(h, [m.species_iv[0], m.species_iv[1]], bp=bp)
+
+    def field(self, have_guess):
+        if not have_guess:
+            self.ctx.gc(self.m.i_phi, 0, True)
+        self.run.field(0, have_guess)
+
+    def advance(self, dt):
+        ctx, m, cfg = self.ctx, self.m, self.cfg
+        for s in range(len(m.species)):
+            ctx.tree_copy_cc(m.species_iv[s], m.species_iv[s] + m.n_states - 1)
+        ctx.tree_copy_cc(m.i_phi, self.iv_phi_copy)
+        lim = 1e100
+        for i, (f, s_deriv, s_prev, w_prev, s_out) in enumerate(self.stages, 1):
+            if i > 1:
+                self.run.field(s_deriv, True)
+            fl = ctx.flux_upwind(s_deriv)
+            last = i == len(self.stages)
+            chem = ctx.update_densities(f * dt, s_deriv, s_prev, w_prev, s_out, last_step=last)
+            lim = min(cfg.dt_max, min(fl[0] * cfg.dt_cfl_number, fl[1], chem if last else 1e100, 1e100))
+        return lim
+
+    def restore(self):
+        ctx, m = self.ctx, self.m
+        for s in range(len(m.species)):
+            ctx.tree_copy_cc(m.species_iv[s] + m.n_states - 1, m.species_iv[s])
+        ctx.tree_copy_cc(self.iv_phi_copy, m.i_phi)
+
+    def auto_vars(self):
+        """(variable, prolongation) of auto_prolong: the densities and rhs by
+        af_prolong_limit (ST_prolongation_method), phi and |E| by the default
+        af_prolong_linear (src/streamer.f90:60-79, afivo/src/m_af_core.f90:
+        343-410)."""
+        m = self.m
+        out = [(m.species_iv[s], "limit") for s in range(len(m.species))]
+        out += [(m.i_phi, "linear"), (m.i_electric_fld, "linear"), (m.i_rhs, "limit")]
+        return out
+
+    def refine(self, desc, restrict_first):
+        ctx, m, tree = self.ctx, self.m, self.tree
+        if restrict_first:
+            for s in range(len(m.species)):
+                ctx.restrict_tree(m.species_iv[s])
+                ctx.gc(m.species_iv[s], 0, True)
+        flags = ctx.refine_flags(desc)
+        new = at.adjust_refinement(tree, flags, AF_MAX_LVL)
+        old_id = at.remap_ids(tree, new)
+        keep = old_id > 0
+        n_add = int(np.count_nonzero(~keep))
+        n_rm = tree.n_boxes - int(np.count_nonzero(keep))
+        if n_add == 0 and n_rm == 0:
+            return 0, 0, np.zeros(0, dtype=np.int32)
+        ctx.tree_remap(new, old_id)
+        self.tree = new
+        self._setup()
+        limiter = m.transport_desc(self.precision).prolong_limiter
+        fresh = np.nonzero(~keep)[0].astype(np.int32) + 1
+        lv = new.lvl[fresh - 1]
+        for lvl in sorted(set(lv.tolist())):
+            ids = fresh[lv == lvl]
+            for iv, how in self.auto_vars():
+                ctx.gc(iv, lvl - 1, True)
+                if how == "limit":
+                    ctx.prolong_limit(iv, ids, limiter)
+                else:
+                    ctx.prolong_linear(iv, ids)
+            for iv, _ in self.auto_vars():
+                ctx.gc(iv, lvl, True)
+        return n_add, n_rm, fresh
+
+    def leaf_values(self, s):
+        t, nc, D = self.tree, self.tree.n_cell, self.tree.ndim
+        h = ag.new_cc(t, 1)
+        self.ctx.download_vars(h, [self.m.species_iv[s]])
+        sl = (slice(1, nc + 1),) * D
+        out = []
+        for lvl in range(1, t.highest_lvl + 1):
+            ids = np.asarray(t.lvl_leaves[lvl - 1], dtype=np.int64) - 1
+            out.append(h[ids, 0][(slice(None),) + sl].reshape(len(ids), nc ** D))
+        return out
+
+    def close(self):
+        self.ctx.close()

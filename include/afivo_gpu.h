@@ -501,6 +501,21 @@ int afg_refine_flags(afg_ctx* ctx, const afg_refine_desc* d, int* box_flags);
  * concurrently). */
 int afg_prolong_limit(afg_ctx* ctx, int iv, int n, const int* ids, int limiter);
 
+/* af_prolong_linear with add = .false. (afivo/src/m_af_prolong.f90:531-679)
+ * of variable iv into the n boxes ids[] (1-based) from their parents: bi- or
+ * trilinear weights (9,3,3,1)/16 and (27,9,3,1)/64; used by auto_prolong
+ * (afivo/src/m_af_core.f90:843-881) for variables whose prolongation method
+ * is the default, e.g. phi and |E| of the streamer program.  Same
+ * preconditions as afg_prolong_limit. */
+int afg_prolong_linear(afg_ctx* ctx, int iv, int n, const int* ids);
+
+/* af_restrict_tree (afivo/src/m_af_restrict.f90:50-59) of variable iv: from
+ * the highest level down, every box restricted into its parent by
+ * af_restrict_box with geometry (cylindrical weights in 2D axisymmetric
+ * trees), as done for the densities before each refinement
+ * (src/streamer.f90:405-406). */
+int afg_restrict_tree(afg_ctx* ctx, int iv);
+
 /* Mirror a new tree (after the caller's af_adjust_refinement) keeping the
  * data: old_id[id-1] is the id box id had in the previous tree, 0 for a new
  * box (whose data starts at zero and is then filled by afg_prolong_limit).

@@ -1,0 +1,75 @@
+"""Whole runs of the reference's regression configurations on the GPU.
+
+The `streamer` program loop (streamer_program.Program) runs test_2d and
+test_cyl of the reference's standard_2d tests with every numerical stage on
+the device (GpuEngine, through the C-ABI): field solves, fluxes, updates,
+refinement flags, restriction, prolongation into new boxes and the data move
+to each new mesh.  The FP64 path follows the CPU restatement step for step
+(the same meshes, step counts and regression rows); both follow the
+reference's stored logs within the bounds its pinning test states.  The
+mixed-precision path (FP32 inner multigrid and transport, FP64 state) runs
+the same program; its rows stay within the stated bound of the logs.
+"""
+import functools
+import os
+
+import numpy as np
+import pytest
+
+import afivo_gpu as ag
+import streamer_program as sp
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "standard_2d")
+CASES = ["test_2d", "test_cyl"]
+
+# FP64 GPU rows against the restatement's: the runs take the same steps,
+# rejections and meshes; single stages are bit-exact, but over a whole run
+# (about 700 steps) the rows separate by up to 7.7e-9 relative.
+FP64_VS_ORACLE = 1e-7
+# every row against the reference's logs (as for the restatement)
+FP64_VS_LOG = 2e-3
+# mixed precision against the logs
+MIXED_VS_LOG = 1e-2
+
+
+def rel_err(a, b):
+    return np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+
+
+def run(name, factory):
+    cfg = sp.ProgramConfig(os.path.join(GOLD, name + ".cfg"))
+    prog = sp.Program(cfg, factory)
+    prog.set_initial_conditions()
+    rows = np.array(prog.run())
+    if hasattr(prog.engine, "close"):
+        prog.engine.close()
+    return prog, rows
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_run_matches_restatement_and_log(gpu_lib, name):
+    import oracle_program as op
+    po, ro = run(name, op.OracleEngine)
+    pg, rg = run(name, functools.partial(sp.GpuEngine, precision=ag.FP64))
+    head, ref = sp.read_regression_log(os.path.join(GOLD, name + "_rtest.log"))
+    assert pg.n_steps == po.n_steps and pg.n_rejected == po.n_rejected
+    assert rg.shape == ro.shape == ref.shape
+    err = rel_err(rg[:, 1:], ro[:, 1:])
+    err[np.abs(ro[:, 1:]) == 0] = np.abs(rg[:, 1:])[np.abs(ro[:, 1:]) == 0]
+    print(f"{name}: FP64 GPU vs restatement per row", " ".join(f"{x:.1e}" for x in err.max(axis=1)))
+    print(f"{name}: FP64 GPU vs restatement max rel {err.max():.3e}; "
+          f"vs log {rel_err(rg[:, 2:], ref[:, 2:])[ref[:, 2:] != 0].max():.3e}")
+    assert err.max() <= FP64_VS_ORACLE
+    assert np.allclose(rg[:, 2:], ref[:, 2:], rtol=FP64_VS_LOG, atol=1e-8)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_mixed_run_matches_log(gpu_lib, name):
+    pm, rm = run(name, functools.partial(sp.GpuEngine, precision=ag.MIXED))
+    head, ref = sp.read_regression_log(os.path.join(GOLD, name + "_rtest.log"))
+    assert rm.shape == ref.shape
+    e = rel_err(rm[:, 2:], ref[:, 2:])[ref[:, 2:] != 0]
+    print(f"{name}: mixed GPU vs log max rel {e.max():.3e} ({pm.n_steps} steps, {pm.n_rejected} rejected)")
+    assert np.allclose(rm[:, 2:], ref[:, 2:], rtol=MIXED_VS_LOG, atol=1e-8)
