@@ -157,6 +157,18 @@ class ProgramConfig:
         self.dt_chemistry_limit_loss = g("dt_chemistry_limit_loss", True, bool)
         self.dt_max_growth_factor = g("dt_max_growth_factor", 2.0)
         self.time_integrator = g("time_integrator", "heuns_method", str)
+        # m_photoi.f90, m_photoi_helmh.f90
+        self.photoi_enabled = g("photoi%enabled", False, bool)
+        self.photoi_per_steps = g("photoi%per_steps", 5, int)
+        self.photoi_method = g("photoi%method", "helmholtz", str)
+        self.photoi_eta = g("photoi%eta", 0.05)
+        self.photoi_quenching_pressure = g("photoi%quenching_pressure", 40e-3)
+        self.photoi_source_type = g("photoi%source_type", "Zheleznyak", str)
+        self.photoi_species = g("photoi%species", "O2_plus", str)
+        self.photoi_helmh_author = g("photoi_helmh%author", "Bourdon-3", str)
+        self.photoi_helmh_lambdas = g("photoi_helmh%lambdas", [], n=None)
+        self.photoi_helmh_coeffs = g("photoi_helmh%coeffs", [], n=None)
+        self.photoi_helmh_max_rel_residual = g("photoi_helmh%max_rel_residual", 1e-2)
         # m_output.f90
         self.output_dt = g("output%dt", 1.0e-10)
         self.output_name = g("output%name", "output/sim", str)
@@ -182,7 +194,7 @@ class ProgramConfig:
     _IGNORED = {"output%name", "memory_limit_GB", "output%regression_test", "output%dt"}
     # keys whose given value must equal the supported one
     _FIXED = {
-        "photoi%enabled": False, "use_electrode": False, "use_dielectric": False,
+        "use_electrode": False, "use_dielectric": False,
         "gas%dynamics": False, "compute_power_density": False,
     }
 
@@ -204,6 +216,13 @@ class ProgramConfig:
             raise Unsupported("species_boundary_condition / prolong_density other than the defaults")
         if self.time_integrator not in TIME_INTEGRATORS:
             raise Unsupported(f"time_integrator = {self.time_integrator}")
+        if self.photoi_enabled:
+            if self.photoi_method != "helmholtz" or self.photoi_source_type != "Zheleznyak":
+                raise Unsupported("photoionization other than helmholtz with the Zheleznyak source")
+            if self.photoi_species != "M_plus":
+                raise Unsupported("photoi%species must be the standard chemistry's M_plus")
+            if self.photoi_helmh_max_rel_residual != 1e-2:
+                raise Unsupported("photoi_helmh%max_rel_residual other than 1e-2")
         unknown = set(self.raw) - self.used - self._IGNORED
         if unknown:
             raise Unsupported("configuration keys not supported on this path: " + ", ".join(sorted(unknown)))
@@ -297,6 +316,43 @@ def old_style_columns(path, N, table_size, td_min, td_max_cfg):
     return x, inv_fac, cols
 
 
+def photoi_parameters(cfg: ProgramConfig):
+    """(lambdas 1/m, coeffs 1/m^2, eta * quenching factor) of the Helmholtz
+    photoionization (photoi_helmh_initialize, src/m_photoi_helmh.f90:44-160,
+    and photoi_set_src, src/m_photoi.f90:153-205)."""
+    p = cfg.gas_pressure
+    frac_O2 = 0.0
+    if "O2" in cfg.gas_components:
+        frac_O2 = cfg.gas_fractions[cfg.gas_components.index("O2")]
+    a = cfg.photoi_helmh_author
+    tables = {
+        "Luque": ([4425.38, 750.06], [337557.38, 19972.14]),
+        "Bourdon-2": ([7305.62, 44081.25], [11814508.38, 998607256.0]),
+        "Bourdon-3": ([4147.85, 10950.93, 66755.67], [1117314.935, 28692377.5, 2748842283.0]),
+    }
+    if a in tables:
+        if frac_O2 <= 0.0:
+            raise ValueError("Photoionization: no oxygen present")
+        lam, co = (np.array(v, dtype=np.float64) for v in tables[a])
+        if a == "Luque":
+            lam = lam * (frac_O2 / 0.2) * p
+            f = (frac_O2 / 0.2) * p
+            co = co * (f * f)
+        else:
+            lam = lam * frac_O2 * p
+            f = frac_O2 * p
+            co = co * (f * f)
+    elif a == "custom":
+        lam = np.array(cfg.photoi_helmh_lambdas, dtype=np.float64) * p
+        co = np.array(cfg.photoi_helmh_coeffs, dtype=np.float64) * (p * p)
+        if len(lam) < 1 or len(lam) != len(co):
+            raise ValueError("custom photoionization lambdas and coeffs missing")
+    else:
+        raise Unsupported(f"photoi_helmh%author = {a}")
+    quench = cfg.photoi_quenching_pressure / (p + cfg.photoi_quenching_pressure)
+    return lam, co, cfg.photoi_eta * quench
+
+
 def model_from_config(cfg: ProgramConfig) -> sm.StreamerModel:
     """The fluid model of a configuration: species e, M+, M- of the standard
     chemistry, the old-style transport table, the integrator's state copies."""
@@ -307,9 +363,13 @@ def model_from_config(cfg: ProgramConfig) -> sm.StreamerModel:
     x, inv_fac, cols = old_style_columns(path, N, cfg.table_size, cfg.table_min_townsend,
                                          cfg.table_max_townsend)
     integ = TIME_INTEGRATORS[cfg.time_integrator]
+    photoi = photoi_parameters(cfg) if cfg.photoi_enabled else None
     m = sm.StreamerModel(ndim=cfg.ndim, n_states=sm.states_needed(integ), N=N,
-                         tabulated=dict(x=x, inv_fac=inv_fac, cols=cols))
+                         tabulated=dict(x=x, inv_fac=inv_fac, cols=cols),
+                         photoi_modes=0 if photoi is None else len(photoi[0]))
     m.integrator = integ
+    m.photoi_params = photoi
+    m.photoi_max_rel_residual = cfg.photoi_helmh_max_rel_residual
     return m
 
 
@@ -442,7 +502,7 @@ def total_volume(tree):
         for b in ids:
             r0 = float(tree.r_min[b, 0])
             r1 = r0 + box_len[0]
-            vol = vol + math.pi * (r1 ** 2 - r0 ** 2) * box_len[-1]
+            vol = vol + math.pi * (r1 * r1 - r0 * r0) * box_len[-1]
         return vol
     return len(ids) * float(np.prod(box_len))
 
@@ -504,7 +564,9 @@ class Program:
     `refine(desc, restrict_first)` (af_restrict_tree + af_gc_tree of the
     densities when `restrict_first`, the refinement flags, af_adjust_refinement
     with auto_prolong; returns (n_add, n_rm, added ids)); and
-    `leaf_values(species)` (interiors of the leaves per level).
+    `leaf_values(species)` (interiors of the leaves per level); with
+    photoionization `photoi()` (photoi_set_src: the source from alpha and the
+    Helmholtz modes).
     """
 
     def __init__(self, cfg: ProgramConfig, engine_factory, log=None):
@@ -581,6 +643,8 @@ class Program:
             write_out = time + dt >= time_last_output + cfg.output_dt
             if write_out:
                 dt = min(dt, max(0.0, time_last_output + cfg.output_dt - time))
+            if cfg.photoi_enabled and it % cfg.photoi_per_steps == 0:
+                eng.photoi()
             dt_lim = 1e100
             for n in range(MAX_ATTEMPTS_PER_TIME_STEP):
                 lim = eng.advance(dt)
@@ -611,6 +675,8 @@ class Program:
                 n_add, n_rm, _ = eng.refine(refine_desc(cfg, self.model, global_time), True)
                 if n_add > 0 or n_rm > 0:
                     eng.field(True)
+                    if cfg.photoi_enabled:
+                        eng.photoi()
         return self.rows
 
 
@@ -642,7 +708,8 @@ class GpuEngine:
         self.ctx.tree_sync(tree, self.n_var, model.n_var_face)
         self.run = sm.StreamerRun(self.ctx, tree, model, voltage, 0.0, precision,
                                   max_rel_residual=cfg.multigrid_max_rel_residual,
-                                  num_vcycles=cfg.multigrid_num_vcycles, integrator=model.integrator)
+                                  num_vcycles=cfg.multigrid_num_vcycles, integrator=model.integrator,
+                                  photoi=model.photoi_params, photoi_per_steps=cfg.photoi_per_steps)
         self._setup()
 
     def _setup(self):
@@ -684,6 +751,10 @@ class GpuEngine:
             lim = min(cfg.dt_max, min(fl[0] * cfg.dt_cfl_number, fl[1], chem if last else 1e100, 1e100))
         return lim
 
+    def photoi(self):
+        lam, coeffs, coeff = self.m.photoi_params
+        self.ctx.photoi_helmh(coeff, self.run.mode_ids, coeffs, 1e-2, 10)
+
     def restore(self):
         ctx, m = self.ctx, self.m
         for s in range(len(m.species)):
@@ -698,6 +769,8 @@ class GpuEngine:
         m = self.m
         out = [(m.species_iv[s], "limit") for s in range(len(m.species))]
         out += [(m.i_phi, "linear"), (m.i_electric_fld, "linear"), (m.i_rhs, "limit")]
+        if m.i_photo:
+            out.append((m.i_photo, "linear"))
         return out
 
     def refine(self, desc, restrict_first):

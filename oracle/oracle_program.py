@@ -48,7 +48,8 @@ class OracleEngine:
         self.tree, self.cc, self.fc = tree, cc, fc
         self.run = osr.OracleStreamerRun(tree, m, self.voltage, 0.0,
                                          max_rel_residual=cfg.multigrid_max_rel_residual,
-                                         num_vcycles=cfg.multigrid_num_vcycles, integrator=m.integrator)
+                                         num_vcycles=cfg.multigrid_num_vcycles, integrator=m.integrator,
+                                         photoi=m.photoi_params, photoi_per_steps=cfg.photoi_per_steps)
         self.run.setup()
         self.o = self.run.o
         # rhs: af_bc_neumann_zero + af_gc_interp (src/streamer.f90:74-79)
@@ -81,6 +82,9 @@ class OracleEngine:
             lim = min(cfg.dt_max, min(fl[0] * cfg.dt_cfl_number, fl[1], chem if last else 1e100, 1e100))
         return lim
 
+    def photoi(self):
+        self.run.photoionization(self.cc)
+
     def restore(self):
         m, cc = self.m, self.cc
         for s in range(len(m.species)):
@@ -92,6 +96,8 @@ class OracleEngine:
         m = self.m
         out = [(m.species_iv[s], "limit") for s in range(len(m.species))]
         out += [(m.i_phi, "linear"), (m.i_electric_fld, "linear"), (m.i_rhs, "limit")]
+        if m.i_photo:
+            out.append((m.i_photo, "linear"))
         return out
 
     def refine(self, desc, restrict_first):

@@ -1,8 +1,9 @@
 """Copy the reference's regression-test inputs and stored logs used as
 golden fixtures (run in a checkout that has the reference next to it).
 
-The files are the reference's own data: two configurations of its
-`standard_2d` program (Cartesian and axisymmetric, no photoionization), the
+The files are the reference's own data: three configurations of its
+`standard_2d` program (Cartesian and axisymmetric without photoionization,
+Cartesian with three-mode Helmholtz photoionization), the
 old-style transport data they read, and the regression logs its test runner
 compares at rtol 1e-5 (programs/standard_2d/tests/, tools/compare_logs.py).
 """
@@ -12,7 +13,7 @@ import sys
 
 SRC = "programs/standard_2d/tests"
 FILES = ["test_2d.cfg", "test_2d_rtest.log", "test_cyl.cfg", "test_cyl_rtest.log",
-         "td_air_siglo_swarm.txt"]
+         "test_2d_photoi.cfg", "test_2d_photoi_rtest.log", "td_air_siglo_swarm.txt"]
 
 
 def main(reference_root):

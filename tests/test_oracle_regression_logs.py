@@ -10,7 +10,9 @@ reference's time-step control, refinement every second step, and the field
 solves with multigrid_num_vcycles = 2 at 1e-4 relative residual.
 
 The first row (initial conditions and initial refinement) agrees to the
-logs' 8 printed digits.  Later rows agree to a few 1e-4 relative, with the
+logs' 8 printed digits.  test_2d_photoi adds the three-mode Helmholtz
+photoionization (Bourdon-3 coefficients, every 5th step and after each mesh
+change).  Later rows agree to a few 1e-4 relative, with the
 largest difference about 1.3e-3 (the 4 ns row of test_2d, where the streamer
 accelerates): the reference's coarse-grid solve is hypre's PFMG at 1e-6
 relative tolerance, this path's an exact direct solve, and each field solve
@@ -32,6 +34,7 @@ GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "stand
 CASES = {
     "test_2d": (1e-4, 3, 2e-3),
     "test_cyl": (5e-4, 1, 2e-3),
+    "test_2d_photoi": (1e-4, 4, 1e-3),
 }
 
 
