@@ -204,8 +204,6 @@ class ProgramConfig:
                 self.used.add(name)
                 if _to_bool(self.raw[name][0]) != want:
                     raise Unsupported(f"{name} = {self.raw[name][0]} is not supported on this path")
-        if not self.input_data_old_style:
-            raise Unsupported("only input_data%old_style = t transport data is supported")
         if self.input_interpolation != "linear" or self.table_xspacing != "linear":
             raise Unsupported("only linear table interpolation and spacing are supported")
         if any(self.periodic):
@@ -219,7 +217,7 @@ class ProgramConfig:
         if self.photoi_enabled:
             if self.photoi_method != "helmholtz" or self.photoi_source_type != "Zheleznyak":
                 raise Unsupported("photoionization other than helmholtz with the Zheleznyak source")
-            if self.photoi_species != "M_plus":
+            if self.input_data_old_style and self.photoi_species != "M_plus":
                 raise Unsupported("photoi%species must be the standard chemistry's M_plus")
             if self.photoi_helmh_max_rel_residual != 1e-2:
                 raise Unsupported("photoi_helmh%max_rel_residual other than 1e-2")
@@ -316,6 +314,123 @@ def old_style_columns(path, N, table_size, td_min, td_max_cfg):
     return x, inv_fac, cols
 
 
+def to_simple_ascii(text):
+    """to_simple_ascii (src/m_chemistry.f90:1359-1400): '+' -> '_plus',
+    '-' -> '_min' (counted as charge outside brackets), '*' -> '_star',
+    '^' -> '_hat', "'" -> 'p', '(' -> '_'; 'e' has charge -1."""
+    out, charge, br = "", 0, False
+    for ch in text:
+        if ch == "(":
+            br = True
+            out += "_"
+        elif ch == ")":
+            br = False
+        elif ch == "*":
+            out += "_star"
+        elif ch == "+":
+            charge += 0 if br else 1
+            out += "_plus"
+        elif ch == "-":
+            charge -= 0 if br else 1
+            out += "_min"
+        elif ch == "^":
+            out += "_hat"
+        elif ch == "'":
+            out += "p"
+        else:
+            out += ch
+    if out in ("e", "stoch_e"):
+        charge = -1
+    return out, charge
+
+
+# rate expressions of read_reactions (src/m_chemistry.f90:1015-1100) that the
+# device evaluates: expression -> (AFG rate type, number of coefficients)
+RATE_FORMS = {
+    "c1": (ag.RATE_CONSTANT, 1),
+    "c1*(Td-c2)": (ag.RATE_LINEAR, 2),
+    "c1*exp(-(c2/(c3+Td))**2)": (ag.RATE_EXP_V1, 3),
+    "c1*exp(-(Td/c2)**2)": (ag.RATE_EXP_V2, 2),
+    "c1*exp(-(c2/(c3+Td))**c4)": (ag.RATE_K13, 4),
+    "c1*exp(-(Td/c2)**c3)": (ag.RATE_K14, 3),
+}
+
+
+def read_reactions(path, gas_components, gas_densities, N):
+    """read_reactions + parse_reaction (src/m_chemistry.f90:857-1278) for a
+    reaction file without groups or ignored species: the plasma species in
+    order of first appearance (simple-ascii names, charges) and per reaction
+    its expression, data, input/output species (0-based plasma indices),
+    output multiplicities and rate factor (gas densities of gas reactants, N
+    for M, the cm unit conversion)."""
+    with open(path) as f:
+        lines = [ln.rstrip("\n") for ln in f]
+    if any(ln.strip() == "ignored_species" for ln in lines):
+        raise Unsupported("reaction files with ignored_species")
+    n = 0
+    while lines[n].strip() != "reaction_list":
+        n += 1
+    n += 1
+    if not lines[n].startswith("-----"):
+        raise ValueError("reaction_list not followed by -----")
+    entries = []
+    for ln in lines[n + 1:]:
+        ln = ln.strip()
+        if ln.startswith("#"):
+            continue
+        if ln.startswith("-----"):
+            break
+        if ln.startswith("@"):
+            raise Unsupported("reaction groups")
+        fields = [x.strip() for x in ln.split(",") if x.strip()]
+        if len(fields) < 3 or len(fields) > 4:
+            raise ValueError(f"invalid chemistry syntax: {ln}")
+        entries.append(fields + ["m"] * (4 - len(fields)))
+    names, reactions = [], []
+    for text, how, data, unit in entries:
+        left, rfac, n_in_total = True, 1.0, 0
+        ix_in, ix_out, mult = [], [], []
+        for comp in text.split():
+            if comp == "+":
+                continue
+            if comp == "->":
+                left = False
+                continue
+            m = 1
+            if "1" <= comp[0] <= "9":
+                m, comp = int(comp[0]), comp[1:]
+            if left:
+                n_in_total += m
+            if comp in gas_components:
+                if left:
+                    rfac = rfac * gas_densities[gas_components.index(comp)]
+                continue
+            if comp == "M":
+                if left:
+                    rfac = rfac * N
+                continue
+            if comp not in names:
+                names.append(comp)
+            ix = names.index(comp)
+            if left:
+                ix_in += [ix] * m
+            elif ix in ix_out:
+                mult[ix_out.index(ix)] += m
+            else:
+                ix_out.append(ix)
+                mult.append(m)
+        if not ix_in:
+            raise ValueError(f"no input species: {text}")
+        if unit == "cm":
+            rfac = rfac * 1e-6 ** (n_in_total - 1)
+        elif unit != "m":
+            raise ValueError(f"invalid length unit {unit}")
+        reactions.append(dict(text=text, how=how, data=data, ix_in=ix_in, ix_out=ix_out, mult=mult,
+                              factor=rfac))
+    species = [to_simple_ascii(nm) for nm in names]
+    return species, reactions
+
+
 def photoi_parameters(cfg: ProgramConfig):
     """(lambdas 1/m, coeffs 1/m^2, eta * quenching factor) of the Helmholtz
     photoionization (photoi_helmh_initialize, src/m_photoi_helmh.f90:44-160,
@@ -353,20 +468,72 @@ def photoi_parameters(cfg: ProgramConfig):
     return lam, co, cfg.photoi_eta * quench
 
 
+def new_style_columns(path, table_size, td_min, td_max_cfg):
+    """td_tbl from new-style data (src/m_transport_data.f90:107-137): x in
+    Td, columns mobility*N, diffusion*N, alpha/N, eta/N as in the file."""
+    xm, ym = table_from_file(path, "Mobility *N (1/m/V/s)")
+    td_max = xm[-1] if td_max_cfg < 0 else td_max_cfg
+    x, inv_fac = sm.table_x(td_min, td_max, table_size)
+    cols = [spaced_data(xm, ym, x)]
+    for name in ("Diffusion coefficient *N (1/m/s)", "Townsend ioniz. coef. alpha/N (m2)",
+                 "Townsend attach. coef. eta/N (m2)"):
+        cols.append(spaced_data(*table_from_file(path, name), x))
+    return x, inv_fac, cols
+
+
 def model_from_config(cfg: ProgramConfig) -> sm.StreamerModel:
-    """The fluid model of a configuration: species e, M+, M- of the standard
-    chemistry, the old-style transport table, the integrator's state copies."""
+    """The fluid model of a configuration: the integrator's state copies, the
+    transport table, and either the standard chemistry (e, M+, M-; old-style
+    data) or the reactions of the data file (chemistry_initialize,
+    src/m_chemistry.f90:181-380)."""
     N = sm.gas_number_density(cfg.gas_pressure, cfg.gas_temperature)
     path = cfg.input_data_file
     if not os.path.isabs(path):
         path = os.path.join(cfg.base_dir, path)
-    x, inv_fac, cols = old_style_columns(path, N, cfg.table_size, cfg.table_min_townsend,
-                                         cfg.table_max_townsend)
     integ = TIME_INTEGRATORS[cfg.time_integrator]
     photoi = photoi_parameters(cfg) if cfg.photoi_enabled else None
+    kw = {}
+    if cfg.input_data_old_style:
+        x, inv_fac, cols = old_style_columns(path, N, cfg.table_size, cfg.table_min_townsend,
+                                             cfg.table_max_townsend)
+        ix_pos = 1
+        photoi_ix = 1
+    else:
+        x, inv_fac, cols = new_style_columns(path, cfg.table_size, cfg.table_min_townsend,
+                                             cfg.table_max_townsend)
+        gas_dens = [f * N for f in cfg.gas_fractions]
+        species, reacts = read_reactions(path, cfg.gas_components, gas_dens, N)
+        if species[0][0] != "e":
+            raise Unsupported("the first plasma species must be the electron")
+        if len(species) > ag.AFG_MAX_SPECIES or len(reacts) > ag.AFG_MAX_REACTIONS:
+            raise Unsupported("too many species or reactions for the device tables")
+        # chemtbl_fld: the tabulated rates on the transport table's grid
+        # (the same x points, src/m_chemistry.f90:348-373)
+        rlist = []
+        for r in reacts:
+            d = dict(ix_in=r["ix_in"], ix_out=r["ix_out"], mult=r["mult"], factor=r["factor"])
+            if r["how"] == "field_table":
+                xd, yd = table_from_file(path, r["data"])
+                d.update(type=ag.RATE_TABULATED_FIELD, col=len(cols))
+                cols.append(spaced_data(xd, yd, x))
+            elif r["how"] in RATE_FORMS:
+                typ, nco = RATE_FORMS[r["how"]]
+                c = [_to_float(v) for v in r["data"].split()[:nco]]
+                d.update(type=typ, c=c)
+            else:
+                raise Unsupported(f"rate expression {r['how']}")
+            rlist.append(d)
+        kw = dict(species=[sm.Species(nm, float(q)) for nm, q in species], reactions=rlist)
+        names = [nm for nm, _ in species]
+        ix_pos = next(i for i, (_, q) in enumerate(species) if q == 1)
+        if cfg.photoi_enabled and cfg.photoi_species not in names:
+            raise Unsupported(f"photoi%species {cfg.photoi_species} is not a species of the chemistry")
+        photoi_ix = names.index(cfg.photoi_species) if cfg.photoi_enabled else 1
     m = sm.StreamerModel(ndim=cfg.ndim, n_states=sm.states_needed(integ), N=N,
                          tabulated=dict(x=x, inv_fac=inv_fac, cols=cols),
-                         photoi_modes=0 if photoi is None else len(photoi[0]))
+                         photoi_modes=0 if photoi is None else len(photoi[0]),
+                         photoi_species_index=photoi_ix, **kw)
+    m.ix_pos_ion = ix_pos
     m.integrator = integ
     m.photoi_params = photoi
     m.photoi_max_rel_residual = cfg.photoi_helmh_max_rel_residual
@@ -729,7 +896,7 @@ class GpuEngine:
         keep = np.zeros(t.n_boxes, dtype=bool)
         keep[idx] = True
         bp.addr[~keep] = 0
-        self.ctx.upload_vars(h, [m.species_iv[0], m.species_iv[1]], bp=bp)
+        self.ctx.upload_vars(h, [m.species_iv[0], m.species_iv[m.ix_pos_ion]], bp=bp)
 
     def field(self, have_guess):
         if not have_guess:

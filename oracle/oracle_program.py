@@ -60,7 +60,7 @@ class OracleEngine:
         idx = np.asarray(ids) - 1
         shp = (len(idx),) + self.cc.shape[2:]
         self.cc[idx, m.species_iv[0] - 1] = e.reshape(shp)
-        self.cc[idx, m.species_iv[1] - 1] = ion.reshape(shp)
+        self.cc[idx, m.species_iv[m.ix_pos_ion] - 1] = ion.reshape(shp)
 
     def field(self, have_guess):
         if not have_guess:

@@ -1,11 +1,13 @@
 """Copy the reference's regression-test inputs and stored logs used as
 golden fixtures (run in a checkout that has the reference next to it).
 
-The files are the reference's own data: three configurations of its
-`standard_2d` program (Cartesian and axisymmetric without photoionization,
-Cartesian with three-mode Helmholtz photoionization), the
-old-style transport data they read, and the regression logs its test runner
-compares at rtol 1e-5 (programs/standard_2d/tests/, tools/compare_logs.py).
+The files are the reference's own data: five configurations of its
+`standard_2d` program (Cartesian and axisymmetric with the standard
+two-reaction chemistry, Cartesian with three-mode Helmholtz
+photoionization, and the air chemistry file with 8 species and 25 reactions
+axisymmetric and Cartesian with photoionization), the transport and
+reaction data they read, and the regression logs its test runner compares
+at rtol 1e-5 (programs/standard_2d/tests/, tools/compare_logs.py).
 """
 import os
 import shutil
@@ -13,7 +15,9 @@ import sys
 
 SRC = "programs/standard_2d/tests"
 FILES = ["test_2d.cfg", "test_2d_rtest.log", "test_cyl.cfg", "test_cyl_rtest.log",
-         "test_2d_photoi.cfg", "test_2d_photoi_rtest.log", "td_air_siglo_swarm.txt"]
+         "test_2d_photoi.cfg", "test_2d_photoi_rtest.log", "td_air_siglo_swarm.txt",
+         "test_cyl_chem.cfg", "test_cyl_chem_rtest.log", "test_2d_photoi_chem.cfg",
+         "test_2d_photoi_chem_rtest.log", "air_chemistry_v1.txt"]
 
 
 def main(reference_root):

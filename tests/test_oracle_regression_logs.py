@@ -12,7 +12,11 @@ solves with multigrid_num_vcycles = 2 at 1e-4 relative residual.
 The first row (initial conditions and initial refinement) agrees to the
 logs' 8 printed digits.  test_2d_photoi adds the three-mode Helmholtz
 photoionization (Bourdon-3 coefficients, every 5th step and after each mesh
-change).  Later rows agree to a few 1e-4 relative, with the
+change).  test_cyl_chem and test_2d_photoi_chem read the reaction file
+air_chemistry_v1.txt (8 species, 25 reactions: tabulated, constant and
+field-dependent exponential rates, gas densities folded into the rate
+factors) with new-style transport tables.  Later rows agree to a few 1e-4
+relative, with the
 largest difference about 1.3e-3 (the 4 ns row of test_2d, where the streamer
 accelerates): the reference's coarse-grid solve is hypre's PFMG at 1e-6
 relative tolerance, this path's an exact direct solve, and each field solve
@@ -35,6 +39,8 @@ CASES = {
     "test_2d": (1e-4, 3, 2e-3),
     "test_cyl": (5e-4, 1, 2e-3),
     "test_2d_photoi": (1e-4, 4, 1e-3),
+    "test_cyl_chem": (3e-4, 6, 3e-4),
+    "test_2d_photoi_chem": (3e-4, 4, 2e-3),
 }
 
 
@@ -79,6 +85,22 @@ def test_config_rejects_unsupported_keys(tmp_path):
                  "use_electrode = t\n")
     with pytest.raises(sp.Unsupported):
         sp.ProgramConfig(str(p))
+
+
+def test_reaction_file_species_and_rates():
+    cfg = sp.ProgramConfig(os.path.join(GOLD, "test_cyl_chem.cfg"))
+    m = sp.model_from_config(cfg)
+    names = [s.name for s in m.species]
+    # order of first appearance in the reaction list, as the log's header
+    head, _ = sp.read_regression_log(os.path.join(GOLD, "test_cyl_chem_rtest.log"))
+    assert ["sum(" + n + ")" for n in names] == head[3:3 + len(names)]
+    assert [s.charge for s in m.species] == [-1, 1, 1, -1, -1, -1, 1, 1]
+    assert len(m.reactions) == 25 and m.species[m.ix_pos_ion].name == "N2_plus"
+    # "e + O2 + O2 -> O2-": two O2 densities in the rate factor
+    N = m.N
+    r = m.reactions[3]
+    assert r["ix_in"] == [0] and r["ix_out"] == [names.index("O2_min")]
+    assert r["factor"] == (1.0 * (0.2 * N)) * (0.2 * N)
 
 
 def test_table_from_file_and_interpolation():
