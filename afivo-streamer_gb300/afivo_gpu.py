@@ -85,6 +85,7 @@ RATE_CONSTANT = 2
 RATE_LINEAR = 3
 RATE_EXP_V1 = 4
 RATE_EXP_V2 = 5
+RATE_K1 = 6
 RATE_K13 = 18
 RATE_K14 = 19
 LIMITER_VANLEER = 1

@@ -475,6 +475,12 @@ __device__ __forceinline__ double rate_of(const LtDev& lt, const afg_reaction& r
         return c0 * r.c[0] * (double)expf(-pow_c((float)td / (float)r.c[1], (float)r.c[2]));
       else
         return c0 * r.c[0] * exp(-pow_c(td / r.c[1], r.c[2]));
+    case AFG_RATE_K1: {
+      // electron temperature from the tabulated mean energy (eV -> K)
+      const double Te = (2 * 1.602176634e-19 / (3 * 1.380649e-23)) * lt_col(lt, r.lt_col, ix, w);
+      if (F32) return c0 * r.c[0] * (double)pow_c(300.0f / (float)Te, (float)r.c[1]);
+      return c0 * r.c[0] * pow_c(300 / Te, r.c[1]);
+    }
   }
   return 0;
 }

@@ -207,6 +207,10 @@ __device__ __forceinline__ float rate32(const LtDevF& lt, const Reac32& r, float
     case AFG_RATE_EXP_V2: { const float q = td / r.c[1]; return r.fa * r.fb * expf(-(q * q)); }
     case AFG_RATE_K13: return r.fa * r.fb * expf(-pow_c(r.c[1] / (r.c[2] + td), r.c[3]));
     case AFG_RATE_K14: return r.fa * r.fb * expf(-pow_c(td / r.c[1], r.c[2]));
+    case AFG_RATE_K1: {
+      const float Te = (float)(2 * 1.602176634e-19 / (3 * 1.380649e-23)) * lt_col_f(lt, r.lt_col, ix, w);
+      return r.fa * r.fb * pow_c(300.0f / Te, r.c[1]);
+    }
   }
   return 0.0f;
 }

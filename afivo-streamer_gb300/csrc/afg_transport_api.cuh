@@ -79,9 +79,10 @@ int afg_transport_setup(afg_ctx* ctx, const afg_transport_desc* d) {
     const afg_reaction& rc = t.reactions[r];
     const int rt = rc.rate_type;
     if (!(rt == AFG_RATE_TABULATED_FIELD || rt == AFG_RATE_CONSTANT || rt == AFG_RATE_LINEAR ||
-          rt == AFG_RATE_EXP_V1 || rt == AFG_RATE_EXP_V2 || rt == AFG_RATE_K13 || rt == AFG_RATE_K14))
+          rt == AFG_RATE_EXP_V1 || rt == AFG_RATE_EXP_V2 || rt == AFG_RATE_K13 || rt == AFG_RATE_K14 ||
+          rt == AFG_RATE_K1))
       return fail(ctx, AFG_ERR_UNSUPPORTED, "reaction %d: unsupported rate form %d", r + 1, rt);
-    if (rt == AFG_RATE_TABULATED_FIELD && (rc.lt_col < 0 || rc.lt_col >= t.lt_n_cols))
+    if ((rt == AFG_RATE_TABULATED_FIELD || rt == AFG_RATE_K1) && (rc.lt_col < 0 || rc.lt_col >= t.lt_n_cols))
       return fail(ctx, AFG_ERR_ARG, "reaction %d: bad table column", r + 1);
     if (rc.n_in < 0 || rc.n_in > 4 || rc.n_out < 0 || rc.n_out > 4) return fail(ctx, AFG_ERR_ARG, "bad reaction size");
     for (int q = 0; q < rc.n_in; q++)

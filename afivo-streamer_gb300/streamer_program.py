@@ -117,6 +117,7 @@ class ProgramConfig:
         self.gas_fractions = g("gas%fractions", [0.8, 0.2], n=None)
         # m_field.f90
         self.field_amplitude = g("field_amplitude", None)
+        self.field_given_by = g("field_given_by", None, str, n=None)
         self.field_bc_type = g("field_bc_type", "homogeneous", str)
         # m_transport_data.f90, m_table_data.f90
         self.input_data_file = g("input_data%file", None, str)
@@ -191,7 +192,7 @@ class ProgramConfig:
         return vals
 
     # keys that only affect output files or are informational
-    _IGNORED = {"output%name", "memory_limit_GB", "output%regression_test", "output%dt"}
+    _IGNORED = {"output%name", "memory_limit_GB", "output%regression_test", "output%dt", "silo_write"}
     # keys whose given value must equal the supported one
     _FIXED = {
         "use_electrode": False, "use_dielectric": False,
@@ -208,8 +209,13 @@ class ProgramConfig:
             raise Unsupported("only linear table interpolation and spacing are supported")
         if any(self.periodic):
             raise Unsupported("periodic domains are not supported")
-        if self.field_bc_type != "homogeneous" or self.field_amplitude is None:
-            raise Unsupported("only field_amplitude with field_bc_type = homogeneous is supported")
+        if self.field_bc_type != "homogeneous":
+            raise Unsupported("only field_bc_type = homogeneous is supported")
+        if self.field_given_by is not None:
+            if len(self.field_given_by) != 2 or self.field_given_by[0] not in ("field", "voltage"):
+                raise Unsupported("field_given_by other than 'field <V/m>' or 'voltage <V>'")
+        elif self.field_amplitude is None:
+            raise ValueError("field_amplitude not specified")
         if self.species_boundary_condition != "neumann_zero" or self.prolong_density != "limit":
             raise Unsupported("species_boundary_condition / prolong_density other than the defaults")
         if self.time_integrator not in TIME_INTEGRATORS:
@@ -353,20 +359,43 @@ RATE_FORMS = {
     "c1*exp(-(Td/c2)**2)": (ag.RATE_EXP_V2, 2),
     "c1*exp(-(c2/(c3+Td))**c4)": (ag.RATE_K13, 4),
     "c1*exp(-(Td/c2)**c3)": (ag.RATE_K14, 3),
+    "c1*(300/Te)**c2": (ag.RATE_K1, 2),
+}
+
+# expressions of the gas temperature only (rate_analytic_k4..k10,
+# src/m_chemistry.f90:731-746): constants at the constant gas temperature,
+# evaluated on the host as c0 * value
+GAS_TEMPERATURE_FORMS = {
+    "c1*(Tg/300)**c2*exp(-c3/Tg)": (3, lambda c, T: c[0] * (T / 300) ** c[1] * math.exp(-c[2] / T)),
+    "c1*exp(-c2/Tg)": (2, lambda c, T: c[0] * math.exp(-c[1] / T)),
+    "c1*Tg**c2": (2, lambda c, T: c[0] * T ** c[1]),
+    "c1*(Tg/c2)**c3": (3, lambda c, T: c[0] * (T / c[1]) ** c[2]),
+    "c1*(300/Tg)**c2": (2, lambda c, T: c[0] * (300 / T) ** c[1]),
+    "c1*exp(-c2*Tg)": (2, lambda c, T: c[0] * math.exp(-c[1] * T)),
 }
 
 
 def read_reactions(path, gas_components, gas_densities, N):
     """read_reactions + parse_reaction (src/m_chemistry.f90:857-1278) for a
-    reaction file without groups or ignored species: the plasma species in
+    reaction file without groups: the plasma species in
     order of first appearance (simple-ascii names, charges) and per reaction
     its expression, data, input/output species (0-based plasma indices),
     output multiplicities and rate factor (gas densities of gas reactants, N
     for M, the cm unit conversion)."""
     with open(path) as f:
         lines = [ln.rstrip("\n") for ln in f]
-    if any(ln.strip() == "ignored_species" for ln in lines):
-        raise Unsupported("reaction files with ignored_species")
+    # read_ignored_species (src/m_chemistry.f90:807-854)
+    ignored = []
+    for q, ln in enumerate(lines):
+        if ln.strip() == "ignored_species":
+            for ln2 in lines[q + 2:]:
+                t = ln2.strip()
+                if t.startswith("#"):
+                    continue
+                if t.startswith("-----"):
+                    break
+                ignored.append(t.split()[0])
+            break
     n = 0
     while lines[n].strip() != "reaction_list":
         n += 1
@@ -388,7 +417,7 @@ def read_reactions(path, gas_components, gas_densities, N):
         entries.append(fields + ["m"] * (4 - len(fields)))
     names, reactions = [], []
     for text, how, data, unit in entries:
-        left, rfac, n_in_total = True, 1.0, 0
+        left, rfac, n_in_total, keep = True, 1.0, 0, True
         ix_in, ix_out, mult = [], [], []
         for comp in text.split():
             if comp == "+":
@@ -409,6 +438,13 @@ def read_reactions(path, gas_components, gas_densities, N):
                 if left:
                     rfac = rfac * N
                 continue
+            if comp in ignored:
+                # an ignored reactant drops the reaction, an ignored product
+                # is left out
+                if left:
+                    keep = False
+                    break
+                continue
             if comp not in names:
                 names.append(comp)
             ix = names.index(comp)
@@ -419,6 +455,8 @@ def read_reactions(path, gas_components, gas_densities, N):
             else:
                 ix_out.append(ix)
                 mult.append(m)
+        if not keep:
+            continue
         if not ix_in:
             raise ValueError(f"no input species: {text}")
         if unit == "cm":
@@ -470,13 +508,14 @@ def photoi_parameters(cfg: ProgramConfig):
 
 def new_style_columns(path, table_size, td_min, td_max_cfg):
     """td_tbl from new-style data (src/m_transport_data.f90:107-137): x in
-    Td, columns mobility*N, diffusion*N, alpha/N, eta/N as in the file."""
+    Td, columns mobility*N, diffusion*N, alpha/N, eta/N and the mean
+    electron energy (eV) as in the file."""
     xm, ym = table_from_file(path, "Mobility *N (1/m/V/s)")
     td_max = xm[-1] if td_max_cfg < 0 else td_max_cfg
     x, inv_fac = sm.table_x(td_min, td_max, table_size)
     cols = [spaced_data(xm, ym, x)]
     for name in ("Diffusion coefficient *N (1/m/s)", "Townsend ioniz. coef. alpha/N (m2)",
-                 "Townsend attach. coef. eta/N (m2)"):
+                 "Townsend attach. coef. eta/N (m2)", "Mean energy (eV)"):
         cols.append(spaced_data(*table_from_file(path, name), x))
     return x, inv_fac, cols
 
@@ -520,6 +559,12 @@ def model_from_config(cfg: ProgramConfig) -> sm.StreamerModel:
                 typ, nco = RATE_FORMS[r["how"]]
                 c = [_to_float(v) for v in r["data"].split()[:nco]]
                 d.update(type=typ, c=c)
+                if typ == ag.RATE_K1:
+                    d.update(col=4)       # td_energy_eV
+            elif r["how"] in GAS_TEMPERATURE_FORMS:
+                nco, fn = GAS_TEMPERATURE_FORMS[r["how"]]
+                c = [_to_float(v) for v in r["data"].split()[:nco]]
+                d.update(type=ag.RATE_CONSTANT, c=[fn(c, cfg.gas_temperature)])
             else:
                 raise Unsupported(f"rate expression {r['how']}")
             rlist.append(d)
@@ -745,7 +790,13 @@ class Program:
         if all(c == -1 for c in cgs):
             cgs = [cfg.box_size * int(round(v / L.min())) for v in L]
         self.cgs = np.asarray(cgs)
-        self.voltage = -cfg.domain_len[D - 1] * cfg.field_amplitude
+        # field_initialize (src/m_field.f90:119-172): field_given_by 'field E'
+        # or the deprecated field_amplitude give -domain_len * E
+        if cfg.field_given_by is not None:
+            kind, val = cfg.field_given_by[0], _to_float(cfg.field_given_by[1])
+            self.voltage = -cfg.domain_len[D - 1] * val if kind == "field" else val
+        else:
+            self.voltage = -cfg.domain_len[D - 1] * cfg.field_amplitude
         self.factory = engine_factory
         self.log = log
         self.rows = []

@@ -304,6 +304,9 @@ int afg_mg_residual(afg_ctx* ctx, int mg_id, int max_lvl);
 #define AFG_RATE_LINEAR          3  /* c0 * c1 * (Td - c2)                   */
 #define AFG_RATE_EXP_V1          4  /* c0 * c1 * exp(-(c2/(c3 + Td))**2)     */
 #define AFG_RATE_EXP_V2          5  /* c0 * c1 * exp(-(Td/c2)**2)            */
+#define AFG_RATE_K1              6  /* c0 * c1 * (300/Te)**c2 with Te = 2 eV /
+                                     * (3 kB) * LT(lt_col, Td), lt_col the mean
+                                     * electron energy in eV (rate_analytic_k1) */
 #define AFG_RATE_K13            18  /* c0 * c1 * exp(-(c2/(c3 + Td))**c4)    */
 #define AFG_RATE_K14            19  /* c0 * c1 * exp(-(Td/c2)**c3)           */
 

@@ -439,6 +439,11 @@ static double rate_of(const Transport& T, const afg_reaction& r, double td, int 
     case AFG_RATE_EXP_V2: { double q = td / c[1]; return c0 * c[0] * std::exp(-(q * q)); }
     case AFG_RATE_K13: return c0 * c[0] * std::exp(-std::pow(c[1] / (c[2] + td), c[3]));
     case AFG_RATE_K14: return c0 * c[0] * std::exp(-std::pow(td / c[1], c[2]));
+    case AFG_RATE_K1: {
+      /* rate_analytic_k1: Te = electron_eV_to_K * LT(td_energy_eV, Td) */
+      const double Te = (2 * ELEM / (3 * 1.380649e-23)) * lt_col(T, r.lt_col, ix, w);
+      return c0 * c[0] * std::pow(300 / Te, c[1]);
+    }
   }
   return 0;
 }

@@ -7,7 +7,10 @@ two-reaction chemistry, Cartesian with three-mode Helmholtz
 photoionization, and the air chemistry file with 8 species and 25 reactions
 axisymmetric and Cartesian with photoionization), the transport and
 reaction data they read, and the regression logs its test runner compares
-at rtol 1e-5 (programs/standard_2d/tests/, tools/compare_logs.py).
+at rtol 1e-5 (programs/standard_2d/tests/, tools/compare_logs.py); and the
+3D configurations of its `standard_3d` program: the standard chemistry,
+the small air chemistry (electron-temperature rates, ignored species) and
+the same with photoionization (programs/standard_3d/tests/).
 """
 import os
 import shutil
@@ -20,12 +23,20 @@ FILES = ["test_2d.cfg", "test_2d_rtest.log", "test_cyl.cfg", "test_cyl_rtest.log
          "test_2d_photoi_chem_rtest.log", "air_chemistry_v1.txt"]
 
 
+SRC_3D = "programs/standard_3d/tests"
+FILES_3D = ["test_3d.cfg", "test_3d_rtest.log", "td_air_siglo_swarm.txt", "test_3d_chem.cfg",
+            "test_3d_chem_rtest.log", "test_3d_photoi_chem.cfg", "test_3d_photoi_chem_rtest.log",
+            "air_chemistry_small_v1.txt"]
+
+
 def main(reference_root):
-    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "standard_2d")
-    os.makedirs(out, exist_ok=True)
-    for f in FILES:
-        shutil.copyfile(os.path.join(reference_root, SRC, f), os.path.join(out, f))
-        print("copied", f)
+    here = os.path.dirname(os.path.abspath(__file__))
+    for src, files, sub in ((SRC, FILES, "standard_2d"), (SRC_3D, FILES_3D, "standard_3d")):
+        out = os.path.join(here, sub)
+        os.makedirs(out, exist_ok=True)
+        for f in files:
+            shutil.copyfile(os.path.join(reference_root, src, f), os.path.join(out, f))
+            print("copied", sub, f)
 
 
 if __name__ == "__main__":

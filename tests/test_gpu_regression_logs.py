@@ -21,7 +21,8 @@ import afivo_gpu as ag
 import streamer_program as sp
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "standard_2d")
-CASES = ["test_2d", "test_cyl", "test_2d_photoi", "test_cyl_chem", "test_2d_photoi_chem"]
+CASES = ["test_2d", "test_cyl", "test_2d_photoi", "test_cyl_chem", "test_2d_photoi_chem", "test_3d",
+         "test_3d_chem", "test_3d_photoi_chem"]
 
 # FP64 GPU rows against the restatement's: the runs take the same steps,
 # rejections and meshes; single stages are bit-exact, but over a whole run
@@ -42,8 +43,16 @@ def rel_err(a, b):
     return np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
 
 
+def case_paths(name):
+    if name.startswith("test_3d"):
+        g = os.path.join(os.path.dirname(GOLD), "standard_3d")
+        return os.path.join(g, name + ".cfg"), os.path.join(g, name + "_rtest.log"), 3
+    return os.path.join(GOLD, name + ".cfg"), os.path.join(GOLD, name + "_rtest.log"), 2
+
+
 def run(name, factory):
-    cfg = sp.ProgramConfig(os.path.join(GOLD, name + ".cfg"))
+    cfg_path, _, ndim = case_paths(name)
+    cfg = sp.ProgramConfig(cfg_path, ndim=ndim)
     prog = sp.Program(cfg, factory)
     prog.set_initial_conditions()
     rows = np.array(prog.run())
@@ -58,7 +67,7 @@ def test_fp64_run_matches_restatement_and_log(gpu_lib, name):
     import oracle_program as op
     po, ro = run(name, op.OracleEngine)
     pg, rg = run(name, functools.partial(sp.GpuEngine, precision=ag.FP64))
-    head, ref = sp.read_regression_log(os.path.join(GOLD, name + "_rtest.log"))
+    head, ref = sp.read_regression_log(case_paths(name)[1])
     assert pg.n_steps == po.n_steps and pg.n_rejected == po.n_rejected
     assert rg.shape == ro.shape == ref.shape
     err = rel_err(rg[:, 1:], ro[:, 1:])
@@ -74,7 +83,7 @@ def test_fp64_run_matches_restatement_and_log(gpu_lib, name):
 @pytest.mark.parametrize("name", CASES)
 def test_mixed_run_matches_log(gpu_lib, name):
     pm, rm = run(name, functools.partial(sp.GpuEngine, precision=ag.MIXED))
-    head, ref = sp.read_regression_log(os.path.join(GOLD, name + "_rtest.log"))
+    head, ref = sp.read_regression_log(case_paths(name)[1])
     assert rm.shape == ref.shape
     assert np.allclose(rm[:, 1], ref[:, 1], rtol=1e-12, atol=0)
     e = rel_err(rm[:, 3:], ref[:, 3:])[ref[:, 3:] != 0]

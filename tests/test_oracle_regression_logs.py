@@ -15,7 +15,11 @@ photoionization (Bourdon-3 coefficients, every 5th step and after each mesh
 change).  test_cyl_chem and test_2d_photoi_chem read the reaction file
 air_chemistry_v1.txt (8 species, 25 reactions: tabulated, constant and
 field-dependent exponential rates, gas densities folded into the rate
-factors) with new-style transport tables.  Later rows agree to a few 1e-4
+factors) with new-style transport tables.  test_3d is the 3D octree
+configuration of the reference's standard_3d program (8^3 boxes, 3 ns);
+test_3d_chem and test_3d_photoi_chem add its small air chemistry (rates of
+the electron temperature from the tabulated mean energy, rates of the gas
+temperature as constants, an ignored species) and photoionization.  Later rows agree to a few 1e-4
 relative, with the
 largest difference about 1.3e-3 (the 4 ns row of test_2d, where the streamer
 accelerates): the reference's coarse-grid solve is hypre's PFMG at 1e-6
@@ -41,15 +45,29 @@ CASES = {
     "test_2d_photoi": (1e-4, 4, 1e-3),
     "test_cyl_chem": (3e-4, 6, 3e-4),
     "test_2d_photoi_chem": (3e-4, 4, 2e-3),
+    "test_3d": (2e-5, 11, 2e-4),
+    "test_3d_chem": (5e-5, 11, 3e-4),
+    "test_3d_photoi_chem": (5e-5, 11, 3e-4),
 }
 
 
+GOLD3 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "standard_3d")
+
+
+def case_paths(name):
+    """(configuration, log, dimension) of a reference regression test."""
+    if name.startswith("test_3d"):
+        return os.path.join(GOLD3, name + ".cfg"), os.path.join(GOLD3, name + "_rtest.log"), 3
+    return os.path.join(GOLD, name + ".cfg"), os.path.join(GOLD, name + "_rtest.log"), 2
+
+
 def run(name):
-    cfg = sp.ProgramConfig(os.path.join(GOLD, name + ".cfg"))
+    cfg_path, log_path, ndim = case_paths(name)
+    cfg = sp.ProgramConfig(cfg_path, ndim=ndim)
     prog = sp.Program(cfg, op.OracleEngine)
     prog.set_initial_conditions()
     rows = np.array(prog.run())
-    head, ref = sp.read_regression_log(os.path.join(GOLD, name + "_rtest.log"))
+    head, ref = sp.read_regression_log(log_path)
     return prog, rows, ref
 
 
@@ -72,7 +90,7 @@ def test_regression_log(name):
     for i in range(1, k + 1):
         assert np.allclose(cols[i], refc[i], rtol=early, atol=1e-8), (i, rel_err(cols[i], refc[i]).max())
     assert np.allclose(cols, refc, rtol=bound, atol=1e-8), rel_err(cols, refc).max()
-    assert prog.n_steps > 500
+    assert prog.n_steps > (80 if name.startswith("test_3d") else 500)
 
 
 def test_config_rejects_unsupported_keys(tmp_path):
