@@ -79,7 +79,7 @@ class MgDesc(C.Structure):
 
 AFG_MAX_SPECIES = 16
 AFG_MAX_REACTIONS = 32
-AFG_MAX_FLUX = 4
+AFG_MAX_FLUX = 8
 RATE_TABULATED_FIELD = 1
 RATE_CONSTANT = 2
 RATE_LINEAR = 3

@@ -49,25 +49,31 @@ class Unsupported(ValueError):
 
 
 def read_cfg(path):
-    """m_config's file format: `name = value(s)` lines, `[section]` lines that
-    prefix the following names with `section%`, `#` comments.  Returns
-    {name: [tokens]} with string tokens."""
+    """m_config's file format (src/config_fortran/m_config.f90:288-356):
+    `name = value(s)` lines, `#` comments, `[section]` lines; a variable line
+    belongs to the last section (its name gets `section%`) only when it
+    starts with a tab or at least two spaces, otherwise it is global.  A
+    later line overrides an earlier one.  Returns {name: [tokens]}."""
     out = {}
-    prefix = ""
+    section = ""
     with open(path) as f:
         for raw in f:
-            line = raw.split("#", 1)[0].strip()
+            body = raw.rstrip("\n").split("#", 1)[0]
+            line = body.strip()
             if not line:
                 continue
-            if line.startswith("[") and line.endswith("]"):
-                prefix = line[1:-1].strip() + "%"
-                continue
             if "=" not in line:
+                if line.startswith("[") and "]" in line:
+                    section = line[1:line.index("]")].strip()
+                    continue
                 raise ValueError(f"{path}: cannot parse line: {raw.strip()}")
-            name, val = line.split("=", 1)
+            if "+=" in line:
+                raise Unsupported("'+=' lines in configuration files")
+            name, val = body.split("=", 1)
+            indented = name.startswith("\t") or name.startswith("  ")
             name = name.strip()
-            if "%" not in name:
-                name = prefix + name
+            if section and indented:
+                name = section + "%" + name
             out[name] = shlex.split(val.replace(",", " "))
     return out
 
@@ -122,6 +128,8 @@ class ProgramConfig:
         # m_transport_data.f90, m_table_data.f90
         self.input_data_file = g("input_data%file", None, str)
         self.input_data_old_style = g("input_data%old_style", False, bool)
+        self.mobile_ions = g("input_data%mobile_ions", [], str, n=None)
+        self.ion_mobilities = g("input_data%ion_mobilities", [], n=None)
         self.table_size = g("table_data%size", 1000, int)
         self.table_min_townsend = g("table_data%min_townsend", 0.0)
         self.table_max_townsend = g("table_data%max_townsend", -1.0)
@@ -209,6 +217,10 @@ class ProgramConfig:
             raise Unsupported("only linear table interpolation and spacing are supported")
         if any(self.periodic):
             raise Unsupported("periodic domains are not supported")
+        if len(self.mobile_ions) != len(self.ion_mobilities) or any(m < 0 for m in self.ion_mobilities):
+            raise ValueError("input_data%mobile_ions and %ion_mobilities must pair up (positive mobilities)")
+        if len(self.mobile_ions) + 1 > ag.AFG_MAX_FLUX:
+            raise Unsupported("too many mobile ions for the device tables")
         if self.field_bc_type != "homogeneous":
             raise Unsupported("only field_bc_type = homogeneous is supported")
         if self.field_given_by is not None:
@@ -574,6 +586,14 @@ def model_from_config(cfg: ProgramConfig) -> sm.StreamerModel:
         if cfg.photoi_enabled and cfg.photoi_species not in names:
             raise Unsupported(f"photoi%species {cfg.photoi_species} is not a species of the chemistry")
         photoi_ix = names.index(cfg.photoi_species) if cfg.photoi_enabled else 1
+    if cfg.mobile_ions:
+        # transport_data_ions (src/m_transport_data.f90:186-208): mobilities at
+        # 1 bar and 300 K, scaled there by the gas density of those conditions
+        names = [sp_.name for sp_ in kw.get("species", [])] or ["e", "M_plus", "M_min"]
+        missing = [n for n in cfg.mobile_ions if n not in names]
+        if missing:
+            raise ValueError(f"mobile ions not in the chemistry: {missing}")
+        kw["mobile_ions"] = [(names.index(n), mob) for n, mob in zip(cfg.mobile_ions, cfg.ion_mobilities)]
     m = sm.StreamerModel(ndim=cfg.ndim, n_states=sm.states_needed(integ), N=N,
                          tabulated=dict(x=x, inv_fac=inv_fac, cols=cols),
                          photoi_modes=0 if photoi is None else len(photoi[0]),

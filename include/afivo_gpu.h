@@ -294,7 +294,7 @@ int afg_mg_residual(afg_ctx* ctx, int mg_id, int max_lvl);
 
 #define AFG_MAX_SPECIES   16
 #define AFG_MAX_REACTIONS 32
-#define AFG_MAX_FLUX       4
+#define AFG_MAX_FLUX       8
 
 /* Reaction-rate forms, values of rate_* in src/m_chemistry.f90:65-126.  Forms
  * that depend only on the (constant) gas temperature are evaluated on the
