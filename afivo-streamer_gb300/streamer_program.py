@@ -1056,3 +1056,56 @@ class GpuEngine:
 
     def close(self):
         self.ctx.close()
+
+
+def fortran_e(x, digits=8, exp_digits=3, width=20):
+    """One field of the Fortran edit descriptor E20.8e3 (`0.dddddddd E+eee`,
+    right-justified), as output_regression_log writes it."""
+    if x == 0:
+        mant, e = "0." + "0" * digits, 0
+    else:
+        s = f"{abs(x):.{digits - 1}e}"          # d.ddddddde+XX
+        m, ex = s.split("e")
+        mant, e = "0." + m.replace(".", ""), int(ex) + 1
+    sign = "-" if x < 0 else ""
+    es = "+" if e >= 0 else "-"
+    return f"{sign}{mant}E{es}{abs(e):0{exp_digits}d}".rjust(width)
+
+
+def write_regression_log(path, species_names, rows):
+    """The log file of output_regression_log (src/m_output.f90:787-842):
+    a header line, then per output `I0` and 3 + 3 * n_species E20.8e3."""
+    with open(path, "w") as f:
+        f.write("it time dt" + "".join(f" sum({n})" for n in species_names)
+                + "".join(f" sum({n}^2)" for n in species_names)
+                + "".join(f" max({n})" for n in species_names) + "\n")
+        for r in rows:
+            f.write(f"{int(r[0])}" + "".join(fortran_e(float(v)) for v in r[1:]) + "\n")
+
+
+def main(argv=None):
+    """Run a reference configuration file on the GPU and write its regression
+    log, e.g. `python streamer_program.py test_2d.cfg --ndim 2 --log out.log`
+    (the reference's tools/compare_logs.py compares such logs)."""
+    import argparse
+    import functools
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("cfg")
+    ap.add_argument("--ndim", type=int, default=2, choices=[2, 3])
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--log", default=None, help="regression log to write (default: <cfg>_rtest.out.log)")
+    ap.add_argument("--end-time", type=float, default=None)
+    a = ap.parse_args(argv)
+    cfg = ProgramConfig(a.cfg, ndim=a.ndim)
+    prec = ag.FP64 if a.precision == "fp64" else ag.MIXED
+    prog = Program(cfg, functools.partial(GpuEngine, precision=prec), log=print)
+    prog.set_initial_conditions()
+    rows = prog.run(end_time=a.end_time)
+    out = a.log or os.path.splitext(a.cfg)[0] + "_rtest.out.log"
+    write_regression_log(out, [s.name for s in prog.model.species], rows)
+    prog.engine.close()
+    print(f"{prog.n_steps} steps ({prog.n_rejected} rejected); log written to {out}")
+
+
+if __name__ == "__main__":
+    main()

@@ -138,6 +138,21 @@ def test_cfg_sections_follow_indentation(tmp_path):
     assert raw["input_data%file"] == ["a.txt"]
 
 
+def test_log_writer_reproduces_reference_logs(tmp_path):
+    """write_regression_log writes the reference's format (I0 and E20.8e3
+    fields): every stored log read and written back is identical."""
+    import glob
+    logs = sorted(glob.glob(os.path.join(GOLD, "*_rtest.log")) + glob.glob(os.path.join(GOLD3, "*_rtest.log")))
+    assert len(logs) == 10
+    for path in logs:
+        head, rows = sp.read_regression_log(path)
+        n = (len(head) - 3) // 3
+        names = [h[4:-1] for h in head[3:3 + n]]
+        out = tmp_path / "x.log"
+        sp.write_regression_log(str(out), names, rows)
+        assert out.read_text() == open(path).read(), path
+
+
 def test_table_from_file_and_interpolation():
     x, y = sp.table_from_file(os.path.join(GOLD, "td_air_siglo_swarm.txt"), "efield[V/m]_vs_mu[m2/Vs]")
     assert x[0] == 5.0e4 and y[0] == 1.9e-1 and np.all(np.diff(x) > 0)
