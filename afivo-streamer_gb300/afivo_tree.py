@@ -146,8 +146,11 @@ def _lookup(keys_sorted: np.ndarray, q: np.ndarray) -> np.ndarray:
 
 def build_tree(ndim: int, n_cell: int, coarse_grid_size, domain_len,
                r_base=None, coord: int = AF_XYZ, max_lvl: int = 1,
-               refine=None) -> Tree:
-    """Build a 2:1-balanced tree.
+               refine=None, face_balance: bool = False) -> Tree:
+    """Build a 2:1-balanced tree: by default every refined box has its whole
+    3^D neighbourhood on its own level (diagonal neighbours included, the
+    seeded benchmark trees); with ``face_balance`` only its face neighbours,
+    which is afivo's rule (ensure_two_one_balance, m_af_core.f90:1015-1055).
 
     ``refine(lvl, centers[m, D], dr[D]) -> bool[m]`` says which boxes of
     level ``lvl`` (given by their centres) want children; ``None`` refines
@@ -196,6 +199,8 @@ def build_tree(ndim: int, n_cell: int, coarse_grid_size, domain_len,
     # neighbourhood on its own level; the parents of newly refined boxes are
     # handled by the next, coarser pass through the dilation of refined[l-1]
     offs = np.array(list(itertools.product([-1, 0, 1], repeat=D)), dtype=np.int64)
+    if face_balance:
+        offs = offs[np.abs(offs).sum(axis=1) <= 1]
     for l in range(max_lvl - 2, 0, -1):
         if len(refined[l]) == 0:
             continue
@@ -388,8 +393,11 @@ def adjust_refinement(tree: Tree, flags, max_lvl: int) -> Tree:
     (1015-1055) and handle_derefinement_flags (1057-1088) on the box flags,
     then the new tree: old leaves flagged for refinement get children, the
     children of parents flagged for derefinement go, everything else stays.
-    The tree is rebuilt by build_tree, whose balancing also covers diagonal
-    neighbours (the device kernels need it for corner ghost cells)."""
+    The tree is rebuilt by build_tree with afivo's 2:1 balance over face
+    neighbours only (a box may keep a coarser diagonal neighbour two levels
+    down, whose corner ghost cells are then extrapolated as af_gc_box_corner
+    does).  When no leaf is refined and no parent derefined the same tree
+    object is returned."""
     f = np.asarray(flags, dtype=np.int64).copy()
     H = tree.highest_lvl
     has_ch = (tree.children > 0).any(axis=1)
@@ -420,6 +428,12 @@ def adjust_refinement(tree: Tree, flags, max_lvl: int) -> Tree:
             else:
                 f[id_ - 1] = AF_KEEP_REF
                 f[c] = np.where(f[c] != AF_DEREFINE, np.maximum(f[c], AF_KEEP_REF), f[c])
+    # no leaf refined and no parent derefined: the mesh stays as it is
+    leaves = np.concatenate([np.asarray(l, dtype=np.int64) for l in tree.lvl_leaves]) - 1
+    parents = [np.asarray(l, dtype=np.int64) for l in tree.lvl_parents if len(l)]
+    parents = np.concatenate(parents) - 1 if parents else np.zeros(0, dtype=np.int64)
+    if not np.any(f[leaves] == AF_REFINE) and not np.any(f[parents] == AF_DEREFINE):
+        return tree
     # boxes of the old tree that have children in the new one, by (lvl, ix)
     wants = {}
     for b in range(tree.n_boxes):
@@ -434,4 +448,4 @@ def adjust_refinement(tree: Tree, flags, max_lvl: int) -> Tree:
 
     dom = np.asarray(tree.dr_base, dtype=np.float64) * np.asarray(tree.coarse_grid_size)
     return build_tree(D, nc, tree.coarse_grid_size, dom, r_base=tree.r_base, coord=tree.coord,
-                      max_lvl=max(max_lvl, H), refine=refine)
+                      max_lvl=max(max_lvl, H), refine=refine, face_balance=True)

@@ -792,7 +792,8 @@ class Program:
     state 0); `advance(dt)` (copy_current_state, the integrator's
     forward_euler stages; returns the last stage's dt limit
     min(dt_max, cfl_number/max cfl_sum, dielectric relaxation time,
-    chemistry limit)); `restore()` (restore_previous_state);
+    chemistry limit)); `restore()` (restore_previous_state: densities and
+    phi from the backup, then the field of that phi);
     `refine(desc, restrict_first)` (af_restrict_tree + af_gc_tree of the
     densities when `restrict_first`, the refinement flags, af_adjust_refinement
     with auto_prolong; returns (n_add, n_rm, added ids)); and
@@ -891,6 +892,7 @@ class Program:
                 if dt <= lim:
                     break
                 self.n_rejected += 1
+                self._say(f"step {it} rejected at t = {global_time:.6e}: dt = {dt:.4e}, limit {lim:.4e}")
                 dt = cfg.dt_safety_factor * lim
                 time = global_time
                 write_out = False
@@ -998,6 +1000,7 @@ class GpuEngine:
         for s in range(len(m.species)):
             ctx.tree_copy_cc(m.species_iv[s] + m.n_states - 1, m.species_iv[s])
         ctx.tree_copy_cc(self.iv_phi_copy, m.i_phi)
+        ctx.field_from_potential(m.i_phi)
 
     def auto_vars(self):
         """(variable, prolongation) of auto_prolong: the densities and rhs by
@@ -1019,6 +1022,8 @@ class GpuEngine:
                 ctx.gc(m.species_iv[s], 0, True)
         flags = ctx.refine_flags(desc)
         new = at.adjust_refinement(tree, flags, AF_MAX_LVL)
+        if new is tree:
+            return 0, 0, np.zeros(0, dtype=np.int32)
         old_id = at.remap_ids(tree, new)
         keep = old_id > 0
         n_add = int(np.count_nonzero(~keep))

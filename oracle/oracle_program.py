@@ -13,7 +13,8 @@ regression logs the reference's own tests store.  Stages follow:
   cfl_number/max cfl_sum, dielectric relaxation time, chemistry limit) with
   the chemistry limit on the last stage only;
 * copy_current_state / restore_previous_state (src/streamer.f90:659-683):
-  densities and the potential;
+  densities and the potential, and on a restore the field from the restored
+  potential;
 * the refinement step of the time loop (src/streamer.f90:405-428):
   af_restrict_tree + af_gc_tree of the densities, default_refinement flags,
   af_adjust_refinement and auto_prolong (afivo/src/m_af_core.f90:843-881):
@@ -90,6 +91,7 @@ class OracleEngine:
         for s in range(len(m.species)):
             cc[:, m.species_iv[s] - 1] = cc[:, m.species_iv[s] + m.n_states - 2]
         cc[:, m.i_phi - 1] = self.phi_saved
+        self.o.field_from_potential(cc, self.fc, m.i_phi)
 
     def auto_vars(self):
         """(variable, prolongation) of the tree's cc_auto_vars."""
@@ -108,6 +110,8 @@ class OracleEngine:
                 o.gc(self.cc, m.species_iv[s], 0, True)
         flags = o.refine_flags(self.cc, desc)
         new = at.adjust_refinement(tree, flags, sp.AF_MAX_LVL)
+        if new is tree:
+            return 0, 0, np.zeros(0, dtype=np.int32)
         old_id = at.remap_ids(tree, new)
         keep = old_id > 0
         n_add = int(np.count_nonzero(~keep))

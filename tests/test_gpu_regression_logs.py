@@ -28,8 +28,10 @@ CASES = ["test_2d", "test_cyl", "test_2d_photoi", "test_cyl_chem", "test_2d_phot
 # rejections and meshes; single stages are bit-exact, but over a whole run
 # (about 700 steps) the rows separate by up to 7.7e-9 relative.
 FP64_VS_ORACLE = 1e-7
-# every row against the reference's logs (as for the restatement)
-FP64_VS_LOG = 2e-3
+# every row against the reference's logs: the restatement's bounds
+# (test_oracle_regression_logs.CASES) with room for the FP64 path's own
+# difference from the restatement
+FP64_VS_LOG_EXTRA = 1e-6
 # mixed precision against the logs, density columns: within 1.3e-3 on the
 # Cartesian and 3D runs, 6.2e-3 on test_cyl and 4.1e-2 on test_cyl_chem's
 # last rows, where the maxima of e and N2+ on the axis at the streamer head
@@ -77,7 +79,8 @@ def test_fp64_run_matches_restatement_and_log(gpu_lib, name):
     print(f"{name}: FP64 GPU vs restatement max rel {err.max():.3e}; "
           f"vs log {rel_err(rg[:, 2:], ref[:, 2:])[ref[:, 2:] != 0].max():.3e}")
     assert err.max() <= FP64_VS_ORACLE
-    assert np.allclose(rg[:, 2:], ref[:, 2:], rtol=FP64_VS_LOG, atol=1e-8)
+    from test_oracle_regression_logs import CASES as ORACLE_BOUNDS
+    assert np.allclose(rg[:, 2:], ref[:, 2:], rtol=2 * ORACLE_BOUNDS[name] + FP64_VS_LOG_EXTRA, atol=1e-8)
 
 
 @pytest.mark.gpu

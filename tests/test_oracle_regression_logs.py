@@ -10,26 +10,26 @@ reference's time-step control, refinement every second step, and the field
 solves with multigrid_num_vcycles = 2 at 1e-4 relative residual.
 
 The first row (initial conditions and initial refinement) agrees to the
-logs' 8 printed digits.  test_2d_photoi adds the three-mode Helmholtz
-photoionization (Bourdon-3 coefficients, every 5th step and after each mesh
-change).  test_cyl_chem and test_2d_photoi_chem read the reaction file
-air_chemistry_v1.txt (8 species, 25 reactions: tabulated, constant and
-field-dependent exponential rates, gas densities folded into the rate
-factors) with new-style transport tables.  test_3d is the 3D octree
+logs' 8 printed digits in every configuration.  test_2d_photoi adds the
+three-mode Helmholtz photoionization (Bourdon-3 coefficients, every 5th step
+and after each mesh change).  test_cyl_chem and test_2d_photoi_chem read the
+reaction file air_chemistry_v1.txt (8 species, 25 reactions: tabulated,
+constant and field-dependent exponential rates, gas densities folded into
+the rate factors) with new-style transport tables.
+test_cyl_ion_motion(_v2) move six ion species.  test_3d is the 3D octree
 configuration of the reference's standard_3d program (8^3 boxes, 3 ns);
-test_cyl_ion_motion(_v2) move six ion species (upwind ion fluxes, their
-conductivity in the dielectric relaxation limit); the v2 run (a weak seed,
-no streamer) agrees with its log to the printed 8 digits in every row;
 test_3d_chem and test_3d_photoi_chem add its small air chemistry (rates of
 the electron temperature from the tabulated mean energy, rates of the gas
-temperature as constants, an ignored species) and photoionization.  Later rows agree to a few 1e-4
-relative, with the
-largest difference about 1.3e-3 (the 4 ns row of test_2d, where the streamer
-accelerates): the reference's coarse-grid solve is hypre's PFMG at 1e-6
-relative tolerance, this path's an exact direct solve, and each field solve
-stops after at most two V-cycles, so the potentials differ at the level of
-that tolerance every step; the mesh decisions that follow from it are
-discrete.  The bounds below are those observed, rounded up.
+temperature as constants, an ignored species) and photoionization.
+
+Every row of test_2d, test_cyl, test_cyl_chem and the two ion-motion runs
+passes the reference's own comparison (rtol 1e-5); test_cyl and
+test_cyl_ion_motion_v2 agree to the printed 8 digits throughout.  The other
+five stay within 4e-5.  What remains is expected at that level: the
+reference solves the coarse grid with hypre's PFMG to 1e-6 relative
+tolerance, this path solves it exactly, and each field solve stops after at
+most two V-cycles at 1e-4 relative residual.  The bounds below are those
+observed, rounded up.
 """
 import os
 
@@ -41,18 +41,19 @@ import streamer_program as sp
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "standard_2d")
 
-# (configuration, rows 1..k bound, k, bound for every row)
+# bound on every row (relative, atol 1e-8 as tools/compare_logs.py); the
+# configurations at 1e-5 pass the reference's own comparison (rtol 1e-5)
 CASES = {
-    "test_2d": (1e-4, 3, 2e-3),
-    "test_cyl": (5e-4, 1, 2e-3),
-    "test_2d_photoi": (1e-4, 4, 1e-3),
-    "test_cyl_chem": (3e-4, 6, 3e-4),
-    "test_2d_photoi_chem": (3e-4, 4, 2e-3),
-    "test_cyl_ion_motion": (6e-4, 9, 2e-3),
-    "test_cyl_ion_motion_v2": (1e-7, 10, 1e-7),
-    "test_3d": (2e-5, 11, 2e-4),
-    "test_3d_chem": (5e-5, 11, 3e-4),
-    "test_3d_photoi_chem": (5e-5, 11, 3e-4),
+    "test_2d": 1e-5,
+    "test_cyl": 1e-5,
+    "test_2d_photoi": 5e-5,
+    "test_cyl_chem": 1e-5,
+    "test_2d_photoi_chem": 1e-4,
+    "test_cyl_ion_motion": 1e-5,
+    "test_cyl_ion_motion_v2": 1e-7,
+    "test_3d": 3e-5,
+    "test_3d_chem": 1e-4,
+    "test_3d_photoi_chem": 1e-4,
 }
 
 
@@ -82,7 +83,7 @@ def rel_err(a, b):
 
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_regression_log(name):
-    early, k, bound = CASES[name]
+    bound = CASES[name]
     prog, rows, ref = run(name)
     assert rows.shape == ref.shape, (rows.shape, ref.shape)
     assert np.array_equal(rows[:, 0], ref[:, 0])
@@ -90,11 +91,7 @@ def test_regression_log(name):
     assert np.allclose(rows[:, 1], ref[:, 1], rtol=1e-12, atol=0)
     # initial conditions and refinement: the log's printed precision
     assert np.allclose(rows[0, 2:], ref[0, 2:], rtol=1e-7, atol=1e-8)
-    cols = rows[:, 2:]
-    refc = ref[:, 2:]
-    for i in range(1, k + 1):
-        assert np.allclose(cols[i], refc[i], rtol=early, atol=1e-8), (i, rel_err(cols[i], refc[i]).max())
-    assert np.allclose(cols, refc, rtol=bound, atol=1e-8), rel_err(cols, refc).max()
+    assert np.allclose(rows[:, 2:], ref[:, 2:], rtol=bound, atol=1e-8), rel_err(rows[:, 2:], ref[:, 2:]).max()
     assert prog.n_steps > (80 if name.startswith("test_3d") else 250)
 
 
