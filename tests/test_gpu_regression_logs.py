@@ -25,17 +25,19 @@ CASES = ["test_2d", "test_cyl", "test_2d_photoi", "test_cyl_chem", "test_2d_phot
          "test_cyl_ion_motion", "test_cyl_ion_motion_v2", "test_3d", "test_3d_chem", "test_3d_photoi_chem"]
 
 # FP64 GPU rows against the restatement's: the runs take the same steps,
-# rejections and meshes; single stages are bit-exact, but over a whole run
-# (about 700 steps) the rows separate by up to 7.7e-9 relative.
+# rejections and meshes; single stages are bit-exact, but over the 2D whole
+# runs (300 to 2000 steps) the rows separate by up to 6e-8 relative (the 3D
+# runs by at most 5e-14).
 FP64_VS_ORACLE = 1e-7
 # every row against the reference's logs: the restatement's bounds
 # (test_oracle_regression_logs.CASES) with room for the FP64 path's own
 # difference from the restatement
 FP64_VS_LOG_EXTRA = 1e-6
-# mixed precision against the logs, density columns: within 1.3e-3 on the
-# Cartesian and 3D runs, 6.2e-3 on test_cyl and 4.1e-2 on test_cyl_chem's
-# last rows, where the maxima of e and N2+ on the axis at the streamer head
-# are the most sensitive values (its rows up to 1 ns stay within 7.2e-4).
+# mixed precision against the logs, density columns: within 1.0e-3 on the
+# Cartesian and 3D runs (7.3e-6 on test_2d), 4.2e-3 on the ion-motion runs,
+# 6.4e-3 on test_cyl and 4.3e-2 on test_cyl_chem's last rows, where the
+# maxima of e and N2+ on the axis at the streamer head are the most
+# sensitive values (its rows up to 1 ns stay within 7.2e-4).
 # The dt column is the step chosen for the next step and is compared for the
 # FP64 path only: after a rejected step the mixed run may pick a different
 # step size (test_cyl_chem's 1.25 ns row).
