@@ -273,6 +273,10 @@ def load_library(path: str = LIB_PATH):
         "afg_prolong_limit": (C.c_int, [P, C.c_int, C.c_int, _IP, C.c_int]),
         "afg_prolong_linear": (C.c_int, [P, C.c_int, C.c_int, _IP]),
         "afg_restrict_tree": (C.c_int, [P, C.c_int]),
+        "afg_adjust_refinement": (C.c_int, [C.POINTER(TreeDesc), _IP, C.c_int, C.POINTER(P)]),
+        "afg_tree_new_sizes": (C.c_int, [P, _IP, _IP]),
+        "afg_tree_new_get": (C.c_int, [P, _IP, _IP, _IP, _IP, _IP, _IP, _DP, _DP, _DP]),
+        "afg_tree_new_free": (None, [P]),
         "afg_tree_remap": (C.c_int, [P, C.POINTER(TreeDesc), _IP]),
         "afg_host_unregister": (C.c_int, [P, C.c_void_p]),
         "afg_sync": (C.c_int, [P]),
@@ -306,6 +310,47 @@ class BoxPointers:
 
 def box_pointers(cc: np.ndarray):
     return BoxPointers(cc)
+
+
+def adjust_refinement(tree, flags, max_lvl: int):
+    """The mesh after af_adjust_refinement, computed by the library's host
+    code (afg_adjust_refinement): from box flags (REF_RM / REF_KEEP / REF_DO
+    per box, as afg_refine_flags returns them) to the new afivo_tree.Tree, or
+    `tree` itself when the mesh does not change.  Needs no GPU."""
+    import afivo_tree as at
+    lib = load_library()
+    holder = TreeDescHolder(tree)
+    f = np.ascontiguousarray(flags, dtype=np.int32)
+    out = C.c_void_p()
+    rc = lib.afg_adjust_refinement(C.byref(holder.desc), _ip(f), int(max_lvl), C.byref(out))
+    if rc != AFG_OK:
+        raise AfgError(rc, "afg_adjust_refinement failed")
+    if not out.value:
+        return tree
+    try:
+        n, h = C.c_int(0), C.c_int(0)
+        lib.afg_tree_new_sizes(out, C.byref(n), C.byref(h))
+        D, N = tree.ndim, n.value
+        arr = dict(lvl=np.zeros(N, np.int32), ix=np.zeros((N, D), np.int32), parent=np.zeros(N, np.int32),
+                   children=np.zeros((N, 2 ** D), np.int32), neighbors=np.zeros((N, 2 * D), np.int32),
+                   neighbor_mat=np.zeros((N, 3 ** D), np.int32), r_min=np.zeros((N, D)), dr=np.zeros((N, D)))
+        drb = np.zeros(D)
+        lib.afg_tree_new_get(out, _ip(arr["lvl"]), _ip(arr["ix"]), _ip(arr["parent"]), _ip(arr["children"]),
+                             _ip(arr["neighbors"]), _ip(arr["neighbor_mat"]), _dp(arr["r_min"]), _dp(arr["dr"]),
+                             _dp(drb))
+    finally:
+        lib.afg_tree_new_free(out)
+    t = at.Tree(ndim=D, n_cell=tree.n_cell, coord=tree.coord, coarse_grid_size=tree.coarse_grid_size,
+                r_base=tree.r_base, dr_base=drb)
+    t.n_boxes, t.highest_lvl = N, h.value
+    for k, v in arr.items():
+        setattr(t, k, v)
+    ids = np.arange(1, N + 1, dtype=np.int32)
+    has_c = (t.children > 0).any(axis=1)
+    t.lvl_ids = [ids[t.lvl == l] for l in range(1, t.highest_lvl + 1)]
+    t.lvl_leaves = [x[~has_c[x - 1]] for x in t.lvl_ids]
+    t.lvl_parents = [x[has_c[x - 1]] for x in t.lvl_ids]
+    return t
 
 
 class Context:

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libafivo_gpu.so")
 OBJ_DIR = os.path.join(HERE, "build")
-UNITS = ["afg_runtime.cu", "afg_noalloc.cu"]
+UNITS = ["afg_runtime.cu", "afg_noalloc.cu", "afg_tree_host.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3",
               "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off",
@@ -46,7 +46,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_unit(u):
         src = os.path.join(CSRC, u)
-        obj = os.path.join(OBJ_DIR, u.replace(".cu", ".o"))
+        obj = os.path.join(OBJ_DIR, os.path.splitext(u)[0] + ".o")
         cmd = [nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd))

@@ -333,14 +333,14 @@ class StreamerRun:
     def refine(self, desc, max_lvl, limiter=ag.LIMITER_MC):
         """One refinement of the mesh with the data on the device
         (src/streamer.f90:397-428): box flags from afg_refine_flags, the new
-        tree from the host's af_adjust_refinement (afivo_tree), the data moved
+        tree from the host's af_adjust_refinement (afg_adjust_refinement), the data moved
         by afg_tree_remap, the new boxes' densities and potential filled by
         afg_prolong_limit level by level (after a ghost fill of the parents'
         level), the operators set up again and the field of the new mesh.
         Returns the box flags and the old id of every new box."""
         ctx, m = self.ctx, self.m
         flags = ctx.refine_flags(desc)
-        new = at.adjust_refinement(self.tree, flags, max_lvl)
+        new = ag.adjust_refinement(self.tree, flags, max_lvl)
         old_id = at.remap_ids(self.tree, new)
         ctx.tree_remap(new, old_id)
         self.tree = new

@@ -1021,7 +1021,7 @@ class GpuEngine:
                 ctx.restrict_tree(m.species_iv[s])
                 ctx.gc(m.species_iv[s], 0, True)
         flags = ctx.refine_flags(desc)
-        new = at.adjust_refinement(tree, flags, AF_MAX_LVL)
+        new = ag.adjust_refinement(tree, flags, AF_MAX_LVL)
         if new is tree:
             return 0, 0, np.zeros(0, dtype=np.int32)
         old_id = at.remap_ids(tree, new)

@@ -527,6 +527,27 @@ int afg_restrict_tree(afg_ctx* ctx, int iv);
  * batched trees. */
 int afg_tree_remap(afg_ctx* ctx, const afg_tree_desc* tree, const int* old_id);
 
+/* Host-side mesh adjustment for a caller that does not keep afivo's own tree
+ * code (a Fortran caller keeps af_adjust_refinement and needs none of this):
+ * af_adjust_refinement (afivo/src/m_af_core.f90:697-1091) after the flag
+ * pass, i.e. from the box flags of afg_refine_flags: max-level clamp,
+ * ensure_two_one_balance, handle_derefinement_flags, then the new tree with
+ * afivo's 2:1 balance over face neighbours, numbered level by level (level 1
+ * in coordinate order, then children of refined parents in parent-id and
+ * child order).  No CUDA call; needs no context.  *out is NULL when the mesh
+ * does not change; otherwise query it with afg_tree_new_sizes, copy it out
+ * with afg_tree_new_get (arrays laid out as in afg_tree_desc; any pointer may
+ * be NULL to skip; dr_base receives ndim values) and release it with
+ * afg_tree_new_free. */
+typedef struct afg_tree_new afg_tree_new;
+int afg_adjust_refinement(const afg_tree_desc* tree, const int* box_flags, int max_lvl,
+                          afg_tree_new** out);
+int afg_tree_new_sizes(const afg_tree_new* t, int* n_boxes, int* highest_lvl);
+int afg_tree_new_get(const afg_tree_new* t, int* lvl, int* ix, int* parent, int* children,
+                     int* neighbors, int* neighbor_mat, double* r_min, double* dr,
+                     double* dr_base);
+void afg_tree_new_free(afg_tree_new* t);
+
 /* ---- accounting and timing (no counterpart in the reference, which keeps
  * wall-clock accumulators wc_time_* in src/m_streamer.f90:184-190) -------- */
 
