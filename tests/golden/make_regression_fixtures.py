@@ -1,12 +1,12 @@
 """Copy the reference's regression-test inputs and stored logs used as
 golden fixtures (run in a checkout that has the reference next to it).
 
-The files are the reference's own data: seven configurations of its
+The files are the reference's own data: eight configurations of its
 `standard_2d` program (Cartesian and axisymmetric with the standard
 two-reaction chemistry, Cartesian with three-mode Helmholtz
 photoionization, and the air chemistry file with 8 species and 25 reactions
-axisymmetric and Cartesian with photoionization, and twice axisymmetric
-with six mobile ion species), the transport and
+axisymmetric and Cartesian with photoionization and axisymmetric with
+both, and twice axisymmetric with six mobile ion species), the transport and
 reaction data they read, and the regression logs its test runner compares
 at rtol 1e-5 (programs/standard_2d/tests/, tools/compare_logs.py); and the
 3D configurations of its `standard_3d` program: the standard chemistry,
@@ -22,7 +22,8 @@ FILES = ["test_2d.cfg", "test_2d_rtest.log", "test_cyl.cfg", "test_cyl_rtest.log
          "test_2d_photoi.cfg", "test_2d_photoi_rtest.log", "td_air_siglo_swarm.txt",
          "test_cyl_chem.cfg", "test_cyl_chem_rtest.log", "test_2d_photoi_chem.cfg",
          "test_2d_photoi_chem_rtest.log", "air_chemistry_v1.txt", "test_cyl_ion_motion.cfg",
-         "test_cyl_ion_motion_rtest.log", "test_cyl_ion_motion_v2.cfg", "test_cyl_ion_motion_v2_rtest.log"]
+         "test_cyl_ion_motion_rtest.log", "test_cyl_ion_motion_v2.cfg", "test_cyl_ion_motion_v2_rtest.log",
+         "test_cyl_photoi_chem.cfg", "test_cyl_photoi_chem_rtest.log"]
 
 
 SRC_3D = "programs/standard_3d/tests"

@@ -22,10 +22,10 @@ test_3d_chem and test_3d_photoi_chem add its small air chemistry (rates of
 the electron temperature from the tabulated mean energy, rates of the gas
 temperature as constants, an ignored species) and photoionization.
 
-Every row of test_2d, test_cyl, test_cyl_chem and the two ion-motion runs
-passes the reference's own comparison (rtol 1e-5); test_cyl and
-test_cyl_ion_motion_v2 agree to the printed 8 digits throughout.  The other
-five stay within 4e-5.  What remains is expected at that level: the
+Every row of test_2d, test_cyl, test_cyl_chem, test_cyl_photoi_chem and
+the two ion-motion runs passes the reference's own comparison (rtol 1e-5);
+test_cyl and test_cyl_ion_motion_v2 agree to the printed 8 digits
+throughout.  The other five stay within 4e-5.  What remains is expected at that level: the
 reference solves the coarse grid with hypre's PFMG to 1e-6 relative
 tolerance, this path solves it exactly, and each field solve stops after at
 most two V-cycles at 1e-4 relative residual.  The bounds below are those
@@ -51,6 +51,7 @@ CASES = {
     "test_2d_photoi_chem": 1e-4,
     "test_cyl_ion_motion": 1e-5,
     "test_cyl_ion_motion_v2": 1e-7,
+    "test_cyl_photoi_chem": 1e-5,
     "test_3d": 3e-5,
     "test_3d_chem": 1e-4,
     "test_3d_photoi_chem": 1e-4,
@@ -140,7 +141,7 @@ def test_log_writer_reproduces_reference_logs(tmp_path):
     fields): every stored log read and written back is identical."""
     import glob
     logs = sorted(glob.glob(os.path.join(GOLD, "*_rtest.log")) + glob.glob(os.path.join(GOLD3, "*_rtest.log")))
-    assert len(logs) == 10
+    assert len(logs) == 11
     for path in logs:
         head, rows = sp.read_regression_log(path)
         n = (len(head) - 3) // 3
