@@ -1098,7 +1098,8 @@ def main(argv=None):
     ap.add_argument("cfg")
     ap.add_argument("--ndim", type=int, default=2, choices=[2, 3])
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
-    ap.add_argument("--log", default=None, help="regression log to write (default: <cfg>_rtest.out.log)")
+    ap.add_argument("--log", default=None,
+                    help="regression log to write (default: <cfg name>_rtest.out.log in the current directory)")
     ap.add_argument("--end-time", type=float, default=None)
     a = ap.parse_args(argv)
     cfg = ProgramConfig(a.cfg, ndim=a.ndim)
@@ -1106,7 +1107,7 @@ def main(argv=None):
     prog = Program(cfg, functools.partial(GpuEngine, precision=prec), log=print)
     prog.set_initial_conditions()
     rows = prog.run(end_time=a.end_time)
-    out = a.log or os.path.splitext(a.cfg)[0] + "_rtest.out.log"
+    out = a.log or os.path.splitext(os.path.basename(a.cfg))[0] + "_rtest.out.log"
     write_regression_log(out, [s.name for s in prog.model.species], rows)
     prog.engine.close()
     print(f"{prog.n_steps} steps ({prog.n_rejected} rejected); log written to {out}")
