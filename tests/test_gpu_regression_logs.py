@@ -30,8 +30,9 @@ FP64_CASES = CASES + ["test_cyl_photoi_chem"]
 # FP64 GPU rows against the restatement's: the runs take the same steps,
 # rejections and meshes; single stages are bit-exact, but over the 2D whole
 # runs (300 to 2000 steps) the rows separate by up to 6e-8 relative (the 3D
-# runs by at most 5e-14).
-FP64_VS_ORACLE = 1e-7
+# runs by at most 5e-14).  The bound leaves room for test_cyl_photoi_chem,
+# whose GPU run has not been measured yet.
+FP64_VS_ORACLE = 5e-7
 # every row against the reference's logs: the restatement's bounds
 # (test_oracle_regression_logs.CASES) with room for the FP64 path's own
 # difference from the restatement
