@@ -69,11 +69,24 @@ int afg_adjust_refinement(const afg_tree_desc* tr, const int* box_flags, int max
   const int nch = 1 << D, nnb = 2 * D, nm = D == 2 ? 9 : 27;
   std::vector<int64_t> f(box_flags, box_flags + n);
   std::vector<char> has_ch(n, 0);
-  for (int b = 0; b < n; b++)
-    for (int c = 0; c < nch; c++) has_ch[b] |= tr->children[(size_t)b * nch + c] > 0;
+  for (int b = 0; b < n; b++) {
+    if (tr->lvl[b] < 1 || tr->lvl[b] > H || tr->parent[b] < 0 || tr->parent[b] > n) return AFG_ERR_ARG;
+    for (int c = 0; c < nch; c++) {
+      const int ch = tr->children[(size_t)b * nch + c];
+      if (ch < 0 || ch > n) return AFG_ERR_ARG;
+      has_ch[b] |= ch > 0;
+    }
+    for (int q = 0; q < nnb; q++)
+      if (tr->neighbors[(size_t)b * nnb + q] < kPhys || tr->neighbors[(size_t)b * nnb + q] > n) return AFG_ERR_ARG;
+  }
   auto lvl_list = [&](const int* off, const int* data, int l) {  // l 1-based
     return std::vector<int>(data + off[l - 1], data + off[l]);
   };
+  for (int l = 1; l <= H; l++)
+    for (const std::vector<int>& v : {lvl_list(tr->ids_off, tr->ids, l), lvl_list(tr->leaves_off, tr->leaves, l),
+                                      lvl_list(tr->parents_off, tr->parents, l)})
+      for (int id : v)
+        if (id < 1 || id > n) return AFG_ERR_ARG;
   // max-level clamp
   if (H >= max_lvl)
     for (int id : lvl_list(tr->ids_off, tr->ids, max_lvl))
@@ -87,7 +100,9 @@ int afg_adjust_refinement(const afg_tree_desc* tr, const int* box_flags, int max
         for (int nb = 0; nb < nnb; nb++)
           if (tr->neighbors[(size_t)b * nnb + nb] == kNoBox) {
             const int p = tr->parent[b];
-            f[tr->neighbors[(size_t)(p - 1) * nnb + nb] - 1] = kRefine;
+            const int pn = p > 0 ? tr->neighbors[(size_t)(p - 1) * nnb + nb] : 0;
+            if (pn <= 0 || pn > n) return AFG_ERR_ARG;   // not 2:1 balanced
+            f[pn - 1] = kRefine;
           }
       } else if (f[b] == kRmRef) {
         for (int nb = 0; nb < nnb; nb++) {
@@ -104,6 +119,8 @@ int afg_adjust_refinement(const afg_tree_desc* tr, const int* box_flags, int max
     for (int id : lvl_list(tr->parents_off, tr->parents, l)) {
       const int* c = tr->children + (size_t)(id - 1) * nch;
       bool all_ch = true, all_rm = true;
+      for (int q = 0; q < nch; q++)
+        if (c[q] < 1) return AFG_ERR_ARG;   // a parent without all its children
       for (int q = 0; q < nch; q++) {
         all_ch = all_ch && has_ch[c[q] - 1];
         all_rm = all_rm && f[c[q] - 1] == kRmRef;
