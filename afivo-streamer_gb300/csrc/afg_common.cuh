@@ -267,17 +267,27 @@ __device__ __forceinline__ void acc_absmax(double& mx, double v) {
   const long long m = __double_as_longlong(mx);
   mx = __longlong_as_double(b > m ? b : m);
 }
-__device__ __forceinline__ void acc_absmax(float& mx, float v) { mx = fmaxf(mx, fabsf(v)); }
+// FP32: the same maximum, a NaN kept once seen (fmaxf would drop it)
+__device__ __forceinline__ void acc_absmax(float& mx, float v) {
+  const float a = fabsf(v);
+  mx = (mx != mx || mx > a) ? mx : a;
+}
 
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
   atomicMax(addr, (unsigned long long)__double_as_longlong(v));
 }
 
+// CTA-wide maximum of non-negative values; a NaN of any thread is the
+// result (a diverged residual must not read as converged)
+template <typename T>
+__device__ __forceinline__ T nan_max(T v, T w) {
+  return (v != v || v > w) ? v : w;
+}
 template <typename T>
 __device__ __forceinline__ T block_max(T v, T* sbuf) {
   for (int o = 16; o > 0; o >>= 1) {
     T w = __shfl_xor_sync(0xffffffffu, v, o);
-    v = v > w ? v : w;
+    v = nan_max(v, w);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) sbuf[warp] = v;
@@ -287,7 +297,7 @@ __device__ __forceinline__ T block_max(T v, T* sbuf) {
     v = lane < nw ? sbuf[lane] : T(0);
     for (int o = 16; o > 0; o >>= 1) {
       T w = __shfl_xor_sync(0xffffffffu, v, o);
-      v = v > w ? v : w;
+      v = nan_max(v, w);
     }
   }
   return v;  // valid in thread 0

@@ -332,10 +332,13 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
     }
     const bool ok = mbar_wait(&bar[st], (it >> 1) & 1);
     if (__syncthreads_or(!ok)) {
+      // give up: drain the copies in flight into both stages (bounded
+      // waits); if they do not complete either, bit 2 of *err tells the
+      // host that the CTA returned with copies outstanding
       if (threadIdx.x == 0) {
-        atomicExch(err, 1u);
-        mbar_wait(&bar[st], (it >> 1) & 1);
-        if (next) mbar_wait(&bar[st ^ 1], ((it + 1) >> 1) & 1);
+        bool drained = mbar_wait(&bar[st], (it >> 1) & 1);
+        if (next) drained = mbar_wait(&bar[st ^ 1], ((it + 1) >> 1) & 1) && drained;
+        atomicOr(err, drained ? 1u : 3u);
       }
       return;
     }

@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict_
     }
     const float res = d2f(f[x] - lp);
     ro[x] = res;
-    mx = fmaxf(mx, fabsf(res));
+    acc_absmax(mx, res);
   }
   mx = block_max<float>(mx, sred);
   if (threadIdx.x == 0) atomic_max_nonneg(inst_max(t, maxbits, slot), f2d(mx));

@@ -28,8 +28,21 @@ double* g_scratch_ptr[kMaxDevices] = {};
 std::once_flag g_once[kMaxDevices];
 cudaError_t g_setup_err[kMaxDevices] = {};
 
+// Maxima of non-negative values (magnitudes, NaN included) compared as
+// integers: the IEEE-754 bit patterns of non-negative doubles order like the
+// numbers, and a NaN magnitude (exponent all ones, mantissa non-zero) sorts
+// above infinity, so a NaN anywhere in the data is the result, exactly as
+// with afg_maxabs.  fmax would drop it.
+__device__ __forceinline__ double max_bits(double a, double b) {
+  const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  return __longlong_as_double(x > y ? x : y);
+}
+__device__ __forceinline__ double abs_bits(double v) {
+  return __longlong_as_double(__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFll);
+}
+
 __device__ __forceinline__ double warp_max(double v) {
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = 16; o > 0; o >>= 1) v = max_bits(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
 
@@ -57,7 +70,7 @@ __global__ void __launch_bounds__(256) k_maxabs_boxes(const double* __restrict__
   for (int w = threadIdx.x; w < count; w += blockDim.x) {
     const int i = w % nc + 1, r = w / nc;
     const int j = ndim == 2 ? r + 1 : r % nc + 1, k = ndim == 2 ? 0 : r / nc + 1;
-    mx = fmax(mx, fabs(a[i + n2 * (j + n2 * k)]));
+    mx = max_bits(mx, abs_bits(a[i + n2 * (j + n2 * k)]));
   }
   mx = block_max_nonneg(mx);
   if (threadIdx.x == 0) scratch[blockIdx.x] = mx;
@@ -66,7 +79,7 @@ __global__ void __launch_bounds__(256) k_maxabs_boxes(const double* __restrict__
 // Pass 2: one CTA folds the n per-box maxima into scratch[AFG_NOALLOC_MAX_BOXES].
 __global__ void __launch_bounds__(1024) k_maxabs_fold(int n, double* __restrict__ scratch) {
   double mx = 0.0;
-  for (int b = threadIdx.x; b < n; b += blockDim.x) mx = fmax(mx, scratch[b]);
+  for (int b = threadIdx.x; b < n; b += blockDim.x) mx = max_bits(mx, scratch[b]);
   mx = block_max_nonneg(mx);
   if (threadIdx.x == 0) scratch[AFG_NOALLOC_MAX_BOXES] = mx;
 }
@@ -89,6 +102,9 @@ extern "C" int afg_maxabs_noalloc(const double* d_pool, const int* d_slots, int 
     *result = 0.0;
     return AFG_OK;
   }
+  // an error left pending by earlier work of the caller is reported here,
+  // before any launch, so that the launch checks below see only this call's
+  if (cudaGetLastError() != cudaSuccess) return AFG_ERR_CUDA;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return AFG_ERR_CUDA;
   std::call_once(g_once[dev], setup_device, dev);

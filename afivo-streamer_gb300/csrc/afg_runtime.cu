@@ -130,6 +130,10 @@ struct afg_ctx {
   // whenever maxima are read back (pinned copy in h_err)
   unsigned* d_err = nullptr;
   unsigned* h_err = nullptr;
+  // set when a kernel reported (error word bit 2) that it returned with
+  // copies into its shared memory still outstanding after its bounded drain:
+  // the context then refuses every further multigrid and transport call
+  bool poisoned = false;
   int n_sm = 0;
   // side streams and events for independent branches (photoionization modes)
   cudaStream_t side[kMaxBranch] = {};
@@ -856,13 +860,22 @@ static double inst_value(const afg_ctx* ctx, int slot, int q) {
 }
 
 // the slot's maximum (over all instances of a batched tree)
+static int wait_failed(afg_ctx* ctx) {
+  if (*ctx->h_err & 2u) {
+    ctx->poisoned = true;
+    return fail(ctx, AFG_ERR_CUDA, "a bounded wait on a copy into shared memory timed out and the copies did "
+                                   "not drain; the context is unusable");
+  }
+  return fail(ctx, AFG_ERR_CUDA, "a bounded wait on a copy into shared memory timed out");
+}
+
 static int read_max(afg_ctx* ctx, int slot, double* out) {
   CK(cudaMemcpyAsync(ctx->h_err, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
   if (!inst_slot(ctx, slot)) {
     CK(cudaMemcpyAsync(ctx->h_max + slot, ctx->d_max + slot, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                        ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    if (*ctx->h_err) return fail(ctx, AFG_ERR_CUDA, "a bounded wait on a copy into shared memory timed out");
+    if (*ctx->h_err) return wait_failed(ctx);
     *out = bits_to_double(ctx->h_max[slot]);
     return AFG_OK;
   }
@@ -870,7 +883,7 @@ static int read_max(afg_ctx* ctx, int slot, double* out) {
   CK(cudaMemcpy2DAsync(ctx->h_max + slot, pitch, ctx->d_max + slot, pitch, sizeof(unsigned long long), ctx->n_inst,
                        cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  if (*ctx->h_err) return fail(ctx, AFG_ERR_CUDA, "a bounded wait on a copy into shared memory timed out");
+  if (*ctx->h_err) return wait_failed(ctx);
   double mx = 0;
   for (int q = 0; q < ctx->n_inst; q++) mx = std::max(mx, inst_value(ctx, slot, q));
   *out = mx;
@@ -1960,6 +1973,7 @@ static int build_coarse(afg_ctx* ctx, MgSlot& m) {
 
 static int get_mg(afg_ctx* ctx, int mg_id, MgSlot** out) {
   if (!ctx) return AFG_ERR_ARG;
+  if (ctx->poisoned) return fail(ctx, AFG_ERR_CUDA, "context unusable after a failed drain of shared-memory copies");
   if (!ctx->have_tree) return fail(ctx, AFG_ERR_STATE, "no tree");
   if (mg_id < 0 || mg_id >= kMaxMg || !ctx->mg[mg_id].used) return fail(ctx, AFG_ERR_STATE, "mg slot %d not set up", mg_id);
   *out = &ctx->mg[mg_id];

@@ -5,6 +5,7 @@
 
 static int need_transport(afg_ctx* ctx) {
   if (!ctx) return AFG_ERR_ARG;
+  if (ctx->poisoned) return fail(ctx, AFG_ERR_CUDA, "context unusable after a failed drain of shared-memory copies");
   if (!ctx->have_tree) return fail(ctx, AFG_ERR_STATE, "no tree");
   if (!ctx->tr.ready) return fail(ctx, AFG_ERR_STATE, "afg_transport_setup not called");
   return AFG_OK;

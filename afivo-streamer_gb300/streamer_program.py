@@ -23,9 +23,11 @@ oracle's tests.  What it restates:
 * set_initial_conditions (src/streamer.f90:480-533) and the time loop
   (src/streamer.f90:181-432).
 
-Keys whose values would need code outside the path (electrodes, dielectrics,
-photoionization, gas dynamics, other integrators' IMEX forms, chemistry
-files, stochastic densities, energy equation) raise `Unsupported`.
+Photoionization by the Helmholtz method, chemistry and reaction files and
+mobile ions are supported.  Keys whose values would need code outside the
+path (electrodes, dielectrics, Monte Carlo photoionization, gas dynamics,
+the IMEX integrators, stochastic densities, the energy equation) raise
+`Unsupported`.
 """
 from __future__ import annotations
 

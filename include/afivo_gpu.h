@@ -4,7 +4,7 @@
  *
  * The reference is Fortran 2008 (MD-CWI/afivo-streamer).  Its callers stay as
  * they are; the bodies of the public afivo routines gain a branch that calls
- * these functions through ISO_C_BINDING (bindings in INTEGRATION.md).  Every
+ * these functions through ISO_C_BINDING interfaces.  Every
  * function returns an int status: AFG_OK (0) or a negative AFG_ERR_* code;
  * afg_last_error() gives a one-line reason.  Nothing here aborts or traps:
  * device-side failures are raised in a device error word that is read back on
@@ -584,16 +584,21 @@ int afg_kernel_stats(afg_ctx* ctx, long long* launches, double* ms, double* byte
  * pool, or run under a fixed device-memory budget) and so cannot create a
  * context: max |v| over the interior cells of the boxes d_slots[0..n_slots-1]
  * (0-based box slots, in device memory) of a caller-owned device pool laid
- * out like one afivo variable, d_pool[slot][(n_cell+2)^ndim] (the
- * af_tree_maxabs_cc reduction).  Nothing is allocated: the scratch is a
- * file-scope device array of AFG_NOALLOC_MAX_BOXES + 1 doubles (2 MiB) that
- * every GPU loading this library holds until the process exits; n_slots
- * beyond AFG_NOALLOC_MAX_BOXES returns AFG_ERR_ARG.  The first call on a
- * device looks up the array's device address; make that first call before
- * any stream capture.  All calls share the array, so calls that overlap on
- * the GPU (other streams, other threads) race; each call writes every entry
- * it reads, so nothing needs clearing.  Runs on `stream` (a cudaStream_t,
- * NULL = default stream) and synchronises it; *result is a host double. */
+ * out like one variable of this library's pools, d_pool[slot][(n_cell+2)^ndim]
+ * (the same reduction as afg_maxabs; a NaN in the data is the result, as
+ * there).  Nothing is allocated: the scratch is a file-scope device array of
+ * AFG_NOALLOC_MAX_BOXES + 1 doubles (2 MiB) that every GPU loading this
+ * library holds until the process exits; n_slots beyond
+ * AFG_NOALLOC_MAX_BOXES returns AFG_ERR_ARG.  The first call on a device
+ * looks up the array's device address with that device current.  Every call
+ * copies the result into host memory and synchronises `stream`, so no call
+ * may be made while any stream is being captured into a CUDA graph.  All
+ * calls share the array, so calls that overlap on the GPU (other streams,
+ * other threads) race; each call writes every entry it reads, so nothing
+ * needs clearing.  A CUDA error left pending by earlier work is returned as
+ * AFG_ERR_CUDA before anything is launched (and cleared, as
+ * cudaGetLastError does).  Runs on `stream` (a cudaStream_t, NULL = default
+ * stream); *result is a host double. */
 #define AFG_NOALLOC_MAX_BOXES 262144
 int afg_maxabs_noalloc(const double* d_pool, const int* d_slots, int n_slots,
                        int ndim, int n_cell, void* stream, double* result);

@@ -41,6 +41,30 @@ def test_maxabs_noalloc_matches_context_entry_point(gpu_lib):
     ctx.close()
 
 
+def test_maxabs_noalloc_propagates_nan_like_context_entry_point(gpu_lib):
+    """A NaN in one interior cell is the result of both entry points (a
+    diverged solve must not read as converged), twice in a row."""
+    torch = pytest.importorskip("torch")
+    tree = refined_tree(2, 16, [32, 32], [1e-2, 1e-2], 4, 2, [0.5e-2, 0.5e-2], 1e-3, seed=5, frac=0.1)
+    rng = np.random.default_rng(77)
+    cc = ag.new_cc(tree, 1)
+    cc[:] = rng.standard_normal(cc.shape)
+    leaves = np.concatenate(tree.lvl_leaves).astype(np.int32) - 1
+    cc[leaves[len(leaves) // 2], 0, 5, 7] = np.nan
+    ctx = ag.Context(0)
+    ctx.tree_sync(tree, 1)
+    ctx.upload(cc)
+    dev = torch.device("cuda:0")
+    pool = torch.from_numpy(np.ascontiguousarray(cc[:, 0].reshape(tree.n_boxes, -1))).to(dev)
+    d_slots = torch.from_numpy(leaves).to(dev)
+    torch.cuda.synchronize()
+    for _ in range(2):
+        got = ag.maxabs_noalloc(pool.data_ptr(), d_slots.data_ptr(), len(leaves), tree.ndim, tree.n_cell)
+        want = ctx.maxabs(1, True)
+        assert np.isnan(got) and np.isnan(want), (got, want)
+    ctx.close()
+
+
 def test_maxabs_noalloc_rejects_oversize(gpu_lib):
     """More boxes than the static scratch holds (AFG_NOALLOC_MAX_BOXES) is an
     argument error, reported before any device work."""
