@@ -5,6 +5,7 @@
 #pragma once
 #include "../../include/afivo_gpu.h"
 #include "afg_common.cuh"
+#include "afg_math.h"
 
 namespace afg {
 
@@ -434,9 +435,10 @@ struct UpdateArgs {
   unsigned long long* min_chem;  // bits of a non-negative double (atomicMin)
 };
 
-// x**c for the exponents of the analytic forms: c == 1 returns x, which is
-// what pow(x, 1) returns exactly, and skips the FP64 pow.
-__device__ __forceinline__ double pow_c(double x, double c) { return c == 1.0 ? x : pow(x, c); }
+// x**c for the exponents of the analytic forms.  FP64: the project's pow
+// (afg_math.h), bit-identical to the CPU restatement's; it returns x itself
+// for c == 1, as the reference's pow does.
+__device__ __forceinline__ double pow_c(double x, double c) { return afg_math::pow(x, c); }
 __device__ __forceinline__ float pow_c(float x, float c) { return c == 1.0f ? x : powf(x, c); }
 
 // Rate coefficient of one reaction (get_rates, src/m_chemistry.f90:672-760).
@@ -455,7 +457,7 @@ __device__ __forceinline__ double rate_of(const LtDev& lt, const afg_reaction& r
         return c0 * r.c[0] * (double)expf(-(q * q));
       } else {
         const double q = r.c[1] / (r.c[2] + td);
-        return c0 * r.c[0] * exp(-(q * q));
+        return c0 * r.c[0] * afg_math::exp(-(q * q));
       }
     case AFG_RATE_EXP_V2:
       if (F32) {
@@ -463,18 +465,18 @@ __device__ __forceinline__ double rate_of(const LtDev& lt, const afg_reaction& r
         return c0 * r.c[0] * (double)expf(-(q * q));
       } else {
         const double q = td / r.c[1];
-        return c0 * r.c[0] * exp(-(q * q));
+        return c0 * r.c[0] * afg_math::exp(-(q * q));
       }
     case AFG_RATE_K13:
       if (F32)
         return c0 * r.c[0] * (double)expf(-pow_c((float)r.c[1] / ((float)r.c[2] + (float)td), (float)r.c[3]));
       else
-        return c0 * r.c[0] * exp(-pow_c(r.c[1] / (r.c[2] + td), r.c[3]));
+        return c0 * r.c[0] * afg_math::exp(-pow_c(r.c[1] / (r.c[2] + td), r.c[3]));
     case AFG_RATE_K14:
       if (F32)
         return c0 * r.c[0] * (double)expf(-pow_c((float)td / (float)r.c[1], (float)r.c[2]));
       else
-        return c0 * r.c[0] * exp(-pow_c(td / r.c[1], r.c[2]));
+        return c0 * r.c[0] * afg_math::exp(-pow_c(td / r.c[1], r.c[2]));
     case AFG_RATE_K1: {
       // electron temperature from the tabulated mean energy (eV -> K)
       const double Te = (2 * 1.602176634e-19 / (3 * 1.380649e-23)) * lt_col(lt, r.lt_col, ix, w);

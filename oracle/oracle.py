@@ -55,6 +55,7 @@ def lib():
             "orc_prolong_limit": (C.c_int, [P, DP, C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int]),
             "orc_prolong_linear": (C.c_int, [P, DP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
             "orc_restrict_tree": (C.c_int, [P, DP, C.c_int]),
+            "orc_math_eval": (C.c_int, [C.c_int, C.c_int, DP, DP, DP]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -194,3 +195,13 @@ class Oracle:
 
     def maxabs(self, cc, iv, leaves_only=True):
         return self.L.orc_maxabs(self.p, _dp(cc), iv, int(leaves_only))
+
+
+def math_eval(which, x, y=None):
+    """The project's exp (which 0), log (1) or pow (2) on arrays, through the
+    restatement's library (host build of the same code the device runs)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(np.zeros_like(x) if y is None else y, dtype=np.float64)
+    out = np.empty_like(x)
+    lib().orc_math_eval(which, len(x), _dp(x), _dp(y), _dp(out))
+    return out

@@ -28,6 +28,10 @@
 #include <omp.h>
 
 #include "oracle_common.h"
+// exp and pow of the analytic rate forms: the project's own functions, so
+// that the restatement and the GPU path evaluate them bit for bit alike (the
+// reference calls its compiler's libm; the project's are within a few ulp)
+#include "../afivo-streamer_gb300/csrc/afg_math.h"
 
 namespace orc {
 
@@ -435,14 +439,14 @@ static double rate_of(const Transport& T, const afg_reaction& r, double td, int 
     case AFG_RATE_TABULATED_FIELD: return c0 * lt_col(T, r.lt_col, ix, w);
     case AFG_RATE_CONSTANT: return c0 * c[0];
     case AFG_RATE_LINEAR: return c0 * c[0] * (td - c[1]);
-    case AFG_RATE_EXP_V1: { double q = c[1] / (c[2] + td); return c0 * c[0] * std::exp(-(q * q)); }
-    case AFG_RATE_EXP_V2: { double q = td / c[1]; return c0 * c[0] * std::exp(-(q * q)); }
-    case AFG_RATE_K13: return c0 * c[0] * std::exp(-std::pow(c[1] / (c[2] + td), c[3]));
-    case AFG_RATE_K14: return c0 * c[0] * std::exp(-std::pow(td / c[1], c[2]));
+    case AFG_RATE_EXP_V1: { double q = c[1] / (c[2] + td); return c0 * c[0] * afg_math::exp(-(q * q)); }
+    case AFG_RATE_EXP_V2: { double q = td / c[1]; return c0 * c[0] * afg_math::exp(-(q * q)); }
+    case AFG_RATE_K13: return c0 * c[0] * afg_math::exp(-afg_math::pow(c[1] / (c[2] + td), c[3]));
+    case AFG_RATE_K14: return c0 * c[0] * afg_math::exp(-afg_math::pow(td / c[1], c[2]));
     case AFG_RATE_K1: {
       /* rate_analytic_k1: Te = electron_eV_to_K * LT(td_energy_eV, Td) */
       const double Te = (2 * ELEM / (3 * 1.380649e-23)) * lt_col(T, r.lt_col, ix, w);
-      return c0 * c[0] * std::pow(300 / Te, c[1]);
+      return c0 * c[0] * afg_math::pow(300 / Te, c[1]);
     }
   }
   return 0;
@@ -1007,6 +1011,14 @@ int orc_restrict_tree(void* p, double* cc, int iv) {
         if (ch > 0) restrict_box_geom(t, cc, ch, iv);
       }
   }
+  return AFG_OK;
+}
+
+/* The project's exp (which 0), log (1) and pow (2) on n arguments, for the
+ * accuracy test of afg_math.h against high-precision values. */
+int orc_math_eval(int which, int n, const double* x, const double* y, double* out) {
+  for (int q = 0; q < n; q++)
+    out[q] = which == 0 ? afg_math::exp(x[q]) : which == 1 ? afg_math::log(x[q]) : afg_math::pow(x[q], y[q]);
   return AFG_OK;
 }
 
