@@ -267,6 +267,7 @@ def load_library(path: str = LIB_PATH):
         "afg_autotune": (C.c_int, [P, C.c_int]),
         "afg_tuning": (C.c_int, [P, _IP]),
         "afg_set_tuning": (C.c_int, [P, _IP]),
+        "afg_set_fp32_layout": (C.c_int, [P, C.c_int]),
         "afg_set_photoi_lockstep": (C.c_int, [P, C.c_int]),
         "afg_check_bounded_wait": (C.c_int, [P, _DP]),
         "afg_refine_flags": (C.c_int, [P, C.POINTER(RefineDesc), _IP]),
@@ -481,14 +482,21 @@ class Context:
         out = (C.c_int * 2)()
         self.check(self.lib.afg_tuning(self.ptr, out), "afg_tuning")
 
-        def name(v):
+        compact = getattr(self, "fp32_compact", True)
+
+        def name(v, fp32=False):
+            if fp32 and compact:
+                if v & GSRB_STAGED:
+                    return (f"compact red-black layout, other colour staged in shared memory (bulk copies), "
+                            f"{v & 15} cells/thread")
+                return "compact red-black layout, one box per CTA"
             if v <= 0:
                 return "generic"
             if v & GSRB_STAGED:
                 what = "phi and rhs" if v & GSRB_STAGED_RHS else "phi"
                 return f"{what} staged in shared memory (bulk copies), {v & 15} cells/thread"
             return f"{v} cells/thread"
-        return {"gsrb_fp32": name(out[0]), "gsrb_fp64": name(out[1]), "codes": [out[0], out[1]]}
+        return {"gsrb_fp32": name(out[0], True), "gsrb_fp64": name(out[1]), "codes": [out[0], out[1]]}
 
     def check_bounded_wait(self):
         """(status, ms): AFG_ERR_DEVICE when a timed-out device wait was
@@ -503,6 +511,12 @@ class Context:
     def set_tuning(self, fp32, fp64):
         a = np.array([fp32, fp64], dtype=np.int32)
         self.check(self.lib.afg_set_tuning(self.ptr, _ip(a)), "afg_set_tuning")
+
+    def set_fp32_layout(self, compact):
+        """afg_set_fp32_layout: FP32 correction buffers of the mixed solves
+        in the compact red-black layout (True, the default) or ghosted."""
+        self.fp32_compact = bool(compact)
+        self.check(self.lib.afg_set_fp32_layout(self.ptr, int(bool(compact))), "afg_set_fp32_layout")
 
     def transfers_wait(self):
         self.check(self.lib.afg_transfers_wait(self.ptr), "afg_transfers_wait")

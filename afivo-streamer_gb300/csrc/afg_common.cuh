@@ -20,6 +20,8 @@ constexpr int kNbRefine = -1; // refinement boundary (af_no_box)
 // Device view of the tree tables, passed to kernels by value.
 struct KTree {
   int D, nc, n2, S, NF;
+  int SI;         // interior cells per box, nc^D
+  long long nbox; // boxes in the pools (compact FP32 buffers: ghost blocks follow nbox interior blocks)
   const int* parent;    // [n] parent slot or -1
   const int* children;  // [n][2^D] child slot or -1
   const int* nbr;       // [n][2D] neighbour slot, kNbRefine or kNbPhys
@@ -81,6 +83,7 @@ __device__ __forceinline__ KTree fix_dims(KTree t) {
     t.n2 = NC + 2;
     t.S = D == 2 ? (NC + 2) * (NC + 2) : (NC + 2) * (NC + 2) * (NC + 2);
     t.NF = D == 2 ? (NC + 1) * (NC + 1) : (NC + 1) * (NC + 1) * (NC + 1);
+    t.SI = D == 2 ? NC * NC : NC * NC * NC;
   }
   return t;
 }

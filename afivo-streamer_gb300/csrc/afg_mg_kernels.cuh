@@ -737,16 +737,17 @@ __global__ void k_coarse_matvec(int n, int nloc, ModeArg<const double> ainv_, Mo
   if (lane == 0) x[row] = s;
 }
 
+// (stride: values per box of phi's blocks, the cell index from ccell)
 template <typename T>
 __global__ void k_coarse_scatter(KTree t, int n, const int* __restrict__ cslot, const int* __restrict__ ccell,
-                                 ModeArg<const double> x_, ModeArg<T> phi_) {
+                                 int stride, ModeArg<const double> x_, ModeArg<T> phi_) {
   const double* __restrict__ x = x_.get();
   T* __restrict__ phi = phi_.get();
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
   const int slot = cslot[g];
   if (box_frozen(t, slot)) return;
-  phi[(size_t)slot * t.S + ccell[g]] = T(x[g]);
+  phi[(size_t)slot * stride + ccell[g]] = T(x[g]);
 }
 
 // Freeze flags of batched instances as the kernels read them: the converged

@@ -22,8 +22,11 @@ namespace afg {
 // the launch and are left alone, since finer boxes' rules read them), then
 // applies the stencil to the stored values.  The Cartesian stencil is one
 // FMA chain (8 FP64 instructions per cell); r is rounded to FP32 by bit
-// truncation and its maximum taken in FP32.
-template <int D, bool CYL, int NC = 0>
+// truncation and its maximum taken in FP32.  RB: the FP32 buffers have the
+// compact red-black layout (afg_mg32.cuh); e's ghost block is cleared only on
+// parents and refinement sources, the boxes whose ghost cells the FP32
+// V-cycle reads before writing them.
+template <int D, bool CYL, int NC = 0, bool RB = false>
 __global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict__ rec, ModeArg<double> phi_,
                                                 ModeArg<const double> rhs_, ModeArg<float> r32_,
                                                 ModeArg<float> e32_, ModeCoef<double> mc_, GcDev g,
@@ -42,10 +45,20 @@ __global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict_
   const int slot = r0.x;
   if (box_frozen(t, slot)) return;
   const int nc = t.nc, n2 = t.n2;
-  float* eo = e32 + (size_t)slot * t.S;
-  for (int x = threadIdx.x; x < t.S; x += blockDim.x) eo[x] = 0.0f;
+  const bool leaf = is_leaf[slot] != 0;
+  if (RB) {
+    float* ei = e32 + (size_t)slot * t.SI;
+    for (int x = threadIdx.x; x < t.SI; x += blockDim.x) ei[x] = 0.0f;
+    if (!leaf || r1.w != 0) {
+      float* eg = e32 + (size_t)t.nbox * t.SI + (size_t)slot * t.S;
+      for (int x = threadIdx.x; x < t.S; x += blockDim.x) eg[x] = 0.0f;
+    }
+  } else {
+    float* eo = e32 + (size_t)slot * t.S;
+    for (int x = threadIdx.x; x < t.S; x += blockDim.x) eo[x] = 0.0f;
+  }
   // parents need no defect: the V-cycle's restriction overwrites their rhs
-  if (!is_leaf[slot]) return;
+  if (!leaf) return;
   double* pw_ = phi + (size_t)slot * t.S;
   if (r1.w == 0) {
     const int nface = D == 2 ? nc : nc * nc;
@@ -61,7 +74,7 @@ __global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict_
   for (int q = 0; q < 7; q++) cd[q] = mc.cb[slot * 8 + q];
   const double* p = pw_;
   const double* f = rhs + (size_t)slot * t.S;
-  float* ro = r32 + (size_t)slot * t.S;
+  float* ro = r32 + (size_t)slot * (RB ? t.SI : t.S);
   float mx = 0.0f;
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;
   for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
@@ -85,7 +98,7 @@ __global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict_
                    fma(cd[4], p[x + n2], fma(cd[3], p[x - n2], fma(cd[2], p[x + 1], fma(cd[1], p[x - 1], cd[0] * p[x]))))));
     }
     const float res = d2f(f[x] - lp);
-    ro[x] = res;
+    ro[RB ? rb_idx<D>(nc, i, j, k) : x] = res;
     acc_absmax(mx, res);
   }
   mx = block_max<float>(mx, sred);
@@ -117,7 +130,45 @@ __global__ void __launch_bounds__(256) k_add_correction(KTree t, const int* __re
   for (int x = threadIdx.x; x < S; x += blockDim.x) p[x] = p[x] + f2d(e[x]);
 }
 
+// phi += e on the interior cells, e in the compact layout.  The boxes are
+// leaves; their ghost cells of phi are filled again before anything reads
+// them (mixed_prepare and the defect's own face ghosts, mixed_finish).
+template <int D, int NC = 0>
+__global__ void __launch_bounds__(256) k_add_correction_rb(KTree t0, const int* __restrict__ list,
+                                                           ModeArg<double> phi_, ModeArg<const float> e32_) {
+  const KTree t = fix_dims<D, NC>(t0);
+  double* __restrict__ phi = phi_.get();
+  const float* __restrict__ e32 = e32_.get();
+  const int slot = list[blockIdx.x];
+  if (box_frozen(t, slot)) return;
+  const int nc = t.nc, n2 = t.n2;
+  double* p = phi + (size_t)slot * t.S;
+  const float* e = e32 + (size_t)slot * t.SI;
+  for (int w = threadIdx.x; w < t.SI; w += blockDim.x) {
+    const int i = w % nc + 1, r = w / nc;
+    const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
+    const int x = D == 2 ? at2(n2, i, j) : at3(n2, i, j, k);
+    p[x] = p[x] + f2d(e[rb_idx<D>(nc, i, j, k)]);
+  }
+}
+
 }  // namespace afg
+
+// phi += e on the boxes of a list (leaves), every lockstep slot
+static int launch_add_correction(afg_ctx* ctx, const int* list, int n, ModeArg<double> phi, ModeArg<const float> e) {
+  if (n <= 0) return AFG_OK;
+  const dim3 grid(n, ctx->ky);
+  const KTree t = ktree(ctx);
+  if (!ctx->rb32)
+    k_add_correction<<<grid, 256, 0, ctx->stream>>>(t, list, phi, e);
+  else if (ctx->D == 3)
+    AFG_NC3(NCV_, k_add_correction_rb<3, NCV_><<<grid, 256, 0, ctx->stream>>>(t, list, phi, e));
+  else
+    AFG_NC2(NCV_, k_add_correction_rb<2, NCV_><<<grid, 256, 0, ctx->stream>>>(t, list, phi, e));
+  ctx->launches++;
+  CKL();
+  return AFG_OK;
+}
 
 // All boxes: the correction starts at zero everywhere (an FMG from zero
 // prolongs the change of the level-1 correction, so it must start at zero
@@ -132,7 +183,17 @@ static int launch_defect(afg_ctx* ctx, MgSlot& m, ModeArg<double> phi, ModeArg<c
   const ModeArg<float> r32 = slot_bufs(ctx, m, &MgSlot::r32), e32 = slot_bufs(ctx, m, &MgSlot::e32);
   const ModeCoef<double> c = coefs<double>(ctx, m);
   const dim3 grid(n, ctx->ky);
-  if (ctx->D == 3)
+  if (ctx->rb32) {
+    if (ctx->D == 3)
+      AFG_NC3(NCV_, k_defect<3, false, NCV_, true><<<grid, 256, 0, ctx->stream>>>(t, list, phi, rhs, r32, e32, c, g,
+                                                                                 ctx->d_is_leaf, maxbits));
+    else if (ctx->coord == AFG_CYL)
+      AFG_NC2(NCV_, k_defect<2, true, NCV_, true><<<grid, 256, 0, ctx->stream>>>(t, list, phi, rhs, r32, e32, c, g,
+                                                                                ctx->d_is_leaf, maxbits));
+    else
+      AFG_NC2(NCV_, k_defect<2, false, NCV_, true><<<grid, 256, 0, ctx->stream>>>(t, list, phi, rhs, r32, e32, c, g,
+                                                                                 ctx->d_is_leaf, maxbits));
+  } else if (ctx->D == 3)
     AFG_NC3(NCV_, k_defect<3, false, NCV_><<<grid, 256, 0, ctx->stream>>>(t, list, phi, rhs, r32, e32, c, g, ctx->d_is_leaf,
                                                    maxbits));
   else if (ctx->coord == AFG_CYL)
@@ -205,10 +266,7 @@ static int mixed_fmg(afg_ctx* ctx, MgSlot& m, ModeArg<double> phi, ModeArg<doubl
   RC(launch_defect(ctx, m, phi, rhs, ModeArg<unsigned long long>(ctx->d_max + 2)));
   RC(mg_fmg<float>(ctx, m, slot_bufs(ctx, m, &MgSlot::e32), slot_bufs(ctx, m, &MgSlot::r32),
                    slot_bufs(ctx, m, &MgSlot::t32), false, false, nullptr, true));
-  k_add_correction<<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(ktree(ctx), list, phi,
-                                                             ModeArg<const float>(slot_bufs(ctx, m, &MgSlot::e32)));
-  ctx->launches++;
-  CKL();
+  RC(launch_add_correction(ctx, list, n, phi, ModeArg<const float>(slot_bufs(ctx, m, &MgSlot::e32))));
   RC(mixed_prepare(ctx, m, phi));
   if (set_residual) RC(launch_defect(ctx, m, phi, rhs, maxbits));
   return mixed_finish(ctx, m, phi);

@@ -16,6 +16,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -23,6 +24,7 @@
 #include "afg_common.cuh"
 #include "afg_gc_kernels.cuh"
 #include "afg_mg_kernels.cuh"
+#include "afg_mg32.cuh"
 #include "afg_transport.cuh"
 
 using namespace afg;
@@ -101,6 +103,7 @@ struct afg_ctx {
   unsigned char* d_is_leaf = nullptr;
   int* d_cslot = nullptr;   // coarse unknown -> slot (instance-major on batched trees)
   int* d_ccell = nullptr;   // coarse unknown -> cell index
+  int* d_ccell_rb = nullptr;  // the same in the compact FP32 layout (interior block)
   // Batched independent instances (afg_tree_sync_batched); n_inst = 0 for a
   // single tree.  The coarse grids of all instances are alike (nloc
   // unknowns each) and share one inverse.
@@ -140,7 +143,10 @@ struct afg_ctx {
   cudaEvent_t ev_fork = nullptr, ev_join[kMaxBranch] = {};
   // smoother work shape (cells of a colour per thread) for the specialized
   // box sizes: [0] FP32, [1] FP64; picked by the autotuner, 0 = default
-  int gsrb_cpt[2] = {0, 0};
+  int gsrb_cpt[3] = {0, 0, 0};  // [2]: FP32 on the compact layout
+  // FP32 correction buffers of the mixed solves in the compact red-black
+  // layout (afg_mg32.cuh); false: the ghosted (nc+2)^D layout
+  bool rb32 = true;
   // lockstep problems (Helmholtz modes as multiple right-hand sides): while
   // ky > 1 every multigrid launch covers the slots grp[0..ky-1], blockIdx.y
   // selecting the slot; ky = 1 otherwise
@@ -206,6 +212,12 @@ static int fail(afg_ctx* c, int code, const char* fmt, ...) {
                   __FILE__, __LINE__);                                                      \
   } while (0)
 
+#define RC(x)                 \
+  do {                        \
+    int rc_ = (x);            \
+    if (rc_ != AFG_OK) return rc_; \
+  } while (0)
+
 template <typename T>
 static cudaError_t dalloc(T** p, size_t n) {
   *p = nullptr;
@@ -226,6 +238,8 @@ static KTree ktree(const afg_ctx* c) {
   t.n2 = c->n2;
   t.S = c->S;
   t.NF = c->NF;
+  t.SI = c->D == 2 ? c->nc * c->nc : c->nc * c->nc * c->nc;
+  t.nbox = c->n_boxes;
   t.parent = c->d_parent;
   t.children = c->d_children;
   t.nbr = c->d_nbr;
@@ -292,7 +306,7 @@ static void free_tree(afg_ctx* c) {
   clear_graphs(c);
   dfree(c->d_parent); dfree(c->d_children); dfree(c->d_nbr); dfree(c->d_pnb); dfree(c->d_nbmat);
   dfree(c->d_ix); dfree(c->d_rmin); dfree(c->d_dr); dfree(c->d_idr); dfree(c->d_idrf); dfree(c->d_lists); dfree(c->d_rec); dfree(c->d_is_leaf); dfree(c->d_geo);
-  dfree(c->d_cslot); dfree(c->d_ccell);
+  dfree(c->d_cslot); dfree(c->d_ccell); dfree(c->d_ccell_rb);
   dfree(c->d_inst); dfree(c->d_frozen); dfree(c->d_frozen_base); dfree(c->d_inst_hl);
   if (c->h_frozen) cudaFreeHost(c->h_frozen);
   c->h_frozen = nullptr;
@@ -321,11 +335,29 @@ static void free_tree(afg_ctx* c) {
 /* ------------------------------------------------------------------------- */
 // Generic launchers dispatching on (D, cylindrical, T)
 
+// the FP32 buffers of the mixed solves in the compact layout (afg_mg32.cuh)
+template <typename T>
+static bool rb_of(const afg_ctx* ctx) {
+  return std::is_same<T, float>::value && ctx->rb32;
+}
+
 template <typename T>
 static int launch_gc(afg_ctx* ctx, const int* list, int n, ModeArg<T> v, const GcDev& g, int corners) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   kt_begin(ctx, AFG_KT_GHOST);
+  if constexpr (std::is_same<T, float>::value) {
+    if (ctx->rb32) {
+      if (ctx->D == 2)
+        AFG_NC2(NCV_, k_gc_rb<2, NCV_><<<dim3(n, ctx->ky), 128, 0, ctx->stream>>>(t, rec_of(ctx, list), v, g, corners));
+      else
+        AFG_NC3(NCV_, k_gc_rb<3, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, rec_of(ctx, list), v, g, corners));
+      kt_end(ctx, AFG_KT_GHOST, 2.0 * sizeof(T) * n * ctx->ky * 2 * ctx->D * (box_cells(ctx) / ctx->nc));
+      ctx->launches++;
+      CKL();
+      return AFG_OK;
+    }
+  }
   if (ctx->D == 2)
     AFG_NC2(NCV_, k_gc<2, T, NCV_><<<dim3(n, ctx->ky), 128, 0, ctx->stream>>>(t, rec_of(ctx, list), v, g, corners));
   else
@@ -339,6 +371,7 @@ static int launch_gc(afg_ctx* ctx, const int* list, int n, ModeArg<T> v, const G
 template <typename T>
 static int launch_gsrb(afg_ctx* ctx, const int* list, int n, T* phi, const T* rhs, int rb, MgCoef<T> lam) {
   if (n <= 0) return AFG_OK;
+  if (rb_of<T>(ctx)) return fail(ctx, AFG_ERR_STATE, "the unfused smoother needs the ghosted FP32 layout");
   KTree t = ktree(ctx);
   const int threads = ctx->D == 2 ? std::min(256, ctx->nc * ctx->nc / 2) : std::min(256, ctx->nc * ctx->nc * ctx->nc / 2);
   kt_begin(ctx, AFG_KT_GSRB);
@@ -440,6 +473,60 @@ static int launch_gsrb_rec(afg_ctx* ctx, const int* rec, int n, ModeArg<T> phi, 
   return AFG_OK;
 }
 
+// Half sweep on the compact FP32 layout.  code: cpt | kGsrbTma selects the
+// shared-memory-staged persistent kernel with cpt cells of the colour per
+// thread (3D 8^3: 1, 2, 4; 2D 16^2: 1, 2, 4); anything else (and box sizes
+// without a specialization) the one-box-per-CTA kernel.
+template <int D, bool CYL, int NC, int CPT>
+static int launch_gsrb_rb_tma(afg_ctx* ctx, const int* rec, int n, ModeArg<float> phi, ModeArg<const float> rhs,
+                              int rb, ModeCoef<float> lam, const GcDev& g) {
+  constexpr int TPB = (D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT;
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gsrb_rb_tma<D, CYL, NC, CPT>, TPB, 0));
+    per_sm = std::max(1, per_sm);
+  }
+  const int grid = std::min(n, std::max(1, per_sm * ctx->n_sm / ctx->ky));
+  k_gsrb_rb_tma<D, CYL, NC, CPT><<<dim3(grid, ctx->ky), TPB, 0, ctx->stream>>>(ktree(ctx), rec, n, phi, rhs, rb, lam,
+                                                                               g, ctx->d_err);
+  return AFG_OK;
+}
+
+static int launch_gsrb_rb(afg_ctx* ctx, const int* rec, int n, ModeArg<float> phi, ModeArg<const float> rhs, int rb,
+                          ModeCoef<float> lam, const GcDev& g, int code) {
+  const KTree t = ktree(ctx);
+  const int c = code & (kGsrbTma - 1);
+  if ((code & kGsrbTma) && gsrb_rec_specialized(ctx) && (c == 1 || c == 2 || c == 4)) {
+    int rc;
+    if (ctx->D == 3) {
+      if (c == 1) rc = launch_gsrb_rb_tma<3, false, 8, 1>(ctx, rec, n, phi, rhs, rb, lam, g);
+      else if (c == 2) rc = launch_gsrb_rb_tma<3, false, 8, 2>(ctx, rec, n, phi, rhs, rb, lam, g);
+      else rc = launch_gsrb_rb_tma<3, false, 8, 4>(ctx, rec, n, phi, rhs, rb, lam, g);
+    } else if (ctx->coord == AFG_CYL) {
+      if (c == 1) rc = launch_gsrb_rb_tma<2, true, 16, 1>(ctx, rec, n, phi, rhs, rb, lam, g);
+      else if (c == 2) rc = launch_gsrb_rb_tma<2, true, 16, 2>(ctx, rec, n, phi, rhs, rb, lam, g);
+      else rc = launch_gsrb_rb_tma<2, true, 16, 4>(ctx, rec, n, phi, rhs, rb, lam, g);
+    } else {
+      if (c == 1) rc = launch_gsrb_rb_tma<2, false, 16, 1>(ctx, rec, n, phi, rhs, rb, lam, g);
+      else if (c == 2) rc = launch_gsrb_rb_tma<2, false, 16, 2>(ctx, rec, n, phi, rhs, rb, lam, g);
+      else rc = launch_gsrb_rb_tma<2, false, 16, 4>(ctx, rec, n, phi, rhs, rb, lam, g);
+    }
+    RC(rc);
+    CKL();
+    return AFG_OK;
+  }
+  const int sh = (ctx->D == 2 ? ctx->nc * ctx->nc : ctx->nc * ctx->nc * ctx->nc) / 2;
+  const int threads = std::max(32, std::min(256, sh));
+  if (ctx->D == 3)
+    AFG_NC3(NCV_, k_gsrb_rb<3, false, NCV_><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g));
+  else if (ctx->coord == AFG_CYL)
+    AFG_NC2(NCV_, k_gsrb_rb<2, true, NCV_><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g));
+  else
+    AFG_NC2(NCV_, k_gsrb_rb<2, false, NCV_><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, rec, phi, rhs, rb, lam, g));
+  CKL();
+  return AFG_OK;
+}
+
 template <typename T>
 static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, ModeArg<const T> rhs, int rb,
                              ModeCoef<T> lam, const GcDev& g) {
@@ -447,6 +534,16 @@ static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, ModeArg<T> ph
   KTree t = ktree(ctx);
   const int threads = ctx->D == 2 ? std::min(256, ctx->nc * ctx->nc / 2) : std::min(256, ctx->nc * ctx->nc * ctx->nc / 2);
   kt_begin(ctx, AFG_KT_GSRB);
+  if constexpr (std::is_same<T, float>::value) {
+    if (ctx->rb32) {
+      // untuned: the staged kernel with 2 cells per thread
+      const int code = ctx->gsrb_cpt[2] == 0 ? (kGsrbTma | 2) : ctx->gsrb_cpt[2];
+      RC(launch_gsrb_rb(ctx, rec_of(ctx, list), n, phi, rhs, rb, lam, g, code));
+      kt_end(ctx, AFG_KT_GSRB, 1.5 * sizeof(T) * n * ctx->ky * box_cells(ctx));
+      ctx->launches++;
+      return AFG_OK;
+    }
+  }
   // the usual box sizes: several cells per thread (tuned), box records
   if (gsrb_rec_specialized(ctx)) {
     const int rc = launch_gsrb_rec<T>(ctx, rec_of(ctx, list), n, phi, rhs, rb, lam, g, gsrb_cpt_of<T>(ctx));
@@ -469,6 +566,7 @@ template <typename T>
 static int launch_residual(afg_ctx* ctx, const int* list, int n, const T* phi, const T* rhs, T* tmp, MgCoef<T> lam,
                            unsigned long long* maxbits) {
   if (n <= 0) return AFG_OK;
+  if (rb_of<T>(ctx)) return fail(ctx, AFG_ERR_STATE, "no residual kernel on the compact FP32 layout");
   KTree t = ktree(ctx);
   if (ctx->D == 3)
     AFG_NC3(NCV_, k_residual<3, false, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, phi, rhs, tmp, lam, ctx->d_is_leaf, maxbits));
@@ -488,6 +586,20 @@ static int launch_rrestrict(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi
   KTree t = ktree(ctx);
   const int hnc = ctx->nc / 2;
   const int threads = std::max(32, std::min(256, ctx->D == 2 ? hnc * hnc : hnc * hnc * hnc));
+  if constexpr (std::is_same<T, float>::value) {
+    if (ctx->rb32) {
+      if (store_child || !otf) return fail(ctx, AFG_ERR_STATE, "compact FP32 restriction: face neighbours on the fly only");
+      if (ctx->D == 3)
+        AFG_NC3(NCV_, k_residual_restrict_rb<3, false, NCV_><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, g));
+      else if (ctx->coord == AFG_CYL)
+        AFG_NC2(NCV_, k_residual_restrict_rb<2, true, NCV_><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, g));
+      else
+        AFG_NC2(NCV_, k_residual_restrict_rb<2, false, NCV_><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, g));
+      ctx->launches++;
+      CKL();
+      return AFG_OK;
+    }
+  }
   if (ctx->D == 3)
     AFG_NC3(NCV_, k_residual_restrict<3, false, T, NCV_><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, store_child, g, otf));
   else if (ctx->coord == AFG_CYL)
@@ -504,6 +616,20 @@ static int launch_coarse_fas(afg_ctx* ctx, const int* list, int n, ModeArg<T> ph
                              ModeCoef<T> lam, int copy_tmp, int fill, const GcDev& g) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
+  if constexpr (std::is_same<T, float>::value) {
+    if (ctx->rb32) {
+      if (!copy_tmp || !fill) return fail(ctx, AFG_ERR_STATE, "compact FP32 FAS update: fill and copy only");
+      if (ctx->D == 3)
+        AFG_NC3(NCV_, k_coarse_fas_rb<3, false, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, g));
+      else if (ctx->coord == AFG_CYL)
+        AFG_NC2(NCV_, k_coarse_fas_rb<2, true, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, g));
+      else
+        AFG_NC2(NCV_, k_coarse_fas_rb<2, false, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, g));
+      ctx->launches++;
+      CKL();
+      return AFG_OK;
+    }
+  }
   if (ctx->D == 3)
     AFG_NC3(NCV_, k_coarse_fas<3, false, T, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, copy_tmp, fill, g));
   else if (ctx->coord == AFG_CYL)
@@ -520,6 +646,17 @@ static int launch_correct(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, 
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   const size_t sm = sizeof(T) * ctx->S;
+  if constexpr (std::is_same<T, float>::value) {
+    if (ctx->rb32) {
+      if (ctx->D == 3)
+        AFG_NC3(NCV_, k_correct_rb<3, NCV_><<<dim3(n, ctx->ky), 256, sm, ctx->stream>>>(t, list, phi, tmp));
+      else
+        AFG_NC2(NCV_, k_correct_rb<2, NCV_><<<dim3(n, ctx->ky), 256, sm, ctx->stream>>>(t, list, phi, tmp));
+      ctx->launches++;
+      CKL();
+      return AFG_OK;
+    }
+  }
   if (ctx->D == 3)
     AFG_NC3(NCV_, k_correct<3, T, NCV_><<<dim3(n, ctx->ky), 256, sm, ctx->stream>>>(t, list, phi, tmp));
   else
@@ -533,6 +670,19 @@ template <typename T>
 static int launch_init_phi_rhs(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, ModeArg<T> rhs) {
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
+  if constexpr (std::is_same<T, float>::value) {
+    if (ctx->rb32) {
+      if (ctx->D == 3)
+        AFG_NC3(NCV_, k_init_phi_rhs_rb<3, false, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, list, phi, rhs));
+      else if (ctx->coord == AFG_CYL)
+        AFG_NC2(NCV_, k_init_phi_rhs_rb<2, true, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, list, phi, rhs));
+      else
+        AFG_NC2(NCV_, k_init_phi_rhs_rb<2, false, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, list, phi, rhs));
+      ctx->launches++;
+      CKL();
+      return AFG_OK;
+    }
+  }
   if (ctx->D == 3)
     AFG_NC3(NCV_, k_init_phi_rhs<3, false, T, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, list, phi, rhs));
   else if (ctx->coord == AFG_CYL)
@@ -547,6 +697,14 @@ static int launch_init_phi_rhs(afg_ctx* ctx, const int* list, int n, ModeArg<T> 
 template <typename T>
 static int launch_copy(afg_ctx* ctx, const int* list, int n, ModeArg<const T> src, ModeArg<T> dst) {
   if (n <= 0) return AFG_OK;
+  if constexpr (std::is_same<T, float>::value) {
+    if (ctx->rb32) {
+      k_copy_rb<<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(ktree(ctx), list, src, dst);
+      ctx->launches++;
+      CKL();
+      return AFG_OK;
+    }
+  }
   k_copy<T><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(ktree(ctx), list, src, dst);
   ctx->launches++;
   CKL();
@@ -566,11 +724,6 @@ static int launch_maxabs(afg_ctx* ctx, const int* list, int n, const T* v, unsig
   return AFG_OK;
 }
 
-#define RC(x)                 \
-  do {                        \
-    int rc_ = (x);            \
-    if (rc_ != AFG_OK) return rc_; \
-  } while (0)
 
 // Run a fixed launch sequence through a cached CUDA graph: captured on first
 // use, replayed afterwards (one launch instead of hundreds).  The body must
@@ -738,14 +891,17 @@ static int mg_coarse_solve(afg_ctx* ctx, MgSlot& m, ModeArg<T> phi, ModeArg<cons
   ModeArg<const double> ainv(m.d_ainv);
   for (int k = 1; k < ctx->ky; k++) ainv.p[k] = ctx->grp[k]->d_ainv;
   const dim3 g128((n + 127) / 128, ctx->ky), g8((n + 7) / 8, ctx->ky);
-  k_coarse_gather<T><<<g128, 128, 0, ctx->stream>>>(n, nloc, ctx->D, ctx->d_cslot, ctx->d_ccell, m.d_b2r, m.d_bmask,
-                                                    bcv, stride, rhs, ctx->S, b);
+  const bool rbl = rb_of<T>(ctx);
+  const int* ccell = rbl ? ctx->d_ccell_rb : ctx->d_ccell;
+  const int cstride = rbl ? (int)ktree(ctx).SI : ctx->S;
+  k_coarse_gather<T><<<g128, 128, 0, ctx->stream>>>(n, nloc, ctx->D, ctx->d_cslot, ccell, m.d_b2r, m.d_bmask,
+                                                    bcv, stride, rhs, cstride, b);
   ctx->launches++;
   CKL();
   k_coarse_matvec<<<g8, 256, 0, ctx->stream>>>(n, nloc, ainv, ModeArg<const double>(b), x);
   ctx->launches++;
   CKL();
-  k_coarse_scatter<T><<<g128, 128, 0, ctx->stream>>>(ktree(ctx), n, ctx->d_cslot, ctx->d_ccell,
+  k_coarse_scatter<T><<<g128, 128, 0, ctx->stream>>>(ktree(ctx), n, ctx->d_cslot, ccell, cstride,
                                                      ModeArg<const double>(x), phi);
   ctx->launches++;
   CKL();
@@ -900,6 +1056,50 @@ static int reset_max(afg_ctx* ctx, int slot) {
   return AFG_OK;
 }
 
+// Autotuner of the compact-layout FP32 smoother: the staged kernel with 1, 2
+// or 4 cells per thread and the one-box-per-CTA kernel, timed like the
+// ghosted-layout variants below on the level with the most boxes.
+static int autotune_gsrb_rb(afg_ctx* ctx, MgSlot& m) {
+  int best_l = 0;
+  for (int l = 0; l < ctx->highest_lvl; l++)
+    if (ctx->lvl_ids[l].size() > ctx->lvl_ids[best_l].size()) best_l = l;
+  const int n = (int)ctx->lvl_ids[best_l].size();
+  if (n < 256) return AFG_OK;  // too small to time; the default stays
+  const int* rec = rec_of(ctx, lst(ctx, ctx->off_ids[best_l]));
+  const GcDev g = mg_gc(ctx, m, true);
+  const int cands[] = {kGsrbTma | 1, kGsrbTma | 2, kGsrbTma | 4, -1};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int best_c = kGsrbTma | 2;
+  int rc = AFG_OK;
+  for (int q = 0; q < 4 && rc == AFG_OK; q++) {
+    float tmin = 1e30f;
+    for (int r = 0; r < 8 && rc == AFG_OK; r++) {
+      cudaEventRecord(e0, ctx->stream);
+      rc = launch_gsrb_rb(ctx, rec, n, m.e32, m.r32, 1 + (r & 1), coef_of<float>(m), g, cands[q]);
+      cudaEventRecord(e1, ctx->stream);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (r > 0) tmin = std::min(tmin, ms);
+    }
+    if (tmin < best) {
+      best = tmin;
+      best_c = cands[q];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  RC(rc);
+  ctx->gsrb_cpt[2] = best_c;
+  const size_t N = (size_t)ctx->n_boxes * (ktree(ctx).SI + ctx->S);
+  CK(cudaMemsetAsync(m.e32, 0, N * sizeof(float), ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return AFG_OK;
+}
+
 // Autotuner of the smoother's work shape: on the level with the most boxes,
 // time every cells-per-thread variant of the FP32 half sweep (CUDA events,
 // best of 7 after a warm-up) on the slot's FP32 buffers, which are scratch
@@ -907,6 +1107,7 @@ static int reset_max(afg_ctx* ctx, int slot) {
 // arithmetic, so the choice changes speed only.
 static int autotune_gsrb(afg_ctx* ctx, MgSlot& m) {
   if (!gsrb_rec_specialized(ctx) || !m.e32) return AFG_OK;
+  if (ctx->rb32) return autotune_gsrb_rb(ctx, m);
   int best_l = 0;
   for (int l = 0; l < ctx->highest_lvl; l++)
     if (ctx->lvl_ids[l].size() > ctx->lvl_ids[best_l].size()) best_l = l;
@@ -1032,10 +1233,7 @@ static int mixed_iter_graph(afg_ctx* ctx, MgSlot& m) {
   RC(run_graph(ctx, gkey("mixed_iter", mg_id), [&]() -> int {
     RC(mg_vcycle<float>(ctx, m, ctx->highest_lvl, m.e32, m.r32, m.t32, false, true, nullptr));
     // leaves only: mixed_prepare restricts the parents from them
-    k_add_correction<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), lst(ctx, ctx->off_all_leaves), phi,
-                                                                m.e32);
-    ctx->launches++;
-    CKL();
+    RC(launch_add_correction(ctx, lst(ctx, ctx->off_all_leaves), ctx->n_all_leaves, phi, m.e32));
     RC(mixed_prepare(ctx, m, phi));
     RC(reset_max(ctx, 2));
     return launch_defect(ctx, m, phi, rhs, ctx->d_max + 2);
@@ -1461,6 +1659,19 @@ int afg_tree_sync_batched(afg_ctx* ctx, const afg_tree_desc* t, int n_var_cell, 
   CK(cudaMemcpy(ctx->d_is_leaf, is_leaf.data(), n, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_cslot, cslot.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_ccell, ccell.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
+  {
+    // the coarse unknowns' cells in the compact FP32 layout (interior block)
+    std::vector<int> crb(ncoarse);
+    const int n2c = nc + 2, hn = nc / 2, sh = (D == 2 ? nc * nc : nc * nc * nc) / 2;
+    for (long g = 0; g < ncoarse; g++) {
+      const int x = ccell[g], i = x % n2c, r = x / n2c;
+      const int j = D == 2 ? r : r % n2c, k = D == 2 ? 0 : r / n2c;
+      const int row = D == 2 ? j - 1 : (k - 1) * nc + (j - 1);
+      crb[g] = (((i + j + k) & 1) ? sh : 0) + row * hn + ((i - 1) >> 1);
+    }
+    CK(dalloc(&ctx->d_ccell_rb, ncoarse));
+    CK(cudaMemcpy(ctx->d_ccell_rb, crb.data(), sizeof(int) * ncoarse, cudaMemcpyHostToDevice));
+  }
   // per-instance tables: depth, finest dr (af_min_dr), cells per level
   ctx->inst_hl.assign(rows, 0);
   ctx->inst_min_dr.assign(rows, 0.0);
@@ -2020,13 +2231,14 @@ int afg_mg_setup(afg_ctx* ctx, int mg_id, const afg_mg_desc* d) {
     CK(cudaStreamSynchronize(ctx->stream));
   }
   if (d->precision == AFG_MIXED) {
-    const size_t N = (size_t)ctx->n_boxes * ctx->S;
+    // room for either FP32 layout: interior blocks plus ghost blocks
+    const size_t N = (size_t)ctx->n_boxes * (ktree(ctx).SI + ctx->S);
     if (dalloc(&m.e32, N) != cudaSuccess || dalloc(&m.r32, N) != cudaSuccess || dalloc(&m.t32, N) != cudaSuccess)
       return fail(ctx, AFG_ERR_NOMEM, "cannot allocate FP32 pools");
     CK(cudaMemset(m.e32, 0, N * sizeof(float)));
     CK(cudaMemset(m.r32, 0, N * sizeof(float)));
     CK(cudaMemset(m.t32, 0, N * sizeof(float)));
-    if (ctx->gsrb_cpt[0] == 0) RC(autotune_gsrb(ctx, m));
+    if (ctx->gsrb_cpt[ctx->rb32 ? 2 : 0] == 0) RC(autotune_gsrb(ctx, m));
   }
   m.used = true;
   // mg_init: phi gets the multigrid ghost-cell methods
@@ -2220,21 +2432,35 @@ int afg_set_tuning(afg_ctx* ctx, const int* in) {
   if (!ctx->have_tree) return fail(ctx, AFG_ERR_STATE, "no tree");
   const int S = kGsrbTma, R = kGsrbTma | kGsrbTmaRhs;
   const int ok3[] = {0, 1, 2, 4, 8, S | 2, S | 4, R | 2, R | 4}, ok2[] = {0, 1, 2, 4, S | 1, S | 2, R | 1, R | 2};
-  for (int k = 0; k < 2; k++) {
+  for (int k = ctx->rb32 ? 1 : 0; k < 2; k++) {
     bool ok = false;
     for (int v : (ctx->D == 3 ? std::vector<int>(ok3, ok3 + 9) : std::vector<int>(ok2, ok2 + 8))) ok = ok || in[k] == v;
     if (!ok) return fail(ctx, AFG_ERR_ARG, "bad smoother variant %d", in[k]);
   }
   clear_graphs(ctx);  // launch shapes are part of captured graphs
-  ctx->gsrb_cpt[0] = in[0];
+  if (ctx->rb32) {
+    const int T = kGsrbTma;
+    if (in[0] != 0 && in[0] != (T | 1) && in[0] != (T | 2) && in[0] != (T | 4))
+      return fail(ctx, AFG_ERR_ARG, "bad compact-layout smoother variant %d", in[0]);
+    ctx->gsrb_cpt[2] = in[0] == 0 ? -1 : in[0];  // -1: the one-box-per-CTA kernel, kept by the autotuner
+  } else {
+    ctx->gsrb_cpt[0] = in[0];
+  }
   ctx->gsrb_cpt[1] = in[1];
+  return AFG_OK;
+}
+
+int afg_set_fp32_layout(afg_ctx* ctx, int compact) {
+  if (!ctx) return AFG_ERR_ARG;
+  clear_graphs(ctx);
+  ctx->rb32 = compact != 0;
   return AFG_OK;
 }
 
 int afg_tuning(const afg_ctx* ctx, int* out) {
   if (!ctx || !out) return AFG_ERR_ARG;
   const bool sp = gsrb_rec_specialized(ctx);
-  out[0] = sp ? gsrb_cpt_of<float>(ctx) : 0;
+  out[0] = sp ? (ctx->rb32 ? std::max(0, ctx->gsrb_cpt[2]) : gsrb_cpt_of<float>(ctx)) : 0;
   out[1] = sp ? gsrb_cpt_of<double>(ctx) : 0;
   return AFG_OK;
 }

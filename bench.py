@@ -28,14 +28,19 @@ uploads the species densities, advances, and downloads the densities and
 final field solve, which does not write them).
 
 `--impl reference` and `cpu_baseline` time the CPU restatement of the same
-step (C++/OpenMP on all host cores) on a bounded sample: for ``3d`` the same
-tree construction two levels coarser (4,361 boxes, ~2.2 M cells).
+step (C++/OpenMP on all host cores) on the same tree when the host has the
+memory for it (the 3D tree needs ~55 GB on the host), otherwise on the same
+construction two levels coarser, stated in `config.workload`.
+`error_mixed_vs_fp64` compares the two GPU paths after the same steps from
+the same initial state: relative maximum over leaf cells of |mixed - FP64|
+divided by the FP64 path's maximum, for phi, |E| and every species.
 """
 import argparse
 import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -62,13 +67,6 @@ CONFIG_TEXT = {
              "grids with sides drawn from {64,128,256,512}, voltages 15-35 kV, seed amplitudes 1e13-1e16), "
              "one forest in one context, 3 species, Heun dt=5e-12 s, Poisson to 1e-8 rel. per instance",
 }
-# DRAM traffic of a kernel class relative to its algorithmic bytes, from the
-# ncu capture of every launch of one step of the same workload
-# (dram__bytes_read.sum + dram__bytes_write.sum; profiles/
-# dram_per_kernel_streamer_steps.md).  The FP32 smoother (staged variant):
-# 3D 82.71 GB over the step's 5 V-cycles against 27.17 GB algorithmic (1.5
-# FP32 words per cell and half sweep); batch 14.47 GB against 7.43 GB.
-NCU_TRAFFIC_RATIO = {("3d", "gsrb"): 82.71 / 27.17, ("batch", "gsrb"): 14.47 / 7.43}
 
 
 class Clocks:
@@ -76,9 +74,9 @@ class Clocks:
 
     def __init__(self, index):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        fd, self.path = tempfile.mkstemp(prefix="afg_clocks_", suffix=".csv")
+        os.close(fd)
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(index), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
@@ -112,6 +110,10 @@ class Clocks:
             for n, v in zip(names, p[4:8]):
                 if v.lower() == "active":
                     reasons.add(n)
+        try:
+            os.unlink(self.path)
+        except OSError:
+            pass
         if not sm_mhz:
             return None
         return {"sm_mhz": float(np.median(sm_mhz)), "sm_max_mhz": sm_max, "reasons": sorted(reasons),
@@ -163,7 +165,7 @@ def run_poisson3d(args, device, config):
     tree = w.tree(coarsen=args.coarsen)
     model = w.model()
     H, ivs = w.initial_host_state(tree, model)
-    ctx = ag.Context(device)
+    ctx = new_context(args, device)
     K = max(3, args.steps)
     lam, coeffs, coeff = w.photoi_lambda, w.photoi_coeffs, w.photoi_eta_quench
     out, fields = {}, {}
@@ -239,7 +241,7 @@ def run_one_at_a_time(args, device, w, trees, model, H, ivs):
     offs = np.cumsum([0] + [t.n_boxes for t in trees])
     t_ms, work = 0.0, 0
     for q, t in enumerate(trees):
-        ctx = ag.Context(device)
+        ctx = new_context(args, device)
         ctx.tree_sync(t, model.n_var_cell, model.n_var_face)
         ctx.upload_vars(H[offs[q]:offs[q + 1]], ivs)
         run = sm.StreamerRun(ctx, t, model, float(w.voltages[q]), w.dt, precision=ag.MIXED, **w.run_kwargs())
@@ -260,11 +262,39 @@ def run_one_at_a_time(args, device, w, trees, model, H, ivs):
                 instances=len(trees))
 
 
+def leaf_snapshot(ctx, tree, ivs):
+    """Leaf-cell interiors of the variables ivs on the device: {iv: array}."""
+    nc, D = tree.n_cell, tree.ndim
+    leaves = np.concatenate(tree.lvl_leaves).astype(np.int64) - 1
+    inner = (slice(None),) + (slice(1, nc + 1),) * D
+    h = ag.new_cc(tree, 1)
+    out = {}
+    for iv in ivs:
+        ctx.download_vars(h, [iv])
+        out[iv] = np.ascontiguousarray(h[leaves, 0][inner])
+    return out
+
+
+def snapshot_vars(model):
+    """(name, variable) pairs compared between the two GPU paths."""
+    out = [("phi", model.i_phi), ("E", model.i_electric_fld)]
+    out += [(sp.name, model.species_iv[s]) for s, sp in enumerate(model.species)]
+    return out
+
+
+def new_context(args, device):
+    ctx = ag.Context(device)
+    ctx.set_fp32_layout(getattr(args, "fp32_layout", "compact") == "compact")
+    return ctx
+
+
 def run_gpu_arm(args, device, w):
     tree, model, H, ivs, voltage, box_inst, trees = problem(args, w)
-    ctx = ag.Context(device)
+    ctx = new_context(args, device)
     results = {}
     arms = (("mixed", ag.MIXED),) if args.profile else (("fp64", ag.FP64), ("mixed", ag.MIXED))
+    svars = snapshot_vars(model)
+    snap64, accuracy = None, None
     for prec_name, prec in arms:
         ctx.tree_sync(tree, model.n_var_cell, model.n_var_face, box_inst=box_inst)     # zeroed pools
         ctx.upload_vars(H, ivs)
@@ -311,10 +341,25 @@ def run_gpu_arm(args, device, w):
         ctx.event_record(3)
         res["vcycle_ms"] = ctx.event_elapsed(2, 3) / max(1, n)
         results[prec_name] = (res, run)
+        # the state after the same steps from the same initial state
+        if not args.profile:
+            if prec_name == "fp64":
+                snap64 = leaf_snapshot(ctx, tree, [iv for _, iv in svars])
+            else:
+                accuracy = {}
+                for name, iv in svars:
+                    b = snap64.pop(iv)
+                    a = leaf_snapshot(ctx, tree, [iv])[iv]
+                    accuracy[name] = float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+                    del a, b
+                accuracy = {"rel_max_over_leaves": accuracy,
+                            "after": f"the initial field solve, {args.warmup} warm-up and {args.steps} timed steps "
+                                     f"and one more field solve, from the same initial state",
+                            "field_target": 1e-6}
     if args.profile:
         tuning = ctx.tuning()
         ctx.close()
-        return tree, results, {}, None, tuning
+        return tree, results, {}, None, tuning, None
     tuning = ctx.tuning()
     # per-kernel-class device time during one mixed step (graphs off while timing)
     run = results["mixed"][1]
@@ -391,26 +436,74 @@ def run_gpu_arm(args, device, w):
         e2e["one_at_a_time"] = one
     if amr is not None:
         e2e["amr"] = amr
-    return tree, results, kstats, e2e, tuning
+    return tree, results, kstats, e2e, tuning, accuracy
+
+
+def host_mem_available():
+    """Bytes of host memory this process can still use (MemAvailable, capped
+    by a cgroup v2 limit), or None if unknown."""
+    avail = None
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    avail = int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    try:
+        with open("/sys/fs/cgroup/memory.max") as f:
+            lim = f.read().strip()
+        with open("/sys/fs/cgroup/memory.current") as f:
+            cur = int(f.read())
+        if lim != "max":
+            left = int(lim) - cur
+            avail = left if avail is None else min(avail, left)
+    except (OSError, ValueError):
+        pass
+    return avail
+
+
+def cpu_state_bytes(tree, model):
+    """Host bytes the CPU restatement holds for a tree: cell and face pools
+    plus the initial-state array, with a quarter in reserve."""
+    S = (tree.n_cell + 2) ** tree.ndim
+    NF = (tree.n_cell + 1) ** tree.ndim
+    cc = tree.n_boxes * model.n_var_cell * S * 8
+    fc = tree.n_boxes * model.n_var_face * tree.ndim * NF * 8
+    H = tree.n_boxes * (1 + len(model.species)) * S * 8
+    return int(1.25 * (cc + fc) + H)
+
+
+def cpu_tree(name, w, model):
+    """The tree the CPU restatement runs: the workload's own when the host
+    has the memory, else (3d) the same construction two levels coarser.
+    Returns (tree, reduced)."""
+    tree = w.tree()
+    if name != "3d":
+        return tree, False
+    avail = host_mem_available()
+    if avail is None or avail > cpu_state_bytes(tree, model):
+        return tree, False
+    del tree
+    return w.tree(reduced=True), True
 
 
 def run_cpu(name, steps, warmup=1, time_limit=None):
-    """The CPU restatement of the step (oracle) on all host cores; for the 3D
-    workload on the reduced tree.  Returns (cell-updates/s, cores, s/step,
-    steps timed, sample text)."""
+    """The CPU restatement of the step (oracle) on all host cores, on the
+    workload's tree (cpu_tree).  Returns (cell-updates/s, cores, s/step,
+    steps timed, sample text, reduced)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from oracle_streamer import OracleStreamerRun
     cores = os.cpu_count() or 1
     oracle.set_num_threads(cores)
     if name == "batch":
-        return run_cpu_batch(steps, warmup, time_limit, cores)
+        return run_cpu_batch(steps, warmup, time_limit, cores) + (False,)
     w = workloads.WORKLOADS[name]()
     if name == "poisson3d":
-        return run_cpu_poisson3d(w, steps, warmup, time_limit, cores)
-    reduced = name == "3d"
-    tree = w.tree(reduced=reduced)
+        return run_cpu_poisson3d(w, steps, warmup, time_limit, cores) + (True,)
     model = w.model()
+    tree, reduced = cpu_tree(name, w, model)
     cc = ag.new_cc(tree, model.n_var_cell)
     fc = ag.new_fc(tree, model.n_var_face)
     H, ivs = initial_host_state(w, tree, model)
@@ -430,11 +523,11 @@ def run_cpu(name, steps, warmup=1, time_limit=None):
             break
     dt = time.perf_counter() - t0
     ncells = tree.n_boxes * tree.n_cell ** tree.ndim
+    coarser = ", the same construction two levels coarser: the host lacks the memory for the full tree"
     sample = (f"{done} step(s) after {warmup} warm-up step(s) of the {'reduced ' if reduced else ''}{name} tree "
-              f"({tree.n_boxes} boxes, {ncells / 1e6:.2f} M cells"
-              f"{', the same construction two levels coarser' if reduced else ''}) on the CPU restatement "
-              f"(C++/OpenMP, {cores} threads)")
-    return work / dt, cores, dt / done, done, sample
+              f"({tree.n_boxes} boxes, {ncells / 1e6:.2f} M cells{coarser if reduced else ''}"
+              f") on the CPU restatement (C++/OpenMP, {cores} threads)")
+    return work / dt, cores, dt / done, done, sample, reduced
 
 
 def run_cpu_poisson3d(w, steps, warmup, time_limit, cores):
@@ -521,6 +614,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU baseline time bound")
     ap.add_argument("--coarsen", type=int, default=0,
                     help="3d only: the same tree construction this many levels coarser (smaller profiling cases)")
+    ap.add_argument("--fp32-layout", default="compact", choices=["compact", "ghosted"],
+                    help="layout of the FP32 correction buffers of the mixed solves")
     ap.add_argument("--profile", action="store_true",
                     help="mixed arm only, timed steps bracketed by cudaProfilerStart/Stop; no e2e or CPU baseline")
     args = ap.parse_args()
@@ -529,13 +624,17 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     config = {"workload": CONFIG_TEXT[args.config] if args.coarsen == 0 else
               f"{CONFIG_TEXT[args.config]} -- coarsened by {args.coarsen} level(s)", "name": args.config,
+              "fp32_layout": args.fp32_layout,
               "l2": "flushed between timed steps (256 MiB write)",
               "parallelism": "replicas" if world > 1 else "1 GPU"}
     if args.impl == "reference":
         if rank != 0:
             return
-        warm = max(0, min(1, args.warmup))
-        v, cores, sps, done, sample = run_cpu(args.config, max(1, args.steps), warmup=warm, time_limit=120.0)
+        warm = max(0, args.warmup)
+        v, cores, sps, done, sample, reduced = run_cpu(args.config, max(1, args.steps), warmup=warm,
+                                                       time_limit=300.0)
+        if reduced:
+            config["workload"] = f"{config['workload']} -- CPU sample: {sample}"
         print(json.dumps({
             "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": done, "warmup": warm, "ms_per_step": 1e3 * sps,
@@ -552,7 +651,7 @@ def main():
             run_poisson3d(args, local, config)
         return
     w = workloads.BatchCyl2d() if args.config == "batch" else workloads.WORKLOADS[args.config]()
-    tree, results, kstats, e2e, tuning = run_gpu_arm(args, local, w)
+    tree, results, kstats, e2e, tuning, accuracy = run_gpu_arm(args, local, w)
     one = e2e.pop("one_at_a_time", None) if e2e else None
     amr = e2e.pop("amr", None) if e2e else None
     if args.profile:
@@ -573,15 +672,12 @@ def main():
     dom = max(kstats, key=lambda k: kstats[k]["ms"])
     ks = kstats[dom]
     achieved = ks["bytes"] / (ks["ms"] * 1e-3) / 1e9 if ks["ms"] > 0 else 0.0
-    traffic = None
-    ratio = NCU_TRAFFIC_RATIO.get((args.config, dom))
-    if ratio is not None and ks["launches"]:
-        traffic = ratio * ks["bytes"] / ks["launches"]
     cpu = None
     if rank == 0 and world == 1 and args.cpu_steps > 0:
-        v, cores, sps, done, sample = run_cpu(args.config, args.cpu_steps, warmup=1, time_limit=args.cpu_seconds)
+        v, cores, sps, done, sample, reduced = run_cpu(args.config, args.cpu_steps, warmup=1,
+                                                       time_limit=args.cpu_seconds)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
-               "ms_per_step": 1e3 * sps}
+               "ms_per_step": 1e3 * sps, "same_tree": not reduced}
     if rank == 0:
         keys = ("ms_per_step", "value", "vcycles_per_step", "vcycle_ms", "launches_per_step", "work_per_step",
                 "photoi_step_ms", "plain_step_ms", "step_ms")
@@ -594,10 +690,12 @@ def main():
                 "fp64": {k: fp64[k] for k in keys},
                 "speedup_mixed_vs_fp64": fp64["ms_per_step"] / mixed["ms_per_step"]},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "traffic_note": "DRAM bytes are not measured inside the timed run (no profiler there)",
                          "algorithmic_bytes_per_launch": ks["bytes"] / max(1, ks["launches"]),
                          "avg_launch_us": 1e3 * ks["ms"] / max(1, ks["launches"])},
             "kernel_classes": kstats, "tuning": tuning,
+            **({"error_mixed_vs_fp64": accuracy} if accuracy else {}),
             **({"one_at_a_time": dict(one, speedup_batched=value / one["value"])} if one else {}),
             **({"amr": amr} if amr else {}),
             "cpu_baseline": cpu, "e2e": e2e, "clocks": mixed["clocks"],

@@ -193,8 +193,21 @@ int afg_tuning(const afg_ctx* ctx, int* out);
  * per thread for the shared-memory-staged persistent variant (bulk copies of
  * each box's phi into shared memory, double-buffered; 3D: 18, 20; 2D: 17,
  * 18), plus 32 when the rhs block is staged as well (3D: 50, 52; 2D: 49,
- * 50).  afg_tuning reports the codes the same way. */
+ * 50).  afg_tuning reports the codes the same way.  With the compact FP32
+ * layout (afg_set_fp32_layout, the default) in[0] selects among 0 (one box
+ * per CTA, any box size) and 16 + 1, 2 or 4 cells per thread for the staged
+ * persistent kernel (8^3 and 16^2 boxes). */
 int afg_set_tuning(afg_ctx* ctx, const int* in);
+
+/* Layout of the FP32 correction buffers of AFG_MIXED solves (internal to
+ * the library): compact != 0 (the default) keeps each box's interior cells
+ * in two colour halves of a red-black ordering with the ghost cells apart,
+ * so a half sweep moves one contiguous half per box and operand; 0 keeps
+ * the (nc+2)^D ghosted layout of the FP64 variables.  Both give the same
+ * results bit for bit.  Takes effect for the next solves; call it before
+ * afg_mg_setup so that the autotuner times the chosen layout.  No
+ * counterpart in the reference. */
+int afg_set_fp32_layout(afg_ctx* ctx, int compact);
 
 /* Check of the device-side failure path: a kernel whose bounded mbarrier
  * wait cannot complete (copies announced, none issued) gives up after 1 s,

@@ -241,20 +241,29 @@ def test_smoother_variants_fp64_bitexact(name, gpu_lib):
     ctx.close()
 
 
-@pytest.mark.parametrize("name", ["2d16", "3d8"])
+COMPACT_VARIANTS = [0, ag.GSRB_STAGED | 1, ag.GSRB_STAGED | 2, ag.GSRB_STAGED | 4]
+
+
+@pytest.mark.parametrize("name", ["2d16", "3d8", "2d8cyl", "3d4"])
 def test_smoother_variants_fp32_identical(name, gpu_lib):
-    """The FP32 smoother variants compute the same values: mixed-precision
-    solves with each variant end bit for bit alike."""
+    """The FP32 smoother variants compute the same values, and so do the two
+    layouts of the FP32 correction buffers (ghosted blocks; compact
+    red-black halves with the ghost cells apart): mixed-precision solves
+    with each variant of each layout end bit for bit alike."""
     tree = CASES[name]()
     cyl = tree.coord == ag.AFG_CYL
     phi_ex, rhs, bc = sine_problem(tree, 0.0, cyl)
     cc = ag.new_cc(tree, 3)
     cc[:, I_RHS - 1] = rhs * 1e10
     desc = ag.mg_desc(I_PHI, I_RHS, I_TMP, bc, precision=ag.MIXED)
-    ctx = ag.Context(0)
-    ctx.tree_sync(tree, 3)
+    specialized = (tree.ndim, tree.n_cell) in ((2, 16), (3, 8))
+    runs = [(False, v) for v in (VARIANTS[tree.ndim] if specialized else [0])]
+    runs += [(True, v) for v in (COMPACT_VARIANTS if specialized else [0])]
     ref = None
-    for v in VARIANTS[tree.ndim]:
+    for compact, v in runs:
+        ctx = ag.Context(0)
+        ctx.tree_sync(tree, 3)
+        ctx.set_fp32_layout(compact)
         ctx.mg_setup(0, desc)
         ctx.set_tuning(v, 0)
         ctx.upload(cc)
@@ -262,7 +271,7 @@ def test_smoother_variants_fp32_identical(name, gpu_lib):
         thr = 1e-8 * np.max(np.abs(rhs * 1e10))
         ctx.mg_solve(0, thr, 40)
         out = download(ctx, tree)
+        ctx.close()
         if ref is None:
             ref = out
-        assert np.array_equal(out.view(np.uint64), ref.view(np.uint64)), f"{name} variant {v}"
-    ctx.close()
+        assert np.array_equal(out.view(np.uint64), ref.view(np.uint64)), f"{name} compact={compact} variant {v}"
