@@ -67,10 +67,26 @@ int afg_adjust_refinement(const afg_tree_desc* tr, const int* box_flags, int max
   const int D = tr->ndim, nc = tr->n_cell, n = tr->n_boxes, H = tr->highest_lvl;
   if ((D != 2 && D != 3) || nc < 2 || n < 1 || H < 1) return AFG_ERR_ARG;
   const int nch = 1 << D, nnb = 2 * D, nm = D == 2 ? 9 : 27;
+  if (!tr->lvl || !tr->parent || !tr->children || !tr->neighbors || !tr->ix || !tr->ids || !tr->ids_off ||
+      !tr->leaves || !tr->leaves_off || !tr->parents || !tr->parents_off)
+    return AFG_ERR_ARG;
+  // level-list offsets: non-negative, non-decreasing, within the box count
+  // (every list holds each box at most once)
+  for (const int* off : {tr->ids_off, tr->leaves_off, tr->parents_off}) {
+    if (off[0] < 0) return AFG_ERR_ARG;
+    for (int l = 1; l <= H; l++)
+      if (off[l] < off[l - 1] || off[l] > n) return AFG_ERR_ARG;
+  }
+  // box flags as afivo knows them: remove, keep or refine (af_rm_ref ..
+  // af_do_ref); af_adjust_refinement stops on others (m_af_core.f90:993-994)
+  for (int b = 0; b < n; b++)
+    if (box_flags[b] < kRmRef || box_flags[b] > kDoRef) return AFG_ERR_ARG;
   std::vector<int64_t> f(box_flags, box_flags + n);
   std::vector<char> has_ch(n, 0);
   for (int b = 0; b < n; b++) {
     if (tr->lvl[b] < 1 || tr->lvl[b] > H || tr->parent[b] < 0 || tr->parent[b] > n) return AFG_ERR_ARG;
+    for (int d = 0; d < D; d++)
+      if (tr->ix[(size_t)b * D + d] < 1) return AFG_ERR_ARG;
     for (int c = 0; c < nch; c++) {
       const int ch = tr->children[(size_t)b * nch + c];
       if (ch < 0 || ch > n) return AFG_ERR_ARG;

@@ -62,3 +62,33 @@ def test_native_rejects_bad_arguments(lib):
     tree = at.uniform_tree(2, 8, [16, 16], [1e-2, 1e-2], 2)
     with pytest.raises(ag.AfgError):
         ag.adjust_refinement(tree, np.zeros(tree.n_boxes, np.int32), 0)
+
+
+def test_native_rejects_corrupted_descriptor(lib):
+    """Level-list offsets that decrease or overrun the box count, box
+    indices below 1 and box flags outside remove/keep/refine are argument
+    errors, found before any table is indexed."""
+    import ctypes as C
+    tree = at.uniform_tree(2, 8, [16, 16], [1e-2, 1e-2], 3)
+    flags = np.zeros(tree.n_boxes, np.int32)
+    L = ag.load_library()
+
+    def call(mutate, f=flags):
+        holder = ag.TreeDescHolder(tree)
+        mutate(holder)
+        out = C.c_void_p()
+        fl = np.ascontiguousarray(f, dtype=np.int32)
+        return L.afg_adjust_refinement(C.byref(holder.desc), fl.ctypes.data_as(C.POINTER(C.c_int)), 5,
+                                       C.byref(out))
+
+    assert call(lambda h: None) == ag.AFG_OK
+    assert call(lambda h: h.arrays["ids_off"].__setitem__(1, tree.n_boxes + 7)) == ag.AFG_ERR_ARG
+    lo = ag.TreeDescHolder(tree).arrays["leaves_off"]
+    assert call(lambda h: h.arrays["leaves_off"].__setitem__(2, lo[3] + 1)) == ag.AFG_ERR_ARG   # decreasing
+    assert call(lambda h: h.arrays["parents_off"].__setitem__(0, -1)) == ag.AFG_ERR_ARG
+    assert call(lambda h: h.arrays["ix"].__setitem__((3, 0), 0)) == ag.AFG_ERR_ARG
+    bad = flags.copy()
+    bad[5] = 7
+    assert call(lambda h: None, bad) == ag.AFG_ERR_ARG
+    bad[5] = -3
+    assert call(lambda h: None, bad) == ag.AFG_ERR_ARG
