@@ -43,6 +43,10 @@ GSRB_STAGED_RHS = 32   # ... with the rhs block staged too
 CYCLE_DOWN = 1
 CYCLE_UP = 3
 KT_NONE, KT_GSRB, KT_GHOST, KT_FLUX, KT_UPDATE, KT_RESIDUAL = 0, 1, 2, 3, 4, 5
+KT_DEFECT, KT_RESTRICT, KT_CORRECT, KT_COARSE, KT_FIELD, KT_COPY, KT_NCLASS, KT_ALL = 6, 7, 8, 9, 10, 11, 12, 15
+KT_NAMES = {KT_GSRB: "gsrb", KT_GHOST: "ghost", KT_FLUX: "flux", KT_UPDATE: "update", KT_RESIDUAL: "residual",
+            KT_DEFECT: "defect", KT_RESTRICT: "restrict", KT_CORRECT: "correct", KT_COARSE: "coarse",
+            KT_FIELD: "field", KT_COPY: "copy"}
 
 _IP = C.POINTER(C.c_int)
 _DP = C.POINTER(C.c_double)
@@ -268,6 +272,7 @@ def load_library(path: str = LIB_PATH):
         "afg_tuning": (C.c_int, [P, _IP]),
         "afg_set_tuning": (C.c_int, [P, _IP]),
         "afg_set_fp32_layout": (C.c_int, [P, C.c_int]),
+        "afg_kernel_stats_all": (C.c_int, [P, C.POINTER(C.c_longlong), _DP, _DP]),
         "afg_set_photoi_lockstep": (C.c_int, [P, C.c_int]),
         "afg_check_bounded_wait": (C.c_int, [P, _DP]),
         "afg_refine_flags": (C.c_int, [P, C.POINTER(RefineDesc), _IP]),
@@ -692,6 +697,14 @@ class Context:
         by = C.c_double(0)
         self.check(self.lib.afg_kernel_stats(self.ptr, C.byref(n), C.byref(ms), C.byref(by)), "afg_kernel_stats")
         return n.value, ms.value, by.value
+
+    def kernel_stats_all(self):
+        """After kernel_timing(KT_ALL): {class name: (launches, ms, bytes)}."""
+        n = (C.c_longlong * KT_NCLASS)()
+        ms = np.zeros(KT_NCLASS)
+        by = np.zeros(KT_NCLASS)
+        self.check(self.lib.afg_kernel_stats_all(self.ptr, n, _dp(ms), _dp(by)), "afg_kernel_stats_all")
+        return {KT_NAMES[c]: (int(n[c]), float(ms[c]), float(by[c])) for c in KT_NAMES if n[c] > 0}
 
     def sync(self):
         self.check(self.lib.afg_sync(self.ptr), "afg_sync")

@@ -157,6 +157,7 @@ __global__ void __launch_bounds__(256) k_add_correction_rb(KTree t0, const int* 
 // phi += e on the boxes of a list (leaves), every lockstep slot
 static int launch_add_correction(afg_ctx* ctx, const int* list, int n, ModeArg<double> phi, ModeArg<const float> e) {
   if (n <= 0) return AFG_OK;
+  KtScope kts(ctx, AFG_KT_CORRECT, 20.0 * n * ctx->ky * ktree(ctx).SI);
   const dim3 grid(n, ctx->ky);
   const KTree t = ktree(ctx);
   if (!ctx->rb32)
@@ -177,6 +178,7 @@ static int launch_defect(afg_ctx* ctx, MgSlot& m, ModeArg<double> phi, ModeArg<c
                          ModeArg<unsigned long long> maxbits) {
   const int n = ctx->n_all;
   if (n <= 0) return AFG_OK;
+  KtScope kts(ctx, AFG_KT_DEFECT, 24.0 * ctx->n_all_leaves * ctx->ky * ktree(ctx).SI);
   KTree t = ktree(ctx);
   const int* list = rec_of(ctx, lst(ctx, ctx->off_all));
   const GcDev g = mg_gc(ctx, m, false);
@@ -218,6 +220,7 @@ static int mixed_prepare(afg_ctx* ctx, MgSlot& m, ModeArg<double> phi) {
     const int n = (int)ctx->lvl_ids[lvl - 1].size();
     if (n == 0) continue;
     const dim3 grid(n, ctx->ky);
+    KtScope kts(ctx, AFG_KT_RESTRICT, 8.0 * n * ctx->ky * ktree(ctx).SI * (1.0 + 1.0 / (1 << ctx->D)));
     if (ctx->D == 3)
       AFG_NC3(NCV_, k_restrict_geom<3, false, NCV_><<<grid, 64, 0, ctx->stream>>>(t, lst(ctx, ctx->off_ids[lvl - 1]), phi));
     else

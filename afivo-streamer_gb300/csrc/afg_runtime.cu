@@ -172,6 +172,8 @@ struct afg_ctx {
   std::vector<cudaEvent_t> kt_ev;  // start/stop pairs
   size_t kt_used = 0;
   double kt_bytes = 0;
+  std::vector<int> kt_cls;         // class of each recorded pair
+  std::vector<double> kt_pbytes;   // algorithmic bytes of each recorded pair
   // CUDA graphs of fixed launch sequences (V-cycle iterations, transport
   // stages), keyed by what determines the sequence; cleared whenever the
   // tree, an operator or boundary values change
@@ -277,8 +279,11 @@ static const int* rec_of(const afg_ctx* c, const int* list) { return c->d_rec + 
 
 // Per-launch timing of one kernel class (afg_kernel_timing): events around
 // each launch of the selected class, algorithmic bytes summed on the host.
+static bool kt_on(const afg_ctx* c, int cls) {
+  return cls != AFG_KT_NONE && (c->kt_class == cls || c->kt_class == AFG_KT_ALL);
+}
 static void kt_begin(afg_ctx* c, int cls) {
-  if (c->kt_class != cls || cls == AFG_KT_NONE) return;
+  if (!kt_on(c, cls)) return;
   if (c->kt_used + 2 > c->kt_ev.size()) {
     if (c->kt_ev.size() >= 40000) return;
     const size_t old = c->kt_ev.size();
@@ -288,12 +293,23 @@ static void kt_begin(afg_ctx* c, int cls) {
   cudaEventRecord(c->kt_ev[c->kt_used], c->stream);
 }
 static void kt_end(afg_ctx* c, int cls, double bytes) {
-  if (c->kt_class != cls || cls == AFG_KT_NONE) return;
+  if (!kt_on(c, cls)) return;
   if (c->kt_used + 2 > c->kt_ev.size()) return;
   cudaEventRecord(c->kt_ev[c->kt_used + 1], c->stream);
   c->kt_used += 2;
   c->kt_bytes += bytes;
+  c->kt_cls.push_back(cls);
+  c->kt_pbytes.push_back(bytes);
 }
+// events around the launches of one helper (a leaf: helpers with a scope do
+// not call each other)
+struct KtScope {
+  afg_ctx* c;
+  int cls;
+  double bytes;
+  KtScope(afg_ctx* c_, int cls_, double bytes_) : c(c_), cls(cls_), bytes(bytes_) { kt_begin(c, cls); }
+  ~KtScope() { kt_end(c, cls, bytes); }
+};
 static double box_cells(const afg_ctx* c) { return c->D == 2 ? (double)c->nc * c->nc : (double)c->nc * c->nc * c->nc; }
 
 static void clear_graphs(afg_ctx* c) {
@@ -566,6 +582,7 @@ template <typename T>
 static int launch_residual(afg_ctx* ctx, const int* list, int n, const T* phi, const T* rhs, T* tmp, MgCoef<T> lam,
                            unsigned long long* maxbits) {
   if (n <= 0) return AFG_OK;
+  KtScope kts(ctx, AFG_KT_RESIDUAL, 3.0 * sizeof(T) * n * box_cells(ctx));
   if (rb_of<T>(ctx)) return fail(ctx, AFG_ERR_STATE, "no residual kernel on the compact FP32 layout");
   KTree t = ktree(ctx);
   if (ctx->D == 3)
@@ -583,6 +600,7 @@ template <typename T>
 static int launch_rrestrict(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, ModeArg<const T> rhs,
                             ModeArg<T> tmp, ModeCoef<T> lam, int store_child, const GcDev& g, int otf) {
   if (n <= 0) return AFG_OK;
+  KtScope kts(ctx, AFG_KT_RESTRICT, sizeof(T) * n * ctx->ky * box_cells(ctx) * (2.0 + 2.0 / (1 << ctx->D)));
   KTree t = ktree(ctx);
   const int hnc = ctx->nc / 2;
   const int threads = std::max(32, std::min(256, ctx->D == 2 ? hnc * hnc : hnc * hnc * hnc));
@@ -615,6 +633,7 @@ template <typename T>
 static int launch_coarse_fas(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, ModeArg<T> rhs, ModeArg<T> tmp,
                              ModeCoef<T> lam, int copy_tmp, int fill, const GcDev& g) {
   if (n <= 0) return AFG_OK;
+  KtScope kts(ctx, AFG_KT_RESTRICT, 4.0 * sizeof(T) * n * ctx->ky * box_cells(ctx));
   KTree t = ktree(ctx);
   if constexpr (std::is_same<T, float>::value) {
     if (ctx->rb32) {
@@ -644,6 +663,7 @@ static int launch_coarse_fas(afg_ctx* ctx, const int* list, int n, ModeArg<T> ph
 template <typename T>
 static int launch_correct(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, ModeArg<T> tmp) {
   if (n <= 0) return AFG_OK;
+  KtScope kts(ctx, AFG_KT_CORRECT, sizeof(T) * n * ctx->ky * box_cells(ctx) * (3.0 + 2.0 * (1 << ctx->D)));
   KTree t = ktree(ctx);
   const size_t sm = sizeof(T) * ctx->S;
   if constexpr (std::is_same<T, float>::value) {
@@ -669,6 +689,7 @@ static int launch_correct(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, 
 template <typename T>
 static int launch_init_phi_rhs(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi, ModeArg<T> rhs) {
   if (n <= 0) return AFG_OK;
+  KtScope kts(ctx, AFG_KT_RESTRICT, 2.0 * sizeof(T) * n * ctx->ky * box_cells(ctx));
   KTree t = ktree(ctx);
   if constexpr (std::is_same<T, float>::value) {
     if (ctx->rb32) {
@@ -697,6 +718,7 @@ static int launch_init_phi_rhs(afg_ctx* ctx, const int* list, int n, ModeArg<T> 
 template <typename T>
 static int launch_copy(afg_ctx* ctx, const int* list, int n, ModeArg<const T> src, ModeArg<T> dst) {
   if (n <= 0) return AFG_OK;
+  KtScope kts(ctx, AFG_KT_COPY, 2.0 * sizeof(T) * n * ctx->ky * box_cells(ctx));
   if constexpr (std::is_same<T, float>::value) {
     if (ctx->rb32) {
       k_copy_rb<<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(ktree(ctx), list, src, dst);
@@ -714,6 +736,7 @@ static int launch_copy(afg_ctx* ctx, const int* list, int n, ModeArg<const T> sr
 template <typename T>
 static int launch_maxabs(afg_ctx* ctx, const int* list, int n, const T* v, unsigned long long* out) {
   if (n <= 0) return AFG_OK;
+  KtScope kts(ctx, AFG_KT_COPY, 1.0 * sizeof(T) * n * box_cells(ctx));
   KTree t = ktree(ctx);
   if (ctx->D == 3)
     AFG_NC3(NCV_, k_maxabs<3, T, NCV_><<<n, 256, 0, ctx->stream>>>(t, list, v, out));
@@ -885,6 +908,8 @@ template <typename T>
 static int mg_coarse_solve(afg_ctx* ctx, MgSlot& m, ModeArg<T> phi, ModeArg<const T> rhs, const GcDev& g,
                            bool homogeneous) {
   const int nloc = m.n_coarse, rows = inst_rows(ctx), n = nloc * rows;
+  {
+  KtScope kts(ctx, AFG_KT_COARSE, 0.0);
   const double* bcv = m.d_bcval + (homogeneous ? 6 * rows : 0);
   const int stride = homogeneous ? 0 : 6;
   const ModeArg<double> b = slot_bufs(ctx, m, &MgSlot::d_b), x = slot_bufs(ctx, m, &MgSlot::d_x);
@@ -905,6 +930,7 @@ static int mg_coarse_solve(afg_ctx* ctx, MgSlot& m, ModeArg<T> phi, ModeArg<cons
                                                      ModeArg<const double>(x), phi);
   ctx->launches++;
   CKL();
+  }
   return mg_gc_lvl<T>(ctx, 1, phi, g, 1);
 }
 
@@ -2414,6 +2440,7 @@ int afg_tree_copy_cc(afg_ctx* ctx, int iv_from, int iv_to) {
   // every box of the tree: one copy of the whole pool (slots of boxes not in
   // use hold no data anyone reads)
   if (iv_from == iv_to) return AFG_OK;
+  KtScope kts(ctx, AFG_KT_COPY, 16.0 * (size_t)ctx->n_boxes * ctx->S);
   CK(cudaMemcpyAsync(ctx->cc[iv_to - 1], ctx->cc[iv_from - 1], sizeof(double) * (size_t)ctx->n_boxes * ctx->S,
                      cudaMemcpyDeviceToDevice, ctx->stream));
   return AFG_OK;
@@ -2499,10 +2526,35 @@ int afg_flush_l2(afg_ctx* ctx, long long bytes) {
 }
 
 int afg_kernel_timing(afg_ctx* ctx, int cls) {
-  if (!ctx || cls < 0 || cls > AFG_KT_RESIDUAL) return AFG_ERR_ARG;
+  if (!ctx || cls < 0 || (cls >= AFG_KT_NCLASS && cls != AFG_KT_ALL)) return AFG_ERR_ARG;
   ctx->kt_class = cls;
   ctx->kt_used = 0;
   ctx->kt_bytes = 0;
+  ctx->kt_cls.clear();
+  ctx->kt_pbytes.clear();
+  return AFG_OK;
+}
+
+int afg_kernel_stats_all(afg_ctx* ctx, long long* launches, double* ms, double* bytes) {
+  if (!ctx || !launches || !ms || !bytes) return AFG_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int c = 0; c < AFG_KT_NCLASS; c++) {
+    launches[c] = 0;
+    ms[c] = 0;
+    bytes[c] = 0;
+  }
+  for (size_t q = 0; q + 1 < ctx->kt_used; q += 2) {
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, ctx->kt_ev[q], ctx->kt_ev[q + 1]));
+    const int c = ctx->kt_cls[q / 2];
+    launches[c]++;
+    ms[c] += t;
+    bytes[c] += ctx->kt_pbytes[q / 2];
+  }
+  ctx->kt_used = 0;
+  ctx->kt_bytes = 0;
+  ctx->kt_cls.clear();
+  ctx->kt_pbytes.clear();
   return AFG_OK;
 }
 
@@ -2520,6 +2572,8 @@ int afg_kernel_stats(afg_ctx* ctx, long long* launches, double* ms, double* byte
   if (bytes) *bytes = ctx->kt_bytes;
   ctx->kt_used = 0;
   ctx->kt_bytes = 0;
+  ctx->kt_cls.clear();
+  ctx->kt_pbytes.clear();
   return AFG_OK;
 }
 

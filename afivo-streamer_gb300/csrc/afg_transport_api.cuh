@@ -230,6 +230,7 @@ int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim) {
     if (ctx->tr.n_rrb > 0) {
       for (int f = 0; f < d.n_flux; f++) {
         double* v = ctx->cc[d.species_iv[d.flux_species[f]] + s_deriv - 1];
+        KtScope kts(ctx, AFG_KT_RESTRICT, 8.0 * ctx->tr.n_rrb * t.SI * (1.0 + 1.0 / (1 << ctx->D)));
         if (ctx->D == 3)
           AFG_NC3(NCV_, k_restrict_geom<3, false, NCV_><<<ctx->tr.n_rrb, 64, 0, ctx->stream>>>(t, ctx->tr.d_rrb, v));
         else if (cyl)
@@ -284,6 +285,7 @@ int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim) {
       CKL();
     }
     if (ctx->tr.n_cflux > 0) {
+      KtScope kts(ctx, AFG_KT_FLUX, 0.0);
       if (ctx->D == 3)
         AFG_NC3(NCV_, k_consistent_flux<3, false, NCV_><<<ctx->tr.n_cflux, 128, 0, ctx->stream>>>(t, ctx->tr.d_cflux, d.n_flux, a));
       else if (cyl)
@@ -438,6 +440,7 @@ static int field_set_rhs(afg_ctx* ctx, int i_rhs, int s_in, unsigned long long* 
   a.rhs = ctx->cc[i_rhs - 1];
   if (ctx->n_all_leaves > 0) {
     const int* list = lst(ctx, ctx->off_all_leaves);
+    KtScope kts(ctx, AFG_KT_FIELD, 8.0 * ctx->n_all_leaves * box_cells(ctx) * (d.n_species + 1));
     if (!mixed_transport(ctx))
       k_field_rhs<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ctx->S, list, a);
     else if (ctx->D == 3)
@@ -460,6 +463,8 @@ int afg_field_from_potential(afg_ctx* ctx, int i_phi) {
   if (!ctx->has_method[d.i_electric_fld - 1])
     return fail(ctx, AFG_ERR_STATE, "no ghost-cell methods for the electric field norm");
   return run_graph(ctx, gkey("efield", i_phi), [&]() -> int {
+    {
+    KtScope kts(ctx, AFG_KT_FIELD, 8.0 * ctx->n_all * box_cells(ctx) * (2.0 + ctx->D));
     if (mixed_transport(ctx)) {
       const int D = ctx->D;
       const size_t smem = sizeof(float) * D * (size_t)ctx->NF;
@@ -475,6 +480,7 @@ int afg_field_from_potential(afg_ctx* ctx, int i_phi) {
       AFG_NC2(NCV_, k_field_grad<2, NCV_><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en));
     ctx->launches++;
     CKL();
+    }
     return afg_gc(ctx, d.i_electric_fld, 0, 1);
   });
 }
@@ -650,6 +656,7 @@ int afg_photoi_helmh(afg_ctx* ctx, double coeff, int n_modes, const int* mg_ids,
     const double* E = ctx->cc[d.i_electric_fld - 1];
     const double* ne = ctx->cc[d.species_iv[d.flux_species[0]] - 1];
     double* rhs = ctx->cc[i_rhs - 1];
+    KtScope kts(ctx, AFG_KT_FIELD, 24.0 * ctx->n_all_leaves * box_cells(ctx));
     if (mixed_transport(ctx)) {
       const float N_inv_td = (float)(kSiToTd / d.gas_number_density);
       const double ch = std::sqrt(std::fabs(coeff));
@@ -786,6 +793,7 @@ int afg_photoi_helmh(afg_ctx* ctx, double coeff, int n_modes, const int* mg_ids,
       if (res / max_rhs < max_rel_residual) break;
     }
     if (ctx->n_all_leaves > 0) {
+      KtScope kts(ctx, AFG_KT_FIELD, 24.0 * ctx->n_all_leaves * box_cells(ctx));
       k_axpy_boxes<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ctx->S, lst(ctx, ctx->off_all_leaves), photo,
                                                               ctx->cc[m->d.i_phi - 1], coeffs[n]);
       ctx->launches++;

@@ -587,9 +587,21 @@ int afg_flush_l2(afg_ctx* ctx, long long bytes);
 #define AFG_KT_GHOST    2  /* ghost-cell fill                       */
 #define AFG_KT_FLUX     3  /* Koren flux                            */
 #define AFG_KT_UPDATE   4  /* density + source update               */
-#define AFG_KT_RESIDUAL 5  /* residual / defect                     */
+#define AFG_KT_RESIDUAL 5  /* residual (FP64 V-cycle)               */
+#define AFG_KT_DEFECT   6  /* FP64 defect of the mixed solves       */
+#define AFG_KT_RESTRICT 7  /* restriction, FAS right-hand side      */
+#define AFG_KT_CORRECT  8  /* prolongation of corrections, phi += e */
+#define AFG_KT_COARSE   9  /* coarse-grid solve                     */
+#define AFG_KT_FIELD   10  /* field rhs, E from phi, photo source   */
+#define AFG_KT_COPY    11  /* whole-variable copies, maxima         */
+#define AFG_KT_NCLASS  12
+#define AFG_KT_ALL     15  /* every class at once (afg_kernel_stats_all) */
 int afg_kernel_timing(afg_ctx* ctx, int kernel_class);
 int afg_kernel_stats(afg_ctx* ctx, long long* launches, double* ms, double* bytes);
+/* With AFG_KT_ALL: per class c < AFG_KT_NCLASS the launches, device time
+ * (ms) and algorithmic bytes recorded since afg_kernel_timing, then resets.
+ * No counterpart in the reference. */
+int afg_kernel_stats_all(afg_ctx* ctx, long long* launches, double* ms, double* bytes);
 
 /* ---- reduction without device allocation -------------------------------
  * No counterpart in the reference.  For callers that may not call
