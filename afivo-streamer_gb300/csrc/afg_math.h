@@ -1,7 +1,8 @@
 // afg_math.h -- exp, log and pow in FP64 written for this project, for the
 // analytic rate forms of the FP64 transport path.  The same code compiles as
 // device code (nvcc) and as host code (g++), and built without floating-point
-// contraction (--fmad=false, -ffp-contract=off) it gives bit-identical
+// contraction (--fmad=false, -ffp-contract=off; the fused multiply-adds are
+// written out, and IEEE fma rounds once everywhere) it gives bit-identical
 // results on the GPU and in the CPU restatement, which the vendor libraries'
 // exp and pow (CUDA's and the C library's) do not.  Accuracy: within two
 // units in the last place of the exact value (tested against 60-digit
@@ -116,6 +117,15 @@ AFG_MATH_HD double floor_d(double x) {
 #endif
 }
 
+// a * b + c rounded once (IEEE fused multiply-add, exact on both sides)
+AFG_MATH_HD double fma_d(double a, double b, double c) {
+#if defined(__CUDA_ARCH__)
+  return fma(a, b, c);
+#else
+  return __builtin_fma(a, b, c);
+#endif
+}
+
 // y 2^m for y in [0.5, 4) and m in [-1076, 1024], one rounding at most
 AFG_MATH_HD double scale(double y, int m) {
   if (m > 1023) return y * pow2i(1023) * pow2i(m - 1023);
@@ -137,12 +147,15 @@ AFG_MATH_HD double exp(double x) {
   const double r1 = x - kd * l1;
   const double r2 = -(kd * l2);
   const double r = r1 + r2;
-  const double q = r * r * (0x1.0000000000000p-1 + r * (0x1.5555555555555p-3 + r * (0x1.5555555555555p-5 +
-                   r * (0x1.1111111111111p-7 + r * 0x1.6c16c16c16c17p-10))));
+  double poly = fma_d(r, 0x1.6c16c16c16c17p-10, 0x1.1111111111111p-7);
+  poly = fma_d(r, poly, 0x1.5555555555555p-5);
+  poly = fma_d(r, poly, 0x1.5555555555555p-3);
+  poly = fma_d(r, poly, 0x1.0000000000000p-1);
+  const double q = (r * r) * poly;
   const double p = r1 + (r2 + q);  // exp(r) - 1
   const double lead = exp2_lead(j), trail = exp2_trail(j);
   const double s = lead + trail;
-  return scale(lead + (trail + s * p), m);
+  return scale(lead + fma_d(s, p, trail), m);
 }
 
 AFG_MATH_HD double log(double x) {
@@ -167,17 +180,17 @@ AFG_MATH_HD double log(double x) {
   const double s = f / (2.0 + f);
   const double z = s * s;
   double poly = 0x1.8618618618618p-5;
-  poly = 0x1.af286bca1af28p-5 + z * poly;
-  poly = 0x1.e1e1e1e1e1e1ep-5 + z * poly;
-  poly = 0x1.1111111111111p-4 + z * poly;
-  poly = 0x1.3b13b13b13b14p-4 + z * poly;
-  poly = 0x1.745d1745d1746p-4 + z * poly;
-  poly = 0x1.c71c71c71c71cp-4 + z * poly;
-  poly = 0x1.2492492492492p-3 + z * poly;
-  poly = 0x1.999999999999ap-3 + z * poly;
-  poly = 0x1.5555555555555p-2 + z * poly;
+  poly = fma_d(z, poly, 0x1.af286bca1af28p-5);
+  poly = fma_d(z, poly, 0x1.e1e1e1e1e1e1ep-5);
+  poly = fma_d(z, poly, 0x1.1111111111111p-4);
+  poly = fma_d(z, poly, 0x1.3b13b13b13b14p-4);
+  poly = fma_d(z, poly, 0x1.745d1745d1746p-4);
+  poly = fma_d(z, poly, 0x1.c71c71c71c71cp-4);
+  poly = fma_d(z, poly, 0x1.2492492492492p-3);
+  poly = fma_d(z, poly, 0x1.999999999999ap-3);
+  poly = fma_d(z, poly, 0x1.5555555555555p-2);
   const double s2 = s + s;
-  const double lm = s2 + s2 * (z * poly);
+  const double lm = fma_d(s2, z * poly, s2);
   if (k == 0) return lm;
   const double kd = (double)k;
   const double ln2_hi = 0x1.62e42fefa3800p-1;  // 42 leading bits of ln2

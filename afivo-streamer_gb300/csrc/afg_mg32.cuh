@@ -155,22 +155,6 @@ __device__ __forceinline__ float nb_val_rb(const KTree& t, const float* __restri
   return face_ghost_rb<D>(t, v, slot, nb, rec_nb(r0, r1, nb), p, q, g);
 }
 
-// apply_lpl_otf on the compact layout (same operation order)
-template <int D, bool CYL>
-__device__ __forceinline__ float apply_lpl_rb(const KTree& t, const float* __restrict__ v, int slot, int i, int j,
-                                              int k, const float c[7], float k1, float k2, float k3, const GcDev& g,
-                                              const int4& r0, const int4& r1) {
-  const float pc = v[(size_t)slot * t.SI + rb_idx<D>(t.nc, i, j, k)];
-  const float pw = nb_val_rb<D>(t, v, slot, i - 1, j, k, g, r0, r1);
-  const float pe = nb_val_rb<D>(t, v, slot, i + 1, j, k, g, r0, r1);
-  const float ps = nb_val_rb<D>(t, v, slot, i, j - 1, k, g, r0, r1);
-  const float pn = nb_val_rb<D>(t, v, slot, i, j + 1, k, g, r0, r1);
-  if (D == 2) return lpl_vals<D, CYL, float>(pc, pw, pe, ps, pn, 0.0f, 0.0f, c, k1, k2, k3);
-  const float pb = nb_val_rb<D>(t, v, slot, i, j, k - 1, g, r0, r1);
-  const float pf = nb_val_rb<D>(t, v, slot, i, j, k + 1, g, r0, r1);
-  return lpl_vals<D, CYL, float>(pc, pw, pe, ps, pn, pb, pf, c, k1, k2, k3);
-}
-
 // Red-black half sweep, one box per CTA, any box size: the cells of colour
 // redblack & 1 from the other colour and the face ghost rules
 // (k_gsrb_fused's arithmetic).
@@ -221,14 +205,15 @@ __global__ void __launch_bounds__(256) k_gsrb_rb(KTree t0, const int* __restrict
 // The same half sweep staged in shared memory for a compile-time box size:
 // a persistent grid walks the box records; per box, thread 0 bulk-copies the
 // next box's other-colour half (SI/2 values, contiguous) into one of two
-// stages while the CTA works on the current box.  The CTA spreads the staged
-// half into a padded (nc+2)^D block, evaluates the face ghosts next to cells
-// of the updated colour there (face_ghost_rb on global memory: the values
-// af_gc would store), and each thread updates CPT cells of the colour from
-// shared memory without branches; right-hand sides and results move as
-// contiguous colour halves.  A wait that times out (1 s) raises *err; the
-// CTA drains its copies (bounded) and returns, raising bit 2 of *err if they
-// did not complete.
+// stages while the CTA works on the current box.  Before waiting for the
+// current box's copy, each thread loads the right-hand sides of its cells
+// (contiguous colour halves) and evaluates its share of the face ghosts next
+// to cells of the updated colour (face_ghost_rb on global memory: the values
+// af_gc would store), so those loads overlap the copy.  The CTA then spreads
+// the staged half and the ghosts into a padded (nc+2)^D block and each thread
+// updates CPT cells of the colour from shared memory without branches.  A
+// wait that times out (1 s) raises *err; the CTA drains its copies (bounded)
+// and returns, raising bit 2 of *err if they did not complete.
 template <int D, bool CYL, int NC, int CPT>
 __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT)
     k_gsrb_rb_tma(KTree t0, const int* __restrict__ rec, int n, ModeArg<float> phi_, ModeArg<const float> rhs_,
@@ -239,6 +224,7 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
   constexpr int S = D == 2 ? n2 * n2 : n2 * n2 * n2;
   constexpr int SI = 2 * SH;
   constexpr int NGF = D == 2 ? hn : nc * hn;  // ghosts read per face and half sweep
+  constexpr int NGT = (2 * D * NGF + TPB - 1) / TPB;  // ghosts per thread
   constexpr unsigned BYTES = SH * sizeof(float);
   static_assert(BYTES % 16 == 0, "bulk copies need 16-byte multiples");
   __shared__ __align__(128) float cst[2][SH];
@@ -270,10 +256,11 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
     const int4 r0 = reinterpret_cast<const int4*>(rec)[2 * e];
     const int4 r1 = reinterpret_cast<const int4*>(rec)[2 * e + 1];
     const int slot = r0.x;
+    const bool active = !box_frozen(t, slot);
     float c[7];
     for (int q = 0; q < 2 * D + 1; q++) c[q] = mc.cb[slot * 8 + q];
     const float inv_c1 = mc.cb[slot * 8 + 7];
-    // this thread's cells and their right-hand sides, loaded before the wait
+    // this thread's cells and their right-hand sides
     const float* f = rhs + (size_t)slot * SI + col * SH;
     float fv[CPT];
     int xs[CPT];
@@ -285,6 +272,31 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
       xs[u] = D == 2 ? at2(n2, i, j) : at3(n2, i, j, k);
       fv[u] = f[w];
     }
+    // this thread's face ghosts next to cells of the updated colour: cell
+    // (i, j[, k]) is updated when i + j (+ k) + redblack is even
+    float gv[NGT];
+    int gx[NGT];
+#pragma unroll
+    for (int u = 0; u < NGT; u++) {
+      const int w = (int)threadIdx.x + u * TPB;
+      gx[u] = -1;
+      gv[u] = 0.0f;
+      if (active && w < 2 * D * NGF) {
+        const int nb = w / NGF, m = w - nb * NGF, d = nb >> 1;
+        const bool low = (nb & 1) == 0;
+        const int a = low ? 1 : nc;  // normal index of the adjacent cell
+        int pt, qt;
+        if (D == 2) {
+          qt = 0;
+          pt = 2 * m + 1 + ((a + 1 + redblack) & 1);
+        } else {
+          qt = m / hn + 1;
+          pt = 2 * (m - (qt - 1) * hn) + 1 + ((a + 1 + qt + redblack) & 1);
+        }
+        gx[u] = face_at<D>(n2, d, low ? 0 : nc + 1, pt, qt);
+        gv[u] = face_ghost_rb<D>(t, phi, slot, nb, rec_nb(r0, r1, nb), pt, qt, g);
+      }
+    }
     const bool ok = mbar_wait(&bar[st], (it >> 1) & 1);
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) {
@@ -294,30 +306,15 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
       }
       return;
     }
-    const bool active = !box_frozen(t, slot);
-    // the other colour into the padded block
+    // the other colour and the ghosts into the padded block
     for (int w = threadIdx.x; active && w < SH; w += TPB) {
       int i, j, k;
       rb_cell<D>(nc, oc, w, i, j, k);
       P[D == 2 ? at2(n2, i, j) : at3(n2, i, j, k)] = cst[st][w];
     }
-    // face ghosts next to cells of the updated colour: cell (i, j[, k]) is
-    // updated when i + j (+ k) + redblack is even
-    for (int w = threadIdx.x; active && w < 2 * D * NGF; w += TPB) {
-      const int nb = w / NGF, m = w - nb * NGF, d = nb >> 1;
-      const bool low = (nb & 1) == 0;
-      const int a = low ? 1 : nc;  // normal index of the adjacent cell
-      int pt, qt;
-      if (D == 2) {
-        qt = 0;
-        pt = 2 * m + 1 + ((a + 1 + redblack) & 1);
-      } else {
-        qt = m / hn + 1;
-        pt = 2 * (m - (qt - 1) * hn) + 1 + ((a + 1 + qt + redblack) & 1);
-      }
-      P[face_at<D>(n2, d, low ? 0 : nc + 1, pt, qt)] =
-          face_ghost_rb<D>(t, phi, slot, nb, rec_nb(r0, r1, nb), pt, qt, g);
-    }
+#pragma unroll
+    for (int u = 0; u < NGT; u++)
+      if (gx[u] >= 0) P[gx[u]] = gv[u];
     __syncthreads();
     if (active) {
       float* out = phi + (size_t)slot * SI + col * SH;
@@ -437,12 +434,17 @@ __global__ void __launch_bounds__(256) k_gc_rb(KTree t0, const int* __restrict__
 
 // update_coarse first half (k_residual_restrict with the face neighbours on
 // the fly): residual of each child box restricted to its parent's tmp (with
-// the cylindrical weights), phi restricted without geometry.
+// the cylindrical weights), phi restricted without geometry.  The CTA first
+// gathers the box's interior and its face ghosts (face_ghost_rb: the values
+// af_gc would store) into a padded (nc+2)^D block in shared memory
+// (dynamic, S floats); the stencil then reads shared memory only.
 template <int D, bool CYL, int NC = 0>
 __global__ void __launch_bounds__(256) k_residual_restrict_rb(KTree t0, const int* __restrict__ rec,
                                                               ModeArg<float> phi_, ModeArg<const float> rhs_,
                                                               ModeArg<float> tmp_, ModeCoef<float> mc_, GcDev g) {
   const KTree t = fix_dims<D, NC>(t0);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* P = reinterpret_cast<float*>(smem_raw);
   float* __restrict__ phi = phi_.get();
   const float* __restrict__ rhs = rhs_.get();
   float* __restrict__ tmp = tmp_.get();
@@ -452,11 +454,25 @@ __global__ void __launch_bounds__(256) k_residual_restrict_rb(KTree t0, const in
   const int slot = r0.x;
   if (box_frozen(t, slot)) return;
   const int pslot = t.parent[slot];
-  const int nc = t.nc, hnc = nc / 2;
-  float c[7];
-  for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
+  const int nc = t.nc, n2 = t.n2, hnc = nc / 2, sk = n2 * n2;
   const float* p = phi + (size_t)slot * t.SI;
   const float* f = rhs + (size_t)slot * t.SI;
+  for (int w = threadIdx.x; w < t.SI; w += blockDim.x) {
+    const int col = w >= t.SI / 2;
+    int i, j, k;
+    rb_cell<D>(nc, col, w - col * (t.SI / 2), i, j, k);
+    P[D == 2 ? at2(n2, i, j) : at3(n2, i, j, k)] = p[w];
+  }
+  const int nface = D == 2 ? nc : nc * nc;
+  for (int w = threadIdx.x; w < 2 * D * nface; w += blockDim.x) {
+    const int nb = w / nface, pq = w - nb * nface;
+    const int pi = pq % nc + 1, qi = D == 3 ? pq / nc + 1 : 0;
+    P[face_at<D>(n2, nb >> 1, (nb & 1) ? nc + 1 : 0, pi, qi)] =
+        face_ghost_rb<D>(t, phi, slot, nb, rec_nb(r0, r1, nb), pi, qi, g);
+  }
+  __syncthreads();
+  float c[7];
+  for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
   float* pp = phi + (size_t)pslot * t.SI;
   float* pt = tmp + (size_t)pslot * t.SI;
   const int o0 = child_offset(t, slot, 0), o1 = child_offset(t, slot, 1);
@@ -476,8 +492,10 @@ __global__ void __launch_bounds__(256) k_residual_restrict_rb(KTree t0, const in
             const float* y = mc.cy + ((size_t)slot * nc + (fi + di - 1)) * 4;
             k1 = y[0]; k2 = y[1]; k3 = y[2];
           }
+          const int x = at2(n2, fi + di, fj + dj);
           res[dj][di] = f[rb_idx<D>(nc, fi + di, fj + dj, 0)] -
-                        apply_lpl_rb<D, CYL>(t, phi, slot, fi + di, fj + dj, 0, c, k1, k2, k3, g, r0, r1);
+                        lpl_vals<D, CYL, float>(P[x], P[x - 1], P[x + 1], P[x - n2], P[x + n2], 0.0f, 0.0f, c, k1,
+                                                k2, k3);
         }
       float rv;
       if (CYL) {
@@ -494,19 +512,20 @@ __global__ void __launch_bounds__(256) k_residual_restrict_rb(KTree t0, const in
       }
       pt[rb_idx<D>(nc, ic, jc, 0)] = rv;
       float s = 0.0f;
-      s = s + p[rb_idx<D>(nc, fi, fj, 0)]; s = s + p[rb_idx<D>(nc, fi + 1, fj, 0)];
-      s = s + p[rb_idx<D>(nc, fi, fj + 1, 0)]; s = s + p[rb_idx<D>(nc, fi + 1, fj + 1, 0)];
+      s = s + P[at2(n2, fi, fj)]; s = s + P[at2(n2, fi + 1, fj)];
+      s = s + P[at2(n2, fi, fj + 1)]; s = s + P[at2(n2, fi + 1, fj + 1)];
       pp[rb_idx<D>(nc, ic, jc, 0)] = 0.25f * s;
     } else {
       float sr = 0.0f, sp = 0.0f;
       for (int dk = 0; dk < 2; dk++)
         for (int dj = 0; dj < 2; dj++)
           for (int di = 0; di < 2; di++) {
-            const int x = rb_idx<D>(nc, fi + di, fj + dj, fk + dk);
-            const float res = f[x] - apply_lpl_rb<D, false>(t, phi, slot, fi + di, fj + dj, fk + dk, c, 0.0f, 0.0f,
-                                                             0.0f, g, r0, r1);
+            const int x = at3(n2, fi + di, fj + dj, fk + dk);
+            const float res = f[rb_idx<D>(nc, fi + di, fj + dj, fk + dk)] -
+                              lpl_vals<D, false, float>(P[x], P[x - 1], P[x + 1], P[x - n2], P[x + n2], P[x - sk],
+                                                        P[x + sk], c, 0.0f, 0.0f, 0.0f);
             sr = sr + res;
-            sp = sp + p[x];
+            sp = sp + P[x];
           }
       pt[rb_idx<D>(nc, ic, jc, kc)] = 0.125f * sr;
       pp[rb_idx<D>(nc, ic, jc, kc)] = 0.125f * sp;

@@ -608,11 +608,11 @@ static int launch_rrestrict(afg_ctx* ctx, const int* list, int n, ModeArg<T> phi
     if (ctx->rb32) {
       if (store_child || !otf) return fail(ctx, AFG_ERR_STATE, "compact FP32 restriction: face neighbours on the fly only");
       if (ctx->D == 3)
-        AFG_NC3(NCV_, k_residual_restrict_rb<3, false, NCV_><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, g));
+        AFG_NC3(NCV_, k_residual_restrict_rb<3, false, NCV_><<<dim3(n, ctx->ky), threads, sizeof(float) * ctx->S, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, g));
       else if (ctx->coord == AFG_CYL)
-        AFG_NC2(NCV_, k_residual_restrict_rb<2, true, NCV_><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, g));
+        AFG_NC2(NCV_, k_residual_restrict_rb<2, true, NCV_><<<dim3(n, ctx->ky), threads, sizeof(float) * ctx->S, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, g));
       else
-        AFG_NC2(NCV_, k_residual_restrict_rb<2, false, NCV_><<<dim3(n, ctx->ky), threads, 0, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, g));
+        AFG_NC2(NCV_, k_residual_restrict_rb<2, false, NCV_><<<dim3(n, ctx->ky), threads, sizeof(float) * ctx->S, ctx->stream>>>(t, rec_of(ctx, list), phi, rhs, tmp, lam, g));
       ctx->launches++;
       CKL();
       return AFG_OK;
@@ -838,13 +838,23 @@ static int mg_gc_lvl(afg_ctx* ctx, int lvl, ModeArg<T> phi, const GcDev& g, int 
 // gsrb_boxes, m_af_multigrid.f90:648-687
 template <typename T>
 static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, ModeArg<T> phi, ModeArg<const T> rhs,
-                         const GcDev& g, bool fill_down = true, bool fill_needed_only = false) {
+                         const GcDev& g, bool fill_down = true, bool fill_needed_only = false,
+                         bool stored_first = false) {
   const int n_cycle = type == AFG_CYCLE_DOWN ? m.d.n_cycle_down : m.d.n_cycle_up;
   const int* list = lst(ctx, ctx->off_ids[lvl - 1]);
   const int n = (int)ctx->lvl_ids[lvl - 1].size();
   ctx->ctr[1] += (long long)n * (long long)box_cells(ctx) * n_cycle * ctx->ky;
   if (ctx->fused_gsrb) {
-    for (int it = 1; it <= 2 * n_cycle; it++) RC(launch_gsrb_fused<T>(ctx, list, n, phi, rhs, it, coefs<T>(ctx, m), g));
+    int it0 = 1;
+    if (stored_first) {
+      // the first half sweep with the ghost cells as they are stored, then
+      // the fill that follows it in the reference (gsrb_boxes)
+      if (ctx->ky != 1 || rb_of<T>(ctx)) return fail(ctx, AFG_ERR_STATE, "stored-ghost half sweep: one FP64 problem");
+      RC(launch_gsrb<T>(ctx, list, n, phi.p[0], rhs.p[0], 1, coef_of<T>(m)));
+      RC(launch_gc<T>(ctx, list, n, phi, g, 0));
+      it0 = 2;
+    }
+    for (int it = it0; it <= 2 * n_cycle; it++) RC(launch_gsrb_fused<T>(ctx, list, n, phi, rhs, it, coefs<T>(ctx, m), g));
     if (type == AFG_CYCLE_DOWN && !fill_down) return AFG_OK;
     if (type != AFG_CYCLE_DOWN && fill_needed_only)
       return launch_gc<T>(ctx, lst(ctx, ctx->off_gcneed[lvl - 1]), (int)ctx->lvl_gcneed[lvl - 1].size(), phi, g, 1);
@@ -958,14 +968,22 @@ static int mg_residual_lvls(afg_ctx* ctx, const MgSlot& m, int max_lvl, const T*
 
 // mg_fas_vcycle, m_af_multigrid.f90:185-264 (the residual, set_residual,
 // for one problem at a time)
+//
+// stored_first: the first half sweep on max_lvl reads the ghost cells as
+// they are stored, as the reference's does.  A V-cycle called on its own
+// cannot know whether they are current: a mesh change leaves old ghost
+// values next to changed neighbours, and the reference's first half sweep
+// uses them.  Every later half sweep sees freshly filled (or equal on-the-fly)
+// values, in the reference as here.  Inside FMG the level was just corrected
+// and filled in the reference, so its ghost values are current there.
 template <typename T>
 static int mg_vcycle(afg_ctx* ctx, MgSlot& m, int max_lvl, ModeArg<T> phi, ModeArg<T> rhs, ModeArg<T> tmp,
-                     bool set_residual, bool homogeneous, unsigned long long* maxbits) {
+                     bool set_residual, bool homogeneous, unsigned long long* maxbits, bool stored_first = false) {
   const GcDev g = mg_gc(ctx, m, homogeneous);
   ctx->ctr[3] += ctx->ky;
   for (int lvl = max_lvl; lvl >= 2; lvl--) {
     // the restriction below computes the face neighbours it needs itself
-    RC(mg_gsrb_boxes<T>(ctx, m, lvl, AFG_CYCLE_DOWN, phi, rhs, g, false));
+    RC(mg_gsrb_boxes<T>(ctx, m, lvl, AFG_CYCLE_DOWN, phi, rhs, g, false, false, stored_first && lvl == max_lvl));
     RC(mg_update_coarse<T>(ctx, m, lvl, phi, rhs, tmp, g));
   }
   RC(mg_coarse_solve<T>(ctx, m, phi, rhs, g, homogeneous));
@@ -1228,14 +1246,17 @@ static void inst_uncount(afg_ctx* ctx, const MgSlot& m, bool fmg) {
 
 // the launch sequences of one solve iteration (shared by the single-tree
 // and the batched loops, so both replay the same graphs)
-static int vcycle_graph(afg_ctx* ctx, MgSlot& m) {
+// first: the first V-cycle of a solve (its first half sweep reads the stored
+// ghost cells, which a mesh change may have left behind; after it they are
+// current and on-the-fly values equal them)
+static int vcycle_graph(afg_ctx* ctx, MgSlot& m, bool first) {
   const int mg_id = (int)(&m - ctx->mg);
   double* phi = ctx->cc[m.d.i_phi - 1];
   double* rhs = ctx->cc[m.d.i_rhs - 1];
   double* tmp = ctx->cc[m.d.i_tmp - 1];
-  RC(run_graph(ctx, gkey("vcycle", mg_id, ctx->highest_lvl, 1), [&]() -> int {
+  RC(run_graph(ctx, gkey(first ? "vcycle" : "vcycle_next", mg_id, ctx->highest_lvl, 1), [&]() -> int {
     RC(reset_max(ctx, 1));
-    return mg_vcycle<double>(ctx, m, ctx->highest_lvl, phi, rhs, tmp, true, false, ctx->d_max + 1);
+    return mg_vcycle<double>(ctx, m, ctx->highest_lvl, phi, rhs, tmp, true, false, ctx->d_max + 1, first);
   }));
   inst_uncount(ctx, m, false);
   return AFG_OK;
@@ -1316,7 +1337,7 @@ static int mg_solve_inst(afg_ctx* ctx, MgSlot& m, const double* thr, int max_cyc
   };
   for (int it = 0; it < max_cycles && !all_done(); it++) {
     RC(set_frozen(ctx, done));
-    RC(mixed ? mixed_iter_graph(ctx, m) : vcycle_graph(ctx, m));
+    RC(mixed ? mixed_iter_graph(ctx, m) : vcycle_graph(ctx, m, it == 0));
     RC(read_max(ctx, slot, &mx));
     for (int q = 0; q < Q; q++) {
       if (done[q]) continue;
@@ -2315,7 +2336,9 @@ int afg_mg_gsrb_lvl(afg_ctx* ctx, int mg_id, int lvl, int type) {
   if (lvl < 1 || lvl > ctx->highest_lvl) return fail(ctx, AFG_ERR_ARG, "bad level");
   MG_VARS(m);
   (void)tmp;
-  return mg_gsrb_boxes<double>(ctx, *m, lvl, type, phi, rhs, mg_gc(ctx, *m, false));
+  // a call on its own: the first half sweep reads the stored ghost cells,
+  // as the reference's gsrb_boxes does
+  return mg_gsrb_boxes<double>(ctx, *m, lvl, type, phi, rhs, mg_gc(ctx, *m, false), true, false, true);
 }
 
 int afg_mg_update_coarse(afg_ctx* ctx, int mg_id, int lvl) {
@@ -2361,7 +2384,7 @@ int afg_mg_vcycle(afg_ctx* ctx, int mg_id, int set_residual, int max_lvl, double
   const int ml = max_lvl <= 0 ? ctx->highest_lvl : std::min(max_lvl, ctx->highest_lvl);
   RC(run_graph(ctx, gkey("vcycle", mg_id, ml, set_residual != 0), [&]() -> int {
     RC(reset_max(ctx, 1));
-    return mg_vcycle<double>(ctx, *m, ml, phi, rhs, tmp, set_residual != 0, false, ctx->d_max + 1);
+    return mg_vcycle<double>(ctx, *m, ml, phi, rhs, tmp, set_residual != 0, false, ctx->d_max + 1, true);
   }));
   inst_uncount(ctx, *m, false);
   if (set_residual && max_res) return read_max(ctx, 1, max_res);
@@ -2403,7 +2426,7 @@ int afg_mg_solve(afg_ctx* ctx, int mg_id, double threshold, int max_cycles, int*
   int n = 0;
   double r = 0;
   for (n = 0; n < max_cycles;) {
-    RC(vcycle_graph(ctx, *m));
+    RC(vcycle_graph(ctx, *m, n == 0));
     RC(read_max(ctx, 1, &r));
     if (residuals) residuals[n] = r;
     n++;

@@ -68,6 +68,7 @@ struct Mg {
   int n_coarse = 0;                // unknowns of the coarse grid
   int gx[3] = {1, 1, 1};           // coarse grid size in cells
   std::vector<double> ainv;        // dense inverse, row-major [n][n]
+  std::vector<double> amat;        // the matrix itself (kept for the inexact-solve experiment)
   std::vector<double> bc_to_rhs;   // [box-of-lvl1][nb][nc^(D-1)]
   GcSpec gc() const {
     GcSpec g;

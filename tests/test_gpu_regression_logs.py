@@ -22,10 +22,9 @@ import streamer_program as sp
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "standard_2d")
 CASES = ["test_2d", "test_cyl", "test_2d_photoi", "test_cyl_chem", "test_2d_photoi_chem",
-         "test_cyl_ion_motion", "test_cyl_ion_motion_v2", "test_3d", "test_3d_chem", "test_3d_photoi_chem"]
-# the FP64 comparison also covers test_cyl_photoi_chem; its mixed-precision
-# run has no measured bound yet and is not part of the mixed comparison
-FP64_CASES = CASES + ["test_cyl_photoi_chem"]
+         "test_cyl_ion_motion", "test_cyl_ion_motion_v2", "test_3d", "test_3d_chem", "test_3d_photoi_chem",
+         "test_cyl_photoi_chem"]
+FP64_CASES = CASES
 
 # FP64 GPU rows against the restatement's: the runs take the same steps,
 # rejections and meshes; single stages are bit-exact, but over the 2D whole
