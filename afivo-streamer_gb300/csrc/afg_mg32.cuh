@@ -215,7 +215,8 @@ __global__ void __launch_bounds__(256) k_gsrb_rb(KTree t0, const int* __restrict
 // wait that times out (1 s) raises *err; the CTA drains its copies (bounded)
 // and returns, raising bit 2 of *err if they did not complete.
 template <int D, bool CYL, int NC, int CPT>
-__global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT)
+__global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT,
+                                  1024 / ((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CPT))
     k_gsrb_rb_tma(KTree t0, const int* __restrict__ rec, int n, ModeArg<float> phi_, ModeArg<const float> rhs_,
                   int redblack, ModeCoef<float> mc_, GcDev g, unsigned* err) {
   constexpr int SH = D == 2 ? NC * NC / 2 : NC * NC * NC / 2;

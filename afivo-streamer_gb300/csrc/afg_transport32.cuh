@@ -401,8 +401,11 @@ __global__ void __launch_bounds__(256) k_field_grad32(KTree t0, const int* __res
   }
 }
 
-// Charge density on interior cells (FP64: n_+ - n_- cancels)
-template <int D, int NC = 0>
+// Charge density on interior cells (FP64: n_+ - n_- cancels).  `a` holds
+// the charged species only (a.ns of them, at most NQ), so that the unrolled
+// species loop indexes the parameter arrays statically and every density
+// load of a cell is issued before the sums.
+template <int D, int NQ, int NC = 0>
 __global__ void __launch_bounds__(256) k_field_rhs_interior(KTree t0, const int* __restrict__ list, RhsArgs a,
                                                             unsigned long long* maxbits) {
   const KTree t = fix_dims<D, NC>(t0);
@@ -412,14 +415,17 @@ __global__ void __launch_bounds__(256) k_field_rhs_interior(KTree t0, const int*
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;
   const size_t base = (size_t)slot * t.S;
   double mx = 0.0;
-#pragma unroll 2
   for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
     const int i = w % nc + 1, r = w / nc;
     const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
     const size_t x = base + (D == 2 ? at2(n2, i, j) : at3(n2, i, j, k));
+    double nv[NQ];
+#pragma unroll
+    for (int s = 0; s < NQ; s++) nv[s] = s < a.ns ? a.n[s][x] : 0.0;
     double v = 0.0;
-    for (int s = 0; s < a.ns; s++)
-      if (a.q[s] != 0.0) v = fma(a.q[s], a.n[s][x], v);
+#pragma unroll
+    for (int s = 0; s < NQ; s++)
+      if (s < a.ns) v = fma(a.q[s], nv[s], v);
     a.rhs[x] = v;
     acc_absmax(mx, v);
   }

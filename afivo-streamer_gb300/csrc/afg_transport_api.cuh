@@ -441,12 +441,36 @@ static int field_set_rhs(afg_ctx* ctx, int i_rhs, int s_in, unsigned long long* 
   if (ctx->n_all_leaves > 0) {
     const int* list = lst(ctx, ctx->off_all_leaves);
     KtScope kts(ctx, AFG_KT_FIELD, 8.0 * ctx->n_all_leaves * box_cells(ctx) * (d.n_species + 1));
-    if (!mixed_transport(ctx))
+    if (!mixed_transport(ctx)) {
       k_field_rhs<<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ctx->S, list, a);
-    else if (ctx->D == 3)
-      AFG_NC3(NCV_, k_field_rhs_interior<3, NCV_><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), list, a, maxbits));
-    else
-      AFG_NC2(NCV_, k_field_rhs_interior<2, NCV_><<<ctx->n_all_leaves, 256, 0, ctx->stream>>>(ktree(ctx), list, a, maxbits));
+    } else {
+      // the charged species only, in order (the sums skip the others)
+      RhsArgs q{};
+      q.rhs = a.rhs;
+      for (int s = 0; s < a.ns; s++)
+        if (a.q[s] != 0.0) {
+          q.n[q.ns] = a.n[s];
+          q.q[q.ns] = a.q[s];
+          q.ns++;
+        }
+      const KTree t = ktree(ctx);
+      const int nl = ctx->n_all_leaves;
+#define AFG_LAUNCH_RHS(NQ)                                                                                   \
+  if (ctx->D == 3)                                                                                           \
+    AFG_NC3(NCV_, k_field_rhs_interior<3, NQ, NCV_><<<nl, 256, 0, ctx->stream>>>(t, list, q, maxbits));     \
+  else                                                                                                       \
+    AFG_NC2(NCV_, k_field_rhs_interior<2, NQ, NCV_><<<nl, 256, 0, ctx->stream>>>(t, list, q, maxbits));
+      if (q.ns <= 2) {
+        AFG_LAUNCH_RHS(2)
+      } else if (q.ns <= 4) {
+        AFG_LAUNCH_RHS(4)
+      } else if (q.ns <= 8) {
+        AFG_LAUNCH_RHS(8)
+      } else {
+        AFG_LAUNCH_RHS(16)
+      }
+#undef AFG_LAUNCH_RHS
+    }
     ctx->launches++;
     CKL();
   }
