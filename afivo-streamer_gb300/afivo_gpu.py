@@ -287,6 +287,13 @@ def load_library(path: str = LIB_PATH):
         "afg_host_unregister": (C.c_int, [P, C.c_void_p]),
         "afg_sync": (C.c_int, [P]),
         "afg_launch_count": (C.c_longlong, [P]),
+        "afg_write_vtk": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double, C.c_int, _IP, C.POINTER(C.c_char_p)]),
+        "afg_leaf_cells": (C.c_int, [P, C.c_int, _DP, C.POINTER(C.c_longlong)]),
+        "afg_interp1": (C.c_int, [P, C.c_longlong, _DP, C.c_int, _IP, _DP, _IP]),
+        "afg_write_line": (C.c_int, [P, C.c_char_p, C.c_int, _IP, C.POINTER(C.c_char_p), _DP, _DP, C.c_int]),
+        "afg_write_plane": (C.c_int, [P, C.c_char_p, C.c_int, _IP, C.POINTER(C.c_char_p), _DP, _DP, _IP]),
+        "afg_write_numpy": (C.c_int, [P, C.c_char_p, _DP, _DP, _IP, C.c_int, C.c_double, C.c_int, _IP,
+                                      C.POINTER(C.c_char_p)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -422,6 +429,62 @@ class Context:
 
     def restrict_tree(self, iv):
         self.check(self.lib.afg_restrict_tree(self.ptr, iv), "afg_restrict_tree")
+
+    # ---- output writers (af_write_vtk, af_write_line, af_write_plane,
+    # af_write_numpy, af_interp1) ----
+    @staticmethod
+    def _names(names):
+        arr = (C.c_char_p * max(1, len(names)))(*[n.encode() for n in names])
+        return arr
+
+    def write_vtk(self, filename, ivs, names, n_cycle=0, time=0.0):
+        """filename + '.vtu' of all leaf cells of variables ivs (1-based)."""
+        a = np.ascontiguousarray(ivs, dtype=np.int32)
+        nm = self._names(names)
+        self.check(self.lib.afg_write_vtk(self.ptr, filename.encode(), int(n_cycle), float(time), len(a), _ip(a), nm),
+                   "afg_write_vtk")
+
+    def leaf_cells(self, iv):
+        n = C.c_longlong(0)
+        self.check(self.lib.afg_leaf_cells(self.ptr, iv, None, C.byref(n)), "afg_leaf_cells")
+        out = np.empty(n.value, dtype=np.float64)
+        self.check(self.lib.afg_leaf_cells(self.ptr, iv, _dp(out), C.byref(n)), "afg_leaf_cells")
+        return out
+
+    def interp1(self, points, ivs):
+        """af_interp1 at points [n][ndim]: (values [n][len(ivs)], success [n])."""
+        r = np.ascontiguousarray(points, dtype=np.float64)
+        a = np.ascontiguousarray(ivs, dtype=np.int32)
+        n = r.shape[0]
+        vals = np.zeros((n, max(1, len(a))), dtype=np.float64)
+        ok = np.zeros(n, dtype=np.int32)
+        self.check(self.lib.afg_interp1(self.ptr, n, _dp(r), len(a), _ip(a), _dp(vals), _ip(ok)), "afg_interp1")
+        return vals[:, :len(a)], ok.astype(bool)
+
+    def write_line(self, filename, ivs, names, r_min, r_max, n_points):
+        a = np.ascontiguousarray(ivs, dtype=np.int32)
+        r0 = np.ascontiguousarray(r_min, dtype=np.float64)
+        r1 = np.ascontiguousarray(r_max, dtype=np.float64)
+        self.check(self.lib.afg_write_line(self.ptr, filename.encode(), len(a), _ip(a), self._names(names),
+                                           _dp(r0), _dp(r1), int(n_points)), "afg_write_line")
+
+    def write_plane(self, filename, ivs, names, r_min, r_max, n_pixels):
+        a = np.ascontiguousarray(ivs, dtype=np.int32)
+        r0 = np.ascontiguousarray(r_min, dtype=np.float64)
+        r1 = np.ascontiguousarray(r_max, dtype=np.float64)
+        npx = np.ascontiguousarray(n_pixels, dtype=np.int32)
+        self.check(self.lib.afg_write_plane(self.ptr, filename.encode(), len(a), _ip(a), self._names(names),
+                                            _dp(r0), _dp(r1), _ip(npx)), "afg_write_plane")
+
+    def write_numpy(self, filename, ivs, names, r_min=None, r_max=None, n_points=None, n_cycle=0, time=0.0):
+        a = np.ascontiguousarray(ivs, dtype=np.int32)
+        r0 = None if r_min is None else np.ascontiguousarray(r_min, dtype=np.float64)
+        r1 = None if r_max is None else np.ascontiguousarray(r_max, dtype=np.float64)
+        npt = None if n_points is None else np.ascontiguousarray(n_points, dtype=np.int32)
+        self.check(self.lib.afg_write_numpy(self.ptr, filename.encode(), None if r0 is None else _dp(r0),
+                                            None if r1 is None else _dp(r1), None if npt is None else _ip(npt),
+                                            int(n_cycle), float(time), len(a), _ip(a), self._names(names)),
+                   "afg_write_numpy")
 
     def tree_remap(self, tree, old_id):
         """Mirror `tree` keeping the data: old_id[b] = id of new box b+1 in

@@ -2604,3 +2604,4 @@ int afg_kernel_stats(afg_ctx* ctx, long long* launches, double* ms, double* byte
 
 #include "afg_transport_api.cuh"
 #include "afg_amr.cuh"
+#include "afg_output.cuh"

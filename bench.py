@@ -292,7 +292,10 @@ def run_gpu_arm(args, device, w):
     tree, model, H, ivs, voltage, box_inst, trees = problem(args, w)
     ctx = new_context(args, device)
     results = {}
-    arms = (("mixed", ag.MIXED),) if args.profile else (("fp64", ag.FP64), ("mixed", ag.MIXED))
+    if args.profile:
+        arms = (("fp64", ag.FP64),) if args.profile_arm == "fp64" else (("mixed", ag.MIXED),)
+    else:
+        arms = (("fp64", ag.FP64), ("mixed", ag.MIXED))
     svars = snapshot_vars(model)
     snap64, accuracy = None, None
     for prec_name, prec in arms:
@@ -305,7 +308,7 @@ def run_gpu_arm(args, device, w):
             run.step()
         ctx.sync()
         times, vcycles = [], 0
-        clocks = Clocks(device) if prec_name == "mixed" else None
+        clocks = Clocks(device) if prec_name == "mixed" or args.profile else None
         c0 = ctx.counters()
         if args.profile:
             cuda_profiler(True)
@@ -625,7 +628,10 @@ def main():
     ap.add_argument("--fp32-layout", default="compact", choices=["compact", "ghosted"],
                     help="layout of the FP32 correction buffers of the mixed solves")
     ap.add_argument("--profile", action="store_true",
-                    help="mixed arm only, timed steps bracketed by cudaProfilerStart/Stop; no e2e or CPU baseline")
+                    help="one arm only (--profile-arm), timed steps bracketed by cudaProfilerStart/Stop; "
+                         "no e2e or CPU baseline")
+    ap.add_argument("--profile-arm", default="mixed", choices=["mixed", "fp64"],
+                    help="the arm --profile runs")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -664,7 +670,8 @@ def main():
     amr = e2e.pop("amr", None) if e2e else None
     if args.profile:
         if rank == 0:
-            print(json.dumps({"profile": True, "config": config, "mixed": results["mixed"][0]}))
+            print(json.dumps({"profile": True, "config": config,
+                              args.profile_arm: results[args.profile_arm][0]}))
         return
     mixed, fp64 = results["mixed"][0], results["fp64"][0]
     ms = mixed["ms_per_step"]

@@ -628,6 +628,69 @@ int afg_kernel_stats_all(afg_ctx* ctx, long long* launches, double* ms, double* 
 int afg_maxabs_noalloc(const double* d_pool, const int* d_slots, int n_slots,
                        int ndim, int n_cell, void* stream, double* result);
 
+/* ---- output (afivo/src/m_af_output.f90) --------------------------------
+ * The device-resident state written without a copy of the tree to the host:
+ * the device gathers leaf cells, generates the mesh or interpolates, and
+ * the host streams the result into the file in 64 MiB chunks.  Variables are
+ * given as 1-based cell-centred indices ivs[0..n_iv-1] (at most 64) with
+ * their names (tree%cc_names); the caller resolves cc_write_output
+ * (get_output_vars, m_af_output.f90:1582-1597).  Ghost cells must be valid
+ * where interpolation reads them, as in the reference. */
+
+/* af_write_vtk (m_af_output.f90:556-752, m_vtk.f90): filename + ".vtu", a
+ * VTK XML unstructured grid of all leaf cells, level by level in
+ * tree%lvls(:)%leaves order: FieldData TIME (Float64) and CYCLE (Int32),
+ * Float32 node coordinates (3 components, z = 0 in 2D), Int32 connectivity,
+ * offsets and types (8 pixel / 11 voxel), one Float64 cell array per
+ * variable, appended raw with 4-byte size headers (8-byte headers and
+ * version 1.0 if an array exceeds 4 GiB).  The add_vars callback of the
+ * reference has no counterpart: compute extra variables into spare
+ * cell-centred variables first. */
+int afg_write_vtk(afg_ctx* ctx, const char* filename, int n_cycle, double time,
+                  int n_iv, const int* ivs, const char* const* names);
+
+/* The cell data of variable iv on all leaves (the order and layout of the
+ * CellData arrays of afg_write_vtk) into out[n_cells]; out = NULL returns
+ * only *n_cells. */
+int afg_leaf_cells(afg_ctx* ctx, int iv, double* out, long long* n_cells);
+
+/* af_interp1 (m_af_interp.f90:43-105) at n_points points r[p][ndim]
+ * (host arrays): the finest box containing the point (af_get_id_at without
+ * a guess, m_af_utils.f90:266-313), multilinear interpolation between the
+ * surrounding cell centres including ghost cells.  vals[p][v]; success[p]
+ * (may be NULL) is 0 for a point outside the tree, whose values are 0. */
+int afg_interp1(afg_ctx* ctx, long long n_points, const double* r, int n_iv,
+                const int* ivs, double* vals, int* success);
+
+/* af_write_line (m_af_output.f90:407-463): n_points points from r_min to
+ * r_max (inclusive) into filename + ".txt": a "# x y[ z] names" header and
+ * one row of coordinates and values per point.  A point outside the tree is
+ * an error (AFG_ERR_ARG, no file), as the reference's error stop. */
+int afg_write_line(afg_ctx* ctx, const char* filename, int n_iv, const int* ivs,
+                   const char* const* names, const double* r_min,
+                   const double* r_max, int n_points);
+
+/* af_write_plane (m_af_output.f90:465-552): n_pixels[0] x n_pixels[1]
+ * points spanning r_min..r_max (3D: the plane of the two coordinates that
+ * differ most; the first of the smallest |r_max - r_min| is dropped) into
+ * filename + ".vtk", legacy ASCII STRUCTURED_POINTS with the reference's
+ * E20.8 number format. */
+int afg_write_plane(afg_ctx* ctx, const char* filename, int n_iv, const int* ivs,
+                    const char* const* names, const double* r_min,
+                    const double* r_max, const int* n_pixels);
+
+/* af_write_numpy (m_af_output.f90:756-901): the cell centres of a uniform
+ * grid over r_min..r_max (NULL: the domain) with n_points[ndim] cells (NULL:
+ * the spacing of the lowest level with a leaf in the region), interpolated.
+ * filename ending in ".npy": one Fortran-ordered float64 array
+ * (nx, ny[, nz], n_iv); ".npz": an uncompressed archive of one array per
+ * variable under its name plus nx, r_min, r_max, dr, coord_t and
+ * time_cycle. */
+int afg_write_numpy(afg_ctx* ctx, const char* filename, const double* r_min,
+                    const double* r_max, const int* n_points, int n_cycle,
+                    double time, int n_iv, const int* ivs,
+                    const char* const* names);
+
 /* Synchronise the context's stream and check the device error word. */
 int afg_sync(afg_ctx* ctx);
 
