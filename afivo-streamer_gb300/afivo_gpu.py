@@ -81,6 +81,45 @@ class MgDesc(C.Structure):
     ]
 
 
+LSF_SPHERE, LSF_ROD, LSF_ROD_CONE_TOP, LSF_ROD_ROD, LSF_SPHERE_ROD, LSF_TWO_ROD_CONE, LSF_COAXIAL = range(1, 8)
+
+
+class LsfDesc(C.Structure):
+    """afg_lsf_desc: the electrode of a field solve (absolute coordinates)."""
+    _fields_ = [
+        ("shape", C.c_int), ("i_lsf", C.c_int),
+        ("r0", C.c_double * 3), ("r1", C.c_double * 3), ("radius", C.c_double),
+        ("r2_0", C.c_double * 3), ("r2_1", C.c_double * 3), ("radius2", C.c_double),
+        ("cone_tip_radius", C.c_double), ("cone_length_frac", C.c_double),
+        ("cone2_tip_radius", C.c_double), ("cone2_length_frac", C.c_double),
+        ("center", C.c_double * 3),
+        ("grounded", C.c_int), ("grounded2", C.c_int),
+        ("length_scale", C.c_double), ("gradient_safety_factor", C.c_double),
+        ("tol", C.c_double), ("min_rel_distance", C.c_double),
+    ]
+
+
+def lsf_desc(shape, i_lsf, r0, r1=None, radius=0.0, r2_0=None, r2_1=None, radius2=0.0, cone_tip_radius=0.0,
+             cone_length_frac=0.0, cone2_tip_radius=0.0, cone2_length_frac=0.0, center=None, grounded=False,
+             grounded2=False, length_scale=None, gradient_safety_factor=1.5, tol=1e-8, min_rel_distance=1e-4):
+    """An afg_lsf_desc with the reference's mg_t defaults (m_af_types.f90:
+    604-619) and length_scale = radius as src/m_field.f90:389 sets it."""
+    d = LsfDesc()
+    d.shape, d.i_lsf = shape, i_lsf
+    for name, v in (("r0", r0), ("r1", r1), ("r2_0", r2_0), ("r2_1", r2_1), ("center", center)):
+        if v is not None:
+            arr = getattr(d, name)
+            for k, x in enumerate(v):
+                arr[k] = x
+    d.radius, d.radius2 = radius, radius2
+    d.cone_tip_radius, d.cone_length_frac = cone_tip_radius, cone_length_frac
+    d.cone2_tip_radius, d.cone2_length_frac = cone2_tip_radius, cone2_length_frac
+    d.grounded, d.grounded2 = int(grounded), int(grounded2)
+    d.length_scale = radius if length_scale is None else length_scale
+    d.gradient_safety_factor, d.tol, d.min_rel_distance = gradient_safety_factor, tol, min_rel_distance
+    return d
+
+
 AFG_MAX_SPECIES = 16
 AFG_MAX_REACTIONS = 32
 AFG_MAX_FLUX = 8
@@ -287,6 +326,9 @@ def load_library(path: str = LIB_PATH):
         "afg_host_unregister": (C.c_int, [P, C.c_void_p]),
         "afg_sync": (C.c_int, [P]),
         "afg_launch_count": (C.c_longlong, [P]),
+        "afg_mg_set_lsf": (C.c_int, [P, C.c_int, C.POINTER(LsfDesc)]),
+        "afg_mg_set_lsf_voltage": (C.c_int, [P, C.c_int, C.c_double]),
+        "afg_mg_lsf_info": (C.c_int, [P, C.c_int, _IP, _IP, _DP, _DP, _DP, _DP]),
         "afg_write_vtk": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double, C.c_int, _IP, C.POINTER(C.c_char_p)]),
         "afg_leaf_cells": (C.c_int, [P, C.c_int, _DP, C.POINTER(C.c_longlong)]),
         "afg_interp1": (C.c_int, [P, C.c_longlong, _DP, C.c_int, _IP, _DP, _IP]),
@@ -631,6 +673,28 @@ class Context:
         a = np.zeros(6)
         a[:len(vals)] = vals
         self.check(self.lib.afg_mg_set_bc_values(self.ptr, mg_id, _dp(a)), "afg_mg_set_bc_values")
+
+    def mg_set_lsf(self, mg_id, desc: LsfDesc):
+        self.check(self.lib.afg_mg_set_lsf(self.ptr, mg_id, C.byref(desc)), "afg_mg_set_lsf")
+
+    def mg_set_lsf_voltage(self, mg_id, voltage):
+        self.check(self.lib.afg_mg_set_lsf_voltage(self.ptr, mg_id, float(voltage)), "afg_mg_set_lsf_voltage")
+
+    def mg_lsf_info(self, mg_id, ndim, n_cell):
+        """(ids, v[n][2D+1][SI], f[n][SI], bcc[n][SI], dd[n][2D][SI])"""
+        n = C.c_int(0)
+        self.check(self.lib.afg_mg_lsf_info(self.ptr, mg_id, C.byref(n), None, None, None, None, None),
+                   "afg_mg_lsf_info")
+        n = n.value
+        SI = n_cell ** ndim
+        ids = np.zeros(max(1, n), dtype=np.int32)
+        v = np.zeros((max(1, n), 2 * ndim + 1, SI))
+        f = np.zeros((max(1, n), SI))
+        bcc = np.zeros((max(1, n), SI))
+        dd = np.zeros((max(1, n), 2 * ndim, SI))
+        self.check(self.lib.afg_mg_lsf_info(self.ptr, mg_id, None, _ip(ids), _dp(v), _dp(f), _dp(bcc), _dp(dd)),
+                   "afg_mg_lsf_info")
+        return ids[:n], v[:n], f[:n], bcc[:n], dd[:n]
 
     def mg_set_bc_values_inst(self, mg_id, vals):
         """vals[q][face] per instance of a batched tree."""

@@ -45,10 +45,17 @@ struct KTree {
   // loops leave the boxes of a frozen instance untouched.
   const int* inst;
   const int* frozen;
+  // electrode boxes of the solve in progress (index of the box's electrode
+  // data or -1; null without an electrode): the kernels of ordinary boxes
+  // skip them, the electrode kernels (afg_lsf.cuh) process them
+  const int* lsf;
 };
 
 // maxima slots per instance in the device maxima array ([instance][slot])
 constexpr int kMaxSlotsDev = 24;
+
+// an electrode box of the solve in progress (handled by afg_lsf.cuh)
+__device__ __forceinline__ bool lsf_box(const KTree& t, int slot) { return t.lsf != nullptr && t.lsf[slot] >= 0; }
 
 __device__ __forceinline__ bool box_frozen(const KTree& t, int slot) {
   return t.frozen != nullptr && t.frozen[t.inst[slot]] != 0;

@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(256) k_gsrb(KTree t0, const int* __restrict__ 
                                               const T* __restrict__ rhs, int redblack, MgCoef<T> mc) {
   const KTree t = fix_dims<D, NC>(t0);
   const int slot = list[blockIdx.x];
-  if (box_frozen(t, slot)) return;
+  if (box_frozen(t, slot) || lsf_box(t, slot)) return;
   const int nc = t.nc, n2 = t.n2, hn = nc / 2;
   T c[7];
   for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(256, 6) k_gsrb_fused(KTree t0, const int* __re
   const T* __restrict__ rhs = rhs_.get();
   const MgCoef<T> mc = mc_.get();
   const int slot = list[blockIdx.x];
-  if (box_frozen(t, slot)) return;
+  if (box_frozen(t, slot) || lsf_box(t, slot)) return;
   const int nc = t.nc, n2 = t.n2, hn = nc / 2;
   T c[7];
   for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(256) k_residual(KTree t0, const int* __restric
   const KTree t = fix_dims<D, NC>(t0);
   __shared__ T sred[32];
   const int slot = list[blockIdx.x];
-  if (box_frozen(t, slot)) return;
+  if (box_frozen(t, slot) || lsf_box(t, slot)) return;
   const int nc = t.nc, n2 = t.n2;
   T c[7];
   for (int q = 0; q < 7; q++) c[q] = mc.cb[slot * 8 + q];
@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(256) k_residual_restrict(KTree t0, const int* 
   int4 r0, r1;
   load_rec(rec, blockIdx.x, r0, r1);
   const int slot = r0.x;
-  if (box_frozen(t, slot)) return;
+  if (box_frozen(t, slot) || lsf_box(t, slot)) return;
   const int pslot = t.parent[slot];
   const int nc = t.nc, n2 = t.n2, hnc = nc / 2;
   T c[7];
@@ -543,7 +543,7 @@ __global__ void __launch_bounds__(256) k_coarse_fas(KTree t0, const int* __restr
   int4 r0, r1;
   load_rec(rec, blockIdx.x, r0, r1);
   const int slot = r0.x;
-  if (box_frozen(t, slot)) return;
+  if (box_frozen(t, slot) || lsf_box(t, slot)) return;
   const int nc = t.nc, n2 = t.n2;
   if (fill) {
     T* a = phi + (size_t)slot * t.S;

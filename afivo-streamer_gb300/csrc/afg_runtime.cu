@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <string>
 #include <type_traits>
 #include <utility>
@@ -22,6 +23,7 @@
 
 #include "../../include/afivo_gpu.h"
 #include "afg_common.cuh"
+#include "afg_lsf.h"
 #include "afg_gc_kernels.cuh"
 #include "afg_mg_kernels.cuh"
 #include "afg_mg32.cuh"
@@ -41,8 +43,41 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
+// Electrode (level-set) data of a multigrid slot (afg_lsf.cuh): per box
+// crossed by the electrode surface the stencil, boundary-value factor,
+// boundary values, rhs correction and distances; lists per level.
+struct LsfState {
+  afg_lsf::Electrode e{};
+  int i_lsf = 0;
+  double voltage = 0.0;
+  int SI = 0;
+  int n = 0;                  // electrode boxes
+  std::vector<int> h_slots;   // [n]
+  int* d_idx = nullptr;       // [n_boxes] electrode index or -1
+  int* d_slots = nullptr;     // [n]
+  double* d_v = nullptr;      // [n][2D+1][SI]
+  double* d_f = nullptr;      // [n][SI]
+  double* d_bcc = nullptr;    // [n][SI]
+  double* d_bv = nullptr;     // [n][SI]
+  double* d_dd = nullptr;     // [n][2D][SI]
+  std::vector<double> h_v1;   // stencils of the level-1 electrode boxes (coarse matrix)
+  std::vector<int> h_q1;      // their electrode indices
+  std::vector<std::vector<int>> lvl_all, lvl_par, lvl_leaf;  // per level, slots
+  int* d_lists = nullptr;
+  std::vector<size_t> off_all, off_par, off_leaf;
+  int n_cb = 0;               // level-1 electrode cells: coarse unknown, flat cell index
+  int* d_cb_g = nullptr;
+  int* d_cb_k = nullptr;
+  ~LsfState() {
+    for (void* p : {(void*)d_idx, (void*)d_slots, (void*)d_v, (void*)d_f, (void*)d_bcc, (void*)d_bv, (void*)d_dd,
+                    (void*)d_lists, (void*)d_cb_g, (void*)d_cb_k})
+      if (p) cudaFree(p);
+  }
+};
+
 struct MgSlot {
   bool used = false;
+  LsfState* lsf = nullptr;  // electrode of the field solve (afg_mg_set_lsf)
   afg_mg_desc d{};
   int n_coarse = 0;
   double* d_ainv = nullptr;
@@ -184,6 +219,9 @@ struct afg_ctx {
   std::map<std::string, Graph> graphs;
   bool use_graphs = true;
   bool fused_gsrb = true;
+  // electrode boxes of the multigrid slot whose kernels are being launched
+  // (KTree::lsf), set by LsfScope
+  const int* cur_lsf = nullptr;
   bool capturing = false;
 };
 
@@ -255,8 +293,18 @@ static KTree ktree(const afg_ctx* c) {
   t.idrf = c->d_idrf;
   t.inst = c->n_inst > 0 ? c->d_inst : nullptr;
   t.frozen = c->n_inst > 0 ? c->d_frozen : nullptr;
+  t.lsf = c->cur_lsf;
   return t;
 }
+
+// the electrode boxes of slot m are skipped by the ordinary kernels launched
+// while this scope lives
+struct LsfScope {
+  afg_ctx* c;
+  const int* prev;
+  LsfScope(afg_ctx* c_, const MgSlot& m) : c(c_), prev(c_->cur_lsf) { c->cur_lsf = m.lsf ? m.lsf->d_idx : nullptr; }
+  ~LsfScope() { c->cur_lsf = prev; }
+};
 
 // instance rows of the per-instance tables (1 for a single tree)
 static int inst_rows(const afg_ctx* c) { return c->n_inst > 0 ? c->n_inst : 1; }
@@ -339,6 +387,8 @@ static void free_tree(afg_ctx* c) {
     dfree(m.d_ainv); dfree(m.d_b); dfree(m.d_x); dfree(m.d_b2r); dfree(m.d_bmask); dfree(m.d_bcval);
     dfree(m.e32); dfree(m.r32); dfree(m.t32);
     dfree(m.d_cb64); dfree(m.d_cb32); dfree(m.d_cy64); dfree(m.d_cy32);
+    delete m.lsf;
+    m.lsf = nullptr;
     m.used = false;
   }
   transport_free(c->tr);
@@ -561,7 +611,7 @@ static int launch_gsrb_fused(afg_ctx* ctx, const int* list, int n, ModeArg<T> ph
     }
   }
   // the usual box sizes: several cells per thread (tuned), box records
-  if (gsrb_rec_specialized(ctx)) {
+  if (gsrb_rec_specialized(ctx) && ctx->cur_lsf == nullptr) {
     const int rc = launch_gsrb_rec<T>(ctx, rec_of(ctx, list), n, phi, rhs, rb, lam, g, gsrb_cpt_of<T>(ctx));
     if (rc != AFG_OK) return rc;
   } else if (ctx->D == 3)
@@ -830,6 +880,30 @@ static GcDev mg_gc(const afg_ctx* ctx, const MgSlot& m, bool homogeneous) {
   return g;
 }
 
+#include "afg_lsf.cuh"
+
+// the electrode boxes' part of the restriction and of the FAS update (FP64)
+template <typename T>
+static int lsf_rrestrict(afg_ctx* ctx, const MgSlot& m, int lvl, ModeArg<T> phi, ModeArg<T> rhs, ModeArg<T> tmp,
+                         int store_child, const GcDev& g, int otf) {
+  if (!m.lsf) return AFG_OK;
+  if constexpr (std::is_same<T, double>::value) {
+    return launch_lsf_rrestrict(ctx, m, lvl, phi.p[0], rhs.p[0], tmp.p[0], store_child, g, otf);
+  } else {
+    return fail(ctx, AFG_ERR_UNSUPPORTED, "electrode boxes in an FP32 solve");
+  }
+}
+template <typename T>
+static int lsf_coarse_fas(afg_ctx* ctx, const MgSlot& m, int plvl, ModeArg<T> phi, ModeArg<T> rhs, ModeArg<T> tmp,
+                          int copy_tmp, int fill, const GcDev& g) {
+  if (!m.lsf) return AFG_OK;
+  if constexpr (std::is_same<T, double>::value) {
+    return launch_lsf_coarse_fas(ctx, m, plvl, phi.p[0], rhs.p[0], tmp.p[0], copy_tmp, fill, g);
+  } else {
+    return fail(ctx, AFG_ERR_UNSUPPORTED, "electrode boxes in an FP32 solve");
+  }
+}
+
 template <typename T>
 static int mg_gc_lvl(afg_ctx* ctx, int lvl, ModeArg<T> phi, const GcDev& g, int corners) {
   return launch_gc<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, g, corners);
@@ -844,6 +918,17 @@ static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, ModeA
   const int* list = lst(ctx, ctx->off_ids[lvl - 1]);
   const int n = (int)ctx->lvl_ids[lvl - 1].size();
   ctx->ctr[1] += (long long)n * (long long)box_cells(ctx) * n_cycle * ctx->ky;
+  LsfScope lsc(ctx, m);
+  // the electrode boxes' half sweep after the ordinary boxes' (otf: ghost
+  // values on the fly as the fused smoother's, else the stored ones)
+  auto lsf_sweep = [&](int it, int otf) -> int {
+    if (!m.lsf) return AFG_OK;
+    if constexpr (std::is_same<T, double>::value) {
+      return launch_lsf_gsrb(ctx, m, lvl, phi.p[0], const_cast<double*>(rhs.p[0]), it, g, otf);
+    } else {
+      return fail(ctx, AFG_ERR_UNSUPPORTED, "electrode boxes in an FP32 solve");
+    }
+  };
   if (ctx->fused_gsrb) {
     int it0 = 1;
     if (stored_first) {
@@ -851,10 +936,14 @@ static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, ModeA
       // the fill that follows it in the reference (gsrb_boxes)
       if (ctx->ky != 1 || rb_of<T>(ctx)) return fail(ctx, AFG_ERR_STATE, "stored-ghost half sweep: one FP64 problem");
       RC(launch_gsrb<T>(ctx, list, n, phi.p[0], rhs.p[0], 1, coef_of<T>(m)));
+      RC(lsf_sweep(1, 0));
       RC(launch_gc<T>(ctx, list, n, phi, g, 0));
       it0 = 2;
     }
-    for (int it = it0; it <= 2 * n_cycle; it++) RC(launch_gsrb_fused<T>(ctx, list, n, phi, rhs, it, coefs<T>(ctx, m), g));
+    for (int it = it0; it <= 2 * n_cycle; it++) {
+      RC(launch_gsrb_fused<T>(ctx, list, n, phi, rhs, it, coefs<T>(ctx, m), g));
+      RC(lsf_sweep(it, 1));
+    }
     if (type == AFG_CYCLE_DOWN && !fill_down) return AFG_OK;
     if (type != AFG_CYCLE_DOWN && fill_needed_only)
       return launch_gc<T>(ctx, lst(ctx, ctx->off_gcneed[lvl - 1]), (int)ctx->lvl_gcneed[lvl - 1].size(), phi, g, 1);
@@ -863,6 +952,7 @@ static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, ModeA
   // unfused reference order (one problem at a time)
   for (int it = 1; it <= 2 * n_cycle; it++) {
     RC(launch_gsrb<T>(ctx, list, n, phi.p[0], rhs.p[0], it, coef_of<T>(m)));
+    RC(lsf_sweep(it, 0));
     const int corners = (type != AFG_CYCLE_DOWN && it == 2 * n_cycle) ? 1 : 0;
     RC(launch_gc<T>(ctx, list, n, phi, g, corners));
   }
@@ -877,10 +967,13 @@ static int mg_gsrb_boxes(afg_ctx* ctx, const MgSlot& m, int lvl, int type, ModeA
 template <typename T>
 static int mg_update_coarse(afg_ctx* ctx, const MgSlot& m, int lvl, ModeArg<T> phi, ModeArg<T> rhs, ModeArg<T> tmp,
                             const GcDev& g, bool otf = true) {
+  LsfScope lsc(ctx, m);
   RC(launch_rrestrict<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs, tmp,
                          coefs<T>(ctx, m), 0, g, otf ? 1 : 0));
+  RC(lsf_rrestrict<T>(ctx, m, lvl, phi, rhs, tmp, 0, g, otf ? 1 : 0));
   RC(launch_coarse_fas<T>(ctx, lst(ctx, ctx->off_parents[lvl - 2]), (int)ctx->lvl_parents[lvl - 2].size(), phi, rhs,
                           tmp, coefs<T>(ctx, m), 1, 1, g));
+  RC(lsf_coarse_fas<T>(ctx, m, lvl - 1, phi, rhs, tmp, 1, 1, g));
   return AFG_OK;
 }
 
@@ -888,12 +981,15 @@ static int mg_update_coarse(afg_ctx* ctx, const MgSlot& m, int lvl, ModeArg<T> p
 template <typename T>
 static int mg_set_coarse_phi_rhs(afg_ctx* ctx, const MgSlot& m, int lvl, ModeArg<T> phi, ModeArg<T> rhs,
                                  ModeArg<T> tmp, const GcDev& g) {
+  LsfScope lsc(ctx, m);
   if (lvl == ctx->highest_lvl) RC(mg_gc_lvl<T>(ctx, lvl, phi, g, 1));
   RC(launch_rrestrict<T>(ctx, lst(ctx, ctx->off_ids[lvl - 1]), (int)ctx->lvl_ids[lvl - 1].size(), phi, rhs, tmp,
                          coefs<T>(ctx, m), 1, g, 0));
+  RC(lsf_rrestrict<T>(ctx, m, lvl, phi, rhs, tmp, 1, g, 0));
   RC(mg_gc_lvl<T>(ctx, lvl - 1, phi, g, 1));
   RC(launch_coarse_fas<T>(ctx, lst(ctx, ctx->off_parents[lvl - 2]), (int)ctx->lvl_parents[lvl - 2].size(), phi, rhs,
                           tmp, coefs<T>(ctx, m), 0, 0, g));
+  RC(lsf_coarse_fas<T>(ctx, m, lvl - 1, phi, rhs, tmp, 0, 0, g));
   return AFG_OK;
 }
 
@@ -933,6 +1029,7 @@ static int mg_coarse_solve(afg_ctx* ctx, MgSlot& m, ModeArg<T> phi, ModeArg<cons
                                                     bcv, stride, rhs, cstride, b);
   ctx->launches++;
   CKL();
+  if (m.lsf && !homogeneous) RC(launch_lsf_coarse_bcc(ctx, m, m.d_b));
   k_coarse_matvec<<<g8, 256, 0, ctx->stream>>>(n, nloc, ainv, ModeArg<const double>(b), x);
   ctx->launches++;
   CKL();
@@ -958,6 +1055,15 @@ static int inst_mask(afg_ctx* ctx, int lo, int hi) {
 template <typename T>
 static int mg_residual_lvls(afg_ctx* ctx, const MgSlot& m, int max_lvl, const T* phi, const T* rhs, T* tmp,
                             unsigned long long* maxbits) {
+  LsfScope lsc(ctx, m);
+  if (m.lsf) {
+    if constexpr (std::is_same<T, double>::value) {
+      const GcDev g = mg_gc(ctx, m, false);
+      for (int lvl = 1; lvl <= max_lvl; lvl++) RC(launch_lsf_residual(ctx, m, lvl, phi, rhs, tmp, g, maxbits));
+    } else {
+      return fail(ctx, AFG_ERR_UNSUPPORTED, "electrode boxes in an FP32 solve");
+    }
+  }
   if (max_lvl == ctx->highest_lvl)  // boxes are independent: one launch over all levels
     return launch_residual<T>(ctx, lst(ctx, ctx->off_all), ctx->n_all, phi, rhs, tmp, coef_of<T>(m), maxbits);
   for (int lvl = 1; lvl <= max_lvl; lvl++)
@@ -2131,12 +2237,24 @@ static int build_coarse(afg_ctx* ctx, MgSlot& m) {
     c[0] = -sum - m.d.helmholtz_lambda;
     const bool cyl = ctx->coord == AFG_CYL;
     const int kn = D == 3 ? nc : 1;
+    // electrode boxes: their own variable stencil (no cylindrical factors:
+    // the axisymmetric term is part of it)
+    const double* vq = nullptr;
+    if (m.lsf) {
+      const LsfState& L = *m.lsf;
+      for (size_t p = 0; p < L.lvl_all[0].size(); p++)
+        if (L.lvl_all[0][p] == s) vq = L.h_v1.data() + p * (size_t)(2 * D + 1) * L.SI;
+    }
     for (int k = 1; k <= kn; k++)
       for (int j = 1; j <= nc; j++)
         for (int i = 1; i <= nc; i++) {
           double st[7];
           for (int q = 0; q < 7; q++) st[q] = c[q];
-          if (cyl) {
+          if (vq) {
+            const int cix = (i - 1) + nc * ((j - 1) + nc * (k - 1));
+            const int SI = m.lsf->SI;
+            for (int q = 0; q < 7; q++) st[q] = q <= 2 * D ? vq[(size_t)q * SI + cix] : 0.0;
+          } else if (cyl) {
             const double r = hrm[0] + (i - 0.5) * h[0];
             const double inv_r = 1 / r;
             const double f1 = (r - 0.5 * h[0]) * inv_r, f2 = (r + 0.5 * h[0]) * inv_r;
@@ -2256,6 +2374,8 @@ int afg_mg_setup(afg_ctx* ctx, int mg_id, const afg_mg_desc* d) {
   dfree(m.d_ainv); dfree(m.d_b); dfree(m.d_x); dfree(m.d_b2r); dfree(m.d_bmask); dfree(m.d_bcval);
   dfree(m.e32); dfree(m.r32); dfree(m.t32);
   dfree(m.d_cb64); dfree(m.d_cb32); dfree(m.d_cy64); dfree(m.d_cy32);
+  delete m.lsf;
+  m.lsf = nullptr;
   m.used = false;
   m.d = *d;
   RC(build_coarse(ctx, m));
@@ -2605,3 +2725,4 @@ int afg_kernel_stats(afg_ctx* ctx, long long* launches, double* ms, double* byte
 #include "afg_transport_api.cuh"
 #include "afg_amr.cuh"
 #include "afg_output.cuh"
+#include "afg_lsf_api.cuh"

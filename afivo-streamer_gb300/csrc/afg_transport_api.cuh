@@ -504,6 +504,11 @@ int afg_field_from_potential(afg_ctx* ctx, int i_phi) {
       AFG_NC2(NCV_, k_field_grad<2, NCV_><<<ctx->n_all, 256, 0, ctx->stream>>>(t, lst(ctx, ctx->off_all), ctx->cc[i_phi - 1], efc, en));
     ctx->launches++;
     CKL();
+    // faces next to the electrode surface on electrode leaf boxes
+    if (const MgSlot* ms = lsf_slot_of(ctx, i_phi)) {
+      if (mixed_transport(ctx)) return fail(ctx, AFG_ERR_UNSUPPORTED, "electrode field in an FP32 transport model");
+      RC(launch_lsf_grad(ctx, *ms, ctx->cc[i_phi - 1], efc, en));
+    }
     }
     return afg_gc(ctx, d.i_electric_fld, 0, 1);
   });
@@ -626,8 +631,13 @@ int afg_field_compute(afg_ctx* ctx, int mg_id, int s_in, int have_guess, double 
   CK(cudaMemcpy(hdr.data(), ctx->d_dr + (size_t)s_fine * ctx->D, sizeof(double) * ctx->D, cudaMemcpyDeviceToHost));
   double min_dr = hdr[0];
   for (int q = 1; q < ctx->D; q++) min_dr = std::min(min_dr, hdr[q]);
+  // with an electrode the round-off estimate is less strict (conv_fac
+  // 1e-8, m_field.f90:468-473) and the electrode gets the voltage or 0
+  // (mg%lsf_boundary_value, 482-487)
+  const double conv_fac = m->lsf ? 1e-8 : 1e-10;
+  if (m->lsf) RC(lsf_set_voltage(ctx, *m, voltage));
   const double threshold =
-      std::max(std::max(1e-6, max_rhs * max_rel_residual), 1e-10 * std::fabs(voltage) / (domain_len * min_dr));
+      std::max(std::max(1e-6, max_rhs * max_rel_residual), conv_fac * std::fabs(voltage) / (domain_len * min_dr));
   int nc_done = 0;
   double r = 0;
   // A mixed-precision slot runs FMG in FP32, whose residual floor on fine

@@ -628,6 +628,61 @@ int afg_kernel_stats_all(afg_ctx* ctx, long long* launches, double* ms, double* 
 int afg_maxabs_noalloc(const double* d_pool, const int* d_slots, int n_slots,
                        int ndim, int n_cell, void* stream, double* result);
 
+/* ---- electrode: internal Dirichlet boundary given by a level set --------
+ * The electrode of the field solve (src/m_field.f90:255-390 with the shapes
+ * of 672-904; afivo/src/m_af_multigrid.f90:954-1853): tree%mg_i_lsf,
+ * mg%lsf, mg%lsf_dist => mg_lsf_dist_gss, mg%lsf_length_scale.
+ * Coordinates are absolute (the reference's relative positions times the
+ * domain length plus the origin). */
+#define AFG_LSF_SPHERE         1   /* sphere_lsf: centre r0, radius          */
+#define AFG_LSF_ROD            2   /* rod_lsf: segment r0-r1, radius         */
+#define AFG_LSF_ROD_CONE_TOP   3   /* conical_rod_lsf                        */
+#define AFG_LSF_ROD_ROD        4   /* rod_rod_lsf, rod_rod_get_potential     */
+#define AFG_LSF_SPHERE_ROD     5   /* sphere_rod_lsf, sphere_rod_get_potential */
+#define AFG_LSF_TWO_ROD_CONE   6   /* two_conical_rods_lsf / _get_potential  */
+#define AFG_LSF_COAXIAL        7   /* coaxial_lsf, coaxial_get_potential     */
+
+typedef struct afg_lsf_desc {
+  int shape;                 /* AFG_LSF_*                                    */
+  int i_lsf;                 /* 1-based cell variable receiving the level set */
+  double r0[3], r1[3];       /* field_rod_r0 / field_rod_r1 (sphere: r0)      */
+  double radius;             /* field_rod_radius                             */
+  double r2_0[3], r2_1[3];   /* field_rod2_r0 / field_rod2_r1                */
+  double radius2;            /* field_rod2_radius                            */
+  double cone_tip_radius, cone_length_frac;    /* rod_cone_top, electrode 1  */
+  double cone2_tip_radius, cone2_length_frac;  /* two_rod_cone_electrodes    */
+  double center[3];          /* coaxial: the domain centre (axis position)   */
+  int grounded, grounded2;   /* field_electrode_grounded / 2                 */
+  double length_scale;       /* mg%lsf_length_scale (field_rod_radius)       */
+  double gradient_safety_factor; /* mg%lsf_gradient_safety_factor (1.5)      */
+  double tol;                /* mg%lsf_tol (1e-8)                            */
+  double min_rel_distance;   /* mg%lsf_min_rel_distance (1e-4)               */
+} afg_lsf_desc;
+
+/* Electrode of an FP64 Poisson slot (helmholtz_lambda = 0), after
+ * afg_mg_setup and again after every tree change: the level-set values of
+ * every box (set_lsf_box, ghost cells included) into i_lsf, the boxes the
+ * surface crosses (root mask, boundary distances by golden-section search
+ * and bisection, mg_set_box_tag 1100-1145), their stencils
+ * (mg_box_lsf_stencil 1779-1853), the coarse-grid matrix with those
+ * stencils; boundary value 0 until afg_mg_set_lsf_voltage or
+ * afg_field_compute (which passes its voltage).  AFG_ERR_ARG when no
+ * level-1 box contains a boundary (check_coarse_representation_lsf
+ * 2144-2161).  The electrode's custom prolongation
+ * (mg%lsf_use_custom_prolongation, off by default) is not provided. */
+int afg_mg_set_lsf(afg_ctx* ctx, int mg_id, const afg_lsf_desc* d);
+
+/* current_voltage for the electrode boundary values: bc_correction =
+ * f * boundary value (mg_set_operators_lvl 1169-1174). */
+int afg_mg_set_lsf_voltage(afg_ctx* ctx, int mg_id, double voltage);
+
+/* The electrode boxes of a slot: *n_boxes, and with non-NULL arrays their
+ * ids (level order) and per box the stencil v[2*ndim+1][nc^ndim], the
+ * boundary-value factor f, the rhs correction bcc and the distances
+ * dd[2*ndim][nc^ndim] (cells i fastest). */
+int afg_mg_lsf_info(afg_ctx* ctx, int mg_id, int* n_boxes, int* ids, double* v,
+                    double* f, double* bcc, double* dd);
+
 /* ---- output (afivo/src/m_af_output.f90) --------------------------------
  * The device-resident state written without a copy of the tree to the host:
  * the device gathers leaf cells, generates the mesh or interpolates, and

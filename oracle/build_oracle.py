@@ -18,7 +18,8 @@ def build(force: bool = False) -> str:
     srcs = [os.path.join(HERE, s) for s in SOURCES if os.path.exists(os.path.join(HERE, s))]
     deps = srcs + [os.path.join(HERE, "oracle_common.h"),
                    os.path.join(HERE, "..", "include", "afivo_gpu.h"),
-                   os.path.join(HERE, "..", "afivo-streamer_gb300", "csrc", "afg_math.h")]
+                   os.path.join(HERE, "..", "afivo-streamer_gb300", "csrc", "afg_math.h"),
+                   os.path.join(HERE, "..", "afivo-streamer_gb300", "csrc", "afg_lsf.h")]
     if not force and os.path.exists(LIB):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in deps if os.path.exists(d)):

@@ -56,6 +56,9 @@ def lib():
             "orc_prolong_linear": (C.c_int, [P, DP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
             "orc_restrict_tree": (C.c_int, [P, DP, C.c_int]),
             "orc_math_eval": (C.c_int, [C.c_int, C.c_int, DP, DP, DP]),
+            "orc_mg_set_lsf": (C.c_int, [P, DP, C.c_int, C.POINTER(ag.LsfDesc)]),
+            "orc_mg_set_lsf_voltage": (C.c_int, [P, C.c_int, C.c_double]),
+            "orc_mg_lsf_info": (C.c_int, [P, C.c_int, IP, IP, DP, DP, DP, DP]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -108,6 +111,28 @@ class Oracle:
         a = np.zeros(6)
         a[:len(vals)] = vals
         self._ck(self.L.orc_mg_set_bc_values(self.p, mg_id, _dp(a)), "mg_set_bc_values")
+
+    def mg_set_lsf(self, cc, mg_id, desc):
+        self._ck(self.L.orc_mg_set_lsf(self.p, _dp(cc), mg_id, C.byref(desc)), "mg_set_lsf")
+
+    def mg_set_lsf_voltage(self, mg_id, voltage):
+        self._ck(self.L.orc_mg_set_lsf_voltage(self.p, mg_id, float(voltage)), "mg_set_lsf_voltage")
+
+    def mg_lsf_info(self, mg_id):
+        t = self.tree
+        D, SI = t.ndim, t.n_cell ** t.ndim
+        n = C.c_int(0)
+        self._ck(self.L.orc_mg_lsf_info(self.p, mg_id, C.byref(n), None, None, None, None, None), "lsf_info")
+        n = n.value
+        ids = np.zeros(max(1, n), dtype=np.int32)
+        v = np.zeros((max(1, n), 2 * D + 1, SI))
+        f = np.zeros((max(1, n), SI))
+        bcc = np.zeros((max(1, n), SI))
+        dd = np.zeros((max(1, n), 2 * D, SI))
+        IPt = C.POINTER(C.c_int)
+        self._ck(self.L.orc_mg_lsf_info(self.p, mg_id, None, ids.ctypes.data_as(IPt), _dp(v), _dp(f), _dp(bcc),
+                                        _dp(dd)), "lsf_info")
+        return ids[:n], v[:n], f[:n], bcc[:n], dd[:n]
 
     def coarse_inverse(self, mg_id):
         n = self.L.orc_mg_coarse_inverse(self.p, mg_id, None, 0)

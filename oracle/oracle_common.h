@@ -22,7 +22,10 @@
 #include <map>
 #include <vector>
 
+#include <memory>
+
 #include "../include/afivo_gpu.h"
+#include "../afivo-streamer_gb300/csrc/afg_lsf.h"
 
 namespace orc {
 
@@ -63,8 +66,28 @@ struct GcSpec {
   int rb;
 };
 
+/* Electrode of a multigrid problem (tree%mg_i_lsf, mg%lsf): per box the
+ * reference stores a distance matrix and a variable operator stencil
+ * (store_lsf_distance_matrix, mg_box_lsf_stencil, m_af_multigrid.f90:
+ * 977-1097, 1779-1853) with bc_correction = f * boundary value; here the
+ * boxes that have them, with the per-cell arrays (cells i fastest). */
+struct Lsf {
+  afg_lsf::Electrode e{};
+  int i_lsf = 0;
+  int SI = 0;
+  std::vector<int> q;      // [n_boxes] index of a box's data or -1
+  std::vector<int> ids;    // [n] electrode boxes, level order
+  std::vector<double> v;   // [n][2D+1][SI]
+  std::vector<double> f;   // [n][SI]
+  std::vector<double> bv;  // [n][SI]
+  std::vector<double> bcc; // [n][SI]
+  std::vector<double> dd;  // [n][2D][SI]
+  int of(int id) const { return q[id - 1]; }
+};
+
 struct Mg {
   afg_mg_desc d;
+  std::shared_ptr<Lsf> lsf;  // electrode (null: none)
   int n_coarse = 0;                // unknowns of the coarse grid
   int gx[3] = {1, 1, 1};           // coarse grid size in cells
   std::vector<double> ainv;        // dense inverse, row-major [n][n]

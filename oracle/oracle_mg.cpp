@@ -288,8 +288,67 @@ static void make_stencil(const Tree& t, const afg_mg_desc& m, int id, Stencil& s
   }
 }
 
+/* stencil_gsrb_357 with a variable stencil and bc_correction
+ * (m_af_stencil.f90:838-998): rhs += bcc on the interior, the half sweep
+ * dividing by v(1), rhs -= bcc; stored ghost cells */
+static void gsrb_box_lsf(const Tree& t, double* cc, const afg_mg_desc& m, const Lsf& L, int id, int redblack) {
+  const int q = L.of(id), SI = L.SI, nc = t.nc, D = t.D;
+  double* p = t.var(cc, id, m.i_phi);
+  double* f = t.var(cc, id, m.i_rhs);
+  const double* v = L.v.data() + (size_t)q * (2 * D + 1) * SI;
+  const double* bcc = L.bcc.data() + (size_t)q * SI;
+  const int kn = D == 3 ? nc : 1, sj = t.n2, sk = t.n2 * t.n2;
+  int c = 0;
+  for (int k = 1; k <= kn; k++)
+    for (int j = 1; j <= nc; j++)
+      for (int i = 1; i <= nc; i++, c++) {
+        const int x = t.at(i, j, D == 3 ? k : 0);
+        f[x] = f[x] + bcc[c];
+      }
+  c = 0;
+  for (int k = 1; k <= kn; k++)
+    for (int j = 1; j <= nc; j++)
+      for (int i = 1; i <= nc; i++, c++) {
+        if (((i + j + (D == 3 ? k : 0) + redblack) & 1) != 0) continue;
+        const int x = t.at(i, j, D == 3 ? k : 0);
+        double val = f[x] - v[(size_t)1 * SI + c] * p[x - 1] - v[(size_t)2 * SI + c] * p[x + 1] -
+                     v[(size_t)3 * SI + c] * p[x - sj] - v[(size_t)4 * SI + c] * p[x + sj];
+        if (D == 3) val = val - v[(size_t)5 * SI + c] * p[x - sk] - v[(size_t)6 * SI + c] * p[x + sk];
+        p[x] = val / v[c];
+      }
+  c = 0;
+  for (int k = 1; k <= kn; k++)
+    for (int j = 1; j <= nc; j++)
+      for (int i = 1; i <= nc; i++, c++) {
+        const int x = t.at(i, j, D == 3 ? k : 0);
+        f[x] = f[x] - bcc[c];
+      }
+}
+
+/* stencil_apply_357 with a variable stencil, then - bc_correction
+ * (m_af_stencil.f90:367-496) into out[c] (interior cells, i fastest) */
+static void apply_lsf(const Tree& t, const double* cc, const afg_mg_desc& m, const Lsf& L, int id, double* out) {
+  const int q = L.of(id), SI = L.SI, nc = t.nc, D = t.D;
+  const double* p = t.var(const_cast<double*>(cc), id, m.i_phi);
+  const double* v = L.v.data() + (size_t)q * (2 * D + 1) * SI;
+  const double* bcc = L.bcc.data() + (size_t)q * SI;
+  const int kn = D == 3 ? nc : 1, sj = t.n2, sk = t.n2 * t.n2;
+  int c = 0;
+  for (int k = 1; k <= kn; k++)
+    for (int j = 1; j <= nc; j++)
+      for (int i = 1; i <= nc; i++, c++) {
+        const int x = t.at(i, j, D == 3 ? k : 0);
+        double lp = v[c] * p[x] + v[(size_t)1 * SI + c] * p[x - 1] + v[(size_t)2 * SI + c] * p[x + 1] +
+                    v[(size_t)3 * SI + c] * p[x - sj] + v[(size_t)4 * SI + c] * p[x + sj];
+        if (D == 3) lp = lp + v[(size_t)5 * SI + c] * p[x - sk] + v[(size_t)6 * SI + c] * p[x + sk];
+        out[c] = lp - bcc[c];
+      }
+}
+
 /* stencil_gsrb_357, m_af_stencil.f90:838-998 */
-static void gsrb_box(const Tree& t, double* cc, const afg_mg_desc& m, int id, int redblack) {
+static void gsrb_box(const Tree& t, double* cc, const Mg& mg, int id, int redblack) {
+  if (mg.lsf && mg.lsf->of(id) >= 0) return gsrb_box_lsf(t, cc, mg.d, *mg.lsf, id, redblack);
+  const afg_mg_desc& m = mg.d;
   Stencil s;
   make_stencil(t, m, id, s);
   double* p = t.var(cc, id, m.i_phi);
@@ -328,8 +387,18 @@ static void gsrb_box(const Tree& t, double* cc, const afg_mg_desc& m, int id, in
 
 /* stencil_apply_357 (m_af_stencil.f90:367-496) then residual_box
  * (m_af_multigrid.f90:801-810): out = rhs - L phi on interior cells */
-static void residual_into(const Tree& t, const double* cc, const afg_mg_desc& m, int id,
+static void residual_into(const Tree& t, const double* cc, const Mg& mg, int id,
                           double* out /* nc^D, i fastest */) {
+  const afg_mg_desc& m = mg.d;
+  if (mg.lsf && mg.lsf->of(id) >= 0) {
+    apply_lsf(t, cc, m, *mg.lsf, id, out);
+    const double* f = t.var(const_cast<double*>(cc), id, m.i_rhs);
+    int c = 0;
+    for (int k = (t.D == 3 ? 1 : 0); k <= (t.D == 3 ? t.nc : 0); k++)
+      for (int j = 1; j <= t.nc; j++)
+        for (int i = 1; i <= t.nc; i++, c++) out[c] = f[t.at(i, j, k)] - out[c];
+    return;
+  }
   Stencil s;
   make_stencil(t, m, id, s);
   const double* p = t.var(const_cast<double*>(cc), id, m.i_phi);
@@ -363,7 +432,18 @@ static void residual_into(const Tree& t, const double* cc, const afg_mg_desc& m,
 }
 
 /* stencil_apply_357 alone into variable iv_out (interior) */
-static void apply_into(const Tree& t, double* cc, const afg_mg_desc& m, int id, int iv_out) {
+static void apply_into(const Tree& t, double* cc, const Mg& mg, int id, int iv_out) {
+  const afg_mg_desc& m = mg.d;
+  if (mg.lsf && mg.lsf->of(id) >= 0) {
+    std::vector<double> out(mg.lsf->SI);
+    apply_lsf(t, cc, m, *mg.lsf, id, out.data());
+    double* o = t.var(cc, id, iv_out);
+    int c = 0;
+    for (int k = (t.D == 3 ? 1 : 0); k <= (t.D == 3 ? t.nc : 0); k++)
+      for (int j = 1; j <= t.nc; j++)
+        for (int i = 1; i <= t.nc; i++, c++) o[t.at(i, j, k)] = out[c];
+    return;
+  }
   Stencil s;
   make_stencil(t, m, id, s);
   const double* p = t.var(cc, id, m.i_phi);
@@ -494,7 +574,7 @@ static void gsrb_boxes(Oracle& o, double* cc, const Mg& m, int lvl, int type) {
   const GcSpec g = m.gc();
   for (int n = 1; n <= 2 * n_cycle; n++) {
 #pragma omp parallel for schedule(static)
-    for (size_t i = 0; i < ids.size(); i++) gsrb_box(t, cc, m.d, ids[i], n);
+    for (size_t i = 0; i < ids.size(); i++) gsrb_box(t, cc, m, ids[i], n);
     const bool use_corners = (type != AFG_CYCLE_DOWN && n == 2 * n_cycle);
 #pragma omp parallel for schedule(static)
     for (size_t i = 0; i < ids.size(); i++) gc_box(t, cc, ids[i], m.d.i_phi, g, use_corners);
@@ -514,7 +594,7 @@ static void update_coarse(Oracle& o, double* cc, const Mg& m, int lvl) {
 #pragma omp for schedule(static)
     for (size_t i = 0; i < ids.size(); i++) {
       int id = ids[i];
-      residual_into(t, cc, m.d, id, r.data());
+      residual_into(t, cc, m, id, r.data());
       restrict_to_parent(t, cc, id, r.data(), false, m.d.i_tmp, true);
       restrict_to_parent(t, cc, id, t.var(cc, id, m.d.i_phi), true, m.d.i_phi, false);
     }
@@ -524,7 +604,7 @@ static void update_coarse(Oracle& o, double* cc, const Mg& m, int lvl) {
 #pragma omp parallel for schedule(static)
   for (size_t i = 0; i < par.size(); i++) {
     int id = par[i];
-    apply_into(t, cc, m.d, id, m.d.i_rhs);
+    apply_into(t, cc, m, id, m.d.i_rhs);
     double* f = t.var(cc, id, m.d.i_rhs);
     double* tm = t.var(cc, id, m.d.i_tmp);
     const double* p = t.var(cc, id, m.d.i_phi);
@@ -545,7 +625,7 @@ static void set_coarse_phi_rhs(Oracle& o, double* cc, const Mg& m, int lvl) {
 #pragma omp for schedule(static)
     for (size_t i = 0; i < ids.size(); i++) {
       int id = ids[i];
-      residual_into(t, cc, m.d, id, r.data());
+      residual_into(t, cc, m, id, r.data());
       double* tm = t.var(cc, id, m.d.i_tmp);
       int n = 0;
       for (int k = (t.D == 3 ? 1 : 0); k <= (t.D == 3 ? t.nc : 0); k++)
@@ -560,7 +640,7 @@ static void set_coarse_phi_rhs(Oracle& o, double* cc, const Mg& m, int lvl) {
 #pragma omp parallel for schedule(static)
   for (size_t i = 0; i < par.size(); i++) {
     int id = par[i];
-    apply_into(t, cc, m.d, id, m.d.i_rhs);
+    apply_into(t, cc, m, id, m.d.i_rhs);
     double* f = t.var(cc, id, m.d.i_rhs);
     double* tm = t.var(cc, id, m.d.i_tmp);
     for (int x = 0; x < t.S; x++) f[x] = f[x] + tm[x];
@@ -618,12 +698,19 @@ static int build_coarse(Oracle& o, Mg& m) {
     Stencil s;
     make_stencil(t, m.d, id, s);
     const int kn = D == 3 ? nc : 1;
+    // an electrode box: its variable stencil (stencil_get_357 of a
+    // variable stencil without cylindrical factors)
+    const double* vq = nullptr;
+    if (m.lsf && m.lsf->of(id) >= 0) vq = m.lsf->v.data() + (size_t)m.lsf->of(id) * (2 * D + 1) * m.lsf->SI;
     for (int k = 1; k <= kn; k++)
       for (int j = 1; j <= nc; j++)
         for (int i = 1; i <= nc; i++) {
           double st[7];
           for (int q = 0; q < 7; q++) st[q] = s.c[q];
-          if (s.cyl) {  // stencil_get_357, m_af_stencil.f90:1073-1084
+          if (vq) {
+            const int c = (i - 1) + nc * ((j - 1) + nc * (k - 1));
+            for (int q = 0; q < 7; q++) st[q] = q <= 2 * D ? vq[(size_t)q * m.lsf->SI + c] : 0.0;
+          } else if (s.cyl) {  // stencil_get_357, m_af_stencil.f90:1073-1084
             st[1] = s.cyl2[i];
             st[2] = s.cyl3[i];
             st[0] = s.cyl1[i];
@@ -749,6 +836,11 @@ static void coarse_solve(Oracle& o, double* cc, const Mg& m) {
             int p = d == 0 ? (D == 3 ? j + nc * (k - 1) : j) : (d == 1 ? (D == 3 ? i + nc * (k - 1) : i) : i + nc * (j - 1));
             v = v + m.bc_to_rhs[(bi * t.nnb() + nb) * fn + (p - 1)] * m.d.bc_val[nb];
           }
+          // the level-set term lsf_fac * boundary value (m_coarse_solver.f90:323-327)
+          if (m.lsf && m.lsf->of(id) >= 0) {
+            const int c = (i - 1) + nc * ((j - 1) + nc * (k - 1));
+            v = v + m.lsf->bcc[(size_t)m.lsf->of(id) * m.lsf->SI + c];
+          }
           long I = (long)(t.ix_of(id, 0) - 1) * nc + (i - 1);
           long J = (long)(t.ix_of(id, 1) - 1) * nc + (j - 1);
           long K = D == 3 ? (long)(t.ix_of(id, 2) - 1) * nc + (k - 1) : 0;
@@ -819,7 +911,7 @@ static void residual_lvls(Oracle& o, double* cc, const Mg& m, int max_lvl) {
 #pragma omp for schedule(static)
       for (size_t i = 0; i < ids.size(); i++) {
         int id = ids[i];
-        residual_into(t, cc, m.d, id, r.data());
+        residual_into(t, cc, m, id, r.data());
         double* tm = t.var(cc, id, m.d.i_tmp);
         int n = 0;
         for (int k = (t.D == 3 ? 1 : 0); k <= (t.D == 3 ? t.nc : 0); k++)
@@ -1052,6 +1144,161 @@ int orc_mg_solve(void* p, double* cc, int mg_id, double threshold, int max_cycle
 double orc_maxabs(void* p, const double* cc, int iv, int leaves_only) {
   Oracle* o = static_cast<Oracle*>(p);
   return maxabs(o->t, cc, iv, leaves_only != 0);
+}
+
+}  // extern "C"
+
+/* ---- electrode (level set) -------------------------------------------- */
+namespace orc {
+
+/* get_conical_rod_properties (src/m_field.f90:406-428); the cone length
+ * uses electrode 1's cone_length_frac for either electrode, as there */
+static void conical_props(const double* r0, const double* r1, int D, double radius, double tip_radius,
+                          double cone_frac, double* center, double& r_curv) {
+  double h[3];
+  for (int d = 0; d < D; d++) h[d] = r1[d] - r0[d];
+  const double len = afg_lsf::norm2(h, D);
+  const double angle = std::atan((radius - tip_radius) / (cone_frac * len));
+  r_curv = tip_radius / std::cos(angle);
+  for (int d = 0; d < D; d++) center[d] = r1[d] - std::sin(angle) * r_curv * (r1[d] - r0[d]) / len;
+}
+
+/* mg_lsf_boundary_value (m_coarse_solver.f90:494-511) per electrode cell
+ * and bc_correction = f * value (mg_set_operators_lvl,
+ * m_af_multigrid.f90:1169-1174) */
+static void lsf_voltage(const Tree& t, Lsf& L, double voltage) {
+  const int SI = L.SI, nc = t.nc, D = t.D;
+  for (size_t q = 0; q < L.ids.size(); q++) {
+    const int id = L.ids[q];
+    for (int c = 0; c < SI; c++) {
+      const int ix[3] = {c % nc + 1, (c / nc) % nc + 1, D == 3 ? c / (nc * nc) + 1 : 0};
+      double r[3];
+      for (int d = 0; d < D; d++) r[d] = t.rmin_of(id, d) + (ix[d] - 0.5) * t.dr_of(id, d);
+      const double b = afg_lsf::boundary_value(L.e, r, voltage);
+      L.bv[q * SI + c] = b;
+      L.bcc[q * SI + c] = L.f[q * SI + c] * b;
+    }
+  }
+}
+
+}  // namespace orc
+
+extern "C" {
+
+/* tree%mg_i_lsf / mg%lsf for problem mg_id: set_lsf_box on every box
+ * (src/m_field.f90:673-683), mg_set_box_tag + store_lsf_distance_matrix
+ * (m_af_multigrid.f90:977-1145) and mg_box_lsf_stencil (1779-1853) for the
+ * boxes with a boundary, the coarse matrix with their stencils
+ * (coarse_solver_initialize); boundary value 0 */
+int orc_mg_set_lsf(void* p, double* cc, int mg_id, const afg_lsf_desc* d) {
+  Oracle* o = static_cast<Oracle*>(p);
+  auto it = o->mg.find(mg_id);
+  if (it == o->mg.end()) return AFG_ERR_STATE;
+  Mg& m = it->second;
+  const Tree& t = o->t;
+  const int D = t.D, nc = t.nc;
+  auto L = std::make_shared<Lsf>();
+  afg_lsf::Electrode& e = L->e;
+  e.shape = d->shape;
+  e.D = D;
+  e.cyl = t.coord == AFG_CYL;
+  for (int k = 0; k < 3; k++) {
+    e.r0[k] = d->r0[k], e.r1[k] = d->r1[k], e.q0[k] = d->r2_0[k], e.q1[k] = d->r2_1[k];
+    e.center[k] = d->center[k];
+  }
+  e.radius = d->radius;
+  e.radius2 = d->radius2;
+  e.tip_radius = d->cone_tip_radius;
+  e.cone_frac = d->cone_length_frac;
+  e.tip_radius2 = d->cone2_tip_radius;
+  e.cone_frac2 = d->cone2_length_frac;
+  e.grounded = d->grounded;
+  e.grounded2 = d->grounded2;
+  e.length_scale = d->length_scale;
+  e.safety = d->gradient_safety_factor;
+  e.tol = d->tol;
+  e.min_rel = d->min_rel_distance;
+  if (e.shape == AFG_LSF_ROD_CONE_TOP || e.shape == AFG_LSF_TWO_ROD_CONE)
+    conical_props(e.r0, e.r1, D, e.radius, e.tip_radius, e.cone_frac, e.tip_center, e.r_curv);
+  if (e.shape == AFG_LSF_TWO_ROD_CONE)
+    conical_props(e.q0, e.q1, D, e.radius2, e.tip_radius2, e.cone_frac, e.tip_center2, e.r_curv2);
+  L->i_lsf = d->i_lsf;
+  L->SI = D == 2 ? nc * nc : nc * nc * nc;
+  const int SI = L->SI;
+  L->q.assign(t.n_boxes, -1);
+  for (int lvl = 1; lvl <= t.highest_lvl; lvl++) {
+    for (int id : t.ids[lvl - 1]) {
+      // set_lsf_box: all cells, ghost cells included
+      double* a = t.var(cc, id, d->i_lsf);
+      for (int x = 0; x < t.S; x++) {
+        const int ix[3] = {x % t.n2, (x / t.n2) % t.n2, D == 3 ? x / (t.n2 * t.n2) : 0};
+        double r[3];
+        for (int dd = 0; dd < D; dd++) r[dd] = t.rmin_of(id, dd) + (ix[dd] - 0.5) * t.dr_of(id, dd);
+        a[x] = afg_lsf::eval(e, r);
+      }
+      // distances of every interior cell; a box with one below 1 is an
+      // electrode box
+      double rm[3], h[3];
+      for (int dd = 0; dd < D; dd++) rm[dd] = t.rmin_of(id, dd), h[dd] = t.dr_of(id, dd);
+      std::vector<double> dist((size_t)2 * D * SI);
+      bool any = false;
+      for (int c = 0; c < SI; c++) {
+        const int ix[3] = {c % nc + 1, (c / nc) % nc + 1, D == 3 ? c / (nc * nc) + 1 : 0};
+        double dv[6];
+        afg_lsf::cell_distances(e, rm, h, ix, dv);
+        for (int n = 0; n < 2 * D; n++) {
+          dist[(size_t)n * SI + c] = dv[n];
+          any = any || dv[n] < 1.0;
+        }
+      }
+      if (!any) continue;
+      const int q = (int)L->ids.size();
+      L->q[id - 1] = q;
+      L->ids.push_back(id);
+      L->dd.insert(L->dd.end(), dist.begin(), dist.end());
+      std::vector<double> v((size_t)(2 * D + 1) * SI), f(SI);
+      for (int c = 0; c < SI; c++) {
+        double dv[6], w[7], fv;
+        for (int n = 0; n < 2 * D; n++) dv[n] = dist[(size_t)n * SI + c];
+        afg_lsf::cell_stencil(D, e.cyl != 0, rm, h, c % nc + 1, dv, w, fv);
+        for (int n = 0; n <= 2 * D; n++) v[(size_t)n * SI + c] = w[n];
+        f[c] = fv;
+      }
+      L->v.insert(L->v.end(), v.begin(), v.end());
+      L->f.insert(L->f.end(), f.begin(), f.end());
+    }
+  }
+  bool coarse_root = false;
+  for (int id : t.ids[0]) coarse_root = coarse_root || L->q[id - 1] >= 0;
+  if (!coarse_root) return AFG_ERR_ARG;  // check_coarse_representation_lsf
+  L->bv.assign(L->ids.size() * SI, 0.0);
+  L->bcc.assign(L->ids.size() * SI, 0.0);
+  lsf_voltage(t, *L, 0.0);
+  m.lsf = L;
+  return build_coarse(*o, m);
+}
+
+int orc_mg_set_lsf_voltage(void* p, int mg_id, double voltage) {
+  Oracle* o = static_cast<Oracle*>(p);
+  auto it = o->mg.find(mg_id);
+  if (it == o->mg.end() || !it->second.lsf) return AFG_ERR_STATE;
+  lsf_voltage(o->t, *it->second.lsf, voltage);
+  return AFG_OK;
+}
+
+int orc_mg_lsf_info(void* p, int mg_id, int* n_boxes, int* ids, double* v, double* f, double* bcc, double* dd) {
+  Oracle* o = static_cast<Oracle*>(p);
+  auto it = o->mg.find(mg_id);
+  if (it == o->mg.end() || !it->second.lsf) return AFG_ERR_STATE;
+  const Lsf& L = *it->second.lsf;
+  const int n = (int)L.ids.size();
+  if (n_boxes) *n_boxes = n;
+  if (ids) std::memcpy(ids, L.ids.data(), sizeof(int) * n);
+  if (v) std::memcpy(v, L.v.data(), sizeof(double) * L.v.size());
+  if (f) std::memcpy(f, L.f.data(), sizeof(double) * L.f.size());
+  if (bcc) std::memcpy(bcc, L.bcc.data(), sizeof(double) * L.bcc.size());
+  if (dd) std::memcpy(dd, L.dd.data(), sizeof(double) * L.dd.size());
+  return AFG_OK;
 }
 
 }  // extern "C"

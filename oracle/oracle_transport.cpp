@@ -650,6 +650,10 @@ int orc_field_from_potential(void* p, double* cc, double* fc, int i_phi) {
   const Tree& t = o->t;
   const afg_transport_desc& d = g_tr.d;
   const int nc = t.nc, D = t.D;
+  // the electrode of the field whose potential this is
+  const Lsf* L = nullptr;
+  for (const auto& kv : o->mg)
+    if (kv.second.lsf && kv.second.d.i_phi == i_phi) L = kv.second.lsf.get();
   for (int lvl = 1; lvl <= t.highest_lvl; lvl++) {
     const std::vector<int>& ids = t.ids[lvl - 1];
 #pragma omp parallel for schedule(static)
@@ -669,6 +673,34 @@ int orc_field_from_potential(void* p, double* cc, double* fc, int i_phi) {
             F[1][fc_at(t, j, i, k)] = inv_dr[1] * (ph[t.at(j, i, kc)] - ph[t.at(j, i - 1, kc)]);
             if (D == 3) F[2][fc_at(t, j, k, i)] = inv_dr[2] * (ph[t.at(j, k, i)] - ph[t.at(j, k, i - 1)]);
           }
+      // mg_box_lpllsf_gradient (m_af_multigrid.f90:2049-2141) on electrode
+      // boxes without children: faces next to a boundary point from cells
+      // with lsf >= 0, in the order of the stored cells
+      bool has_children = false;
+      for (int c = 0; c < t.nchild(); c++) has_children = has_children || t.child_of(id, c) > 0;
+      if (L && L->of(id) >= 0 && !has_children) {
+        const int q = L->of(id), SI = L->SI;
+        const double* dd = L->dd.data() + (size_t)q * 2 * D * SI;
+        const double* bv = L->bv.data() + (size_t)q * SI;
+        const double* ls = t.var(cc, id, L->i_lsf);
+        for (int c = 0; c < SI; c++) {
+          bool any = false;
+          for (int n = 0; n < 2 * D; n++) any = any || dd[(size_t)n * SI + c] < 1.0;
+          if (!any) continue;
+          const int i = c % nc + 1, j = (c / nc) % nc + 1, k = D == 3 ? c / (nc * nc) + 1 : 0;
+          const int kk = D == 3 ? k : 1;
+          const int x = t.at(i, j, k);
+          for (int n = 0; n < 2 * D; n++) {
+            const double dn = dd[(size_t)n * SI + c];
+            if (!(dn < 1 && ls[x] >= 0)) continue;
+            const int dim = n / 2;
+            const bool hi = n % 2;
+            int fi = i, fj = j, fk = kk;
+            if (hi) (dim == 0 ? fi : dim == 1 ? fj : fk) += 1;
+            F[dim][fc_at(t, fi, fj, fk)] = hi ? inv_dr[dim] * (bv[c] - ph[x]) / dn : inv_dr[dim] * (ph[x] - bv[c]) / dn;
+          }
+        }
+      }
       double* en = t.var(cc, id, d.i_electric_fld);
       for (int k = 1; k <= kn; k++)
         for (int j = 1; j <= nc; j++)
