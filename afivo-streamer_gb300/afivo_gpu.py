@@ -162,6 +162,7 @@ class RefineDesc(C.Structure):
         ("region_rmax", _R3 * AFG_MAX_REFINE_ITEMS), ("region_dr", C.c_double * AFG_MAX_REFINE_ITEMS),
         ("n_limits", C.c_int), ("limit_rmin", _R3 * AFG_MAX_REFINE_ITEMS),
         ("limit_rmax", _R3 * AFG_MAX_REFINE_ITEMS), ("limit_dr", C.c_double * AFG_MAX_REFINE_ITEMS),
+        ("electrode_mg", C.c_int), ("electrode_dx", C.c_double),
     ]
 
 
@@ -327,6 +328,9 @@ def load_library(path: str = LIB_PATH):
         "afg_sync": (C.c_int, [P]),
         "afg_launch_count": (C.c_longlong, [P]),
         "afg_mg_set_lsf": (C.c_int, [P, C.c_int, C.POINTER(LsfDesc)]),
+        "afg_transport_set_electrode": (C.c_int, [P, C.c_int]),
+        "afg_electrode_init_densities": (C.c_int, [P, C.c_int, C.c_int, _IP]),
+        "afg_electrode_species_bc": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int]),
         "afg_mg_set_lsf_voltage": (C.c_int, [P, C.c_int, C.c_double]),
         "afg_mg_lsf_info": (C.c_int, [P, C.c_int, _IP, _IP, _DP, _DP, _DP, _DP]),
         "afg_write_vtk": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double, C.c_int, _IP, C.POINTER(C.c_char_p)]),
@@ -676,6 +680,18 @@ class Context:
 
     def mg_set_lsf(self, mg_id, desc: LsfDesc):
         self.check(self.lib.afg_mg_set_lsf(self.ptr, mg_id, C.byref(desc)), "afg_mg_set_lsf")
+
+    def transport_set_electrode(self, i_lsf):
+        self.check(self.lib.afg_transport_set_electrode(self.ptr, int(i_lsf)), "afg_transport_set_electrode")
+
+    def electrode_init_densities(self, mg_id, ids):
+        a = np.ascontiguousarray(ids, dtype=np.int32)
+        self.check(self.lib.afg_electrode_init_densities(self.ptr, mg_id, len(a), _ip(a)),
+                   "afg_electrode_init_densities")
+
+    def electrode_species_bc(self, mg_id, electron, ion, neumann=True):
+        self.check(self.lib.afg_electrode_species_bc(self.ptr, mg_id, electron, ion, int(neumann)),
+                   "afg_electrode_species_bc")
 
     def mg_set_lsf_voltage(self, mg_id, voltage):
         self.check(self.lib.afg_mg_set_lsf_voltage(self.ptr, mg_id, float(voltage)), "afg_mg_set_lsf_voltage")

@@ -20,7 +20,8 @@ namespace afg {
 template <int D>
 __global__ void __launch_bounds__(128) k_refine_flags(KTree t, const int* __restrict__ list,
                                                       const double* __restrict__ E, const double* __restrict__ ne,
-                                                      LtDev lt, afg_refine_desc a, int* __restrict__ flags) {
+                                                      LtDev lt, afg_refine_desc a, int* __restrict__ flags,
+                                                      const int* __restrict__ lsf_idx) {
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2;
   __shared__ int s_do, s_keep;
@@ -105,6 +106,8 @@ __global__ void __launch_bounds__(128) k_refine_flags(KTree t, const int* __rest
       const double dist = sqrt(s2);
       if (dist - a.seed_width[n] < 2 * max_dx && max_dx > a.init_fac * a.seed_width[n]) f = AFG_REF_DO;
     }
+    // refine around the electrode: boxes the electrode surface crosses
+    if (lsf_idx != nullptr && lsf_idx[slot] >= 0 && a.electrode_dx > 0 && max_dx > a.electrode_dx) f = AFG_REF_DO;
     // fixed regions mark the centre cell, limits turn do into keep
     const bool centre = i == hc && j == hc && (D == 2 || k == hc);
     if (centre && in_region) f = AFG_REF_DO;
@@ -274,6 +277,11 @@ int afg_refine_flags(afg_ctx* ctx, const afg_refine_desc* d, int* box_flags) {
     return fail(ctx, AFG_ERR_ARG, "too many refinement seeds, regions or limits");
   if (d->ref_buffer < 0 || d->ref_buffer > ctx->nc) return fail(ctx, AFG_ERR_ARG, "bad ref_buffer");
   if (!(d->gas_number_density > 0) || !(d->adx_fac > 0)) return fail(ctx, AFG_ERR_ARG, "bad gas density or adx_fac");
+  // the electrode boxes of the field's slot (box tag mg_lsf_box)
+  const int* lidx = nullptr;
+  if (d->electrode_mg >= 0 && d->electrode_mg < kMaxMg && ctx->mg[d->electrode_mg].used &&
+      ctx->mg[d->electrode_mg].lsf)
+    lidx = ctx->mg[d->electrode_mg].lsf->d_idx;
   const int n = ctx->n_boxes;
   // the leaves, and every parent of a leaf once (consistent_ref_flags
   // evaluates it for the first of its children that is not refined)
@@ -308,9 +316,9 @@ int afg_refine_flags(afg_ctx* ctx, const afg_refine_desc* d, int* box_flags) {
     const double* E = ctx->cc[d->i_electric_fld - 1];
     const double* ne = ctx->cc[d->i_electron - 1];
     if (ctx->D == 3)
-      k_refine_flags<3><<<(int)list.size(), 128, 0, ctx->stream>>>(t, d_list, E, ne, lt_dev(ctx), *d, d_flags);
+      k_refine_flags<3><<<(int)list.size(), 128, 0, ctx->stream>>>(t, d_list, E, ne, lt_dev(ctx), *d, d_flags, lidx);
     else
-      k_refine_flags<2><<<(int)list.size(), 128, 0, ctx->stream>>>(t, d_list, E, ne, lt_dev(ctx), *d, d_flags);
+      k_refine_flags<2><<<(int)list.size(), 128, 0, ctx->stream>>>(t, d_list, E, ne, lt_dev(ctx), *d, d_flags, lidx);
     ctx->launches++;
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(box_flags, d_flags, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->stream);

@@ -437,6 +437,58 @@ __global__ void k_lsf_bcc(KTree t, const int* __restrict__ slots, afg_lsf::Elect
   }
 }
 
+/* ---- electrode rules of the streamer's densities ----------------------- */
+
+struct DensPtrs {
+  int ns;
+  double* p[AFG_MAX_SPECIES];
+};
+
+// init_cond_set_box's electrode rule (src/m_init_cond.f90:284-288), every
+// cell of the listed boxes, ghost cells included
+__global__ void k_electrode_init(int S, const int* __restrict__ list, const double* __restrict__ lsfv, DensPtrs dn) {
+  const size_t base = (size_t)list[blockIdx.x] * S;
+  for (int x = threadIdx.x; x < S; x += blockDim.x)
+    if (lsfv[base + x] <= 0.0)
+      for (int s = 0; s < dn.ns; s++) dn.p[s][base + x] = 0.0;
+}
+
+// electrode_species_bc (src/streamer.f90:598-656) on electrode boxes: cells
+// inside the electrode lose their densities; next to a gas cell (and with
+// Neumann species boundaries) they take the mean electron density of their
+// gas neighbours, the ion density equal to it.  Only cells inside are
+// written and only gas cells read, so the cells are independent.
+template <int D>
+__global__ void k_electrode_species_bc(KTree t, const int* __restrict__ list, const double* __restrict__ lsfv,
+                                       DensPtrs dn, int ie, int ii, int neumann) {
+  const int slot = list[blockIdx.x];
+  const int nc = t.nc, n2 = t.n2, SI = D == 2 ? nc * nc : nc * nc * nc;
+  const size_t base = (size_t)slot * t.S;
+  for (int c = threadIdx.x; c < SI; c += blockDim.x) {
+    int i, j, k;
+    lsf_ijk<D>(nc, c, i, j, k);
+    const int x = lsf_at<D>(n2, i, j, k);
+    if (!(lsfv[base + x] < 0)) continue;
+    for (int s = 0; s < dn.ns; s++) dn.p[s][base + x] = 0.0;
+    const int st[3] = {1, n2, n2 * n2};
+    bool any = false;
+    for (int nb = 0; nb < 2 * D; nb++) any = any || lsfv[base + x + ((nb & 1) ? 1 : -1) * st[nb >> 1]] > 0;
+    if (!(any && neumann)) continue;
+    double sum = 0.0;
+    int cnt = 0;
+    for (int nb = 0; nb < 2 * D; nb++) {
+      const int y = x + ((nb & 1) ? 1 : -1) * st[nb >> 1];
+      if (lsfv[base + y] > 0) {
+        sum = sum + dn.p[ie][base + y];
+        cnt++;
+      }
+    }
+    const double v = sum / (double)cnt;
+    dn.p[ie][base + x] = v;
+    dn.p[ii][base + x] = v;
+  }
+}
+
 }  // namespace afg
 
 /* ---- host side: launchers used by the multigrid driver ------------------ */

@@ -273,3 +273,79 @@ int afg_mg_lsf_info(afg_ctx* ctx, int mg_id, int* n_boxes, int* ids, double* v, 
   }
   return AFG_OK;
 }
+
+/* ---- the electrode in the species update and the initial state ---------- */
+
+int afg_transport_set_electrode(afg_ctx* ctx, int i_lsf) {
+  RC(need_transport(ctx));
+  if (i_lsf != 0) RC(check_var(ctx, i_lsf));
+  ctx->tr.mask_iv = i_lsf;
+  clear_graphs(ctx);
+  return AFG_OK;
+}
+
+static int electrode_dens(afg_ctx* ctx, afg::DensPtrs& dn) {
+  const afg_transport_desc& td = ctx->tr.d;
+  dn.ns = td.n_species;
+  for (int s = 0; s < td.n_species; s++) {
+    RC(check_var(ctx, td.species_iv[s]));
+    dn.p[s] = ctx->cc[td.species_iv[s] - 1];
+  }
+  return AFG_OK;
+}
+
+int afg_electrode_init_densities(afg_ctx* ctx, int mg_id, int n, const int* ids) {
+  RC(need_transport(ctx));
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  if (!m->lsf) return fail(ctx, AFG_ERR_STATE, "slot %d has no electrode", mg_id);
+  if (n < 0 || (n > 0 && !ids)) return fail(ctx, AFG_ERR_ARG, "bad box list");
+  if (n == 0) return AFG_OK;
+  afg::DensPtrs dn{};
+  RC(electrode_dens(ctx, dn));
+  std::vector<int> slots(n);
+  for (int q = 0; q < n; q++) {
+    if (ids[q] < 1 || ids[q] > ctx->n_boxes) return fail(ctx, AFG_ERR_ARG, "bad box id %d", ids[q]);
+    slots[q] = ids[q] - 1;
+  }
+  int* d_list = nullptr;
+  CK(dalloc(&d_list, n));
+  cudaError_t e = cudaMemcpyAsync(d_list, slots.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) {
+    afg::k_electrode_init<<<n, 128, 0, ctx->stream>>>(ctx->S, d_list, ctx->cc[m->lsf->i_lsf - 1], dn);
+    ctx->launches++;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  dfree(d_list);
+  if (e != cudaSuccess) return fail(ctx, AFG_ERR_CUDA, "electrode initial densities: %s", cudaGetErrorString(e));
+  return AFG_OK;
+}
+
+int afg_electrode_species_bc(afg_ctx* ctx, int mg_id, int electron, int ion, int neumann) {
+  RC(need_transport(ctx));
+  MgSlot* m;
+  RC(get_mg(ctx, mg_id, &m));
+  if (!m->lsf) return fail(ctx, AFG_ERR_STATE, "slot %d has no electrode", mg_id);
+  const afg_transport_desc& td = ctx->tr.d;
+  if (electron < 0 || electron >= td.n_species || ion < 0 || ion >= td.n_species)
+    return fail(ctx, AFG_ERR_ARG, "bad species index");
+  afg::DensPtrs dn{};
+  RC(electrode_dens(ctx, dn));
+  const LsfState& L = *m->lsf;
+  KTree t = ktree(ctx);
+  for (int lvl = 1; lvl <= ctx->highest_lvl; lvl++) {
+    const int n = (int)L.lvl_all[lvl - 1].size();
+    if (n == 0) continue;
+    if (ctx->D == 3)
+      afg::k_electrode_species_bc<3><<<n, 128, 0, ctx->stream>>>(t, L.d_lists + L.off_all[lvl - 1], ctx->cc[L.i_lsf - 1],
+                                                                  dn, electron, ion, neumann);
+    else
+      afg::k_electrode_species_bc<2><<<n, 128, 0, ctx->stream>>>(t, L.d_lists + L.off_all[lvl - 1], ctx->cc[L.i_lsf - 1],
+                                                                  dn, electron, ion, neumann);
+    ctx->launches++;
+    CKL();
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return AFG_OK;
+}

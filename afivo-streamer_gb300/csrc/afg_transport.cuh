@@ -27,6 +27,8 @@ struct TransportState {
   int n_rrb = 0;
   int* d_cflux = nullptr;              // pairs (slot, nb)
   int n_cflux = 0;
+  // electrode: the level-set variable whose cells <= 0 the update leaves out
+  int mask_iv = 0;
 };
 
 inline void transport_free(TransportState& s) {
@@ -433,6 +435,9 @@ struct UpdateArgs {
   double nmin;
   int limit_loss;
   unsigned long long* min_chem;  // bits of a non-negative double (atomicMin)
+  // electrode: level-set values; cells with lsf <= 0 keep the weighted
+  // previous states (set_box_mask, src/m_fluid.f90:469-515); null = none
+  const double* mask;
 };
 
 // x**c for the exponents of the analytic forms.  FP64: the project's pow
@@ -517,10 +522,22 @@ __global__ void __launch_bounds__(128) k_update(KTree t0, const int* __restrict_
   for (int q = 0; q < D; q++) dt_dr[q] = a.dt / t.dr[slot * D + q];
   double my_chem = 1e100;
   const size_t base = (size_t)slot * t.S;
+  // a box without gas cells adds no source terms and no chemistry limit
+  // (add_source_terms returns early, src/m_fluid.f90:332)
+  int any_gas = a.mask == nullptr ? 1 : 0;
+  if (a.mask != nullptr) {
+    for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
+      const int i = w % nc + 1, r = w / nc;
+      const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
+      any_gas |= a.mask[base + (D == 2 ? at2(n2, i, j) : at3(n2, i, j, k))] > 0.0;
+    }
+    any_gas = __syncthreads_or(any_gas);
+  }
   for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
     const int i = w % nc + 1, r = w / nc;
     const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
     const int x = D == 2 ? at2(n2, i, j) : at3(n2, i, j, k);
+    const bool gas = a.mask == nullptr || a.mask[base + x] > 0.0;
     double outv[NSMAX], dens[NSMAX], der[NSMAX];
 #pragma unroll
     for (int s = 0; s < NSMAX; s++) {
@@ -547,7 +564,7 @@ __global__ void __launch_bounds__(128) k_update(KTree t0, const int* __restrict_
       for (int q = 0; q < rc.n_in; q++) add_to<NSMAX>(der, rc.ix_in[q], -rate);
       for (int q = 0; q < rc.n_out; q++) add_to<NSMAX>(der, rc.ix_out[q], rate * rc.mult_out[q]);
     }
-    if (a.last_step) {
+    if (a.last_step && any_gas) {
       const double eps = 1e-100;
       double tmp = 1e100;
 #pragma unroll
@@ -564,6 +581,12 @@ __global__ void __launch_bounds__(128) k_update(KTree t0, const int* __restrict_
       const double ph = a.photo[base + x];
       add_to<NSMAX>(der, a.flux_species[0], ph);
       add_to<NSMAX>(der, a.photoi_species, ph);
+    }
+    if (!gas) {
+#pragma unroll
+      for (int s = 0; s < NSMAX; s++)
+        if (s < a.ns) a.out[s][base + x] = outv[s];
+      continue;
     }
 #pragma unroll
     for (int s = 0; s < NSMAX; s++) outv[s] = outv[s] + a.dt * der[s];

@@ -346,6 +346,9 @@ int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev, const
   a.nmin = d.dt_chemistry_nmin;
   a.limit_loss = d.dt_chemistry_limit_loss;
   a.min_chem = ctx->d_max + 5;
+  a.mask = ctx->tr.mask_iv > 0 ? ctx->cc[ctx->tr.mask_iv - 1] : nullptr;
+  if (mixed_transport(ctx) && a.mask != nullptr)
+    return fail(ctx, AFG_ERR_UNSUPPORTED, "electrode mask in the FP32 transport update");
   const double big = 1e100;
   unsigned long long bits;
   memcpy(&bits, &big, sizeof(bits));

@@ -68,6 +68,7 @@ class StreamerModel:
     # a transport table read from data (x in Td, its inv_fac, and the columns
     # mobility*N, diffusion*N, alpha/N, eta/N); replaces mu/dif/alpha/eta
     tabulated: dict = None
+    electrode: bool = False           # a level-set variable for the field's electrode
 
     # variable layout (1-based tree indices)
     def __post_init__(self):
@@ -86,6 +87,10 @@ class StreamerModel:
         self.i_modes = []
         for _ in range(self.photoi_modes):
             self.i_modes.append(nxt)
+            nxt += 1
+        self.i_lsf = 0
+        if self.electrode:
+            self.i_lsf = nxt
             nxt += 1
         self.n_var_cell = nxt - 1
         self.f_efield = 1

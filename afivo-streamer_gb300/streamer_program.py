@@ -127,6 +127,23 @@ class ProgramConfig:
         self.field_amplitude = g("field_amplitude", None)
         self.field_given_by = g("field_given_by", None, str, n=None)
         self.field_bc_type = g("field_bc_type", "homogeneous", str)
+        # electrode (m_streamer.f90:318-326, m_field.f90:196-229)
+        self.use_electrode = g("use_electrode", False, bool)
+        self.field_electrode_grounded = g("field_electrode_grounded", False, bool)
+        self.field_electrode2_grounded = g("field_electrode2_grounded", False, bool)
+        self.field_electrode_type = g("field_electrode_type", "rod", str)
+        self.field_rod_r0 = g("field_rod_r0", [-1.0e100] * D, n=D)
+        self.field_rod_r1 = g("field_rod_r1", [-1.0e100] * D, n=D)
+        self.field_rod2_r0 = g("field_rod2_r0", [-1.0e100] * D, n=D)
+        self.field_rod2_r1 = g("field_rod2_r1", [-1.0e100] * D, n=D)
+        self.field_rod_radius = g("field_rod_radius", -1.0e100)
+        self.field_rod2_radius = g("field_rod2_radius", -1.0e100)
+        self.cone_tip_radius = g("cone_tip_radius", -1.0e100)
+        self.cone_length_frac = g("cone_length_frac", -1.0e100)
+        self.cone2_tip_radius = g("cone2_tip_radius", -1.0e100)
+        self.cone2_length_frac = g("cone2_length_frac", -1.0e100)
+        self.refine_electrode_dx = g("refine_electrode_dx", 1e99)
+        self.electrode_derefine_factor = g("electrode_derefine_factor", 1.0)
         # m_transport_data.f90, m_table_data.f90
         self.input_data_file = g("input_data%file", None, str)
         self.input_data_old_style = g("input_data%old_style", False, bool)
@@ -205,7 +222,7 @@ class ProgramConfig:
     _IGNORED = {"output%name", "memory_limit_GB", "output%regression_test", "output%dt", "silo_write"}
     # keys whose given value must equal the supported one
     _FIXED = {
-        "use_electrode": False, "use_dielectric": False,
+        "use_dielectric": False,
         "gas%dynamics": False, "compute_power_density": False,
     }
 
@@ -230,6 +247,11 @@ class ProgramConfig:
                 raise Unsupported("field_given_by other than 'field <V/m>' or 'voltage <V>'")
         elif self.field_amplitude is None:
             raise ValueError("field_amplitude not specified")
+        if self.use_electrode:
+            if self.field_electrode_type not in ELECTRODE_SHAPES:
+                raise Unsupported(f"field_electrode_type = {self.field_electrode_type}")
+            if self.electrode_derefine_factor != 1.0:
+                raise Unsupported("electrode_derefine_factor other than 1")
         if self.species_boundary_condition != "neumann_zero" or self.prolong_density != "limit":
             raise Unsupported("species_boundary_condition / prolong_density other than the defaults")
         if self.time_integrator not in TIME_INTEGRATORS:
@@ -244,6 +266,36 @@ class ProgramConfig:
         unknown = set(self.raw) - self.used - self._IGNORED
         if unknown:
             raise Unsupported("configuration keys not supported on this path: " + ", ".join(sorted(unknown)))
+
+
+# field_electrode_type (src/m_field.f90:255-380) -> afg_lsf_desc shapes
+ELECTRODE_SHAPES = {
+    "sphere": ag.LSF_SPHERE, "rod": ag.LSF_ROD, "rod_cone_top": ag.LSF_ROD_CONE_TOP, "rod_rod": ag.LSF_ROD_ROD,
+    "sphere_rod": ag.LSF_SPHERE_ROD, "two_rod_cone_electrodes": ag.LSF_TWO_ROD_CONE, "coaxial": ag.LSF_COAXIAL,
+}
+
+
+def electrode_desc(cfg, i_lsf):
+    """The electrode of field_initialize (src/m_field.f90:255-390): positions
+    relative to the domain (times ST_domain_len plus ST_domain_origin),
+    mg%lsf_length_scale = field_rod_radius."""
+    D = cfg.ndim
+    L = np.asarray(cfg.domain_len, dtype=np.float64)
+    O = np.asarray(cfg.domain_origin, dtype=np.float64)
+
+    def absolute(rel):
+        return list(np.asarray(rel, dtype=np.float64) * L + O)
+    if cfg.field_rod_radius <= 0:
+        raise ValueError("set field_rod_radius to smallest length scale of electrode")
+    center = [0.0, O[1] + 0.5 * L[1]] if cfg.cylindrical else list(O + 0.5 * L)
+    return ag.lsf_desc(ELECTRODE_SHAPES[cfg.field_electrode_type], i_lsf,
+                       r0=absolute(cfg.field_rod_r0), r1=absolute(cfg.field_rod_r1), radius=cfg.field_rod_radius,
+                       r2_0=absolute(cfg.field_rod2_r0), r2_1=absolute(cfg.field_rod2_r1),
+                       radius2=cfg.field_rod2_radius, cone_tip_radius=cfg.cone_tip_radius,
+                       cone_length_frac=cfg.cone_length_frac, cone2_tip_radius=cfg.cone2_tip_radius,
+                       cone2_length_frac=cfg.cone2_length_frac, center=center,
+                       grounded=cfg.field_electrode_grounded, grounded2=cfg.field_electrode2_grounded,
+                       length_scale=cfg.field_rod_radius)
 
 
 # af_integrator_names (afivo/src/m_af_advance.f90) -> the stage tables of
@@ -599,7 +651,7 @@ def model_from_config(cfg: ProgramConfig) -> sm.StreamerModel:
     m = sm.StreamerModel(ndim=cfg.ndim, n_states=sm.states_needed(integ), N=N,
                          tabulated=dict(x=x, inv_fac=inv_fac, cols=cols),
                          photoi_modes=0 if photoi is None else len(photoi[0]),
-                         photoi_species_index=photoi_ix, **kw)
+                         photoi_species_index=photoi_ix, electrode=cfg.use_electrode, **kw)
     m.ix_pos_ion = ix_pos
     m.integrator = integ
     m.photoi_params = photoi
@@ -713,6 +765,9 @@ def refine_desc(cfg: ProgramConfig, model: sm.StreamerModel, time: float):
                           derefine_dx=cfg.derefine_dx, max_dx=cfg.refine_max_dx, min_dx=cfg.refine_min_dx,
                           ref_buffer=cfg.refine_buffer_width, init_fac=cfg.refine_init_fac,
                           use_alpha_effective=int(cfg.refine_use_alpha_effective))
+    if cfg.use_electrode:
+        # current_electrode_dx (src/streamer.f90:216-225; electrode_derefine_factor 1)
+        d.electrode_mg, d.electrode_dx = 0, cfg.refine_electrode_dx
     if time < cfg.refine_init_time:
         sd = seeds(cfg)
         if len(sd) > ag.AFG_MAX_REFINE_ITEMS:
@@ -886,6 +941,8 @@ class Program:
                 dt = min(dt, max(0.0, time_last_output + cfg.output_dt - time))
             if cfg.photoi_enabled and it % cfg.photoi_per_steps == 0:
                 eng.photoi()
+            if cfg.use_electrode:
+                eng.electrode_densities()
             dt_lim = 1e100
             for n in range(MAX_ATTEMPTS_PER_TIME_STEP):
                 lim = eng.advance(dt)
@@ -960,6 +1017,15 @@ class GpuEngine:
         self.run.setup()
         # rhs: af_bc_neumann_zero + af_gc_interp (src/streamer.f90:74-79)
         self.ctx.set_cc_methods(m.i_rhs, [ag.BC_NEUMANN] * (2 * self.tree.ndim), None, ag.RB_INTERP)
+        if m.electrode:
+            # the field's electrode on every box (set_lsf_box, mg_set_box_tag)
+            # and the update's gas mask
+            self.ctx.mg_set_lsf(0, electrode_desc(self.cfg, m.i_lsf))
+            self.ctx.transport_set_electrode(m.i_lsf)
+
+    def electrode_densities(self):
+        """set_electrode_densities (src/streamer.f90:590-594)."""
+        self.ctx.electrode_species_bc(0, 0, self.m.ix_pos_ion, True)
 
     def set_initial(self, ids, e, ion):
         m, t = self.m, self.tree
@@ -972,6 +1038,8 @@ class GpuEngine:
         keep[idx] = True
         bp.addr[~keep] = 0
         self.ctx.upload_vars(h, [m.species_iv[0], m.species_iv[m.ix_pos_ion]], bp=bp)
+        if m.electrode:
+            self.ctx.electrode_init_densities(0, ids)
 
     def field(self, have_guess):
         if not have_guess:

@@ -499,6 +499,10 @@ typedef struct afg_refine_desc {
   double limit_rmin[AFG_MAX_REFINE_ITEMS][3];
   double limit_rmax[AFG_MAX_REFINE_ITEMS][3];
   double limit_dr[AFG_MAX_REFINE_ITEMS];
+  int electrode_mg;            /* multigrid slot of the field's electrode   */
+  double electrode_dx;         /* current_electrode_dx: the electrode boxes
+                                  of that slot refine while max_dx exceeds it
+                                  (src/m_refine.f90:261-265); 0 = no rule  */
 } afg_refine_desc;
 
 /* The flag pass of consistent_ref_flags (afivo/src/m_af_core.f90:929-991)
@@ -682,6 +686,25 @@ int afg_mg_set_lsf_voltage(afg_ctx* ctx, int mg_id, double voltage);
  * dd[2*ndim][nc^ndim] (cells i fastest). */
 int afg_mg_lsf_info(afg_ctx* ctx, int mg_id, int* n_boxes, int* ids, double* v,
                     double* f, double* bcc, double* dd);
+
+/* The electrode in the streamer's species update and initial state:
+ * afg_transport_set_electrode(ctx, i_lsf) leaves the cells with level set
+ * <= 0 out of afg_update_densities' flux and source terms (set_box_mask,
+ * src/m_fluid.f90:469-515; a box without gas cells adds no chemistry time
+ * step limit); i_lsf = 0 switches it off.  FP64 transport only. */
+int afg_transport_set_electrode(afg_ctx* ctx, int i_lsf);
+
+/* init_cond_set_box's electrode rule (src/m_init_cond.f90:284-288): every
+ * cell (ghost cells included) of boxes ids[0..n-1] whose level set is <= 0
+ * gets zero densities of all transport species (state 0). */
+int afg_electrode_init_densities(afg_ctx* ctx, int mg_id, int n, const int* ids);
+
+/* set_electrode_densities / electrode_species_bc (src/streamer.f90:
+ * 590-656) on the electrode boxes of slot mg_id: cells with level set < 0
+ * get zero densities (state 0); with neumann != 0 (bc_species =
+ * af_bc_neumann_zero) a cell next to a gas cell gets the mean electron
+ * density of its gas neighbours, and the ion (species index ion) the same. */
+int afg_electrode_species_bc(afg_ctx* ctx, int mg_id, int electron, int ion, int neumann);
 
 /* ---- output (afivo/src/m_af_output.f90) --------------------------------
  * The device-resident state written without a copy of the tree to the host:

@@ -57,6 +57,9 @@ def lib():
             "orc_restrict_tree": (C.c_int, [P, DP, C.c_int]),
             "orc_math_eval": (C.c_int, [C.c_int, C.c_int, DP, DP, DP]),
             "orc_mg_set_lsf": (C.c_int, [P, DP, C.c_int, C.POINTER(ag.LsfDesc)]),
+            "orc_transport_set_electrode": (C.c_int, [P, C.c_int]),
+            "orc_electrode_init_densities": (C.c_int, [P, DP, C.c_int, C.c_int, IP]),
+            "orc_electrode_species_bc": (C.c_int, [P, DP, C.c_int, C.c_int, C.c_int, C.c_int]),
             "orc_mg_set_lsf_voltage": (C.c_int, [P, C.c_int, C.c_double]),
             "orc_mg_lsf_info": (C.c_int, [P, C.c_int, IP, IP, DP, DP, DP, DP]),
         }
@@ -114,6 +117,18 @@ class Oracle:
 
     def mg_set_lsf(self, cc, mg_id, desc):
         self._ck(self.L.orc_mg_set_lsf(self.p, _dp(cc), mg_id, C.byref(desc)), "mg_set_lsf")
+
+    def transport_set_electrode(self, i_lsf):
+        self._ck(self.L.orc_transport_set_electrode(self.p, int(i_lsf)), "transport_set_electrode")
+
+    def electrode_init_densities(self, cc, mg_id, ids):
+        a = np.ascontiguousarray(ids, dtype=np.int32)
+        self._ck(self.L.orc_electrode_init_densities(self.p, _dp(cc), mg_id, len(a),
+                                                     a.ctypes.data_as(C.POINTER(C.c_int))), "electrode_init")
+
+    def electrode_species_bc(self, cc, mg_id, electron, ion, neumann=True):
+        self._ck(self.L.orc_electrode_species_bc(self.p, _dp(cc), mg_id, electron, ion, int(neumann)),
+                 "electrode_species_bc")
 
     def mg_set_lsf_voltage(self, mg_id, voltage):
         self._ck(self.L.orc_mg_set_lsf_voltage(self.p, mg_id, float(voltage)), "mg_set_lsf_voltage")

@@ -55,6 +55,13 @@ class OracleEngine:
         self.o = self.run.o
         # rhs: af_bc_neumann_zero + af_gc_interp (src/streamer.f90:74-79)
         self.o.set_cc_methods(m.i_rhs, [ag.BC_NEUMANN] * (2 * tree.ndim), None, ag.RB_INTERP)
+        if m.electrode:
+            self.o.mg_set_lsf(cc, 0, sp.electrode_desc(cfg, m.i_lsf))
+            self.o.transport_set_electrode(m.i_lsf)
+
+    def electrode_densities(self):
+        """set_electrode_densities (src/streamer.f90:590-594)."""
+        self.o.electrode_species_bc(self.cc, 0, 0, self.m.ix_pos_ion, True)
 
     def set_initial(self, ids, e, ion):
         m = self.m
@@ -62,6 +69,8 @@ class OracleEngine:
         shp = (len(idx),) + self.cc.shape[2:]
         self.cc[idx, m.species_iv[0] - 1] = e.reshape(shp)
         self.cc[idx, m.species_iv[m.ix_pos_ion] - 1] = ion.reshape(shp)
+        if m.electrode:
+            self.o.electrode_init_densities(self.cc, 0, ids)
 
     def field(self, have_guess):
         if not have_guess:

@@ -104,7 +104,12 @@ class OracleStreamerRun:
         H = self.tree.highest_lvl
         o.field_set_rhs(cc, m.i_rhs, s_in)
         max_rhs = o.maxabs(cc, m.i_rhs)
-        thr = max(1e-6, max_rhs * self.rel, 1e-10 * abs(self.voltage) / (self.L * self.min_dr))
+        # with an electrode: conv_fac 1e-8 and the electrode at the voltage
+        # or grounded (field_compute, src/m_field.f90:468-487)
+        conv = 1e-8 if m.electrode else 1e-10
+        if m.electrode:
+            o.mg_set_lsf_voltage(0, self.voltage)
+        thr = max(1e-6, max_rhs * self.rel, conv * abs(self.voltage) / (self.L * self.min_dr))
         work = nv = 0
         if not have_guess:
             res = []

@@ -512,6 +512,14 @@ int orc_flux_upwind(void* p, double* cc, double* fc, int s_deriv, double* dt_lim
 }
 
 /* flux_update_densities + add_source_terms */
+/* the electrode's level-set variable for set_box_mask (0: none) */
+static int g_mask_iv = 0;
+
+int orc_transport_set_electrode(void*, int i_lsf) {
+  g_mask_iv = i_lsf;
+  return AFG_OK;
+}
+
 int orc_update_densities(void* p, double* cc, double* fc, double dt, int s_deriv, int n_prev, const int* s_prev,
                          const double* w_prev, int s_out, int last_step, double* dt_chem) {
   Oracle* o = static_cast<Oracle*>(p);
@@ -524,6 +532,14 @@ int orc_update_densities(void* p, double* cc, double* fc, double dt, int s_deriv
 #pragma omp parallel for schedule(static) reduction(min : chem)
     for (size_t bi = 0; bi < lv.size(); bi++) {
       const int id = lv[bi];
+      /* set_box_mask (src/m_fluid.f90:469-515): gas cells have lsf > 0;
+       * add_source_terms returns at once for a box without any (332) */
+      const double* lsf = g_mask_iv > 0 ? t.var(cc, id, g_mask_iv) : nullptr;
+      auto gas = [&](int x) { return lsf == nullptr || lsf[x] > 0.0; };
+      bool any_gas = false;
+      for (int k = (D == 3 ? 1 : 0); k <= (D == 3 ? nc : 0); k++)
+        for (int j = 1; j <= nc; j++)
+          for (int i = 1; i <= nc; i++) any_gas = any_gas || gas(t.at(i, j, k));
       double dt_dr[3];
       for (int q = 0; q < D; q++) dt_dr[q] = dt / t.dr_of(id, q);
       // weighted sum of previous states
@@ -565,6 +581,7 @@ int orc_update_densities(void* p, double* cc, double* fc, double dt, int s_deriv
               for (int q = 0; q < r.n_in; q++) der[r.ix_in[q]] = der[r.ix_in[q]] - rate;
               for (int q = 0; q < r.n_out; q++) der[r.ix_out[q]] = der[r.ix_out[q]] + rate * r.mult_out[q];
             }
+            if (!any_gas) continue;
             if (last_step) {
               const double eps = 1e-100;
               double tmp = 1e100;
@@ -580,6 +597,7 @@ int orc_update_densities(void* p, double* cc, double* fc, double dt, int s_deriv
               der[d.flux_species[0]] = der[d.flux_species[0]] + ph[x];
               der[d.photoi_species] = der[d.photoi_species] + ph[x];
             }
+            if (!gas(x)) continue;
             for (int s = 0; s < ns; s++) {
               double* out = t.var(cc, id, d.species_iv[s] + s_out);
               out[x] = out[x] + dt * der[s];
@@ -597,6 +615,7 @@ int orc_update_densities(void* p, double* cc, double* fc, double dt, int s_deriv
             for (int i = 1; i <= nc; i++) {
               const int x = t.at(i, j, k);
               const int kk = D == 3 ? k : 1;
+              if (!gas(x)) continue;
               if (D == 2 && t.coord == AFG_CYL) {
                 const double r = t.rmin_of(id, 0) + (i - 0.5) * t.dr_of(id, 0);
                 const double inv_r = 1 / r;
@@ -760,7 +779,7 @@ int orc_photoi_source(void* p, double* cc, double coeff, int i_rhs) {
 /* default_refinement (src/m_refine.f90:197-298) for one box: cell flags,
  * i fastest; constant gas density, no electrode boxes. */
 static void default_refinement(const Tree& t, const double* cc, int id, const afg_refine_desc& a,
-                               std::vector<int>& cf) {
+                               std::vector<int>& cf, const Lsf* L = nullptr) {
   const int nc = t.nc, D = t.D;
   const double* E = t.var(const_cast<double*>(cc), id, a.i_electric_fld);
   const double* ne = t.var(const_cast<double*>(cc), id, a.i_electron);
@@ -819,6 +838,9 @@ static void default_refinement(const Tree& t, const double* cc, int id, const af
           const double dist = std::sqrt(s2);
           if (dist - a.seed_width[n] < 2 * max_dx && max_dx > a.init_fac * a.seed_width[n]) f = AFG_REF_DO;
         }
+        /* refine around the electrode (src/m_refine.f90:261-265): boxes with
+         * the mg_lsf_box tag of the field */
+        if (L && L->of(id) >= 0 && a.electrode_dx > 0 && max_dx > a.electrode_dx) f = AFG_REF_DO;
         cf[(size_t)(i - 1) + nc * ((j - 1) + (size_t)nc * (k - 1))] = f;
       }
   double rmin[3], rmax[3];
@@ -896,9 +918,12 @@ int orc_refine_flags(void* p, const double* cc, const afg_refine_desc* a, int* f
   const Tree& t = o->t;
   const int unset = -2147483647 - 1;
   std::vector<int> rf(t.n_boxes, unset), cf;
+  const Lsf* L = nullptr;
+  auto mit = o->mg.find(a->electrode_mg);
+  if (mit != o->mg.end() && mit->second.lsf) L = mit->second.lsf.get();
   for (int lvl = 1; lvl <= t.highest_lvl; lvl++)
     for (int id : t.leaves[lvl - 1]) {
-      default_refinement(t, cc, id, *a, cf);
+      default_refinement(t, cc, id, *a, cf, L);
       cell_to_ref_flags(t, cf, id, a->ref_buffer, rf);
       if (lvl > 1) {
         const int p_id = t.parent[id - 1];
@@ -911,7 +936,7 @@ int orc_refine_flags(void* p, const double* cc, const afg_refine_desc* a, int* f
           if (t.child_of(ch_id, 0) <= 0) break;
         }
         if (i_ch == ich) {
-          default_refinement(t, cc, p_id, *a, cf);
+          default_refinement(t, cc, p_id, *a, cf, L);
           cell_to_ref_flags(t, cf, p_id, a->ref_buffer, rf);
         }
       }
@@ -1051,6 +1076,68 @@ int orc_restrict_tree(void* p, double* cc, int iv) {
 int orc_math_eval(int which, int n, const double* x, const double* y, double* out) {
   for (int q = 0; q < n; q++)
     out[q] = which == 0 ? afg_math::exp(x[q]) : which == 1 ? afg_math::log(x[q]) : afg_math::pow(x[q], y[q]);
+  return AFG_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+/* init_cond_set_box's electrode rule (src/m_init_cond.f90:284-288) on
+ * boxes ids[], every cell */
+int orc_electrode_init_densities(void* p, double* cc, int mg_id, int n, const int* ids) {
+  Oracle* o = static_cast<Oracle*>(p);
+  const Tree& t = o->t;
+  auto it = o->mg.find(mg_id);
+  if (it == o->mg.end() || !it->second.lsf) return AFG_ERR_STATE;
+  const int iv = it->second.lsf->i_lsf;
+  const afg_transport_desc& d = g_tr.d;
+  for (int q = 0; q < n; q++) {
+    const double* lsf = t.var(cc, ids[q], iv);
+    for (int x = 0; x < t.S; x++)
+      if (lsf[x] <= 0)
+        for (int s = 0; s < d.n_species; s++) t.var(cc, ids[q], d.species_iv[s])[x] = 0.0;
+  }
+  return AFG_OK;
+}
+
+/* set_electrode_densities: electrode_species_bc (src/streamer.f90:598-656)
+ * on the boxes with the mg_lsf_box tag, all levels */
+int orc_electrode_species_bc(void* p, double* cc, int mg_id, int electron, int ion, int neumann) {
+  Oracle* o = static_cast<Oracle*>(p);
+  const Tree& t = o->t;
+  auto it = o->mg.find(mg_id);
+  if (it == o->mg.end() || !it->second.lsf) return AFG_ERR_STATE;
+  const Lsf& L = *it->second.lsf;
+  const afg_transport_desc& d = g_tr.d;
+  const int nc = t.nc, D = t.D;
+  const int st[3] = {1, t.n2, t.n2 * t.n2};
+  for (int id : L.ids) {
+    const double* lsf = t.var(cc, id, L.i_lsf);
+    double* ne = t.var(cc, id, d.species_iv[electron]);
+    double* ni = t.var(cc, id, d.species_iv[ion]);
+    for (int k = (D == 3 ? 1 : 0); k <= (D == 3 ? nc : 0); k++)
+      for (int j = 1; j <= nc; j++)
+        for (int i = 1; i <= nc; i++) {
+          const int x = t.at(i, j, k);
+          if (!(lsf[x] < 0)) continue;
+          for (int s = 0; s < d.n_species; s++) t.var(cc, id, d.species_iv[s])[x] = 0.0;
+          bool any = false;
+          for (int nb = 0; nb < 2 * D; nb++) any = any || lsf[x + ((nb & 1) ? 1 : -1) * st[nb >> 1]] > 0;
+          if (!(any && neumann)) continue;
+          double sum = 0.0;
+          int cnt = 0;
+          for (int nb = 0; nb < 2 * D; nb++) {
+            const int y = x + ((nb & 1) ? 1 : -1) * st[nb >> 1];
+            if (lsf[y] > 0) {
+              sum = sum + ne[y];
+              cnt++;
+            }
+          }
+          ne[x] = sum / (double)cnt;
+          ni[x] = ne[x];
+        }
+  }
   return AFG_OK;
 }
 

@@ -24,7 +24,9 @@ GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "stand
 CASES = ["test_2d", "test_cyl", "test_2d_photoi", "test_cyl_chem", "test_2d_photoi_chem",
          "test_cyl_ion_motion", "test_cyl_ion_motion_v2", "test_3d", "test_3d_chem", "test_3d_photoi_chem",
          "test_cyl_photoi_chem"]
-FP64_CASES = CASES
+# the electrode runs (grounded rod, positive and negative field): FP64 only,
+# the electrode operator has no FP32 solve
+FP64_CASES = CASES + ["test_2d_pos_electrode", "test_2d_neg_electrode"]
 
 # FP64 GPU rows against the restatement's: identical (every stage is
 # bit-exact, the first smoothing of a solve reads the stored ghost cells as
