@@ -185,6 +185,15 @@ class TransportDesc(C.Structure):
     ]
 
 
+class StageDesc(C.Structure):
+    """afg_stage_desc: the settings forward_euler reads (m_field's solver and
+    convergence settings, m_dt's dt_cfl_number and dt_max)."""
+    _fields_ = [
+        ("mg_id", C.c_int), ("domain_len", C.c_double), ("max_rel_residual", C.c_double),
+        ("num_vcycles", C.c_int), ("dt_cfl_number", C.c_double), ("dt_max", C.c_double),
+    ]
+
+
 def _ip(a):
     return a.ctypes.data_as(_IP)
 
@@ -298,6 +307,10 @@ def load_library(path: str = LIB_PATH):
                                         C.c_double, C.c_int, _IP, _DP]),
         "afg_photoi_helmh": (C.c_int, [P, C.c_double, C.c_int, _IP, _DP, C.c_double, C.c_int]),
         "afg_tree_copy_cc": (C.c_int, [P, C.c_int, C.c_int]),
+        "afg_stage_setup": (C.c_int, [P, C.POINTER(StageDesc)]),
+        "afg_set_flux_staged": (C.c_int, [P, C.c_int]),
+        "afg_forward_euler": (C.c_int, [P, C.c_double, C.c_double, C.c_int, C.c_int, _IP, _DP, C.c_int,
+                                        C.c_int, C.c_int, _DP, _IP]),
         "afg_counters": (C.c_int, [P, C.POINTER(C.c_longlong)]),
         "afg_event_record": (C.c_int, [P, C.c_int]),
         "afg_event_elapsed": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_float)]),
@@ -780,6 +793,25 @@ class Context:
         self.check(self.lib.afg_update_densities(self.ptr, dt, s_deriv, len(sp), _ip(sp), _dp(wp), s_out,
                                                  int(last_step), C.byref(chem)), "afg_update_densities")
         return chem.value
+
+    def set_flux_staged(self, on):
+        self.check(self.lib.afg_set_flux_staged(self.ptr, int(bool(on))), "afg_set_flux_staged")
+
+    def stage_setup(self, mg_id, domain_len, max_rel_residual, num_vcycles, dt_cfl_number=0.5,
+                    dt_max=1e-11):
+        d = StageDesc(mg_id, domain_len, max_rel_residual, num_vcycles, dt_cfl_number, dt_max)
+        self.check(self.lib.afg_stage_setup(self.ptr, C.byref(d)), "afg_stage_setup")
+
+    def forward_euler(self, dt, voltage, s_deriv, s_prev, w_prev, s_out, i_step, n_steps):
+        """One forward_euler stage (afg_forward_euler); returns (dt limit,
+        field cycles of the stage)."""
+        sp = np.ascontiguousarray(s_prev, dtype=np.int32)
+        wp = np.ascontiguousarray(w_prev, dtype=np.float64)
+        lim = C.c_double(0)
+        n = C.c_int(0)
+        self.check(self.lib.afg_forward_euler(self.ptr, dt, voltage, s_deriv, len(sp), _ip(sp), _dp(wp), s_out,
+                                              i_step, n_steps, C.byref(lim), C.byref(n)), "afg_forward_euler")
+        return lim.value, n.value
 
     def field_set_rhs(self, i_rhs, s_in):
         self.check(self.lib.afg_field_set_rhs(self.ptr, i_rhs, s_in), "afg_field_set_rhs")

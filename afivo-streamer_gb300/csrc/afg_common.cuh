@@ -127,21 +127,18 @@ __device__ __forceinline__ KTree fix_dims(KTree t) {
 // stays NaN); f2d is exact for normal numbers, zero, infinity and NaN and
 // flushes FP32 subnormals to signed zero.
 __device__ __forceinline__ float d2f(double d) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-  const unsigned sign = hi & 0x80000000u;
-  const int e = (int)((hi >> 20) & 0x7FFu);
-  const unsigned mant = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-  unsigned r;
-  if (e == 0x7FF)
-    r = sign | 0x7F800000u | (mant != 0u || (lo & 0x1FFFFFFFu) != 0u ? 0x400000u : 0u);
-  else if (e - 896 >= 255)
-    r = sign | 0x7F800000u;
-  else if (e - 896 <= 0)
-    r = sign;
-  else
-    r = sign | ((unsigned)(e - 896) << 23) | mant;
-  return __uint_as_float(r);
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned ah = hi & 0x7FFFFFFFu;
+  // normal range (biased FP64 exponent 897..1150): the FP32 exponent and the
+  // top 23 mantissa bits are the high word less the bias difference, shifted
+  // left by 3 with the low word's top 3 bits
+  unsigned r = __funnelshift_l(lo, ah - (896u << 20), 3);
+  if (ah < (897u << 20)) r = 0u;  // below the FP32 normal range
+  if (ah >= (1151u << 20)) {      // above it, infinity or NaN
+    const bool nan = ah > 0x7FF00000u || (ah == 0x7FF00000u && lo != 0u);
+    r = 0x7F800000u | (nan ? 0x400000u : 0u);
+  }
+  return __uint_as_float(r | (hi & 0x80000000u));
 }
 __device__ __forceinline__ double f2d(float f) {
   const unsigned u = __float_as_uint(f);

@@ -188,6 +188,7 @@ struct afg_ctx {
   int ky = 1;
   MgSlot* grp[kMaxModes] = {};
   bool photoi_lockstep = true;  // Helmholtz modes in lockstep (else parallel branches)
+  bool flux_staged = true;      // FP32 fluxes by k_flux32s where it applies (else k_flux32)
   // asynchronous downloads (afg_cc_download_async)
   cudaStream_t xfer_stream = nullptr;
   cudaEvent_t ev_xfer = nullptr;
@@ -196,6 +197,8 @@ struct afg_ctx {
   MgSlot mg[kMaxMg];
   // transport state (afg_transport.cuh)
   TransportState tr;
+  // integrator-stage settings (afg_stage_setup); stage.mg_id < 0 = unset
+  afg_stage_desc stage{-1, 0.0, 0.0, 0, 0.0, 0.0};
   // accounting and timing
   long long ctr[4] = {0, 0, 0, 0};
   cudaEvent_t ev[64] = {};

@@ -188,28 +188,233 @@ __global__ void __launch_bounds__(256) k_flux32(KTree t0, const int* __restrict_
   if (threadIdx.x == 0) atomic_max_nonneg(a.max_sigma, f2d(smax));
 }
 
+// k_flux32 for a compile-time box size with the box's data staged in shared
+// memory: thread 0 bulk-copies |E| and the flux species of the box (whole
+// boxes, ghost cells included, contiguous) while every thread evaluates its
+// share of the two-layer ghost values (gc2_value on global memory) and loads
+// E on its faces, so those loads overlap the copies.  After the wait the
+// staged values are converted into the padded FP32 tile (face-ghost cells
+// left to the ghost values), the first ghost layer is written back, and the
+// faces and cells are done as in k_flux32, with the same arithmetic, so the
+// results are bit-identical.  At most NFMAX flux species.  The FP32 face
+// values and diffusion coefficients reuse the staging buffer.  A wait that
+// times out (1 s) raises *err; the CTA drains its copies (bounded) and
+// returns, raising bit 2 of *err if they did not complete.
+template <int D, bool CYL, int NC, int NFMAX>
+__global__ void __launch_bounds__(256) k_flux32s(KTree t0, const int* __restrict__ rec, FluxArgs32 a32,
+                                                unsigned* err) {
+  constexpr int nc = NC, n2 = NC + 2, m = NC + 4, nf1 = NC + 1;
+  constexpr int S = D == 2 ? n2 * n2 : n2 * n2 * n2;
+  constexpr int tile = D == 2 ? m * m : m * m * m;
+  constexpr int nfaces = D == 2 ? nc * nf1 : nc * nc * nf1;  // per dimension
+  constexpr int NFT = (D * nfaces + 255) / 256;               // faces per thread
+  constexpr int nface = D == 2 ? nc : nc * nc;                // cells on one box face
+  constexpr int NG = 2 * D * nface * 2;                       // two-layer ghosts per species
+  constexpr int NGT = (NG + 255) / 256;
+  constexpr unsigned SB = S * sizeof(double);
+  static_assert(SB % 16 == 0, "bulk copies need 16-byte multiples");
+  const KTree t = fix_dims<D, NC>(t0);
+  extern __shared__ __align__(16) unsigned char smb[];
+  __shared__ float sred[32];
+  __shared__ __align__(8) unsigned long long bar;
+  const FluxArgs& a = a32.a;
+  const int nf = a.nf;
+  double* rawE = reinterpret_cast<double*>(smb);  // staged |E|, then the species
+  double* rawN = rawE + S;
+  float* vf = reinterpret_cast<float*>(smb);      // [D][nfaces], after the conversion
+  float* df = vf + D * nfaces;
+  const size_t offA = ((size_t)max((int)(SB * (nf + 1)), (int)(8 * D * nfaces)) + 15) & ~(size_t)15;
+  float* big = reinterpret_cast<float*>(smb + offA);  // [nf][tile]
+  float* Es = big + nf * tile;                         // [S]
+  const int4 r0 = reinterpret_cast<const int4*>(rec)[2 * blockIdx.x];
+  const int4 r1 = reinterpret_cast<const int4*>(rec)[2 * blockIdx.x + 1];
+  const int slot = r0.x;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(&bar, SB * (unsigned)(nf + 1));
+    bulk_copy_g2s(rawE, a.E + (size_t)slot * S, SB, &bar);
+    for (int q = 0; q < nf; q++) bulk_copy_g2s(rawN + q * S, a.n[q] + (size_t)slot * S, SB, &bar);
+  }
+  // this thread's ghost values (both layers) and face fields
+  double gval[NFMAX][NGT];
+#pragma unroll
+  for (int q = 0; q < NFMAX; q++)
+#pragma unroll
+    for (int u = 0; u < NGT; u++) {
+      const int w = (int)threadIdx.x + u * 256;
+      gval[q][u] = 0.0;
+      if (q < nf && w < NG) {
+        const int layer = w & 1, w2 = w >> 1;
+        const int nb = w2 / nface, pq = w2 - nb * nface;
+        const int p = pq % nc + 1, qq = D == 3 ? pq / nc + 1 : 0;
+        gval[q][u] = gc2_value<D>(t, a.n[q], slot, nb, rec_nb(r0, r1, nb), layer, p, qq, a.bc, a.limiter);
+      }
+    }
+  float ex[NFT];
+#pragma unroll
+  for (int u = 0; u < NFT; u++) {
+    const int w = (int)threadIdx.x + u * 256;
+    ex[u] = 0.0f;
+    if (w < D * nfaces) {
+      const int dim = w / nfaces, fw = w - dim * nfaces;
+      const int f = fw % nf1 + 1, ln = fw / nf1;
+      const int jj = ln % nc + 1, kk = D == 3 ? ln / nc + 1 : 1;
+      int fidx;
+      if (D == 2) fidx = dim == 0 ? fc_at(nf1, f, jj, 1) : fc_at(nf1, jj, f, 1);
+      else if (dim == 0) fidx = fc_at(nf1, f, jj, kk);
+      else if (dim == 1) fidx = fc_at(nf1, jj, f, kk);
+      else fidx = fc_at(nf1, jj, kk, f);
+      ex[u] = d2f(a.Efc[((size_t)slot * D + dim) * t.NF + fidx]);
+    }
+  }
+  const bool ok = mbar_wait(&bar, 0);
+  if (__syncthreads_or(!ok)) {
+    if (threadIdx.x == 0) atomicOr(err, mbar_wait(&bar, 0) ? 1u : 3u);
+    return;
+  }
+  // staged values into the tile; the face-ghost cells (one index outside)
+  // come from the ghost values
+  for (int q = 0; q < nf; q++)
+    for (int x = threadIdx.x; x < S; x += 256) {
+      const int i = x % n2, r = x / n2;
+      const int j = D == 2 ? r : r % n2, k = D == 2 ? 0 : r / n2;
+      const int out = (i == 0 || i == n2 - 1) + (j == 0 || j == n2 - 1) + (D == 3 && (k == 0 || k == n2 - 1));
+      if (out != 1) big[q * tile + big_at<D>(m, i, j, k)] = d2f(rawN[q * S + x]);
+    }
+  for (int x = threadIdx.x; x < S; x += 256) Es[x] = d2f(rawE[x]);
+#pragma unroll
+  for (int q = 0; q < NFMAX; q++)
+#pragma unroll
+    for (int u = 0; u < NGT; u++) {
+      const int w = (int)threadIdx.x + u * 256;
+      if (q < nf && w < NG) {
+        const int layer = w & 1, w2 = w >> 1;
+        const int nb = w2 / nface, pq = w2 - nb * nface;
+        const int p = pq % nc + 1, qq = D == 3 ? pq / nc + 1 : 0;
+        const int d = nb >> 1;
+        const bool low = (nb & 1) == 0;
+        const int x = low ? -layer : nc + 1 + layer;
+        big[q * tile + big_face<D>(m, d, x, p, qq)] = d2f(gval[q][u]);
+        if (layer == 0) a.n[q][(size_t)slot * S + face_at<D>(n2, d, x, p, qq)] = gval[q][u];
+      }
+    }
+  __syncthreads();
+  float smax = 0.0f;
+#pragma unroll
+  for (int u = 0; u < NFT; u++) {
+    const int w = (int)threadIdx.x + u * 256;
+    if (w < D * nfaces) {
+    const int dim = w / nfaces, fw = w - dim * nfaces;
+    const int f = fw % nf1 + 1, ln = fw / nf1;
+    const int jj = ln % nc + 1, kk = D == 3 ? ln / nc + 1 : 1;
+    const float inv_dx = t.idrf[slot * D + dim];
+    int fidx;
+    if (D == 2) fidx = dim == 0 ? fc_at(nf1, f, jj, 1) : fc_at(nf1, jj, f, 1);
+    else if (dim == 0) fidx = fc_at(nf1, f, jj, kk);
+    else if (dim == 1) fidx = fc_at(nf1, jj, f, kk);
+    else fidx = fc_at(nf1, jj, kk, f);
+    const float Ex = ex[u];
+    auto cidx = [&](int x) -> int {
+      if (D == 2) return dim == 0 ? at2(n2, x, jj) : at2(n2, jj, x);
+      if (dim == 0) return at3(n2, x, jj, kk);
+      if (dim == 1) return at3(n2, jj, x, kk);
+      return at3(n2, jj, kk, x);
+    };
+    auto bidx = [&](int x) -> int {
+      if (D == 2) return dim == 0 ? big_at<D>(m, x, jj, 0) : big_at<D>(m, jj, x, 0);
+      if (dim == 0) return big_at<D>(m, x, jj, kk);
+      if (dim == 1) return big_at<D>(m, jj, x, kk);
+      return big_at<D>(m, jj, kk, x);
+    };
+    const float td = 0.5f * (Es[cidx(f - 1)] + Es[cidx(f)]) * a32.N_inv_td;
+    int ix;
+    float lw;
+    lt_loc_f(a32.lt, td, ix, lw);
+    const float mu = lt_col_f(a32.lt, a.col_mu, ix, lw) * a32.N_inv;
+    const float dc = lt_col_f(a32.lt, a.col_dc, ix, lw) * a32.N_inv;
+    const float v = -mu * Ex;
+    float sigma = 0.0f;
+    for (int q = 0; q < nf; q++) {
+      const float* L = big + q * tile;
+      const float lm2 = L[bidx(f - 2)], lm1 = L[bidx(f - 1)], l0 = L[bidx(f)], lp1 = L[bidx(f + 1)];
+      const bool pos = a32.sign[q] * Ex > 0.0f;
+      const float uu = pos ? lm1 + 0.5f * koren_f(l0 - lm1, lm1 - lm2) : l0 - 0.5f * koren_f(l0 - lm1, lp1 - l0);
+      float fl;
+      if (q == 0) {
+        fl = v * uu - dc * inv_dx * (l0 - lm1);
+        sigma = mu * uu;
+      } else {
+        const float vi = a32.sign[q] * a32.mu_ion[q] * Ex;
+        fl = vi * uu;
+        sigma = sigma + a32.mu_ion[q] * uu;
+      }
+      a.flux[q][((size_t)slot * D + dim) * t.NF + fidx] = f2d(fl);
+    }
+    smax = sigma > smax ? sigma : smax;
+    vf[w] = v;
+    df[w] = dc;
+    }
+  }
+  __syncthreads();
+  float cmax = 0.0f;
+  constexpr int ncell = D == 2 ? nc * nc : nc * nc * nc;
+  for (int w = threadIdx.x; w < ncell; w += 256) {
+    const int i = w % nc + 1, r = w / nc;
+    const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 1 : r / nc + 1;
+    float cfl = 0.0f;
+    for (int dim = 0; dim < D; dim++) {
+      const float inv_dx = t.idrf[slot * D + dim];
+      int c, ln;
+      if (D == 2) { c = dim == 0 ? i : j; ln = dim == 0 ? j - 1 : i - 1; }
+      else if (dim == 0) { c = i; ln = (j - 1) + nc * (k - 1); }
+      else if (dim == 1) { c = j; ln = (i - 1) + nc * (k - 1); }
+      else { c = k; ln = (i - 1) + nc * (j - 1); }
+      const int base = dim * nfaces + ln * nf1;
+      const float vmax = fmaxf(fabsf(vf[base + c]), fabsf(vf[base + c - 1]));
+      const float dmax = fmaxf(df[base + c], df[base + c - 1]);
+      cfl = cfl + (vmax * inv_dx + 2.0f * dmax * (inv_dx * inv_dx));
+    }
+    cmax = cfl > cmax ? cfl : cmax;
+  }
+  cmax = block_max<float>(cmax, sred);
+  if (threadIdx.x == 0) atomic_max_nonneg(a.max_cfl, f2d(cmax));
+  __syncthreads();
+  smax = block_max<float>(smax, sred);
+  if (threadIdx.x == 0) atomic_max_nonneg(a.max_sigma, f2d(smax));
+}
+
 // Reaction in FP32 form: rate = fa * fb * form(Td) (the factors split so that
 // a large rate_factor, e.g. N^2 of a three-body reaction, stays in range).
-struct Reac32 {
-  int rate_type, lt_col;
-  float fa, fb;      // product = rate_factor * c1 (analytic) or rate_factor (tabulated)
-  float c[4];
-  int n_in, ix_in[4], n_out, ix_out[4];
-  float mult_out[4];
+// The update kernel reads the records from shared memory: in_off are the
+// input species' offsets in the per-thread columns (species * 128) and the
+// n_upd (species offset, coefficient) pairs are the reaction's net effect on
+// each species it touches (outputs' multiplicities less the inputs' counts).
+struct alignas(16) Reac32 {
+  int rate_type, lt_col, n_in, n_upd;
+  float fa, fb, c1, c2;
+  float c3, pad0, pad1, pad2;
+  int in_off[4];
+  int upd_off[8];
+  float upd_coef[8];
 };
+static_assert(sizeof(Reac32) == 128, "Reac32 is 32 words");
 
 __device__ __forceinline__ float rate32(const LtDevF& lt, const Reac32& r, float td, int ix, float w) {
   switch (r.rate_type) {
     case AFG_RATE_TABULATED_FIELD: return r.fb * (r.fa * lt_col_f(lt, r.lt_col, ix, w));
     case AFG_RATE_CONSTANT: return r.fa * r.fb;
-    case AFG_RATE_LINEAR: return r.fa * r.fb * (td - r.c[1]);
-    case AFG_RATE_EXP_V1: { const float q = r.c[1] / (r.c[2] + td); return r.fa * r.fb * expf(-(q * q)); }
-    case AFG_RATE_EXP_V2: { const float q = td / r.c[1]; return r.fa * r.fb * expf(-(q * q)); }
-    case AFG_RATE_K13: return r.fa * r.fb * expf(-pow_c(r.c[1] / (r.c[2] + td), r.c[3]));
-    case AFG_RATE_K14: return r.fa * r.fb * expf(-pow_c(td / r.c[1], r.c[2]));
+    case AFG_RATE_LINEAR: return r.fa * r.fb * (td - r.c1);
+    case AFG_RATE_EXP_V1: { const float q = r.c1 / (r.c2 + td); return r.fa * r.fb * expf(-(q * q)); }
+    case AFG_RATE_EXP_V2: { const float q = td / r.c1; return r.fa * r.fb * expf(-(q * q)); }
+    case AFG_RATE_K13: return r.fa * r.fb * expf(-pow_c(r.c1 / (r.c2 + td), r.c3));
+    case AFG_RATE_K14: return r.fa * r.fb * expf(-pow_c(td / r.c1, r.c2));
     case AFG_RATE_K1: {
       const float Te = (float)(2 * 1.602176634e-19 / (3 * 1.380649e-23)) * lt_col_f(lt, r.lt_col, ix, w);
-      return r.fa * r.fb * pow_c(300.0f / Te, r.c[1]);
+      return r.fa * r.fb * pow_c(300.0f / Te, r.c1);
     }
   }
   return 0.0f;
@@ -227,14 +432,6 @@ struct UpdateArgs32 {
 };
 
 template <int NSMAX>
-__device__ __forceinline__ float pickf(const float (&v)[NSMAX], int s) {
-  float r = 0.0f;
-#pragma unroll
-  for (int k = 0; k < NSMAX; k++)
-    if (k == s) r = v[k];
-  return r;
-}
-template <int NSMAX>
 __device__ __forceinline__ void add_tof(float (&v)[NSMAX], int s, float x) {
 #pragma unroll
   for (int k = 0; k < NSMAX; k++)
@@ -242,17 +439,28 @@ __device__ __forceinline__ void add_tof(float (&v)[NSMAX], int s, float x) {
 }
 
 // flux_update_densities + add_source_terms with FP32 sources; the weights of
-// the previous states sum to one (forward Euler and Heun stages).
+// the previous states sum to one (forward Euler and Heun stages).  The
+// reaction records sit in dynamic shared memory (n_reactions of them); each
+// thread keeps its cell's densities and sources in its own shared-memory
+// column, since the records index species at run time.  The fluxes and the
+// first previous state are loaded before the chemistry, so that their
+// latency overlaps it.
 template <int D, bool CYL, int NSMAX, int NC = 0>
-__global__ void __launch_bounds__(128, 12) k_update32(KTree t0, const int* __restrict__ list, UpdateArgs32 u) {
+__global__ void __launch_bounds__(128, 8) k_update32(KTree t0, const int* __restrict__ list, UpdateArgs32 u) {
   const KTree t = fix_dims<D, NC>(t0);
   __shared__ float sred[32];
-  // each thread's species densities and sources in its own shared-memory
-  // column: the reaction table indexes species at run time, which registers
-  // cannot be (one shared-memory access instead of an unrolled select)
   __shared__ float s_dens[NSMAX * 128], s_der[NSMAX * 128];
   __shared__ double s_raw[NSMAX * 128];  // the derivative state as read
+  extern __shared__ __align__(16) int s_rwords[];
+  const Reac32* rec = reinterpret_cast<const Reac32*>(s_rwords);
   const UpdateArgs& a = u.a;
+  const int nr = a.n_reactions;
+  {
+    const int4* src = reinterpret_cast<const int4*>(u.reactions);
+    int4* dst = reinterpret_cast<int4*>(s_rwords);
+    for (int x = threadIdx.x; x < nr * 8; x += blockDim.x) dst[x] = src[x];
+  }
+  __syncthreads();
   const int slot = list[blockIdx.x];
   const int nc = t.nc, n2 = t.n2, nf1 = nc + 1;
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;
@@ -261,31 +469,59 @@ __global__ void __launch_bounds__(128, 12) k_update32(KTree t0, const int* __res
   for (int q = 0; q < D; q++) dt_dr[q] = u.dt * t.idrf[slot * D + q];
   float my_chem = 3.0e38f;
   const size_t base = (size_t)slot * t.S;
+  const bool n0_raw = u.prev_is_deriv == 0;
+  // registers for the early load of the first previous state (up to 8 species)
+  constexpr bool kPre = NSMAX <= 8;
   for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
     const int i = w % nc + 1, r = w / nc;
     const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
     const int x = D == 2 ? at2(n2, i, j) : at3(n2, i, j, k);
+    const int kk = D == 3 ? k : 1;
     float* dens = s_dens + tid;  // species s at dens[s * 128]
     float* der = s_der + tid;
+    // every global load of the cell first
+    double raw[NSMAX], n0v[NSMAX];
+#pragma unroll
+    for (int s = 0; s < NSMAX; s++) {
+      raw[s] = s < a.ns ? a.deriv[s][base + x] : 0.0;
+      n0v[s] = (kPre && s < a.ns && !n0_raw) ? a.prev[0][s][base + x] : 0.0;
+    }
+    const double Ec = a.E[base + x];
+    const double phc = a.photo != nullptr ? a.photo[base + x] : 0.0;
+    double fx[2 * D];
+    {
+      const double* F = a.flux[0] + (size_t)slot * D * t.NF;
+      if (D == 2) {
+        fx[0] = F[fc_at(nf1, i, j, 1)];
+        fx[1] = F[fc_at(nf1, i + 1, j, 1)];
+        fx[2] = F[t.NF + fc_at(nf1, i, j, 1)];
+        fx[3] = F[t.NF + fc_at(nf1, i, j + 1, 1)];
+      } else {
+        fx[0] = F[fc_at(nf1, i, j, kk)];
+        fx[1] = F[fc_at(nf1, i + 1, j, kk)];
+        fx[2] = F[t.NF + fc_at(nf1, i, j, kk)];
+        fx[3] = F[t.NF + fc_at(nf1, i, j + 1, kk)];
+        fx[4] = F[2 * t.NF + fc_at(nf1, i, j, kk)];
+        fx[5] = F[2 * t.NF + fc_at(nf1, i, j, kk + 1)];
+      }
+    }
 #pragma unroll
     for (int s = 0; s < NSMAX; s++) {
       if (s < a.ns) {
-        const double raw = a.deriv[s][base + x];
-        s_raw[s * 128 + tid] = raw;
-        dens[s * 128] = fmaxf(d2f(raw), 0.0f);
+        s_raw[s * 128 + tid] = raw[s];
+        dens[s * 128] = fmaxf(d2f(raw[s]), 0.0f);
         der[s * 128] = 0.0f;
       }
     }
-    const float td = u.N_inv_td * d2f(a.E[base + x]);
+    const float td = u.N_inv_td * d2f(Ec);
     int ix;
     float lw;
     lt_loc_f(u.lt, td, ix, lw);
-    for (int n = 0; n < a.n_reactions; n++) {
-      const Reac32& rc = u.reactions[n];
+    for (int n = 0; n < nr; n++) {
+      const Reac32& rc = rec[n];
       float rate = rate32(u.lt, rc, td, ix, lw);
-      for (int q = 0; q < rc.n_in; q++) rate = rate * dens[rc.ix_in[q] * 128];
-      for (int q = 0; q < rc.n_in; q++) der[rc.ix_in[q] * 128] -= rate;
-      for (int q = 0; q < rc.n_out; q++) der[rc.ix_out[q] * 128] += rate * rc.mult_out[q];
+      for (int q = 0; q < rc.n_in; q++) rate = rate * dens[rc.in_off[q]];
+      for (int q = 0; q < rc.n_upd; q++) der[rc.upd_off[q]] = fmaf(rc.upd_coef[q], rate, der[rc.upd_off[q]]);
     }
     if (a.last_step) {
       const float eps = 1e-30f;
@@ -302,7 +538,7 @@ __global__ void __launch_bounds__(128, 12) k_update32(KTree t0, const int* __res
       my_chem = fminf(my_chem, tmp);
     }
     if (a.photo != nullptr) {
-      const float ph = d2f(a.photo[base + x]);
+      const float ph = d2f(phc);
       der[a.flux_species[0] * 128] += ph;
       der[a.photoi_species * 128] += ph;
     }
@@ -310,31 +546,38 @@ __global__ void __launch_bounds__(128, 12) k_update32(KTree t0, const int* __res
 #pragma unroll
     for (int s = 0; s < NSMAX; s++) inc[s] = s < a.ns ? u.dt * der[s * 128] : 0.0f;
     for (int f = 0; f < a.nf; f++) {
-      const int s = a.flux_species[f];
-      const double* F0 = a.flux[f] + ((size_t)slot * D + 0) * t.NF;
-      const double* F1 = a.flux[f] + ((size_t)slot * D + 1) * t.NF;
-      const int kk = D == 3 ? k : 1;
+      double g[2 * D];
+      if (f == 0) {
+#pragma unroll
+        for (int q = 0; q < 2 * D; q++) g[q] = fx[q];
+      } else {
+        const double* F = a.flux[f] + (size_t)slot * D * t.NF;
+        g[0] = F[fc_at(nf1, i, j, kk)];
+        g[1] = F[fc_at(nf1, i + 1, j, kk)];
+        g[2] = F[t.NF + fc_at(nf1, i, j, kk)];
+        g[3] = F[t.NF + fc_at(nf1, i, j + 1, kk)];
+        if (D == 3) {
+          g[4] = F[2 * t.NF + fc_at(nf1, i, j, kk)];
+          g[5] = F[2 * t.NF + fc_at(nf1, i, j, kk + 1)];
+        }
+      }
       float div;
       if (D == 2 && CYL) {
         const double* gw = t.geo + ((size_t)slot * nc + (i - 1)) * 4;
         const float f1 = d2f(gw[0]), f2 = d2f(gw[1]);
-        div = dt_dr[0] * (f1 * d2f(F0[fc_at(nf1, i, j, 1)]) - f2 * d2f(F0[fc_at(nf1, i + 1, j, 1)])) +
-              dt_dr[1] * (d2f(F1[fc_at(nf1, i, j, 1)]) - d2f(F1[fc_at(nf1, i, j + 1, 1)]));
+        div = dt_dr[0] * (f1 * d2f(g[0]) - f2 * d2f(g[1])) + dt_dr[1] * (d2f(g[2]) - d2f(g[3]));
       } else if (D == 2) {
-        div = dt_dr[0] * (d2f(F0[fc_at(nf1, i, j, 1)]) - d2f(F0[fc_at(nf1, i + 1, j, 1)])) +
-              dt_dr[1] * (d2f(F1[fc_at(nf1, i, j, 1)]) - d2f(F1[fc_at(nf1, i, j + 1, 1)]));
+        div = dt_dr[0] * (d2f(g[0]) - d2f(g[1])) + dt_dr[1] * (d2f(g[2]) - d2f(g[3]));
       } else {
-        const double* F2 = a.flux[f] + ((size_t)slot * D + 2) * t.NF;
-        div = dt_dr[0] * (d2f(F0[fc_at(nf1, i, j, kk)]) - d2f(F0[fc_at(nf1, i + 1, j, kk)])) +
-              dt_dr[1] * (d2f(F1[fc_at(nf1, i, j, kk)]) - d2f(F1[fc_at(nf1, i, j + 1, kk)])) +
-              dt_dr[2] * (d2f(F2[fc_at(nf1, i, j, kk)]) - d2f(F2[fc_at(nf1, i, j, kk + 1)]));
+        div = dt_dr[0] * (d2f(g[0]) - d2f(g[1])) + dt_dr[1] * (d2f(g[2]) - d2f(g[3])) +
+              dt_dr[2] * (d2f(g[4]) - d2f(g[5]));
       }
-      add_tof<NSMAX>(inc, s, div);
+      add_tof<NSMAX>(inc, a.flux_species[f], div);
     }
 #pragma unroll
     for (int s = 0; s < NSMAX; s++) {
       if (s >= a.ns) continue;
-      const double n0 = u.prev_is_deriv == 0 ? s_raw[s * 128 + tid] : a.prev[0][s][base + x];
+      const double n0 = n0_raw ? s_raw[s * 128 + tid] : kPre ? n0v[s] : a.prev[0][s][base + x];
       float d = inc[s];
       for (int mm = 1; mm < a.n_prev; mm++) {
         const double nm = u.prev_is_deriv == mm ? s_raw[s * 128 + tid] : a.prev[mm][s][base + x];

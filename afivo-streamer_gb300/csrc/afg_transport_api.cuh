@@ -48,6 +48,17 @@ static size_t flux32_smem(const afg_ctx* ctx, int n_flux) {
   return sizeof(float) * ((size_t)n_flux * tile + 2 * (size_t)D * nfaces + ctx->S);
 }
 
+// dynamic shared memory of k_flux32s: the staging buffer (|E| and the
+// species, FP64; later the FP32 face values and diffusion coefficients),
+// the FP32 tiles and |E| in FP32
+static size_t flux32s_smem(const afg_ctx* ctx, int n_flux) {
+  const int D = ctx->D, nc = ctx->nc, m = nc + 4;
+  const int tile = D == 2 ? m * m : m * m * m;
+  const size_t nfaces = D == 2 ? (size_t)nc * (nc + 1) : (size_t)nc * nc * (nc + 1);
+  const size_t offA = (std::max(sizeof(double) * ctx->S * (n_flux + 1), 2 * sizeof(float) * D * nfaces) + 15) & ~(size_t)15;
+  return offA + sizeof(float) * ((size_t)n_flux * tile + ctx->S);
+}
+
 extern "C" {
 
 int afg_transport_setup(afg_ctx* ctx, const afg_transport_desc* d) {
@@ -122,14 +133,30 @@ int afg_transport_setup(afg_ctx* ctx, const afg_transport_desc* d) {
         o.fa = (float)(rc.rate_factor * rc.c[0]);
         o.fb = 1.0f;
       }
-      for (int q = 0; q < 4; q++) o.c[q] = (float)rc.c[q];
+      o.c1 = (float)rc.c[1];
+      o.c2 = (float)rc.c[2];
+      o.c3 = (float)rc.c[3];
+      // inputs as column offsets; the net change of every species touched:
+      // each output's multiplicity less one per occurrence as an input
       o.n_in = rc.n_in;
-      o.n_out = rc.n_out;
-      for (int q = 0; q < 4; q++) {
-        o.ix_in[q] = rc.ix_in[q];
-        o.ix_out[q] = rc.ix_out[q];
-        o.mult_out[q] = (float)rc.mult_out[q];
+      for (int q = 0; q < rc.n_in; q++) o.in_off[q] = rc.ix_in[q] * 128;
+      double coef[AFG_MAX_SPECIES] = {};
+      bool touched[AFG_MAX_SPECIES] = {};
+      for (int q = 0; q < rc.n_in; q++) {
+        coef[rc.ix_in[q]] -= 1.0;
+        touched[rc.ix_in[q]] = true;
       }
+      for (int q = 0; q < rc.n_out; q++) {
+        coef[rc.ix_out[q]] += rc.mult_out[q];
+        touched[rc.ix_out[q]] = true;
+      }
+      o.n_upd = 0;
+      for (int sp = 0; sp < t.n_species; sp++)
+        if (touched[sp] && coef[sp] != 0.0) {
+          o.upd_off[o.n_upd] = sp * 128;
+          o.upd_coef[o.n_upd] = (float)coef[sp];
+          o.n_upd++;
+        }
       if (t.precision == AFG_MIXED && (!std::isfinite(o.fa) || !std::isfinite(o.fb)))
         return fail(ctx, AFG_ERR_UNSUPPORTED, "reaction %d: rate factor outside the FP32 range", r + 1);
     }
@@ -266,7 +293,18 @@ int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim) {
           a32.mu_ion[f] = (float)(d.ion_mobility_N[f] / d.gas_number_density);
         }
         const size_t smem32 = flux32_smem(ctx, d.n_flux);
-        if (ctx->D == 3)
+        const bool staged = ctx->flux_staged && d.n_flux <= 2 &&
+                            ((ctx->D == 3 && ctx->nc == 8) || (ctx->D == 2 && ctx->nc == 16));
+        if (staged) {
+          // the box's |E| and species staged by bulk copies (k_flux32s)
+          const size_t sm = flux32s_smem(ctx, d.n_flux);
+          if (ctx->D == 3)
+            k_flux32s<3, false, 8, 2><<<n, 256, sm, ctx->stream>>>(t, rec_of(ctx, list), a32, ctx->d_err);
+          else if (cyl)
+            k_flux32s<2, true, 16, 2><<<n, 256, sm, ctx->stream>>>(t, rec_of(ctx, list), a32, ctx->d_err);
+          else
+            k_flux32s<2, false, 16, 2><<<n, 256, sm, ctx->stream>>>(t, rec_of(ctx, list), a32, ctx->d_err);
+        } else if (ctx->D == 3)
           AFG_NC3(NCV_, k_flux32<3, false, NCV_><<<n, 256, smem32, ctx->stream>>>(t, rec_of(ctx, list), a32));
         else if (cyl)
           AFG_NC2(NCV_, k_flux32<2, true, NCV_><<<n, 256, smem32, ctx->stream>>>(t, rec_of(ctx, list), a32));
@@ -374,13 +412,14 @@ int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev, const
       u.prev_is_deriv = -1;
       for (int m = 0; m < n_prev; m++)
         if (s_prev[m] == s_deriv) u.prev_is_deriv = m;
+      const size_t rsm = sizeof(Reac32) * (size_t)d.n_reactions;  // the records in shared memory
 #define AFG_LAUNCH_UPDATE32(NSM)                                                               \
   if (ctx->D == 3)                                                                             \
-    AFG_NC3(NCV_, k_update32<3, false, NSM, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, u));    \
+    AFG_NC3(NCV_, k_update32<3, false, NSM, NCV_><<<n, 128, rsm, ctx->stream>>>(t, list, u));  \
   else if (cyl)                                                                                \
-    AFG_NC2(NCV_, k_update32<2, true, NSM, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, u));     \
+    AFG_NC2(NCV_, k_update32<2, true, NSM, NCV_><<<n, 128, rsm, ctx->stream>>>(t, list, u));   \
   else                                                                                         \
-    AFG_NC2(NCV_, k_update32<2, false, NSM, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, u));
+    AFG_NC2(NCV_, k_update32<2, false, NSM, NCV_><<<n, 128, rsm, ctx->stream>>>(t, list, u));
       if (d.n_species <= 4) {
         AFG_LAUNCH_UPDATE32(4)
       } else if (d.n_species <= 8) {
@@ -675,6 +714,48 @@ int afg_field_compute(afg_ctx* ctx, int mg_id, int s_in, int have_guess, double 
   RC(afg_field_from_potential(ctx, m->d.i_phi));
   if (n_cycles) *n_cycles = nc_done;
   if (residual) *residual = r;
+  return AFG_OK;
+}
+
+int afg_set_flux_staged(afg_ctx* ctx, int on) {
+  if (!ctx) return AFG_ERR_ARG;
+  if (ctx->flux_staged != (on != 0)) clear_graphs(ctx);
+  ctx->flux_staged = on != 0;
+  return AFG_OK;
+}
+
+int afg_stage_setup(afg_ctx* ctx, const afg_stage_desc* d) {
+  if (!d) return fail(ctx, AFG_ERR_ARG, "null stage descriptor");
+  MgSlot* m;
+  RC(get_mg(ctx, d->mg_id, &m));
+  if (d->num_vcycles < 0 || !(d->domain_len > 0) || !(d->dt_max > 0) || !(d->dt_cfl_number > 0))
+    return fail(ctx, AFG_ERR_ARG, "bad stage settings");
+  ctx->stage = *d;
+  return AFG_OK;
+}
+
+// forward_euler (src/m_fluid.f90:21-99); the limits combine as at lines
+// 96-98, the chemistry limit counting on the last step only (add_source_terms
+// computes it there, 402-418)
+int afg_forward_euler(afg_ctx* ctx, double dt, double voltage, int s_deriv, int n_prev, const int* s_prev,
+                      const double* w_prev, int s_out, int i_step, int n_steps, double* dt_lim, int* n_cycles) {
+  const afg_stage_desc& sd = ctx->stage;
+  if (sd.mg_id < 0) return fail(ctx, AFG_ERR_ARG, "afg_stage_setup not called");
+  if (i_step < 1 || i_step > n_steps) return fail(ctx, AFG_ERR_ARG, "bad integrator step");
+  int nc = 0;
+  if (i_step > 1) {
+    double res;
+    RC(afg_field_compute(ctx, sd.mg_id, s_deriv, 1, voltage, sd.domain_len, sd.max_rel_residual, sd.num_vcycles,
+                         &nc, &res));
+  }
+  double fl[2];
+  RC(afg_flux_upwind(ctx, s_deriv, fl));
+  const bool last = i_step == n_steps;
+  double chem = 1e100;
+  RC(afg_update_densities(ctx, dt, s_deriv, n_prev, s_prev, w_prev, s_out, last ? 1 : 0, &chem));
+  if (!last) chem = 1e100;
+  if (dt_lim) *dt_lim = std::min(sd.dt_max, std::min(std::min(fl[0] * sd.dt_cfl_number, fl[1]), std::min(chem, 1e100)));
+  if (n_cycles) *n_cycles = nc;
   return AFG_OK;
 }
 

@@ -286,7 +286,8 @@ class StreamerRun:
     counts each instance's cycles."""
 
     def __init__(self, ctx, tree, model, voltage, dt, precision=ag.FP64, max_rel_residual=1e-8,
-                 num_vcycles=30, photoi=None, photoi_per_steps=5, integrator="heun"):
+                 num_vcycles=30, photoi=None, photoi_per_steps=5, integrator="heun", dt_cfl_number=0.5,
+                 dt_max=1e-11):
         if model.n_states < states_needed(integrator):
             raise ValueError(f"{integrator} needs {states_needed(integrator)} copies of each density")
         self.stages = INTEGRATORS[integrator]
@@ -300,6 +301,7 @@ class StreamerRun:
         self.num_vcycles = num_vcycles
         self.photoi = photoi          # (lambdas 1/m, coeffs 1/m^2, eta*quench)
         self.photoi_per_steps = photoi_per_steps
+        self.dt_cfl_number, self.dt_max = dt_cfl_number, dt_max
         self.it = 0
         self.L = float(tree.dr[0, -1] * tree.coarse_grid_size[-1])
         self.last = {}
@@ -316,6 +318,8 @@ class StreamerRun:
             ctx.set_cc_methods(m.i_photo, *m.photo_gc())
         v0 = float(self.voltage[0]) if self.batched else self.voltage
         ctx.mg_setup(0, m.field_mg(v0, self.precision))
+        if not self.batched:
+            ctx.stage_setup(0, self.L, self.rel, self.num_vcycles, self.dt_cfl_number, self.dt_max)
         self.mode_ids = []
         if self.photoi is not None:
             lam, coeffs, _ = self.photoi
@@ -377,18 +381,23 @@ class StreamerRun:
         # copy_current_state: densities to the backup copy
         for s in range(len(m.species)):
             ctx.tree_copy_cc(m.species_iv[s], m.species_iv[s] + m.n_states - 1)
-        cfl = drt = 1e100
-        chem = 0.0
+        n_st = len(self.stages)
+        lim = 1e100
         for i, (f, s_deriv, s_prev, w_prev, s_out) in enumerate(self.stages, 1):
+            if not self.batched:
+                # the whole stage in one call (afg_forward_euler)
+                lim, nc = ctx.forward_euler(f * dt, self.voltage, s_deriv, s_prev, w_prev, s_out, i, n_st)
+                self.last["vcycles"] += nc
+                continue
+            # batched instances: the field converges per instance
             if i > 1:
                 self.field(s_deriv, True)
-            lim = ctx.flux_upwind(s_deriv)
-            cfl, drt = min(cfl, lim[0]), min(drt, lim[1])
-            chem = ctx.update_densities(f * dt, s_deriv, s_prev, w_prev, s_out,
-                                        last_step=(i == len(self.stages)))
+            fl = ctx.flux_upwind(s_deriv)
+            chem = ctx.update_densities(f * dt, s_deriv, s_prev, w_prev, s_out, last_step=(i == n_st))
+            lim = min(self.dt_max, fl[0] * self.dt_cfl_number, fl[1], chem if i == n_st else 1e100)
         if after_update is not None:
             after_update()
         # field of the new state
         n, r = self.field(0, True)
-        self.last.update(cfl=cfl, drt=drt, chem=chem, residual=r)
+        self.last.update(dt_lim=lim, residual=r)
         self.it += 1

@@ -1008,7 +1008,8 @@ class GpuEngine:
         self.run = sm.StreamerRun(self.ctx, tree, model, voltage, 0.0, precision,
                                   max_rel_residual=cfg.multigrid_max_rel_residual,
                                   num_vcycles=cfg.multigrid_num_vcycles, integrator=model.integrator,
-                                  photoi=model.photoi_params, photoi_per_steps=cfg.photoi_per_steps)
+                                  photoi=model.photoi_params, photoi_per_steps=cfg.photoi_per_steps,
+                                  dt_cfl_number=cfg.dt_cfl_number, dt_max=cfg.dt_max)
         self._setup()
 
     def _setup(self):
@@ -1047,18 +1048,14 @@ class GpuEngine:
         self.run.field(0, have_guess)
 
     def advance(self, dt):
-        ctx, m, cfg = self.ctx, self.m, self.cfg
+        ctx, m = self.ctx, self.m
         for s in range(len(m.species)):
             ctx.tree_copy_cc(m.species_iv[s], m.species_iv[s] + m.n_states - 1)
         ctx.tree_copy_cc(m.i_phi, self.iv_phi_copy)
         lim = 1e100
         for i, (f, s_deriv, s_prev, w_prev, s_out) in enumerate(self.stages, 1):
-            if i > 1:
-                self.run.field(s_deriv, True)
-            fl = ctx.flux_upwind(s_deriv)
-            last = i == len(self.stages)
-            chem = ctx.update_densities(f * dt, s_deriv, s_prev, w_prev, s_out, last_step=last)
-            lim = min(cfg.dt_max, min(fl[0] * cfg.dt_cfl_number, fl[1], chem if last else 1e100, 1e100))
+            lim, _ = ctx.forward_euler(f * dt, self.run.voltage, s_deriv, s_prev, w_prev, s_out, i,
+                                       len(self.stages))
         return lim
 
     def photoi(self):

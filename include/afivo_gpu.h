@@ -451,10 +451,46 @@ int afg_photoi_helmh(afg_ctx* ctx, double coeff, int n_modes, const int* mg_ids,
  * Both give the same results.  No counterpart in the reference. */
 int afg_set_photoi_lockstep(afg_ctx* ctx, int on);
 
+/* Which kernel computes the AFG_MIXED fluxes of afg_flux_upwind for boxes of
+ * 8^3 or 16^2 cells and at most two flux species: on != 0 (default) the one
+ * that stages each box's |E| and densities in shared memory by bulk copies,
+ * on == 0 the one that reads them from global memory.  Both give the same
+ * results.  No counterpart in the reference. */
+int afg_set_flux_staged(afg_ctx* ctx, int on);
+
 /* af_tree_copy_cc (afivo/src/m_af_utils.f90:590-598): whole-array copy of
  * variable iv_from to iv_to on all boxes (used by copy_current_state,
  * src/streamer.f90:659-671). */
 int afg_tree_copy_cc(afg_ctx* ctx, int iv_from, int iv_to);
+
+/* ---- one stage of the explicit integrators (src/m_fluid.f90:21-99) -------
+ * The module settings that forward_euler reads (m_field's solver and its
+ * convergence settings, m_dt's dt_cfl_number and dt_max). */
+typedef struct {
+  int mg_id;                /* solver slot of the field (m_field's mg) */
+  double domain_len;        /* length of the last dimension (the field's round-off threshold) */
+  double max_rel_residual;  /* relative residual the field's V-cycles stop at */
+  int num_vcycles;          /* V-cycle limit of the field */
+  double dt_cfl_number;     /* dt_cfl_number (src/m_dt.f90:31) */
+  double dt_max;            /* dt_max (src/m_dt.f90:40) */
+} afg_stage_desc;
+int afg_stage_setup(afg_ctx* ctx, const afg_stage_desc* d);
+
+/* forward_euler (src/m_fluid.f90:21-99), the stage every explicit integrator
+ * of af_advance (afivo/src/m_af_advance.f90:150-199) is made of: when
+ * i_step > 1 the field of state s_deriv (afg_field_compute with a guess and
+ * the boundary value `voltage`, the applied voltage at the stage's time), the
+ * upwind fluxes of state s_deriv (afg_flux_upwind), then state s_out from
+ * the previous states, the sources and the flux divergence
+ * (afg_update_densities, the chemistry limit on the last step, i_step ==
+ * n_steps).  *dt_lim = min(dt_max, dt_cfl_number * CFL limit, dielectric
+ * relaxation time, chemistry limit of the last step); *n_cycles (optional)
+ * = the field's FMG + V-cycles (0 when i_step == 1).  AFG_ERR_ARG without
+ * afg_stage_setup; on a batched tree the field is the one-voltage
+ * afg_field_compute. */
+int afg_forward_euler(afg_ctx* ctx, double dt, double voltage, int s_deriv, int n_prev,
+                      const int* s_prev, const double* w_prev, int s_out, int i_step,
+                      int n_steps, double* dt_lim, int* n_cycles);
 
 /* ---- adaptive refinement on the device (src/streamer.f90:397-428) -------
  * The refinement decision per cell and box, the prolongation into new boxes

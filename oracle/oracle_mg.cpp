@@ -987,7 +987,12 @@ using namespace orc;
 
 extern "C" {
 
+int orc_transport_set_electrode(void*, int i_lsf);
+
 void* orc_create(const afg_tree_desc* d, int n_var, int n_var_face) {
+  // the transport state is process-wide: a new instance starts without the
+  // electrode mask of an earlier one
+  orc_transport_set_electrode(nullptr, 0);
   Oracle* o = new Oracle();
   Tree& t = o->t;
   t.D = d->ndim;
