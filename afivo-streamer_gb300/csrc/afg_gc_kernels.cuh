@@ -116,12 +116,14 @@ __device__ __forceinline__ int nbmat_at(const KTree& t, int slot, int dx, int dy
 }
 
 // Edge (3D) and corner ghosts of one box; face ghosts must be in place.
+// Threads lane, lane + nl, ... of the CTA work on the box (all threads of
+// the CTA reach the barrier; active == false: the box is skipped).
 template <int D, typename T>
-__device__ void corner_ghosts(const KTree& t, T* __restrict__ v, int slot) {
+__device__ void corner_ghosts(const KTree& t, T* __restrict__ v, int slot, int lane, int nl, bool active) {
   const int nc = t.nc, n2 = t.n2;
   T* a = v + (size_t)slot * t.S;
   if (D == 3) {
-    for (int w = threadIdx.x; w < 12 * nc; w += blockDim.x) {
+    for (int w = lane; active && w < 12 * nc; w += nl) {
       const int n = w / nc, pp = w % nc + 1;
       const int dim = c_edge_dim[n];
       const int dx = c_edge_dir[n][0], dy = c_edge_dir[n][1], dz = c_edge_dir[n][2];
@@ -148,7 +150,7 @@ __device__ void corner_ghosts(const KTree& t, T* __restrict__ v, int slot) {
     __syncthreads();
   }
   const int nch = 1 << D;
-  for (int n = threadIdx.x; n < nch; n += blockDim.x) {
+  for (int n = lane; active && n < nch; n += nl) {
     const int cd0 = n & 1, cd1 = (n >> 1) & 1, cd2 = (n >> 2) & 1;
     const int dx = 2 * cd0 - 1, dy = 2 * cd1 - 1, dz = D == 3 ? 2 * cd2 - 1 : 0;
     const int x = cd0 * (nc + 1), y = cd1 * (nc + 1), z = D == 3 ? cd2 * (nc + 1) : 0;
@@ -173,22 +175,36 @@ __device__ void corner_ghosts(const KTree& t, T* __restrict__ v, int slot) {
   }
 }
 
-// af_gc_lvl on a box list: one CTA per box.
+// the whole CTA on one box
+template <int D, typename T>
+__device__ void corner_ghosts(const KTree& t, T* __restrict__ v, int slot) {
+  corner_ghosts<D, T>(t, v, slot, threadIdx.x, blockDim.x, true);
+}
+
+// af_gc_lvl on a box list: kGcLanes<D> threads per box, blockDim.x /
+// kGcLanes<D> boxes per CTA (a box's ghost work is a few hundred cells in
+// dependent phases, so several boxes share a CTA to keep loads in flight).
+template <int D>
+constexpr int kGcLanes = D == 3 ? 64 : 32;
+
 template <int D, typename T, int NC = 0>
-__global__ void __launch_bounds__(256) k_gc(KTree t0, const int* __restrict__ rec, ModeArg<T> v_, GcDev g,
+__global__ void __launch_bounds__(256) k_gc(KTree t0, const int* __restrict__ rec, int n, ModeArg<T> v_, GcDev g,
                                             int corners) {
   const KTree t = fix_dims<D, NC>(t0);
   T* __restrict__ v = v_.get();
-  int4 r0, r1;
-  load_rec(rec, blockIdx.x, r0, r1);
+  constexpr int L = kGcLanes<D>;
+  const int e = blockIdx.x * (blockDim.x / L) + threadIdx.x / L, lane = threadIdx.x % L;
+  int4 r0 = make_int4(0, 0, 0, 0), r1 = r0;
+  bool active = e < n;
+  if (active) load_rec(rec, e, r0, r1);
   const int slot = r0.x;
-  if (box_frozen(t, slot)) return;
+  active = active && !box_frozen(t, slot);
   const int nc = t.nc;
   const int nface = D == 2 ? nc : nc * nc;
   T* a = v + (size_t)slot * t.S;
   // corners: 0 = face ghosts, 1 = faces then edges/corners, 2 = only the
   // edges/corners (face ghosts already valid)
-  for (int w = threadIdx.x; corners != 2 && w < 2 * D * nface; w += blockDim.x) {
+  for (int w = lane; active && corners != 2 && w < 2 * D * nface; w += L) {
     const int nb = w / nface, pq = w - nb * nface;
     const int p = pq % nc + 1, q = D == 3 ? pq / nc + 1 : 0;
     const int d = nb >> 1;
@@ -198,7 +214,7 @@ __global__ void __launch_bounds__(256) k_gc(KTree t0, const int* __restrict__ re
   }
   if (corners) {
     __syncthreads();
-    corner_ghosts<D, T>(t, v, slot);
+    corner_ghosts<D, T>(t, v, slot, lane, L, active);
   }
 }
 

@@ -204,12 +204,12 @@ __global__ void __launch_bounds__(256) k_gsrb_rb(KTree t0, const int* __restrict
 
 // The same half sweep staged in shared memory for a compile-time box size:
 // a persistent grid walks the box records; per box, thread 0 bulk-copies the
-// next box's other-colour half (SI/2 values, contiguous) into one of two
-// stages while the CTA works on the current box.  Before waiting for the
-// current box's copy, each thread loads the right-hand sides of its cells
-// (contiguous colour halves) and evaluates its share of the face ghosts next
-// to cells of the updated colour (face_ghost_rb on global memory: the values
-// af_gc would store), so those loads overlap the copy.  The CTA then spreads
+// next box's other-colour half and the right-hand sides of its updated colour
+// (SI/2 values each, contiguous) into one of two stages while the CTA works
+// on the current box.  Before waiting for the current box's copies, each
+// thread evaluates its share of the face ghosts next to cells of the updated
+// colour (face_ghost_rb on global memory: the values af_gc would store), so
+// those loads overlap the copies.  The CTA then spreads
 // the staged half and the ghosts into a padded (nc+2)^D block and each thread
 // updates CPT cells of the colour from shared memory without branches.  A
 // wait that times out (1 s) raises *err; the CTA drains its copies (bounded)
@@ -228,7 +228,8 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
   constexpr int NGT = (2 * D * NGF + TPB - 1) / TPB;  // ghosts per thread
   constexpr unsigned BYTES = SH * sizeof(float);
   static_assert(BYTES % 16 == 0, "bulk copies need 16-byte multiples");
-  __shared__ __align__(128) float cst[2][SH];
+  __shared__ __align__(128) float cst[2][SH];  // other colour
+  __shared__ __align__(128) float rst[2][SH];  // right-hand sides of the updated colour
   __shared__ float P[S];
   __shared__ __align__(8) unsigned long long bar[2];
   float* __restrict__ phi = phi_.get();
@@ -245,8 +246,9 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
   auto issue = [&](int e, int st) {
     const int s = rec[8 * e];
     fence_proxy_async_smem();
-    mbar_arrive_expect_tx(&bar[st], BYTES);
+    mbar_arrive_expect_tx(&bar[st], 2 * BYTES);
     bulk_copy_g2s(cst[st], phi + (size_t)s * SI + oc * SH, BYTES, &bar[st]);
+    bulk_copy_g2s(rst[st], rhs + (size_t)s * SI + col * SH, BYTES, &bar[st]);
   };
   if (threadIdx.x == 0 && (int)blockIdx.x < n) issue(blockIdx.x, 0);
   int it = 0;
@@ -261,9 +263,7 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
     float c[7];
     for (int q = 0; q < 2 * D + 1; q++) c[q] = mc.cb[slot * 8 + q];
     const float inv_c1 = mc.cb[slot * 8 + 7];
-    // this thread's cells and their right-hand sides
-    const float* f = rhs + (size_t)slot * SI + col * SH;
-    float fv[CPT];
+    // this thread's cells
     int xs[CPT];
 #pragma unroll
     for (int u = 0; u < CPT; u++) {
@@ -271,7 +271,6 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
       int i, j, k;
       rb_cell<D>(nc, col, w, i, j, k);
       xs[u] = D == 2 ? at2(n2, i, j) : at3(n2, i, j, k);
-      fv[u] = f[w];
     }
     // this thread's face ghosts next to cells of the updated colour: cell
     // (i, j[, k]) is updated when i + j (+ k) + redblack is even
@@ -323,16 +322,17 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
 #pragma unroll
       for (int u = 0; u < CPT; u++) {
         const int x = xs[u];
+        const float fv = rst[st][threadIdx.x + u * TPB];
         if (D == 2) {
           if (CYL) {
             const int i = x % n2;
             const float* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
-            val[u] = (fv[u] - y[1] * P[x - 1] - y[2] * P[x + 1] - c[3] * P[x - n2] - c[4] * P[x + n2]) * y[3];
+            val[u] = (fv - y[1] * P[x - 1] - y[2] * P[x + 1] - c[3] * P[x - n2] - c[4] * P[x + n2]) * y[3];
           } else {
-            val[u] = (fv[u] - c[1] * P[x - 1] - c[2] * P[x + 1] - c[3] * P[x - n2] - c[4] * P[x + n2]) * inv_c1;
+            val[u] = (fv - c[1] * P[x - 1] - c[2] * P[x + 1] - c[3] * P[x - n2] - c[4] * P[x + n2]) * inv_c1;
           }
         } else {
-          val[u] = (fv[u] - c[1] * P[x - 1] - c[2] * P[x + 1] - c[3] * P[x - n2] - c[4] * P[x + n2] -
+          val[u] = (fv - c[1] * P[x - 1] - c[2] * P[x + 1] - c[3] * P[x - n2] - c[4] * P[x + n2] -
                     c[5] * P[x - sk] - c[6] * P[x + sk]) *
                    inv_c1;
         }
@@ -347,11 +347,11 @@ __global__ void __launch_bounds__((D == 2 ? NC * NC / 2 : NC * NC * NC / 2) / CP
 // Edge (3D) and corner ghosts of one box on the compact layout; the face
 // ghosts must be in place (corner_ghosts of afg_gc_kernels.cuh).
 template <int D>
-__device__ void corner_ghosts_rb(const KTree& t, float* __restrict__ v, int slot) {
+__device__ void corner_ghosts_rb(const KTree& t, float* __restrict__ v, int slot, int lane, int nl, bool active) {
   const int nc = t.nc;
   auto at = [&](int b, int i, int j, int k) -> float& { return *rb_ptr<D>(t, v, b, i, j, k); };
   if (D == 3) {
-    for (int w = threadIdx.x; w < 12 * nc; w += blockDim.x) {
+    for (int w = lane; active && w < 12 * nc; w += nl) {
       const int n = w / nc, pp = w % nc + 1;
       const int dim = c_edge_dim[n];
       const int dx = c_edge_dir[n][0], dy = c_edge_dir[n][1], dz = c_edge_dir[n][2];
@@ -382,7 +382,7 @@ __device__ void corner_ghosts_rb(const KTree& t, float* __restrict__ v, int slot
     __syncthreads();
   }
   const int nch = 1 << D;
-  for (int n = threadIdx.x; n < nch; n += blockDim.x) {
+  for (int n = lane; active && n < nch; n += nl) {
     const int cd0 = n & 1, cd1 = (n >> 1) & 1, cd2 = (n >> 2) & 1;
     const int dx = 2 * cd0 - 1, dy = 2 * cd1 - 1, dz = D == 3 ? 2 * cd2 - 1 : 0;
     const int x = cd0 * (nc + 1), y = cd1 * (nc + 1), z = D == 3 ? cd2 * (nc + 1) : 0;
@@ -399,13 +399,20 @@ __device__ void corner_ghosts_rb(const KTree& t, float* __restrict__ v, int slot
   }
 }
 
-// face ghosts (all positions) of one box into its ghost block
+// the whole CTA on one box
+template <int D>
+__device__ void corner_ghosts_rb(const KTree& t, float* __restrict__ v, int slot) {
+  corner_ghosts_rb<D>(t, v, slot, threadIdx.x, blockDim.x, true);
+}
+
+// face ghosts (all positions) of one box into its ghost block, by threads
+// lane, lane + nl, ...
 template <int D>
 __device__ __forceinline__ void face_ghosts_rb(const KTree& t, float* __restrict__ v, int slot, const int4& r0,
-                                               const int4& r1, const GcDev& g) {
+                                               const int4& r1, const GcDev& g, int lane, int nl) {
   const int nc = t.nc;
   const int nface = D == 2 ? nc : nc * nc;
-  for (int w = threadIdx.x; w < 2 * D * nface; w += blockDim.x) {
+  for (int w = lane; w < 2 * D * nface; w += nl) {
     const int nb = w / nface, pq = w - nb * nface;
     const int p = pq % nc + 1, q = D == 3 ? pq / nc + 1 : 0;
     const float val = face_ghost_rb<D>(t, v, slot, nb, rec_nb(r0, r1, nb), p, q, g);
@@ -415,21 +422,30 @@ __device__ __forceinline__ void face_ghosts_rb(const KTree& t, float* __restrict
   }
 }
 
-// af_gc_lvl on a box list (k_gc): 0 = face ghosts, 1 = faces then edges and
-// corners, 2 = only the edges and corners
+template <int D>
+__device__ __forceinline__ void face_ghosts_rb(const KTree& t, float* __restrict__ v, int slot, const int4& r0,
+                                               const int4& r1, const GcDev& g) {
+  face_ghosts_rb<D>(t, v, slot, r0, r1, g, threadIdx.x, blockDim.x);
+}
+
+// af_gc_lvl on a box list (k_gc, kGcLanes<D> threads per box): 0 = face
+// ghosts, 1 = faces then edges and corners, 2 = only the edges and corners
 template <int D, int NC = 0>
-__global__ void __launch_bounds__(256) k_gc_rb(KTree t0, const int* __restrict__ rec, ModeArg<float> v_, GcDev g,
-                                               int corners) {
+__global__ void __launch_bounds__(256) k_gc_rb(KTree t0, const int* __restrict__ rec, int n, ModeArg<float> v_,
+                                               GcDev g, int corners) {
   const KTree t = fix_dims<D, NC>(t0);
   float* __restrict__ v = v_.get();
-  int4 r0, r1;
-  load_rec(rec, blockIdx.x, r0, r1);
+  constexpr int L = kGcLanes<D>;
+  const int e = blockIdx.x * (blockDim.x / L) + threadIdx.x / L, lane = threadIdx.x % L;
+  int4 r0 = make_int4(0, 0, 0, 0), r1 = r0;
+  bool active = e < n;
+  if (active) load_rec(rec, e, r0, r1);
   const int slot = r0.x;
-  if (box_frozen(t, slot)) return;
-  if (corners != 2) face_ghosts_rb<D>(t, v, slot, r0, r1, g);
+  active = active && !box_frozen(t, slot);
+  if (active && corners != 2) face_ghosts_rb<D>(t, v, slot, r0, r1, g, lane, L);
   if (corners) {
     __syncthreads();
-    corner_ghosts_rb<D>(t, v, slot);
+    corner_ghosts_rb<D>(t, v, slot, lane, L, active);
   }
 }
 

@@ -415,12 +415,16 @@ static int launch_gc(afg_ctx* ctx, const int* list, int n, ModeArg<T> v, const G
   if (n <= 0) return AFG_OK;
   KTree t = ktree(ctx);
   kt_begin(ctx, AFG_KT_GHOST);
+  // four boxes per CTA (kGcLanes threads each)
+  const int nb4 = (n + 3) / 4;
   if constexpr (std::is_same<T, float>::value) {
     if (ctx->rb32) {
       if (ctx->D == 2)
-        AFG_NC2(NCV_, k_gc_rb<2, NCV_><<<dim3(n, ctx->ky), 128, 0, ctx->stream>>>(t, rec_of(ctx, list), v, g, corners));
+        AFG_NC2(NCV_, k_gc_rb<2, NCV_><<<dim3(nb4, ctx->ky), 4 * kGcLanes<2>, 0, ctx->stream>>>(t, rec_of(ctx, list), n,
+                                                                                                v, g, corners));
       else
-        AFG_NC3(NCV_, k_gc_rb<3, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, rec_of(ctx, list), v, g, corners));
+        AFG_NC3(NCV_, k_gc_rb<3, NCV_><<<dim3(nb4, ctx->ky), 4 * kGcLanes<3>, 0, ctx->stream>>>(t, rec_of(ctx, list), n,
+                                                                                                v, g, corners));
       kt_end(ctx, AFG_KT_GHOST, 2.0 * sizeof(T) * n * ctx->ky * 2 * ctx->D * (box_cells(ctx) / ctx->nc));
       ctx->launches++;
       CKL();
@@ -428,9 +432,11 @@ static int launch_gc(afg_ctx* ctx, const int* list, int n, ModeArg<T> v, const G
     }
   }
   if (ctx->D == 2)
-    AFG_NC2(NCV_, k_gc<2, T, NCV_><<<dim3(n, ctx->ky), 128, 0, ctx->stream>>>(t, rec_of(ctx, list), v, g, corners));
+    AFG_NC2(NCV_, k_gc<2, T, NCV_><<<dim3(nb4, ctx->ky), 4 * kGcLanes<2>, 0, ctx->stream>>>(t, rec_of(ctx, list), n, v,
+                                                                                           g, corners));
   else
-    AFG_NC3(NCV_, k_gc<3, T, NCV_><<<dim3(n, ctx->ky), 256, 0, ctx->stream>>>(t, rec_of(ctx, list), v, g, corners));
+    AFG_NC3(NCV_, k_gc<3, T, NCV_><<<dim3(nb4, ctx->ky), 4 * kGcLanes<3>, 0, ctx->stream>>>(t, rec_of(ctx, list), n, v,
+                                                                                           g, corners));
   kt_end(ctx, AFG_KT_GHOST, 2.0 * sizeof(T) * n * ctx->ky * 2 * ctx->D * (box_cells(ctx) / ctx->nc));
   ctx->launches++;
   CKL();

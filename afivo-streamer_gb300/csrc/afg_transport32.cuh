@@ -658,19 +658,30 @@ __global__ void __launch_bounds__(256) k_field_rhs_interior(KTree t0, const int*
   const int ncell = D == 2 ? nc * nc : nc * nc * nc;
   const size_t base = (size_t)slot * t.S;
   double mx = 0.0;
-  for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
-    const int i = w % nc + 1, r = w / nc;
-    const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
-    const size_t x = base + (D == 2 ? at2(n2, i, j) : at3(n2, i, j, k));
-    double nv[NQ];
+  // CPT cells per thread, every density load of them issued first
+  constexpr int CPT = 4;
+  for (int w0 = threadIdx.x; w0 < ncell; w0 += CPT * blockDim.x) {
+    double nv[CPT][NQ];
+    size_t xs[CPT];
 #pragma unroll
-    for (int s = 0; s < NQ; s++) nv[s] = s < a.ns ? a.n[s][x] : 0.0;
-    double v = 0.0;
+    for (int u = 0; u < CPT; u++) {
+      const int w = w0 + u * blockDim.x;
+      const int i = w % nc + 1, r = w / nc;
+      const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
+      xs[u] = base + (D == 2 ? at2(n2, i, j) : at3(n2, i, j, k));
 #pragma unroll
-    for (int s = 0; s < NQ; s++)
-      if (s < a.ns) v = fma(a.q[s], nv[s], v);
-    a.rhs[x] = v;
-    acc_absmax(mx, v);
+      for (int s = 0; s < NQ; s++) nv[u][s] = (s < a.ns && w < ncell) ? a.n[s][xs[u]] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < CPT; u++) {
+      if (w0 + u * (int)blockDim.x >= ncell) continue;
+      double v = 0.0;
+#pragma unroll
+      for (int s = 0; s < NQ; s++)
+        if (s < a.ns) v = fma(a.q[s], nv[u][s], v);
+      a.rhs[xs[u]] = v;
+      acc_absmax(mx, v);
+    }
   }
   // max |rhs| over the leaves (af_tree_maxabs_cc), fused
   if (maxbits != nullptr) {

@@ -499,9 +499,9 @@ static int field_set_rhs(afg_ctx* ctx, int i_rhs, int s_in, unsigned long long* 
       const int nl = ctx->n_all_leaves;
 #define AFG_LAUNCH_RHS(NQ)                                                                                   \
   if (ctx->D == 3)                                                                                           \
-    AFG_NC3(NCV_, k_field_rhs_interior<3, NQ, NCV_><<<nl, 256, 0, ctx->stream>>>(t, list, q, maxbits));     \
+    AFG_NC3(NCV_, k_field_rhs_interior<3, NQ, NCV_><<<nl, 128, 0, ctx->stream>>>(t, list, q, maxbits));     \
   else                                                                                                       \
-    AFG_NC2(NCV_, k_field_rhs_interior<2, NQ, NCV_><<<nl, 256, 0, ctx->stream>>>(t, list, q, maxbits));
+    AFG_NC2(NCV_, k_field_rhs_interior<2, NQ, NCV_><<<nl, 64, 0, ctx->stream>>>(t, list, q, maxbits));
       if (q.ns <= 2) {
         AFG_LAUNCH_RHS(2)
       } else if (q.ns <= 4) {
