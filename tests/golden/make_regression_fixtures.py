@@ -8,7 +8,7 @@ photoionization, and the air chemistry file with 8 species and 25 reactions
 axisymmetric and Cartesian with photoionization and axisymmetric with
 both, twice axisymmetric with six mobile ion species, and a grounded rod
 electrode in the Cartesian domain under a positive and a negative applied
-field), the transport and
+field, without and with photoionization), the transport and
 reaction data they read, and the regression logs its test runner compares
 at rtol 1e-5 (programs/standard_2d/tests/, tools/compare_logs.py); and the
 3D configurations of its `standard_3d` program: the standard chemistry,
@@ -27,7 +27,9 @@ FILES = ["test_2d.cfg", "test_2d_rtest.log", "test_cyl.cfg", "test_cyl_rtest.log
          "test_cyl_ion_motion_rtest.log", "test_cyl_ion_motion_v2.cfg", "test_cyl_ion_motion_v2_rtest.log",
          "test_cyl_photoi_chem.cfg", "test_cyl_photoi_chem_rtest.log",
          "test_2d_pos_electrode.cfg", "test_2d_pos_electrode_rtest.log",
-         "test_2d_neg_electrode.cfg", "test_2d_neg_electrode_rtest.log"]
+         "test_2d_neg_electrode.cfg", "test_2d_neg_electrode_rtest.log",
+         "test_2d_pos_electrode_photoi.cfg", "test_2d_pos_electrode_photoi_rtest.log",
+         "test_2d_neg_electrode_photoi.cfg", "test_2d_neg_electrode_photoi_rtest.log"]
 
 
 SRC_3D = "programs/standard_3d/tests"

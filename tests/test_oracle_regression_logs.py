@@ -149,7 +149,7 @@ def test_log_writer_reproduces_reference_logs(tmp_path):
     fields): every stored log read and written back is identical."""
     import glob
     logs = sorted(glob.glob(os.path.join(GOLD, "*_rtest.log")) + glob.glob(os.path.join(GOLD3, "*_rtest.log")))
-    assert len(logs) == 13
+    assert len(logs) == 15
     for path in logs:
         head, rows = sp.read_regression_log(path)
         n = (len(head) - 3) // 3
