@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(256) k_flux32(KTree t0, const int* __restrict_
 // staged values are converted into the padded FP32 tile (face-ghost cells
 // left to the ghost values), the first ghost layer is written back, and the
 // faces and cells are done as in k_flux32, with the same arithmetic, so the
-// results are bit-identical.  At most NFMAX flux species.  The FP32 face
+// results are bit-identical.  At most NFMAX flux species (NFMAX = 1: exactly one).  The FP32 face
 // values and diffusion coefficients reuse the staging buffer.  A wait that
 // times out (1 s) raises *err; the CTA drains its copies (bounded) and
 // returns, raising bit 2 of *err if they did not complete.
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(256) k_flux32s(KTree t0, const int* __restrict
   __shared__ float sred[32];
   __shared__ __align__(8) unsigned long long bar;
   const FluxArgs& a = a32.a;
-  const int nf = a.nf;
+  const int nf = NFMAX == 1 ? 1 : a.nf;
   double* rawE = reinterpret_cast<double*>(smb);  // staged |E|, then the species
   double* rawN = rawE + S;
   float* vf = reinterpret_cast<float*>(smb);      // [D][nfaces], after the conversion

@@ -298,12 +298,19 @@ int afg_flux_upwind(afg_ctx* ctx, int s_deriv, double* dt_lim) {
         if (staged) {
           // the box's |E| and species staged by bulk copies (k_flux32s)
           const size_t sm = flux32s_smem(ctx, d.n_flux);
-          if (ctx->D == 3)
-            k_flux32s<3, false, 8, 2><<<n, 256, sm, ctx->stream>>>(t, rec_of(ctx, list), a32, ctx->d_err);
+const int* rl = rec_of(ctx, list);
+          if (ctx->D == 3 && d.n_flux == 1)
+            k_flux32s<3, false, 8, 1><<<n, 256, sm, ctx->stream>>>(t, rl, a32, ctx->d_err);
+          else if (ctx->D == 3)
+            k_flux32s<3, false, 8, 2><<<n, 256, sm, ctx->stream>>>(t, rl, a32, ctx->d_err);
+          else if (cyl && d.n_flux == 1)
+            k_flux32s<2, true, 16, 1><<<n, 256, sm, ctx->stream>>>(t, rl, a32, ctx->d_err);
           else if (cyl)
-            k_flux32s<2, true, 16, 2><<<n, 256, sm, ctx->stream>>>(t, rec_of(ctx, list), a32, ctx->d_err);
+            k_flux32s<2, true, 16, 2><<<n, 256, sm, ctx->stream>>>(t, rl, a32, ctx->d_err);
+          else if (d.n_flux == 1)
+            k_flux32s<2, false, 16, 1><<<n, 256, sm, ctx->stream>>>(t, rl, a32, ctx->d_err);
           else
-            k_flux32s<2, false, 16, 2><<<n, 256, sm, ctx->stream>>>(t, rec_of(ctx, list), a32, ctx->d_err);
+            k_flux32s<2, false, 16, 2><<<n, 256, sm, ctx->stream>>>(t, rl, a32, ctx->d_err);
         } else if (ctx->D == 3)
           AFG_NC3(NCV_, k_flux32<3, false, NCV_><<<n, 256, smem32, ctx->stream>>>(t, rec_of(ctx, list), a32));
         else if (cyl)
@@ -422,6 +429,8 @@ int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev, const
     AFG_NC2(NCV_, k_update32<2, false, NSM, NCV_><<<n, 128, rsm, ctx->stream>>>(t, list, u));
       if (d.n_species <= 4) {
         AFG_LAUNCH_UPDATE32(4)
+      } else if (d.n_species <= 6) {
+        AFG_LAUNCH_UPDATE32(6)
       } else if (d.n_species <= 8) {
         AFG_LAUNCH_UPDATE32(8)
       } else {
