@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libafivo_gpu.so")
 OBJ_DIR = os.path.join(HERE, "build")
-UNITS = ["afg_runtime.cu", "afg_noalloc.cu", "afg_tree_host.cpp", "afg_output_host.cpp"]
+UNITS = ["afg_runtime.cu", "afg_species_update.cu", "afg_noalloc.cu", "afg_tree_host.cpp", "afg_output_host.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3",
               "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off",

@@ -73,7 +73,7 @@ namespace afg {
 // phase cannot complete; the wait gives up after kWaitLimitNs and raises
 // *err exactly as a staged kernel does.  No copy is in flight when the CTA
 // returns.
-__global__ void k_wait_check(unsigned bytes, unsigned* err) {
+static __global__ void k_wait_check(unsigned bytes, unsigned* err) {
   __shared__ __align__(8) unsigned long long bar;
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);

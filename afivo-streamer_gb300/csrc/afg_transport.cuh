@@ -638,7 +638,7 @@ struct RhsArgs {
   double q[AFG_MAX_SPECIES];  // charge * (-e/eps0), 0 = uncharged (skipped)
   double* rhs;
 };
-__global__ void __launch_bounds__(256) k_field_rhs(int S, const int* __restrict__ list, RhsArgs a) {
+static __global__ void __launch_bounds__(256) k_field_rhs(int S, const int* __restrict__ list, RhsArgs a) {
   const size_t base = (size_t)list[blockIdx.x] * S;
   for (int x = threadIdx.x; x < S; x += blockDim.x) {
     double v = 0.0;
@@ -719,7 +719,7 @@ __global__ void __launch_bounds__(256) k_photo_source(KTree t0, const int* __res
 }
 
 // i_photo = i_photo - coeff * phi_n on whole leaf arrays
-__global__ void __launch_bounds__(256) k_axpy_boxes(int S, const int* __restrict__ list, double* __restrict__ y,
+static __global__ void __launch_bounds__(256) k_axpy_boxes(int S, const int* __restrict__ list, double* __restrict__ y,
                                                     const double* __restrict__ x, double c) {
   const size_t base = (size_t)list[blockIdx.x] * S;
   for (int q = threadIdx.x; q < S; q += blockDim.x) y[base + q] = y[base + q] - c * x[base + q];

@@ -16,6 +16,7 @@
 //   - charge density: FP64 (n_+ - n_- cancels), interior cells only.
 // The same routines of the reference are cited at the FP64 kernels.
 #pragma once
+#include "afg_tma.cuh"
 #include "afg_transport.cuh"
 
 namespace afg {

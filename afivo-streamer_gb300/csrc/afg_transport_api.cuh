@@ -29,6 +29,14 @@ static LtDevF lt_dev_f(const afg_ctx* ctx) {
   return lt;
 }
 
+// species-update launchers (afg_species_update.cu)
+namespace afg {
+void launch_update32(int D, bool cyl, int nc, int ns, int n, const KTree& t, const int* list, const UpdateArgs32& u,
+                     size_t smem, cudaStream_t st);
+void launch_update64(int D, bool cyl, int nc, int ns, int n, const KTree& t, const int* list, const UpdateArgs& a,
+                     cudaStream_t st);
+}  // namespace afg
+
 static bool mixed_transport(const afg_ctx* ctx) { return ctx->tr.ready && ctx->tr.d.precision == AFG_MIXED; }
 
 static GcDev gc_from_desc(const afg_gc_desc& g) {
@@ -420,39 +428,9 @@ int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev, const
       for (int m = 0; m < n_prev; m++)
         if (s_prev[m] == s_deriv) u.prev_is_deriv = m;
       const size_t rsm = sizeof(Reac32) * (size_t)d.n_reactions;  // the records in shared memory
-#define AFG_LAUNCH_UPDATE32(NSM)                                                               \
-  if (ctx->D == 3)                                                                             \
-    AFG_NC3(NCV_, k_update32<3, false, NSM, NCV_><<<n, 128, rsm, ctx->stream>>>(t, list, u));  \
-  else if (cyl)                                                                                \
-    AFG_NC2(NCV_, k_update32<2, true, NSM, NCV_><<<n, 128, rsm, ctx->stream>>>(t, list, u));   \
-  else                                                                                         \
-    AFG_NC2(NCV_, k_update32<2, false, NSM, NCV_><<<n, 128, rsm, ctx->stream>>>(t, list, u));
-      if (d.n_species <= 4) {
-        AFG_LAUNCH_UPDATE32(4)
-      } else if (d.n_species <= 6) {
-        AFG_LAUNCH_UPDATE32(6)
-      } else if (d.n_species <= 8) {
-        AFG_LAUNCH_UPDATE32(8)
-      } else {
-        AFG_LAUNCH_UPDATE32(16)
-      }
-#undef AFG_LAUNCH_UPDATE32
+      launch_update32(ctx->D, cyl, ctx->nc, d.n_species, n, t, list, u, rsm, ctx->stream);
     } else {
-#define AFG_LAUNCH_UPDATE(NSM)                                                             \
-  if (ctx->D == 3)                                                                         \
-    AFG_NC3(NCV_, k_update<3, false, NSM, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, a));  \
-  else if (cyl)                                                                            \
-    AFG_NC2(NCV_, k_update<2, true, NSM, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, a));   \
-  else                                                                                     \
-    AFG_NC2(NCV_, k_update<2, false, NSM, NCV_><<<n, 128, 0, ctx->stream>>>(t, list, a));
-      if (d.n_species <= 4) {
-        AFG_LAUNCH_UPDATE(4)
-      } else if (d.n_species <= 8) {
-        AFG_LAUNCH_UPDATE(8)
-      } else {
-        AFG_LAUNCH_UPDATE(16)
-      }
-#undef AFG_LAUNCH_UPDATE
+      launch_update64(ctx->D, cyl, ctx->nc, d.n_species, n, t, list, a, ctx->stream);
     }
     // per leaf cell: read S*(n_prev+1) densities (+|E|, D*F fluxes, photo), write S densities
     kt_end(ctx, AFG_KT_UPDATE, 8.0 * n * box_cells(ctx) *
@@ -515,6 +493,8 @@ static int field_set_rhs(afg_ctx* ctx, int i_rhs, int s_in, unsigned long long* 
         AFG_LAUNCH_RHS(2)
       } else if (q.ns <= 4) {
         AFG_LAUNCH_RHS(4)
+      } else if (q.ns <= 6) {
+        AFG_LAUNCH_RHS(6)
       } else if (q.ns <= 8) {
         AFG_LAUNCH_RHS(8)
       } else {
