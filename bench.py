@@ -707,9 +707,8 @@ def main():
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
                          "traffic_note": ("DRAM bytes are not measured inside the timed run (no profiler there); "
-                                          "the launch list of the same workload under ncu (2026-12-04, "
-                                          "profiles/dram_per_kernel_streamer_steps.md) gives 21.2 GB per "
-                                          "k_update32 launch against 17.8 GB algorithmic"),
+                                          "every kernel's DRAM bytes for the same workload under ncu are in "
+                                          "profiles/dram_per_kernel_streamer_steps.md (2026-12-04)"),
                          "algorithmic_bytes_per_launch": ks["bytes"] / max(1, ks["launches"]),
                          "avg_launch_us": 1e3 * ks["ms"] / max(1, ks["launches"])},
             "kernel_classes": kstats, "tuning": tuning,
