@@ -21,7 +21,8 @@ namespace afg {
 // refinement rules; boxes flagged as refinement sources were filled before
 // the launch and are left alone, since finer boxes' rules read them), then
 // applies the stencil to the stored values.  The Cartesian stencil is one
-// FMA chain (8 FP64 instructions per cell); r is rounded to FP32 by bit
+// FMA chain from f with negated coefficients (7 FP64 instructions per cell
+// in 3D); r is rounded to FP32 by bit
 // truncation and its maximum taken in FP32.  RB: the FP32 buffers have the
 // compact red-black layout (afg_mg32.cuh); e's ghost block is cleared only on
 // parents and refinement sources, the boxes whose ghost cells the FP32
@@ -70,8 +71,10 @@ __global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict_
     }
   }
   __syncthreads();
+  // negated coefficients: r = f - sum c_q p_q as one chain of 2D+1 FMAs
+  // starting from f (one FP64 instruction fewer than summing L(phi) first)
   double cd[7];
-  for (int q = 0; q < 7; q++) cd[q] = mc.cb[slot * 8 + q];
+  for (int q = 0; q < 7; q++) cd[q] = -mc.cb[slot * 8 + q];
   const double* p = pw_;
   const double* f = rhs + (size_t)slot * t.S;
   float* ro = r32 + (size_t)slot * (RB ? t.SI : t.S);
@@ -80,24 +83,27 @@ __global__ void __launch_bounds__(256) k_defect(KTree t0, const int* __restrict_
   for (int w = threadIdx.x; w < ncell; w += blockDim.x) {
     const int i = w % nc + 1, r = w / nc;
     const int j = D == 2 ? r + 1 : r % nc + 1, k = D == 2 ? 0 : r / nc + 1;
-    double lp;
+    double rd;
     int x;
     if (D == 2) {
       x = at2(n2, i, j);
       if (CYL) {
         const double* y = mc.cy + ((size_t)slot * nc + (i - 1)) * 4;
-        lp = fma(cd[4], p[x + n2], fma(cd[3], p[x - n2], fma(y[2], p[x + 1], fma(y[1], p[x - 1], y[0] * p[x]))));
+        rd = fma(cd[4], p[x + n2],
+                 fma(cd[3], p[x - n2], fma(-y[2], p[x + 1], fma(-y[1], p[x - 1], fma(-y[0], p[x], f[x])))));
       } else {
-        lp = fma(cd[4], p[x + n2], fma(cd[3], p[x - n2], fma(cd[2], p[x + 1], fma(cd[1], p[x - 1], cd[0] * p[x]))));
+        rd = fma(cd[4], p[x + n2],
+                 fma(cd[3], p[x - n2], fma(cd[2], p[x + 1], fma(cd[1], p[x - 1], fma(cd[0], p[x], f[x])))));
       }
     } else {
       x = at3(n2, i, j, k);
       const int sk = n2 * n2;
-      lp = fma(cd[6], p[x + sk],
+      rd = fma(cd[6], p[x + sk],
                fma(cd[5], p[x - sk],
-                   fma(cd[4], p[x + n2], fma(cd[3], p[x - n2], fma(cd[2], p[x + 1], fma(cd[1], p[x - 1], cd[0] * p[x]))))));
+                   fma(cd[4], p[x + n2],
+                       fma(cd[3], p[x - n2], fma(cd[2], p[x + 1], fma(cd[1], p[x - 1], fma(cd[0], p[x], f[x])))))));
     }
-    const float res = d2f(f[x] - lp);
+    const float res = d2f(rd);
     ro[RB ? rb_idx<D>(nc, i, j, k) : x] = res;
     acc_absmax(mx, res);
   }
