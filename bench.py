@@ -605,6 +605,18 @@ def run_cpu_batch(steps, warmup, time_limit, cores):
     return work / t_run, cores, t_run / max(1, done_steps), done_steps, sample
 
 
+def combine_replicas(ms, work_per_step, world):
+    """Whole-job figures of N independent replicas (one rank per GPU, an
+    initialised process group): the step time is the maximum over the ranks
+    and the value counts the work of all of them."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    return ms, world * work_per_step / (ms * 1e-3)
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -677,12 +689,7 @@ def main():
     ms = mixed["ms_per_step"]
     value = mixed["value"]
     if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        value = world * mixed["work_per_step"] / (ms * 1e-3)
+        ms, value = combine_replicas(ms, mixed["work_per_step"], world)
     peak, peak_kind = peaks()
     dom = max((k for k in kstats if not k.startswith("_")), key=lambda k: kstats[k]["ms"])
     ks = kstats[dom]
