@@ -24,9 +24,10 @@ GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "stand
 CASES = ["test_2d", "test_cyl", "test_2d_photoi", "test_cyl_chem", "test_2d_photoi_chem",
          "test_cyl_ion_motion", "test_cyl_ion_motion_v2", "test_3d", "test_3d_chem", "test_3d_photoi_chem",
          "test_cyl_photoi_chem"]
-# the electrode runs (grounded rod, positive and negative field): FP64 only,
-# the electrode operator has no FP32 solve
-FP64_CASES = CASES + ["test_2d_pos_electrode", "test_2d_neg_electrode"]
+# the electrode runs (grounded rod, positive and negative field, without and
+# with photoionization): FP64 only, the electrode operator has no FP32 solve
+FP64_CASES = CASES + ["test_2d_pos_electrode", "test_2d_neg_electrode", "test_2d_pos_electrode_photoi",
+                      "test_2d_neg_electrode_photoi"]
 
 # FP64 GPU rows against the restatement's: identical (every stage is
 # bit-exact, the first smoothing of a solve reads the stored ghost cells as
@@ -108,31 +109,3 @@ def test_mixed_run_matches_log(gpu_lib, name):
     print(f"{name}: mixed GPU vs log max rel {e.max():.3e} ({pm.n_steps} steps, {pm.n_rejected} rejected)")
     assert np.allclose(rm[:, 3:], ref[:, 3:], rtol=MIXED_VS_LOG[name], atol=1e-8)
 
-
-# The rod-electrode runs with photoionization (photoi%species M_plus, a lower
-# background density): their restatement runs take over 40 minutes on one
-# CPU core, so the FP64 GPU rows, identical to the restatement's wherever
-# both run (the cases above), are compared with the stored logs directly.
-# Bounds: the observed maxima, rounded up; the negative-polarity run
-# separates from its log after the second output (6e-4, then up to 1.1e-2),
-# as its run without photoionization does, less strongly (1.1e-3).
-ELECTRODE_PHOTOI_VS_LOG = {
-    "test_2d_pos_electrode_photoi": 5e-5,
-    "test_2d_neg_electrode_photoi": 1.5e-2,
-}
-
-
-@pytest.mark.gpu
-@pytest.mark.parametrize("name", sorted(ELECTRODE_PHOTOI_VS_LOG))
-def test_fp64_electrode_photoi_run_matches_log(gpu_lib, name):
-    pg, rg = run(name, functools.partial(sp.GpuEngine, precision=ag.FP64))
-    head, ref = sp.read_regression_log(case_paths(name)[1])
-    assert rg.shape == ref.shape
-    assert np.array_equal(rg[:, 0], ref[:, 0])
-    assert np.allclose(rg[:, 1], ref[:, 1], rtol=1e-12, atol=0)
-    # the initial state and refinement agree to the log's printed digits
-    assert np.allclose(rg[0, 2:], ref[0, 2:], rtol=1e-7, atol=1e-8)
-    e = rel_err(rg[:, 2:], ref[:, 2:])[ref[:, 2:] != 0]
-    print(f"{name}: FP64 GPU vs log max rel {e.max():.3e} ({pg.n_steps} steps)")
-    assert np.allclose(rg[:, 2:], ref[:, 2:], rtol=ELECTRODE_PHOTOI_VS_LOG[name], atol=1e-8)
-    assert pg.n_steps > 200

@@ -26,7 +26,11 @@ electrode (level-set internal boundary of the field, electrode refinement,
 species rules at the electrode) under a positive and a negative applied
 field: the first rows agree to 3e-10 and 4e-8; the positive run stays
 within 6.1e-5, the negative within 1.1e-3 from its third row on (an
-inexact coarse solve at 1e-6 does not change that figure, 1.09e-3).
+inexact coarse solve at 1e-6 does not change that figure, 1.09e-3).  The
+same two runs with photoionization (photoi%species M_plus, a lower
+background density): 3.7e-5 and 1.1e-2; the negative-field runs separate
+from their logs between the first and second outputs (0.2-0.4 ns) in every
+column at once, with the same step sizes.
 
 Every row of test_2d, test_cyl, test_cyl_chem, test_cyl_photoi_chem and
 the two ion-motion runs passes the reference's own comparison (rtol 1e-5);
@@ -63,6 +67,8 @@ CASES = {
     "test_3d_photoi_chem": 1e-4,
     "test_2d_pos_electrode": 1e-4,
     "test_2d_neg_electrode": 2e-3,
+    "test_2d_pos_electrode_photoi": 5e-5,
+    "test_2d_neg_electrode_photoi": 1.5e-2,
 }
 
 
