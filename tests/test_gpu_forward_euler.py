@@ -77,16 +77,19 @@ def test_forward_euler_needs_stage_setup():
     ctx.close()
 
 
-@pytest.mark.parametrize("name", ["cyl2d", "3d"])
+@pytest.mark.parametrize("name", ["cyl2d", "3d", "cyl2d_ion", "3d_ion"])
 def test_staged_flux_equals_direct(name):
     """The FP32 fluxes with the box's |E| and densities staged by bulk copies
-    (the default; boxes of 16^2 and 8^3 cells) and read from global memory
-    give the same bits: fluxes, the written-back ghost layer and both
-    limits."""
-    w, tree, model = make(name)
-    if name == "cyl2d":
+    (the default; boxes of 16^2 and 8^3 cells, electrons alone or with one
+    mobile ion species) and read from global memory give the same bits:
+    fluxes, the written-back ghost layer and both limits."""
+    w, tree, model = make(name.split("_")[0])
+    if name.startswith("cyl2d"):
         tree = refined_tree(2, 16, [16, 32], [1e-2, 2e-2], 4, 2, [0.0, 1.2e-2], 0.8e-3,
                             coord=ag.AFG_CYL, seed=2, frac=0.1)
+    if name.endswith("_ion"):
+        model = sm.StreamerModel(tree.ndim, alpha=sm.baseline_alpha, eta=sm.baseline_eta,
+                                 mobile_ions=[(1, 2.2e-4)], photoi_modes=3)
     cc, fc = initial_state(tree, model, seed=9, voltage=w.voltage)
     ctx = ag.Context(0)
     ctx.tree_sync(tree, model.n_var_cell, model.n_var_face)
