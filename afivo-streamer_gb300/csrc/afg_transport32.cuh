@@ -447,7 +447,7 @@ __device__ __forceinline__ void add_tof(float (&v)[NSMAX], int s, float x) {
 // first previous state are loaded before the chemistry, so that their
 // latency overlaps it.
 template <int D, bool CYL, int NSMAX, int NC = 0>
-__global__ void __launch_bounds__(128, 8) k_update32(KTree t0, const int* __restrict__ list, UpdateArgs32 u) {
+__global__ void __launch_bounds__(128, NSMAX <= 6 ? 9 : 8) k_update32(KTree t0, const int* __restrict__ list, UpdateArgs32 u) {
   const KTree t = fix_dims<D, NC>(t0);
   __shared__ float sred[32];
   __shared__ float s_dens[NSMAX * 128], s_der[NSMAX * 128];
