@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(256) k_flux32(KTree t0, const int* __restrict_
 // times out (1 s) raises *err; the CTA drains its copies (bounded) and
 // returns, raising bit 2 of *err if they did not complete.
 template <int D, bool CYL, int NC, int NFMAX>
-__global__ void __launch_bounds__(256) k_flux32s(KTree t0, const int* __restrict__ rec, FluxArgs32 a32,
+__global__ void __launch_bounds__(256, 5) k_flux32s(KTree t0, const int* __restrict__ rec, FluxArgs32 a32,
                                                 unsigned* err) {
   constexpr int nc = NC, n2 = NC + 2, m = NC + 4, nf1 = NC + 1;
   constexpr int S = D == 2 ? n2 * n2 : n2 * n2 * n2;

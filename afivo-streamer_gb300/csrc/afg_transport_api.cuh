@@ -111,6 +111,21 @@ int afg_transport_setup(afg_ctx* ctx, const afg_transport_desc* d) {
       if (rc.ix_out[q] < 0 || rc.ix_out[q] >= t.n_species) return fail(ctx, AFG_ERR_ARG, "bad reaction species");
   }
   clear_graphs(ctx);
+  {
+    // the staged flux kernel keeps 5 CTAs per SM (its register bound) only
+    // with the shared-memory carveout at its maximum
+    static bool carveout_set = false;
+    if (!carveout_set) {
+      const int pct = cudaSharedmemCarveoutMaxShared;
+      CK(cudaFuncSetAttribute(k_flux32s<3, false, 8, 1>, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+      CK(cudaFuncSetAttribute(k_flux32s<3, false, 8, 2>, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+      CK(cudaFuncSetAttribute(k_flux32s<2, true, 16, 1>, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+      CK(cudaFuncSetAttribute(k_flux32s<2, true, 16, 2>, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+      CK(cudaFuncSetAttribute(k_flux32s<2, false, 16, 1>, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+      CK(cudaFuncSetAttribute(k_flux32s<2, false, 16, 2>, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+      carveout_set = true;
+    }
+  }
   TransportState& s = ctx->tr;
   transport_free(s);
   s.d = t;
