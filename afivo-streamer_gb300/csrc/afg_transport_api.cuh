@@ -447,9 +447,14 @@ int afg_update_densities(afg_ctx* ctx, double dt, int s_deriv, int n_prev, const
     } else {
       launch_update64(ctx->D, cyl, ctx->nc, d.n_species, n, t, list, a, ctx->stream);
     }
-    // per leaf cell: read S*(n_prev+1) densities (+|E|, D*F fluxes, photo), write S densities
+    // per leaf cell: read the S densities of every distinct state (s_deriv
+    // and the previous states; s_deriv counts once when it is one of them),
+    // |E|, D*F fluxes and the photoionization source; write S densities
+    int n_states_read = n_prev + 1;
+    for (int m = 0; m < n_prev; m++)
+      if (s_prev[m] == s_deriv) n_states_read = n_prev;
     kt_end(ctx, AFG_KT_UPDATE, 8.0 * n * box_cells(ctx) *
-                                   (d.n_species * (n_prev + 1) + ctx->D * d.n_flux + 1 + (d.i_photo > 0) + d.n_species));
+                                   (d.n_species * n_states_read + ctx->D * d.n_flux + 1 + (d.i_photo > 0) + d.n_species));
     ctx->launches++;
     CKL();
   }
